@@ -1,0 +1,160 @@
+/*
+ * bssn_gb300.h -- C ABI of the GB300 (sm_103a) BSSN evolution kernels.
+ *
+ * Every entry point takes plain device pointers, sizes and a cudaStream_t
+ * (passed as void*), launches asynchronously on that stream, never allocates
+ * on the hot path (work buffers are caller-provided; sizes come from
+ * bssn_workspace_bytes), and returns an int status: 0 on success, a positive
+ * BSSN_ERR_* code otherwise.  bssn_last_error() returns a message for the
+ * calling thread's most recent failure.
+ *
+ * Field layout at the boundary is the reference's: seven C-ordered float64
+ * arrays with the spatial axes last and z fastest (JAX_BSSN/bssn/variables.py:8-16,
+ * docs/bssn.rst:11-49):
+ *   conformal_metric (3,3,nx,ny,nz)  conformal_factor W (nx,ny,nz)
+ *   traceless_K      (3,3,nx,ny,nz)  trace_K (nx,ny,nz)
+ *   conformal_connection (3,nx,ny,nz) lapse (nx,ny,nz)  shift (3,nx,ny,nz)
+ * Symmetric tensors are read from their upper triangle and written to both
+ * halves.
+ *
+ * Resident state ("patch" layout) is the GB300-side working format: 21
+ * independent float64 components, each a contiguous padded block of
+ * (nx+2G)(ny+2G)(nz+2G) samples, z fastest, owned samples at [G, G+n).
+ * Component order: gt_xx gt_xy gt_xz gt_yy gt_yz gt_zz, W,
+ * At_xx At_xy At_xz At_yy At_yz At_zz, K, Gt_x Gt_y Gt_z, alpha, beta_x beta_y beta_z.
+ */
+#ifndef BSSN_GB300_H
+#define BSSN_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BSSN_ABI_VERSION 1
+
+/* status codes */
+#define BSSN_OK 0
+#define BSSN_ERR_INVALID 1      /* argument validation failed (host side) */
+#define BSSN_ERR_WORKSPACE 2    /* workspace pointer null or too small */
+#define BSSN_ERR_CUDA 3         /* a CUDA launch or runtime call failed */
+#define BSSN_ERR_NONFINITE 4    /* non-finite value detected in the state */
+#define BSSN_ERR_TIMEOUT 5      /* a bounded device wait gave up */
+
+#define BSSN_NCOMP 21           /* independent evolved components */
+#define BSSN_NLEAF_VALUES 27    /* stored values per point in the reference layout */
+
+/* Mirrors BSSNParameters (JAX_BSSN/bssn/variables.py:19-46).  Face codes:
+ * 0 periodic, 1 Sommerfeld, in xl xr yl yr zl zr order. */
+typedef struct BssnParams {
+    double eta, kappa, nu, g, dx, dt;
+    int32_t zero_shift;      /* 1 holds the shift fixed */
+    int32_t gauge;           /* 0 harmonic, 1 1+log */
+    int32_t bc[6];
+    double xmin[3];          /* coordinate of array index 0 on each axis */
+    double mad_q;            /* D4 weight of the MAD D4/D6 blend */
+    int32_t guard_cells;     /* lower padding before the first owned sample */
+    int32_t owned_shape[3];  /* owned samples per axis; -1: the whole array */
+    int32_t owned_faces[6];  /* 1 when this array owns the global face */
+    int32_t reduced_axes[3]; /* 1 reduced, 0 not, -1 infer (owned count == 1 when owned_shape given) */
+} BssnParams;
+
+/* The seven reference leaves as device pointers (float64). */
+typedef struct BssnFields {
+    double* conformal_metric;
+    double* conformal_factor;
+    double* traceless_K;
+    double* trace_K;
+    double* conformal_connection;
+    double* lapse;
+    double* shift;
+} BssnFields;
+
+/* Optional matter sources in the reference layout: rho (n), S_i (3,n), S_ij (3,3,n).
+ * All three null selects the vacuum equations. */
+typedef struct BssnMatter {
+    const double* energy_density;
+    const double* momentum_density;
+    const double* spatial_stress;
+} BssnMatter;
+
+/* Operation selector for bssn_workspace_bytes. */
+#define BSSN_OP_RHS 1
+#define BSSN_OP_RK4 2
+#define BSSN_OP_CONSTRAINTS 3
+
+const char* bssn_last_error(void);
+int bssn_abi_version(void);
+
+/* Bytes of device workspace an operation needs on an (nx,ny,nz) array. */
+size_t bssn_workspace_bytes(int op, const int32_t shape[3], const BssnParams* params);
+
+/* compute_bssn_rhs(vars, params) -> rhs (JAX_BSSN/evolution/time_evolve.py:41-57),
+ * and compute_bssn_rhs_with_matter (time_evolve.py:60-91) when matter is non-null
+ * (not yet supported: returns BSSN_ERR_INVALID).  Like the reference, the RHS is
+ * evaluated at every sample of the array, with periodic wrap across the array
+ * extent and face closures/Sommerfeld replacement on the owned range given by
+ * guard_cells/owned_shape. */
+int bssn_rhs(const BssnFields* in, BssnFields* out, const int32_t shape[3],
+             const BssnParams* params, const BssnMatter* matter,
+             void* workspace, size_t workspace_bytes, void* stream);
+
+/* enforce_algebraic_constraints(vars) (time_evolve.py:134-141): det(gt)=1 then
+ * trace-free At.  In place on all samples of the array. */
+int bssn_project(BssnFields* state, const int32_t shape[3], void* stream);
+
+/* rk4_step(vars, params) (time_evolve.py:144-217), repeated `steps` times, in place. */
+int bssn_rk4_step(BssnFields* state, const int32_t shape[3], const BssnParams* params,
+                  int32_t steps, void* workspace, size_t workspace_bytes, void* stream);
+
+/* compute_all_constraints(vars, params) (JAX_BSSN/bssn/constraints.py:387-412):
+ * writes H (n), M (3,n), det-1 (n), trace A (n), Gamma constraint (3,n). */
+int bssn_constraints(const BssnFields* in, const int32_t shape[3], const BssnParams* params,
+                     double* hamiltonian, double* momentum, double* det_gamma,
+                     double* trace_A, double* gamma_condition,
+                     void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---------------- resident patch layout (fast path) ---------------- */
+
+typedef struct BssnPatch {
+    int32_t n[3];     /* owned samples per axis */
+    int32_t ghost;    /* padding G on every face */
+} BssnPatch;
+
+size_t bssn_patch_values(const BssnPatch* patch);            /* 21 * prod(n+2G) */
+size_t bssn_patch_workspace_bytes(const BssnPatch* patch, const BssnParams* params);
+
+/* Reference layout (nx,ny,nz) -> patch owned samples (ghosts left untouched). */
+int bssn_patch_import(const BssnFields* in, double* patch_state, const BssnPatch* patch, void* stream);
+/* Patch owned samples -> reference layout. */
+int bssn_patch_export(const double* patch_state, BssnFields* out, const BssnPatch* patch, void* stream);
+/* Fill the ghost shell by periodic wrap of owned samples (parallel/communication.py:45-52). */
+int bssn_patch_fill_periodic(double* patch_state, const BssnPatch* patch, void* stream);
+/* `steps` RK4 steps of a periodic/Sommerfeld patch, in place (time_evolve.py:144-217). */
+int bssn_patch_rk4(double* patch_state, const BssnPatch* patch, const BssnParams* params,
+                   int32_t steps, void* workspace, size_t workspace_bytes, void* stream);
+/* Count of non-finite owned values into *flag (device int32), for step monitors. */
+int bssn_patch_check_finite(const double* patch_state, const BssnPatch* patch,
+                            int32_t* device_flag, void* stream);
+
+/* ---------------- instrumentation ---------------- */
+
+/* Kernel launches issued by this library since load (all threads). */
+long long bssn_launch_count(void);
+/* Per-kernel-class device-time accounting with CUDA events on each launch's
+ * stream; off by default.  Classes: fill, first derivatives, gauge RHS, K/Gt
+ * RHS, At RHS, momentum derived fields, momentum damping, Sommerfeld, RK4
+ * stage, projection, import, export, constraints, FMR transfer, Cartoon,
+ * other.  bssn_profile_read synchronises the recorded events, accumulates and
+ * returns the number of classes. */
+void bssn_profile_enable(int on);
+void bssn_profile_reset(void);
+int bssn_profile_read(double* ms, long long* counts, int n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BSSN_GB300_H */

@@ -1,0 +1,147 @@
+"""ctypes binding of ``libbssn_gb300.so`` (C ABI in ``include/bssn_gb300.h``).
+
+The structs below mirror the header field for field.  Every call returns an
+int status; non-zero raises ``ValueError`` for validation failures (the
+reference raises ValueError from its host-side validators) and
+``RuntimeError`` otherwise, carrying ``bssn_last_error()``.
+
+There is no fallback: importing this module on a machine without the built
+library, or calling into it without a CUDA device, fails loudly.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+from .build import LIBRARY
+
+c_double_p = ctypes.POINTER(ctypes.c_double)
+
+BSSN_OK = 0
+BSSN_ERR_INVALID = 1
+BSSN_ERR_WORKSPACE = 2
+BSSN_ERR_CUDA = 3
+BSSN_ERR_NONFINITE = 4
+BSSN_ERR_TIMEOUT = 5
+
+OP_RHS = 1
+OP_RK4 = 2
+OP_CONSTRAINTS = 3
+
+
+class BssnParams(ctypes.Structure):
+    _fields_ = [
+        ("eta", ctypes.c_double), ("kappa", ctypes.c_double), ("nu", ctypes.c_double),
+        ("g", ctypes.c_double), ("dx", ctypes.c_double), ("dt", ctypes.c_double),
+        ("zero_shift", ctypes.c_int32), ("gauge", ctypes.c_int32),
+        ("bc", ctypes.c_int32 * 6),
+        ("xmin", ctypes.c_double * 3),
+        ("mad_q", ctypes.c_double),
+        ("guard_cells", ctypes.c_int32),
+        ("owned_shape", ctypes.c_int32 * 3),
+        ("owned_faces", ctypes.c_int32 * 6),
+        ("reduced_axes", ctypes.c_int32 * 3),
+    ]
+
+
+class BssnFields(ctypes.Structure):
+    _fields_ = [(name, ctypes.c_void_p) for name in (
+        "conformal_metric", "conformal_factor", "traceless_K", "trace_K",
+        "conformal_connection", "lapse", "shift")]
+
+
+class BssnMatter(ctypes.Structure):
+    _fields_ = [("energy_density", ctypes.c_void_p), ("momentum_density", ctypes.c_void_p),
+                ("spatial_stress", ctypes.c_void_p)]
+
+
+class BssnPatch(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int32 * 3), ("ghost", ctypes.c_int32)]
+
+
+Shape3 = ctypes.c_int32 * 3
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "bssn_last_error": (ctypes.c_char_p, []),
+    "bssn_abi_version": (ctypes.c_int, []),
+    "bssn_workspace_bytes": (ctypes.c_size_t, [ctypes.c_int, Shape3, ctypes.POINTER(BssnParams)]),
+    "bssn_rhs": (ctypes.c_int, [ctypes.POINTER(BssnFields), ctypes.POINTER(BssnFields), Shape3,
+                                ctypes.POINTER(BssnParams), ctypes.POINTER(BssnMatter),
+                                ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    "bssn_project": (ctypes.c_int, [ctypes.POINTER(BssnFields), Shape3, ctypes.c_void_p]),
+    "bssn_rk4_step": (ctypes.c_int, [ctypes.POINTER(BssnFields), Shape3, ctypes.POINTER(BssnParams),
+                                     ctypes.c_int32, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    "bssn_constraints": (ctypes.c_int, [ctypes.POINTER(BssnFields), Shape3, ctypes.POINTER(BssnParams),
+                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    "bssn_patch_values": (ctypes.c_size_t, [ctypes.POINTER(BssnPatch)]),
+    "bssn_patch_workspace_bytes": (ctypes.c_size_t, [ctypes.POINTER(BssnPatch), ctypes.POINTER(BssnParams)]),
+    "bssn_patch_import": (ctypes.c_int, [ctypes.POINTER(BssnFields), ctypes.c_void_p,
+                                         ctypes.POINTER(BssnPatch), ctypes.c_void_p]),
+    "bssn_patch_export": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BssnFields),
+                                         ctypes.POINTER(BssnPatch), ctypes.c_void_p]),
+    "bssn_patch_fill_periodic": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BssnPatch), ctypes.c_void_p]),
+    "bssn_patch_rk4": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BssnPatch), ctypes.POINTER(BssnParams),
+                                      ctypes.c_int32, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    "bssn_patch_check_finite": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BssnPatch),
+                                               ctypes.c_void_p, ctypes.c_void_p]),
+    "bssn_launch_count": (ctypes.c_longlong, []),
+    "bssn_profile_enable": (None, [ctypes.c_int]),
+    "bssn_profile_reset": (None, []),
+    "bssn_profile_read": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
+}
+
+KERNEL_CLASSES = ("fill", "first_derivs", "rhs_gauge", "rhs_k_gamma", "rhs_at", "mom_derived", "mom_damping",
+                  "sommerfeld", "rk4_stage", "project", "import", "export", "constraints", "fmr_transfer",
+                  "cartoon", "other")
+
+
+def profile_read() -> dict:
+    """{class: (milliseconds, launches)} accumulated since bssn_profile_reset."""
+    lib = load()
+    n = len(KERNEL_CLASSES)
+    ms = (ctypes.c_double * n)()
+    counts = (ctypes.c_longlong * n)()
+    lib.bssn_profile_read(ctypes.cast(ms, ctypes.c_void_p), ctypes.cast(counts, ctypes.c_void_p), n)
+    return {name: (ms[i], counts[i]) for i, name in enumerate(KERNEL_CLASSES) if counts[i]}
+
+_lib = None
+
+
+def library_path() -> Path:
+    return LIBRARY
+
+
+def load(path: Path | None = None):
+    """Load the CUDA library once; raises if it has not been built."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    path = Path(path or LIBRARY)
+    if not path.exists():
+        raise RuntimeError(
+            f"{path} is missing: build the CUDA extension first "
+            "(python -c 'import __graft_entry__ as g; g.build()')")
+    lib = ctypes.CDLL(str(path))
+    for name, (restype, argtypes) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = restype
+        fn.argtypes = argtypes
+    if path == LIBRARY:
+        _lib = lib
+    return lib
+
+
+def last_error() -> str:
+    return load().bssn_last_error().decode(errors="replace")
+
+
+def check(status: int, what: str) -> None:
+    if status == BSSN_OK:
+        return
+    message = f"{what}: {last_error()}"
+    if status in (BSSN_ERR_INVALID, BSSN_ERR_WORKSPACE):
+        raise ValueError(message)
+    raise RuntimeError(message)

@@ -1,0 +1,654 @@
+// C ABI, geometry set-up and the point-wise kernels around the RHS:
+// reference-layout import/export, periodic ghost fill, the algebraic
+// projection (JAX_BSSN/evolution/time_evolve.py:94-141) and the RK4 stage
+// epilogue (time_evolve.py:144-217).
+//
+// Stage combinations are evaluated with round-to-nearest intrinsics in the
+// reference's order: u0 + (c*dt)*k for the stages, the accumulator
+// ((k1 + 2 k2) + 2 k3) + k4 and u0 + (dt/6)*sum (serial, tiled and Cartoon
+// steppers) or u0 + (dt*sum)/6 (JAX_BSSN/fmr/tiled.py:279-280).  Together
+// with the bit-exact projection this keeps the evolved state identical to the
+// float64 reference wherever the RHS agrees to the last bit.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "../../include/bssn_gb300.h"
+#include "bssn_driver.h"
+#include "bssn_fields.cuh"
+#include "bssn_kernels.h"
+#include "bssn_profile.h"
+
+namespace bssn {
+
+static thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+int cuda_status(cudaError_t e, const char* where) {
+    if (e == cudaSuccess) return BSSN_OK;
+    return fail(BSSN_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+constexpr int kThreads = 256;
+static inline unsigned nblocks(long long n) { return (unsigned)((n + kThreads - 1) / kThreads); }
+
+// ---------------------------------------------------------------------------
+// geometry
+// ---------------------------------------------------------------------------
+int validate_params(const BssnParams* p) {
+    if (p == nullptr) return fail(BSSN_ERR_INVALID, "params is null");
+    if (!(std::isfinite(p->dx) && p->dx > 0.0)) return fail(BSSN_ERR_INVALID, "dx must be finite and positive");
+    if (!std::isfinite(p->dt)) return fail(BSSN_ERR_INVALID, "dt must be finite");
+    for (int f = 0; f < 6; ++f)
+        if (p->bc[f] != 0 && p->bc[f] != 1)
+            return fail(BSSN_ERR_INVALID, "boundary codes must be 0 (periodic) or 1 (Sommerfeld)");
+    if (p->gauge != 0 && p->gauge != 1) return fail(BSSN_ERR_INVALID, "gauge must be 0 or 1");
+    return BSSN_OK;
+}
+
+// Geometry of an array of extent S embedded at padded offset `org` in a
+// padded block of extent P.  The owned range follows the reference's
+// guard_cells/owned_shape (JAX_BSSN/evolution/spatial_derivatives.py:18-41),
+// the Sommerfeld mask follows boundaries.py:44-71.
+int make_geo(const BssnParams* p, const int S[3], const int org[3], const int P[3], Geo& G) {
+    std::memset(&G, 0, sizeof(G));
+    const bool owned_given = p->owned_shape[0] >= 0;
+    for (int d = 0; d < 3; ++d) {
+        Axis& a = G.ax[d];
+        a.P = P[d];
+        a.org = org[d];
+        a.lo = org[d];
+        a.hi = org[d] + S[d];
+        const int count = owned_given ? p->owned_shape[d] : S[d];
+        a.start = org[d] + p->guard_cells;
+        a.end = a.start + count;
+        if (count < 1 || p->guard_cells < 0 || p->guard_cells + count > S[d])
+            return fail(BSSN_ERR_INVALID, "owned range does not fit the array");
+        const int lcode = p->bc[2 * d], rcode = p->bc[2 * d + 1];
+        const bool lown = p->owned_faces[2 * d] != 0, rown = p->owned_faces[2 * d + 1] != 0;
+        a.lbc = (lcode == kSommerfeld) && lown;
+        a.rbc = (rcode == kSommerfeld) && rown;
+        const bool physical_global = lcode == kSommerfeld || rcode == kSommerfeld;
+        a.q = physical_global ? 1.0 : p->mad_q;
+        a.omq = 1.0 - a.q;
+        a.mad = a.q != 1.0;
+        if (p->reduced_axes[d] >= 0) a.reduced = p->reduced_axes[d] != 0;
+        else a.reduced = owned_given ? (count == 1) : 0;
+        const bool counts_ok = owned_given ? count > 1 : true;
+        a.slo = a.lbc && counts_ok;
+        a.shi = a.rbc && counts_ok;
+        a.xmin = p->xmin[d];
+        if ((a.lbc || a.rbc) && !a.reduced && count < 8)
+            return fail(BSSN_ERR_INVALID, "Sommerfeld/KO closures require eight owned samples along the axis");
+        if (a.lo < 4 || a.hi > P[d] - 4)
+            return fail(BSSN_ERR_INVALID, "padded block needs four samples of margin around the compute range");
+    }
+    G.st[2] = 1;
+    G.st[1] = P[2];
+    G.st[0] = (long long)P[1] * P[2];
+    G.cs = (long long)P[0] * P[1] * P[2];
+    const double dx = p->dx;
+    G.dx = dx;
+    G.inv_dx = 1.0 / dx;
+    G.inv_12dx = 1.0 / (12.0 * dx);
+    G.inv_60dx = 1.0 / (60.0 * dx);
+    G.inv_12dx2 = 1.0 / (12.0 * (dx * dx));
+    G.inv_dx2 = 1.0 / (dx * dx);
+    G.inv_dx6h5 = std::pow(dx, 5.0) / std::pow(dx, 6.0);
+    G.nu64 = p->nu / 64.0;
+    G.eta = p->eta;
+    G.kappa = p->kappa;
+    G.g = p->g;
+    G.dt = p->dt;
+    G.gauge = p->gauge;
+    G.zero_shift = p->zero_shift;
+    G.any_sommerfeld = 0;
+    for (int f = 0; f < 6; ++f) G.any_sommerfeld |= (p->bc[f] == kSommerfeld);
+    return BSSN_OK;
+}
+
+Box box_of(const Geo& G) {
+    Box b;
+    b.count = 1;
+    for (int d = 0; d < 3; ++d) {
+        b.lo[d] = G.ax[d].lo;
+        b.n[d] = G.ax[d].hi - G.ax[d].lo;
+        b.count *= b.n[d];
+    }
+    return b;
+}
+
+Box full_box(const Geo& G) {
+    Box b;
+    b.count = 1;
+    for (int d = 0; d < 3; ++d) {
+        b.lo[d] = 0;
+        b.n[d] = G.ax[d].P;
+        b.count *= b.n[d];
+    }
+    return b;
+}
+
+size_t rhs_work_blocks(bool with_mom) {
+    return with_mom ? (size_t)(3 * (NMIX + NMIX_MOM) + 24 + 6) : (size_t)(3 * NMIX);
+}
+
+RhsWork carve_rhs_work(double* base, long long cs, bool with_mom) {
+    RhsWork w;
+    w.d1 = base;
+    if (with_mom) {
+        w.der = base + (long long)(3 * (NMIX + NMIX_MOM)) * cs;
+        w.damp = w.der + 24LL * cs;
+    }
+    return w;
+}
+
+// ---------------------------------------------------------------------------
+// point-wise kernels
+// ---------------------------------------------------------------------------
+struct Leaves {
+    const double* f[7];
+};
+struct LeavesOut {
+    double* f[7];
+};
+
+__device__ __forceinline__ void leaf_of(int comp, int& leaf, int& idx) {
+    // component -> (leaf, flat component index inside the leaf) in the reference layout
+    if (comp < 6) { leaf = 0; const int i = comp < 3 ? 0 : (comp < 5 ? 1 : 2); const int j = comp < 3 ? comp : (comp < 5 ? comp - 2 : 2); idx = 3 * i + j; }
+    else if (comp == CW) { leaf = 1; idx = 0; }
+    else if (comp < CK) { leaf = 2; const int c = comp - AXX; const int i = c < 3 ? 0 : (c < 5 ? 1 : 2); const int j = c < 3 ? c : (c < 5 ? c - 2 : 2); idx = 3 * i + j; }
+    else if (comp == CK) { leaf = 3; idx = 0; }
+    else if (comp < CALPHA) { leaf = 4; idx = comp - GTX; }
+    else if (comp == CALPHA) { leaf = 5; idx = 0; }
+    else { leaf = 6; idx = comp - BX; }
+}
+
+// reference layout (shape S) -> padded block at org
+__global__ void k_import(Leaves in, double* __restrict__ u, Geo G, Box region, long long npts) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= region.count * NCOMP) return;
+    const int comp = (int)(t / region.count);
+    const long long r = t - (long long)comp * region.count;
+    int ix[3];
+    region.coords(r, ix);
+    int leaf, idx;
+    leaf_of(comp, leaf, idx);
+    u[comp * G.cs + lin(G, ix)] = in.f[leaf][idx * npts + r];
+}
+
+// padded block -> reference layout; symmetric tensors written to both halves
+__global__ void k_export(const double* __restrict__ u, LeavesOut out, Geo G, Box region, long long npts) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= region.count * NCOMP) return;
+    const int comp = (int)(t / region.count);
+    const long long r = t - (long long)comp * region.count;
+    int ix[3];
+    region.coords(r, ix);
+    int leaf, idx;
+    leaf_of(comp, leaf, idx);
+    const double v = u[comp * G.cs + lin(G, ix)];
+    out.f[leaf][idx * npts + r] = v;
+    if (leaf == 0 || leaf == 2) {
+        const int i = idx / 3, j = idx % 3;
+        if (i != j) out.f[leaf][(3 * j + i) * npts + r] = v;
+    }
+}
+
+// Periodic wrap of the array region [lo, lo+n) into every other padded sample
+// (np.roll semantics of the reference on an unpadded array, and the self-wrap
+// of a single tile, JAX_BSSN/parallel/communication.py:45-52).
+__global__ void k_fill_periodic(double* __restrict__ u, int ncomp, Geo G, Box region, Box all) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= all.count) return;
+    int ix[3];
+    all.coords(t, ix);
+    bool inside = true;
+    int src[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        int rel = ix[d] - region.lo[d];
+        if (rel < 0 || rel >= region.n[d]) inside = false;
+        rel %= region.n[d];
+        if (rel < 0) rel += region.n[d];
+        src[d] = region.lo[d] + rel;
+    }
+    if (inside) return;
+    const long long dst = lin(G, ix), s = lin(G, src);
+    for (int c = 0; c < ncomp; ++c) u[c * G.cs + dst] = u[c * G.cs + s];
+}
+
+// Bit-exact algebraic projection of one point held in registers.
+__device__ __forceinline__ void project_point(double (&g)[6], double (&A)[6]) {
+    const double s = inv_cbrt_cr(det_sym_rn(g));
+#pragma unroll
+    for (int c = 0; c < 6; ++c) g[c] = __dmul_rn(g[c], s);
+    double gi[6];
+    inverse_metric_rn(g, gi);
+    // trace gt^ij At_ij over all nine (i, j) in row-major order
+    double tr = __dmul_rn(gi[0], A[0]);
+    tr = __dadd_rn(tr, __dmul_rn(gi[1], A[1]));
+    tr = __dadd_rn(tr, __dmul_rn(gi[2], A[2]));
+    tr = __dadd_rn(tr, __dmul_rn(gi[1], A[1]));
+    tr = __dadd_rn(tr, __dmul_rn(gi[3], A[3]));
+    tr = __dadd_rn(tr, __dmul_rn(gi[4], A[4]));
+    tr = __dadd_rn(tr, __dmul_rn(gi[2], A[2]));
+    tr = __dadd_rn(tr, __dmul_rn(gi[4], A[4]));
+    tr = __dadd_rn(tr, __dmul_rn(gi[5], A[5]));
+#pragma unroll
+    for (int c = 0; c < 6; ++c) A[c] = __dadd_rn(A[c], -__dmul_rn(__dmul_rn(1.0 / 3.0, g[c]), tr));
+}
+
+__global__ void k_project(double* __restrict__ u, Geo G, Box B) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= B.count) return;
+    int ix[3];
+    B.coords(t, ix);
+    const long long p = lin(G, ix), cs = G.cs;
+    double g[6], A[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) { g[c] = u[(GXX + c) * cs + p]; A[c] = u[(AXX + c) * cs + p]; }
+    project_point(g, A);
+#pragma unroll
+    for (int c = 0; c < 6; ++c) { u[(GXX + c) * cs + p] = g[c]; u[(AXX + c) * cs + p] = A[c]; }
+}
+
+// Projection in place on the reference layout (all samples).
+__global__ void k_project_ref(LeavesOut f, long long npts) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= npts) return;
+    constexpr int ij[6][2] = {{0, 0}, {0, 1}, {0, 2}, {1, 1}, {1, 2}, {2, 2}};
+    double g[6], A[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        g[c] = f.f[0][(3 * ij[c][0] + ij[c][1]) * npts + t];
+        A[c] = f.f[2][(3 * ij[c][0] + ij[c][1]) * npts + t];
+    }
+    project_point(g, A);
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        const int a = ij[c][0], b = ij[c][1];
+        f.f[0][(3 * a + b) * npts + t] = g[c];
+        f.f[0][(3 * b + a) * npts + t] = g[c];
+        f.f[2][(3 * a + b) * npts + t] = A[c];
+        f.f[2][(3 * b + a) * npts + t] = A[c];
+    }
+}
+
+// RK4 stage epilogue.  stage 1..3: out = u0 + h*k, acc updated; stage 4:
+// out = u0 + (dt/6)*(acc + k)  [final_form 0]  or  (dt*(acc + k))/6  [1].
+__global__ void k_rk4_stage(const double* __restrict__ u0, const double* __restrict__ k,
+                            double* __restrict__ acc, double* __restrict__ out, Geo G, Box B,
+                            int stage, double h, double dt, int final_form, int project) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= B.count) return;
+    int ix[3];
+    B.coords(t, ix);
+    const long long p = lin(G, ix), cs = G.cs;
+    double v[NCOMP];
+#pragma unroll
+    for (int c = 0; c < NCOMP; ++c) {
+        const long long q = c * cs + p;
+        const double kv = k[q];
+        if (stage < 4) {
+            v[c] = __dadd_rn(u0[q], __dmul_rn(h, kv));
+            acc[q] = (stage == 1) ? kv : __dadd_rn(acc[q], __dmul_rn(2.0, kv));
+        } else {
+            const double s = __dadd_rn(acc[q], kv);
+            const double inc = final_form ? __ddiv_rn(__dmul_rn(dt, s), 6.0) : __dmul_rn(dt / 6.0, s);
+            v[c] = __dadd_rn(u0[q], inc);
+        }
+    }
+    if (project) {
+        double g[6], A[6];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) { g[c] = v[GXX + c]; A[c] = v[AXX + c]; }
+        project_point(g, A);
+#pragma unroll
+        for (int c = 0; c < 6; ++c) { v[GXX + c] = g[c]; v[AXX + c] = A[c]; }
+    }
+#pragma unroll
+    for (int c = 0; c < NCOMP; ++c) out[c * cs + p] = v[c];
+}
+
+__global__ void k_count_nonfinite(const double* __restrict__ u, Geo G, Box B, int* flag) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= B.count) return;
+    int ix[3];
+    B.coords(t, ix);
+    const long long p = lin(G, ix);
+    int bad = 0;
+    for (int c = 0; c < NCOMP; ++c) bad += !isfinite(u[c * G.cs + p]);
+    if (bad) atomicAdd(flag, bad);
+}
+
+__global__ void k_zero(double* __restrict__ u, long long n) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) u[t] = 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// launchers shared by the C ABI, FMR and Cartoon drivers
+// ---------------------------------------------------------------------------
+cudaError_t launch_fill_periodic(double* u, int ncomp, const Geo& G, cudaStream_t s) {
+    const Box region = box_of(G);
+    const Box all = full_box(G);
+    BSSN_LAUNCH(KC_FILL, k_fill_periodic, nblocks(all.count), kThreads, s, u, ncomp, G, region, all);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_project(double* u, const Geo& G, const Box& B, cudaStream_t s) {
+    BSSN_LAUNCH(KC_PROJECT, k_project, nblocks(B.count), kThreads, s, u, G, B);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rk4_stage(const double* u0, const double* k, double* acc, double* out, const Geo& G,
+                             const Box& B, int stage, double dt, int final_form, int project,
+                             cudaStream_t s) {
+    const double h = stage == 3 ? dt : 0.5 * dt;
+    BSSN_LAUNCH(KC_STAGE, k_rk4_stage, nblocks(B.count), kThreads, s, u0, k, acc, out, G, B, stage, h, dt, final_form, project);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_zero(double* u, long long n, cudaStream_t s) {
+    BSSN_LAUNCH(KC_OTHER, k_zero, nblocks(n), kThreads, s, u, n);
+    return cudaGetLastError();
+}
+
+// One classical RK4 step of the state u0 (in place), with the RHS over the
+// box B and the projection both before the first stage (serial stepper) and
+// after every combination.
+cudaError_t rk4_step_patch(double* u0, double* ustage, double* k, double* acc, const RhsWork& w,
+                           const Geo& G, const Box& B, bool fill, int final_form, cudaStream_t s) {
+    cudaError_t e;
+    for (int stage = 1; stage <= 4; ++stage) {
+        const double* src = stage == 1 ? u0 : ustage;
+        if (fill && (e = launch_fill_periodic(const_cast<double*>(src), NCOMP, G, s)) != cudaSuccess) return e;
+        if ((e = launch_rhs(src, k, w, G, B, s)) != cudaSuccess) return e;
+        double* out = stage == 4 ? u0 : ustage;
+        if ((e = launch_rk4_stage(u0, k, acc, out, G, B, stage, G.dt, final_form, 1, s)) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+}  // namespace bssn
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+using namespace bssn;
+
+namespace {
+
+constexpr int kMargin = 4;
+
+struct RefLayout {
+    int S[3];
+    int org[3];
+    int P[3];
+    long long npts;
+    long long cs;
+};
+
+int ref_layout(const int32_t shape[3], RefLayout& L) {
+    if (shape == nullptr) return fail(BSSN_ERR_INVALID, "shape is null");
+    L.npts = 1;
+    L.cs = 1;
+    for (int d = 0; d < 3; ++d) {
+        if (shape[d] < 1) return fail(BSSN_ERR_INVALID, "array extents must be positive");
+        L.S[d] = shape[d];
+        L.org[d] = kMargin;
+        L.P[d] = shape[d] + 2 * kMargin;
+        L.npts *= shape[d];
+        L.cs *= L.P[d];
+    }
+    return BSSN_OK;
+}
+
+bool fields_ok(const BssnFields* f) {
+    return f && f->conformal_metric && f->conformal_factor && f->traceless_K && f->trace_K &&
+           f->conformal_connection && f->lapse && f->shift;
+}
+
+Leaves leaves_in(const BssnFields* f) {
+    return Leaves{{f->conformal_metric, f->conformal_factor, f->traceless_K, f->trace_K,
+                   f->conformal_connection, f->lapse, f->shift}};
+}
+LeavesOut leaves_out(BssnFields* f) {
+    return LeavesOut{{f->conformal_metric, f->conformal_factor, f->traceless_K, f->trace_K,
+                      f->conformal_connection, f->lapse, f->shift}};
+}
+
+size_t ref_workspace_values(int op, const RefLayout& L, bool with_mom) {
+    if (op == BSSN_OP_CONSTRAINTS) return (size_t)(NCOMP + 3 * NMIX + 24) * (size_t)L.cs;
+    const size_t blocks = (op == BSSN_OP_RK4 ? 4 * NCOMP : 2 * NCOMP) + rhs_work_blocks(with_mom);
+    return blocks * (size_t)L.cs;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* bssn_last_error(void) { return g_last_error.c_str(); }
+
+int bssn_abi_version(void) { return BSSN_ABI_VERSION; }
+
+size_t bssn_workspace_bytes(int op, const int32_t shape[3], const BssnParams* params) {
+    RefLayout L;
+    if (ref_layout(shape, L) != BSSN_OK) return 0;
+    const bool with_mom = params && params->kappa != 0.0;
+    return ref_workspace_values(op, L, with_mom) * sizeof(double);
+}
+
+int bssn_rhs(const BssnFields* in, BssnFields* out, const int32_t shape[3], const BssnParams* params,
+             const BssnMatter* matter, void* workspace, size_t workspace_bytes, void* stream) {
+    if (!fields_ok(in) || !fields_ok(out)) return fail(BSSN_ERR_INVALID, "null field pointer");
+    if (matter && (matter->energy_density || matter->momentum_density || matter->spatial_stress))
+        return fail(BSSN_ERR_INVALID, "matter sources are not supported by this build");
+    int st = validate_params(params);
+    if (st) return st;
+    RefLayout L;
+    if ((st = ref_layout(shape, L))) return st;
+    Geo G;
+    if ((st = make_geo(params, L.S, L.org, L.P, G))) return st;
+    const bool with_mom = params->kappa != 0.0;
+    if (!workspace || workspace_bytes < ref_workspace_values(BSSN_OP_RHS, L, with_mom) * sizeof(double))
+        return fail(BSSN_ERR_WORKSPACE, "workspace missing or smaller than bssn_workspace_bytes(BSSN_OP_RHS)");
+    cudaStream_t s = (cudaStream_t)stream;
+    double* u = (double*)workspace;
+    double* k = u + NCOMP * L.cs;
+    RhsWork w = carve_rhs_work(k + NCOMP * L.cs, L.cs, with_mom);
+    const Box region = box_of(G);
+    BSSN_LAUNCH(KC_IMPORT, k_import, nblocks(region.count * NCOMP), kThreads, s, leaves_in(in), u, G, region, L.npts);
+    cudaError_t e = launch_fill_periodic(u, NCOMP, G, s);
+    if (e == cudaSuccess) e = launch_rhs(u, k, w, G, region, s);
+    if (e == cudaSuccess) {
+        BSSN_LAUNCH(KC_EXPORT, k_export, nblocks(region.count * NCOMP), kThreads, s, k, leaves_out(out), G, region, L.npts);
+        e = cudaGetLastError();
+    }
+    return cuda_status(e, "bssn_rhs");
+}
+
+int bssn_project(BssnFields* state, const int32_t shape[3], void* stream) {
+    if (!fields_ok(state)) return fail(BSSN_ERR_INVALID, "null field pointer");
+    RefLayout L;
+    int st = ref_layout(shape, L);
+    if (st) return st;
+    BSSN_LAUNCH(KC_PROJECT, k_project_ref, nblocks(L.npts), kThreads, (cudaStream_t)stream, leaves_out(state), L.npts);
+    return cuda_status(cudaGetLastError(), "bssn_project");
+}
+
+int bssn_rk4_step(BssnFields* state, const int32_t shape[3], const BssnParams* params, int32_t steps,
+                  void* workspace, size_t workspace_bytes, void* stream) {
+    if (!fields_ok(state)) return fail(BSSN_ERR_INVALID, "null field pointer");
+    if (steps < 0) return fail(BSSN_ERR_INVALID, "steps must be non-negative");
+    int st = validate_params(params);
+    if (st) return st;
+    RefLayout L;
+    if ((st = ref_layout(shape, L))) return st;
+    Geo G;
+    if ((st = make_geo(params, L.S, L.org, L.P, G))) return st;
+    const bool with_mom = params->kappa != 0.0;
+    if (!workspace || workspace_bytes < ref_workspace_values(BSSN_OP_RK4, L, with_mom) * sizeof(double))
+        return fail(BSSN_ERR_WORKSPACE, "workspace missing or smaller than bssn_workspace_bytes(BSSN_OP_RK4)");
+    cudaStream_t s = (cudaStream_t)stream;
+    double* u0 = (double*)workspace;
+    double* us = u0 + NCOMP * L.cs;
+    double* k = us + NCOMP * L.cs;
+    double* acc = k + NCOMP * L.cs;
+    RhsWork w = carve_rhs_work(acc + NCOMP * L.cs, L.cs, with_mom);
+    const Box region = box_of(G);
+    BSSN_LAUNCH(KC_IMPORT, k_import, nblocks(region.count * NCOMP), kThreads, s, leaves_in(state), u0, G, region, L.npts);
+    cudaError_t e = cudaGetLastError();
+    for (int n = 0; n < steps && e == cudaSuccess; ++n) {
+        e = launch_project(u0, G, region, s);
+        if (e == cudaSuccess) e = rk4_step_patch(u0, us, k, acc, w, G, region, true, 0, s);
+    }
+    if (e == cudaSuccess) {
+        BSSN_LAUNCH(KC_EXPORT, k_export, nblocks(region.count * NCOMP), kThreads, s, u0, leaves_out(state), G, region, L.npts);
+        e = cudaGetLastError();
+    }
+    return cuda_status(e, "bssn_rk4_step");
+}
+
+int bssn_constraints(const BssnFields* in, const int32_t shape[3], const BssnParams* params,
+                     double* hamiltonian, double* momentum, double* det_gamma, double* trace_A,
+                     double* gamma_condition, void* workspace, size_t workspace_bytes, void* stream) {
+    if (!fields_ok(in)) return fail(BSSN_ERR_INVALID, "null field pointer");
+    if (!hamiltonian || !momentum || !det_gamma || !trace_A || !gamma_condition)
+        return fail(BSSN_ERR_INVALID, "null constraint output pointer");
+    int st = validate_params(params);
+    if (st) return st;
+    RefLayout L;
+    if ((st = ref_layout(shape, L))) return st;
+    Geo G;
+    if ((st = make_geo(params, L.S, L.org, L.P, G))) return st;
+    if (!workspace || workspace_bytes < ref_workspace_values(BSSN_OP_CONSTRAINTS, L, false) * sizeof(double))
+        return fail(BSSN_ERR_WORKSPACE, "workspace missing or smaller than bssn_workspace_bytes(BSSN_OP_CONSTRAINTS)");
+    cudaStream_t s = (cudaStream_t)stream;
+    double* u = (double*)workspace;
+    RhsWork w;
+    w.d1 = u + NCOMP * L.cs;
+    w.der = w.d1 + 3LL * NMIX * L.cs;
+    const Box region = box_of(G);
+    BSSN_LAUNCH(KC_IMPORT, k_import, nblocks(region.count * NCOMP), kThreads, s, leaves_in(in), u, G, region, L.npts);
+    cudaError_t e = launch_fill_periodic(u, NCOMP, G, s);
+    if (e == cudaSuccess)
+        e = launch_constraints(u, w, G, region, hamiltonian, momentum, det_gamma, trace_A, gamma_condition, s);
+    return cuda_status(e, "bssn_constraints");
+}
+
+// ---------------- resident patch layout ----------------
+
+static int patch_geo(const BssnPatch* patch, const BssnParams* params, Geo& G) {
+    if (!patch) return fail(BSSN_ERR_INVALID, "patch is null");
+    if (patch->ghost < 4) return fail(BSSN_ERR_INVALID, "patch ghost width must be at least 4");
+    int S[3], org[3], P[3];
+    for (int d = 0; d < 3; ++d) {
+        if (patch->n[d] < 1) return fail(BSSN_ERR_INVALID, "patch extents must be positive");
+        S[d] = patch->n[d];
+        org[d] = patch->ghost;
+        P[d] = patch->n[d] + 2 * patch->ghost;
+    }
+    BssnParams p;
+    if (params) p = *params;
+    else {
+        std::memset(&p, 0, sizeof(p));
+        p.dx = 1.0;
+        p.mad_q = 1.0;
+        for (int f = 0; f < 6; ++f) p.owned_faces[f] = 1;
+        for (int d = 0; d < 3; ++d) { p.owned_shape[d] = -1; p.reduced_axes[d] = -1; }
+    }
+    p.guard_cells = 0;
+    for (int d = 0; d < 3; ++d) p.owned_shape[d] = -1;
+    return make_geo(&p, S, org, P, G);
+}
+
+size_t bssn_patch_values(const BssnPatch* patch) {
+    if (!patch) return 0;
+    size_t n = NCOMP;
+    for (int d = 0; d < 3; ++d) n *= (size_t)(patch->n[d] + 2 * patch->ghost);
+    return n;
+}
+
+size_t bssn_patch_workspace_bytes(const BssnPatch* patch, const BssnParams* params) {
+    if (!patch) return 0;
+    size_t cs = 1;
+    for (int d = 0; d < 3; ++d) cs *= (size_t)(patch->n[d] + 2 * patch->ghost);
+    const bool with_mom = params && params->kappa != 0.0;
+    return (3 * NCOMP + rhs_work_blocks(with_mom)) * cs * sizeof(double);
+}
+
+int bssn_patch_import(const BssnFields* in, double* patch_state, const BssnPatch* patch, void* stream) {
+    if (!fields_ok(in) || !patch_state) return fail(BSSN_ERR_INVALID, "null pointer");
+    Geo G;
+    int st = patch_geo(patch, nullptr, G);
+    if (st) return st;
+    const Box region = box_of(G);
+    BSSN_LAUNCH(KC_IMPORT, k_import, nblocks(region.count * NCOMP), kThreads, (cudaStream_t)stream, leaves_in(in), patch_state, G,
+                                                                                  region, region.count);
+    return cuda_status(cudaGetLastError(), "bssn_patch_import");
+}
+
+int bssn_patch_export(const double* patch_state, BssnFields* out, const BssnPatch* patch, void* stream) {
+    if (!fields_ok(out) || !patch_state) return fail(BSSN_ERR_INVALID, "null pointer");
+    Geo G;
+    int st = patch_geo(patch, nullptr, G);
+    if (st) return st;
+    const Box region = box_of(G);
+    BSSN_LAUNCH(KC_EXPORT, k_export, nblocks(region.count * NCOMP), kThreads, (cudaStream_t)stream, patch_state, leaves_out(out), G,
+                                                                                  region, region.count);
+    return cuda_status(cudaGetLastError(), "bssn_patch_export");
+}
+
+int bssn_patch_fill_periodic(double* patch_state, const BssnPatch* patch, void* stream) {
+    if (!patch_state) return fail(BSSN_ERR_INVALID, "null pointer");
+    Geo G;
+    int st = patch_geo(patch, nullptr, G);
+    if (st) return st;
+    return cuda_status(launch_fill_periodic(patch_state, NCOMP, G, (cudaStream_t)stream), "bssn_patch_fill_periodic");
+}
+
+int bssn_patch_rk4(double* patch_state, const BssnPatch* patch, const BssnParams* params, int32_t steps,
+                   void* workspace, size_t workspace_bytes, void* stream) {
+    if (!patch_state) return fail(BSSN_ERR_INVALID, "null pointer");
+    if (steps < 0) return fail(BSSN_ERR_INVALID, "steps must be non-negative");
+    int st = validate_params(params);
+    if (st) return st;
+    Geo G;
+    if ((st = patch_geo(patch, params, G))) return st;
+    const bool with_mom = params->kappa != 0.0;
+    if (!workspace || workspace_bytes < bssn_patch_workspace_bytes(patch, params))
+        return fail(BSSN_ERR_WORKSPACE, "workspace missing or smaller than bssn_patch_workspace_bytes");
+    cudaStream_t s = (cudaStream_t)stream;
+    double* us = (double*)workspace;
+    double* k = us + NCOMP * G.cs;
+    double* acc = k + NCOMP * G.cs;
+    RhsWork w = carve_rhs_work(acc + NCOMP * G.cs, G.cs, with_mom);
+    const Box region = box_of(G);
+    cudaError_t e = cudaSuccess;
+    for (int n = 0; n < steps && e == cudaSuccess; ++n) {
+        e = launch_project(patch_state, G, region, s);
+        if (e == cudaSuccess) e = rk4_step_patch(patch_state, us, k, acc, w, G, region, true, 0, s);
+    }
+    return cuda_status(e, "bssn_patch_rk4");
+}
+
+int bssn_patch_check_finite(const double* patch_state, const BssnPatch* patch, int32_t* device_flag,
+                            void* stream) {
+    if (!patch_state || !device_flag) return fail(BSSN_ERR_INVALID, "null pointer");
+    Geo G;
+    int st = patch_geo(patch, nullptr, G);
+    if (st) return st;
+    const Box region = box_of(G);
+    BSSN_LAUNCH(KC_OTHER, k_count_nonfinite, nblocks(region.count), kThreads, (cudaStream_t)stream, patch_state, G, region,
+                                                                                   (int*)device_flag);
+    return cuda_status(cudaGetLastError(), "bssn_patch_check_finite");
+}
+
+}  // extern "C"

@@ -1,0 +1,190 @@
+// Component numbering, point addressing and pointwise tensor algebra.
+//
+// Pointwise algebra follows JAX_BSSN/bssn/tensor_algebra.py: the inverse
+// conformal metric by the explicit Cholesky factor (:20-71), the closed-form
+// 3x3 determinant (:74-96), Christoffel symbols (:148-193) and the trace-free
+// part (:359-381).  The algebraic projection (JAX_BSSN/evolution/time_evolve.py:94-141)
+// is written with round-to-nearest intrinsics in the reference's operation
+// order and a correctly rounded det^(-1/3), so a projected conformal metric is
+// bit-identical to the float64 reference: that matters because its second
+// derivatives enter the Ricci tensor with a 1/dx^2 gain on any last-bit
+// difference.
+#pragma once
+
+#include "bssn_stencil.cuh"
+
+namespace bssn {
+
+enum Comp {
+    GXX = 0, GXY, GXZ, GYY, GYZ, GZZ, CW,
+    AXX, AXY, AXZ, AYY, AYZ, AZZ, CK,
+    GTX, GTY, GTZ, CALPHA, BX, BY, BZ, NCOMP
+};
+
+__host__ __device__ constexpr int sym(int i, int j) {
+    return (i == j) ? (i == 0 ? 0 : (i == 1 ? 3 : 5))
+                    : ((i + j == 1) ? 1 : ((i + j == 2) ? 2 : 4));
+}
+
+// Fields whose first derivatives are stored for composed mixed second
+// derivatives: gt (6), W, alpha, beta (3).
+constexpr int NMIX = 11;
+constexpr int MIX_G = 0, MIX_W = 6, MIX_ALPHA = 7, MIX_B = 8;
+__host__ __device__ constexpr int mix_source(int f) {
+    return f < 6 ? GXX + f : (f == 6 ? CW : (f == 7 ? CALPHA : BX + (f - 8)));
+}
+
+// Fields whose first derivatives are stored when kappa != 0 for the
+// momentum-constraint derivative: At (6), K, B_i^j (9) -- the latter from the
+// derived-field buffer.  Indexed after the NMIX base set.
+constexpr int NMIX_MOM = 16;
+
+// Compute box: linear thread index -> padded (x, y, z), z fastest.
+struct Box {
+    int lo[3];
+    int n[3];
+    long long count;
+    __device__ __forceinline__ void coords(long long t, int (&ix)[3]) const {
+        const long long yz = (long long)n[1] * n[2];
+        const int x = (int)(t / yz);
+        const long long r = t - (long long)x * yz;
+        const int y = (int)(r / n[2]);
+        ix[0] = lo[0] + x;
+        ix[1] = lo[1] + y;
+        ix[2] = lo[2] + (int)(r - (long long)y * n[2]);
+    }
+};
+
+__device__ __forceinline__ long long lin(const Geo& G, const int (&ix)[3]) {
+    return (long long)ix[0] * G.st[0] + (long long)ix[1] * G.st[1] + ix[2];
+}
+
+// ---------------------------------------------------------------------------
+// inverse metric by explicit Cholesky (tensor_algebra.py:20-71), FMA allowed
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void inverse_metric(const double (&g)[6], double (&gi)[6]) {
+    const double l00 = sqrt(g[0]);
+    const double r00 = 1.0 / l00;
+    const double l10 = g[1] * r00;
+    const double l20 = g[2] * r00;
+    const double l11 = sqrt(g[3] - l10 * l10);
+    const double r11 = 1.0 / l11;
+    const double l21 = (g[4] - l20 * l10) * r11;
+    const double l22 = sqrt(g[5] - l20 * l20 - l21 * l21);
+    const double r22 = 1.0 / l22;
+    const double m00 = r00, m11 = r11, m22 = r22;
+    const double m10 = -l10 * r00 * r11;
+    const double m20 = (l10 * l21 - l20 * l11) * (r00 * r11 * r22);
+    const double m21 = -l21 * r11 * r22;
+    gi[0] = m00 * m00 + m10 * m10 + m20 * m20;
+    gi[1] = m10 * m11 + m20 * m21;
+    gi[2] = m20 * m22;
+    gi[3] = m11 * m11 + m21 * m21;
+    gi[4] = m21 * m22;
+    gi[5] = m22 * m22;
+}
+
+// The same factorisation with every operation rounded in the reference's
+// order (used by the projection, whose output is part of the state).
+__device__ __forceinline__ void inverse_metric_rn(const double (&g)[6], double (&gi)[6]) {
+    const double l00 = __dsqrt_rn(g[0]);
+    const double l10 = __ddiv_rn(g[1], l00);
+    const double l20 = __ddiv_rn(g[2], l00);
+    const double l11 = __dsqrt_rn(__dadd_rn(g[3], -__dmul_rn(l10, l10)));
+    const double l21 = __ddiv_rn(__dadd_rn(g[4], -__dmul_rn(l20, l10)), l11);
+    const double l22 = __dsqrt_rn(__dadd_rn(__dadd_rn(g[5], -__dmul_rn(l20, l20)), -__dmul_rn(l21, l21)));
+    const double m00 = __ddiv_rn(1.0, l00);
+    const double m10 = __ddiv_rn(-l10, __dmul_rn(l00, l11));
+    const double m11 = __ddiv_rn(1.0, l11);
+    const double m20 = __ddiv_rn(__dadd_rn(__dmul_rn(l10, l21), -__dmul_rn(l20, l11)),
+                                 __dmul_rn(__dmul_rn(l00, l11), l22));
+    const double m21 = __ddiv_rn(-l21, __dmul_rn(l11, l22));
+    const double m22 = __ddiv_rn(1.0, l22);
+    gi[0] = __dadd_rn(__dadd_rn(__dmul_rn(m00, m00), __dmul_rn(m10, m10)), __dmul_rn(m20, m20));
+    gi[1] = __dadd_rn(__dmul_rn(m10, m11), __dmul_rn(m20, m21));
+    gi[2] = __dmul_rn(m20, m22);
+    gi[3] = __dadd_rn(__dmul_rn(m11, m11), __dmul_rn(m21, m21));
+    gi[4] = __dmul_rn(m21, m22);
+    gi[5] = __dmul_rn(m22, m22);
+}
+
+// Closed-form determinant of a symmetric 3x3 (six Sarrus products, fixed order).
+__device__ __forceinline__ double det_sym_rn(const double (&g)[6]) {
+    // g00 g11 g22 + g01 g12 g20 + g02 g10 g21 - g02 g11 g20 - g00 g12 g21 - g01 g10 g22
+    double acc = __dmul_rn(__dmul_rn(g[0], g[3]), g[5]);
+    acc = __dadd_rn(acc, __dmul_rn(__dmul_rn(g[1], g[4]), g[2]));
+    acc = __dadd_rn(acc, __dmul_rn(__dmul_rn(g[2], g[1]), g[4]));
+    acc = __dadd_rn(acc, -__dmul_rn(__dmul_rn(g[2], g[3]), g[2]));
+    acc = __dadd_rn(acc, -__dmul_rn(__dmul_rn(g[0], g[4]), g[4]));
+    acc = __dadd_rn(acc, -__dmul_rn(__dmul_rn(g[1], g[1]), g[5]));
+    return acc;
+}
+
+// ---------------------------------------------------------------------------
+// Correctly rounded x^(-1/3) for x > 0 (the projection's det^(-1/3)).
+//
+// rcbrt() gives y within a couple of ulp; one Newton step for y^-3 = x carried
+// in double-double (Dekker/Knuth error-free transformations) gives ~100 bits,
+// and the final rounding of the double-double sum yields the correctly
+// rounded result except within ~2^-100 of a rounding midpoint.  The float64
+// reference evaluates pow(det, -1.0/3.0); the double exponent exceeds -1/3 by
+// kPowThirdOffset, so the result is x^(-1/3) * (1 + kPowThirdOffset*ln x),
+// folded into the same correction before the single final rounding.
+// ---------------------------------------------------------------------------
+constexpr double kPowThirdOffset = 1.850371707708594e-17;
+
+__device__ __forceinline__ void two_prod(double a, double b, double& p, double& e) {
+    p = a * b;
+    e = fma(a, b, -p);
+}
+__device__ __forceinline__ void two_sum(double a, double b, double& s, double& e) {
+    s = a + b;
+    const double bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+__device__ __forceinline__ double inv_cbrt_cr(double x) {
+    if (!(x > 0.0) || isinf(x)) return pow(x, -1.0 / 3.0);
+    double y = rcbrt(x);
+    // r = 1 - x*y^3 in double-double, then y' = y + y*r/3.
+    double y2h, y2l;
+    two_prod(y, y, y2h, y2l);
+    double y3h, y3l;
+    two_prod(y2h, y, y3h, y3l);
+    y3l = fma(y2l, y, y3l);
+    double xyh, xyl;
+    two_prod(x, y3h, xyh, xyl);
+    xyl = fma(x, y3l, xyl);
+    double rh, rl;
+    two_sum(1.0, -xyh, rh, rl);
+    rl -= xyl;
+    const double r = rh + rl;
+    // correction c = y * (r/3 + offset*ln x), added to y then rounded once
+    const double c = y * (r * (1.0 / 3.0) + kPowThirdOffset * log(x));
+    double sh, sl;
+    two_sum(y, c, sh, sl);
+    return sh + sl;
+}
+
+// ---------------------------------------------------------------------------
+// Christoffel symbols from dg[k][sym(i,j)] = d_k g_ij
+//   c1[i][sym(j,k)] = Gamma_ijk = (d_k g_ij + d_j g_ik - d_i g_jk)/2
+//   c2[i][sym(j,k)] = Gamma^i_jk = g^im Gamma_mjk
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void christoffel(const double (&dg)[3][6], const double (&gi)[6],
+                                            double (&c1)[3][6], double (&c2)[3][6]) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+#pragma unroll
+            for (int k = j; k < 3; ++k)
+                c1[i][sym(j, k)] = 0.5 * (dg[k][sym(i, j)] + dg[j][sym(i, k)] - dg[i][sym(j, k)]);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int s = 0; s < 6; ++s)
+            c2[i][s] = gi[sym(i, 0)] * c1[0][s] + gi[sym(i, 1)] * c1[1][s] + gi[sym(i, 2)] * c1[2][s];
+}
+
+}  // namespace bssn

@@ -1,0 +1,31 @@
+// Internal host-side interface between the C ABI and the kernel launchers.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "bssn_stencil.cuh"
+
+namespace bssn {
+
+struct Box;
+
+// Device scratch of one RHS evaluation on a patch (component stride Geo::cs).
+struct RhsWork {
+    double* d1 = nullptr;    // inner first derivatives: 3 * (NMIX [+ NMIX_MOM]) blocks
+    double* der = nullptr;   // kappa != 0: gt^ij, B_i^j, B_i^j/W (24 blocks)
+    double* damp = nullptr;  // kappa != 0: constraint-damping term for At (6 blocks)
+};
+
+size_t rhs_work_blocks(bool with_mom);
+RhsWork carve_rhs_work(double* base, long long cs, bool with_mom);
+
+cudaError_t launch_rhs(const double* u, double* k, const RhsWork& w, const Geo& G, const Box& box,
+                       cudaStream_t stream);
+
+// H, M_i (3 blocks), det-1, tr At, Gamma constraint (3 blocks) on the box,
+// each block box.count long in the box's linear order.  Uses w.d1 (NMIX set)
+// and w.der.
+cudaError_t launch_constraints(const double* u, const RhsWork& w, const Geo& G, const Box& box, double* H,
+                               double* M, double* detm1, double* trA, double* gam, cudaStream_t stream);
+
+}  // namespace bssn

@@ -1,0 +1,64 @@
+"""Device-resident evolution of one grid in the padded patch layout.
+
+The drop-in ``rk4_step`` converts the seven reference leaves to the kernels'
+working layout on every call.  ``PatchEvolution`` keeps the state resident
+instead -- 21 independent float64 components, each a padded
+(nx+2G)(ny+2G)(nz+2G) block -- so a run of steps touches only HBM.  It is the
+same algorithm as ``rk4_step`` repeated (JAX_BSSN/evolution/time_evolve.py:144-217)
+on a periodic/Sommerfeld grid.
+"""
+
+from __future__ import annotations
+
+import torch
+
+from .. import _device, _native
+from ..bssn.variables import BSSNParameters, BSSNVariables
+
+NCOMP = 21
+
+
+class PatchEvolution:
+    def __init__(self, vars: BSSNVariables, params: BSSNParameters, ghost: int = 4):
+        if params.guard_cells or params.owned_shape is not None:
+            raise ValueError("PatchEvolution evolves a whole unpadded grid (guard_cells=0, owned_shape=None)")
+        self.lib = _native.load()
+        state, _ = _device.device_state(vars)
+        self.device = state.lapse.device
+        self.shape = _device.spatial_shape(state)
+        self.params = params
+        self.patch = _native.BssnPatch()
+        for d in range(3):
+            self.patch.n[d] = self.shape[d]
+        self.patch.ghost = int(ghost)
+        self.cparams = _device.to_params(params)
+        values = self.lib.bssn_patch_values(self.patch)
+        if values == 0:
+            raise ValueError("invalid patch description")
+        self.padded = tuple(n + 2 * ghost for n in self.shape)
+        self.u = torch.zeros(values, dtype=torch.float64, device=self.device)
+        nbytes = self.lib.bssn_patch_workspace_bytes(self.patch, self.cparams)
+        self.ws = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
+        _native.check(self.lib.bssn_patch_import(_device.fields_struct(state), self.u.data_ptr(), self.patch,
+                                                 _device.stream_handle()), "bssn_patch_import")
+
+    def step(self, steps: int = 1) -> None:
+        _native.check(self.lib.bssn_patch_rk4(self.u.data_ptr(), self.patch, self.cparams, int(steps),
+                                              self.ws.data_ptr(), self.ws.numel(), _device.stream_handle()),
+                      "bssn_patch_rk4")
+
+    def state(self) -> BSSNVariables:
+        out = _device.empty_state(self.shape, self.device)
+        _native.check(self.lib.bssn_patch_export(self.u.data_ptr(), _device.fields_struct(out), self.patch,
+                                                 _device.stream_handle()), "bssn_patch_export")
+        return out
+
+    def components(self) -> torch.Tensor:
+        """View of the resident state as (21, nx+2G, ny+2G, nz+2G)."""
+        return self.u.view(NCOMP, *self.padded)
+
+    def nonfinite_count(self) -> int:
+        flag = torch.zeros(1, dtype=torch.int32, device=self.device)
+        _native.check(self.lib.bssn_patch_check_finite(self.u.data_ptr(), self.patch, flag.data_ptr(),
+                                                       _device.stream_handle()), "bssn_patch_check_finite")
+        return int(flag.item())

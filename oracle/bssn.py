@@ -372,7 +372,7 @@ def compute_rhs(v, p):
 def project(v):
     """det(gamma_tilde) -> 1, then A_tilde -> trace-free (time_evolve.py:94-141)."""
     g = np.asarray(v.conformal_metric)
-    g = g * determinant(g) ** (-1.0 / 3.0)
+    g = g * inv_cbrt(determinant(g))
     A = trace_free(np.asarray(v.traceless_K), g, inverse_metric(g))
     return BSSNVariables(g, np.asarray(v.conformal_factor), A, np.asarray(v.trace_K),
                          np.asarray(v.conformal_connection), np.asarray(v.lapse), np.asarray(v.shift))
@@ -419,3 +419,57 @@ def constraint_norms(v, p):
         out[name + "_l2"] = float(np.sqrt(np.mean(field ** 2)))
         out[name + "_linf"] = float(np.max(np.abs(field)))
     return out
+
+
+# ----------------------------------------------------------------------------
+# correctly rounded x^(-1/3)
+# ----------------------------------------------------------------------------
+
+def _split(a):
+    c = 134217729.0 * a
+    hi = c - (c - a)
+    return hi, a - hi
+
+
+def _two_prod(a, b):
+    """Dekker's exact product a*b = p + e (no FMA needed)."""
+    p = a * b
+    ah, al = _split(a)
+    bh, bl = _split(b)
+    e = ((ah * bh - p) + ah * bl + al * bh) + al * bl
+    return p, e
+
+
+def _two_sum(a, b):
+    s = a + b
+    bb = s - a
+    return s, (a - (s - bb)) + (b - bb)
+
+
+# The double nearest -1/3 exceeds -1/3 by this much; pow(x, -1.0/3.0) is
+# x^(-1/3) * x^POW_THIRD_OFFSET.
+POW_THIRD_OFFSET = float(__import__("fractions").Fraction(-1.0 / 3.0) + __import__("fractions").Fraction(1, 3))
+
+
+def inv_cbrt(x):
+    """Correctly rounded pow(x, -1.0/3.0), as libm evaluates ``det ** (-1/3)``.
+
+    One Newton step for y^-3 = x carried in double-double, plus the tiny
+    correction for the double exponent differing from -1/3, then one rounding.
+    NumPy's SIMD power can differ from libm's in the last bit, so it only
+    supplies the starting guess.
+    """
+    x = np.asarray(x, dtype=np.float64)
+    with np.errstate(all="ignore"):
+        y = np.power(x, -1.0 / 3.0)
+        y2h, y2l = _two_prod(y, y)
+        y3h, y3l = _two_prod(y2h, y)
+        y3l = y3l + y2l * y
+        xyh, xyl = _two_prod(x, y3h)
+        xyl = xyl + x * y3l
+        rh, rl = _two_sum(np.ones_like(x), -xyh)
+        r = rh + (rl - xyl)
+        c = y * (r * (1.0 / 3.0) + POW_THIRD_OFFSET * np.log(x))
+        out = y + c
+    good = np.isfinite(x) & (x > 0)
+    return np.where(good, out, np.power(x, -1.0 / 3.0))

@@ -53,6 +53,12 @@ class ndarray(_np.ndarray):
     def block_until_ready(self):
         return self
 
+    def __pow__(self, other):
+        return power(self, other)
+
+    def __rpow__(self, other):
+        return power(other, self)
+
 
 Array = ndarray
 
@@ -209,7 +215,24 @@ tan = _w(_np.tan)
 exp = _w(_np.exp)
 log = _w(_np.log)
 arctan2 = _w(_np.arctan2)
-power = _w(_np.power)
+
+
+def power(x, y):
+    """Elementwise power through the platform libm (correctly rounded pow).
+
+    NumPy may route float64 ``power`` through SIMD approximations that differ
+    from libm in the last bit on some CPUs; the goldens must not depend on the
+    machine that generated them.  Squares are exact products.
+    """
+    import math
+    x = _np.asarray(x)
+    if _np.ndim(y) == 0 and float(y) == 2.0:
+        return _wrap(x * x)
+    y = _np.asarray(y, dtype=_np.float64)
+    xb, yb = _np.broadcast_arrays(x.astype(_np.float64), y)
+    out = _np.frompyfunc(math.pow, 2, 1)(xb, yb).astype(_np.float64)
+    return _wrap(out)
+
 floor = _w(_np.floor)
 ceil = _w(_np.ceil)
 round = _w(_np.round)

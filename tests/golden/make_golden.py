@@ -1,0 +1,146 @@
+"""Generate golden vectors by running the unmodified reference (uwplasma/JAX_BSSN).
+
+JAX is not installable in this environment, so the reference source is
+imported with ``tests/golden/jaxshim`` -- a NumPy stand-in for the part of the
+``jax`` API the hot path uses (``jit`` = identity, ``lax.cond`` = Python
+branch, single-device collectives) -- placed first on ``sys.path``.  Under it
+the reference's own derivative, boundary, FMR and Cartoon test suites pass.
+
+Usage (needs the reference checkout; the GPU machine does not have it):
+    python tests/golden/make_golden.py [/path/to/reference] [--no-long]
+
+Outputs ``tests/golden/*.npz``; each archive stores the inputs, the
+parameters (as a JSON string) and the reference outputs.
+"""
+
+from __future__ import annotations
+
+import json
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+REPO = HERE.parent.parent
+
+
+def _setup(reference: Path):
+    sys.path.insert(0, str(HERE / "jaxshim"))
+    sys.path.insert(0, str(reference))
+    sys.path.insert(0, str(REPO))
+
+
+def _params_json(params) -> str:
+    d = params._asdict()
+    return json.dumps({k: (list(v) if isinstance(v, tuple) else v) for k, v in d.items()})
+
+
+def _state_arrays(prefix, state):
+    names = ("conformal_metric", "conformal_factor", "traceless_K", "trace_K",
+             "conformal_connection", "lapse", "shift")
+    return {f"{prefix}.{n}": np.asarray(v, dtype=np.float64) for n, v in zip(names, state)}
+
+
+def make_stencils(out: Path):
+    from JAX_BSSN.evolution.derivatives import diff1_field, diff1_upwind_field, diff2_field, diff6_field
+    rng = np.random.default_rng(814)
+    shape = (12, 10, 14)
+    f = rng.normal(size=shape)
+    coef = rng.normal(size=shape)
+    coef[rng.random(shape) < 0.2] = 0.0
+    dx = 0.17
+    data = {"field": f, "coefficient": coef, "dx": np.float64(dx)}
+    cases = {"periodic": (0, 0), "sommerfeld": (1, 1), "left": (1, 0), "right": (0, 1)}
+    for cname, (lbc, rbc) in cases.items():
+        for q in (1.0, 1.0 / 16.0):
+            for axis in range(3):
+                key = f"{cname}.q{q:g}.axis{axis}"
+                data[f"d1.{key}"] = np.asarray(diff1_field(f, axis, dx, lbc, rbc, mad_q=q))
+                data[f"d2.{key}"] = np.asarray(diff2_field(f, axis, dx, lbc, rbc, mad_q=q))
+                data[f"up.{key}"] = np.asarray(diff1_upwind_field(f, coef, axis, dx, lbc, rbc, mad_q=q))
+                if q == 1.0:
+                    data[f"d6.{key}"] = np.asarray(diff6_field(f, axis, dx, lbc, rbc))
+    np.savez_compressed(out, **data)
+
+
+def rhs_cases():
+    from jax_bssn_gb300.initial_data import gauge_wave_config, random_smooth_state
+    from JAX_BSSN.bssn.variables import BSSNParameters as P
+    cases = {}
+    state, params = gauge_wave_config(n=12, nu=0.1)
+    cases["gauge_wave"] = (state, P(**params._asdict()))
+    smooth = random_smooth_state((10, 10, 10), seed=3)
+    cases["generic_kappa"] = (smooth, P(eta=2.0, kappa=0.3, nu=0.05, g=0.75, dx=0.1, dt=0.02,
+                                         gauge=1, zero_shift=0, x_min=-0.4, y_min=0.1, z_min=0.3))
+    cases["sommerfeld"] = (random_smooth_state((10, 9, 11), seed=5),
+                           P(eta=1.0, kappa=0.0, nu=0.02, g=0.75, dx=0.1, dt=0.02, gauge=1,
+                             xl_bc=1, xr_bc=1, yl_bc=1, yr_bc=1, zl_bc=1, zr_bc=1,
+                             x_min=-0.45, y_min=-0.4, z_min=-0.5))
+    cases["mad_mixed"] = (random_smooth_state((10, 10, 10), seed=7),
+                          P(eta=1.0, kappa=0.1, nu=0.02, g=0.75, dx=0.1, dt=0.02, gauge=0,
+                            mad_q=1.0 / 16.0, xl_bc=1, xr_bc=0, x_min=-0.3, y_min=0.2, z_min=-0.1))
+    cases["mad_periodic_zero_shift"] = (random_smooth_state((10, 10, 10), seed=9, shift=False),
+                                        P(eta=1.0, kappa=0.0, nu=0.02, g=0.75, dx=0.1, dt=0.02, gauge=0,
+                                          mad_q=1.0 / 16.0, zero_shift=1))
+    return cases
+
+
+def make_rhs(out_dir: Path):
+    from JAX_BSSN.evolution.time_evolve import compute_bssn_rhs, rk4_step, enforce_algebraic_constraints
+    from JAX_BSSN.bssn.constraints import compute_all_constraints
+    for name, (state, params) in rhs_cases().items():
+        data = {"params": np.asarray(_params_json(params))}
+        data.update(_state_arrays("input", state))
+        data.update(_state_arrays("rhs", compute_bssn_rhs(state, params)))
+        data.update(_state_arrays("project", enforce_algebraic_constraints(state)))
+        step = rk4_step(state, params)
+        data.update(_state_arrays("rk4_1", step))
+        data.update(_state_arrays("rk4_2", rk4_step(step, params)))
+        c = compute_all_constraints(state, params)
+        for field in c._fields:
+            data[f"constraints.{field}"] = np.asarray(getattr(c, field))
+        np.savez_compressed(out_dir / f"rhs_{name}.npz", **data)
+
+
+def make_long_runs(out_dir: Path):
+    """Multi-step reference runs on the headline parity workloads."""
+    from JAX_BSSN.evolution.time_evolve import rk4_step
+    from JAX_BSSN.bssn.variables import BSSNParameters as P
+    from jax_bssn_gb300.initial_data import gauge_wave_config, teukolsky_config
+    # 32^3 periodic gauge wave, A=0.1, harmonic, zero shift, CFL 0.25, nu=0.1: 1 and 100 steps
+    state, params = gauge_wave_config(n=32, nu=0.1)
+    params = P(**params._asdict())
+    data = {"params": np.asarray(_params_json(params))}
+    data.update(_state_arrays("input", state))
+    for n in range(1, 101):
+        state = rk4_step(state, params)
+        if n in (1, 10, 100):
+            data.update(_state_arrays(f"rk4_{n}", state))
+    np.savez_compressed(out_dir / "run_gauge_wave32.npz", **data)
+    # linearised Teukolsky wave on 24^3 (Sommerfeld, 1+log, Gamma-driver): 1 and 10 steps
+    state, params = teukolsky_config(n=24)
+    params = P(**params._asdict())
+    data = {"params": np.asarray(_params_json(params))}
+    data.update(_state_arrays("input", state))
+    for n in range(1, 11):
+        state = rk4_step(state, params)
+        if n in (1, 10):
+            data.update(_state_arrays(f"rk4_{n}", state))
+    np.savez_compressed(out_dir / "run_teukolsky24.npz", **data)
+
+
+def main(argv):
+    args = [a for a in argv[1:] if not a.startswith("--")]
+    reference = Path(args[0]) if args else Path("/root/reference")
+    _setup(reference)
+    make_stencils(HERE / "stencils.npz")
+    make_rhs(HERE)
+    if "--no-long" not in argv:
+        make_long_runs(HERE)
+    for path in sorted(HERE.glob("*.npz")):
+        print(f"{path.name}: {path.stat().st_size / 1024:.0f} KiB")
+
+
+if __name__ == "__main__":
+    main(sys.argv)

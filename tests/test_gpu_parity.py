@@ -1,0 +1,156 @@
+"""CUDA path (through the C ABI) against the reference goldens and the oracle.
+
+Metric: per reference leaf, max|cuda - ref| / max|ref| (norm-relative).
+Tolerances are the ones the target states for the plain FP64 kernels:
+1e-12 after one RK4 step, 1e-10 after 100 steps; the RHS itself is held to
+1e-11 (it is a sum of large terms whose last-bit rounding is not pinned).
+"""
+
+import numpy as np
+import pytest
+
+from oracle import bssn as ob
+from oracle.state import BSSNParameters as OracleParams
+from oracle.state import BSSNVariables as OracleVars
+
+from .helpers import RHS_CASES, field_errors, golden_params, golden_state, load_golden, worst
+
+pytestmark = pytest.mark.gpu
+
+RHS_TOL = 1e-11
+STEP_TOL = 1e-12
+LONG_TOL = 1e-10
+
+
+@pytest.fixture(scope="module")
+def gb(cuda, native):
+    import jax_bssn_gb300 as pkg
+    from jax_bssn_gb300.evolution import time_evolve
+    from jax_bssn_gb300.bssn import constraints
+    return pkg, time_evolve, constraints
+
+
+def _inputs(data, pkg):
+    return golden_state(data, "input", pkg.BSSNVariables), golden_params(data, pkg.BSSNParameters)
+
+
+@pytest.mark.parametrize("name", RHS_CASES)
+def test_rhs_matches_reference(gb, name):
+    pkg, te, _ = gb
+    data = load_golden(f"rhs_{name}")
+    state, params = _inputs(data, pkg)
+    rhs = te.compute_bssn_rhs(state, params)
+    err = field_errors(rhs, golden_state(data, "rhs", OracleVars))
+    print(name, "rhs", {k: f"{v:.2e}" for k, v in err.items()})
+    assert worst(err) < RHS_TOL
+
+
+@pytest.mark.parametrize("name", RHS_CASES)
+def test_projection_is_bitwise(gb, name):
+    pkg, te, _ = gb
+    data = load_golden(f"rhs_{name}")
+    state, _ = _inputs(data, pkg)
+    out = te.enforce_algebraic_constraints(state)
+    expect = ob.project(golden_state(data, "input", OracleVars))
+    err = field_errors(out, expect)
+    assert err["conformal_metric"] == 0.0, err
+    assert worst(err) < 1e-15, err
+
+
+@pytest.mark.parametrize("name", RHS_CASES)
+def test_rk4_two_steps(gb, name):
+    pkg, te, _ = gb
+    data = load_golden(f"rhs_{name}")
+    state, params = _inputs(data, pkg)
+    one = te.rk4_step(state, params)
+    e1 = field_errors(one, golden_state(data, "rk4_1", OracleVars))
+    two = te.rk4_step(one, params)
+    e2 = field_errors(two, golden_state(data, "rk4_2", OracleVars))
+    print(name, "rk4 1:", f"{worst(e1):.2e}", "2:", f"{worst(e2):.2e}")
+    assert worst(e1) < STEP_TOL
+    assert worst(e2) < 2 * STEP_TOL
+
+
+@pytest.mark.parametrize("name", RHS_CASES)
+def test_constraints(gb, name):
+    pkg, _, cons = gb
+    data = load_golden(f"rhs_{name}")
+    state, params = _inputs(data, pkg)
+    out = cons.compute_all_constraints(state, params)
+    for value, field in zip(out, ("hamiltonian", "momentum", "det_gamma", "trace_A", "gamma_condition")):
+        ref = data[f"constraints.{field}"]
+        scale = max(float(np.max(np.abs(ref))), 1e-300)
+        err = float(np.max(np.abs(value - ref))) / scale
+        print(name, field, f"{err:.2e}")
+        # det-1 and tr A of a generic state are O(1e-2) differences of O(1) numbers
+        assert err < (1e-13 if field in ("det_gamma", "trace_A") else RHS_TOL), field
+
+
+def test_gauge_wave_32_one_and_hundred_steps(gb):
+    """Target parity: 1e-12 after one RK4 step, 1e-10 after 100 (32^3, A=0.1)."""
+    pkg, te, _ = gb
+    data = load_golden("run_gauge_wave32")
+    state, params = _inputs(data, pkg)
+    one = te.rk4_step(state, params)
+    e1 = field_errors(one, golden_state(data, "rk4_1", OracleVars))
+    ten = te.rk4_steps(one, params, 9)
+    e10 = field_errors(ten, golden_state(data, "rk4_10", OracleVars))
+    hundred = te.rk4_steps(ten, params, 90)
+    e100 = field_errors(hundred, golden_state(data, "rk4_100", OracleVars))
+    print("gauge wave 1:", {k: f"{v:.1e}" for k, v in e1.items()})
+    print("gauge wave 100:", {k: f"{v:.1e}" for k, v in e100.items()})
+    assert worst(e1) < STEP_TOL
+    assert worst(e10) < LONG_TOL
+    assert worst(e100) < LONG_TOL
+
+
+def test_teukolsky_24_steps(gb):
+    """Linearised Teukolsky wave, Sommerfeld faces, 1+log + Gamma driver."""
+    pkg, te, _ = gb
+    data = load_golden("run_teukolsky24")
+    state, params = _inputs(data, pkg)
+    one = te.rk4_step(state, params)
+    e1 = field_errors(one, golden_state(data, "rk4_1", OracleVars))
+    ten = te.rk4_steps(one, params, 9)
+    e10 = field_errors(ten, golden_state(data, "rk4_10", OracleVars))
+    print("teukolsky 1:", {k: f"{v:.1e}" for k, v in e1.items()})
+    print("teukolsky 10:", {k: f"{v:.1e}" for k, v in e10.items()})
+    assert worst(e1) < STEP_TOL
+    assert worst(e10) < LONG_TOL
+
+
+def test_patch_evolution_matches_reference_layout(gb):
+    """The resident patch path is the same arithmetic as rk4_step."""
+    pkg, te, _ = gb
+    from jax_bssn_gb300.evolution import PatchEvolution
+    from jax_bssn_gb300.initial_data import teukolsky_config
+    state, params = teukolsky_config(n=20)
+    ref = te.rk4_steps(state, params, 3)
+    evo = PatchEvolution(state, params)
+    evo.step(3)
+    err = field_errors(evo.state(), ref)
+    assert worst(err) == 0.0, err
+    assert evo.nonfinite_count() == 0
+
+
+def test_cuda_against_oracle_generic_state(gb):
+    """A generic smooth state with every term active, against the oracle."""
+    pkg, te, _ = gb
+    from jax_bssn_gb300.initial_data import random_smooth_state
+    state = random_smooth_state((14, 12, 16), seed=21)
+    params = pkg.BSSNParameters(eta=1.5, kappa=0.05, nu=0.03, g=0.75, dx=0.07, dt=0.01, gauge=1,
+                                xl_bc=1, xr_bc=1, zl_bc=1, zr_bc=1, x_min=-0.4, y_min=0.0, z_min=-0.5)
+    rhs = te.compute_bssn_rhs(state, params)
+    expect = ob.compute_rhs(OracleVars(*state), OracleParams(**params._asdict()))
+    assert worst(field_errors(rhs, expect)) < RHS_TOL
+    step = te.rk4_step(state, params)
+    expect = ob.rk4_step(OracleVars(*state), OracleParams(**params._asdict()))
+    assert worst(field_errors(step, expect)) < STEP_TOL
+
+
+def test_invalid_input_raises_value_error(gb):
+    pkg, te, _ = gb
+    from jax_bssn_gb300.initial_data import random_smooth_state
+    state = random_smooth_state((6, 10, 10), seed=1)
+    with pytest.raises(ValueError):
+        te.compute_bssn_rhs(state, pkg.BSSNParameters(dx=0.1, xl_bc=1))

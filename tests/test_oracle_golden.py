@@ -1,0 +1,79 @@
+"""The oracle against golden vectors produced by the reference itself.
+
+The goldens come from running the unmodified reference source under a NumPy
+jax stand-in (tests/golden/make_golden.py).  The oracle restates the same
+arithmetic; agreement is bit-level except where the reference's libm pow
+rounds det^(-1/3) differently from the correctly rounded value the oracle
+uses (a last-bit effect on a fraction of points).
+"""
+
+import numpy as np
+import pytest
+
+from oracle import bssn as ob
+from oracle import stencils as st
+from oracle.state import BSSNParameters, BSSNVariables
+
+from .helpers import RHS_CASES, field_errors, golden_params, golden_state, load_golden, worst
+
+
+@pytest.fixture(scope="module")
+def stencil_data():
+    return load_golden("stencils")
+
+
+@pytest.mark.parametrize("case,lbc,rbc", [("periodic", 0, 0), ("sommerfeld", 1, 1), ("left", 1, 0), ("right", 0, 1)])
+@pytest.mark.parametrize("q", [1.0, 1.0 / 16.0])
+@pytest.mark.parametrize("axis", [0, 1, 2])
+def test_stencils_bitwise(stencil_data, case, lbc, rbc, q, axis):
+    f, c, dx = stencil_data["field"], stencil_data["coefficient"], float(stencil_data["dx"])
+    key = f"{case}.q{q:g}.axis{axis}"
+    np.testing.assert_array_equal(st.d1(f, axis, dx, lbc, rbc, q), stencil_data[f"d1.{key}"])
+    np.testing.assert_array_equal(st.d2(f, axis, dx, lbc, rbc, q), stencil_data[f"d2.{key}"])
+    np.testing.assert_array_equal(st.d1_upwind(f, c, axis, dx, lbc, rbc, q), stencil_data[f"up.{key}"])
+    if q == 1.0:
+        np.testing.assert_array_equal(st.d6(f, axis, dx, lbc, rbc), stencil_data[f"d6.{key}"])
+
+
+@pytest.mark.parametrize("name", RHS_CASES)
+def test_rhs_matches_reference(name):
+    data = load_golden(f"rhs_{name}")
+    state = golden_state(data, "input", BSSNVariables)
+    params = golden_params(data, BSSNParameters)
+    rhs = ob.compute_rhs(state, params)
+    assert worst(field_errors(rhs, golden_state(data, "rhs", BSSNVariables))) == 0.0
+
+
+@pytest.mark.parametrize("name", RHS_CASES)
+def test_projection_and_rk4_match_reference(name):
+    data = load_golden(f"rhs_{name}")
+    state = golden_state(data, "input", BSSNVariables)
+    params = golden_params(data, BSSNParameters)
+    assert worst(field_errors(ob.project(state), golden_state(data, "project", BSSNVariables))) < 1e-15
+    one = ob.rk4_step(state, params)
+    assert worst(field_errors(one, golden_state(data, "rk4_1", BSSNVariables))) < 1e-13
+    two = ob.rk4_step(one, params)
+    assert worst(field_errors(two, golden_state(data, "rk4_2", BSSNVariables))) < 1e-13
+
+
+@pytest.mark.parametrize("name", RHS_CASES)
+def test_constraints_match_reference(name):
+    data = load_golden(f"rhs_{name}")
+    state = golden_state(data, "input", BSSNVariables)
+    params = golden_params(data, BSSNParameters)
+    ours = ob.constraints(state, params)
+    for value, field in zip(ours, ("hamiltonian", "momentum", "det_gamma", "trace_A", "gamma_condition")):
+        ref = data[f"constraints.{field}"]
+        scale = max(np.max(np.abs(ref)), 1e-300)
+        assert np.max(np.abs(value - ref)) / scale < 1e-13, field
+
+
+def test_inv_cbrt_is_correctly_rounded():
+    import decimal
+    decimal.getcontext().prec = 60
+    rng = np.random.default_rng(11)
+    x = np.concatenate([1 + 1e-3 * rng.normal(size=400), np.exp(rng.normal(size=400))])
+    y = ob.inv_cbrt(x)
+    exponent = decimal.Decimal(-1.0 / 3.0)
+    exact = np.array([float(decimal.Decimal(float(v)) ** exponent) for v in x])
+    np.testing.assert_array_equal(y, exact)
