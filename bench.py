@@ -47,7 +47,7 @@ RHS_AT_BYTES_PER_POINT = 480     # k_rhs_at: 21 state + 33 derivative values rea
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
     ap.add_argument("--n", type=int, default=128)
