@@ -101,6 +101,20 @@ int bssn_rhs(const BssnFields* in, BssnFields* out, const int32_t shape[3],
              const BssnParams* params, const BssnMatter* matter,
              void* workspace, size_t workspace_bytes, void* stream);
 
+/* No counterpart in the reference.  bssn_rhs for callers that cannot allocate
+ * device memory (a host framework that owns all device memory, a solver with a
+ * memory budget fixed at start-up, a loop that must avoid the synchronisation
+ * of cudaMalloc/cudaFree): same inputs, outputs and results as bssn_rhs, but
+ * the work buffer is an array built into the library (26.9 MB of device
+ * memory, held on every GPU that loads the library until the process exits).
+ * Limit: (nx+8)*(ny+8)*(nz+8) <= 21952 samples (e.g. 20x20x20); larger arrays
+ * return BSSN_ERR_INVALID.  The first call on each device looks up the
+ * array's device address with that device current; make that first call
+ * before any stream capture.  All calls share the one array, so calls that
+ * overlap on the GPU (different streams or threads) race; serialise them. */
+int bssn_rhs_noalloc(const BssnFields* in, BssnFields* out, const int32_t shape[3],
+                     const BssnParams* params, void* stream);
+
 /* enforce_algebraic_constraints(vars) (time_evolve.py:134-141): det(gt)=1 then
  * trace-free At.  In place on all samples of the array. */
 int bssn_project(BssnFields* state, const int32_t shape[3], void* stream);

@@ -70,6 +70,8 @@ SIGNATURES = {
     "bssn_rhs": (ctypes.c_int, [ctypes.POINTER(BssnFields), ctypes.POINTER(BssnFields), Shape3,
                                 ctypes.POINTER(BssnParams), ctypes.POINTER(BssnMatter),
                                 ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    "bssn_rhs_noalloc": (ctypes.c_int, [ctypes.POINTER(BssnFields), ctypes.POINTER(BssnFields), Shape3,
+                                        ctypes.POINTER(BssnParams), ctypes.c_void_p]),
     "bssn_project": (ctypes.c_int, [ctypes.POINTER(BssnFields), Shape3, ctypes.c_void_p]),
     "bssn_rk4_step": (ctypes.c_int, [ctypes.POINTER(BssnFields), Shape3, ctypes.POINTER(BssnParams),
                                      ctypes.c_int32, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
