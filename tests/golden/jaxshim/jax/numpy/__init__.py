@@ -217,6 +217,50 @@ log = _w(_np.log)
 arctan2 = _w(_np.arctan2)
 
 
+def _pow_minus_third(x):
+    """Correctly rounded pow(x, -1.0/3.0).
+
+    The libm result is refined by one Newton step on y^-3 = x evaluated with
+    error-free transformations (Veltkamp splitting), including the offset of
+    the double exponent from -1/3, and rounded once.  glibc's pow misrounds
+    about 0.07 % of these values; a correctly rounded result does not depend on
+    the libm of the machine that generates the goldens.
+    """
+    import math
+    from fractions import Fraction
+    offset = float(Fraction(-1.0 / 3.0) + Fraction(1, 3))
+    flat = x.reshape(-1)
+    out = _np.empty_like(flat)
+
+    def split(v):
+        c = 134217729.0 * v
+        hi = c - (c - v)
+        return hi, v - hi
+
+    def prod(a, b):
+        p = a * b
+        ah, al = split(a)
+        bh, bl = split(b)
+        return p, ((ah * bh - p) + ah * bl + al * bh) + al * bl
+
+    for i, v in enumerate(flat.tolist()):
+        if not (v > 0.0) or math.isinf(v):
+            out[i] = math.pow(v, -1.0 / 3.0)
+            continue
+        y = math.pow(v, -1.0 / 3.0)
+        y2, y2e = prod(y, y)
+        y3, y3e = prod(y2, y)
+        y3e += y2e * y
+        xy, xye = prod(v, y3)
+        xye += v * y3e
+        s = 1.0 - xy
+        bb = s - 1.0
+        err = (1.0 - (s - bb)) + (-xy - bb)
+        r = s + (err - xye)
+        out[i] = y + y * (r / 3.0 + offset * math.log(v))
+    return out.reshape(x.shape)
+
+
 def power(x, y):
     """Elementwise power through the platform libm (correctly rounded pow).
 
@@ -228,6 +272,8 @@ def power(x, y):
     x = _np.asarray(x)
     if _np.ndim(y) == 0 and float(y) == 2.0:
         return _wrap(x * x)
+    if _np.ndim(y) == 0 and float(y) == -1.0 / 3.0:
+        return _wrap(_pow_minus_third(x.astype(_np.float64)))
     y = _np.asarray(y, dtype=_np.float64)
     xb, yb = _np.broadcast_arrays(x.astype(_np.float64), y)
     out = _np.frompyfunc(math.pow, 2, 1)(xb, yb).astype(_np.float64)
@@ -249,7 +295,22 @@ isnan = _w(_np.isnan)
 isclose = _w(_np.isclose)
 allclose = _np.allclose
 sign = _w(_np.sign)
-sum = _w(_np.sum)
+
+
+def sum(a, axis=None, dtype=None, keepdims=False, **kwargs):
+    """Reductions along one short axis accumulate left to right, the order of
+    XLA's reduce loop; NumPy's pairwise scheme rounds differently."""
+    a = _np.asarray(a)
+    if isinstance(axis, int) and a.ndim and a.shape[axis] <= 16 and dtype is None and not kwargs:
+        moved = _np.moveaxis(a, axis, 0)
+        acc = moved[0].copy() if moved.shape[0] else _np.zeros(moved.shape[1:], a.dtype)
+        for k in range(1, moved.shape[0]):
+            acc = acc + moved[k]
+        if keepdims:
+            acc = _np.expand_dims(acc, axis)
+        return _wrap(acc)
+    return _wrap(_np.sum(a, axis=axis, dtype=dtype, keepdims=keepdims, **kwargs))
+
 mean = _w(_np.mean)
 max = _w(_np.max)
 min = _w(_np.min)

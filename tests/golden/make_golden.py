@@ -36,6 +36,10 @@ def _params_json(params) -> str:
     return json.dumps({k: (list(v) if isinstance(v, tuple) else v) for k, v in d.items()})
 
 
+LEAF_NAMES = ("conformal_metric", "conformal_factor", "traceless_K", "trace_K",
+              "conformal_connection", "lapse", "shift")
+
+
 def _state_arrays(prefix, state):
     names = ("conformal_metric", "conformal_factor", "traceless_K", "trace_K",
              "conformal_connection", "lapse", "shift")
@@ -130,12 +134,84 @@ def make_long_runs(out_dir: Path):
     np.savez_compressed(out_dir / "run_teukolsky24.npz", **data)
 
 
+def _owned_arrays(prefix, states, guard_first=0):
+    """Owned samples of tiled states (tile axes dropped)."""
+    out = {}
+    for patch, state in enumerate(states):
+        for name, leaf in zip(LEAF_NAMES, state):
+            a = np.asarray(leaf)
+            a = a.reshape(a.shape[:-6] + a.shape[-3:])
+            g = 4
+            out[f"{prefix}.{patch}.{name}"] = a[..., g:-g, g:-g, g:-g]
+    return out
+
+
+def _padded_arrays(prefix, state, patch):
+    out = {}
+    for name, leaf in zip(LEAF_NAMES, state):
+        a = np.asarray(leaf)
+        out[f"{prefix}.{patch}.{name}"] = a.reshape(a.shape[:-6] + a.shape[-3:])
+    return out
+
+
+def fmr_cases():
+    from JAX_BSSN.bssn.variables import BSSNParameters as P, BSSNVariables as V
+    from JAX_BSSN.fmr import FMRHierarchySpec, FMRPatchSpec
+    from jax_bssn_gb300.initial_data import gauge_wave_state
+
+    def smooth(coordinates, params):
+        x, y, z = np.broadcast_arrays(*[np.asarray(c) for c in coordinates])
+        phase = x + 0.03 * np.sin(2 * np.pi * y) * np.cos(2 * np.pi * z)
+        state = gauge_wave_state(phase, y, z, amplitude=0.01)
+        shift = np.stack((0.1 + 0.01 * np.sin(2 * np.pi * y), -0.05 + 0.005 * np.cos(2 * np.pi * z),
+                          0.025 + 0.003 * np.sin(2 * np.pi * x)))
+        return V(*state[:-1], shift)
+
+    cases = {}
+    cases["three_level_mad"] = (smooth, P(dx=1 / 12, dt=0.0005, eta=0.0, g=0.0, nu=0.005,
+                                          x_min=-0.5, y_min=-0.5, z_min=-0.5), (12, 12, 12),
+                                FMRHierarchySpec((FMRPatchSpec((3,) * 3, (8,) * 3), FMRPatchSpec((2,) * 3, (4,) * 3))))
+    cases["sommerfeld_kappa"] = (smooth, P(dx=1 / 14, dt=0.001, eta=1.0, g=0.75, nu=0.02, kappa=0.1, gauge=1,
+                                           xl_bc=1, xr_bc=1, yl_bc=1, yr_bc=1, zl_bc=1, zr_bc=1,
+                                           x_min=-0.45, y_min=-0.45, z_min=-0.45), (14, 14, 14),
+                                 FMRHierarchySpec((FMRPatchSpec((5,) * 3, (8,) * 3),)))
+    cases["siblings_no_mad"] = (smooth, P(dx=1 / 12, dt=0.0005, eta=0.5, g=0.5, nu=0.01,
+                                          x_min=-0.5, y_min=-0.5, z_min=-0.5), (12, 12, 12),
+                                FMRHierarchySpec((FMRPatchSpec((2,) * 3, (4,) * 3),
+                                                  FMRPatchSpec((6, 2, 3), (9, 5, 6), parent=0)), use_mad=False))
+    return cases
+
+
+def make_fmr(out_dir: Path):
+    from JAX_BSSN.fmr import initialize_tiled_fmr, fmr_stage, fmr_rk4_step, fmr_constraint_norms
+    for name, (initial, params, shape, hierarchy) in fmr_cases().items():
+        states, parameters, layouts = initialize_tiled_fmr(initial, params, shape, hierarchy)
+        data = {"hierarchy": np.asarray(json.dumps({
+            "patches": [[list(s.coarse_lo), list(s.coarse_hi), s.parent] for s in hierarchy.patches],
+            "use_mad": hierarchy.use_mad})), "root_params": np.asarray(_params_json(params)),
+            "root_shape": np.asarray(shape)}
+        data.update(_owned_arrays("initial", states))
+        prepared, rhs = fmr_stage(states, parameters, hierarchy, layouts=layouts)
+        data.update(_owned_arrays("stage1_rhs", rhs))
+        last = len(states) - 1
+        data.update(_padded_arrays("stage1_prepared", prepared[last], last))
+        one = fmr_rk4_step(states, parameters, hierarchy, layouts=layouts)
+        data.update(_owned_arrays("rk4_1", one))
+        data.update(_padded_arrays("rk4_1_padded", one[last], last))
+        two = fmr_rk4_step(one, parameters, hierarchy, layouts=layouts)
+        data.update(_owned_arrays("rk4_2", two))
+        norms = fmr_constraint_norms(two, parameters, hierarchy, layouts=layouts)
+        data["norms"] = np.asarray(json.dumps({k: float(v) for k, v in norms.items()}))
+        np.savez_compressed(out_dir / f"fmr_{name}.npz", **data)
+
+
 def main(argv):
     args = [a for a in argv[1:] if not a.startswith("--")]
     reference = Path(args[0]) if args else Path("/root/reference")
     _setup(reference)
     make_stencils(HERE / "stencils.npz")
     make_rhs(HERE)
+    make_fmr(HERE)
     if "--no-long" not in argv:
         make_long_runs(HERE)
     for path in sorted(HERE.glob("*.npz")):

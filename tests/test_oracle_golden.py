@@ -1,10 +1,9 @@
 """The oracle against golden vectors produced by the reference itself.
 
 The goldens come from running the unmodified reference source under a NumPy
-jax stand-in (tests/golden/make_golden.py).  The oracle restates the same
-arithmetic; agreement is bit-level except where the reference's libm pow
-rounds det^(-1/3) differently from the correctly rounded value the oracle
-uses (a last-bit effect on a fraction of points).
+jax stand-in (tests/golden/make_golden.py), which evaluates pow(det, -1/3)
+correctly rounded.  The oracle restates the same arithmetic and agrees with
+the goldens bit for bit.
 """
 
 import numpy as np
@@ -49,11 +48,11 @@ def test_projection_and_rk4_match_reference(name):
     data = load_golden(f"rhs_{name}")
     state = golden_state(data, "input", BSSNVariables)
     params = golden_params(data, BSSNParameters)
-    assert worst(field_errors(ob.project(state), golden_state(data, "project", BSSNVariables))) < 1e-15
+    assert worst(field_errors(ob.project(state), golden_state(data, "project", BSSNVariables))) == 0.0
     one = ob.rk4_step(state, params)
-    assert worst(field_errors(one, golden_state(data, "rk4_1", BSSNVariables))) < 1e-13
+    assert worst(field_errors(one, golden_state(data, "rk4_1", BSSNVariables))) == 0.0
     two = ob.rk4_step(one, params)
-    assert worst(field_errors(two, golden_state(data, "rk4_2", BSSNVariables))) < 1e-13
+    assert worst(field_errors(two, golden_state(data, "rk4_2", BSSNVariables))) == 0.0
 
 
 @pytest.mark.parametrize("name", RHS_CASES)
