@@ -153,6 +153,57 @@ int bssn_patch_rk4(double* patch_state, const BssnPatch* patch, const BssnParams
 int bssn_patch_check_finite(const double* patch_state, const BssnPatch* patch,
                             int32_t* device_flag, void* stream);
 
+/* Whole-array conversion between the reference layout (seven leaves) and the
+ * 21-component layout, over all samples of an array of the given extent
+ * (e.g. a padded FMR patch, whose guards are part of the array). */
+int bssn_fields_to_components(const BssnFields* in, double* state, const int32_t extent[3], void* stream);
+int bssn_components_to_fields(const double* state, BssnFields* out, const int32_t extent[3], void* stream);
+
+/* ---------------- fixed mesh refinement (single-tile patches) ---------------- */
+
+/* One patch of a vertex-centred 2:1 hierarchy (JAX_BSSN/fmr/refinement.py:15-75).
+ * States are in the resident layout with ghost 4: 21 x (n+8)^3 doubles. */
+typedef struct BssnFmrPatch {
+    int32_t n[3];          /* active (owned) samples per axis; children: 2*(hi-lo)+1 */
+    int32_t parent;        /* parent patch index (< own index), -1 for the root */
+    int32_t coarse_lo[3];  /* inclusive bounds in the parent's active indices */
+    int32_t coarse_hi[3];
+} BssnFmrPatch;
+
+/* Workspace for bssn_fmr_rk4_step / bssn_fmr_stage_rhs on this hierarchy. */
+size_t bssn_fmr_workspace_bytes(const BssnFmrPatch* patches, const BssnParams* params, int32_t npatch);
+/* refresh_bssn_halos of one single-tile patch: periodic self-wrap, linear
+ * exterior on Sommerfeld faces (JAX_BSSN/parallel/communication.py:144-214). */
+int bssn_fmr_refresh(double* state, const int32_t n[3], const int32_t codes[6], void* stream);
+/* fill_tiled_fine_ghosts (JAX_BSSN/fmr/transfer.py:237-244): six-node Lagrange
+ * prolongation of the prepared parent into the child's exterior shell. */
+int bssn_fmr_prolong(const double* parent, const int32_t parent_n[3], double* child,
+                     const int32_t child_n[3], const int32_t coarse_lo[3], void* stream);
+/* restrict_tiled_to_coarse (JAX_BSSN/fmr/transfer.py:247-252): injection of
+ * coincident owned fine vertices into the parent. */
+int bssn_fmr_inject(double* parent, const int32_t parent_n[3], const double* child,
+                    const int32_t child_n[3], const int32_t coarse_lo[3], void* stream);
+/* prepare_fmr_states (JAX_BSSN/fmr/tiled.py:230-250): project owned samples
+ * (when project != 0), refresh halos and prolong child shells, parent first. */
+int bssn_fmr_prepare(double* const* states, const BssnFmrPatch* patches, const BssnParams* params,
+                     int32_t npatch, int32_t project, void* stream);
+/* fmr_stage (JAX_BSSN/fmr/tiled.py:253-263): prepare in place, then the RHS of
+ * every patch on its owned samples into rhs[p] (resident layout). */
+int bssn_fmr_stage_rhs(double* const* states, double* const* rhs, const BssnFmrPatch* patches,
+                       const BssnParams* params, int32_t npatch, void* workspace,
+                       size_t workspace_bytes, void* stream);
+/* fmr_rk4_step (JAX_BSSN/fmr/tiled.py:266-293), `steps` times, in place.
+ * params[p] are the per-patch evolution parameters (MAD weight, child faces periodic). */
+int bssn_fmr_rk4_step(double* const* states, const BssnFmrPatch* patches, const BssnParams* params,
+                      int32_t npatch, int32_t steps, void* workspace, size_t workspace_bytes, void* stream);
+/* fmr_constraint_norms statistics (JAX_BSSN/fmr/tiled.py:296-330): prepares the
+ * states (no projection) and accumulates, over owned samples not covered by a
+ * child, the sum of squares and max |.| of H, M, det-1, tr A, Gamma into
+ * stats[10] (device, pairs per constraint).  Workspace: see the implementation. */
+int bssn_fmr_constraint_stats(double* const* states, const BssnFmrPatch* patches, const BssnParams* params,
+                              int32_t npatch, double* stats, void* workspace, size_t workspace_bytes,
+                              void* stream);
+
 /* ---------------- instrumentation ---------------- */
 
 /* Kernel launches issued by this library since load (all threads). */

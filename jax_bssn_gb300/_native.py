@@ -56,6 +56,11 @@ class BssnMatter(ctypes.Structure):
                 ("spatial_stress", ctypes.c_void_p)]
 
 
+class BssnFmrPatch(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int32 * 3), ("parent", ctypes.c_int32),
+                ("coarse_lo", ctypes.c_int32 * 3), ("coarse_hi", ctypes.c_int32 * 3)]
+
+
 class BssnPatch(ctypes.Structure):
     _fields_ = [("n", ctypes.c_int32 * 3), ("ghost", ctypes.c_int32)]
 
@@ -89,6 +94,25 @@ SIGNATURES = {
                                       ctypes.c_int32, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     "bssn_patch_check_finite": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BssnPatch),
                                                ctypes.c_void_p, ctypes.c_void_p]),
+    "bssn_fields_to_components": (ctypes.c_int, [ctypes.POINTER(BssnFields), ctypes.c_void_p, Shape3,
+                                                 ctypes.c_void_p]),
+    "bssn_components_to_fields": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BssnFields), Shape3,
+                                                 ctypes.c_void_p]),
+    "bssn_fmr_workspace_bytes": (ctypes.c_size_t, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32]),
+    "bssn_fmr_refresh": (ctypes.c_int, [ctypes.c_void_p, Shape3, ctypes.c_void_p, ctypes.c_void_p]),
+    "bssn_fmr_prolong": (ctypes.c_int, [ctypes.c_void_p, Shape3, ctypes.c_void_p, Shape3, Shape3,
+                                        ctypes.c_void_p]),
+    "bssn_fmr_inject": (ctypes.c_int, [ctypes.c_void_p, Shape3, ctypes.c_void_p, Shape3, Shape3,
+                                       ctypes.c_void_p]),
+    "bssn_fmr_prepare": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
+                                        ctypes.c_int32, ctypes.c_void_p]),
+    "bssn_fmr_stage_rhs": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.c_int32, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    "bssn_fmr_rk4_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
+                                         ctypes.c_int32, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    "bssn_fmr_constraint_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                                 ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                                                 ctypes.c_size_t, ctypes.c_void_p]),
     "bssn_launch_count": (ctypes.c_longlong, []),
     "bssn_profile_enable": (None, [ctypes.c_int]),
     "bssn_profile_reset": (None, []),

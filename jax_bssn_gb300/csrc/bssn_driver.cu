@@ -543,6 +543,41 @@ int bssn_constraints(const BssnFields* in, const int32_t shape[3], const BssnPar
     return cuda_status(e, "bssn_constraints");
 }
 
+// ---------------- whole-array layout conversion ----------------
+
+static Geo plain_geo(const int32_t extent[3]) {
+    Geo G;
+    std::memset(&G, 0, sizeof(G));
+    for (int d = 0; d < 3; ++d) G.ax[d].P = extent[d];
+    G.st[2] = 1;
+    G.st[1] = extent[2];
+    G.st[0] = (long long)extent[1] * extent[2];
+    G.cs = (long long)extent[0] * extent[1] * extent[2];
+    return G;
+}
+
+int bssn_fields_to_components(const BssnFields* in, double* state, const int32_t extent[3], void* stream) {
+    if (!fields_ok(in) || !state || !extent) return fail(BSSN_ERR_INVALID, "null pointer");
+    for (int d = 0; d < 3; ++d)
+        if (extent[d] < 1) return fail(BSSN_ERR_INVALID, "array extents must be positive");
+    const Geo G = plain_geo(extent);
+    const Box region = full_box(G);
+    BSSN_LAUNCH(KC_IMPORT, k_import, nblocks(region.count * NCOMP), kThreads, (cudaStream_t)stream, leaves_in(in),
+                state, G, region, region.count);
+    return cuda_status(cudaGetLastError(), "bssn_fields_to_components");
+}
+
+int bssn_components_to_fields(const double* state, BssnFields* out, const int32_t extent[3], void* stream) {
+    if (!fields_ok(out) || !state || !extent) return fail(BSSN_ERR_INVALID, "null pointer");
+    for (int d = 0; d < 3; ++d)
+        if (extent[d] < 1) return fail(BSSN_ERR_INVALID, "array extents must be positive");
+    const Geo G = plain_geo(extent);
+    const Box region = full_box(G);
+    BSSN_LAUNCH(KC_EXPORT, k_export, nblocks(region.count * NCOMP), kThreads, (cudaStream_t)stream, state,
+                leaves_out(out), G, region, region.count);
+    return cuda_status(cudaGetLastError(), "bssn_components_to_fields");
+}
+
 // ---------------- resident patch layout ----------------
 
 static int patch_geo(const BssnPatch* patch, const BssnParams* params, Geo& G) {
