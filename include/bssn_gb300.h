@@ -204,6 +204,41 @@ int bssn_fmr_constraint_stats(double* const* states, const BssnFmrPatch* patches
                               int32_t npatch, double* stats, void* workspace, size_t workspace_bytes,
                               void* stream);
 
+/* ---------------- Cartoon reductions ---------------- */
+
+/* Compact Cartoon states in the 21-component layout (bssn_fields_to_components
+ * over the compact extent): axisymmetric (axisymmetric != 0) shape
+ * (Nrho+4, 1, Nz), spherical (Nr+4, 1, 1); x index 0..3 are parity ghosts.
+ * params must satisfy validate_axisymmetric_grid
+ * (JAX_BSSN/cartoon/axisymmetry/reconstruction.py:65-112) or
+ * validate_cartoon_grid (JAX_BSSN/cartoon/spherical_symmetry/reconstruction.py:61-111),
+ * with no guard description. */
+size_t bssn_cartoon_workspace_bytes(int32_t axisymmetric, const int32_t shape[3], const BssnParams* params);
+/* Axisymmetric: fill_axisymmetric_ghosts (axisymmetry/reconstruction.py:131-143).
+ * Spherical: enforce_spherical_symmetry (spherical_symmetry/reconstruction.py:174-189).
+ * In place. */
+int bssn_cartoon_fill_ghosts(int32_t axisymmetric, double* compact, const int32_t shape[3], void* stream);
+/* reconstruct_axisymmetric_support (axisymmetry/reconstruction.py:251-289) into a
+ * 21 x (Nrho+4) x 9 x Nz support, or reconstruct_cartoon_support
+ * (spherical_symmetry/reconstruction.py:336-385) into 21 x (Nr+4) x 9 x 9. */
+int bssn_cartoon_reconstruct(int32_t axisymmetric, const double* compact, double* support, const int32_t shape[3],
+                             const BssnParams* params, void* stream);
+/* compute_axisymmetric_rhs (axisymmetry/evolution.py:18-26) / compute_cartoon_rhs
+ * (spherical_symmetry/evolution.py:17-25): the compact RHS with parity ghosts. */
+int bssn_cartoon_rhs(int32_t axisymmetric, const double* compact, double* rhs, const int32_t shape[3],
+                     const BssnParams* params, void* workspace, size_t workspace_bytes, void* stream);
+/* axisymmetric_rk4_step (axisymmetry/evolution.py:40-65) / cartoon_rk4_step
+ * (spherical_symmetry/evolution.py:44-72), `steps` times, in place. */
+int bssn_cartoon_rk4_step(int32_t axisymmetric, double* compact, const int32_t shape[3], const BssnParams* params,
+                          int32_t steps, void* workspace, size_t workspace_bytes, void* stream);
+/* compute_axisymmetric_constraints (axisymmetry/diagnostics.py:22-37) /
+ * compute_cartoon_constraints (spherical_symmetry/diagnostics.py:21-37): nine
+ * compact blocks of the compact extent -- H, M_x, M_y, M_z, det-1, tr A,
+ * G_x, G_y, G_z -- with parity ghosts. */
+int bssn_cartoon_constraints(int32_t axisymmetric, const double* compact, const int32_t shape[3],
+                             const BssnParams* params, double* out, void* workspace, size_t workspace_bytes,
+                             void* stream);
+
 /* ---------------- instrumentation ---------------- */
 
 /* Kernel launches issued by this library since load (all threads). */

@@ -113,6 +113,18 @@ SIGNATURES = {
     "bssn_fmr_constraint_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                                  ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
                                                  ctypes.c_size_t, ctypes.c_void_p]),
+    "bssn_cartoon_workspace_bytes": (ctypes.c_size_t, [ctypes.c_int32, Shape3, ctypes.POINTER(BssnParams)]),
+    "bssn_cartoon_fill_ghosts": (ctypes.c_int, [ctypes.c_int32, ctypes.c_void_p, Shape3, ctypes.c_void_p]),
+    "bssn_cartoon_reconstruct": (ctypes.c_int, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, Shape3,
+                                                ctypes.POINTER(BssnParams), ctypes.c_void_p]),
+    "bssn_cartoon_rhs": (ctypes.c_int, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, Shape3,
+                                        ctypes.POINTER(BssnParams), ctypes.c_void_p, ctypes.c_size_t,
+                                        ctypes.c_void_p]),
+    "bssn_cartoon_rk4_step": (ctypes.c_int, [ctypes.c_int32, ctypes.c_void_p, Shape3, ctypes.POINTER(BssnParams),
+                                             ctypes.c_int32, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    "bssn_cartoon_constraints": (ctypes.c_int, [ctypes.c_int32, ctypes.c_void_p, Shape3,
+                                                ctypes.POINTER(BssnParams), ctypes.c_void_p, ctypes.c_void_p,
+                                                ctypes.c_size_t, ctypes.c_void_p]),
     "bssn_launch_count": (ctypes.c_longlong, []),
     "bssn_profile_enable": (None, [ctypes.c_int]),
     "bssn_profile_reset": (None, []),

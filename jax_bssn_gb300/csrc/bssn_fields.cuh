@@ -123,6 +123,9 @@ __device__ __forceinline__ double det_sym_rn(const double (&g)[6]) {
 // ---------------------------------------------------------------------------
 // Correctly rounded x^(-1/3) for x > 0 (the projection's det^(-1/3)).
 //
+// Near x = 1 -- where every projected metric's determinant sits, often on
+// values like 1 - 3*2^-53 whose cube root lies within 2^-106 of a rounding
+// midpoint -- the result is decided by exact midpoint tests.  Elsewhere
 // rcbrt() gives y within a couple of ulp; one Newton step for y^-3 = x carried
 // in double-double (Dekker/Knuth error-free transformations) gives ~100 bits,
 // and the final rounding of the double-double sum yields the correctly
@@ -143,8 +146,40 @@ __device__ __forceinline__ void two_sum(double a, double b, double& s, double& e
     e = (a - (s - bb)) + (b - bb);
 }
 
+// Is y* = pow(x, -1/3 + kPowThirdOffset) above the midpoint m = 1 + mu, for
+// x = 1 + xi with |xi| < 2^-28?  y* > m  <=>  x m^3 - 1 < 3*offset*ln x.  xi and
+// mu are exact multiples of 2^-54, and x m^3 - 1 = (xi + 3 mu) + 3 mu (mu + xi)
+// + mu^2 (mu + 3 xi) + xi mu^3, whose first term is either exactly zero or at
+// least 2^-54 while the rest stay below 2^-55: the comparison is exact.
+__device__ __forceinline__ bool cbrt_above_midpoint(double xi, double mu) {
+    const double a1 = xi + 3.0 * mu;  // exact: both multiples of 2^-54 with few bits
+    if (a1 != 0.0) return a1 < 0.0;
+    double ph, pl;
+    two_prod(3.0 * mu, mu + xi, ph, pl);  // mu + xi and 3 mu are exact
+    const double a3 = mu * mu * (mu + 3.0 * xi);
+    const double f = 3.0 * kPowThirdOffset * (xi - 0.5 * xi * xi);
+    return ((ph - f) + (pl + a3)) < 0.0;
+}
+
 __device__ __forceinline__ double inv_cbrt_cr(double x) {
     if (!(x > 0.0) || isinf(x)) return pow(x, -1.0 / 3.0);
+    const double xi = x - 1.0;
+    if (fabs(xi) < 0x1p-28) {
+        // Near one (every projected metric): pick the correctly rounded double
+        // by exact midpoint tests around a first-order candidate.  Below
+        // 2^-28 the candidate is within two ulp and the first-order term of
+        // the midpoint test is either zero or larger than all the others.
+        double y = 1.0 - xi * (1.0 / 3.0);
+#pragma unroll 1
+        for (int it = 0; it < 4; ++it) {
+            const double up = nextafter(y, 2.0);
+            if (cbrt_above_midpoint(xi, (y - 1.0) + 0.5 * (up - y))) { y = up; continue; }
+            const double dn = nextafter(y, 0.0);
+            if (!cbrt_above_midpoint(xi, (y - 1.0) - 0.5 * (y - dn))) { y = dn; continue; }
+            break;
+        }
+        return y;
+    }
     double y = rcbrt(x);
     // r = 1 - x*y^3 in double-double, then y' = y + y*r/3.
     double y2h, y2l;

@@ -275,3 +275,44 @@ def cfl_timestep(dx, cfl):
 
 
 __all__ = [name for name in dir() if not name.startswith("_") and name not in ("annotations", "math", "np")]
+
+
+def brill_lindquist_plane_state(masses=(0.5, 0.5), separation=2.0, num_radial_points=256, r_max=8.0):
+    """Two time-symmetric punctures on the z axis as a compact axisymmetric
+    Cartoon state (Nrho+4, 1, 2 Nrho).
+
+    Zero-momentum Bowen-York data: the Hamiltonian constraint is solved by the
+    Brill-Lindquist conformal factor psi = 1 + sum_i m_i / (2 |x - x_i|)
+    exactly (JAX_BSSN tests/test_bowen_york.py:113-127), A_ij = 0.  As in
+    bowen_york_plane_data (demos/axisymmetric_blackhole_collision/
+    axisymmetric_blackhole_collision.py:59-136): cell-centred rho = (i+1/2) dx,
+    z = -r_max + (k+1/2) dx, dx = r_max / Nrho, W = psi^-2, pre-collapsed lapse
+    alpha = W, flat conformal metric, K = Gamma = beta = 0, four parity ghosts.
+    """
+    n = int(num_radial_points)
+    dx = r_max / n
+    rho = (np.arange(n, dtype=np.float64) + 0.5) * dx
+    z = -r_max + (np.arange(2 * n, dtype=np.float64) + 0.5) * dx
+    R, Z = np.meshgrid(rho, z, indexing="ij")
+    psi = np.ones_like(R)
+    for m, zc in zip(masses, (-separation / 2.0, separation / 2.0)):
+        psi = psi + m / (2.0 * np.sqrt(R * R + (Z - zc) ** 2))
+    W = psi ** -2
+    full = np.concatenate((W[3::-1], W), axis=0)[:, None, :]       # even parity ghosts
+    shape = full.shape
+    g = np.broadcast_to(np.eye(3)[:, :, None, None, None], (3, 3) + shape).copy()
+    zeros = np.zeros(shape)
+    return BSSNVariables(g, full.copy(), np.zeros((3, 3) + shape), zeros.copy(), np.zeros((3,) + shape),
+                         full.copy(), np.zeros((3,) + shape)), dx
+
+
+def brill_lindquist_config(masses=(0.5, 0.5), separation=2.0, num_radial_points=256, r_max=8.0, cfl=0.2,
+                           eta=2.0, g=0.75, nu=0.02, kappa=0.002):
+    """The axisymmetric head-on configuration: compact state plus the demo's
+    parameters (1+log lapse, Gamma-driver, Sommerfeld x-right and z faces,
+    x_min = -3.5 dx, y_min = -4 dx, z_min = -r_max + dx/2, dt = cfl dx)."""
+    state, dx = brill_lindquist_plane_state(masses, separation, num_radial_points, r_max)
+    params = BSSNParameters(eta=eta, kappa=kappa, nu=nu, g=g, dx=dx, dt=cfl * dx, zero_shift=0, gauge=1,
+                            xl_bc=0, xr_bc=SOMMERFELD, yl_bc=0, yr_bc=0, zl_bc=SOMMERFELD, zr_bc=SOMMERFELD,
+                            x_min=-3.5 * dx, y_min=-4.0 * dx, z_min=-r_max + 0.5 * dx, mad_q=1.0)
+    return state, params

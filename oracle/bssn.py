@@ -451,13 +451,28 @@ def _two_sum(a, b):
 POW_THIRD_OFFSET = float(__import__("fractions").Fraction(-1.0 / 3.0) + __import__("fractions").Fraction(1, 3))
 
 
+def _above_midpoint(xi, mu):
+    """Is pow(1+xi, -1/3 + offset) above the midpoint 1 + mu?  Exact for
+    |xi| < 2^-28: y* > m <=> x m^3 - 1 < 3*offset*ln x, where
+    x m^3 - 1 = (xi + 3mu) + 3mu(mu + xi) + mu^2(mu + 3xi) + ...; the first
+    term is a multiple of 2^-54 that is either zero or larger than the rest."""
+    a1 = xi + 3.0 * mu
+    ph, pl = _two_prod(3.0 * mu, mu + xi)
+    a3 = mu * mu * (mu + 3.0 * xi)
+    f = 3.0 * POW_THIRD_OFFSET * (xi - 0.5 * xi * xi)
+    second = ((ph - f) + (pl + a3)) < 0.0
+    return np.where(a1 != 0.0, a1 < 0.0, second)
+
+
 def inv_cbrt(x):
     """Correctly rounded pow(x, -1.0/3.0), as libm evaluates ``det ** (-1/3)``.
 
-    One Newton step for y^-3 = x carried in double-double, plus the tiny
-    correction for the double exponent differing from -1/3, then one rounding.
-    NumPy's SIMD power can differ from libm's in the last bit, so it only
-    supplies the starting guess.
+    Near x = 1 (every projected metric's determinant) the result is chosen
+    by exact midpoint tests -- values such as 1 - 3*2^-53 have cube roots
+    within 2^-106 of a rounding midpoint.  Elsewhere one Newton step for
+    y^-3 = x carried in double-double, plus the tiny correction for the
+    double exponent differing from -1/3, is rounded once.  NumPy's SIMD power
+    can differ from libm's in the last bit, so it only supplies the guess.
     """
     x = np.asarray(x, dtype=np.float64)
     with np.errstate(all="ignore"):
@@ -471,5 +486,18 @@ def inv_cbrt(x):
         r = rh + (rl - xyl)
         c = y * (r * (1.0 / 3.0) + POW_THIRD_OFFSET * np.log(x))
         out = y + c
+        xi = x - 1.0
+        near = np.abs(xi) < 2.0 ** -28
+        if np.any(near):
+            xn = xi[near]
+            yn = 1.0 - xn * (1.0 / 3.0)
+            for _ in range(4):
+                up = np.nextafter(yn, 2.0)
+                go_up = _above_midpoint(xn, (yn - 1.0) + 0.5 * (up - yn))
+                dn = np.nextafter(yn, 0.0)
+                go_dn = ~go_up & ~_above_midpoint(xn, (yn - 1.0) - 0.5 * (yn - dn))
+                yn = np.where(go_up, up, np.where(go_dn, dn, yn))
+            out = np.array(out, copy=True)
+            out[near] = yn
     good = np.isfinite(x) & (x > 0)
     return np.where(good, out, np.power(x, -1.0 / 3.0))

@@ -243,9 +243,30 @@ def _pow_minus_third(x):
         bh, bl = split(b)
         return p, ((ah * bh - p) + ah * bl + al * bh) + al * bl
 
+    third = Fraction(-1.0 / 3.0)
+    off_f = Fraction(offset)
     for i, v in enumerate(flat.tolist()):
         if not (v > 0.0) or math.isinf(v):
             out[i] = math.pow(v, -1.0 / 3.0)
+            continue
+        if abs(v - 1.0) < 2.0 ** -20:
+            # Exact rational midpoint tests: y* > m <=> x m^3 < x^(3 offset),
+            # with x^(3 offset) = 1 + 3 offset ln x to far below any margin.
+            xf = Fraction(v)
+            xi = xf - 1
+            rhs = 1 + 3 * off_f * (xi - xi * xi / 2 + xi ** 3 / 3)
+            y = math.pow(v, -1.0 / 3.0)
+            for _ in range(8):
+                up = math.nextafter(y, 2.0)
+                if xf * ((Fraction(y) + Fraction(up)) / 2) ** 3 < rhs:
+                    y = up
+                    continue
+                dn = math.nextafter(y, 0.0)
+                if not xf * ((Fraction(y) + Fraction(dn)) / 2) ** 3 < rhs:
+                    y = dn
+                    continue
+                break
+            out[i] = y
             continue
         y = math.pow(v, -1.0 / 3.0)
         y2, y2e = prod(y, y)

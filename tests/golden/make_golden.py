@@ -7,7 +7,7 @@ branch, single-device collectives) -- placed first on ``sys.path``.  Under it
 the reference's own derivative, boundary, FMR and Cartoon test suites pass.
 
 Usage (needs the reference checkout; the GPU machine does not have it):
-    python tests/golden/make_golden.py [/path/to/reference] [--no-long]
+    python tests/golden/make_golden.py [/path/to/reference] [--no-long] [--only=rhs,...]
 
 Outputs ``tests/golden/*.npz``; each archive stores the inputs, the
 parameters (as a JSON string) and the reference outputs.
@@ -205,15 +205,122 @@ def make_fmr(out_dir: Path):
         np.savez_compressed(out_dir / f"fmr_{name}.npz", **data)
 
 
+def cartoon_cases():
+    """Generic smooth data on the compact Cartoon grids (every component set)."""
+    from JAX_BSSN.bssn.variables import BSSNParameters as P, BSSNVariables as V
+    rng = np.random.default_rng(44)
+    nrho, nz = 12, 20
+    dx = 0.1
+    x = (np.arange(nrho + 4) - 3.5) * dx
+    z = -0.5 * (nz - 1) * dx + dx * np.arange(nz)
+    X, Z = np.meshgrid(x, z, indexing="ij")
+
+    def f2d(amp):
+        c = rng.normal(size=5)
+        return amp * (c[0] * np.cos(1.3 * X + c[1]) * np.sin(0.9 * Z + c[2]) + c[3] * np.cos(2.1 * Z + c[4]))
+
+    def axi_field(rank, base):
+        shape = (3,) * rank
+        out = np.zeros(shape + (nrho + 4, 1, nz))
+        for idx in np.ndindex(*shape):
+            if rank == 2 and idx[0] > idx[1]:
+                continue
+            val = f2d(0.05) + (base if (rank == 0 or (rank == 2 and idx[0] == idx[1])) else 0.0)
+            out[idx + (slice(None), 0, slice(None))] = val
+            if rank == 2:
+                out[(idx[1], idx[0]) + (slice(None), 0, slice(None))] = val
+        return out
+
+    axi = V(axi_field(2, 1.0), axi_field(0, 1.0), axi_field(2, 0.0), axi_field(0, 0.0), axi_field(1, 0.0),
+            axi_field(0, 1.0), axi_field(1, 0.0))
+    axi_params = P(eta=2.0, kappa=0.002, nu=0.02, g=0.75, dx=dx, dt=0.2 * dx, gauge=1, zero_shift=0,
+                   xl_bc=0, xr_bc=1, yl_bc=0, yr_bc=0, zl_bc=1, zr_bc=1, x_min=-3.5 * dx, y_min=-4.0 * dx,
+                   z_min=float(z[0]))
+    nr = 16
+    r = (np.arange(nr + 4) - 3.5) * dx
+
+    def f1d(amp):
+        c = rng.normal(size=3)
+        return amp * (c[0] * np.cos(1.7 * r + c[1]) + c[2] * np.exp(-r * r))
+
+    def sph_field(rank, base):
+        shape = (3,) * rank
+        out = np.zeros(shape + (nr + 4, 1, 1))
+        if rank == 0:
+            out[:, 0, 0] = base + f1d(0.05)
+        elif rank == 1:
+            out[0, :, 0, 0] = f1d(0.05)
+        else:
+            out[0, 0, :, 0, 0] = base + f1d(0.05)
+            t = base + f1d(0.05)
+            out[1, 1, :, 0, 0] = t
+            out[2, 2, :, 0, 0] = t
+        return out
+
+    sph = V(sph_field(2, 1.0), sph_field(0, 1.0), sph_field(2, 0.0), sph_field(0, 0.0), sph_field(1, 0.0),
+            sph_field(0, 1.0), sph_field(1, 0.0))
+    sph_params = P(eta=2.0, kappa=0.0, nu=0.02, g=0.75, dx=dx, dt=0.2 * dx, gauge=1, zero_shift=0,
+                   xl_bc=0, xr_bc=1, x_min=-3.5 * dx, y_min=-4.0 * dx, z_min=-4.0 * dx)
+    return {"axisymmetric": (axi, axi_params), "spherical": (sph, sph_params)}
+
+
+def make_cartoon(out_dir: Path):
+    from JAX_BSSN.cartoon.axisymmetry import (axisymmetric_rk4_step, compute_axisymmetric_rhs,
+                                              compute_axisymmetric_constraints, reconstruct_axisymmetric_support,
+                                              compute_axisymmetric_constraint_norms, fill_axisymmetric_ghosts)
+    from JAX_BSSN.cartoon.spherical_symmetry.evolution import cartoon_rk4_step, compute_cartoon_rhs
+    from JAX_BSSN.cartoon.spherical_symmetry.diagnostics import (compute_cartoon_constraint_norms,
+                                                                 compute_cartoon_constraints,
+                                                                 compute_spherical_symmetry_norms)
+    from JAX_BSSN.cartoon.spherical_symmetry.reconstruction import reconstruct_cartoon_support
+    cases = cartoon_cases()
+    state, params = cases["axisymmetric"]
+    state = fill_axisymmetric_ghosts(state)
+    data = {"params": np.asarray(_params_json(params))}
+    data.update(_state_arrays("input", state))
+    data.update(_state_arrays("support", reconstruct_axisymmetric_support(state, params)))
+    data.update(_state_arrays("rhs", compute_axisymmetric_rhs(state, params)))
+    one = axisymmetric_rk4_step(state, params)
+    data.update(_state_arrays("rk4_1", one))
+    data.update(_state_arrays("rk4_2", axisymmetric_rk4_step(one, params)))
+    violations = compute_axisymmetric_constraints(one, params)
+    for field in violations._fields:
+        data[f"constraints.{field}"] = np.asarray(getattr(violations, field))
+    norms = compute_axisymmetric_constraint_norms(violations, params=params)
+    data["norms"] = np.asarray(json.dumps({k: float(v) for k, v in norms.items()}))
+    np.savez_compressed(out_dir / "cartoon_axisymmetric.npz", **data)
+    state, params = cases["spherical"]
+    data = {"params": np.asarray(_params_json(params))}
+    data.update(_state_arrays("input", state))
+    data.update(_state_arrays("support", reconstruct_cartoon_support(state, params)))
+    data.update(_state_arrays("rhs", compute_cartoon_rhs(state, params)))
+    one = cartoon_rk4_step(state, params)
+    data.update(_state_arrays("rk4_1", one))
+    data.update(_state_arrays("rk4_2", cartoon_rk4_step(one, params)))
+    violations = compute_cartoon_constraints(one, params)
+    for field in violations._fields:
+        data[f"constraints.{field}"] = np.asarray(getattr(violations, field))
+    norms = compute_cartoon_constraint_norms(violations)
+    data["norms"] = np.asarray(json.dumps({k: float(v) for k, v in norms.items()}))
+    sym = compute_spherical_symmetry_norms(compute_cartoon_rhs(state, params))
+    data["symmetry_norms"] = np.asarray(json.dumps({k: float(v) for k, v in sym.items()}))
+    np.savez_compressed(out_dir / "cartoon_spherical.npz", **data)
+
+
 def main(argv):
     args = [a for a in argv[1:] if not a.startswith("--")]
     reference = Path(args[0]) if args else Path("/root/reference")
     _setup(reference)
-    make_stencils(HERE / "stencils.npz")
-    make_rhs(HERE)
-    make_fmr(HERE)
-    if "--no-long" not in argv:
-        make_long_runs(HERE)
+    only = [part for a in argv if a.startswith("--only=") for part in a.split("=", 1)[1].split(",")]
+    parts = {"stencils": lambda: make_stencils(HERE / "stencils.npz"), "rhs": lambda: make_rhs(HERE),
+             "fmr": lambda: make_fmr(HERE), "cartoon": lambda: make_cartoon(HERE),
+             "long": lambda: make_long_runs(HERE)}
+    for name, build in parts.items():
+        if only and name not in only:
+            continue
+        if name == "long" and "--no-long" in argv:
+            continue
+        build()
     for path in sorted(HERE.glob("*.npz")):
         print(f"{path.name}: {path.stat().st_size / 1024:.0f} KiB")
 

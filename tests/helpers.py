@@ -45,3 +45,14 @@ def worst(errors: dict) -> float:
 
 
 RHS_CASES = ("gauge_wave", "generic_kappa", "sommerfeld", "mad_mixed", "mad_periodic_zero_shift")
+
+
+def assert_norms_match(got: dict, ref: dict, rel: float = 1e-9) -> None:
+    """Constraint norms against the reference's.  det(gt)-1 and tr(At) vanish
+    for projected data up to roundoff of O(1) products, so their norms are
+    compared absolutely at that O(1) scale; the others relatively."""
+    for key, value in ref.items():
+        if key.startswith(("det_gamma", "trace_A")):
+            assert abs(got[key] - value) < 1e-14, (key, got[key], value)
+        else:
+            assert abs(got[key] - value) <= rel * abs(value) + 1e-18, (key, got[key], value)

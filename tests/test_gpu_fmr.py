@@ -15,7 +15,7 @@ from oracle import fmr as ofmr
 from oracle.state import BSSNVariables as OracleVars
 
 from .fmr_helpers import G, load_case, owned_of, owned_states
-from .helpers import LEAVES, field_errors, worst
+from .helpers import assert_norms_match, LEAVES, field_errors, worst
 
 pytestmark = pytest.mark.gpu
 
@@ -104,8 +104,7 @@ def test_rk4_steps_and_norms_match_reference(gpu_case):
         assert worst(field_errors(owned_of(_untile(two[p]), n), expect[p])) < 2 * STEP_TOL, (name, p)
     norms = fmr_constraint_norms(two, params, h, layouts=layouts)
     ref = json.loads(str(data["norms"]))
-    for key, value in ref.items():
-        assert norms[key] == pytest.approx(value, rel=1e-9, abs=1e-18), key
+    assert_norms_match(norms, ref)
 
 
 def test_resident_evolution_matches_drop_in(gpu_case):

@@ -156,3 +156,21 @@ def test_invalid_input_raises_value_error(gb):
     state = random_smooth_state((6, 10, 10), seed=1)
     with pytest.raises(ValueError):
         te.compute_bssn_rhs(state, pkg.BSSNParameters(dx=0.1, xl_bc=1))
+
+
+def test_device_cube_root_is_correctly_rounded(gb):
+    """det^(-1/3) of the projection on the GPU, through a diagonal metric with
+    gt_xx = det: exact against 90-digit decimal arithmetic."""
+    pkg, te, _ = gb
+    from .test_oracle_golden import exact_pow_minus_third, near_one_lattice
+    x = near_one_lattice()
+    n = x.size
+    g = np.zeros((3, 3, n, 1, 1))
+    g[0, 0, :, 0, 0] = x
+    g[1, 1] = 1.0
+    g[2, 2] = 1.0
+    z = np.zeros((n, 1, 1))
+    state = pkg.BSSNVariables(g, z + 1.0, np.zeros((3, 3, n, 1, 1)), z, np.zeros((3, n, 1, 1)), z + 1.0,
+                              np.zeros((3, n, 1, 1)))
+    got = np.asarray(te.enforce_algebraic_constraints(state).conformal_metric)[1, 1, :, 0, 0]
+    np.testing.assert_array_equal(got, exact_pow_minus_third(x))

@@ -67,12 +67,24 @@ def test_constraints_match_reference(name):
         assert np.max(np.abs(value - ref)) / scale < 1e-13, field
 
 
-def test_inv_cbrt_is_correctly_rounded():
-    import decimal
-    decimal.getcontext().prec = 60
+def near_one_lattice():
+    """Determinants as the projection meets them: 1 + k ulp (both sides of one),
+    plus a scatter of small perturbations and a wide range."""
+    ks = np.arange(-400, 401)
     rng = np.random.default_rng(11)
-    x = np.concatenate([1 + 1e-3 * rng.normal(size=400), np.exp(rng.normal(size=400))])
-    y = ob.inv_cbrt(x)
+    return np.concatenate([1 + ks * 2.0 ** -52, 1 + ks * 2.0 ** -53, 1 + 1e-9 * rng.normal(size=300),
+                           1 + 2.0 ** -28 * (1 + rng.random(100)), 1 - 2.0 ** -28 * (1 + rng.random(100)),
+                           1 + 1e-7 * rng.normal(size=300), 1 + 5e-7 * rng.normal(size=300),
+                           1 + 1e-3 * rng.normal(size=300), np.exp(rng.normal(size=300))])
+
+
+def exact_pow_minus_third(x):
+    import decimal
+    decimal.getcontext().prec = 90
     exponent = decimal.Decimal(-1.0 / 3.0)
-    exact = np.array([float(decimal.Decimal(float(v)) ** exponent) for v in x])
-    np.testing.assert_array_equal(y, exact)
+    return np.array([float(decimal.Decimal(float(v)) ** exponent) for v in x])
+
+
+def test_inv_cbrt_is_correctly_rounded():
+    x = near_one_lattice()
+    np.testing.assert_array_equal(ob.inv_cbrt(x), exact_pow_minus_third(x))
