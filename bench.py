@@ -1,24 +1,32 @@
 """Benchmark: BSSN grid-point RK4 updates/s on GB300 (one JSON line on rank 0).
 
-Workload (N=1): the linearised Teukolsky quadrupole wave on a single 128^3
-vertex grid over [-4,4]^3 -- amplitude 1e-5, width 1, 1+log lapse,
+Default workload (N=1): the linearised Teukolsky quadrupole wave on a single
+128^3 vertex grid over [-4,4]^3 -- amplitude 1e-5, width 1, 1+log lapse,
 Gamma-driver shift (eta=2, g=0.75), KO nu=0.02, Sommerfeld faces, CFL 0.25,
 float64 state and arithmetic (the plain FP64 kernels).  A "step" is one RK4
-step of the whole grid.  Inputs are synthetic (generated on the host from the
-analytic solution).  The resident state is 21 x 136^3 doubles (~420 MB),
+step of the whole grid.  The resident state is 21 x 136^3 doubles (~420 MB),
 larger than the 129 MB L2, so no flush is needed between steps.
+
+Other workloads (--workload):
+  fmr           linear wave (A=1e-8, lambda=4) through a 3-level nested 2:1
+                hierarchy: root 96^3 periodic on [-8,8)^3, level 1 65^3, level 2
+                49^3, stage-synchronous RK4 at dt = 0.25 dx_finest; updates
+                count every patch's owned samples.
+  axisymmetric  two zero-momentum punctures (Brill-Lindquist, m=0.5 at z=+-1) on
+                the compact Cartoon plane 256 x 512, dx=1/32, kappa=0.002, CFL 0.2;
+                updates count the 256 x 512 evolved samples.
+All inputs are synthetic (analytic initial data generated on the host).
 
 Arms:
   --impl gb300 (default)  the CUDA kernels; `value` is device-resident
-                          throughput, `e2e` goes through the public rk4_step
-                          call with pinned host buffers copied in and out
-                          every step.
+                          throughput, `e2e` goes through the public step call
+                          with pinned host buffers copied in and out every step.
   --impl reference        the reference algorithm's CPU implementation on the
                           host cores: JAX is not installed, so this is the
                           NumPy restatement of the reference (oracle/), timed
                           on a bounded sample of the same workload.
 
-Multi-GPU (torchrun): independent replicas, one grid per rank (the path has
+Multi-GPU (torchrun): independent replicas, one problem per rank (the path has
 no exchange step on one box); value = all ranks' updates / max rank time.
 """
 
@@ -41,7 +49,15 @@ sys.path.insert(0, str(ROOT))
 METRIC = "BSSN grid-point RK4 updates/s"
 UNIT = "updates/s"
 BYTES_PER_UPDATE = 2856          # algorithmic HBM bytes per point per RK4 step (21 comps, 357 doubles)
-RHS_AT_BYTES_PER_POINT = 480     # k_rhs_at: 21 state + 33 derivative values read, 6 written (x 8 B)
+# Algorithmic HBM bytes per point of one launch, per kernel class (values read + written x 8 B).
+CLASS_BYTES = {
+    "rhs_at": 480,         # 21 state + 33 first derivatives read, 6 written
+    "rhs_kgt": 464,        # 21 state + 33 first derivatives read, 4 written
+    "rhs_gauge": 328,      # 21 state + 9 first derivatives read, 11 written
+    "first_derivs": 352,   # 11 fields read, 33 derivatives written
+    "rk4_stage": 714,      # mean of 63, 105, 105, 84 values over the four stages
+}
+RHS_CLASSES = ("rhs_at", "rhs_kgt", "rhs_gauge", "first_derivs")
 
 
 def parse():
@@ -50,7 +66,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
-    ap.add_argument("--n", type=int, default=128)
+    ap.add_argument("--workload", choices=("teukolsky", "fmr", "axisymmetric"), default="teukolsky")
+    ap.add_argument("--n", type=int, default=None, help="grid size (teukolsky n, fmr root n, axisymmetric Nrho)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     return ap.parse_args()
@@ -63,11 +80,171 @@ def dist_setup():
     return world, rank, local
 
 
-def config_dict(n):
-    return {"workload": f"linearised Teukolsky quadrupole wave, {n}^3 vertex grid over [-4,4]^3, FP64 plain kernels",
-            "grid": [n, n, n], "amplitude": 1e-5, "width": 1.0, "gauge": "1+log", "shift": "Gamma-driver eta=2 g=0.75",
-            "nu": 0.02, "kappa": 0.0, "boundaries": "Sommerfeld on all faces", "cfl": 0.25,
-            "l2": "resident state > 129 MB L2; no flush", "parallelism": "replicas"}
+# ----------------------------------------------------------------------------
+# workloads
+# ----------------------------------------------------------------------------
+
+class Teukolsky:
+    name = "teukolsky"
+
+    def __init__(self, n=None):
+        self.n = n or 128
+
+    def config(self):
+        n = self.n
+        return {"workload": f"linearised Teukolsky quadrupole wave, {n}^3 vertex grid over [-4,4]^3, "
+                            "FP64 plain kernels",
+                "grid": [n, n, n], "amplitude": 1e-5, "width": 1.0, "gauge": "1+log",
+                "shift": "Gamma-driver eta=2 g=0.75", "nu": 0.02, "kappa": 0.0,
+                "boundaries": "Sommerfeld on all faces", "cfl": 0.25,
+                "l2": "resident state > 129 MB L2; no flush", "parallelism": "replicas"}
+
+    def setup(self, device):
+        from jax_bssn_gb300.initial_data import teukolsky_config
+        self.state, self.params = teukolsky_config(n=self.n)
+        self.points = self.n ** 3
+
+    def resident(self):
+        from jax_bssn_gb300.evolution import PatchEvolution
+        return PatchEvolution(self.state, self.params)
+
+    def host_leaves(self):
+        return [f for f in self.state]
+
+    def public_step(self, leaves):
+        from jax_bssn_gb300.bssn.variables import BSSNVariables
+        from jax_bssn_gb300.evolution.time_evolve import rk4_step
+        return list(rk4_step(BSSNVariables(*leaves), self.params))
+
+    def cpu_sample(self, steps=1, n=36):
+        from jax_bssn_gb300.initial_data import teukolsky_config
+        from oracle import bssn as ob
+        from oracle.state import BSSNParameters as OP, BSSNVariables as OV
+        state, params = teukolsky_config(n=n)
+        s, p = OV(*state), OP(**params._asdict())
+
+        def run(k):
+            nonlocal s
+            for _ in range(k):
+                s = ob.rk4_step(s, p)
+        return run, n ** 3, f"RK4 step(s) of the same Teukolsky configuration on a {n}^3 grid"
+
+
+class NestedFMR:
+    name = "fmr"
+
+    def __init__(self, n=None):
+        self.root = n or 96
+
+    def config(self):
+        from jax_bssn_gb300.fmr import fine_active_shape
+        from jax_bssn_gb300.initial_data import fmr_linear_wave_hierarchy
+        shapes = [[self.root] * 3] + [list(fine_active_shape(s)) for s in fmr_linear_wave_hierarchy(self.root).patches]
+        return {"workload": f"linear wave through a 3-level nested FMR hierarchy, root {self.root}^3 on [-8,8)^3, "
+                            "stage-synchronous RK4, FP64 plain kernels",
+                "patch_shapes": shapes, "amplitude": 1e-8, "wavelength": 4.0, "gauge": "harmonic, zero shift",
+                "mad": True, "cfl": "0.25 of the finest spacing",
+                "deviation": "active extents are 2(hi-lo)+1, so 65^3 and 49^3 stand for 64^3 and 48^3",
+                "l2": "resident patches (~255 MB) > 129 MB L2; no flush", "parallelism": "replicas"}
+
+    def setup(self, device):
+        from jax_bssn_gb300.fmr import initialize_tiled_fmr
+        from jax_bssn_gb300.initial_data import fmr_linear_wave_hierarchy, fmr_linear_wave_root, linear_wave_callback
+        self.hierarchy = fmr_linear_wave_hierarchy(self.root)
+        root = fmr_linear_wave_root(self.root)
+        self.states, self.parameters, self.layouts = initialize_tiled_fmr(
+            linear_wave_callback(), root, (self.root,) * 3, self.hierarchy)
+        self.points = sum(math.prod(l.active_shape) for l in self.layouts)
+
+    def resident(self):
+        from jax_bssn_gb300.fmr import FMREvolution
+        return FMREvolution(self.states, self.parameters, self.hierarchy, self.layouts)
+
+    def host_leaves(self):
+        return [leaf.cpu().numpy() for s in self.states for leaf in s]
+
+    def public_step(self, leaves):
+        from jax_bssn_gb300.bssn.variables import BSSNVariables
+        from jax_bssn_gb300.fmr import fmr_rk4_step
+        states = tuple(BSSNVariables(*leaves[7 * p:7 * p + 7]) for p in range(len(self.layouts)))
+        out = fmr_rk4_step(states, self.parameters, self.hierarchy, layouts=self.layouts)
+        return [leaf for s in out for leaf in s]
+
+    def cpu_sample(self, steps=1, root=24):
+        import numpy as np
+        from jax_bssn_gb300.initial_data import fmr_linear_wave_hierarchy, fmr_linear_wave_root, linear_wave_state
+        from oracle import fmr as of
+        from oracle.state import BSSNParameters as OP, BSSNVariables as OV
+        h = fmr_linear_wave_hierarchy(root)
+        oh = of.FMRHierarchySpec(tuple(of.FMRPatchSpec(s.coarse_lo, s.coarse_hi, parent=s.parent) for s in h.patches),
+                                 use_mad=h.use_mad)
+        params, shapes = of.patch_parameters(OP(**fmr_linear_wave_root(root)._asdict()), (root,) * 3, oh)
+        states = []
+        for p, n in zip(params, shapes):
+            axes = [o + p.dx * np.arange(m, dtype=np.float64) for o, m in zip((p.x_min, p.y_min, p.z_min), n)]
+            X, Y, Z = np.meshgrid(*axes, indexing="ij")
+            owned = linear_wave_state(X, Y, Z, 1e-8, 4.0)
+            leaves = []
+            for leaf in owned:
+                full = np.zeros(leaf.shape[:-3] + tuple(m + 2 * of.GUARD for m in n))
+                full[(Ellipsis,) + tuple(slice(of.GUARD, of.GUARD + m) for m in n)] = leaf
+                leaves.append(full)
+            states.append(OV(*leaves))
+        states = of.prepare(tuple(states), params, shapes, oh, project=False)
+
+        def run(k):
+            nonlocal states
+            for _ in range(k):
+                states = of.rk4_step(states, params, shapes, oh)
+        pts = sum(math.prod(n) for n in shapes)
+        return run, pts, f"stage-synchronous RK4 step(s) of the same 3-level hierarchy scaled to a {root}^3 root"
+
+
+class Axisymmetric:
+    name = "axisymmetric"
+
+    def __init__(self, n=None):
+        self.nrho = n or 256
+
+    def config(self):
+        return {"workload": f"axisymmetric Cartoon head-on punctures (Brill-Lindquist, m=0.5 at z=+-1), compact "
+                            f"{self.nrho + 4}x1x{2 * self.nrho}, dx=1/32, FP64 plain kernels",
+                "evolved": [self.nrho, 2 * self.nrho], "gauge": "1+log, Gamma-driver eta=2 g=0.75",
+                "kappa": 0.002, "nu": 0.02, "cfl": 0.2, "boundaries": "Sommerfeld x-right and z faces",
+                "l2": "support state and work (~1.3 GB) > 129 MB L2; no flush", "parallelism": "replicas"}
+
+    def setup(self, device):
+        from jax_bssn_gb300.initial_data import brill_lindquist_config
+        self.state, self.params = brill_lindquist_config(num_radial_points=self.nrho, r_max=self.nrho / 32.0)
+        self.points = self.nrho * 2 * self.nrho
+
+    def resident(self):
+        from jax_bssn_gb300.cartoon.axisymmetry import AxisymmetricEvolution
+        return AxisymmetricEvolution(self.state, self.params)
+
+    def host_leaves(self):
+        return [f for f in self.state]
+
+    def public_step(self, leaves):
+        from jax_bssn_gb300.bssn.variables import BSSNVariables
+        from jax_bssn_gb300.cartoon.axisymmetry import axisymmetric_rk4_step
+        return list(axisymmetric_rk4_step(BSSNVariables(*leaves), self.params))
+
+    def cpu_sample(self, steps=1, nrho=32):
+        from jax_bssn_gb300.initial_data import brill_lindquist_config
+        from oracle import cartoon as oc
+        from oracle.state import BSSNParameters as OP, BSSNVariables as OV
+        state, params = brill_lindquist_config(num_radial_points=nrho, r_max=nrho / 8.0)
+        s, p = OV(*state), OP(**params._asdict())
+
+        def run(k):
+            nonlocal s
+            for _ in range(k):
+                s = oc.axi_rk4_step(s, p)
+        return run, nrho * 2 * nrho, f"RK4 step(s) of the same punctures on a {nrho}x{2 * nrho} compact plane (dx=1/8)"
+
+
+WORKLOADS = {w.name: w for w in (Teukolsky, NestedFMR, Axisymmetric)}
 
 
 # ----------------------------------------------------------------------------
@@ -134,10 +311,39 @@ class ClockSampler:
 # GB300 arm
 # ----------------------------------------------------------------------------
 
+def _max_over_ranks(ms, world, device):
+    if world == 1:
+        return ms
+    import torch
+    t = torch.tensor([ms], device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def roofline_of(prof, points, profiled_steps, hbm_peak, peak_src, value_per_gpu):
+    """Live roofline of the dominant kernel class from the per-launch CUDA-event
+    accounting: algorithmic bytes of all its launches in the profiled steps
+    divided by their summed device time."""
+    total = sum(v[0] for v in prof.values()) or 1.0
+    name, (ms, launches) = max(prof.items(), key=lambda kv: kv[1][0])
+    per_point = CLASS_BYTES.get(name)
+    achieved = None
+    if per_point is not None and ms > 0:
+        alg = per_point * points * 4 * profiled_steps
+        achieved = alg / (ms / 1e3) / 1e9
+    return {
+        "bound": "hbm", "kernel": f"k_{name}", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+        "frac": (achieved / hbm_peak) if achieved else None, "traffic": None, "peak_source": peak_src,
+        "kernel_share": ms / total, "kernel_ms_per_launch": ms / max(launches, 1),
+        "algorithmic_bytes_per_point": per_point,
+        "step_hbm_frac": value_per_gpu * BYTES_PER_UPDATE / (hbm_peak * 1e9),
+        "note": "plain FP64 form is FP64-pipe bound on GB300; HBM fraction reported as the metric asks",
+    }
+
+
 def run_gb300(args, world, rank, local):
     import numpy as np
     import torch
-
     torch.cuda.set_device(local)
     device = torch.device("cuda", local)
     if world > 1:
@@ -148,20 +354,17 @@ def run_gb300(args, world, rank, local):
     if not build.LIBRARY.exists():
         build.build()
     lib = _native.load()
-    from jax_bssn_gb300.evolution import PatchEvolution
-    from jax_bssn_gb300.evolution.time_evolve import rk4_step
-    from jax_bssn_gb300.initial_data import teukolsky_config
 
-    n = args.n
-    state, params = teukolsky_config(n=n)
-    points = n ** 3
+    wl = WORKLOADS[args.workload](args.n)
+    wl.setup(device)
+    points = wl.points
 
     def barrier():
         if world > 1:
             torch.distributed.barrier()
 
     # ---- device-resident throughput ----
-    evo = PatchEvolution(state, params)
+    evo = wl.resident()
     for _ in range(args.warmup):
         evo.step(1)
     torch.cuda.synchronize()
@@ -181,18 +384,14 @@ def run_gb300(args, world, rank, local):
     barrier()
     launches = lib.bssn_launch_count() - launches0
     clock_info = clocks.stop()
-    ms = t0.elapsed_time(t1)
-    if world > 1:
-        t = torch.tensor([ms], device=device)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = _max_over_ranks(t0.elapsed_time(t1), world, device)
     value = world * points * args.steps / (ms / 1e3)
-    nonfinite = evo.nonfinite_count()
 
     # ---- per-kernel device time (profiled pass, not part of `value`) ----
+    profiled_steps = 2
     lib.bssn_profile_reset()
     lib.bssn_profile_enable(1)
-    evo.step(2)
+    evo.step(profiled_steps)
     torch.cuda.synchronize()
     lib.bssn_profile_enable(0)
     prof = _native.profile_read()
@@ -204,32 +403,19 @@ def run_gb300(args, world, rank, local):
         peaks = json.loads(peaks_path.read_text())
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    roofline = roofline_of(prof, points, profiled_steps, hbm_peak, peak_src, value / world)
     total_prof = sum(v[0] for v in prof.values()) or 1.0
-    dominant = max(prof.items(), key=lambda kv: kv[1][0])
-    dom_name, (dom_ms, dom_launches) = dominant
-    per_launch_ms = dom_ms / max(dom_launches, 1)
-    alg_bytes = points * RHS_AT_BYTES_PER_POINT if dom_name == "rhs_at" else None
-    achieved = (alg_bytes / (per_launch_ms / 1e3) / 1e9) if alg_bytes else None
-    roofline = {
-        "bound": "hbm", "kernel": f"k_{dom_name}", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-        "frac": (achieved / hbm_peak) if achieved else None, "traffic": None,
-        "peak_source": peak_src, "kernel_share": dom_ms / total_prof, "kernel_ms_per_launch": per_launch_ms,
-        "algorithmic_bytes_per_point": RHS_AT_BYTES_PER_POINT,
-        "step_hbm_frac": value / world * BYTES_PER_UPDATE / (hbm_peak * 1e9),
-        "note": "plain FP64 form is FP64-pipe bound on GB300; HBM fraction reported as the metric asks",
-    }
     kernel_table = {k: {"ms": round(v[0], 3), "launches": v[1], "share": round(v[0] / total_prof, 4)}
                     for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}
 
     # ---- end to end through the public API, pinned host buffers ----
     e2e = None
     if not args.no_e2e:
-        host = [torch.from_numpy(np.ascontiguousarray(f)).pin_memory() for f in state]
+        host = [torch.from_numpy(np.ascontiguousarray(f)).pin_memory() for f in wl.host_leaves()]
         dev = [h.to(device, non_blocking=True) for h in host]
-        h2d = sum(h.numel() * 8 for h in host)
-        from jax_bssn_gb300.bssn.variables import BSSNVariables
+        h2d = sum(h.numel() * h.element_size() for h in host)
         torch.cuda.synchronize()
-        rk4_step(BSSNVariables(*dev), params)  # warm the workspace cache
+        wl.public_step(dev)  # warm the workspace cache
         torch.cuda.synchronize()
         barrier()
         e0 = torch.cuda.Event(enable_timing=True)
@@ -238,23 +424,19 @@ def run_gb300(args, world, rank, local):
         for _ in range(args.steps):
             for d, h in zip(dev, host):
                 d.copy_(h, non_blocking=True)
-            out = rk4_step(BSSNVariables(*dev), params)
+            out = wl.public_step(dev)
             for h, o in zip(host, out):
                 h.copy_(o, non_blocking=True)
         e1.record(stream)
         torch.cuda.synchronize()
         barrier()
-        ems = e0.elapsed_time(e1)
-        if world > 1:
-            t = torch.tensor([ems], device=device)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ems = float(t.item())
+        ems = _max_over_ranks(e0.elapsed_time(e1), world, device)
         e2e = {"value": world * points * args.steps / (ems / 1e3), "unit": UNIT,
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d, "ms_per_step": ems / args.steps}
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        cpu = cpu_baseline(sample_n=36)
+        cpu = cpu_baseline(wl)
 
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -263,10 +445,9 @@ def run_gb300(args, world, rank, local):
     return {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (analytic Teukolsky initial data on the host)",
-        "config": config_dict(n), "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (analytic initial data generated on the host)",
+        "config": wl.config(), "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
         "gpu_launches": launches, "clocks": clock_info, "kernels": kernel_table,
-        "nonfinite_after": nonfinite,
     }
 
 
@@ -274,48 +455,35 @@ def run_gb300(args, world, rank, local):
 # CPU baseline / reference arm
 # ----------------------------------------------------------------------------
 
-def cpu_baseline(sample_n=36, steps=1):
-    """The reference algorithm on the host (NumPy restatement, one thread),
-    one or more RK4 steps of the same Teukolsky configuration on a smaller grid."""
-    from jax_bssn_gb300.initial_data import teukolsky_config
-    from oracle import bssn as ob
-    from oracle.state import BSSNParameters as OP, BSSNVariables as OV
-    state, params = teukolsky_config(n=sample_n)
-    s = OV(*state)
-    p = OP(**params._asdict())
+def cpu_baseline(wl, steps=1):
+    """The reference algorithm on the host (NumPy restatement, one thread) on a
+    bounded sample of the same workload."""
+    run, pts, what = wl.cpu_sample()
     t = time.perf_counter()
-    for _ in range(steps):
-        s = ob.rk4_step(s, p)
+    run(steps)
     dt = time.perf_counter() - t
-    return {"value": sample_n ** 3 * steps / dt, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"{steps} RK4 step(s) of the same Teukolsky configuration on a {sample_n}^3 grid "
-                      f"(NumPy restatement of the reference, single thread; JAX not installed)",
+    return {"value": pts * steps / dt, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{steps} {what} (NumPy restatement of the reference, single thread; JAX not installed)",
             "seconds": dt}
 
 
 def run_reference(args, world, rank):
     if rank != 0:
         return None
-    from jax_bssn_gb300.initial_data import teukolsky_config
-    from oracle import bssn as ob
-    from oracle.state import BSSNParameters as OP, BSSNVariables as OV
-    n = 24
-    state, params = teukolsky_config(n=n)
-    s = OV(*state)
-    p = OP(**params._asdict())
-    for _ in range(args.warmup):
-        s = ob.rk4_step(s, p)
+    wl = WORKLOADS[args.workload](args.n)
+    small = {"teukolsky": {"n": 24}, "fmr": {"root": 16}, "axisymmetric": {"nrho": 16}}[wl.name]
+    run, pts, what = wl.cpu_sample(**small)
+    run(args.warmup)
     t = time.perf_counter()
-    for _ in range(args.steps):
-        s = ob.rk4_step(s, p)
+    run(args.steps)
     dt = time.perf_counter() - t
-    value = n ** 3 * args.steps / dt
-    sample = (f"each step one RK4 step of the Teukolsky configuration on a {n}^3 grid, NumPy restatement "
-              "of the reference (the reference's JAX CPU path cannot be installed here), single thread")
+    value = pts * args.steps / dt
+    sample = (f"each step one of the {what}, NumPy restatement of the reference (the reference's JAX CPU "
+              "path cannot be installed here), single thread")
     return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": config_dict(args.n), "impl": "reference",
+            "config": wl.config(), "impl": "reference",
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 

@@ -316,3 +316,39 @@ def brill_lindquist_config(masses=(0.5, 0.5), separation=2.0, num_radial_points=
                             xl_bc=0, xr_bc=SOMMERFELD, yl_bc=0, yr_bc=0, zl_bc=SOMMERFELD, zr_bc=SOMMERFELD,
                             x_min=-3.5 * dx, y_min=-4.0 * dx, z_min=-r_max + 0.5 * dx, mad_q=1.0)
     return state, params
+
+
+FMR_LINEAR_WAVE_PATCHES = (((32, 32, 32), (64, 64, 64), None), ((20, 20, 20), (44, 44, 44), 1))
+
+
+def fmr_linear_wave_hierarchy(root=96, patches=FMR_LINEAR_WAVE_PATCHES):
+    """Nested 2:1 hierarchy: level 1 over root samples [32, 64] (65^3 active),
+    level 2 over level-1 samples [20, 44] (49^3 active), MAD weights on."""
+    from .fmr import FMRHierarchySpec, FMRPatchSpec
+    scale = root / 96.0
+    specs = []
+    for lo, hi, parent in patches:
+        lo = tuple(int(round(v * scale)) for v in lo)
+        hi = tuple(int(round(v * scale)) for v in hi)
+        specs.append(FMRPatchSpec(lo, hi, parent=parent))
+    return FMRHierarchySpec(tuple(specs), use_mad=True)
+
+
+def fmr_linear_wave_root(root=96, half_width=8.0, wavelength=4.0, cfl=0.25, levels=3):
+    """Root parameters of the nested linear-wave run: periodic [-half_width,
+    half_width)^3 with dx = 2 half_width / root, harmonic lapse, zero shift,
+    no damping or dissipation (demos/gravitational_waves/linear_wave.py:116-122),
+    dt = cfl * dx_finest."""
+    dx = 2.0 * half_width / root
+    dt = cfl * dx / 2 ** (levels - 1)
+    return BSSNParameters(eta=0.0, kappa=0.0, nu=0.0, g=0.0, dx=dx, dt=dt, zero_shift=1, gauge=0,
+                          x_min=-half_width, y_min=-half_width, z_min=-half_width)
+
+
+def linear_wave_callback(amplitude=1.0e-8, wavelength=4.0):
+    """Initial-data callback for ``initialize_tiled_fmr``: the plus-polarised
+    linear wave on a patch's owned samples (linear_wave.py:36-56)."""
+    def initial(coordinates, local_params):
+        X, Y, Z = np.broadcast_arrays(*coordinates)
+        return linear_wave_state(X, Y, Z, amplitude, wavelength)
+    return initial
