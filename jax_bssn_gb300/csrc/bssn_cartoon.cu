@@ -110,96 +110,117 @@ struct AxiGeom {
     double dx, zmin;
 };
 
-// source sample s (reflected plane + three-sample 1/r buffer) of component c at z
-__device__ inline double axi_source(const double* __restrict__ f, const Compact& C, int c, int s, int z,
-                                    const AxiGeom& A, double par) {
-    if (s < kCG) return par * f[(long long)(2 * kCG - 1 - s) * C.nz + z];
-    if (s < C.nx) return f[(long long)s * C.nz + z];
-    const int b = s - C.nx;  // 0..2
-    const double dx = A.dx;
-    const double rho_edge = RN_MUL((double)(C.nx - kCG) - 0.5, dx);
-    const double zc = RN_ADD(A.zmin, RN_MUL(dx, (double)z));
-    const double rho_b = RN_ADD(rho_edge, RN_MUL(dx, (double)(b + 1)));
-    const double zz = RN_MUL(zc, zc);
-    const double r_edge = __dsqrt_rn(RN_ADD(RN_MUL(rho_edge, rho_edge), zz));
-    const double r_b = __dsqrt_rn(RN_ADD(RN_MUL(rho_b, rho_b), zz));
-    const double ratio = RN_DIV(r_edge, r_b);
-    const double asym = comp_asymptote(c);
-    return RN_ADD(asym, RN_MUL(RN_ADD(f[(long long)(C.nx - 1) * C.nz + z], -asym), ratio));
-}
-
 // Write the reconstructed support: point (x, j, z) -> dst at (ox+x, oy+j, oz+z)
-// of a block with strides (sx, sy, 1) and component stride dcs.
-__global__ void k_axi_reconstruct(const double* __restrict__ u, Compact C, AxiGeom A, double* __restrict__ dst,
-                                  long long dcs, long long sx, long long sy, int ox, int oy, int oz) {
-    const long long n = (long long)C.nx * kSup * C.nz;
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n) return;
-    const int x = (int)(t / ((long long)kSup * C.nz));
-    const long long r = t - (long long)x * kSup * C.nz;
-    const int j = (int)(r / C.nz);
-    const int z = (int)(r - (long long)j * C.nz);
-    const double X = RN_MUL((double)x - 3.5, A.dx);
-    const double Y = RN_MUL((double)j - 4.0, A.dx);
-    const double rho = __dsqrt_rn(RN_ADD(RN_MUL(X, X), RN_MUL(Y, Y)));
-    const double q = RN_ADD(RN_ADD(RN_DIV(rho, A.dx), 4.0), -0.5);
-    const int size = C.nx + 3;
-    int start;
+// of a block with strides (sx, sy, 1) and component stride dcs.  One block per
+// (x, j) column and a range of z: the node window, the six weights and the
+// rotation depend on (x, j) alone and are computed once into shared memory;
+// the threads then gather along z (coalesced) and rotate.
+constexpr int kAxiThreads = 128;
+
+__global__ void __launch_bounds__(kAxiThreads) k_axi_reconstruct(const double* __restrict__ u, Compact C, AxiGeom A,
+                                                                 double* __restrict__ dst, long long dcs, long long sx,
+                                                                 long long sy, int ox, int oy, int oz) {
+    __shared__ double s_w[6];
+    __shared__ double s_cs, s_sn;
+    __shared__ int s_start, s_valid;
+    const int col = blockIdx.x;            // x * 9 + j
+    const int x = col / kSup, j = col - (col / kSup) * kSup;
+    if (threadIdx.x == 0) {
+        const double X = RN_MUL((double)x - 3.5, A.dx);
+        const double Y = RN_MUL((double)j - 4.0, A.dx);
+        const double rho = __dsqrt_rn(RN_ADD(RN_MUL(X, X), RN_MUL(Y, Y)));
+        const double q = RN_ADD(RN_ADD(RN_DIV(rho, A.dx), 4.0), -0.5);
+        int start;
+        double w[6];
+        s_valid = lagrange_nodes(q, C.nx + 3, start, w) ? 1 : 0;
+        s_start = start;
+        for (int k = 0; k < 6; ++k) s_w[k] = w[k];
+        // rotation by phi about z: L = [[c,-s,0],[s,c,0],[0,0,1]]
+        s_cs = rho <= 0.0 ? 1.0 : RN_DIV(X, rho);
+        s_sn = rho <= 0.0 ? 0.0 : RN_DIV(Y, rho);
+    }
+    __syncthreads();
+    const int z = blockIdx.y * kAxiThreads + threadIdx.x;
+    if (z >= C.nz) return;
+    const int start = s_start;
+    const bool valid = s_valid != 0;
     double w[6];
-    const bool valid = lagrange_nodes(q, size, start, w);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) w[k] = s_w[k];
+    // 1/r continuation ratios of the three buffer samples at this z (reconstruction.py:146-167)
+    double ratio[3] = {0.0, 0.0, 0.0};
+    if (start + 5 >= C.nx) {
+        const double rho_edge = RN_MUL((double)(C.nx - kCG) - 0.5, A.dx);
+        const double zc = RN_ADD(A.zmin, RN_MUL(A.dx, (double)z));
+        const double zz = RN_MUL(zc, zc);
+        const double r_edge = __dsqrt_rn(RN_ADD(RN_MUL(rho_edge, rho_edge), zz));
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            const double rho_b = RN_ADD(rho_edge, RN_MUL(A.dx, (double)(b + 1)));
+            ratio[b] = RN_DIV(r_edge, __dsqrt_rn(RN_ADD(RN_MUL(rho_b, rho_b), zz)));
+        }
+    }
     const double par3[3] = {-1.0, -1.0, 1.0};
-    double val[NCOMP];
-#pragma unroll 1
-    for (int c = 0; c < NCOMP; ++c) {
+    const double nan = __longlong_as_double(0x7ff8000000000000LL);
+    // six-node sum of component c (reflected plane, then the buffer)
+    auto interp = [&](int c) -> double {
         const double* f = u + (long long)c * C.cs;
         const double par = comp_parity(c, par3);
-        double acc = RN_MUL(axi_source(f, C, c, start, z, A, par), w[0]);
+        const double asym = comp_asymptote(c);
+        double acc = 0.0;
 #pragma unroll
-        for (int k = 1; k < 6; ++k) acc = RN_ADD(acc, RN_MUL(axi_source(f, C, c, start + k, z, A, par), w[k]));
-        val[c] = valid ? acc : __longlong_as_double(0x7ff8000000000000LL);
+        for (int k = 0; k < 6; ++k) {
+            const int src = start + k;
+            double v;
+            if (src < kCG) v = par * f[(long long)(2 * kCG - 1 - src) * C.nz + z];
+            else if (src < C.nx) v = f[(long long)src * C.nz + z];
+            else v = RN_ADD(asym, RN_MUL(RN_ADD(f[(long long)(C.nx - 1) * C.nz + z], -asym), ratio[src - C.nx]));
+            acc = k == 0 ? RN_MUL(v, w[0]) : RN_ADD(acc, RN_MUL(v, w[k]));
+        }
+        return valid ? acc : nan;
+    };
+    // L = R_z(phi) = [[c,-s,0],[s,c,0],[0,0,1]].  Its four literal zeros
+    // (L_i2, L_2a for i, a < 2) only add (+-0) T terms to the reference's
+    // sums, so they are skipped: the remaining terms keep the reference's
+    // order (vector: j ascending; tensor: a-major, b-minor over (L_ia L_jb) T_ab),
+    // and the result differs at most in the sign of a zero (or, for a
+    // non-finite input, in not turning 0 * inf into NaN).
+    const double L[3][3] = {{s_cs, -s_sn, 0.0}, {s_sn, s_cs, 0.0}, {0.0, 0.0, 1.0}};
+    const long long d = (long long)(ox + x) * sx + (long long)(oy + j) * sy + (oz + z);
+    dst[(long long)CW * dcs + d] = interp(CW);
+    dst[(long long)CK * dcs + d] = interp(CK);
+    dst[(long long)CALPHA * dcs + d] = interp(CALPHA);
+#pragma unroll 1
+    for (int base = 0; base < 2; ++base) {
+        const int off = base == 0 ? GTX : BX;
+        const double v0 = interp(off), v1 = interp(off + 1), v2 = interp(off + 2);
+#pragma unroll
+        for (int i = 0; i < 2; ++i) dst[(long long)(off + i) * dcs + d] = RN_ADD(RN_MUL(L[i][0], v0), RN_MUL(L[i][1], v1));
+        dst[(long long)(off + 2) * dcs + d] = v2;
     }
-    // rotation by phi about z: L = [[c,-s,0],[s,c,0],[0,0,1]]
-    const double cs = rho <= 0.0 ? 1.0 : RN_DIV(X, rho);
-    const double sn = rho <= 0.0 ? 0.0 : RN_DIV(Y, rho);
-    const double L[3][3] = {{cs, -sn, 0.0}, {sn, cs, 0.0}, {0.0, 0.0, 1.0}};
-    double out[NCOMP];
-#pragma unroll
-    for (int c = 0; c < NCOMP; ++c) out[c] = val[c];
-#pragma unroll
+#pragma unroll 1
     for (int base = 0; base < 2; ++base) {
         const int off = base == 0 ? GXX : AXX;
-        double T[3][3];
+        double T6[6];
 #pragma unroll
-        for (int a = 0; a < 3; ++a)
-#pragma unroll
-            for (int b = 0; b < 3; ++b) T[a][b] = val[off + sym(a, b)];
+        for (int c = 0; c < 6; ++c) T6[c] = interp(off + c);
 #pragma unroll
         for (int i = 0; i < 3; ++i)
 #pragma unroll
             for (int jj = i; jj < 3; ++jj) {
-                double acc = RN_MUL(RN_MUL(L[i][0], L[jj][0]), T[0][0]);
+                double acc = 0.0;
+                bool first = true;
 #pragma unroll
-                for (int ab = 1; ab < 9; ++ab) {
-                    const int a = ab / 3, b = ab % 3;
-                    acc = RN_ADD(acc, RN_MUL(RN_MUL(L[i][a], L[jj][b]), T[a][b]));
+                for (int ab = 0; ab < 9; ++ab) {
+                    const int a2 = ab / 3, b2 = ab % 3;
+                    if ((i == 2) != (a2 == 2) || (jj == 2) != (b2 == 2)) continue;   // literal zero of L
+                    const double term = RN_MUL(RN_MUL(L[i][a2], L[jj][b2]), T6[sym(a2, b2)]);
+                    acc = first ? term : RN_ADD(acc, term);
+                    first = false;
                 }
-                out[off + sym(i, jj)] = acc;
+                dst[(long long)(off + sym(i, jj)) * dcs + d] = acc;
             }
     }
-#pragma unroll
-    for (int base = 0; base < 2; ++base) {
-        const int off = base == 0 ? GTX : BX;
-#pragma unroll
-        for (int i = 0; i < 3; ++i) {
-            double acc = RN_MUL(L[i][0], val[off]);
-            acc = RN_ADD(acc, RN_MUL(L[i][1], val[off + 1]));
-            acc = RN_ADD(acc, RN_MUL(L[i][2], val[off + 2]));
-            out[off + i] = acc;
-        }
-    }
-    const long long d = (long long)(ox + x) * sx + (long long)(oy + j) * sy + (oz + z);
-#pragma unroll
-    for (int c = 0; c < NCOMP; ++c) dst[(long long)c * dcs + d] = out[c];
 }
 
 // ---------------------------------------------------------------------------
@@ -450,8 +471,8 @@ cudaError_t reconstruct(const CartoonPlan& P, const BssnParams* p, const double*
     const long long sx = P.Gs.st[0], sy = P.Gs.st[1];
     if (P.axi) {
         const AxiGeom A{p->dx, p->xmin[2]};
-        const long long n = (long long)P.C.nx * kSup * P.C.nz;
-        BSSN_LAUNCH(KC_CARTOON, k_axi_reconstruct, blocks(n), kThr, s, u, P.C, A, us, P.scs, sx, sy, 4, 4, 4);
+        const dim3 grid((unsigned)(P.C.nx * kSup), (unsigned)((P.C.nz + kAxiThreads - 1) / kAxiThreads));
+        BSSN_LAUNCH(KC_CARTOON, k_axi_reconstruct, grid, kAxiThreads, s, u, P.C, A, us, P.scs, sx, sy, 4, 4, 4);
     } else {
         const long long n = (long long)P.C.nx * kSup * kSup;
         BSSN_LAUNCH(KC_CARTOON, k_sph_reconstruct, blocks(n), kThr, s, u, P.C.nx, p->dx, us, P.scs, sx, sy, 4, 4, 4);
@@ -549,9 +570,9 @@ int bssn_cartoon_reconstruct(int32_t axisymmetric, const double* compact, double
     cudaStream_t s = (cudaStream_t)stream;
     if (P.axi) {
         const AxiGeom A{params->dx, params->xmin[2]};
-        const long long n = (long long)P.C.nx * kSup * P.C.nz;
-        const long long dcs = n;
-        BSSN_LAUNCH(KC_CARTOON, k_axi_reconstruct, blocks(n), kThr, s, compact, P.C, A, support, dcs,
+        const long long dcs = (long long)P.C.nx * kSup * P.C.nz;
+        const dim3 grid((unsigned)(P.C.nx * kSup), (unsigned)((P.C.nz + kAxiThreads - 1) / kAxiThreads));
+        BSSN_LAUNCH(KC_CARTOON, k_axi_reconstruct, grid, kAxiThreads, s, compact, P.C, A, support, dcs,
                     (long long)kSup * P.C.nz, (long long)P.C.nz, 0, 0, 0);
     } else {
         const long long n = (long long)P.C.nx * kSup * kSup;

@@ -28,6 +28,7 @@
 namespace bssn {
 
 constexpr int kFmrGuard = 4;
+static_assert(kFmrGuard % 2 == 0, "prolongation pairs child z samples by the parity of (z - guard)");
 constexpr int kFmrThreads = 256;
 static inline unsigned fmr_blocks(long long n) { return (unsigned)((n + kFmrThreads - 1) / kFmrThreads); }
 
@@ -128,62 +129,119 @@ static void lagrange6(double frac, double (&w)[6]) {
     }
 }
 
-__global__ void k_fmr_prolong(const double* __restrict__ parent, PatchDims Dp, double* __restrict__ child,
-                              PatchDims Dc, int lo0, int lo1, int lo2, ProlongWeights W, long long shell_count) {
-    // enumerate padded child points with at least one coordinate in the guard
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long total = (long long)Dc.P[0] * Dc.P[1] * Dc.P[2];
-    if (t >= total) return;
-    const int x = (int)(t / ((long long)Dc.P[1] * Dc.P[2]));
-    const long long r = t - (long long)x * Dc.P[1] * Dc.P[2];
-    const int y = (int)(r / Dc.P[2]);
-    const int z = (int)(r - (long long)y * Dc.P[2]);
-    const int g = kFmrGuard;
-    const int ix[3] = {x, y, z};
-    bool shell = false;
+// Shell enumeration.  The child's guard shell is three dense slabs of
+// (x, y, z-pair) work items: X = guard x planes (all y, all pairs), Y =
+// interior x with guard y (all pairs), Z = interior x and y with the guard
+// pairs only.  Within a slab, x and y are enumerated evens first, then odds,
+// and pairs fastest, so a warp shares one (x parity, y parity) class and every
+// lane has work: on a part whose FP64 pipe issues two lanes per clock per SM,
+// idle or divergent lanes cost as much as busy ones.
+struct AxisSet {
+    int lo0, hi0, lo1, hi1;   // [lo0, hi0) U [lo1, hi1)
+};
+
+__device__ __forceinline__ int parity_count(int a, int b, int f) {  // #v in [a, b), v % 2 == f
+    if (b <= a) return 0;
+    return ((b + 1 - f) >> 1) - ((a + 1 - f) >> 1);
+}
+
+__device__ __forceinline__ int set_count(const AxisSet& S) { return (S.hi0 - S.lo0) + (S.hi1 - S.lo1); }
+
+// k-th element of S in the order: even elements ascending, then odd ones
+__device__ __forceinline__ int set_pick(const AxisSet& S, int k) {
 #pragma unroll
-    for (int a = 0; a < 3; ++a) shell = shell || ix[a] < g || ix[a] >= g + Dc.n[a];
-    if (!shell) return;
-    (void)shell_count;
+    for (int f = 0; f < 2; ++f) {
+        const int c0 = parity_count(S.lo0, S.hi0, f), c1 = parity_count(S.lo1, S.hi1, f);
+        if (k < c0) return S.lo0 + ((S.lo0 ^ f) & 1) + 2 * k;
+        k -= c0;
+        if (k < c1) return S.lo1 + ((S.lo1 ^ f) & 1) + 2 * k;
+        k -= c1;
+    }
+    return -1;
+}
+
+struct ShellSlabs {
+    AxisSet x[3], y[3];
+    int pair_lo[3][2], pair_n[3][2];   // pair ranges [lo, lo + n) (two per slab)
+    long long count[3];
+};
+
+// With g = 4 even, a child sample's parity along an axis decides its parent
+// target: even samples sit on a parent node (frac 0), odd ones half-way (frac
+// 1).  The six-node weights at frac 0 are exactly (0, 0, 1, 0, 0, 0), so the
+// reference's sum there equals the node value (up to the sign of a zero
+// result, and except that a non-finite neighbour would make the reference's
+// sum NaN); such axes are skipped.  An even/odd z pair shares the same six z
+// nodes (the even sample is node 2), so both come from one set of
+// y-interpolated lines.  Every remaining sum runs x, then y, then z over the
+// nodes in order with round-to-nearest operations, as the reference's
+// separable application does.
+__global__ void k_fmr_prolong(const double* __restrict__ parent, PatchDims Dp, double* __restrict__ child,
+                              PatchDims Dc, int lo0, int lo1, int lo2, ProlongWeights W, ShellSlabs S) {
+    const int slab = blockIdx.y;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= S.count[slab]) return;
+    const int np0 = S.pair_n[slab][0], npairs = np0 + S.pair_n[slab][1];
+    const int ny = set_count(S.y[slab]);
+    const long long row = t / npairs;
+    const int k = (int)(t - row * npairs);
+    const int x = set_pick(S.x[slab], (int)(row / ny));
+    const int y = set_pick(S.y[slab], (int)(row - (row / ny) * ny));
+    const int pr = k < np0 ? S.pair_lo[slab][0] + k : S.pair_lo[slab][1] + (k - np0);
+    const int z0 = 2 * pr, z1 = z0 + 1;
+    const int g = kFmrGuard;
+    const bool xy_shell = x < g || x >= g + Dc.n[0] || y < g || y >= g + Dc.n[1];
+    const bool s0 = xy_shell || z0 < g || z0 >= g + Dc.n[2];
+    const bool s1 = z1 < Dc.P[2] && (xy_shell || z1 < g || z1 >= g + Dc.n[2]);
+    if (!s0 && !s1) return;
     const int lo[3] = {lo0, lo1, lo2};
-    int node0[3];
-    int frac[3];
+    const int ix[3] = {x, y, z0};
+    int node0[3], frac[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         // parent padded target = lo + (ix - g)/2 + g; floor and parity
         const int twice = 2 * (lo[a] + g) + (ix[a] - g);   // 2 * target
         const int fl = twice >= 0 ? twice / 2 : -((-twice + 1) / 2);
-        frac[a] = twice - 2 * fl;                          // 0 or 1
+        frac[a] = twice - 2 * fl;                          // 0 or 1 (0 for z0)
         node0[a] = fl - 2;
     }
-    const double* wx = W.w[frac[0]];
-    const double* wy = W.w[frac[1]];
-    const double* wz = W.w[frac[2]];
-    const long long dst = Dc.at(x, y, z);
+    double w[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) w[k] = W.w[1][k];
+    const long long sx = (long long)Dp.P[1] * Dp.P[2];
+    const bool fx = frac[0] != 0, fy = frac[1] != 0;
 #pragma unroll 1
     for (int c = 0; c < NCOMP; ++c) {
         const double* f = parent + (long long)c * Dp.cs;
-        double sy[6];
+        // x-interpolated value at parent (py, pz)
+        auto xval = [&](int py, int pz) -> double {
+            const double* row = f + Dp.at(node0[0], py, pz);
+            if (!fx) return row[2 * sx];
+            double v = __dmul_rn(row[0], w[0]);
+#pragma unroll
+            for (int k = 1; k < 6; ++k) v = __dadd_rn(v, __dmul_rn(row[k * sx], w[k]));
+            return v;
+        };
+        // x- then y-interpolated value at parent z index pz
+        auto yval = [&](int pz) -> double {
+            if (!fy) return xval(node0[1] + 2, pz);
+            double v = __dmul_rn(xval(node0[1], pz), w[0]);
 #pragma unroll 1
-        for (int jz = 0; jz < 6; ++jz) {
-            double sx[6];
+            for (int k = 1; k < 6; ++k) v = __dadd_rn(v, __dmul_rn(xval(node0[1] + k, pz), w[k]));
+            return v;
+        };
+        if (s1) {
+            double line[6];
 #pragma unroll
-            for (int jy = 0; jy < 6; ++jy) {
-                const double* line = f + Dp.at(node0[0], node0[1] + jy, node0[2] + jz);
-                double acc = __dmul_rn(line[0], wx[0]);
+            for (int k = 0; k < 6; ++k) line[k] = yval(node0[2] + k);
+            if (s0) child[(long long)c * Dc.cs + Dc.at(x, y, z0)] = line[2];
+            double acc = __dmul_rn(line[0], w[0]);
 #pragma unroll
-                for (int k = 1; k < 6; ++k) acc = __dadd_rn(acc, __dmul_rn(line[(long long)k * Dp.P[1] * Dp.P[2]], wx[k]));
-                sx[jy] = acc;
-            }
-            double acc = __dmul_rn(sx[0], wy[0]);
-#pragma unroll
-            for (int k = 1; k < 6; ++k) acc = __dadd_rn(acc, __dmul_rn(sx[k], wy[k]));
-            sy[jz] = acc;
+            for (int k = 1; k < 6; ++k) acc = __dadd_rn(acc, __dmul_rn(line[k], w[k]));
+            child[(long long)c * Dc.cs + Dc.at(x, y, z1)] = acc;
+        } else {
+            child[(long long)c * Dc.cs + Dc.at(x, y, z0)] = yval(node0[2] + 2);
         }
-        double acc = __dmul_rn(sy[0], wz[0]);
-#pragma unroll
-        for (int k = 1; k < 6; ++k) acc = __dadd_rn(acc, __dmul_rn(sy[k], wz[k]));
-        child[(long long)c * Dc.cs + dst] = acc;
     }
 }
 
@@ -194,11 +252,41 @@ static ProlongWeights prolong_weights() {
     return W;
 }
 
+static AxisSet guard_set(int n, int g) { return AxisSet{0, g, g + n, n + 2 * g}; }
+static AxisSet interior_set(int n, int g) { return AxisSet{g, g + n, 0, 0}; }
+static AxisSet full_set(int n, int g) { return AxisSet{0, n + 2 * g, 0, 0}; }
+
+static ShellSlabs shell_slabs(const PatchDims& Dc) {
+    const int g = kFmrGuard;
+    const int pairs = (Dc.P[2] + 1) / 2;
+    // pairs holding a guard z sample: z < g (pairs [0, g/2)) and z >= g + n
+    const int hi_first = (g + Dc.n[2] - 1) / 2;   // first pair whose odd member reaches the upper guard
+    ShellSlabs S;
+    S.x[0] = guard_set(Dc.n[0], g);    S.y[0] = full_set(Dc.n[1], g);
+    S.x[1] = interior_set(Dc.n[0], g); S.y[1] = guard_set(Dc.n[1], g);
+    S.x[2] = interior_set(Dc.n[0], g); S.y[2] = interior_set(Dc.n[1], g);
+    for (int k = 0; k < 2; ++k) {
+        S.pair_lo[k][0] = 0; S.pair_n[k][0] = pairs;
+        S.pair_lo[k][1] = 0; S.pair_n[k][1] = 0;
+    }
+    S.pair_lo[2][0] = 0;        S.pair_n[2][0] = g / 2;
+    S.pair_lo[2][1] = hi_first; S.pair_n[2][1] = pairs - hi_first;
+    for (int k = 0; k < 3; ++k) {
+        const long long nx = (S.x[k].hi0 - S.x[k].lo0) + (S.x[k].hi1 - S.x[k].lo1);
+        const long long ny = (S.y[k].hi0 - S.y[k].lo0) + (S.y[k].hi1 - S.y[k].lo1);
+        S.count[k] = nx * ny * (S.pair_n[k][0] + S.pair_n[k][1]);
+    }
+    return S;
+}
+
 cudaError_t launch_fmr_prolong(const double* parent, const PatchDims& Dp, double* child, const PatchDims& Dc,
                                const int lo[3], cudaStream_t s) {
-    const long long total = (long long)Dc.P[0] * Dc.P[1] * Dc.P[2];
-    BSSN_LAUNCH(KC_TRANSFER, k_fmr_prolong, fmr_blocks(total), kFmrThreads, s, parent, Dp, child, Dc, lo[0], lo[1],
-                lo[2], prolong_weights(), 0LL);
+    const ShellSlabs S = shell_slabs(Dc);
+    long long most = 0;
+    for (int k = 0; k < 3; ++k) most = S.count[k] > most ? S.count[k] : most;
+    const dim3 grid(fmr_blocks(most), 3);
+    BSSN_LAUNCH(KC_TRANSFER, k_fmr_prolong, grid, kFmrThreads, s, parent, Dp, child, Dc, lo[0], lo[1], lo[2],
+                prolong_weights(), S);
     return cudaGetLastError();
 }
 

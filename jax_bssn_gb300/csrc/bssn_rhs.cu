@@ -664,57 +664,58 @@ k_constraints(const double* __restrict__ u, const double* __restrict__ d1, const
     trA[t] = contract_sym(gi, A);
 }
 
-cudaError_t launch_constraints(const double* u, const RhsWork& w, const Geo& G, const Box& box, double* H,
-                               double* M, double* detm1, double* trA, double* gam, cudaStream_t stream) {
-    Box all;
-    for (int d = 0; d < 3; ++d) { all.lo[d] = 0; all.n[d] = G.ax[d].P; }
-    all.count = (long long)all.n[0] * all.n[1] * all.n[2];
-    BSSN_LAUNCH(KC_MOM_DERIVED, k_mom_derived, (unsigned)((all.count + kThreads - 1) / kThreads), kThreads, stream, u, w.der, G, all);
-    Box ext;
-    int reach = 2;
-    for (int d = 0; d < 3; ++d) if (G.ax[d].mad) reach = 3;
-    ext.count = 1;
+// The box grown by `by` samples on every side, clipped to the padded block.
+static Box grown_box(const Box& box, const Geo& G, int by) {
+    Box b;
+    b.count = 1;
     for (int d = 0; d < 3; ++d) {
-        int lo = box.lo[d] - reach, hi = box.lo[d] + box.n[d] + reach;
+        int lo = box.lo[d] - by, hi = box.lo[d] + box.n[d] + by;
         if (lo < 0) lo = 0;
         if (hi > G.ax[d].P) hi = G.ax[d].P;
-        ext.lo[d] = lo;
-        ext.n[d] = hi - lo;
-        ext.count *= ext.n[d];
+        b.lo[d] = lo;
+        b.n[d] = hi - lo;
+        b.count *= b.n[d];
     }
-    BSSN_LAUNCH(KC_FIRST, k_first_derivs, (unsigned)((ext.count + kThreads - 1) / kThreads), kThreads, stream, u, w.der, w.d1, G,
-                                                                                              ext, 0);
-    BSSN_LAUNCH(KC_CONSTRAINTS, k_constraints, (unsigned)((box.count + kThreads - 1) / kThreads), kThreads, stream, u, w.d1, w.der, G, box,
-                                                                                            H, M, detm1, trA, gam);
+    return b;
+}
+
+// First derivatives are needed on the box grown by the reach of the
+// second-derivative composition (D1 of D1): 2 samples, 3 with MAD weights.
+static int composition_reach(const Geo& G) {
+    int reach = 2;
+    for (int d = 0; d < 3; ++d) if (G.ax[d].mad) reach = 3;
+    return reach;
+}
+
+static inline unsigned blocks_for(long long n) { return (unsigned)((n + kThreads - 1) / kThreads); }
+
+cudaError_t launch_constraints(const double* u, const RhsWork& w, const Geo& G, const Box& box, double* H,
+                               double* M, double* detm1, double* trA, double* gam, cudaStream_t stream) {
+    const Box ext = grown_box(box, G, composition_reach(G));
+    // derived fields are pointwise and read on the box only
+    BSSN_LAUNCH(KC_MOM_DERIVED, k_mom_derived, blocks_for(ext.count), kThreads, stream, u, w.der, G, ext);
+    BSSN_LAUNCH(KC_FIRST, k_first_derivs, blocks_for(ext.count), kThreads, stream, u, w.der, w.d1, G, ext, 0);
+    BSSN_LAUNCH(KC_CONSTRAINTS, k_constraints, blocks_for(box.count), kThreads, stream, u, w.d1, w.der, G, box,
+                H, M, detm1, trA, gam);
     return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------
 // host-side launch sequence of one RHS evaluation
 // ---------------------------------------------------------------------------
-static inline unsigned blocks_for(long long n) { return (unsigned)((n + kThreads - 1) / kThreads); }
 
 cudaError_t launch_rhs(const double* u, double* k, const RhsWork& w, const Geo& G, const Box& box,
                        cudaStream_t stream) {
     const int with_mom = G.kappa != 0.0;
     const int nfield = with_mom ? NMIX + NMIX_MOM : NMIX;
+    const int reach = composition_reach(G);
+    const Box ext = grown_box(box, G, reach);
     if (with_mom) {
-        Box all;
-        for (int d = 0; d < 3; ++d) { all.lo[d] = 0; all.n[d] = G.ax[d].P; }
-        all.count = (long long)all.n[0] * all.n[1] * all.n[2];
-        BSSN_LAUNCH(KC_MOM_DERIVED, k_mom_derived, blocks_for(all.count), kThreads, stream, u, w.der, G, all);
-    }
-    Box ext;
-    int reach = 2;
-    for (int d = 0; d < 3; ++d) if (G.ax[d].mad) reach = 3;
-    ext.count = 1;
-    for (int d = 0; d < 3; ++d) {
-        int lo = box.lo[d] - reach, hi = box.lo[d] + box.n[d] + reach;
-        if (lo < 0) lo = 0;
-        if (hi > G.ax[d].P) hi = G.ax[d].P;
-        ext.lo[d] = lo;
-        ext.n[d] = hi - lo;
-        ext.count *= ext.n[d];
+        // The derived fields are differentiated on ext, so they must be valid
+        // on ext grown by the first-derivative reach (3); being pointwise, they
+        // take the same values there whatever region is computed.
+        const Box region = grown_box(box, G, reach + 3);
+        BSSN_LAUNCH(KC_MOM_DERIVED, k_mom_derived, blocks_for(region.count), kThreads, stream, u, w.der, G, region);
     }
     BSSN_LAUNCH(KC_FIRST, k_first_derivs, blocks_for(ext.count), kThreads, stream, u, w.der, w.d1, G, ext, with_mom);
     if (with_mom)
@@ -722,7 +723,7 @@ cudaError_t launch_rhs(const double* u, double* k, const RhsWork& w, const Geo& 
     BSSN_LAUNCH(KC_GAUGE, k_rhs_gauge, blocks_for(box.count), kThreads, stream, u, w.d1, k, G, box, nfield);
     BSSN_LAUNCH(KC_KGT, k_rhs_kgt, blocks_for(box.count), kThreads, stream, u, w.d1, k, G, box, nfield);
     BSSN_LAUNCH(KC_AT, k_rhs_at, blocks_for(box.count), kThreads, stream, u, w.d1, with_mom ? w.damp : nullptr, k, G, box,
-                                                             nfield);
+                nfield);
     if (G.any_sommerfeld) BSSN_LAUNCH(KC_SOMMERFELD, k_sommerfeld, blocks_for(box.count), kThreads, stream, u, k, G, box);
     return cudaGetLastError();
 }

@@ -88,3 +88,15 @@ def exact_pow_minus_third(x):
 def test_inv_cbrt_is_correctly_rounded():
     x = near_one_lattice()
     np.testing.assert_array_equal(ob.inv_cbrt(x), exact_pow_minus_third(x))
+
+
+@pytest.mark.parametrize("name", ["run_gauge_wave32", "run_teukolsky24"])
+def test_long_run_first_step_matches_reference(name):
+    """The oracle's RK4 step reproduces the first step of the reference's long
+    runs (gauge wave 32^3, Teukolsky 24^3 with Sommerfeld faces) bit for bit;
+    the later steps of those runs are the GPU's long-horizon targets."""
+    data = load_golden(name)
+    state = golden_state(data, "input", BSSNVariables)
+    params = golden_params(data, BSSNParameters)
+    one = ob.rk4_step(state, params)
+    assert worst(field_errors(one, golden_state(data, "rk4_1", BSSNVariables))) == 0.0
