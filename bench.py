@@ -58,6 +58,23 @@ CLASS_BYTES = {
     "rk4_stage": 714,      # mean of 63, 105, 105, 84 values over the four stages
 }
 RHS_CLASSES = ("rhs_at", "rhs_kgt", "rhs_gauge", "first_derivs")
+# FP32 form: float state and derivatives (4 B), FP64 RHS written (8 B), W and alpha read from the FP64 state
+CLASS_BYTES_F32 = {
+    "rhs_at": (21 + 33) * 4 + 2 * 8 + 6 * 8,
+    "rhs_kgt": (21 + 33) * 4 + 2 * 8 + 4 * 8,
+    "rhs_gauge": (21 + 9) * 4 + 2 * 8 + 11 * 8,
+    "first_derivs": 11 * 4 + 33 * 4,
+}
+LEAVES = ("conformal_metric", "conformal_factor", "traceless_K", "trace_K", "conformal_connection", "lapse",
+          "shift")
+
+
+def background(leaf, t):
+    """Flat background of a leaf tensor: identity metric, W = alpha = 1, else 0."""
+    import torch
+    if leaf == "conformal_metric":
+        return torch.eye(3, dtype=t.dtype, device=t.device).reshape((3, 3) + (1,) * (t.ndim - 2))
+    return 1.0 if leaf in ("conformal_factor", "lapse") else 0.0
 
 
 def parse():
@@ -104,9 +121,16 @@ class Teukolsky:
         self.state, self.params = teukolsky_config(n=self.n)
         self.points = self.n ** 3
 
-    def resident(self):
+    def resident(self, precision):
         from jax_bssn_gb300.evolution import PatchEvolution
-        return PatchEvolution(self.state, self.params)
+        return PatchEvolution(self.state, self.params, precision=precision)
+
+    def states(self, evo):
+        return [evo.state()]
+
+    def norms(self, evo):
+        from jax_bssn_gb300.bssn.constraints import compute_all_constraints, compute_constraint_norms
+        return compute_constraint_norms(compute_all_constraints(evo.state(), self.params))
 
     def host_leaves(self):
         return [f for f in self.state]
@@ -156,9 +180,15 @@ class NestedFMR:
             linear_wave_callback(), root, (self.root,) * 3, self.hierarchy)
         self.points = sum(math.prod(l.active_shape) for l in self.layouts)
 
-    def resident(self):
+    def resident(self, precision):
         from jax_bssn_gb300.fmr import FMREvolution
-        return FMREvolution(self.states, self.parameters, self.hierarchy, self.layouts)
+        return FMREvolution(self.states, self.parameters, self.hierarchy, self.layouts, precision=precision)
+
+    def states(self, evo):
+        return list(evo.states())
+
+    def norms(self, evo):
+        return evo.constraint_norms()
 
     def host_leaves(self):
         return [leaf.cpu().numpy() for s in self.states for leaf in s]
@@ -218,9 +248,16 @@ class Axisymmetric:
         self.state, self.params = brill_lindquist_config(num_radial_points=self.nrho, r_max=self.nrho / 32.0)
         self.points = self.nrho * 2 * self.nrho
 
-    def resident(self):
+    def resident(self, precision):
         from jax_bssn_gb300.cartoon.axisymmetry import AxisymmetricEvolution
-        return AxisymmetricEvolution(self.state, self.params)
+        return AxisymmetricEvolution(self.state, self.params, precision=precision)
+
+    def states(self, evo):
+        return [evo.state()]
+
+    def norms(self, evo):
+        from jax_bssn_gb300.cartoon.axisymmetry import compute_axisymmetric_constraint_norms
+        return compute_axisymmetric_constraint_norms(evo.constraints(), params=self.params)
 
     def host_leaves(self):
         return [f for f in self.state]
@@ -320,13 +357,15 @@ def _max_over_ranks(ms, world, device):
     return float(t.item())
 
 
-def roofline_of(prof, points, profiled_steps, hbm_peak, peak_src, value_per_gpu):
+def roofline_of(prof, points, profiled_steps, hbm_peak, peak_src, value_per_gpu, precision="fp64"):
     """Live roofline of the dominant kernel class from the per-launch CUDA-event
     accounting: algorithmic bytes of all its launches in the profiled steps
     divided by their summed device time."""
     total = sum(v[0] for v in prof.values()) or 1.0
     name, (ms, launches) = max(prof.items(), key=lambda kv: kv[1][0])
     per_point = CLASS_BYTES.get(name)
+    if per_point is not None and precision == "fp32" and name in RHS_CLASSES:
+        per_point = CLASS_BYTES_F32.get(name)
     achieved = None
     if per_point is not None and ms > 0:
         alg = per_point * points * 4 * profiled_steps
@@ -337,7 +376,8 @@ def roofline_of(prof, points, profiled_steps, hbm_peak, peak_src, value_per_gpu)
         "kernel_share": ms / total, "kernel_ms_per_launch": ms / max(launches, 1),
         "algorithmic_bytes_per_point": per_point,
         "step_hbm_frac": value_per_gpu * BYTES_PER_UPDATE / (hbm_peak * 1e9),
-        "note": "plain FP64 form is FP64-pipe bound on GB300; HBM fraction reported as the metric asks",
+        "note": ("plain FP64 form is FP64-pipe bound on GB300; HBM fraction reported as the metric asks"
+                 if precision == "fp64" else "FP32-arithmetic form: float reads of the state and derivatives"),
     }
 
 
@@ -363,76 +403,107 @@ def run_gb300(args, world, rank, local):
         if world > 1:
             torch.distributed.barrier()
 
-    # ---- device-resident throughput ----
-    evo = wl.resident()
-    for _ in range(args.warmup):
-        evo.step(1)
-    torch.cuda.synchronize()
-    stream = torch.cuda.current_stream()
-    clocks = ClockSampler(local)
-    clocks.start()
-    barrier()
-    torch.cuda.synchronize()
-    launches0 = lib.bssn_launch_count()
-    t0 = torch.cuda.Event(enable_timing=True)
-    t1 = torch.cuda.Event(enable_timing=True)
-    t0.record(stream)
-    for _ in range(args.steps):
-        evo.step(1)
-    t1.record(stream)
-    torch.cuda.synchronize()
-    barrier()
-    launches = lib.bssn_launch_count() - launches0
-    clock_info = clocks.stop()
-    ms = _max_over_ranks(t0.elapsed_time(t1), world, device)
-    value = world * points * args.steps / (ms / 1e3)
-
-    # ---- per-kernel device time (profiled pass, not part of `value`) ----
-    profiled_steps = 2
-    lib.bssn_profile_reset()
-    lib.bssn_profile_enable(1)
-    evo.step(profiled_steps)
-    torch.cuda.synchronize()
-    lib.bssn_profile_enable(0)
-    prof = _native.profile_read()
-    lib.bssn_profile_reset()
-
     peaks = {}
     peaks_path = ROOT / "MEASURED_PEAKS.json"
     if peaks_path.exists():
         peaks = json.loads(peaks_path.read_text())
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    roofline = roofline_of(prof, points, profiled_steps, hbm_peak, peak_src, value / world)
-    total_prof = sum(v[0] for v in prof.values()) or 1.0
-    kernel_table = {k: {"ms": round(v[0], 3), "launches": v[1], "share": round(v[0] / total_prof, 4)}
-                    for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}
+    stream = torch.cuda.current_stream()
 
-    # ---- end to end through the public API, pinned host buffers ----
-    e2e = None
-    if not args.no_e2e:
-        host = [torch.from_numpy(np.ascontiguousarray(f)).pin_memory() for f in wl.host_leaves()]
-        dev = [h.to(device, non_blocking=True) for h in host]
-        h2d = sum(h.numel() * h.element_size() for h in host)
+    def measure(precision):
+        """Device-resident throughput of one arithmetic form, its per-kernel
+        profile and live roofline, and end-to-end public-API throughput."""
+        evo = wl.resident(precision)
+        for _ in range(args.warmup):
+            evo.step(1)
         torch.cuda.synchronize()
-        wl.public_step(dev)  # warm the workspace cache
-        torch.cuda.synchronize()
+        clocks = ClockSampler(local)
+        clocks.start()
         barrier()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
+        torch.cuda.synchronize()
+        launches0 = lib.bssn_launch_count()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
         for _ in range(args.steps):
-            for d, h in zip(dev, host):
-                d.copy_(h, non_blocking=True)
-            out = wl.public_step(dev)
-            for h, o in zip(host, out):
-                h.copy_(o, non_blocking=True)
-        e1.record(stream)
+            evo.step(1)
+        t1.record(stream)
         torch.cuda.synchronize()
         barrier()
-        ems = _max_over_ranks(e0.elapsed_time(e1), world, device)
-        e2e = {"value": world * points * args.steps / (ems / 1e3), "unit": UNIT,
-               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d, "ms_per_step": ems / args.steps}
+        launches = lib.bssn_launch_count() - launches0
+        clock_info = clocks.stop()
+        ms = _max_over_ranks(t0.elapsed_time(t1), world, device)
+        value = world * points * args.steps / (ms / 1e3)
+        # per-kernel device time (profiled pass, not part of `value`)
+        profiled_steps = 2
+        lib.bssn_profile_reset()
+        lib.bssn_profile_enable(1)
+        evo.step(profiled_steps)
+        torch.cuda.synchronize()
+        lib.bssn_profile_enable(0)
+        prof = _native.profile_read()
+        lib.bssn_profile_reset()
+        roofline = roofline_of(prof, points, profiled_steps, hbm_peak, peak_src, value / world, precision)
+        total_prof = sum(v[0] for v in prof.values()) or 1.0
+        kernels = {k: {"ms": round(v[0], 3), "launches": v[1], "share": round(v[0] / total_prof, 4)}
+                   for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}
+        e2e = None
+        if not args.no_e2e:
+            import jax_bssn_gb300 as pkg
+            host = [torch.from_numpy(np.ascontiguousarray(f)).pin_memory() for f in wl.host_leaves()]
+            dev = [h.to(device, non_blocking=True) for h in host]
+            h2d = sum(h.numel() * h.element_size() for h in host)
+            with pkg.arithmetic(precision):
+                torch.cuda.synchronize()
+                wl.public_step(dev)  # warm the workspace cache
+                torch.cuda.synchronize()
+                barrier()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                for _ in range(args.steps):
+                    for d, h in zip(dev, host):
+                        d.copy_(h, non_blocking=True)
+                    out = wl.public_step(dev)
+                    for h, o in zip(host, out):
+                        h.copy_(o, non_blocking=True)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                barrier()
+            ems = _max_over_ranks(e0.elapsed_time(e1), world, device)
+            e2e = {"value": world * points * args.steps / (ems / 1e3), "unit": UNIT,
+                   "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d, "ms_per_step": ems / args.steps}
+        return {"evo": evo, "value": value, "ms": ms, "launches": launches, "clocks": clock_info,
+                "roofline": roofline, "kernels": kernels, "e2e": e2e}
+
+    plain = measure("fp64")
+    chosen = measure("fp32")
+    # error of the FP32 form against the FP64 run after the same number of steps,
+    # relative to each leaf's deviation from the flat background
+    errors = {}
+    for s64, s32 in zip(wl.states(plain["evo"]), wl.states(chosen["evo"])):
+        for leaf, a, b in zip(LEAVES, s64, s32):
+            dev64 = a - background(leaf, a)
+            scale = float(torch.max(torch.abs(dev64)))
+            err = float(torch.max(torch.abs(b - a)))
+            errors[leaf] = max(errors.get(leaf, 0.0), err / scale if scale > 0 else err)
+    n64, n32 = wl.norms(plain["evo"]), wl.norms(chosen["evo"])
+    norm_keys = [k for k in ("hamiltonian_l2", "momentum_l2") if k in n64]
+    chosen_form = {
+        "arithmetic": "FP32 RHS stencils and algebra on perturbations about the flat background; "
+                      "FP64 state, RK4 combination, projection, W/alpha/1/W and constraints",
+        "dtype": "f32 (f64 state)", "value": chosen["value"], "unit": UNIT, "ms_per_step": chosen["ms"] / args.steps,
+        "speedup_vs_fp64": chosen["value"] / plain["value"], "roofline": chosen["roofline"],
+        "e2e": chosen["e2e"], "gpu_launches": chosen["launches"], "clocks": chosen["clocks"],
+        "kernels": chosen["kernels"],
+        "error_vs_fp64": {"metric": "max|fp32 - fp64| / max|fp64 - background| per leaf after "
+                                    f"{args.warmup + args.steps + 2} steps", "per_leaf": errors},
+        "constraint_norms": {k: {"fp64": n64[k], "fp32": n32[k], "rel_diff": abs(n32[k] - n64[k]) / abs(n64[k])
+                                 if n64[k] else None} for k in norm_keys},
+    }
+    value, ms, launches, clock_info = plain["value"], plain["ms"], plain["launches"], plain["clocks"]
+    roofline, kernel_table, e2e = plain["roofline"], plain["kernels"], plain["e2e"]
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -447,7 +518,7 @@ def run_gb300(args, world, rank, local):
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (analytic initial data generated on the host)",
         "config": wl.config(), "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-        "gpu_launches": launches, "clocks": clock_info, "kernels": kernel_table,
+        "gpu_launches": launches, "clocks": clock_info, "kernels": kernel_table, "chosen_form": chosen_form,
     }
 
 

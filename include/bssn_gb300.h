@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define BSSN_ABI_VERSION 1
+#define BSSN_ABI_VERSION 2
 
 /* status codes */
 #define BSSN_OK 0
@@ -59,7 +59,16 @@ typedef struct BssnParams {
     int32_t owned_shape[3];  /* owned samples per axis; -1: the whole array */
     int32_t owned_faces[6];  /* 1 when this array owns the global face */
     int32_t reduced_axes[3]; /* 1 reduced, 0 not, -1 infer (owned count == 1 when owned_shape given) */
+    int32_t precision;       /* BSSN_PRECISION_F64 (default) or BSSN_PRECISION_F32; no reference counterpart */
 } BssnParams;
+
+/* Arithmetic of the RHS kernels.  F64: plain float64 throughout, matching the
+ * reference to roundoff.  F32: the RHS stencils and algebra in float on
+ * perturbations about the flat background, W, alpha and 1/W from the float64
+ * state, the RHS written in float64; the state, the RK4 combination, the
+ * projection and the constraints stay float64. */
+#define BSSN_PRECISION_F64 0
+#define BSSN_PRECISION_F32 1
 
 /* The seven reference leaves as device pointers (float64). */
 typedef struct BssnFields {

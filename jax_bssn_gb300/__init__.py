@@ -7,4 +7,5 @@ in-tree CUDA library ``lib/libbssn_gb300.so``; there is no CPU fallback.
 
 __version__ = "0.1.0"
 
+from ._device import arithmetic, current_arithmetic, set_arithmetic  # noqa: E402,F401
 from .bssn.variables import BSSNParameters, BSSNVariables  # noqa: E402,F401

@@ -7,6 +7,8 @@ tensors) or host arrays (copied in and the results copied back as NumPy).
 
 from __future__ import annotations
 
+import contextlib
+import contextvars
 import ctypes
 import math
 import threading
@@ -27,9 +29,43 @@ def require_cuda() -> torch.device:
     return torch.device("cuda", torch.cuda.current_device())
 
 
-def to_params(params) -> _native.BssnParams:
-    """BSSNParameters -> the C struct (JAX_BSSN/bssn/variables.py:19-46)."""
+# Arithmetic of the RHS kernels for calls made in this context: "fp64" (plain
+# float64, the default) or "fp32" (float RHS arithmetic on a float64 state).
+PRECISIONS = {"fp64": _native.PRECISION_F64, "fp32": _native.PRECISION_F32}
+_ARITHMETIC = contextvars.ContextVar("jax_bssn_gb300_arithmetic", default="fp64")
+
+
+def _checked(name: str) -> str:
+    if name not in PRECISIONS:
+        raise ValueError(f"arithmetic must be one of {sorted(PRECISIONS)}, got {name!r}")
+    return name
+
+
+def current_arithmetic() -> str:
+    return _ARITHMETIC.get()
+
+
+def set_arithmetic(name: str) -> None:
+    """Select the RHS arithmetic for subsequent calls in this context."""
+    _ARITHMETIC.set(_checked(name))
+
+
+@contextlib.contextmanager
+def arithmetic(name: str):
+    """``with arithmetic("fp32"): ...`` -- the RHS arithmetic inside the block."""
+    token = _ARITHMETIC.set(_checked(name))
+    try:
+        yield
+    finally:
+        _ARITHMETIC.reset(token)
+
+
+def to_params(params, precision: str | None = None) -> _native.BssnParams:
+    """BSSNParameters -> the C struct (JAX_BSSN/bssn/variables.py:19-46).
+
+    ``precision`` ("fp64" / "fp32") overrides the context's arithmetic."""
     p = _native.BssnParams()
+    p.precision = PRECISIONS[_checked(precision) if precision is not None else _ARITHMETIC.get()]
     p.eta, p.kappa, p.nu, p.g = float(params.eta), float(params.kappa), float(params.nu), float(params.g)
     p.dx, p.dt = float(params.dx), float(params.dt)
     p.zero_shift, p.gauge = int(params.zero_shift), int(params.gauge)

@@ -25,6 +25,9 @@ BSSN_ERR_CUDA = 3
 BSSN_ERR_NONFINITE = 4
 BSSN_ERR_TIMEOUT = 5
 
+PRECISION_F64 = 0
+PRECISION_F32 = 1
+
 OP_RHS = 1
 OP_RK4 = 2
 OP_CONSTRAINTS = 3
@@ -42,6 +45,7 @@ class BssnParams(ctypes.Structure):
         ("owned_shape", ctypes.c_int32 * 3),
         ("owned_faces", ctypes.c_int32 * 6),
         ("reduced_axes", ctypes.c_int32 * 3),
+        ("precision", ctypes.c_int32),
     ]
 
 
@@ -133,7 +137,7 @@ SIGNATURES = {
 
 KERNEL_CLASSES = ("fill", "first_derivs", "rhs_gauge", "rhs_k_gamma", "rhs_at", "mom_derived", "mom_damping",
                   "sommerfeld", "rk4_stage", "project", "import", "export", "constraints", "fmr_transfer",
-                  "cartoon", "other")
+                  "cartoon", "convert", "other")
 
 
 def profile_read() -> dict:

@@ -113,11 +113,12 @@ class CartoonEvolution:
     conversion; ``state()`` converts back to the seven leaves.
     """
 
-    def __init__(self, vars: BSSNVariables, params: BSSNParameters, axisymmetric: bool):
+    def __init__(self, vars: BSSNVariables, params: BSSNParameters, axisymmetric: bool,
+                 precision: str | None = None):
         self.lib, state, _, self.shape = _prepare(vars)
         self.axi = bool(axisymmetric)
         self.params = params
-        self.cparams = _device.to_params(params)
+        self.cparams = _device.to_params(params, precision)
         self.device = state.lapse.device
         self.u = to_components(self.lib, state, self.shape)
         nbytes = self.lib.bssn_cartoon_workspace_bytes(int(self.axi), _device.shape3(self.shape), self.cparams)

@@ -32,8 +32,8 @@ def axisymmetric_rk4_steps(vars: BSSNVariables, params: BSSNParameters, steps: i
 class AxisymmetricEvolution(_calls.CartoonEvolution):
     """Resident compact axisymmetric state: ``step(n)`` without layout conversion."""
 
-    def __init__(self, vars: BSSNVariables, params: BSSNParameters):
-        super().__init__(vars, params, axisymmetric=True)
+    def __init__(self, vars: BSSNVariables, params: BSSNParameters, precision: str | None = None):
+        super().__init__(vars, params, axisymmetric=True, precision=precision)
 
 
 __all__ = ["AxisymmetricEvolution", "axisymmetric_rk4_step", "axisymmetric_rk4_steps", "compute_axisymmetric_rhs"]

@@ -31,8 +31,8 @@ def cartoon_rk4_steps(vars: BSSNVariables, params: BSSNParameters, steps: int) -
 class SphericalEvolution(_calls.CartoonEvolution):
     """Resident compact spherical state: ``step(n)`` without layout conversion."""
 
-    def __init__(self, vars: BSSNVariables, params: BSSNParameters):
-        super().__init__(vars, params, axisymmetric=False)
+    def __init__(self, vars: BSSNVariables, params: BSSNParameters, precision: str | None = None):
+        super().__init__(vars, params, axisymmetric=False, precision=precision)
 
 
 __all__ = ["SphericalEvolution", "cartoon_rk4_step", "cartoon_rk4_steps", "compute_cartoon_rhs"]

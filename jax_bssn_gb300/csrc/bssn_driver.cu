@@ -48,6 +48,8 @@ int validate_params(const BssnParams* p) {
         if (p->bc[f] != 0 && p->bc[f] != 1)
             return fail(BSSN_ERR_INVALID, "boundary codes must be 0 (periodic) or 1 (Sommerfeld)");
     if (p->gauge != 0 && p->gauge != 1) return fail(BSSN_ERR_INVALID, "gauge must be 0 or 1");
+    if (p->precision != BSSN_PRECISION_F64 && p->precision != BSSN_PRECISION_F32)
+        return fail(BSSN_ERR_INVALID, "precision must be BSSN_PRECISION_F64 or BSSN_PRECISION_F32");
     return BSSN_OK;
 }
 
@@ -83,6 +85,8 @@ int make_geo(const BssnParams* p, const int S[3], const int org[3], const int P[
         a.slo = a.lbc && counts_ok;
         a.shi = a.rbc && counts_ok;
         a.xmin = p->xmin[d];
+        a.fq = static_cast<float>(a.q);
+        a.fomq = static_cast<float>(a.omq);
         if ((a.lbc || a.rbc) && !a.reduced && count < 8)
             return fail(BSSN_ERR_INVALID, "Sommerfeld/KO closures require eight owned samples along the axis");
         if (a.lo < 4 || a.hi > P[d] - 4)
@@ -109,6 +113,17 @@ int make_geo(const BssnParams* p, const int S[3], const int org[3], const int P[
     G.zero_shift = p->zero_shift;
     G.any_sommerfeld = 0;
     for (int f = 0; f < 6; ++f) G.any_sommerfeld |= (p->bc[f] == kSommerfeld);
+    G.precision = p->precision;
+    G.gf.inv_dx = static_cast<float>(G.inv_dx);
+    G.gf.inv_12dx = static_cast<float>(G.inv_12dx);
+    G.gf.inv_60dx = static_cast<float>(G.inv_60dx);
+    G.gf.inv_12dx2 = static_cast<float>(G.inv_12dx2);
+    G.gf.inv_dx2 = static_cast<float>(G.inv_dx2);
+    G.gf.inv_dx6h5 = static_cast<float>(G.inv_dx6h5);
+    G.gf.nu64 = static_cast<float>(G.nu64);
+    G.gf.eta = static_cast<float>(G.eta);
+    G.gf.kappa = static_cast<float>(G.kappa);
+    G.gf.g = static_cast<float>(G.g);
     return BSSN_OK;
 }
 
@@ -144,6 +159,15 @@ RhsWork carve_rhs_work(double* base, long long cs, bool with_mom) {
     if (with_mom) {
         w.der = base + (long long)(3 * (NMIX + NMIX_MOM)) * cs;
         w.damp = w.der + 24LL * cs;
+    }
+    // FP32 views of the same memory: 21 + 3 * nfield (+ 24 + 6) floats per
+    // sample, within the 3 * nfield (+ 24 + 6) doubles of the FP64 layout.
+    const int nfield = with_mom ? NMIX + NMIX_MOM : NMIX;
+    w.uf = reinterpret_cast<float*>(base);
+    w.d1f = w.uf + (long long)NCOMP * cs;
+    if (with_mom) {
+        w.derf = w.d1f + (long long)(3 * nfield) * cs;
+        w.dampf = w.derf + 24LL * cs;
     }
     return w;
 }

@@ -60,22 +60,25 @@ __device__ __forceinline__ long long lin(const Geo& G, const int (&ix)[3]) {
 }
 
 // ---------------------------------------------------------------------------
-// inverse metric by explicit Cholesky (tensor_algebra.py:20-71), FMA allowed
+// inverse metric by explicit Cholesky (tensor_algebra.py:20-71), FMA allowed;
+// a template on the arithmetic type (sqrt and reciprocals in that type)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void inverse_metric(const double (&g)[6], double (&gi)[6]) {
-    const double l00 = sqrt(g[0]);
-    const double r00 = 1.0 / l00;
-    const double l10 = g[1] * r00;
-    const double l20 = g[2] * r00;
-    const double l11 = sqrt(g[3] - l10 * l10);
-    const double r11 = 1.0 / l11;
-    const double l21 = (g[4] - l20 * l10) * r11;
-    const double l22 = sqrt(g[5] - l20 * l20 - l21 * l21);
-    const double r22 = 1.0 / l22;
-    const double m00 = r00, m11 = r11, m22 = r22;
-    const double m10 = -l10 * r00 * r11;
-    const double m20 = (l10 * l21 - l20 * l11) * (r00 * r11 * r22);
-    const double m21 = -l21 * r11 * r22;
+template <typename R>
+__device__ __forceinline__ void inverse_metric(const R (&g)[6], R (&gi)[6]) {
+    const R one = R(1);
+    const R l00 = sqrt(g[0]);
+    const R r00 = one / l00;
+    const R l10 = g[1] * r00;
+    const R l20 = g[2] * r00;
+    const R l11 = sqrt(g[3] - l10 * l10);
+    const R r11 = one / l11;
+    const R l21 = (g[4] - l20 * l10) * r11;
+    const R l22 = sqrt(g[5] - l20 * l20 - l21 * l21);
+    const R r22 = one / l22;
+    const R m00 = r00, m11 = r11, m22 = r22;
+    const R m10 = -l10 * r00 * r11;
+    const R m20 = (l10 * l21 - l20 * l11) * (r00 * r11 * r22);
+    const R m21 = -l21 * r11 * r22;
     gi[0] = m00 * m00 + m10 * m10 + m20 * m20;
     gi[1] = m10 * m11 + m20 * m21;
     gi[2] = m20 * m22;
@@ -206,15 +209,15 @@ __device__ __forceinline__ double inv_cbrt_cr(double x) {
 //   c1[i][sym(j,k)] = Gamma_ijk = (d_k g_ij + d_j g_ik - d_i g_jk)/2
 //   c2[i][sym(j,k)] = Gamma^i_jk = g^im Gamma_mjk
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void christoffel(const double (&dg)[3][6], const double (&gi)[6],
-                                            double (&c1)[3][6], double (&c2)[3][6]) {
+template <typename R>
+__device__ __forceinline__ void christoffel(const R (&dg)[3][6], const R (&gi)[6], R (&c1)[3][6], R (&c2)[3][6]) {
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
         for (int j = 0; j < 3; ++j)
 #pragma unroll
             for (int k = j; k < 3; ++k)
-                c1[i][sym(j, k)] = 0.5 * (dg[k][sym(i, j)] + dg[j][sym(i, k)] - dg[i][sym(j, k)]);
+                c1[i][sym(j, k)] = R(0.5) * (dg[k][sym(i, j)] + dg[j][sym(i, k)] - dg[i][sym(j, k)]);
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll

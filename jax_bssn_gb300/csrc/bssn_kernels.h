@@ -14,6 +14,11 @@ struct RhsWork {
     double* d1 = nullptr;    // inner first derivatives: 3 * (NMIX [+ NMIX_MOM]) blocks
     double* der = nullptr;   // kappa != 0: gt^ij, B_i^j, B_i^j/W (24 blocks)
     double* damp = nullptr;  // kappa != 0: constraint-damping term for At (6 blocks)
+    // FP32-arithmetic form, carved from the same memory (a launch uses one form):
+    float* uf = nullptr;     // float perturbations of the state (21 blocks)
+    float* d1f = nullptr;    // first derivatives
+    float* derf = nullptr;   // derived fields (kappa != 0)
+    float* dampf = nullptr;  // damping term (kappa != 0)
 };
 
 size_t rhs_work_blocks(bool with_mom);

@@ -1,4 +1,4 @@
-// BSSN right-hand side on a padded patch (sm_103a, FP64).
+// BSSN right-hand side on a padded patch (sm_103a).
 //
 // One RHS evaluation is a short pipeline of point-parallel kernels over the
 // compute box of a padded patch:
@@ -21,6 +21,17 @@
 //                    (JAX_BSSN/evolution/boundaries.py:150-171)
 // Operators commute along different axes, so each mixed derivative is formed
 // once (outer axis = the larger index) and used for both orderings.
+//
+// Two arithmetic forms share this source (template parameter R):
+//   double  the plain FP64 form; kernels read the FP64 state directly.
+//   float   the FP32-arithmetic form: k_perturb first writes the state as
+//           float perturbations about the constant background (1 for the
+//           conformal-metric diagonal, W and alpha; 0 otherwise), so small
+//           deviations keep float's relative precision through every
+//           stencil; the algebra then runs in float.  W and alpha enter the
+//           pointwise terms as full values read from the FP64 state, and 1/W
+//           (large near punctures) is formed in FP64.  The RHS is written in
+//           FP64, and the RK4 combination stays FP64.
 #include "bssn_fields.cuh"
 #include "bssn_kernels.h"
 #include "bssn_profile.h"
@@ -29,14 +40,58 @@ namespace bssn {
 
 constexpr int kThreads = 128;
 
+template <typename R>
+constexpr bool kPerturbative = std::is_same<R, float>::value;
+
+__host__ __device__ constexpr bool has_background(int c) {
+    return c == GXX || c == GYY || c == GZZ || c == CW || c == CALPHA;
+}
+
 __device__ __forceinline__ bool in_range(const Axis& a, int i) { return i >= a.lo && i < a.hi; }
+
+// Full value of component c at sample p of the R-typed state.
+template <typename R>
+__device__ __forceinline__ R full(const R* __restrict__ u, int c, long long cs, long long p) {
+    R v = u[c * cs + p];
+    if constexpr (kPerturbative<R>) {
+        if (has_background(c)) v += R(1);
+    }
+    return v;
+}
+
+// W or alpha as a full value: from the FP64 state in the FP32 form (no
+// background cancellation near a puncture), from u itself in the FP64 form.
+template <typename R>
+__device__ __forceinline__ R full_exact(const R* __restrict__ u, const double* __restrict__ u64, int c,
+                                        long long cs, long long p) {
+    if constexpr (kPerturbative<R>) return static_cast<R>(u64[c * cs + p]);
+    else return u[c * cs + p];
+}
+
+// ---------------------------------------------------------------------------
+// FP32 form: float perturbations of the state on a region
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads)
+k_perturb(const double* __restrict__ u, float* __restrict__ uf, Geo G, Box region) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= region.count) return;
+    int ix[3];
+    region.coords(t, ix);
+    const long long p = lin(G, ix), cs = G.cs;
+#pragma unroll
+    for (int c = 0; c < NCOMP; ++c) {
+        const double v = u[c * cs + p];
+        uf[c * cs + p] = static_cast<float>(has_background(c) ? v - 1.0 : v);
+    }
+}
 
 // ---------------------------------------------------------------------------
 // inner first derivatives
 // ---------------------------------------------------------------------------
+template <typename R>
 __global__ void __launch_bounds__(kThreads)
-k_first_derivs(const double* __restrict__ u, const double* __restrict__ der,
-               double* __restrict__ d1, Geo G, Box ext, int with_mom) {
+k_first_derivs(const R* __restrict__ u, const R* __restrict__ der, R* __restrict__ d1, Geo G, Box ext,
+               int with_mom) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ext.count) return;
     int ix[3];
@@ -75,15 +130,15 @@ __device__ __forceinline__ bool point(const Box& B, PointCtx& c, const Geo& G) {
 }
 
 // d1 buffer accessor: first derivative along d of stored field f.
-__device__ __forceinline__ const double* d1ptr(const double* d1, const Geo& G, int nfield, int d, int f,
-                                               long long p) {
+template <typename R>
+__device__ __forceinline__ const R* d1ptr(const R* d1, const Geo& G, int nfield, int d, int f, long long p) {
     return d1 + ((long long)(d * nfield + f)) * G.cs + p;
 }
 
 // Mixed second derivative d_m d_n of stored field f (m != n): outer axis is
 // max(m,n), inner axis min(m,n).
-__device__ __forceinline__ double mixed(const double* d1, const Geo& G, int nfield, int f, int m, int n,
-                                        const PointCtx& c) {
+template <typename R>
+__device__ __forceinline__ R mixed(const R* d1, const Geo& G, int nfield, int f, int m, int n, const PointCtx& c) {
     const int inner = m < n ? m : n;
     const int outer = m < n ? n : m;
     return D1(d1ptr(d1, G, nfield, inner, f, c.p), G, outer, c.ix[outer]);
@@ -91,9 +146,10 @@ __device__ __forceinline__ double mixed(const double* d1, const Geo& G, int nfie
 
 // Symmetric Hessian of stored field f whose state component is comp:
 // h[sym(i,j)] = d_i d_j f, D2 on the diagonal.
-__device__ __forceinline__ void hessian(const double* __restrict__ u, const double* d1, const Geo& G,
-                                        int nfield, int comp, int f, const PointCtx& c, double (&h)[6]) {
-    const double* fp = u + comp * G.cs + c.p;
+template <typename R>
+__device__ __forceinline__ void hessian(const R* __restrict__ u, const R* d1, const Geo& G, int nfield, int comp,
+                                        int f, const PointCtx& c, R (&h)[6]) {
+    const R* fp = u + comp * G.cs + c.p;
     h[0] = D2(fp, G, 0, c.ix[0]);
     h[3] = D2(fp, G, 1, c.ix[1]);
     h[5] = D2(fp, G, 2, c.ix[2]);
@@ -102,43 +158,45 @@ __device__ __forceinline__ void hessian(const double* __restrict__ u, const doub
     h[4] = mixed(d1, G, nfield, f, 1, 2, c);
 }
 
-__device__ __forceinline__ double contract_sym(const double (&a)[6], const double (&b)[6]) {
-    return a[0] * b[0] + a[3] * b[3] + a[5] * b[5] + 2.0 * (a[1] * b[1] + a[2] * b[2] + a[4] * b[4]);
+template <typename R>
+__device__ __forceinline__ R contract_sym(const R (&a)[6], const R (&b)[6]) {
+    return a[0] * b[0] + a[3] * b[3] + a[5] * b[5] + R(2) * (a[1] * b[1] + a[2] * b[2] + a[4] * b[4]);
 }
 
 // W^2 D_i D_j alpha (JAX_BSSN/bssn/geometry.py:122-186)
-__device__ __forceinline__ void w2_lapse_hessian(const double* __restrict__ u, const double* d1,
-                                                 const Geo& G, int nfield, const PointCtx& c,
-                                                 const double (&g)[6], const double (&gi)[6],
-                                                 const double (&c2)[3][6], const double (&dW)[3],
-                                                 const double (&da)[3], double W, double (&out)[6]) {
-    double h[6];
+template <typename R>
+__device__ __forceinline__ void w2_lapse_hessian(const R* __restrict__ u, const R* d1, const Geo& G, int nfield,
+                                                 const PointCtx& c, const R (&g)[6], const R (&gi)[6],
+                                                 const R (&c2)[3][6], const R (&dW)[3], const R (&da)[3], R W,
+                                                 R (&out)[6]) {
+    R h[6];
     hessian(u, d1, G, nfield, CALPHA, MIX_ALPHA, c, h);
-    double gw = 0.0;
+    R gw = R(0);
 #pragma unroll
     for (int m = 0; m < 3; ++m)
 #pragma unroll
         for (int n = 0; n < 3; ++n) gw += gi[sym(m, n)] * dW[m] * da[n];
-    const double W2 = W * W;
+    const R W2 = W * W;
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
         for (int j = i; j < 3; ++j) {
             const int s = sym(i, j);
-            const double conf = h[s] - (c2[0][s] * da[0] + c2[1][s] * da[1] + c2[2][s] * da[2]);
-            const double grad = dW[i] * da[j] + dW[j] * da[i] - g[s] * gw;
+            const R conf = h[s] - (c2[0][s] * da[0] + c2[1][s] * da[1] + c2[2][s] * da[2]);
+            const R grad = dW[i] * da[j] + dW[j] * da[i] - g[s] * gw;
             out[s] = W2 * conf + W * grad;
         }
 }
 
-__device__ __forceinline__ void load_sym(const double* __restrict__ u, int base, const Geo& G, long long p,
-                                         double (&v)[6]) {
+template <typename R>
+__device__ __forceinline__ void load_sym(const R* __restrict__ u, int base, const Geo& G, long long p, R (&v)[6]) {
 #pragma unroll
-    for (int s = 0; s < 6; ++s) v[s] = u[(base + s) * G.cs + p];
+    for (int s = 0; s < 6; ++s) v[s] = full(u, base + s, G.cs, p);
 }
 
-__device__ __forceinline__ void load_metric_derivs(const double* d1, const Geo& G, int nfield, long long p,
-                                                   double (&dg)[3][6]) {
+template <typename R>
+__device__ __forceinline__ void load_metric_derivs(const R* d1, const Geo& G, int nfield, long long p,
+                                                   R (&dg)[3][6]) {
 #pragma unroll
     for (int k = 0; k < 3; ++k)
 #pragma unroll
@@ -146,23 +204,22 @@ __device__ __forceinline__ void load_metric_derivs(const double* d1, const Geo& 
 }
 
 // W^2 R_ij without inverse powers of W (JAX_BSSN/bssn/geometry.py:21-119).
-__device__ __forceinline__ void w2_ricci(const double* __restrict__ u, const double* d1, const Geo& G,
-                                         int nfield, const PointCtx& c, const double (&g)[6],
-                                         const double (&gi)[6], const double (&c1)[3][6],
-                                         const double (&c2)[3][6], const double (&dW)[3], double W,
-                                         double (&w2r)[6]) {
+template <typename R>
+__device__ __forceinline__ void w2_ricci(const R* __restrict__ u, const R* d1, const Geo& G, int nfield,
+                                         const PointCtx& c, const R (&g)[6], const R (&gi)[6], const R (&c1)[3][6],
+                                         const R (&c2)[3][6], const R (&dW)[3], R W, R (&w2r)[6]) {
     const long long cs = G.cs, p = c.p;
     // --- conformal Ricci tensor (geometry.py:44-81) ---
-    double ric[6];
+    R ric[6];
 #pragma unroll 1
     for (int s = 0; s < 6; ++s) {
-        double h[6];
+        R h[6];
         hessian(u, d1, G, nfield, GXX + s, MIX_G + s, c, h);
-        ric[s] = -0.5 * contract_sym(gi, h);
+        ric[s] = R(-0.5) * contract_sym(gi, h);
     }
     {
-        const double Gt[3] = {u[GTX * cs + p], u[GTY * cs + p], u[GTZ * cs + p]};
-        double dG[3][3];  // dG[d][i] = d_d Gt^i
+        const R Gt[3] = {u[GTX * cs + p], u[GTY * cs + p], u[GTZ * cs + p]};
+        R dG[3][3];  // dG[d][i] = d_d Gt^i
 #pragma unroll 1
         for (int d = 0; d < 3; ++d)
 #pragma unroll 1
@@ -171,19 +228,19 @@ __device__ __forceinline__ void w2_ricci(const double* __restrict__ u, const dou
         for (int i = 0; i < 3; ++i)
 #pragma unroll
             for (int j = i; j < 3; ++j) {
-                double t2 = 0.0, t3 = 0.0;
+                R t2 = R(0), t3 = R(0);
 #pragma unroll
                 for (int m = 0; m < 3; ++m) {
                     t2 += g[sym(m, i)] * dG[j][m] + g[sym(m, j)] * dG[i][m];
                     t3 += Gt[m] * (c1[i][sym(j, m)] + c1[j][sym(i, m)]);
                 }
-                ric[sym(i, j)] += 0.5 * t2 + 0.5 * t3;
+                ric[sym(i, j)] += R(0.5) * t2 + R(0.5) * t3;
             }
     }
     // term4 + term5: loop over k to bound live registers.
 #pragma unroll 1
     for (int kk = 0; kk < 3; ++kk) {
-        double X[3][3], Y[3][3];  // X[n][i] = g^mn Gamma^k_mi ; Y[m][j] = g^mn Gamma_kjn
+        R X[3][3], Y[3][3];  // X[n][i] = g^mn Gamma^k_mi ; Y[m][j] = g^mn Gamma_kjn
 #pragma unroll
         for (int a = 0; a < 3; ++a)
 #pragma unroll
@@ -197,7 +254,7 @@ __device__ __forceinline__ void w2_ricci(const double* __restrict__ u, const dou
         for (int i = 0; i < 3; ++i)
 #pragma unroll
             for (int j = i; j < 3; ++j) {
-                double t4 = 0.0, t5 = 0.0;
+                R t4 = R(0), t5 = R(0);
 #pragma unroll
                 for (int n = 0; n < 3; ++n) {
                     // term4: g^mn Gamma^k_mi Gamma_jkn + (i<->j); c1[j][sym(k,n)] = Gamma_jkn
@@ -210,74 +267,75 @@ __device__ __forceinline__ void w2_ricci(const double* __restrict__ u, const dou
     }
     // --- W terms: W (D_i D_j W + gt_ij lap W) - 2 gt_ij |dW|^2 (geometry.py:84-117) ---
     {
-        double hW[6];
+        R hW[6];
         hessian(u, d1, G, nfield, CW, MIX_W, c, hW);
 #pragma unroll
         for (int s = 0; s < 6; ++s) hW[s] -= c2[0][s] * dW[0] + c2[1][s] * dW[1] + c2[2][s] * dW[2];
-        const double lap = contract_sym(gi, hW);
-        double grad2 = 0.0;
+        const R lap = contract_sym(gi, hW);
+        R grad2 = R(0);
 #pragma unroll
         for (int m = 0; m < 3; ++m)
 #pragma unroll
             for (int n = 0; n < 3; ++n) grad2 += gi[sym(m, n)] * dW[m] * dW[n];
-        const double W2 = W * W;
+        const R W2 = W * W;
 #pragma unroll
-        for (int s = 0; s < 6; ++s) w2r[s] = W2 * ric[s] + (W * (hW[s] + g[s] * lap) - 2.0 * g[s] * grad2);
+        for (int s = 0; s < 6; ++s) w2r[s] = W2 * ric[s] + (W * (hW[s] + g[s] * lap) - R(2) * g[s] * grad2);
     }
 }
 
 // ---------------------------------------------------------------------------
 // dt gt_ij, dt W, dt alpha, dt beta^i
 // ---------------------------------------------------------------------------
+template <typename R>
 __global__ void __launch_bounds__(kThreads)
-k_rhs_gauge(const double* __restrict__ u, const double* __restrict__ d1, double* __restrict__ k,
-            Geo G, Box B, int nfield) {
+k_rhs_gauge(const R* __restrict__ u, const double* __restrict__ u64, const R* __restrict__ d1,
+            double* __restrict__ k, Geo G, Box B, int nfield) {
     PointCtx c;
     if (!point(B, c, G)) return;
     const long long cs = G.cs, p = c.p;
-    const double beta[3] = {u[BX * cs + p], u[BY * cs + p], u[BZ * cs + p]};
-    double db[3][3];  // db[i][j] = d_j beta^i
+    const R beta[3] = {u[BX * cs + p], u[BY * cs + p], u[BZ * cs + p]};
+    R db[3][3];  // db[i][j] = d_j beta^i
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
         for (int j = 0; j < 3; ++j) db[i][j] = d1ptr(d1, G, nfield, j, MIX_B + i, p)[0];
-    const double div = db[0][0] + db[1][1] + db[2][2];
-    const double alpha = u[CALPHA * cs + p];
-    const double K = u[CK * cs + p];
-    const double W = u[CW * cs + p];
-    double g[6];
+    const R div = db[0][0] + db[1][1] + db[2][2];
+    const R alpha = full_exact(u, u64, CALPHA, cs, p);
+    const R K = u[CK * cs + p];
+    const R W = full_exact(u, u64, CW, cs, p);
+    R g[6];
     load_sym(u, GXX, G, p, g);
 
 #pragma unroll 1
     for (int s = 0; s < 6; ++s) {
         const int i = s < 3 ? 0 : (s < 5 ? 1 : 2);
         const int j = s < 3 ? s : (s < 5 ? s - 2 : 2);
-        const double* f = u + (GXX + s) * cs + p;
-        double lie = 0.0;
+        const R* f = u + (GXX + s) * cs + p;
+        R lie = R(0);
 #pragma unroll
         for (int m = 0; m < 3; ++m) lie += g[sym(m, i)] * db[m][j] + g[sym(m, j)] * db[m][i];
-        const double v = ADV(f, G, c.ix, beta) + lie + (-2.0 / 3.0) * g[s] * div
-                         + (-2.0) * alpha * u[(AXX + s) * cs + p];
+        const R v = ADV(f, G, c.ix, beta) + lie + R(-2.0 / 3.0) * g[s] * div
+                    + R(-2.0) * alpha * u[(AXX + s) * cs + p];
         k[(GXX + s) * cs + p] = v + KO(f, G, c.ix);
     }
     {
-        const double* f = u + CW * cs + p;
-        const double v = ADV(f, G, c.ix, beta) + (1.0 / 3.0) * alpha * W * K - (1.0 / 3.0) * W * div;
+        const R* f = u + CW * cs + p;
+        const R v = ADV(f, G, c.ix, beta) + R(1.0 / 3.0) * alpha * W * K - R(1.0 / 3.0) * W * div;
         k[CW * cs + p] = v + KO(f, G, c.ix);
     }
     {
-        const double* f = u + CALPHA * cs + p;
-        const double slicing = (G.gauge == 0) ? -(alpha * alpha) * K : -2.0 * alpha * K;
+        const R* f = u + CALPHA * cs + p;
+        const R slicing = (G.gauge == 0) ? -(alpha * alpha) * K : R(-2.0) * alpha * K;
         k[CALPHA * cs + p] = slicing + ADV(f, G, c.ix, beta) + KO(f, G, c.ix);
     }
 #pragma unroll 1
     for (int i = 0; i < 3; ++i) {
-        const double* f = u + (BX + i) * cs + p;
-        double v;
+        const R* f = u + (BX + i) * cs + p;
+        R v;
         if (G.zero_shift) {
-            v = 0.0 * beta[i];
+            v = R(0) * beta[i];
         } else {
-            v = G.g * u[(GTX + i) * cs + p] + ADV(f, G, c.ix, beta) + (-G.eta) * beta[i];
+            v = BSSN_CO(R, G, g) * u[(GTX + i) * cs + p] + ADV(f, G, c.ix, beta) + (-BSSN_CO(R, G, eta)) * beta[i];
             v = v + KO(f, G, c.ix);
         }
         k[(BX + i) * cs + p] = v;
@@ -287,40 +345,41 @@ k_rhs_gauge(const double* __restrict__ u, const double* __restrict__ d1, double*
 // ---------------------------------------------------------------------------
 // dt K and dt Gt^i
 // ---------------------------------------------------------------------------
+template <typename R>
 __global__ void __launch_bounds__(kThreads)
-k_rhs_kgt(const double* __restrict__ u, const double* __restrict__ d1, double* __restrict__ k,
-          Geo G, Box B, int nfield) {
+k_rhs_kgt(const R* __restrict__ u, const double* __restrict__ u64, const R* __restrict__ d1,
+          double* __restrict__ k, Geo G, Box B, int nfield) {
     PointCtx c;
     if (!point(B, c, G)) return;
     const long long cs = G.cs, p = c.p;
-    double g[6], gi[6];
+    R g[6], gi[6];
     load_sym(u, GXX, G, p, g);
     inverse_metric(g, gi);
-    double c1[3][6], c2[3][6];
+    R c1[3][6], c2[3][6];
     {
-        double dg[3][6];
+        R dg[3][6];
         load_metric_derivs(d1, G, nfield, p, dg);
         christoffel(dg, gi, c1, c2);
     }
-    double dW[3], da[3], dK[3];
+    R dW[3], da[3], dK[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         dW[d] = d1ptr(d1, G, nfield, d, MIX_W, p)[0];
         da[d] = d1ptr(d1, G, nfield, d, MIX_ALPHA, p)[0];
         dK[d] = D1(u + CK * cs + p, G, d, c.ix[d]);
     }
-    const double W = u[CW * cs + p];
-    const double alpha = u[CALPHA * cs + p];
-    const double K = u[CK * cs + p];
-    const double beta[3] = {u[BX * cs + p], u[BY * cs + p], u[BZ * cs + p]};
-    double A[6];
+    const R W = full_exact(u, u64, CW, cs, p);
+    const R alpha = full_exact(u, u64, CALPHA, cs, p);
+    const R K = u[CK * cs + p];
+    const R beta[3] = {u[BX * cs + p], u[BY * cs + p], u[BZ * cs + p]};
+    R A[6];
     load_sym(u, AXX, G, p, A);
-    double Au[6];  // A^ij = g^ik g^jl A_kl
+    R Au[6];  // A^ij = g^ik g^jl A_kl
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
         for (int j = i; j < 3; ++j) {
-            double acc = 0.0;
+            R acc = R(0);
 #pragma unroll
             for (int kk = 0; kk < 3; ++kk)
 #pragma unroll
@@ -330,33 +389,40 @@ k_rhs_kgt(const double* __restrict__ u, const double* __restrict__ d1, double* _
 
     // dt K
     {
-        double h[6];
+        R h[6];
         w2_lapse_hessian(u, d1, G, nfield, c, g, gi, c2, dW, da, W, h);
-        const double first = -contract_sym(gi, h);
-        const double second = alpha * contract_sym(A, Au);
-        const double third = alpha * (K * K) / 3.0;
-        const double* f = u + CK * cs + p;
+        const R first = -contract_sym(gi, h);
+        const R second = alpha * contract_sym(A, Au);
+        const R third = alpha * (K * K) / R(3.0);
+        const R* f = u + CK * cs + p;
         k[CK * cs + p] = first + second + third + ADV(f, G, c.ix, beta) + KO(f, G, c.ix);
     }
 
     // dt Gt^i
-    double db[3][3];
+    R db[3][3];
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
         for (int j = 0; j < 3; ++j) db[i][j] = d1ptr(d1, G, nfield, j, MIX_B + i, p)[0];
-    const double div = db[0][0] + db[1][1] + db[2][2];
-    const double Wf = fmax(W, 1.0e-12);
-    double hb[3][6];  // hb[i][sym(m,n)] = d_m d_n beta^i
+    const R div = db[0][0] + db[1][1] + db[2][2];
+    // -6 alpha / max(W, 1e-12); the FP32 form takes 1/W in FP64 (puncture values)
+    R six_alpha_over_w;
+    if constexpr (kPerturbative<R>) {
+        six_alpha_over_w = R(-6.0) * alpha * static_cast<R>(1.0 / fmax(u64[CW * cs + p], 1.0e-12));
+    } else {
+        const R Wf = fmax(W, 1.0e-12);
+        six_alpha_over_w = -6.0 * alpha / Wf;
+    }
+    R hb[3][6];  // hb[i][sym(m,n)] = d_m d_n beta^i
 #pragma unroll 1
     for (int i = 0; i < 3; ++i) hessian(u, d1, G, nfield, BX + i, MIX_B + i, c, hb[i]);
-    double graddiv[3];
+    R graddiv[3];
 #pragma unroll
     for (int m = 0; m < 3; ++m) graddiv[m] = hb[0][sym(m, 0)] + hb[1][sym(m, 1)] + hb[2][sym(m, 2)];
-    const double Gt[3] = {u[GTX * cs + p], u[GTY * cs + p], u[GTZ * cs + p]};
+    const R Gt[3] = {u[GTX * cs + p], u[GTY * cs + p], u[GTZ * cs + p]};
 #pragma unroll 1
     for (int i = 0; i < 3; ++i) {
-        double t1 = 0.0, t3 = 0.0, t4 = 0.0, t7 = 0.0, t9 = 0.0;
+        R t1 = R(0), t3 = R(0), t4 = R(0), t7 = R(0), t9 = R(0);
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
             t1 += gi[sym(i, j)] * dK[j];
@@ -365,12 +431,12 @@ k_rhs_kgt(const double* __restrict__ u, const double* __restrict__ d1, double* _
             t7 += Gt[j] * db[i][j];
             t9 += gi[sym(i, j)] * graddiv[j];
         }
-        const double t2 = contract_sym(c2[i], Au);
-        const double t8 = contract_sym(gi, hb[i]);
-        const double* f = u + (GTX + i) * cs + p;
-        const double v = (-4.0 / 3.0) * alpha * t1 + 2.0 * alpha * t2 + (-6.0 * alpha / Wf) * t3
-                         - 2.0 * t4 + ADV(f, G, c.ix, beta) + (2.0 / 3.0) * Gt[i] * div - t7 + t8
-                         + (1.0 / 3.0) * t9;
+        const R t2 = contract_sym(c2[i], Au);
+        const R t8 = contract_sym(gi, hb[i]);
+        const R* f = u + (GTX + i) * cs + p;
+        const R v = R(-4.0 / 3.0) * alpha * t1 + R(2.0) * alpha * t2 + six_alpha_over_w * t3
+                    - R(2.0) * t4 + ADV(f, G, c.ix, beta) + R(2.0 / 3.0) * Gt[i] * div - t7 + t8
+                    + R(1.0 / 3.0) * t9;
         k[(GTX + i) * cs + p] = v + KO(f, G, c.ix);
     }
 }
@@ -378,124 +444,133 @@ k_rhs_kgt(const double* __restrict__ u, const double* __restrict__ d1, double* _
 // ---------------------------------------------------------------------------
 // dt At_ij
 // ---------------------------------------------------------------------------
+template <typename R>
 __global__ void __launch_bounds__(kThreads)
-k_rhs_at(const double* __restrict__ u, const double* __restrict__ d1, const double* __restrict__ damp,
-         double* __restrict__ k, Geo G, Box B, int nfield) {
+k_rhs_at(const R* __restrict__ u, const double* __restrict__ u64, const R* __restrict__ d1,
+         const R* __restrict__ damp, double* __restrict__ k, Geo G, Box B, int nfield) {
     PointCtx c;
     if (!point(B, c, G)) return;
     const long long cs = G.cs, p = c.p;
-    double g[6], gi[6];
+    R g[6], gi[6];
     load_sym(u, GXX, G, p, g);
     inverse_metric(g, gi);
-    double c1[3][6], c2[3][6];
+    R c1[3][6], c2[3][6];
     {
-        double dg[3][6];
+        R dg[3][6];
         load_metric_derivs(d1, G, nfield, p, dg);
         christoffel(dg, gi, c1, c2);
     }
-    double dW[3], da[3];
+    R dW[3], da[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         dW[d] = d1ptr(d1, G, nfield, d, MIX_W, p)[0];
         da[d] = d1ptr(d1, G, nfield, d, MIX_ALPHA, p)[0];
     }
-    const double W = u[CW * cs + p];
-    const double alpha = u[CALPHA * cs + p];
+    const R W = full_exact(u, u64, CW, cs, p);
+    const R alpha = full_exact(u, u64, CALPHA, cs, p);
 
-    double w2r[6];
+    R w2r[6];
     w2_ricci(u, d1, G, nfield, c, g, gi, c1, c2, dW, W, w2r);
     // --- [alpha W^2 R_ij - W^2 D_i D_j alpha]^TF ---
-    double T[6];
+    R T[6];
     {
-        double h[6];
+        R h[6];
         w2_lapse_hessian(u, d1, G, nfield, c, g, gi, c2, dW, da, W, h);
 #pragma unroll
         for (int s = 0; s < 6; ++s) T[s] = alpha * w2r[s] - h[s];
-        const double tr = contract_sym(gi, T);
+        const R tr = contract_sym(gi, T);
 #pragma unroll
-        for (int s = 0; s < 6; ++s) T[s] = T[s] - (1.0 / 3.0) * g[s] * tr;
+        for (int s = 0; s < 6; ++s) T[s] = T[s] - R(1.0 / 3.0) * g[s] * tr;
     }
     // --- remaining terms ---
-    const double K = u[CK * cs + p];
-    double A[6];
+    const R K = u[CK * cs + p];
+    R A[6];
     load_sym(u, AXX, G, p, A);
-    const double beta[3] = {u[BX * cs + p], u[BY * cs + p], u[BZ * cs + p]};
-    double db[3][3];
+    const R beta[3] = {u[BX * cs + p], u[BY * cs + p], u[BZ * cs + p]};
+    R db[3][3];
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
         for (int j = 0; j < 3; ++j) db[i][j] = d1ptr(d1, G, nfield, j, MIX_B + i, p)[0];
-    const double div = db[0][0] + db[1][1] + db[2][2];
+    const R div = db[0][0] + db[1][1] + db[2][2];
 #pragma unroll 1
     for (int s = 0; s < 6; ++s) {
         const int i = s < 3 ? 0 : (s < 5 ? 1 : 2);
-        const double* f = u + (AXX + s) * cs + p;
+        const R* f = u + (AXX + s) * cs + p;
         const int j = s < 3 ? s : (s < 5 ? s - 2 : 2);
-        double AgA = 0.0, lie = 0.0;
+        R AgA = R(0), lie = R(0);
 #pragma unroll
         for (int kk = 0; kk < 3; ++kk) {
 #pragma unroll
             for (int l = 0; l < 3; ++l) AgA += A[sym(i, kk)] * gi[sym(kk, l)] * A[sym(l, j)];
             lie += A[sym(kk, i)] * db[kk][j] + A[sym(kk, j)] * db[kk][i];
         }
-        double v = alpha * K * A[s] - 2.0 * alpha * AgA + T[s] + ADV(f, G, c.ix, beta) + lie
-                   + (-2.0 / 3.0) * A[s] * div;
+        R v = alpha * K * A[s] - R(2.0) * alpha * AgA + T[s] + ADV(f, G, c.ix, beta) + lie
+              + R(-2.0 / 3.0) * A[s] * div;
         if (damp != nullptr) v += damp[s * cs + p];
         k[(AXX + s) * cs + p] = v + KO(f, G, c.ix);
     }
 }
 
 // ---------------------------------------------------------------------------
-// kappa != 0: derived fields on the whole patch (constraints.py:112-118):
+// kappa != 0: pointwise derived fields (constraints.py:112-118):
 //   der[0..5]  = gt^ij        der[6..14] = B_i^j = gt^jk At_ik
 //   der[15..23]= B_i^j / max(W, 1e-12)
 // ---------------------------------------------------------------------------
+template <typename R>
 __global__ void __launch_bounds__(kThreads)
-k_mom_derived(const double* __restrict__ u, double* __restrict__ der, Geo G, Box all) {
+k_mom_derived(const R* __restrict__ u, const double* __restrict__ u64, R* __restrict__ der, Geo G, Box all) {
     PointCtx c;
     if (!point(all, c, G)) return;
     const long long cs = G.cs, p = c.p;
-    double g[6], gi[6], A[6];
+    R g[6], gi[6], A[6];
     load_sym(u, GXX, G, p, g);
     load_sym(u, AXX, G, p, A);
     inverse_metric(g, gi);
-    const double Wf = fmax(u[CW * cs + p], 1.0e-12);
+    R inv_w;
+    if constexpr (kPerturbative<R>) inv_w = static_cast<R>(1.0 / fmax(u64[CW * cs + p], 1.0e-12));
 #pragma unroll
     for (int s = 0; s < 6; ++s) der[s * cs + p] = gi[s];
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
-            const double b = gi[sym(j, 0)] * A[sym(i, 0)] + gi[sym(j, 1)] * A[sym(i, 1)] + gi[sym(j, 2)] * A[sym(i, 2)];
+            const R b = gi[sym(j, 0)] * A[sym(i, 0)] + gi[sym(j, 1)] * A[sym(i, 1)] + gi[sym(j, 2)] * A[sym(i, 2)];
             der[(6 + 3 * i + j) * cs + p] = b;
-            der[(15 + 3 * i + j) * cs + p] = b / Wf;
+            if constexpr (kPerturbative<R>) {
+                der[(15 + 3 * i + j) * cs + p] = b * inv_w;
+            } else {
+                const R Wf = fmax(u[CW * cs + p], 1.0e-12);
+                der[(15 + 3 * i + j) * cs + p] = b / Wf;
+            }
         }
 }
 
 // kappa/2 alpha (D_j M_i + D_i M_j) into damp[6] (extrinsic_curvature.py:390-404)
+template <typename R>
 __global__ void __launch_bounds__(kThreads)
-k_mom_damping(const double* __restrict__ u, const double* __restrict__ der, const double* __restrict__ d1,
-              double* __restrict__ damp, Geo G, Box B, int nfield) {
+k_mom_damping(const R* __restrict__ u, const double* __restrict__ u64, const R* __restrict__ der,
+              const R* __restrict__ d1, R* __restrict__ damp, Geo G, Box B, int nfield) {
     PointCtx c;
     if (!point(B, c, G)) return;
     const long long cs = G.cs, p = c.p;
     const int fA = NMIX, fK = NMIX + 6, fB = NMIX + 7;
-    double gi[6];
+    R gi[6];
 #pragma unroll
     for (int s = 0; s < 6; ++s) gi[s] = der[s * cs + p];
-    const double W = u[CW * cs + p];
-    const double Wf = fmax(W, 1.0e-12);
-    double dW[3], dK[3];
+    R three_over_w;  // 3 / max(W, 1e-12), from the FP64 state in the FP32 form
+    if constexpr (kPerturbative<R>) three_over_w = static_cast<R>(3.0 / fmax(u64[CW * cs + p], 1.0e-12));
+    R dW[3], dK[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         dW[d] = d1ptr(d1, G, nfield, d, MIX_W, p)[0];
         dK[d] = d1ptr(d1, G, nfield, d, fK, p)[0];
     }
     // M_i (constraints.py:61-97)
-    double M[3];
+    R M[3];
 #pragma unroll 1
     for (int i = 0; i < 3; ++i) {
-        double first = 0.0, second = 0.0, third = 0.0;
+        R first = R(0), second = R(0), third = R(0);
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
             first += d1ptr(d1, G, nfield, j, fB + 3 * i + j, p)[0];
@@ -503,70 +578,77 @@ k_mom_damping(const double* __restrict__ u, const double* __restrict__ der, cons
         }
 #pragma unroll
         for (int s = 0; s < 6; ++s) {
-            const double w = (s == 0 || s == 3 || s == 5) ? 1.0 : 2.0;
+            const R w = (s == 0 || s == 3 || s == 5) ? R(1.0) : R(2.0);
             second += w * gi[s] * d1ptr(d1, G, nfield, i, fA + s, p)[0];
         }
-        M[i] = first - 0.5 * second - 3.0 * third / Wf - (2.0 / 3.0) * dK[i];
+        if constexpr (kPerturbative<R>) {
+            M[i] = first - R(0.5) * second - third * three_over_w - R(2.0 / 3.0) * dK[i];
+        } else {
+            const R Wf = fmax(u[CW * cs + p], 1.0e-12);
+            M[i] = first - 0.5 * second - 3.0 * third / Wf - (2.0 / 3.0) * dK[i];
+        }
     }
     // d_l M_i (constraints.py:186-213), dM[i][l]
-    double hW[6];
+    R hW[6];
     hessian(u, d1, G, nfield, CW, MIX_W, c, hW);
-    double dM[3][3];
+    R dM[3][3];
 #pragma unroll 1
     for (int i = 0; i < 3; ++i) {
 #pragma unroll 1
         for (int l = 0; l < 3; ++l) {
-            double divd = 0.0, conf = 0.0, met = 0.0, met2 = 0.0;
+            R divd = R(0), conf = R(0), met = R(0), met2 = R(0);
 #pragma unroll 1
             for (int j = 0; j < 3; ++j) {
                 // d_l d_j B_ij
                 const int fb = fB + 3 * i + j;
                 divd += (l == j) ? D2(der + (6 + 3 * i + j) * cs + p, G, l, c.ix[l])
                                  : mixed(d1, G, nfield, fb, l, j, c);
-                const double dBW = D1(der + (15 + 3 * i + j) * cs + p, G, l, c.ix[l]);
+                const R dBW = D1(der + (15 + 3 * i + j) * cs + p, G, l, c.ix[l]);
                 conf += dBW * dW[j] + der[(15 + 3 * i + j) * cs + p] * hW[sym(l, j)];
             }
 #pragma unroll 1
             for (int s = 0; s < 6; ++s) {
-                const double w = (s == 0 || s == 3 || s == 5) ? 1.0 : 2.0;
-                const double dgi = D1(der + s * cs + p, G, l, c.ix[l]);
+                const R w = (s == 0 || s == 3 || s == 5) ? R(1.0) : R(2.0);
+                const R dgi = D1(der + s * cs + p, G, l, c.ix[l]);
                 met += w * dgi * d1ptr(d1, G, nfield, i, fA + s, p)[0];
-                const double d2A = (l == i) ? D2(u + (AXX + s) * cs + p, G, l, c.ix[l])
-                                            : mixed(d1, G, nfield, fA + s, l, i, c);
+                const R d2A = (l == i) ? D2(u + (AXX + s) * cs + p, G, l, c.ix[l])
+                                       : mixed(d1, G, nfield, fA + s, l, i, c);
                 met2 += w * gi[s] * d2A;
             }
-            const double d2K = (l == i) ? D2(u + CK * cs + p, G, l, c.ix[l]) : mixed(d1, G, nfield, fK, l, i, c);
-            dM[i][l] = divd - 0.5 * met - 0.5 * met2 - 3.0 * conf - (2.0 / 3.0) * d2K;
+            const R d2K = (l == i) ? D2(u + CK * cs + p, G, l, c.ix[l]) : mixed(d1, G, nfield, fK, l, i, c);
+            dM[i][l] = divd - R(0.5) * met - R(0.5) * met2 - R(3.0) * conf - R(2.0 / 3.0) * d2K;
         }
     }
     // Christoffels for D_j M_i = d_j M_i - Gamma^k_ij M_k
-    double g[6], gl[6];
+    R g[6], gl[6];
     load_sym(u, GXX, G, p, g);
     inverse_metric(g, gl);
-    double c1[3][6], c2[3][6];
+    R c1[3][6], c2[3][6];
     {
-        double dg[3][6];
+        R dg[3][6];
         load_metric_derivs(d1, G, nfield, p, dg);
         christoffel(dg, gl, c1, c2);
     }
-    const double scale = G.kappa / 2.0 * u[CALPHA * cs + p];
+    const R scale = BSSN_CO(R, G, kappa) / R(2.0) * full_exact(u, u64, CALPHA, cs, p);
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
         for (int j = i; j < 3; ++j) {
             const int s = sym(i, j);
-            const double gm = c2[0][s] * M[0] + c2[1][s] * M[1] + c2[2][s] * M[2];
-            const double DjMi = dM[i][j] - gm;
-            const double DiMj = dM[j][i] - gm;
+            const R gm = c2[0][s] * M[0] + c2[1][s] * M[1] + c2[2][s] * M[2];
+            const R DjMi = dM[i][j] - gm;
+            const R DiMj = dM[j][i] - gm;
             damp[s * cs + p] = scale * (DjMi + DiMj);
         }
 }
 
 // ---------------------------------------------------------------------------
 // Sommerfeld faces: rhs = -(x^i/r d_i u + (u - u_inf)/r) (boundaries.py:74-147)
+// In the FP32 form the stored perturbation is already u - u_inf.
 // ---------------------------------------------------------------------------
+template <typename R>
 __global__ void __launch_bounds__(kThreads)
-k_sommerfeld(const double* __restrict__ u, double* __restrict__ k, Geo G, Box B) {
+k_sommerfeld(const R* __restrict__ u, double* __restrict__ k, Geo G, Box B) {
     PointCtx c;
     if (!point(B, c, G)) return;
     bool face = false;
@@ -585,21 +667,28 @@ k_sommerfeld(const double* __restrict__ u, double* __restrict__ k, Geo G, Box B)
                                           __dmul_rn(X[2], X[2])));
     const double rs = r > 0.0 ? r : 1.0;
     const long long cs = G.cs, p = c.p;
+    const R xr[3] = {static_cast<R>(X[0]), static_cast<R>(X[1]), static_cast<R>(X[2])};
+    const R rr = static_cast<R>(rs);
 #pragma unroll 1
     for (int comp = 0; comp < NCOMP; ++comp) {
-        const double* f = u + comp * cs + p;
-        const double radial = (X[0] * D1(f, G, 0, c.ix[0]) + X[1] * D1(f, G, 1, c.ix[1])
-                               + X[2] * D1(f, G, 2, c.ix[2])) / rs;
-        double asym = 0.0;
-        if (comp == GXX || comp == GYY || comp == GZZ || comp == CW || comp == CALPHA) asym = 1.0;
-        k[comp * cs + p] = -(radial + (f[0] - asym) / rs);
+        const R* f = u + comp * cs + p;
+        const R radial = (xr[0] * D1(f, G, 0, c.ix[0]) + xr[1] * D1(f, G, 1, c.ix[1])
+                          + xr[2] * D1(f, G, 2, c.ix[2])) / rr;
+        R offset;
+        if constexpr (kPerturbative<R>) {
+            offset = f[0];
+        } else {
+            const R asym = has_background(comp) ? 1.0 : 0.0;
+            offset = f[0] - asym;
+        }
+        k[comp * cs + p] = -(radial + offset / rr);
     }
 }
 
 // ---------------------------------------------------------------------------
 // Constraint fields (JAX_BSSN/bssn/constraints.py:22-97, 271-412): H, M_i,
 // det(gt) - 1, gt^ij At_ij and Gt^i - gt^jk Gamma^i_jk, written in the
-// reference layout at the box's linear index.
+// reference layout at the box's linear index.  FP64 only.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kThreads)
 k_constraints(const double* __restrict__ u, const double* __restrict__ d1, const double* __restrict__ der,
@@ -693,8 +782,8 @@ cudaError_t launch_constraints(const double* u, const RhsWork& w, const Geo& G, 
                                double* M, double* detm1, double* trA, double* gam, cudaStream_t stream) {
     const Box ext = grown_box(box, G, composition_reach(G));
     // derived fields are pointwise and read on the box only
-    BSSN_LAUNCH(KC_MOM_DERIVED, k_mom_derived, blocks_for(ext.count), kThreads, stream, u, w.der, G, ext);
-    BSSN_LAUNCH(KC_FIRST, k_first_derivs, blocks_for(ext.count), kThreads, stream, u, w.der, w.d1, G, ext, 0);
+    BSSN_LAUNCH(KC_MOM_DERIVED, k_mom_derived<double>, blocks_for(ext.count), kThreads, stream, u, u, w.der, G, ext);
+    BSSN_LAUNCH(KC_FIRST, k_first_derivs<double>, blocks_for(ext.count), kThreads, stream, u, w.der, w.d1, G, ext, 0);
     BSSN_LAUNCH(KC_CONSTRAINTS, k_constraints, blocks_for(box.count), kThreads, stream, u, w.d1, w.der, G, box,
                 H, M, detm1, trA, gam);
     return cudaGetLastError();
@@ -703,9 +792,9 @@ cudaError_t launch_constraints(const double* u, const RhsWork& w, const Geo& G, 
 // ---------------------------------------------------------------------------
 // host-side launch sequence of one RHS evaluation
 // ---------------------------------------------------------------------------
-
-cudaError_t launch_rhs(const double* u, double* k, const RhsWork& w, const Geo& G, const Box& box,
-                       cudaStream_t stream) {
+template <typename R>
+static void launch_rhs_form(const R* u, const double* u64, double* k, R* d1, R* der, R* damp, const Geo& G,
+                            const Box& box, cudaStream_t stream) {
     const int with_mom = G.kappa != 0.0;
     const int nfield = with_mom ? NMIX + NMIX_MOM : NMIX;
     const int reach = composition_reach(G);
@@ -715,16 +804,33 @@ cudaError_t launch_rhs(const double* u, double* k, const RhsWork& w, const Geo& 
         // on ext grown by the first-derivative reach (3); being pointwise, they
         // take the same values there whatever region is computed.
         const Box region = grown_box(box, G, reach + 3);
-        BSSN_LAUNCH(KC_MOM_DERIVED, k_mom_derived, blocks_for(region.count), kThreads, stream, u, w.der, G, region);
+        BSSN_LAUNCH(KC_MOM_DERIVED, k_mom_derived<R>, blocks_for(region.count), kThreads, stream, u, u64, der, G,
+                    region);
     }
-    BSSN_LAUNCH(KC_FIRST, k_first_derivs, blocks_for(ext.count), kThreads, stream, u, w.der, w.d1, G, ext, with_mom);
+    BSSN_LAUNCH(KC_FIRST, k_first_derivs<R>, blocks_for(ext.count), kThreads, stream, u, der, d1, G, ext, with_mom);
     if (with_mom)
-        BSSN_LAUNCH(KC_MOM_DAMP, k_mom_damping, blocks_for(box.count), kThreads, stream, u, w.der, w.d1, w.damp, G, box, nfield);
-    BSSN_LAUNCH(KC_GAUGE, k_rhs_gauge, blocks_for(box.count), kThreads, stream, u, w.d1, k, G, box, nfield);
-    BSSN_LAUNCH(KC_KGT, k_rhs_kgt, blocks_for(box.count), kThreads, stream, u, w.d1, k, G, box, nfield);
-    BSSN_LAUNCH(KC_AT, k_rhs_at, blocks_for(box.count), kThreads, stream, u, w.d1, with_mom ? w.damp : nullptr, k, G, box,
-                nfield);
-    if (G.any_sommerfeld) BSSN_LAUNCH(KC_SOMMERFELD, k_sommerfeld, blocks_for(box.count), kThreads, stream, u, k, G, box);
+        BSSN_LAUNCH(KC_MOM_DAMP, k_mom_damping<R>, blocks_for(box.count), kThreads, stream, u, u64, der, d1, damp, G,
+                    box, nfield);
+    BSSN_LAUNCH(KC_GAUGE, k_rhs_gauge<R>, blocks_for(box.count), kThreads, stream, u, u64, d1, k, G, box, nfield);
+    BSSN_LAUNCH(KC_KGT, k_rhs_kgt<R>, blocks_for(box.count), kThreads, stream, u, u64, d1, k, G, box, nfield);
+    BSSN_LAUNCH(KC_AT, k_rhs_at<R>, blocks_for(box.count), kThreads, stream, u, u64, d1,
+                with_mom ? static_cast<const R*>(damp) : nullptr, k, G, box, nfield);
+    if (G.any_sommerfeld)
+        BSSN_LAUNCH(KC_SOMMERFELD, k_sommerfeld<R>, blocks_for(box.count), kThreads, stream, u, k, G, box);
+}
+
+cudaError_t launch_rhs(const double* u, double* k, const RhsWork& w, const Geo& G, const Box& box,
+                       cudaStream_t stream) {
+    if (G.precision == kPrecisionF32) {
+        // Every sample the RHS kernels read lies within 6 of the box: first
+        // derivatives on the box grown by 3 with a 3-sample reach; KO and
+        // upwind stencils reach 4.
+        const Box region = grown_box(box, G, 6);
+        BSSN_LAUNCH(KC_CONVERT, k_perturb, blocks_for(region.count), kThreads, stream, u, w.uf, G, region);
+        launch_rhs_form<float>(w.uf, u, k, w.d1f, w.derf, w.dampf, G, box, stream);
+    } else {
+        launch_rhs_form<double>(u, u, k, w.d1, w.der, w.damp, G, box, stream);
+    }
     return cudaGetLastError();
 }
 

@@ -1,4 +1,4 @@
-// Device-side finite-difference stencils of the BSSN hot path (sm_103a, FP64).
+// Device-side finite-difference stencils of the BSSN hot path (sm_103a).
 //
 // Operators follow the reference's definitions (uwplasma/JAX_BSSN):
 //   centred D1, MAD blend, closures    JAX_BSSN/evolution/derivatives.py:42-163
@@ -8,20 +8,29 @@
 //   KO dissipation                     JAX_BSSN/evolution/spatial_derivatives.py:81-92
 //
 // Every stencil reads a field through a pointer to the sample at the point and
-// the stride of the axis, so one code path serves x, y and z.  Numerators whose
-// terms cancel (D2, upwind, the sixth difference and all one-sided closures)
-// are accumulated with explicit round-to-nearest intrinsics in the reference's
-// term order, so the compiler cannot contract them into FMAs: their rounding
-// then matches the float64 reference bit for bit and is not amplified by the
-// 1/dx^2 scaling.  Centred differences of neighbouring pairs carry no such
-// amplification and are left free for FMA contraction.
+// the stride of the axis, so one code path serves x, y and z.
+//
+// The stencils are templates on the arithmetic type R.  R = double is the
+// plain FP64 form: numerators whose terms cancel (D2, upwind, the sixth
+// difference and all one-sided closures) are accumulated with explicit
+// round-to-nearest intrinsics in the reference's term order, so the compiler
+// cannot contract them into FMAs and their rounding matches the float64
+// reference bit for bit (it is not amplified by the 1/dx^2 scaling).  Centred
+// differences of neighbouring pairs carry no such amplification and are left
+// free for FMA contraction.  R = float is the FP32-arithmetic form: the same
+// operators on float samples (perturbations about a constant background),
+// with every coefficient taken in float so no FP64 instruction is issued, and
+// contraction allowed throughout.
 #pragma once
 
 #include <cstdint>
+#include <type_traits>
 
 namespace bssn {
 
 constexpr int kSommerfeld = 1;
+constexpr int kPrecisionF64 = 0;   // plain FP64 arithmetic
+constexpr int kPrecisionF32 = 1;   // FP32 RHS arithmetic, FP64 state and RK4
 
 // One axis of a padded patch: extent, compute range, closure range and the
 // face/MAD policy for this array (JAX_BSSN/evolution/spatial_derivatives.py:18-41).
@@ -36,6 +45,12 @@ struct Axis {
     int org;          // padded index of array index 0 (coordinates and closures)
     double q, omq;    // q and 1 - q
     double xmin;      // coordinate of array index 0: x = xmin + dx * (i - org)
+    float fq, fomq;   // q and 1 - q in float (FP32-arithmetic form)
+};
+
+// Float copies of the scalar coefficients (FP32-arithmetic form).
+struct GeoF {
+    float inv_dx, inv_12dx, inv_60dx, inv_12dx2, inv_dx2, inv_dx6h5, nu64, eta, kappa, g;
 };
 
 // Per-launch geometry and scalar parameters (passed by value).
@@ -54,22 +69,44 @@ struct Geo {
     double eta, kappa, g, dt;
     int gauge, zero_shift;
     int any_sommerfeld;
+    int precision;    // kPrecisionF64 or kPrecisionF32
+    GeoF gf;
 };
 
-#define BSSN_RN_ADD(a, b) __dadd_rn((a), (b))
-#define BSSN_RN_MUL(a, b) __dmul_rn((a), (b))
+// Pick the coefficient copy of the arithmetic type R.
+template <typename R>
+__host__ __device__ __forceinline__ R coef_pick(double d, float f) {
+    if constexpr (std::is_same<R, float>::value) return f;
+    else return d;
+}
+#define BSSN_CO(R, G, name) (::bssn::coef_pick<R>((G).name, (G).gf.name))
+#define BSSN_AQ(R, a) (::bssn::coef_pick<R>((a).q, (a).fq))
+#define BSSN_AOMQ(R, a) (::bssn::coef_pick<R>((a).omq, (a).fomq))
 
-__device__ __forceinline__ double ld(const double* __restrict__ p, long long off) {
+// Rounded sum and product of the arithmetic type: explicit round-to-nearest
+// for double (no contraction), plain operators for float.
+template <typename R> struct Num;
+template <> struct Num<double> {
+    static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+    static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+};
+template <> struct Num<float> {
+    static __device__ __forceinline__ float add(float a, float b) { return a + b; }
+    static __device__ __forceinline__ float mul(float a, float b) { return a * b; }
+};
+
+template <typename R>
+__device__ __forceinline__ R ld(const R* __restrict__ p, long long off) {
     return __ldg(p + off);
 }
 
 // Ordered sum c0*f(o0) + c1*f(o1) + ... with every product and sum rounded.
-template <int N>
-__device__ __forceinline__ double ordered(const double* __restrict__ p, long long s,
-                                          const int (&off)[N], const double (&c)[N]) {
-    double acc = BSSN_RN_MUL(c[0], ld(p, off[0] * s));
+template <typename R, int N>
+__device__ __forceinline__ R ordered(const R* __restrict__ p, long long s, const int (&off)[N],
+                                     const double (&c)[N]) {
+    R acc = Num<R>::mul(static_cast<R>(c[0]), ld(p, off[0] * s));
 #pragma unroll
-    for (int t = 1; t < N; ++t) acc = BSSN_RN_ADD(acc, BSSN_RN_MUL(c[t], ld(p, off[t] * s)));
+    for (int t = 1; t < N; ++t) acc = Num<R>::add(acc, Num<R>::mul(static_cast<R>(c[t]), ld(p, off[t] * s)));
     return acc;
 }
 
@@ -78,13 +115,12 @@ __device__ __forceinline__ double ordered(const double* __restrict__ p, long lon
 // `p` points at the sample where the closure is evaluated; `first` is the
 // offset (in samples along the axis) of the first closure node.
 // ---------------------------------------------------------------------------
-template <int N>
-__device__ __forceinline__ double closure(const double* __restrict__ p, long long s, int first,
-                                          const double (&c)[N]) {
-    double acc = BSSN_RN_MUL(c[0], ld(p, (long long)first * s));
+template <typename R, int N>
+__device__ __forceinline__ R closure(const R* __restrict__ p, long long s, int first, const double (&c)[N]) {
+    R acc = Num<R>::mul(static_cast<R>(c[0]), ld(p, (long long)first * s));
 #pragma unroll
     for (int t = 1; t < N; ++t)
-        acc = BSSN_RN_ADD(acc, BSSN_RN_MUL(c[t], ld(p, (long long)(first + t) * s)));
+        acc = Num<R>::add(acc, Num<R>::mul(static_cast<R>(c[t]), ld(p, (long long)(first + t) * s)));
     return acc;
 }
 
@@ -103,80 +139,81 @@ __device__ __forceinline__ int left_row(const Axis& a, int i, int width) {
 // ---------------------------------------------------------------------------
 // centred first derivative
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double d1_interior_d4(const double* __restrict__ p, long long s,
-                                                 const Geo& G) {
-    const double a = ld(p, s) - ld(p, -s);
-    const double b = ld(p, 2 * s) - ld(p, -2 * s);
-    return (2.0 / 3.0 * a + (-1.0 / 12.0) * b) * G.inv_dx;
+template <typename R>
+__device__ __forceinline__ R d1_interior(const R* __restrict__ p, long long s, const Axis& a, const Geo& G,
+                                         bool mad) {
+    const R c1 = ld(p, s) - ld(p, -s);
+    const R c2 = ld(p, 2 * s) - ld(p, -2 * s);
+    const R d4 = (static_cast<R>(2.0 / 3.0) * c1 + static_cast<R>(-1.0 / 12.0) * c2) * BSSN_CO(R, G, inv_dx);
+    if (!mad) return d4;
+    const R c3 = ld(p, 3 * s) - ld(p, -3 * s);
+    const R d6 = (static_cast<R>(3.0 / 4.0) * c1 - static_cast<R>(3.0 / 20.0) * c2 + static_cast<R>(1.0 / 60.0) * c3)
+                 * BSSN_CO(R, G, inv_dx);
+    return BSSN_AQ(R, a) * d4 + BSSN_AOMQ(R, a) * d6;
 }
 
-__device__ __forceinline__ double d1_interior(const double* __restrict__ p, long long s,
-                                              const Axis& a, const Geo& G) {
-    const double c1 = ld(p, s) - ld(p, -s);
-    const double c2 = ld(p, 2 * s) - ld(p, -2 * s);
-    const double d4 = (2.0 / 3.0 * c1 + (-1.0 / 12.0) * c2) * G.inv_dx;
-    if (!a.mad) return d4;
-    const double c3 = ld(p, 3 * s) - ld(p, -3 * s);
-    const double d6 = (3.0 / 4.0 * c1 - 3.0 / 20.0 * c2 + 1.0 / 60.0 * c3) * G.inv_dx;
-    return a.q * d4 + a.omq * d6;
-}
-
-__device__ __forceinline__ double d1_closed(const double* __restrict__ p, long long s,
-                                            const Axis& a, int i, const Geo& G) {
+template <typename R>
+__device__ __forceinline__ R d1_closed(const R* __restrict__ p, long long s, const Axis& a, int i, const Geo& G,
+                                       bool mad) {
     constexpr double L0[5] = {-25.0 / 12.0, 4.0, -3.0, 4.0 / 3.0, -1.0 / 4.0};
     constexpr double L1[5] = {-1.0 / 4.0, -5.0 / 6.0, 3.0 / 2.0, -1.0 / 2.0, 1.0 / 12.0};
     constexpr double R0[5] = {1.0 / 4.0, -4.0 / 3.0, 3.0, -4.0, 25.0 / 12.0};
     constexpr double R1[5] = {-1.0 / 12.0, 1.0 / 2.0, -3.0 / 2.0, 5.0 / 6.0, 1.0 / 4.0};
+    const R inv_dx = BSSN_CO(R, G, inv_dx);
     int r = right_row(a, i, 2);
-    if (r == 0) return closure(p, s, -4, R0) * G.inv_dx;
-    if (r == 1) return closure(p, s, -3, R1) * G.inv_dx;
+    if (r == 0) return closure(p, s, -4, R0) * inv_dx;
+    if (r == 1) return closure(p, s, -3, R1) * inv_dx;
     r = left_row(a, i, 2);
-    if (r == 0) return closure(p, s, 0, L0) * G.inv_dx;
-    if (r == 1) return closure(p, s, -1, L1) * G.inv_dx;
-    return d1_interior(p, s, a, G);
+    if (r == 0) return closure(p, s, 0, L0) * inv_dx;
+    if (r == 1) return closure(p, s, -1, L1) * inv_dx;
+    return d1_interior(p, s, a, G, mad);
 }
 
 // D1 along axis d at padded index i (reduced axes give zero).
-__device__ __forceinline__ double D1(const double* __restrict__ p, const Geo& G, int d, int i) {
+template <typename R>
+__device__ __forceinline__ R D1(const R* __restrict__ p, const Geo& G, int d, int i) {
     const Axis& a = G.ax[d];
-    if (a.reduced) return 0.0;
-    return d1_closed(p, G.st[d], a, i, G);
+    if (a.reduced) return R(0);
+    return d1_closed(p, G.st[d], a, i, G, a.mad != 0);
 }
 
 // ---------------------------------------------------------------------------
 // pure second derivative
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double D2(const double* __restrict__ p, const Geo& G, int d, int i) {
+template <typename R>
+__device__ __forceinline__ R D2(const R* __restrict__ p, const Geo& G, int d, int i) {
     const Axis& a = G.ax[d];
-    if (a.reduced) return 0.0;
+    if (a.reduced) return R(0);
     const long long s = G.st[d];
     constexpr double L0[6] = {15.0 / 4.0, -77.0 / 6.0, 107.0 / 6.0, -13.0, 61.0 / 12.0, -5.0 / 6.0};
     constexpr double L1[6] = {5.0 / 6.0, -5.0 / 4.0, -1.0 / 3.0, 7.0 / 6.0, -1.0 / 2.0, 1.0 / 12.0};
     constexpr double R0[6] = {-5.0 / 6.0, 61.0 / 12.0, -13.0, 107.0 / 6.0, -77.0 / 6.0, 15.0 / 4.0};
     constexpr double R1[6] = {1.0 / 12.0, -1.0 / 2.0, 7.0 / 6.0, -1.0 / 3.0, -5.0 / 4.0, 5.0 / 6.0};
+    const R inv_dx2 = BSSN_CO(R, G, inv_dx2);
     int r = right_row(a, i, 2);
-    if (r == 0) return closure(p, s, -5, R0) * G.inv_dx2;
-    if (r == 1) return closure(p, s, -4, R1) * G.inv_dx2;
+    if (r == 0) return closure(p, s, -5, R0) * inv_dx2;
+    if (r == 1) return closure(p, s, -4, R1) * inv_dx2;
     r = left_row(a, i, 2);
-    if (r == 0) return closure(p, s, 0, L0) * G.inv_dx2;
-    if (r == 1) return closure(p, s, -1, L1) * G.inv_dx2;
+    if (r == 0) return closure(p, s, 0, L0) * inv_dx2;
+    if (r == 1) return closure(p, s, -1, L1) * inv_dx2;
     constexpr int o4[5] = {2, 1, 0, -1, -2};
     constexpr double c4[5] = {-1.0, 16.0, -30.0, 16.0, -1.0};
-    const double d4 = ordered(p, s, o4, c4) * G.inv_12dx2;
+    const R d4 = ordered(p, s, o4, c4) * BSSN_CO(R, G, inv_12dx2);
     if (!a.mad) return d4;
     constexpr int o6[7] = {3, 2, 1, 0, -1, -2, -3};
     constexpr double c6[7] = {1.0 / 90.0, -3.0 / 20.0, 3.0 / 2.0, -49.0 / 18.0,
                               3.0 / 2.0, -3.0 / 20.0, 1.0 / 90.0};
-    const double d6 = ordered(p, s, o6, c6) * G.inv_dx2;
-    return a.q * d4 + a.omq * d6;
+    const R d6 = ordered(p, s, o6, c6) * inv_dx2;
+    return BSSN_AQ(R, a) * d4 + BSSN_AOMQ(R, a) * d6;
 }
 
 // ---------------------------------------------------------------------------
 // h^5 * sixth derivative (one KO term, without nu/64)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double KO1(const double* __restrict__ p, const Geo& G, int d, int i) {
+template <typename R>
+__device__ __forceinline__ R KO1(const R* __restrict__ p, const Geo& G, int d, int i) {
     const Axis& a = G.ax[d];
-    if (a.reduced) return 0.0;
+    if (a.reduced) return R(0);
     const long long s = G.st[d];
     constexpr double L0[8] = {4.0, -27.0, 78.0, -125.0, 120.0, -69.0, 22.0, -3.0};
     constexpr double L1[8] = {3.0, -20.0, 57.0, -90.0, 85.0, -48.0, 15.0, -2.0};
@@ -184,7 +221,7 @@ __device__ __forceinline__ double KO1(const double* __restrict__ p, const Geo& G
     constexpr double R0[8] = {-3.0, 22.0, -69.0, 120.0, -125.0, 78.0, -27.0, 4.0};
     constexpr double R1[8] = {-2.0, 15.0, -48.0, 85.0, -90.0, 57.0, -20.0, 3.0};
     constexpr double R2[8] = {-1.0, 8.0, -27.0, 50.0, -55.0, 36.0, -13.0, 2.0};
-    double num;
+    R num;
     int r = right_row(a, i, 3);
     if (r == 0) num = closure(p, s, -7, R0);
     else if (r == 1) num = closure(p, s, -6, R1);
@@ -200,22 +237,23 @@ __device__ __forceinline__ double KO1(const double* __restrict__ p, const Geo& G
             num = ordered(p, s, o, c);
         }
     }
-    return num * G.inv_dx6h5;
+    return num * BSSN_CO(R, G, inv_dx6h5);
 }
 
 // nu/64 * sum_d h^5 D6_d f  (JAX_BSSN/evolution/spatial_derivatives.py:81-92)
-__device__ __forceinline__ double KO(const double* __restrict__ p, const Geo& G, const int (&ix)[3]) {
-    const double t = KO1(p, G, 0, ix[0]) + KO1(p, G, 1, ix[1]);
-    return G.nu64 * (t + KO1(p, G, 2, ix[2]));
+template <typename R>
+__device__ __forceinline__ R KO(const R* __restrict__ p, const Geo& G, const int (&ix)[3]) {
+    const R t = KO1(p, G, 0, ix[0]) + KO1(p, G, 1, ix[1]);
+    return BSSN_CO(R, G, nu64) * (t + KO1(p, G, 2, ix[2]));
 }
 
 // ---------------------------------------------------------------------------
 // upwind first derivative selected by the sign of the RHS coefficient c
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double UP1(const double* __restrict__ p, const Geo& G, int d, int i,
-                                      double c) {
+template <typename R>
+__device__ __forceinline__ R UP1(const R* __restrict__ p, const Geo& G, int d, int i, R c) {
     const Axis& a = G.ax[d];
-    if (a.reduced) return 0.0;
+    if (a.reduced) return R(0);
     const long long s = G.st[d];
     const bool physical = a.lbc || a.rbc;
     if (physical) {
@@ -228,38 +266,36 @@ __device__ __forceinline__ double UP1(const double* __restrict__ p, const Geo& G
         int lo_l = a.start;
         if (lo_l < 0) lo_l = 0;
         if (lo_l > a.P - w) lo_l = a.P - w;
-        if ((a.rbc && i >= lo_r && i < lo_r + w) || (a.lbc && i >= lo_l && i < lo_l + w)) {
-            Axis a4 = a;
-            a4.mad = 0;
-            return d1_closed(p, s, a4, i, G);
-        }
+        if ((a.rbc && i >= lo_r && i < lo_r + w) || (a.lbc && i >= lo_l && i < lo_l + w))
+            return d1_closed(p, s, a, i, G, false);
     }
-    if (c > 0.0) {
+    const R inv_12dx = BSSN_CO(R, G, inv_12dx);
+    if (c > R(0)) {
         constexpr int o[5] = {-1, 0, 1, 2, 3};
         constexpr double k[5] = {-3.0, -10.0, 18.0, -6.0, 1.0};
-        const double d4 = ordered(p, s, o, k) * G.inv_12dx;
+        const R d4 = ordered(p, s, o, k) * inv_12dx;
         if (!a.mad) return d4;
         constexpr int o6[7] = {-2, -1, 0, 1, 2, 3, 4};
         constexpr double k6[7] = {2.0, -24.0, -35.0, 80.0, -30.0, 8.0, -1.0};
-        return a.q * d4 + a.omq * (ordered(p, s, o6, k6) * G.inv_60dx);
+        return BSSN_AQ(R, a) * d4 + BSSN_AOMQ(R, a) * (ordered(p, s, o6, k6) * BSSN_CO(R, G, inv_60dx));
     }
-    if (c < 0.0) {
+    if (c < R(0)) {
         constexpr int o[5] = {-3, -2, -1, 0, 1};
         constexpr double k[5] = {-1.0, 6.0, -18.0, 10.0, 3.0};
-        const double d4 = ordered(p, s, o, k) * G.inv_12dx;
+        const R d4 = ordered(p, s, o, k) * inv_12dx;
         if (!a.mad) return d4;
         constexpr int o6[7] = {-4, -3, -2, -1, 0, 1, 2};
         constexpr double k6[7] = {1.0, -8.0, 30.0, -80.0, 35.0, 24.0, -2.0};
-        return a.q * d4 + a.omq * (ordered(p, s, o6, k6) * G.inv_60dx);
+        return BSSN_AQ(R, a) * d4 + BSSN_AOMQ(R, a) * (ordered(p, s, o6, k6) * BSSN_CO(R, G, inv_60dx));
     }
     // zero coefficient (or NaN): centred (JAX_BSSN/evolution/derivatives.py:238-241,272-276)
-    return d1_interior(p, s, a, G);
+    return d1_interior(p, s, a, G, a.mad != 0);
 }
 
 // beta^d d_d f summed over d (JAX_BSSN/bssn/shift_and_lapse.py:43-63)
-__device__ __forceinline__ double ADV(const double* __restrict__ p, const Geo& G, const int (&ix)[3],
-                                      const double (&beta)[3]) {
-    const double t = beta[0] * UP1(p, G, 0, ix[0], beta[0]) + beta[1] * UP1(p, G, 1, ix[1], beta[1]);
+template <typename R>
+__device__ __forceinline__ R ADV(const R* __restrict__ p, const Geo& G, const int (&ix)[3], const R (&beta)[3]) {
+    const R t = beta[0] * UP1(p, G, 0, ix[0], beta[0]) + beta[1] * UP1(p, G, 1, ix[1], beta[1]);
     return t + beta[2] * UP1(p, G, 2, ix[2], beta[2]);
 }
 

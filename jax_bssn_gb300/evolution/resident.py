@@ -19,7 +19,7 @@ NCOMP = 21
 
 
 class PatchEvolution:
-    def __init__(self, vars: BSSNVariables, params: BSSNParameters, ghost: int = 4):
+    def __init__(self, vars: BSSNVariables, params: BSSNParameters, ghost: int = 4, precision: str | None = None):
         if params.guard_cells or params.owned_shape is not None:
             raise ValueError("PatchEvolution evolves a whole unpadded grid (guard_cells=0, owned_shape=None)")
         self.lib = _native.load()
@@ -31,7 +31,7 @@ class PatchEvolution:
         for d in range(3):
             self.patch.n[d] = self.shape[d]
         self.patch.ghost = int(ghost)
-        self.cparams = _device.to_params(params)
+        self.cparams = _device.to_params(params, precision)
         values = self.lib.bssn_patch_values(self.patch)
         if values == 0:
             raise ValueError("invalid patch description")

@@ -127,7 +127,7 @@ def validate_hierarchy(states, parameters, hierarchy, layouts):
 # C structs and layout conversion
 # ----------------------------------------------------------------------------
 
-def _plan(parameters, hierarchy, shapes):
+def _plan(parameters, hierarchy, shapes, precision=None):
     parents = hierarchy_parents(hierarchy)
     n = len(shapes)
     patches = (_native.BssnFmrPatch * n)()
@@ -141,7 +141,7 @@ def _plan(parameters, hierarchy, shapes):
             for a in range(3):
                 patches[p].coarse_lo[a] = spec.coarse_lo[a]
                 patches[p].coarse_hi[a] = spec.coarse_hi[a]
-        cparams[p] = _device.to_params(parameters[p])
+        cparams[p] = _device.to_params(parameters[p], precision)
     return patches, cparams
 
 
@@ -345,14 +345,14 @@ class FMREvolution:
     """All patches resident in the 21-component layout; ``step(n)`` runs n
     stage-synchronous RK4 steps without leaving the device."""
 
-    def __init__(self, states, parameters, hierarchy, layouts):
+    def __init__(self, states, parameters, hierarchy, layouts, precision=None):
         self.parameters = evolution_parameters(tuple(parameters), hierarchy)
         self.hierarchy = hierarchy
         self.layouts = tuple(layouts)
         self.shapes = validate_hierarchy(tuple(states), self.parameters, hierarchy, self.layouts)
         self.device = _device.require_cuda()
         self.buffers = [_to_components(s, n, self.device) for s, n in zip(states, self.shapes)]
-        self.patches, self.cparams = _plan(self.parameters, hierarchy, self.shapes)
+        self.patches, self.cparams = _plan(self.parameters, hierarchy, self.shapes, precision)
         self.lib = _native.load()
         nbytes = self.lib.bssn_fmr_workspace_bytes(self.patches, self.cparams, len(self.shapes))
         self.ws = torch.empty(nbytes, dtype=torch.uint8, device=self.device)

@@ -1,0 +1,182 @@
+"""The FP32-arithmetic form (float RHS arithmetic, float64 state and RK4)
+against the float64 reference goldens.
+
+Error metric: per leaf, max|fp32-form - ref| divided by the leaf's deviation
+from its flat background, max|ref - background| (background 1 on the
+conformal-metric diagonal, W and alpha, 0 elsewhere).  That is the relative
+error of the physics the state carries: for a 1e-5 wave on a unit metric a
+plain max|ref| normalisation would hide five digits.  Tolerances, stated per
+test, follow float's 6e-8 unit roundoff amplified by the stencils (up to
+about 64/12 / (dx^2 k^2) for the second derivatives) and stay far below the
+discretisation error of these grids.
+"""
+
+import json
+
+import numpy as np
+import pytest
+
+from oracle.state import BSSNVariables as OracleVars
+
+from .helpers import LEAVES, RHS_CASES, golden_params, golden_state, load_golden
+
+pytestmark = pytest.mark.gpu
+
+BACKGROUND = {"conformal_metric": np.eye(3)[:, :, None, None, None], "conformal_factor": 1.0,
+              "traceless_K": 0.0, "trace_K": 0.0, "conformal_connection": 0.0, "lapse": 1.0, "shift": 0.0}
+
+
+def _np(x):
+    return x.detach().cpu().numpy() if hasattr(x, "detach") else np.asarray(x)
+
+
+def deviation_errors(got, ref, background=True):
+    """max|got - ref| / max(|ref - bg|) per leaf (bg = flat background or 0)."""
+    out = {}
+    for leaf, x, y in zip(LEAVES, got, ref):
+        x, y = _np(x), _np(y)
+        bg = BACKGROUND[leaf] if background else 0.0
+        scale = float(np.max(np.abs(y - bg)))
+        out[leaf] = float(np.max(np.abs(x - y))) / scale if scale > 0 else float(np.max(np.abs(x - y)))
+    return out
+
+
+@pytest.fixture(scope="module")
+def gb(cuda, native):
+    import jax_bssn_gb300 as pkg
+    from jax_bssn_gb300.evolution import time_evolve
+    return pkg, time_evolve
+
+
+def _inputs(data, pkg):
+    return golden_state(data, "input", pkg.BSSNVariables), golden_params(data, pkg.BSSNParameters)
+
+
+@pytest.mark.parametrize("name", RHS_CASES)
+def test_fp32_rhs_against_reference(gb, name):
+    """RHS of the FP32 form, error relative to the reference RHS's own scale."""
+    pkg, te = gb
+    data = load_golden(f"rhs_{name}")
+    state, params = _inputs(data, pkg)
+    with pkg.arithmetic("fp32"):
+        rhs = te.compute_bssn_rhs(state, params)
+    err = deviation_errors(rhs, golden_state(data, "rhs", OracleVars), background=False)
+    print(name, "fp32 rhs", {k: f"{v:.1e}" for k, v in err.items()})
+    assert max(err.values()) < 2e-4
+
+
+@pytest.mark.parametrize("name", RHS_CASES)
+def test_fp32_rk4_step_against_reference(gb, name):
+    pkg, te = gb
+    data = load_golden(f"rhs_{name}")
+    state, params = _inputs(data, pkg)
+    with pkg.arithmetic("fp32"):
+        one = te.rk4_step(state, params)
+    err = deviation_errors(one, golden_state(data, "rk4_1", OracleVars))
+    print(name, "fp32 rk4 1", {k: f"{v:.1e}" for k, v in err.items()})
+    assert max(err.values()) < 1e-5
+
+
+def test_fp32_gauge_wave_hundred_steps(gb):
+    """32^3 gauge wave (A = 0.1): after 100 steps the FP32 form stays within
+    1e-5 of the float64 reference relative to the wave's amplitude."""
+    pkg, te = gb
+    data = load_golden("run_gauge_wave32")
+    state, params = _inputs(data, pkg)
+    with pkg.arithmetic("fp32"):
+        hundred = te.rk4_steps(state, params, 100)
+    err = deviation_errors(hundred, golden_state(data, "rk4_100", OracleVars))
+    print("fp32 gauge wave 100", {k: f"{v:.1e}" for k, v in err.items()})
+    assert max(err.values()) < 1e-5
+
+
+def test_fp32_teukolsky_ten_steps_and_constraint_norms(gb):
+    """Teukolsky 24^3 (amplitude 1e-5, Sommerfeld faces): ten steps, then the
+    Hamiltonian and momentum constraint L2 norms within 1% of the float64 run's."""
+    pkg, te = gb
+    from jax_bssn_gb300.bssn.constraints import compute_all_constraints, compute_constraint_norms
+    data = load_golden("run_teukolsky24")
+    state, params = _inputs(data, pkg)
+    with pkg.arithmetic("fp32"):
+        ten = te.rk4_steps(state, params, 10)
+    ref = golden_state(data, "rk4_10", OracleVars)
+    err = deviation_errors(ten, ref)
+    print("fp32 teukolsky 10", {k: f"{v:.1e}" for k, v in err.items()})
+    assert max(err.values()) < 1e-4
+    n32 = compute_constraint_norms(compute_all_constraints(ten, params))
+    n64 = compute_constraint_norms(compute_all_constraints(pkg.BSSNVariables(*ref), params))
+    for key in ("hamiltonian_l2", "momentum_l2"):
+        print(key, n32[key], n64[key])
+        assert n32[key] == pytest.approx(n64[key], rel=1e-2), key
+
+
+def test_fp32_resident_patch_matches_drop_in(gb):
+    pkg, te = gb
+    from jax_bssn_gb300.evolution import PatchEvolution
+    data = load_golden("run_teukolsky24")
+    state, params = _inputs(data, pkg)
+    evo = PatchEvolution(state, params, precision="fp32")
+    evo.step(3)
+    with pkg.arithmetic("fp32"):
+        want = te.rk4_steps(state, params, 3)
+    for a, b in zip(evo.state(), want):
+        np.testing.assert_array_equal(_np(a), _np(b))
+
+
+def test_fp32_fmr_against_reference(gb):
+    """Nested FMR (three levels, MAD): two stage-synchronous RK4 steps."""
+    pkg, _ = gb
+    from jax_bssn_gb300.fmr import FMRHierarchySpec, FMRPatchSpec, TileLayout, fmr_rk4_step, prepare_fmr_states
+    from .fmr_helpers import G, load_case, owned_of, owned_states
+    data, hierarchy, oparams, shapes, _ = load_case("three_level_mad")
+    h = FMRHierarchySpec(tuple(FMRPatchSpec(s.coarse_lo, s.coarse_hi, parent=s.parent) for s in hierarchy.patches),
+                         use_mad=hierarchy.use_mad)
+    params = tuple(pkg.BSSNParameters(**p._asdict()) for p in oparams)
+    layouts = tuple(TileLayout(n) for n in shapes)
+    raw = []
+    for s, n in zip(owned_states(data, "initial", len(shapes)), shapes):
+        leaves = []
+        for leaf in s:
+            full = np.zeros(leaf.shape[:-3] + tuple(m + 2 * G for m in n))
+            full[(Ellipsis,) + tuple(slice(G, G + m) for m in n)] = leaf
+            leaves.append(full.reshape(leaf.shape[:-3] + (1, 1, 1) + full.shape[-3:]))
+        raw.append(pkg.BSSNVariables(*leaves))
+    initial = prepare_fmr_states(tuple(raw), params, h, layouts=layouts, project=False)
+    with pkg.arithmetic("fp32"):
+        two = fmr_rk4_step(fmr_rk4_step(initial, params, h, layouts=layouts), params, h, layouts=layouts)
+    expect = owned_states(data, "rk4_2", len(shapes))
+    for p, n in enumerate(shapes):
+        got = OracleVars(*(_np(leaf).reshape(_np(leaf).shape[:-6] + _np(leaf).shape[-3:]) for leaf in two[p]))
+        err = deviation_errors(owned_of(got, n), expect[p])
+        print("fp32 fmr patch", p, {k: f"{v:.1e}" for k, v in err.items()})
+        assert max(err.values()) < 1e-5, (p, err)
+
+
+def test_fp32_cartoon_against_reference(gb):
+    pkg, _ = gb
+    from jax_bssn_gb300.cartoon.axisymmetry import axisymmetric_rk4_step, compute_axisymmetric_rhs
+    from jax_bssn_gb300.cartoon.spherical_symmetry import cartoon_rk4_step
+    data = load_golden("cartoon_axisymmetric")
+    state, params = _inputs(data, pkg)
+    with pkg.arithmetic("fp32"):
+        rhs = compute_axisymmetric_rhs(state, params)
+        two = axisymmetric_rk4_step(axisymmetric_rk4_step(state, params), params)
+    e_rhs = deviation_errors(rhs, golden_state(data, "rhs", OracleVars), background=False)
+    e_two = deviation_errors(two, golden_state(data, "rk4_2", OracleVars))
+    print("fp32 axisymmetric rhs", f"{max(e_rhs.values()):.1e}", "rk4 2", f"{max(e_two.values()):.1e}")
+    assert max(e_rhs.values()) < 2e-4
+    assert max(e_two.values()) < 1e-5
+    data = load_golden("cartoon_spherical")
+    state, params = _inputs(data, pkg)
+    with pkg.arithmetic("fp32"):
+        two = cartoon_rk4_step(cartoon_rk4_step(state, params), params)
+    e_two = deviation_errors(two, golden_state(data, "rk4_2", OracleVars))
+    print("fp32 spherical rk4 2", {k: f"{v:.1e}" for k, v in e_two.items()})
+    assert max(e_two.values()) < 1e-5
+
+
+def test_precision_argument_is_validated(gb):
+    pkg, _ = gb
+    with pytest.raises(ValueError):
+        with pkg.arithmetic("fp16"):
+            pass

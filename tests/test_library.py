@@ -28,7 +28,7 @@ def test_every_declared_symbol_is_exported(native):
 
 
 def test_abi_version(native):
-    assert native.bssn_abi_version() == 1
+    assert native.bssn_abi_version() == 2
 
 
 def test_workspace_sizes(native):
