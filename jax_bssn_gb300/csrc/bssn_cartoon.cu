@@ -437,6 +437,7 @@ int cartoon_plan(bool axi, const int32_t shape[3], const BssnParams* p, CartoonP
     P.centre.n[2] = axi ? nz : 1;
     P.centre.count = (long long)P.centre.n[0] * P.centre.n[1] * P.centre.n[2];
     std::memset(&P.Gc, 0, sizeof(P.Gc));
+    P.Gc.precision = p->precision;
     P.Gc.st[2] = 1;
     P.Gc.st[1] = P.C.nz;
     P.Gc.st[0] = P.C.nz;

@@ -268,6 +268,39 @@ __device__ __forceinline__ void project_point(double (&g)[6], double (&A)[6]) {
     for (int c = 0; c < 6; ++c) A[c] = __dadd_rn(A[c], -__dmul_rn(__dmul_rn(1.0 / 3.0, g[c]), tr));
 }
 
+// Projection of the FP32-arithmetic form.  The state stays FP64; the
+// correction is formed cheaply: det(gt) with FMAs, det^(-1/3) by its binomial
+// series (|det - 1| < 1e-3, truncation below 2e-16) or rcbrt, and the trace
+// gt^ij At_ij in float (the trace is itself a small correction, so float's
+// relative precision is kept relative to it).
+__device__ __forceinline__ void project_point_light(double (&g)[6], double (&A)[6]) {
+    const double det = g[0] * (g[3] * g[5] - g[4] * g[4]) - g[1] * (g[1] * g[5] - g[4] * g[2])
+                       + g[2] * (g[1] * g[4] - g[3] * g[2]);
+    const double e = det - 1.0;
+    const double s = fabs(e) < 1.0e-3
+                         ? 1.0 + e * (-1.0 / 3.0 + e * (2.0 / 9.0 + e * (-14.0 / 81.0 + e * (35.0 / 243.0))))
+                         : rcbrt(det);
+    float gf[6], gi[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        g[c] *= s;
+        gf[c] = static_cast<float>(g[c]);
+    }
+    inverse_metric(gf, gi);
+    float Af[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) Af[c] = static_cast<float>(A[c]);
+    const float tr = gi[0] * Af[0] + gi[3] * Af[3] + gi[5] * Af[5]
+                     + 2.0f * (gi[1] * Af[1] + gi[2] * Af[2] + gi[4] * Af[4]);
+#pragma unroll
+    for (int c = 0; c < 6; ++c) A[c] -= static_cast<double>((1.0f / 3.0f) * gf[c] * tr);
+}
+
+__device__ __forceinline__ void project_form(double (&g)[6], double (&A)[6], int precision) {
+    if (precision == kPrecisionF32) project_point_light(g, A);
+    else project_point(g, A);
+}
+
 __global__ void k_project(double* __restrict__ u, Geo G, Box B) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= B.count) return;
@@ -277,7 +310,7 @@ __global__ void k_project(double* __restrict__ u, Geo G, Box B) {
     double g[6], A[6];
 #pragma unroll
     for (int c = 0; c < 6; ++c) { g[c] = u[(GXX + c) * cs + p]; A[c] = u[(AXX + c) * cs + p]; }
-    project_point(g, A);
+    project_form(g, A, G.precision);
 #pragma unroll
     for (int c = 0; c < 6; ++c) { u[(GXX + c) * cs + p] = g[c]; u[(AXX + c) * cs + p] = A[c]; }
 }
@@ -306,6 +339,10 @@ __global__ void k_project_ref(LeavesOut f, long long npts) {
 
 // RK4 stage epilogue.  stage 1..3: out = u0 + h*k, acc updated; stage 4:
 // out = u0 + (dt/6)*(acc + k)  [final_form 0]  or  (dt*(acc + k))/6  [1].
+// Light = false: every operation rounded as the reference orders it and the
+// bit-exact projection.  Light = true (FP32-arithmetic form): the same
+// combination with FMAs, a multiply by 1/6 and the light projection.
+template <bool Light>
 __global__ void k_rk4_stage(const double* __restrict__ u0, const double* __restrict__ k,
                             double* __restrict__ acc, double* __restrict__ out, Geo G, Box B,
                             int stage, double h, double dt, int final_form, int project) {
@@ -319,20 +356,30 @@ __global__ void k_rk4_stage(const double* __restrict__ u0, const double* __restr
     for (int c = 0; c < NCOMP; ++c) {
         const long long q = c * cs + p;
         const double kv = k[q];
-        if (stage < 4) {
-            v[c] = __dadd_rn(u0[q], __dmul_rn(h, kv));
-            acc[q] = (stage == 1) ? kv : __dadd_rn(acc[q], __dmul_rn(2.0, kv));
+        if constexpr (Light) {
+            if (stage < 4) {
+                v[c] = fma(h, kv, u0[q]);
+                acc[q] = (stage == 1) ? kv : fma(2.0, kv, acc[q]);
+            } else {
+                v[c] = fma(dt * (1.0 / 6.0), acc[q] + kv, u0[q]);
+            }
         } else {
-            const double s = __dadd_rn(acc[q], kv);
-            const double inc = final_form ? __ddiv_rn(__dmul_rn(dt, s), 6.0) : __dmul_rn(dt / 6.0, s);
-            v[c] = __dadd_rn(u0[q], inc);
+            if (stage < 4) {
+                v[c] = __dadd_rn(u0[q], __dmul_rn(h, kv));
+                acc[q] = (stage == 1) ? kv : __dadd_rn(acc[q], __dmul_rn(2.0, kv));
+            } else {
+                const double s = __dadd_rn(acc[q], kv);
+                const double inc = final_form ? __ddiv_rn(__dmul_rn(dt, s), 6.0) : __dmul_rn(dt / 6.0, s);
+                v[c] = __dadd_rn(u0[q], inc);
+            }
         }
     }
     if (project) {
         double g[6], A[6];
 #pragma unroll
         for (int c = 0; c < 6; ++c) { g[c] = v[GXX + c]; A[c] = v[AXX + c]; }
-        project_point(g, A);
+        if constexpr (Light) project_point_light(g, A);
+        else project_point(g, A);
 #pragma unroll
         for (int c = 0; c < 6; ++c) { v[GXX + c] = g[c]; v[AXX + c] = A[c]; }
     }
@@ -375,7 +422,12 @@ cudaError_t launch_rk4_stage(const double* u0, const double* k, double* acc, dou
                              const Box& B, int stage, double dt, int final_form, int project,
                              cudaStream_t s) {
     const double h = stage == 3 ? dt : 0.5 * dt;
-    BSSN_LAUNCH(KC_STAGE, k_rk4_stage, nblocks(B.count), kThreads, s, u0, k, acc, out, G, B, stage, h, dt, final_form, project);
+    if (G.precision == kPrecisionF32)
+        BSSN_LAUNCH(KC_STAGE, k_rk4_stage<true>, nblocks(B.count), kThreads, s, u0, k, acc, out, G, B, stage, h, dt,
+                    final_form, project);
+    else
+        BSSN_LAUNCH(KC_STAGE, k_rk4_stage<false>, nblocks(B.count), kThreads, s, u0, k, acc, out, G, B, stage, h, dt,
+                    final_form, project);
     return cudaGetLastError();
 }
 

@@ -49,6 +49,12 @@ __host__ __device__ constexpr bool has_background(int c) {
 
 __device__ __forceinline__ bool in_range(const Axis& a, int i) { return i >= a.lo && i < a.hi; }
 
+// Up to six boxes covered by one launch; blockIdx.y selects the box.
+struct BoxSet {
+    Box b[6];
+    int n;
+};
+
 // Full value of component c at sample p of the R-typed state.
 template <typename R>
 __device__ __forceinline__ R full(const R* __restrict__ u, int c, long long cs, long long p) {
@@ -88,10 +94,11 @@ k_perturb(const double* __restrict__ u, float* __restrict__ uf, Geo G, Box regio
 // ---------------------------------------------------------------------------
 // inner first derivatives
 // ---------------------------------------------------------------------------
-template <typename R>
+template <typename R, bool Closed>
 __global__ void __launch_bounds__(kThreads)
-k_first_derivs(const R* __restrict__ u, const R* __restrict__ der, R* __restrict__ d1, Geo G, Box ext,
+k_first_derivs(const R* __restrict__ u, const R* __restrict__ der, R* __restrict__ d1, Geo G, BoxSet S,
                int with_mom) {
+    const Box& ext = S.b[blockIdx.y];
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ext.count) return;
     int ix[3];
@@ -104,14 +111,14 @@ k_first_derivs(const R* __restrict__ u, const R* __restrict__ der, R* __restrict
         if (!in_range(G.ax[d], ix[d])) continue;
 #pragma unroll 1
         for (int f = 0; f < NMIX; ++f)
-            d1[((long long)(d * nfield + f)) * cs + p] = D1(u + mix_source(f) * cs + p, G, d, ix[d]);
+            d1[((long long)(d * nfield + f)) * cs + p] = D1<R, Closed>(u + mix_source(f) * cs + p, G, d, ix[d]);
         if (with_mom) {
 #pragma unroll 1
             for (int f = 0; f < 7; ++f)  // At (6), K
-                d1[((long long)(d * nfield + NMIX + f)) * cs + p] = D1(u + (AXX + f) * cs + p, G, d, ix[d]);
+                d1[((long long)(d * nfield + NMIX + f)) * cs + p] = D1<R, Closed>(u + (AXX + f) * cs + p, G, d, ix[d]);
 #pragma unroll 1
             for (int f = 0; f < 9; ++f)  // B_i^j from the derived buffer (slots 6..14)
-                d1[((long long)(d * nfield + NMIX + 7 + f)) * cs + p] = D1(der + (6 + f) * cs + p, G, d, ix[d]);
+                d1[((long long)(d * nfield + NMIX + 7 + f)) * cs + p] = D1<R, Closed>(der + (6 + f) * cs + p, G, d, ix[d]);
         }
     }
 }
@@ -137,25 +144,25 @@ __device__ __forceinline__ const R* d1ptr(const R* d1, const Geo& G, int nfield,
 
 // Mixed second derivative d_m d_n of stored field f (m != n): outer axis is
 // max(m,n), inner axis min(m,n).
-template <typename R>
+template <typename R, bool Closed>
 __device__ __forceinline__ R mixed(const R* d1, const Geo& G, int nfield, int f, int m, int n, const PointCtx& c) {
     const int inner = m < n ? m : n;
     const int outer = m < n ? n : m;
-    return D1(d1ptr(d1, G, nfield, inner, f, c.p), G, outer, c.ix[outer]);
+    return D1<R, Closed>(d1ptr(d1, G, nfield, inner, f, c.p), G, outer, c.ix[outer]);
 }
 
 // Symmetric Hessian of stored field f whose state component is comp:
 // h[sym(i,j)] = d_i d_j f, D2 on the diagonal.
-template <typename R>
+template <typename R, bool Closed>
 __device__ __forceinline__ void hessian(const R* __restrict__ u, const R* d1, const Geo& G, int nfield, int comp,
                                         int f, const PointCtx& c, R (&h)[6]) {
     const R* fp = u + comp * G.cs + c.p;
-    h[0] = D2(fp, G, 0, c.ix[0]);
-    h[3] = D2(fp, G, 1, c.ix[1]);
-    h[5] = D2(fp, G, 2, c.ix[2]);
-    h[1] = mixed(d1, G, nfield, f, 0, 1, c);
-    h[2] = mixed(d1, G, nfield, f, 0, 2, c);
-    h[4] = mixed(d1, G, nfield, f, 1, 2, c);
+    h[0] = D2<R, Closed>(fp, G, 0, c.ix[0]);
+    h[3] = D2<R, Closed>(fp, G, 1, c.ix[1]);
+    h[5] = D2<R, Closed>(fp, G, 2, c.ix[2]);
+    h[1] = mixed<R, Closed>(d1, G, nfield, f, 0, 1, c);
+    h[2] = mixed<R, Closed>(d1, G, nfield, f, 0, 2, c);
+    h[4] = mixed<R, Closed>(d1, G, nfield, f, 1, 2, c);
 }
 
 template <typename R>
@@ -164,13 +171,13 @@ __device__ __forceinline__ R contract_sym(const R (&a)[6], const R (&b)[6]) {
 }
 
 // W^2 D_i D_j alpha (JAX_BSSN/bssn/geometry.py:122-186)
-template <typename R>
+template <typename R, bool Closed>
 __device__ __forceinline__ void w2_lapse_hessian(const R* __restrict__ u, const R* d1, const Geo& G, int nfield,
                                                  const PointCtx& c, const R (&g)[6], const R (&gi)[6],
                                                  const R (&c2)[3][6], const R (&dW)[3], const R (&da)[3], R W,
                                                  R (&out)[6]) {
     R h[6];
-    hessian(u, d1, G, nfield, CALPHA, MIX_ALPHA, c, h);
+    hessian<R, Closed>(u, d1, G, nfield, CALPHA, MIX_ALPHA, c, h);
     R gw = R(0);
 #pragma unroll
     for (int m = 0; m < 3; ++m)
@@ -204,7 +211,7 @@ __device__ __forceinline__ void load_metric_derivs(const R* d1, const Geo& G, in
 }
 
 // W^2 R_ij without inverse powers of W (JAX_BSSN/bssn/geometry.py:21-119).
-template <typename R>
+template <typename R, bool Closed>
 __device__ __forceinline__ void w2_ricci(const R* __restrict__ u, const R* d1, const Geo& G, int nfield,
                                          const PointCtx& c, const R (&g)[6], const R (&gi)[6], const R (&c1)[3][6],
                                          const R (&c2)[3][6], const R (&dW)[3], R W, R (&w2r)[6]) {
@@ -214,7 +221,7 @@ __device__ __forceinline__ void w2_ricci(const R* __restrict__ u, const R* d1, c
 #pragma unroll 1
     for (int s = 0; s < 6; ++s) {
         R h[6];
-        hessian(u, d1, G, nfield, GXX + s, MIX_G + s, c, h);
+        hessian<R, Closed>(u, d1, G, nfield, GXX + s, MIX_G + s, c, h);
         ric[s] = R(-0.5) * contract_sym(gi, h);
     }
     {
@@ -223,7 +230,7 @@ __device__ __forceinline__ void w2_ricci(const R* __restrict__ u, const R* d1, c
 #pragma unroll 1
         for (int d = 0; d < 3; ++d)
 #pragma unroll 1
-            for (int i = 0; i < 3; ++i) dG[d][i] = D1(u + (GTX + i) * cs + p, G, d, c.ix[d]);
+            for (int i = 0; i < 3; ++i) dG[d][i] = D1<R, Closed>(u + (GTX + i) * cs + p, G, d, c.ix[d]);
 #pragma unroll
         for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -268,7 +275,7 @@ __device__ __forceinline__ void w2_ricci(const R* __restrict__ u, const R* d1, c
     // --- W terms: W (D_i D_j W + gt_ij lap W) - 2 gt_ij |dW|^2 (geometry.py:84-117) ---
     {
         R hW[6];
-        hessian(u, d1, G, nfield, CW, MIX_W, c, hW);
+        hessian<R, Closed>(u, d1, G, nfield, CW, MIX_W, c, hW);
 #pragma unroll
         for (int s = 0; s < 6; ++s) hW[s] -= c2[0][s] * dW[0] + c2[1][s] * dW[1] + c2[2][s] * dW[2];
         const R lap = contract_sym(gi, hW);
@@ -286,12 +293,12 @@ __device__ __forceinline__ void w2_ricci(const R* __restrict__ u, const R* d1, c
 // ---------------------------------------------------------------------------
 // dt gt_ij, dt W, dt alpha, dt beta^i
 // ---------------------------------------------------------------------------
-template <typename R>
+template <typename R, bool Closed>
 __global__ void __launch_bounds__(kThreads)
 k_rhs_gauge(const R* __restrict__ u, const double* __restrict__ u64, const R* __restrict__ d1,
-            double* __restrict__ k, Geo G, Box B, int nfield) {
+            double* __restrict__ k, Geo G, BoxSet S, int nfield) {
     PointCtx c;
-    if (!point(B, c, G)) return;
+    if (!point(S.b[blockIdx.y], c, G)) return;
     const long long cs = G.cs, p = c.p;
     const R beta[3] = {u[BX * cs + p], u[BY * cs + p], u[BZ * cs + p]};
     R db[3][3];  // db[i][j] = d_j beta^i
@@ -314,19 +321,19 @@ k_rhs_gauge(const R* __restrict__ u, const double* __restrict__ u64, const R* __
         R lie = R(0);
 #pragma unroll
         for (int m = 0; m < 3; ++m) lie += g[sym(m, i)] * db[m][j] + g[sym(m, j)] * db[m][i];
-        const R v = ADV(f, G, c.ix, beta) + lie + R(-2.0 / 3.0) * g[s] * div
+        const R v = ADV<R, Closed>(f, G, c.ix, beta) + lie + R(-2.0 / 3.0) * g[s] * div
                     + R(-2.0) * alpha * u[(AXX + s) * cs + p];
-        k[(GXX + s) * cs + p] = v + KO(f, G, c.ix);
+        k[(GXX + s) * cs + p] = v + KO<R, Closed>(f, G, c.ix);
     }
     {
         const R* f = u + CW * cs + p;
-        const R v = ADV(f, G, c.ix, beta) + R(1.0 / 3.0) * alpha * W * K - R(1.0 / 3.0) * W * div;
-        k[CW * cs + p] = v + KO(f, G, c.ix);
+        const R v = ADV<R, Closed>(f, G, c.ix, beta) + R(1.0 / 3.0) * alpha * W * K - R(1.0 / 3.0) * W * div;
+        k[CW * cs + p] = v + KO<R, Closed>(f, G, c.ix);
     }
     {
         const R* f = u + CALPHA * cs + p;
         const R slicing = (G.gauge == 0) ? -(alpha * alpha) * K : R(-2.0) * alpha * K;
-        k[CALPHA * cs + p] = slicing + ADV(f, G, c.ix, beta) + KO(f, G, c.ix);
+        k[CALPHA * cs + p] = slicing + ADV<R, Closed>(f, G, c.ix, beta) + KO<R, Closed>(f, G, c.ix);
     }
 #pragma unroll 1
     for (int i = 0; i < 3; ++i) {
@@ -335,8 +342,8 @@ k_rhs_gauge(const R* __restrict__ u, const double* __restrict__ u64, const R* __
         if (G.zero_shift) {
             v = R(0) * beta[i];
         } else {
-            v = BSSN_CO(R, G, g) * u[(GTX + i) * cs + p] + ADV(f, G, c.ix, beta) + (-BSSN_CO(R, G, eta)) * beta[i];
-            v = v + KO(f, G, c.ix);
+            v = BSSN_CO(R, G, g) * u[(GTX + i) * cs + p] + ADV<R, Closed>(f, G, c.ix, beta) + (-BSSN_CO(R, G, eta)) * beta[i];
+            v = v + KO<R, Closed>(f, G, c.ix);
         }
         k[(BX + i) * cs + p] = v;
     }
@@ -345,12 +352,12 @@ k_rhs_gauge(const R* __restrict__ u, const double* __restrict__ u64, const R* __
 // ---------------------------------------------------------------------------
 // dt K and dt Gt^i
 // ---------------------------------------------------------------------------
-template <typename R>
+template <typename R, bool Closed>
 __global__ void __launch_bounds__(kThreads)
 k_rhs_kgt(const R* __restrict__ u, const double* __restrict__ u64, const R* __restrict__ d1,
-          double* __restrict__ k, Geo G, Box B, int nfield) {
+          double* __restrict__ k, Geo G, BoxSet S, int nfield) {
     PointCtx c;
-    if (!point(B, c, G)) return;
+    if (!point(S.b[blockIdx.y], c, G)) return;
     const long long cs = G.cs, p = c.p;
     R g[6], gi[6];
     load_sym(u, GXX, G, p, g);
@@ -366,7 +373,7 @@ k_rhs_kgt(const R* __restrict__ u, const double* __restrict__ u64, const R* __re
     for (int d = 0; d < 3; ++d) {
         dW[d] = d1ptr(d1, G, nfield, d, MIX_W, p)[0];
         da[d] = d1ptr(d1, G, nfield, d, MIX_ALPHA, p)[0];
-        dK[d] = D1(u + CK * cs + p, G, d, c.ix[d]);
+        dK[d] = D1<R, Closed>(u + CK * cs + p, G, d, c.ix[d]);
     }
     const R W = full_exact(u, u64, CW, cs, p);
     const R alpha = full_exact(u, u64, CALPHA, cs, p);
@@ -390,12 +397,12 @@ k_rhs_kgt(const R* __restrict__ u, const double* __restrict__ u64, const R* __re
     // dt K
     {
         R h[6];
-        w2_lapse_hessian(u, d1, G, nfield, c, g, gi, c2, dW, da, W, h);
+        w2_lapse_hessian<R, Closed>(u, d1, G, nfield, c, g, gi, c2, dW, da, W, h);
         const R first = -contract_sym(gi, h);
         const R second = alpha * contract_sym(A, Au);
         const R third = alpha * (K * K) / R(3.0);
         const R* f = u + CK * cs + p;
-        k[CK * cs + p] = first + second + third + ADV(f, G, c.ix, beta) + KO(f, G, c.ix);
+        k[CK * cs + p] = first + second + third + ADV<R, Closed>(f, G, c.ix, beta) + KO<R, Closed>(f, G, c.ix);
     }
 
     // dt Gt^i
@@ -415,7 +422,7 @@ k_rhs_kgt(const R* __restrict__ u, const double* __restrict__ u64, const R* __re
     }
     R hb[3][6];  // hb[i][sym(m,n)] = d_m d_n beta^i
 #pragma unroll 1
-    for (int i = 0; i < 3; ++i) hessian(u, d1, G, nfield, BX + i, MIX_B + i, c, hb[i]);
+    for (int i = 0; i < 3; ++i) hessian<R, Closed>(u, d1, G, nfield, BX + i, MIX_B + i, c, hb[i]);
     R graddiv[3];
 #pragma unroll
     for (int m = 0; m < 3; ++m) graddiv[m] = hb[0][sym(m, 0)] + hb[1][sym(m, 1)] + hb[2][sym(m, 2)];
@@ -435,21 +442,21 @@ k_rhs_kgt(const R* __restrict__ u, const double* __restrict__ u64, const R* __re
         const R t8 = contract_sym(gi, hb[i]);
         const R* f = u + (GTX + i) * cs + p;
         const R v = R(-4.0 / 3.0) * alpha * t1 + R(2.0) * alpha * t2 + six_alpha_over_w * t3
-                    - R(2.0) * t4 + ADV(f, G, c.ix, beta) + R(2.0 / 3.0) * Gt[i] * div - t7 + t8
+                    - R(2.0) * t4 + ADV<R, Closed>(f, G, c.ix, beta) + R(2.0 / 3.0) * Gt[i] * div - t7 + t8
                     + R(1.0 / 3.0) * t9;
-        k[(GTX + i) * cs + p] = v + KO(f, G, c.ix);
+        k[(GTX + i) * cs + p] = v + KO<R, Closed>(f, G, c.ix);
     }
 }
 
 // ---------------------------------------------------------------------------
 // dt At_ij
 // ---------------------------------------------------------------------------
-template <typename R>
+template <typename R, bool Closed>
 __global__ void __launch_bounds__(kThreads)
 k_rhs_at(const R* __restrict__ u, const double* __restrict__ u64, const R* __restrict__ d1,
-         const R* __restrict__ damp, double* __restrict__ k, Geo G, Box B, int nfield) {
+         const R* __restrict__ damp, double* __restrict__ k, Geo G, BoxSet S, int nfield) {
     PointCtx c;
-    if (!point(B, c, G)) return;
+    if (!point(S.b[blockIdx.y], c, G)) return;
     const long long cs = G.cs, p = c.p;
     R g[6], gi[6];
     load_sym(u, GXX, G, p, g);
@@ -470,12 +477,12 @@ k_rhs_at(const R* __restrict__ u, const double* __restrict__ u64, const R* __res
     const R alpha = full_exact(u, u64, CALPHA, cs, p);
 
     R w2r[6];
-    w2_ricci(u, d1, G, nfield, c, g, gi, c1, c2, dW, W, w2r);
+    w2_ricci<R, Closed>(u, d1, G, nfield, c, g, gi, c1, c2, dW, W, w2r);
     // --- [alpha W^2 R_ij - W^2 D_i D_j alpha]^TF ---
     R T[6];
     {
         R h[6];
-        w2_lapse_hessian(u, d1, G, nfield, c, g, gi, c2, dW, da, W, h);
+        w2_lapse_hessian<R, Closed>(u, d1, G, nfield, c, g, gi, c2, dW, da, W, h);
 #pragma unroll
         for (int s = 0; s < 6; ++s) T[s] = alpha * w2r[s] - h[s];
         const R tr = contract_sym(gi, T);
@@ -505,10 +512,10 @@ k_rhs_at(const R* __restrict__ u, const double* __restrict__ u64, const R* __res
             for (int l = 0; l < 3; ++l) AgA += A[sym(i, kk)] * gi[sym(kk, l)] * A[sym(l, j)];
             lie += A[sym(kk, i)] * db[kk][j] + A[sym(kk, j)] * db[kk][i];
         }
-        R v = alpha * K * A[s] - R(2.0) * alpha * AgA + T[s] + ADV(f, G, c.ix, beta) + lie
+        R v = alpha * K * A[s] - R(2.0) * alpha * AgA + T[s] + ADV<R, Closed>(f, G, c.ix, beta) + lie
               + R(-2.0 / 3.0) * A[s] * div;
         if (damp != nullptr) v += damp[s * cs + p];
-        k[(AXX + s) * cs + p] = v + KO(f, G, c.ix);
+        k[(AXX + s) * cs + p] = v + KO<R, Closed>(f, G, c.ix);
     }
 }
 
@@ -547,12 +554,12 @@ k_mom_derived(const R* __restrict__ u, const double* __restrict__ u64, R* __rest
 }
 
 // kappa/2 alpha (D_j M_i + D_i M_j) into damp[6] (extrinsic_curvature.py:390-404)
-template <typename R>
+template <typename R, bool Closed>
 __global__ void __launch_bounds__(kThreads)
 k_mom_damping(const R* __restrict__ u, const double* __restrict__ u64, const R* __restrict__ der,
-              const R* __restrict__ d1, R* __restrict__ damp, Geo G, Box B, int nfield) {
+              const R* __restrict__ d1, R* __restrict__ damp, Geo G, BoxSet S, int nfield) {
     PointCtx c;
-    if (!point(B, c, G)) return;
+    if (!point(S.b[blockIdx.y], c, G)) return;
     const long long cs = G.cs, p = c.p;
     const int fA = NMIX, fK = NMIX + 6, fB = NMIX + 7;
     R gi[6];
@@ -590,7 +597,7 @@ k_mom_damping(const R* __restrict__ u, const double* __restrict__ u64, const R* 
     }
     // d_l M_i (constraints.py:186-213), dM[i][l]
     R hW[6];
-    hessian(u, d1, G, nfield, CW, MIX_W, c, hW);
+    hessian<R, Closed>(u, d1, G, nfield, CW, MIX_W, c, hW);
     R dM[3][3];
 #pragma unroll 1
     for (int i = 0; i < 3; ++i) {
@@ -601,21 +608,21 @@ k_mom_damping(const R* __restrict__ u, const double* __restrict__ u64, const R* 
             for (int j = 0; j < 3; ++j) {
                 // d_l d_j B_ij
                 const int fb = fB + 3 * i + j;
-                divd += (l == j) ? D2(der + (6 + 3 * i + j) * cs + p, G, l, c.ix[l])
-                                 : mixed(d1, G, nfield, fb, l, j, c);
-                const R dBW = D1(der + (15 + 3 * i + j) * cs + p, G, l, c.ix[l]);
+                divd += (l == j) ? D2<R, Closed>(der + (6 + 3 * i + j) * cs + p, G, l, c.ix[l])
+                                 : mixed<R, Closed>(d1, G, nfield, fb, l, j, c);
+                const R dBW = D1<R, Closed>(der + (15 + 3 * i + j) * cs + p, G, l, c.ix[l]);
                 conf += dBW * dW[j] + der[(15 + 3 * i + j) * cs + p] * hW[sym(l, j)];
             }
 #pragma unroll 1
             for (int s = 0; s < 6; ++s) {
                 const R w = (s == 0 || s == 3 || s == 5) ? R(1.0) : R(2.0);
-                const R dgi = D1(der + s * cs + p, G, l, c.ix[l]);
+                const R dgi = D1<R, Closed>(der + s * cs + p, G, l, c.ix[l]);
                 met += w * dgi * d1ptr(d1, G, nfield, i, fA + s, p)[0];
-                const R d2A = (l == i) ? D2(u + (AXX + s) * cs + p, G, l, c.ix[l])
-                                       : mixed(d1, G, nfield, fA + s, l, i, c);
+                const R d2A = (l == i) ? D2<R, Closed>(u + (AXX + s) * cs + p, G, l, c.ix[l])
+                                       : mixed<R, Closed>(d1, G, nfield, fA + s, l, i, c);
                 met2 += w * gi[s] * d2A;
             }
-            const R d2K = (l == i) ? D2(u + CK * cs + p, G, l, c.ix[l]) : mixed(d1, G, nfield, fK, l, i, c);
+            const R d2K = (l == i) ? D2<R, Closed>(u + CK * cs + p, G, l, c.ix[l]) : mixed<R, Closed>(d1, G, nfield, fK, l, i, c);
             dM[i][l] = divd - R(0.5) * met - R(0.5) * met2 - R(3.0) * conf - R(2.0 / 3.0) * d2K;
         }
     }
@@ -646,11 +653,13 @@ k_mom_damping(const R* __restrict__ u, const double* __restrict__ u64, const R* 
 // Sommerfeld faces: rhs = -(x^i/r d_i u + (u - u_inf)/r) (boundaries.py:74-147)
 // In the FP32 form the stored perturbation is already u - u_inf.
 // ---------------------------------------------------------------------------
+// Sommerfeld replacement on one-sample slabs at the active faces; an edge
+// sample in two slabs is computed twice with the same result.
 template <typename R>
 __global__ void __launch_bounds__(kThreads)
-k_sommerfeld(const R* __restrict__ u, double* __restrict__ k, Geo G, Box B) {
+k_sommerfeld(const R* __restrict__ u, double* __restrict__ k, Geo G, BoxSet S) {
     PointCtx c;
-    if (!point(B, c, G)) return;
+    if (!point(S.b[blockIdx.y], c, G)) return;
     bool face = false;
     bool owned = true;
 #pragma unroll
@@ -672,8 +681,8 @@ k_sommerfeld(const R* __restrict__ u, double* __restrict__ k, Geo G, Box B) {
 #pragma unroll 1
     for (int comp = 0; comp < NCOMP; ++comp) {
         const R* f = u + comp * cs + p;
-        const R radial = (xr[0] * D1(f, G, 0, c.ix[0]) + xr[1] * D1(f, G, 1, c.ix[1])
-                          + xr[2] * D1(f, G, 2, c.ix[2])) / rr;
+        const R radial = (xr[0] * D1<R, true>(f, G, 0, c.ix[0]) + xr[1] * D1<R, true>(f, G, 1, c.ix[1])
+                          + xr[2] * D1<R, true>(f, G, 2, c.ix[2])) / rr;
         R offset;
         if constexpr (kPerturbative<R>) {
             offset = f[0];
@@ -713,12 +722,12 @@ k_constraints(const double* __restrict__ u, const double* __restrict__ d1, const
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         dW[d] = d1ptr(d1, G, NMIX, d, MIX_W, p)[0];
-        dK[d] = D1(u + CK * cs + p, G, d, c.ix[d]);
+        dK[d] = D1<double, true>(u + CK * cs + p, G, d, c.ix[d]);
     }
     const double W = u[CW * cs + p];
     const double K = u[CK * cs + p];
     double w2r[6];
-    w2_ricci(u, d1, G, NMIX, c, g, gi, c1, c2, dW, W, w2r);
+    w2_ricci<double, true>(u, d1, G, NMIX, c, g, gi, c1, c2, dW, W, w2r);
     double Au[6];
 #pragma unroll
     for (int i = 0; i < 3; ++i)
@@ -738,13 +747,13 @@ k_constraints(const double* __restrict__ u, const double* __restrict__ d1, const
         double first = 0.0, second = 0.0, third = 0.0;
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
-            first += D1(der + (6 + 3 * i + j) * cs + p, G, j, c.ix[j]);
+            first += D1<double, true>(der + (6 + 3 * i + j) * cs + p, G, j, c.ix[j]);
             third += der[(6 + 3 * i + j) * cs + p] * dW[j];
         }
 #pragma unroll 1
         for (int s = 0; s < 6; ++s) {
             const double w = (s == 0 || s == 3 || s == 5) ? 1.0 : 2.0;
-            second += w * gi[s] * D1(u + (AXX + s) * cs + p, G, i, c.ix[i]);
+            second += w * gi[s] * D1<double, true>(u + (AXX + s) * cs + p, G, i, c.ix[i]);
         }
         Mo[i * n + t] = first - 0.5 * second - 3.0 * third / Wf - (2.0 / 3.0) * dK[i];
         gam[i * n + t] = u[(GTX + i) * cs + p] - contract_sym(gi, c2[i]);
@@ -778,19 +787,118 @@ static int composition_reach(const Geo& G) {
 
 static inline unsigned blocks_for(long long n) { return (unsigned)((n + kThreads - 1) / kThreads); }
 
+static Box make_box(const int lo[3], const int hi[3]) {
+    Box b;
+    b.count = 1;
+    for (int d = 0; d < 3; ++d) {
+        b.lo[d] = lo[d];
+        b.n[d] = hi[d] > lo[d] ? hi[d] - lo[d] : 0;
+        b.count *= b.n[d];
+    }
+    return b;
+}
+
+static void add_box(BoxSet& S, const Box& b) {
+    if (b.count > 0) S.b[S.n++] = b;
+}
+
+static long long largest(const BoxSet& S) {
+    long long m = 0;
+    for (int i = 0; i < S.n; ++i) m = S.b[i].count > m ? S.b[i].count : m;
+    return m;
+}
+
+// A box split into its interior -- samples at least kClosureRows from every
+// closed (Sommerfeld) owned face, where no stencil needs a one-sided closure --
+// and the rest of the box as up to six slabs.
+struct SplitBox {
+    BoxSet interior, shell;
+};
+
+static SplitBox split_box(const Geo& G, const Box& box) {
+    int blo[3], bhi[3], lo[3], hi[3];
+    for (int d = 0; d < 3; ++d) {
+        const Axis& a = G.ax[d];
+        blo[d] = box.lo[d];
+        bhi[d] = box.lo[d] + box.n[d];
+        lo[d] = blo[d];
+        hi[d] = bhi[d];
+        if (a.lbc && !a.reduced) lo[d] = lo[d] > a.start + kClosureRows ? lo[d] : a.start + kClosureRows;
+        if (a.rbc && !a.reduced) hi[d] = hi[d] < a.end - kClosureRows ? hi[d] : a.end - kClosureRows;
+        if (lo[d] > bhi[d]) lo[d] = bhi[d];
+        if (hi[d] < lo[d]) hi[d] = lo[d];
+    }
+    SplitBox S;
+    S.interior.n = 0;
+    S.shell.n = 0;
+    add_box(S.interior, make_box(lo, hi));
+    // x slabs over the whole box in y and z; y slabs inside x; z slabs inside x and y
+    for (int d = 0; d < 3; ++d) {
+        int l0[3], h0[3], l1[3], h1[3];
+        for (int e = 0; e < 3; ++e) {
+            const bool inner = e < d;   // axes already sliced take the interior range
+            l0[e] = l1[e] = inner ? lo[e] : blo[e];
+            h0[e] = h1[e] = inner ? hi[e] : bhi[e];
+        }
+        l0[d] = blo[d]; h0[d] = lo[d];
+        l1[d] = hi[d];  h1[d] = bhi[d];
+        add_box(S.shell, make_box(l0, h0));
+        add_box(S.shell, make_box(l1, h1));
+    }
+    return S;
+}
+
+static BoxSet single(const Box& b) {
+    BoxSet S;
+    S.n = 0;
+    add_box(S, b);
+    return S;
+}
+
+// The box's samples on each active Sommerfeld face (owned face index on that
+// axis, the box's range on the others).
+static BoxSet face_slabs(const Geo& G, const Box& box) {
+    BoxSet S;
+    S.n = 0;
+    for (int d = 0; d < 3; ++d) {
+        const Axis& a = G.ax[d];
+        const int faces[2] = {a.slo ? a.start : -1, a.shi ? a.end - 1 : -1};
+        for (int f = 0; f < 2; ++f) {
+            const int i = faces[f];
+            if (i < 0 || i < box.lo[d] || i >= box.lo[d] + box.n[d]) continue;
+            if (f == 1 && a.slo && i == a.start) continue;   // one-sample axis: same slab
+            Box b = box;
+            b.lo[d] = i;
+            b.n[d] = 1;
+            b.count = (long long)b.n[0] * b.n[1] * b.n[2];
+            S.b[S.n++] = b;
+        }
+    }
+    return S;
+}
+
+#define BSSN_LAUNCH_SET(cls, kernel, set, stream, ...)                                                     \
+    do {                                                                                                  \
+        if ((set).n > 0)                                                                                  \
+            BSSN_LAUNCH(cls, kernel, dim3(blocks_for(largest(set)), (set).n), kThreads, stream, __VA_ARGS__); \
+    } while (0)
+
 cudaError_t launch_constraints(const double* u, const RhsWork& w, const Geo& G, const Box& box, double* H,
                                double* M, double* detm1, double* trA, double* gam, cudaStream_t stream) {
     const Box ext = grown_box(box, G, composition_reach(G));
     // derived fields are pointwise and read on the box only
     BSSN_LAUNCH(KC_MOM_DERIVED, k_mom_derived<double>, blocks_for(ext.count), kThreads, stream, u, u, w.der, G, ext);
-    BSSN_LAUNCH(KC_FIRST, k_first_derivs<double>, blocks_for(ext.count), kThreads, stream, u, w.der, w.d1, G, ext, 0);
+    const BoxSet es = single(ext);
+    BSSN_LAUNCH_SET(KC_FIRST, (k_first_derivs<double, true>), es, stream, u, w.der, w.d1, G, es, 0);
     BSSN_LAUNCH(KC_CONSTRAINTS, k_constraints, blocks_for(box.count), kThreads, stream, u, w.d1, w.der, G, box,
                 H, M, detm1, trA, gam);
     return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------
-// host-side launch sequence of one RHS evaluation
+// host-side launch sequence of one RHS evaluation: every stencil kernel runs
+// as a closure-free instantiation on the box interior and a general one on
+// the shell slabs
 // ---------------------------------------------------------------------------
 template <typename R>
 static void launch_rhs_form(const R* u, const double* u64, double* k, R* d1, R* der, R* damp, const Geo& G,
@@ -807,16 +915,27 @@ static void launch_rhs_form(const R* u, const double* u64, double* k, R* d1, R* 
         BSSN_LAUNCH(KC_MOM_DERIVED, k_mom_derived<R>, blocks_for(region.count), kThreads, stream, u, u64, der, G,
                     region);
     }
-    BSSN_LAUNCH(KC_FIRST, k_first_derivs<R>, blocks_for(ext.count), kThreads, stream, u, der, d1, G, ext, with_mom);
-    if (with_mom)
-        BSSN_LAUNCH(KC_MOM_DAMP, k_mom_damping<R>, blocks_for(box.count), kThreads, stream, u, u64, der, d1, damp, G,
-                    box, nfield);
-    BSSN_LAUNCH(KC_GAUGE, k_rhs_gauge<R>, blocks_for(box.count), kThreads, stream, u, u64, d1, k, G, box, nfield);
-    BSSN_LAUNCH(KC_KGT, k_rhs_kgt<R>, blocks_for(box.count), kThreads, stream, u, u64, d1, k, G, box, nfield);
-    BSSN_LAUNCH(KC_AT, k_rhs_at<R>, blocks_for(box.count), kThreads, stream, u, u64, d1,
-                with_mom ? static_cast<const R*>(damp) : nullptr, k, G, box, nfield);
-    if (G.any_sommerfeld)
-        BSSN_LAUNCH(KC_SOMMERFELD, k_sommerfeld<R>, blocks_for(box.count), kThreads, stream, u, k, G, box);
+    const SplitBox se = split_box(G, ext);
+    BSSN_LAUNCH_SET(KC_FIRST, (k_first_derivs<R, false>), se.interior, stream, u, der, d1, G, se.interior, with_mom);
+    BSSN_LAUNCH_SET(KC_FIRST, (k_first_derivs<R, true>), se.shell, stream, u, der, d1, G, se.shell, with_mom);
+    const SplitBox sb = split_box(G, box);
+    const R* dmp = with_mom ? static_cast<const R*>(damp) : nullptr;
+    if (with_mom) {
+        BSSN_LAUNCH_SET(KC_MOM_DAMP, (k_mom_damping<R, false>), sb.interior, stream, u, u64, der, d1, damp, G,
+                        sb.interior, nfield);
+        BSSN_LAUNCH_SET(KC_MOM_DAMP, (k_mom_damping<R, true>), sb.shell, stream, u, u64, der, d1, damp, G, sb.shell,
+                        nfield);
+    }
+    BSSN_LAUNCH_SET(KC_GAUGE, (k_rhs_gauge<R, false>), sb.interior, stream, u, u64, d1, k, G, sb.interior, nfield);
+    BSSN_LAUNCH_SET(KC_GAUGE, (k_rhs_gauge<R, true>), sb.shell, stream, u, u64, d1, k, G, sb.shell, nfield);
+    BSSN_LAUNCH_SET(KC_KGT, (k_rhs_kgt<R, false>), sb.interior, stream, u, u64, d1, k, G, sb.interior, nfield);
+    BSSN_LAUNCH_SET(KC_KGT, (k_rhs_kgt<R, true>), sb.shell, stream, u, u64, d1, k, G, sb.shell, nfield);
+    BSSN_LAUNCH_SET(KC_AT, (k_rhs_at<R, false>), sb.interior, stream, u, u64, d1, dmp, k, G, sb.interior, nfield);
+    BSSN_LAUNCH_SET(KC_AT, (k_rhs_at<R, true>), sb.shell, stream, u, u64, d1, dmp, k, G, sb.shell, nfield);
+    if (G.any_sommerfeld) {
+        const BoxSet S = face_slabs(G, box);
+        BSSN_LAUNCH_SET(KC_SOMMERFELD, k_sommerfeld<R>, S, stream, u, k, G, S);
+    }
 }
 
 cudaError_t launch_rhs(const double* u, double* k, const RhsWork& w, const Geo& G, const Box& box,

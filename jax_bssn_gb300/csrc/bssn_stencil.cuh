@@ -127,11 +127,19 @@ __device__ __forceinline__ R closure(const R* __restrict__ p, long long s, int f
 // Which closure row (0, 1, 2) applies at padded index i, or -1.  The upper
 // face is checked first because the reference applies it last (it wins when
 // the two faces overlap on a tiny axis).
+// Closed = false instantiates a stencil for samples at least kClosureRows
+// from every closed face (the interior of a box): no face-row checks at all.
+constexpr int kClosureRows = 3;
+
+template <bool Closed = true>
 __device__ __forceinline__ int right_row(const Axis& a, int i, int width) {
+    if constexpr (!Closed) return -1;
     int r = a.end - 1 - i;
     return (a.rbc && r >= 0 && r < width) ? r : -1;
 }
+template <bool Closed = true>
 __device__ __forceinline__ int left_row(const Axis& a, int i, int width) {
+    if constexpr (!Closed) return -1;
     int r = i - a.start;
     return (a.lbc && r >= 0 && r < width) ? r : -1;
 }
@@ -152,7 +160,7 @@ __device__ __forceinline__ R d1_interior(const R* __restrict__ p, long long s, c
     return BSSN_AQ(R, a) * d4 + BSSN_AOMQ(R, a) * d6;
 }
 
-template <typename R>
+template <typename R, bool Closed = true>
 __device__ __forceinline__ R d1_closed(const R* __restrict__ p, long long s, const Axis& a, int i, const Geo& G,
                                        bool mad) {
     constexpr double L0[5] = {-25.0 / 12.0, 4.0, -3.0, 4.0 / 3.0, -1.0 / 4.0};
@@ -160,27 +168,27 @@ __device__ __forceinline__ R d1_closed(const R* __restrict__ p, long long s, con
     constexpr double R0[5] = {1.0 / 4.0, -4.0 / 3.0, 3.0, -4.0, 25.0 / 12.0};
     constexpr double R1[5] = {-1.0 / 12.0, 1.0 / 2.0, -3.0 / 2.0, 5.0 / 6.0, 1.0 / 4.0};
     const R inv_dx = BSSN_CO(R, G, inv_dx);
-    int r = right_row(a, i, 2);
+    int r = right_row<Closed>(a, i, 2);
     if (r == 0) return closure(p, s, -4, R0) * inv_dx;
     if (r == 1) return closure(p, s, -3, R1) * inv_dx;
-    r = left_row(a, i, 2);
+    r = left_row<Closed>(a, i, 2);
     if (r == 0) return closure(p, s, 0, L0) * inv_dx;
     if (r == 1) return closure(p, s, -1, L1) * inv_dx;
     return d1_interior(p, s, a, G, mad);
 }
 
 // D1 along axis d at padded index i (reduced axes give zero).
-template <typename R>
+template <typename R, bool Closed = true>
 __device__ __forceinline__ R D1(const R* __restrict__ p, const Geo& G, int d, int i) {
     const Axis& a = G.ax[d];
     if (a.reduced) return R(0);
-    return d1_closed(p, G.st[d], a, i, G, a.mad != 0);
+    return d1_closed<R, Closed>(p, G.st[d], a, i, G, a.mad != 0);
 }
 
 // ---------------------------------------------------------------------------
 // pure second derivative
 // ---------------------------------------------------------------------------
-template <typename R>
+template <typename R, bool Closed = true>
 __device__ __forceinline__ R D2(const R* __restrict__ p, const Geo& G, int d, int i) {
     const Axis& a = G.ax[d];
     if (a.reduced) return R(0);
@@ -190,10 +198,10 @@ __device__ __forceinline__ R D2(const R* __restrict__ p, const Geo& G, int d, in
     constexpr double R0[6] = {-5.0 / 6.0, 61.0 / 12.0, -13.0, 107.0 / 6.0, -77.0 / 6.0, 15.0 / 4.0};
     constexpr double R1[6] = {1.0 / 12.0, -1.0 / 2.0, 7.0 / 6.0, -1.0 / 3.0, -5.0 / 4.0, 5.0 / 6.0};
     const R inv_dx2 = BSSN_CO(R, G, inv_dx2);
-    int r = right_row(a, i, 2);
+    int r = right_row<Closed>(a, i, 2);
     if (r == 0) return closure(p, s, -5, R0) * inv_dx2;
     if (r == 1) return closure(p, s, -4, R1) * inv_dx2;
-    r = left_row(a, i, 2);
+    r = left_row<Closed>(a, i, 2);
     if (r == 0) return closure(p, s, 0, L0) * inv_dx2;
     if (r == 1) return closure(p, s, -1, L1) * inv_dx2;
     constexpr int o4[5] = {2, 1, 0, -1, -2};
@@ -210,7 +218,7 @@ __device__ __forceinline__ R D2(const R* __restrict__ p, const Geo& G, int d, in
 // ---------------------------------------------------------------------------
 // h^5 * sixth derivative (one KO term, without nu/64)
 // ---------------------------------------------------------------------------
-template <typename R>
+template <typename R, bool Closed = true>
 __device__ __forceinline__ R KO1(const R* __restrict__ p, const Geo& G, int d, int i) {
     const Axis& a = G.ax[d];
     if (a.reduced) return R(0);
@@ -222,12 +230,12 @@ __device__ __forceinline__ R KO1(const R* __restrict__ p, const Geo& G, int d, i
     constexpr double R1[8] = {-2.0, 15.0, -48.0, 85.0, -90.0, 57.0, -20.0, 3.0};
     constexpr double R2[8] = {-1.0, 8.0, -27.0, 50.0, -55.0, 36.0, -13.0, 2.0};
     R num;
-    int r = right_row(a, i, 3);
+    int r = right_row<Closed>(a, i, 3);
     if (r == 0) num = closure(p, s, -7, R0);
     else if (r == 1) num = closure(p, s, -6, R1);
     else if (r == 2) num = closure(p, s, -5, R2);
     else {
-        r = left_row(a, i, 3);
+        r = left_row<Closed>(a, i, 3);
         if (r == 0) num = closure(p, s, 0, L0);
         else if (r == 1) num = closure(p, s, -1, L1);
         else if (r == 2) num = closure(p, s, -2, L2);
@@ -241,21 +249,21 @@ __device__ __forceinline__ R KO1(const R* __restrict__ p, const Geo& G, int d, i
 }
 
 // nu/64 * sum_d h^5 D6_d f  (JAX_BSSN/evolution/spatial_derivatives.py:81-92)
-template <typename R>
+template <typename R, bool Closed = true>
 __device__ __forceinline__ R KO(const R* __restrict__ p, const Geo& G, const int (&ix)[3]) {
-    const R t = KO1(p, G, 0, ix[0]) + KO1(p, G, 1, ix[1]);
-    return BSSN_CO(R, G, nu64) * (t + KO1(p, G, 2, ix[2]));
+    const R t = KO1<R, Closed>(p, G, 0, ix[0]) + KO1<R, Closed>(p, G, 1, ix[1]);
+    return BSSN_CO(R, G, nu64) * (t + KO1<R, Closed>(p, G, 2, ix[2]));
 }
 
 // ---------------------------------------------------------------------------
 // upwind first derivative selected by the sign of the RHS coefficient c
 // ---------------------------------------------------------------------------
-template <typename R>
+template <typename R, bool Closed = true>
 __device__ __forceinline__ R UP1(const R* __restrict__ p, const Geo& G, int d, int i, R c) {
     const Axis& a = G.ax[d];
     if (a.reduced) return R(0);
     const long long s = G.st[d];
-    const bool physical = a.lbc || a.rbc;
+    const bool physical = Closed && (a.lbc || a.rbc);
     if (physical) {
         // Outer three owned samples at a Sommerfeld face use the closed centred D4
         // (JAX_BSSN/evolution/derivatives.py:296-331).
@@ -293,10 +301,10 @@ __device__ __forceinline__ R UP1(const R* __restrict__ p, const Geo& G, int d, i
 }
 
 // beta^d d_d f summed over d (JAX_BSSN/bssn/shift_and_lapse.py:43-63)
-template <typename R>
+template <typename R, bool Closed = true>
 __device__ __forceinline__ R ADV(const R* __restrict__ p, const Geo& G, const int (&ix)[3], const R (&beta)[3]) {
-    const R t = beta[0] * UP1(p, G, 0, ix[0], beta[0]) + beta[1] * UP1(p, G, 1, ix[1], beta[1]);
-    return t + beta[2] * UP1(p, G, 2, ix[2], beta[2]);
+    const R t = beta[0] * UP1<R, Closed>(p, G, 0, ix[0], beta[0]) + beta[1] * UP1<R, Closed>(p, G, 1, ix[1], beta[1]);
+    return t + beta[2] * UP1<R, Closed>(p, G, 2, ix[2], beta[2]);
 }
 
 }  // namespace bssn
