@@ -65,6 +65,10 @@ CLASS_BYTES_F32 = {
     "rhs_gauge": (21 + 9) * 4 + 2 * 8 + 11 * 8,
     "first_derivs": 11 * 4 + 33 * 4,
 }
+# Executed flops per point of one k_rhs_at launch (FMA = 2), from an ncu count
+# of the 96^3 Teukolsky configuration's interior launch (DADD + DMUL + 2 DFMA,
+# resp. FADD + FMUL + 2 FFMA over the launch's threads).
+RHS_AT_FLOPS_PER_POINT = {"fp64": 2512, "fp32": 2395}
 LEAVES = ("conformal_metric", "conformal_factor", "traceless_K", "trace_K", "conformal_connection", "lapse",
           "shift")
 
@@ -125,7 +129,7 @@ class Teukolsky:
         from jax_bssn_gb300.evolution import PatchEvolution
         return PatchEvolution(self.state, self.params, precision=precision)
 
-    def states(self, evo):
+    def snapshot(self, evo):
         return [evo.state()]
 
     def norms(self, evo):
@@ -184,7 +188,7 @@ class NestedFMR:
         from jax_bssn_gb300.fmr import FMREvolution
         return FMREvolution(self.states, self.parameters, self.hierarchy, self.layouts, precision=precision)
 
-    def states(self, evo):
+    def snapshot(self, evo):
         return list(evo.states())
 
     def norms(self, evo):
@@ -252,7 +256,7 @@ class Axisymmetric:
         from jax_bssn_gb300.cartoon.axisymmetry import AxisymmetricEvolution
         return AxisymmetricEvolution(self.state, self.params, precision=precision)
 
-    def states(self, evo):
+    def snapshot(self, evo):
         return [evo.state()]
 
     def norms(self, evo):
@@ -357,6 +361,20 @@ def _max_over_ranks(ms, world, device):
     return float(t.item())
 
 
+def compute_roofline_of(prof, points, profiled_steps, peak_gflops, precision):
+    """FP64 / FP32 pipe roofline of k_rhs_at: executed flops of its launches in
+    the profiled steps over their summed device time, against the live FMA peak."""
+    if "rhs_at" not in prof or not peak_gflops:
+        return None
+    ms, launches = prof["rhs_at"]
+    flops = RHS_AT_FLOPS_PER_POINT[precision] * points * 4 * profiled_steps
+    achieved = flops / (ms / 1e3) / 1e12
+    peak = peak_gflops / 1e3
+    return {"bound": precision, "kernel": "k_rhs_at", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak, "flops_per_point": RHS_AT_FLOPS_PER_POINT[precision],
+            "peak_source": "measured live by bssn_probe_fma_peak"}
+
+
 def roofline_of(prof, points, profiled_steps, hbm_peak, peak_src, value_per_gpu, precision="fp64"):
     """Live roofline of the dominant kernel class from the per-launch CUDA-event
     accounting: algorithmic bytes of all its launches in the profiled steps
@@ -410,6 +428,8 @@ def run_gb300(args, world, rank, local):
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
     stream = torch.cuda.current_stream()
+    fma_peaks = {"fp64": _native.fma_peak_gflops(_native.PRECISION_F64),
+                 "fp32": _native.fma_peak_gflops(_native.PRECISION_F32)}
 
     def measure(precision):
         """Device-resident throughput of one arithmetic form, its per-kernel
@@ -445,6 +465,7 @@ def run_gb300(args, world, rank, local):
         prof = _native.profile_read()
         lib.bssn_profile_reset()
         roofline = roofline_of(prof, points, profiled_steps, hbm_peak, peak_src, value / world, precision)
+        compute = compute_roofline_of(prof, points, profiled_steps, fma_peaks.get(precision), precision)
         total_prof = sum(v[0] for v in prof.values()) or 1.0
         kernels = {k: {"ms": round(v[0], 3), "launches": v[1], "share": round(v[0] / total_prof, 4)}
                    for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}
@@ -475,14 +496,14 @@ def run_gb300(args, world, rank, local):
             e2e = {"value": world * points * args.steps / (ems / 1e3), "unit": UNIT,
                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d, "ms_per_step": ems / args.steps}
         return {"evo": evo, "value": value, "ms": ms, "launches": launches, "clocks": clock_info,
-                "roofline": roofline, "kernels": kernels, "e2e": e2e}
+                "roofline": roofline, "compute": compute, "kernels": kernels, "e2e": e2e}
 
     plain = measure("fp64")
     chosen = measure("fp32")
     # error of the FP32 form against the FP64 run after the same number of steps,
     # relative to each leaf's deviation from the flat background
     errors = {}
-    for s64, s32 in zip(wl.states(plain["evo"]), wl.states(chosen["evo"])):
+    for s64, s32 in zip(wl.snapshot(plain["evo"]), wl.snapshot(chosen["evo"])):
         for leaf, a, b in zip(LEAVES, s64, s32):
             dev64 = a - background(leaf, a)
             scale = float(torch.max(torch.abs(dev64)))
@@ -495,6 +516,7 @@ def run_gb300(args, world, rank, local):
                       "FP64 state, RK4 combination, projection, W/alpha/1/W and constraints",
         "dtype": "f32 (f64 state)", "value": chosen["value"], "unit": UNIT, "ms_per_step": chosen["ms"] / args.steps,
         "speedup_vs_fp64": chosen["value"] / plain["value"], "roofline": chosen["roofline"],
+        "roofline_compute": chosen["compute"],
         "e2e": chosen["e2e"], "gpu_launches": chosen["launches"], "clocks": chosen["clocks"],
         "kernels": chosen["kernels"],
         "error_vs_fp64": {"metric": "max|fp32 - fp64| / max|fp64 - background| per leaf after "
@@ -518,7 +540,8 @@ def run_gb300(args, world, rank, local):
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (analytic initial data generated on the host)",
         "config": wl.config(), "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-        "gpu_launches": launches, "clocks": clock_info, "kernels": kernel_table, "chosen_form": chosen_form,
+        "gpu_launches": launches, "clocks": clock_info, "kernels": kernel_table,
+        "roofline_compute": plain["compute"], "fma_peaks_gflops": fma_peaks, "chosen_form": chosen_form,
     }
 
 

@@ -250,6 +250,12 @@ int bssn_cartoon_constraints(int32_t axisymmetric, const double* compact, const 
 
 /* ---------------- instrumentation ---------------- */
 
+/* No reference counterpart.  FMA throughput of this GPU in GFLOP/s (FMA = 2
+ * flops) for BSSN_PRECISION_F64 or BSSN_PRECISION_F32: sixteen independent FMA
+ * chains per thread, 8 x 256 threads per SM, one timed launch after a warm-up
+ * (synchronous; the denominator of the RHS kernels' compute roofline). */
+int bssn_probe_fma_peak(int32_t precision, double* gflops);
+
 /* Kernel launches issued by this library since load (all threads). */
 long long bssn_launch_count(void);
 /* Per-kernel-class device-time accounting with CUDA events on each launch's

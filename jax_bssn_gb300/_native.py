@@ -129,6 +129,7 @@ SIGNATURES = {
     "bssn_cartoon_constraints": (ctypes.c_int, [ctypes.c_int32, ctypes.c_void_p, Shape3,
                                                 ctypes.POINTER(BssnParams), ctypes.c_void_p, ctypes.c_void_p,
                                                 ctypes.c_size_t, ctypes.c_void_p]),
+    "bssn_probe_fma_peak": (ctypes.c_int, [ctypes.c_int32, ctypes.POINTER(ctypes.c_double)]),
     "bssn_launch_count": (ctypes.c_longlong, []),
     "bssn_profile_enable": (None, [ctypes.c_int]),
     "bssn_profile_reset": (None, []),
@@ -187,3 +188,11 @@ def check(status: int, what: str) -> None:
     if status in (BSSN_ERR_INVALID, BSSN_ERR_WORKSPACE):
         raise ValueError(message)
     raise RuntimeError(message)
+
+
+def fma_peak_gflops(precision: int) -> float:
+    """Measured FMA throughput (GFLOP/s) of the current GPU, FP64 or FP32."""
+    lib = load()
+    out = ctypes.c_double(0.0)
+    check(lib.bssn_probe_fma_peak(int(precision), ctypes.byref(out)), "bssn_probe_fma_peak")
+    return out.value

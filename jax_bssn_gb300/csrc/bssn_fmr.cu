@@ -130,7 +130,7 @@ static void lagrange6(double frac, double (&w)[6]) {
 }
 
 // Shell enumeration.  The child's guard shell is three dense slabs of
-// (x, y, z-pair) work items: X = guard x planes (all y, all pairs), Y =
+// (x, y, z-pair) work items (one component per grid z slice): X = guard x planes (all y, all pairs), Y =
 // interior x with guard y (all pairs), Z = interior x and y with the guard
 // pairs only.  Within a slab, x and y are enumerated evens first, then odds,
 // and pairs fastest, so a warp shares one (x parity, y parity) class and every
@@ -210,8 +210,8 @@ __global__ void k_fmr_prolong(const double* __restrict__ parent, PatchDims Dp, d
     for (int k = 0; k < 6; ++k) w[k] = W.w[1][k];
     const long long sx = (long long)Dp.P[1] * Dp.P[2];
     const bool fx = frac[0] != 0, fy = frac[1] != 0;
-#pragma unroll 1
-    for (int c = 0; c < NCOMP; ++c) {
+    {
+        const int c = blockIdx.z;   // one component per grid z slice
         const double* f = parent + (long long)c * Dp.cs;
         // x-interpolated value at parent (py, pz)
         auto xval = [&](int py, int pz) -> double {
@@ -284,7 +284,7 @@ cudaError_t launch_fmr_prolong(const double* parent, const PatchDims& Dp, double
     const ShellSlabs S = shell_slabs(Dc);
     long long most = 0;
     for (int k = 0; k < 3; ++k) most = S.count[k] > most ? S.count[k] : most;
-    const dim3 grid(fmr_blocks(most), 3);
+    const dim3 grid(fmr_blocks(most), 3, NCOMP);
     BSSN_LAUNCH(KC_TRANSFER, k_fmr_prolong, grid, kFmrThreads, s, parent, Dp, child, Dc, lo[0], lo[1], lo[2],
                 prolong_weights(), S);
     return cudaGetLastError();
