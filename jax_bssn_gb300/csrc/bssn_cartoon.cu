@@ -112,10 +112,14 @@ struct AxiGeom {
 
 // Write the reconstructed support: point (x, j, z) -> dst at (ox+x, oy+j, oz+z)
 // of a block with strides (sx, sy, 1) and component stride dcs.  One block per
-// (x, j) column and a range of z: the node window, the six weights and the
-// rotation depend on (x, j) alone and are computed once into shared memory;
-// the threads then gather along z (coalesced) and rotate.
+// (x, plane pair) and a range of z.  The planes j and 8 - j (y and -y) share
+// rho, hence the node window, the six weights and every interpolated profile
+// value, and their rotations differ only in the sign of sin(phi): each pair is
+// interpolated once and rotated twice.  The window, weights and rotation are
+// computed once per block into shared memory; the threads then gather along
+// z (coalesced) and rotate.
 constexpr int kAxiThreads = 128;
+constexpr int kAxiPairs = kCenter + 1;   // planes (j, 8 - j) for j = 0..3, and the centre plane
 
 __global__ void __launch_bounds__(kAxiThreads) k_axi_reconstruct(const double* __restrict__ u, Compact C, AxiGeom A,
                                                                  double* __restrict__ dst, long long dcs, long long sx,
@@ -123,8 +127,8 @@ __global__ void __launch_bounds__(kAxiThreads) k_axi_reconstruct(const double* _
     __shared__ double s_w[6];
     __shared__ double s_cs, s_sn;
     __shared__ int s_start, s_valid;
-    const int col = blockIdx.x;            // x * 9 + j
-    const int x = col / kSup, j = col - (col / kSup) * kSup;
+    const int col = blockIdx.x;            // x * kAxiPairs + j
+    const int x = col / kAxiPairs, j = col - (col / kAxiPairs) * kAxiPairs;
     if (threadIdx.x == 0) {
         const double X = RN_MUL((double)x - 3.5, A.dx);
         const double Y = RN_MUL((double)j - 4.0, A.dx);
@@ -162,8 +166,10 @@ __global__ void __launch_bounds__(kAxiThreads) k_axi_reconstruct(const double* _
     }
     const double par3[3] = {-1.0, -1.0, 1.0};
     const double nan = __longlong_as_double(0x7ff8000000000000LL);
-    // six-node sum of component c (reflected plane, then the buffer)
-    auto interp = [&](int c) -> double {
+    // six-node sum of every component (reflected plane, then the buffer)
+    double val[NCOMP];
+#pragma unroll
+    for (int c = 0; c < NCOMP; ++c) {
         const double* f = u + (long long)c * C.cs;
         const double par = comp_parity(c, par3);
         const double asym = comp_asymptote(c);
@@ -177,50 +183,52 @@ __global__ void __launch_bounds__(kAxiThreads) k_axi_reconstruct(const double* _
             else v = RN_ADD(asym, RN_MUL(RN_ADD(f[(long long)(C.nx - 1) * C.nz + z], -asym), ratio[src - C.nx]));
             acc = k == 0 ? RN_MUL(v, w[0]) : RN_ADD(acc, RN_MUL(v, w[k]));
         }
-        return valid ? acc : nan;
-    };
+        val[c] = valid ? acc : nan;
+    }
     // L = R_z(phi) = [[c,-s,0],[s,c,0],[0,0,1]].  Its four literal zeros
     // (L_i2, L_2a for i, a < 2) only add (+-0) T terms to the reference's
     // sums, so they are skipped: the remaining terms keep the reference's
     // order (vector: j ascending; tensor: a-major, b-minor over (L_ia L_jb) T_ab),
     // and the result differs at most in the sign of a zero (or, for a
-    // non-finite input, in not turning 0 * inf into NaN).
-    const double L[3][3] = {{s_cs, -s_sn, 0.0}, {s_sn, s_cs, 0.0}, {0.0, 0.0, 1.0}};
-    const long long d = (long long)(ox + x) * sx + (long long)(oy + j) * sy + (oz + z);
-    dst[(long long)CW * dcs + d] = interp(CW);
-    dst[(long long)CK * dcs + d] = interp(CK);
-    dst[(long long)CALPHA * dcs + d] = interp(CALPHA);
-#pragma unroll 1
-    for (int base = 0; base < 2; ++base) {
-        const int off = base == 0 ? GTX : BX;
-        const double v0 = interp(off), v1 = interp(off + 1), v2 = interp(off + 2);
+    // non-finite input, in not turning 0 * inf into NaN).  The mirrored plane
+    // has y -> -y, so sin(phi) -> -sin(phi) exactly.
+    auto rotate_write = [&](int plane, double sn) {
+        const double L[3][3] = {{s_cs, -sn, 0.0}, {sn, s_cs, 0.0}, {0.0, 0.0, 1.0}};
+        const long long d = (long long)(ox + x) * sx + (long long)(oy + plane) * sy + (oz + z);
+        dst[(long long)CW * dcs + d] = val[CW];
+        dst[(long long)CK * dcs + d] = val[CK];
+        dst[(long long)CALPHA * dcs + d] = val[CALPHA];
 #pragma unroll
-        for (int i = 0; i < 2; ++i) dst[(long long)(off + i) * dcs + d] = RN_ADD(RN_MUL(L[i][0], v0), RN_MUL(L[i][1], v1));
-        dst[(long long)(off + 2) * dcs + d] = v2;
-    }
-#pragma unroll 1
-    for (int base = 0; base < 2; ++base) {
-        const int off = base == 0 ? GXX : AXX;
-        double T6[6];
+        for (int base = 0; base < 2; ++base) {
+            const int off = base == 0 ? GTX : BX;
 #pragma unroll
-        for (int c = 0; c < 6; ++c) T6[c] = interp(off + c);
+            for (int i = 0; i < 2; ++i)
+                dst[(long long)(off + i) * dcs + d] = RN_ADD(RN_MUL(L[i][0], val[off]), RN_MUL(L[i][1], val[off + 1]));
+            dst[(long long)(off + 2) * dcs + d] = val[off + 2];
+        }
 #pragma unroll
-        for (int i = 0; i < 3; ++i)
+        for (int base = 0; base < 2; ++base) {
+            const int off = base == 0 ? GXX : AXX;
 #pragma unroll
-            for (int jj = i; jj < 3; ++jj) {
-                double acc = 0.0;
-                bool first = true;
+            for (int i = 0; i < 3; ++i)
 #pragma unroll
-                for (int ab = 0; ab < 9; ++ab) {
-                    const int a2 = ab / 3, b2 = ab % 3;
-                    if ((i == 2) != (a2 == 2) || (jj == 2) != (b2 == 2)) continue;   // literal zero of L
-                    const double term = RN_MUL(RN_MUL(L[i][a2], L[jj][b2]), T6[sym(a2, b2)]);
-                    acc = first ? term : RN_ADD(acc, term);
-                    first = false;
+                for (int jj = i; jj < 3; ++jj) {
+                    double acc = 0.0;
+                    bool first = true;
+#pragma unroll
+                    for (int ab = 0; ab < 9; ++ab) {
+                        const int a2 = ab / 3, b2 = ab % 3;
+                        if ((i == 2) != (a2 == 2) || (jj == 2) != (b2 == 2)) continue;   // literal zero of L
+                        const double term = RN_MUL(RN_MUL(L[i][a2], L[jj][b2]), val[off + sym(a2, b2)]);
+                        acc = first ? term : RN_ADD(acc, term);
+                        first = false;
+                    }
+                    dst[(long long)(off + sym(i, jj)) * dcs + d] = acc;
                 }
-                dst[(long long)(off + sym(i, jj)) * dcs + d] = acc;
-            }
-    }
+        }
+    };
+    rotate_write(j, s_sn);
+    if (j != kCenter) rotate_write(kSup - 1 - j, -s_sn);
 }
 
 // ---------------------------------------------------------------------------
@@ -472,7 +480,7 @@ cudaError_t reconstruct(const CartoonPlan& P, const BssnParams* p, const double*
     const long long sx = P.Gs.st[0], sy = P.Gs.st[1];
     if (P.axi) {
         const AxiGeom A{p->dx, p->xmin[2]};
-        const dim3 grid((unsigned)(P.C.nx * kSup), (unsigned)((P.C.nz + kAxiThreads - 1) / kAxiThreads));
+        const dim3 grid((unsigned)(P.C.nx * kAxiPairs), (unsigned)((P.C.nz + kAxiThreads - 1) / kAxiThreads));
         BSSN_LAUNCH(KC_CARTOON, k_axi_reconstruct, grid, kAxiThreads, s, u, P.C, A, us, P.scs, sx, sy, 4, 4, 4);
     } else {
         const long long n = (long long)P.C.nx * kSup * kSup;
@@ -572,7 +580,7 @@ int bssn_cartoon_reconstruct(int32_t axisymmetric, const double* compact, double
     if (P.axi) {
         const AxiGeom A{params->dx, params->xmin[2]};
         const long long dcs = (long long)P.C.nx * kSup * P.C.nz;
-        const dim3 grid((unsigned)(P.C.nx * kSup), (unsigned)((P.C.nz + kAxiThreads - 1) / kAxiThreads));
+        const dim3 grid((unsigned)(P.C.nx * kAxiPairs), (unsigned)((P.C.nz + kAxiThreads - 1) / kAxiThreads));
         BSSN_LAUNCH(KC_CARTOON, k_axi_reconstruct, grid, kAxiThreads, s, compact, P.C, A, support, dcs,
                     (long long)kSup * P.C.nz, (long long)P.C.nz, 0, 0, 0);
     } else {
