@@ -93,6 +93,7 @@ typedef struct BssnMatter {
 #define BSSN_OP_RHS 1
 #define BSSN_OP_RK4 2
 #define BSSN_OP_CONSTRAINTS 3
+#define BSSN_OP_RHS_MATTER 4   /* bssn_rhs with matter sources */
 
 const char* bssn_last_error(void);
 int bssn_abi_version(void);
@@ -101,8 +102,9 @@ int bssn_abi_version(void);
 size_t bssn_workspace_bytes(int op, const int32_t shape[3], const BssnParams* params);
 
 /* compute_bssn_rhs(vars, params) -> rhs (JAX_BSSN/evolution/time_evolve.py:41-57),
- * and compute_bssn_rhs_with_matter (time_evolve.py:60-91) when matter is non-null
- * (not yet supported: returns BSSN_ERR_INVALID).  Like the reference, the RHS is
+ * and compute_bssn_rhs_with_matter (time_evolve.py:60-91) when matter holds the
+ * three source arrays (workspace: bssn_workspace_bytes(BSSN_OP_RHS_MATTER); S_ij is
+ * read from its upper triangle, a symmetric stress).  Like the reference, the RHS is
  * evaluated at every sample of the array, with periodic wrap across the array
  * extent and face closures/Sommerfeld replacement on the owned range given by
  * guard_cells/owned_shape. */

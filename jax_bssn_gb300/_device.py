@@ -91,14 +91,16 @@ def spatial_shape(state) -> tuple[int, int, int]:
     return shape
 
 
-def _as_device(leaf, shape, device) -> torch.Tensor:
+def as_device(leaf, shape, device, name: str = "field") -> torch.Tensor:
+    """A contiguous float64 CUDA tensor of the given shape (host arrays are copied in)."""
     if isinstance(leaf, torch.Tensor):
         t = leaf.to(device=device, dtype=torch.float64)
     else:
         t = torch.as_tensor(np.asarray(leaf, dtype=np.float64), device=device)
-    if tuple(t.shape) != shape:
-        raise ValueError(f"field has shape {tuple(t.shape)}; expected {shape}")
+    if tuple(t.shape) != tuple(shape):
+        raise ValueError(f"{name} has shape {tuple(t.shape)}; expected {tuple(shape)}")
     return t.contiguous()
+
 
 
 def device_state(state) -> tuple[BSSNVariables, bool]:
@@ -107,7 +109,7 @@ def device_state(state) -> tuple[BSSNVariables, bool]:
     device = require_cuda()
     shape = spatial_shape(state)
     host = not isinstance(state.conformal_factor, torch.Tensor) or not state.conformal_factor.is_cuda
-    leaves = tuple(_as_device(leaf, lead + shape, device) for leaf, lead in zip(state, LEAF_SHAPES))
+    leaves = tuple(as_device(leaf, lead + shape, device) for leaf, lead in zip(state, LEAF_SHAPES))
     return BSSNVariables(*leaves), host
 
 

@@ -31,6 +31,7 @@ PRECISION_F32 = 1
 OP_RHS = 1
 OP_RK4 = 2
 OP_CONSTRAINTS = 3
+OP_RHS_MATTER = 4
 
 
 class BssnParams(ctypes.Structure):

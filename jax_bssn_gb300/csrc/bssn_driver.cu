@@ -224,6 +224,30 @@ __global__ void k_export(const double* __restrict__ u, LeavesOut out, Geo G, Box
     }
 }
 
+// Matter sources in the reference layout -> a padded block of kMatterComps
+// components: rho, S_x, S_y, S_z, then the upper triangle of S_ij.
+__global__ void k_import_matter(const double* __restrict__ rho, const double* __restrict__ Si,
+                                const double* __restrict__ Sij, double* __restrict__ m, Geo G, Box region,
+                                long long npts) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= region.count * kMatterComps) return;
+    const int comp = (int)(t / region.count);
+    const long long r = t - (long long)comp * region.count;
+    int ix[3];
+    region.coords(r, ix);
+    double v;
+    if (comp == 0) {
+        v = rho[r];
+    } else if (comp < 4) {
+        v = Si[(comp - 1) * npts + r];
+    } else {
+        constexpr int ij[6][2] = {{0, 0}, {0, 1}, {0, 2}, {1, 1}, {1, 2}, {2, 2}};
+        const int s = comp - 4;
+        v = Sij[(3 * ij[s][0] + ij[s][1]) * npts + r];
+    }
+    m[comp * G.cs + lin(G, ix)] = v;
+}
+
 // Periodic wrap of the array region [lo, lo+n) into every other padded sample
 // (np.roll semantics of the reference on an unpadded array, and the self-wrap
 // of a single tile, JAX_BSSN/parallel/communication.py:45-52).
@@ -502,8 +526,13 @@ LeavesOut leaves_out(BssnFields* f) {
 
 size_t ref_workspace_values(int op, const RefLayout& L, bool with_mom) {
     if (op == BSSN_OP_CONSTRAINTS) return (size_t)(NCOMP + 3 * NMIX + 24) * (size_t)L.cs;
-    const size_t blocks = (op == BSSN_OP_RK4 ? 4 * NCOMP : 2 * NCOMP) + rhs_work_blocks(with_mom);
+    size_t blocks = (op == BSSN_OP_RK4 ? 4 * NCOMP : 2 * NCOMP) + rhs_work_blocks(with_mom);
+    if (op == BSSN_OP_RHS_MATTER) blocks += kMatterComps;
     return blocks * (size_t)L.cs;
+}
+
+bool matter_given(const BssnMatter* m) {
+    return m && (m->energy_density || m->momentum_density || m->spatial_stress);
 }
 
 }  // namespace
@@ -524,8 +553,9 @@ size_t bssn_workspace_bytes(int op, const int32_t shape[3], const BssnParams* pa
 int bssn_rhs(const BssnFields* in, BssnFields* out, const int32_t shape[3], const BssnParams* params,
              const BssnMatter* matter, void* workspace, size_t workspace_bytes, void* stream) {
     if (!fields_ok(in) || !fields_ok(out)) return fail(BSSN_ERR_INVALID, "null field pointer");
-    if (matter && (matter->energy_density || matter->momentum_density || matter->spatial_stress))
-        return fail(BSSN_ERR_INVALID, "matter sources are not supported by this build");
+    const bool with_matter = matter_given(matter);
+    if (with_matter && !(matter->energy_density && matter->momentum_density && matter->spatial_stress))
+        return fail(BSSN_ERR_INVALID, "matter sources need energy_density, momentum_density and spatial_stress");
     int st = validate_params(params);
     if (st) return st;
     RefLayout L;
@@ -533,8 +563,11 @@ int bssn_rhs(const BssnFields* in, BssnFields* out, const int32_t shape[3], cons
     Geo G;
     if ((st = make_geo(params, L.S, L.org, L.P, G))) return st;
     const bool with_mom = params->kappa != 0.0;
-    if (!workspace || workspace_bytes < ref_workspace_values(BSSN_OP_RHS, L, with_mom) * sizeof(double))
-        return fail(BSSN_ERR_WORKSPACE, "workspace missing or smaller than bssn_workspace_bytes(BSSN_OP_RHS)");
+    const int op = with_matter ? BSSN_OP_RHS_MATTER : BSSN_OP_RHS;
+    if (!workspace || workspace_bytes < ref_workspace_values(op, L, with_mom) * sizeof(double))
+        return fail(BSSN_ERR_WORKSPACE, with_matter
+                    ? "workspace missing or smaller than bssn_workspace_bytes(BSSN_OP_RHS_MATTER)"
+                    : "workspace missing or smaller than bssn_workspace_bytes(BSSN_OP_RHS)");
     cudaStream_t s = (cudaStream_t)stream;
     double* u = (double*)workspace;
     double* k = u + NCOMP * L.cs;
@@ -542,6 +575,13 @@ int bssn_rhs(const BssnFields* in, BssnFields* out, const int32_t shape[3], cons
     const Box region = box_of(G);
     BSSN_LAUNCH(KC_IMPORT, k_import, nblocks(region.count * NCOMP), kThreads, s, leaves_in(in), u, G, region, L.npts);
     cudaError_t e = launch_fill_periodic(u, NCOMP, G, s);
+    if (e == cudaSuccess && with_matter) {
+        double* m = k + (long long)(NCOMP + rhs_work_blocks(with_mom)) * L.cs;
+        BSSN_LAUNCH(KC_IMPORT, k_import_matter, nblocks(region.count * kMatterComps), kThreads, s,
+                    matter->energy_density, matter->momentum_density, matter->spatial_stress, m, G, region, L.npts);
+        e = launch_fill_periodic(m, kMatterComps, G, s);
+        w.mat = m;
+    }
     if (e == cudaSuccess) e = launch_rhs(u, k, w, G, region, s);
     if (e == cudaSuccess) {
         BSSN_LAUNCH(KC_EXPORT, k_export, nblocks(region.count * NCOMP), kThreads, s, k, leaves_out(out), G, region, L.npts);

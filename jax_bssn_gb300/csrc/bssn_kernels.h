@@ -19,7 +19,12 @@ struct RhsWork {
     float* d1f = nullptr;    // first derivatives
     float* derf = nullptr;   // derived fields (kappa != 0)
     float* dampf = nullptr;  // damping term (kappa != 0)
+    // Matter sources (null: vacuum): kMatterComps padded blocks -- rho, S_i,
+    // upper triangle of S_ij -- in the state's geometry.
+    const double* mat = nullptr;
 };
+
+constexpr int kMatterComps = 10;
 
 size_t rhs_work_blocks(bool with_mom);
 RhsWork carve_rhs_work(double* base, long long cs, bool with_mom);

@@ -39,6 +39,7 @@
 namespace bssn {
 
 constexpr int kThreads = 128;
+constexpr double kPi = 3.141592653589793;   // the double nearest pi (numpy.pi)
 
 template <typename R>
 constexpr bool kPerturbative = std::is_same<R, float>::value;
@@ -355,7 +356,7 @@ k_rhs_gauge(const R* __restrict__ u, const double* __restrict__ u64, const R* __
 template <typename R, bool Closed>
 __global__ void __launch_bounds__(kThreads)
 k_rhs_kgt(const R* __restrict__ u, const double* __restrict__ u64, const R* __restrict__ d1,
-          double* __restrict__ k, Geo G, BoxSet S, int nfield) {
+          const double* __restrict__ mat, double* __restrict__ k, Geo G, BoxSet S, int nfield) {
     PointCtx c;
     if (!point(S.b[blockIdx.y], c, G)) return;
     const long long cs = G.cs, p = c.p;
@@ -402,7 +403,19 @@ k_rhs_kgt(const R* __restrict__ u, const double* __restrict__ u64, const R* __re
         const R second = alpha * contract_sym(A, Au);
         const R third = alpha * (K * K) / R(3.0);
         const R* f = u + CK * cs + p;
-        k[CK * cs + p] = first + second + third + ADV<R, Closed>(f, G, c.ix, beta) + KO<R, Closed>(f, G, c.ix);
+        R bulk = first + second + third + ADV<R, Closed>(f, G, c.ix, beta);
+        if (mat != nullptr) {
+            // + 4 pi alpha (rho + W^2 gt^ij S_ij) (extrinsic_curvature.py:78-87)
+            const R wf = static_cast<R>(fmax(u64[CW * cs + p], 1.0e-12));
+            const R wf2 = wf * wf;
+            R trace = R(0);
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) trace += (wf2 * gi[sym(i, j)]) * static_cast<R>(mat[(4 + sym(i, j)) * cs + p]);
+            bulk = bulk + R(4.0 * kPi) * alpha * (static_cast<R>(mat[p]) + trace);
+        }
+        k[CK * cs + p] = bulk + KO<R, Closed>(f, G, c.ix);
     }
 
     // dt Gt^i
@@ -444,7 +457,15 @@ k_rhs_kgt(const R* __restrict__ u, const double* __restrict__ u64, const R* __re
         const R v = R(-4.0 / 3.0) * alpha * t1 + R(2.0) * alpha * t2 + six_alpha_over_w * t3
                     - R(2.0) * t4 + ADV<R, Closed>(f, G, c.ix, beta) + R(2.0 / 3.0) * Gt[i] * div - t7 + t8
                     + R(1.0 / 3.0) * t9;
-        k[(GTX + i) * cs + p] = v + KO<R, Closed>(f, G, c.ix);
+        R out = v + KO<R, Closed>(f, G, c.ix);
+        if (mat != nullptr) {
+            // - 16 pi alpha gt^ij S_j (conformal_connection.py:166-178)
+            R gs = R(0);
+#pragma unroll
+            for (int j = 0; j < 3; ++j) gs += gi[sym(i, j)] * static_cast<R>(mat[(1 + j) * cs + p]);
+            out = out + R(-16.0 * kPi) * alpha * gs;
+        }
+        k[(GTX + i) * cs + p] = out;
     }
 }
 
@@ -454,7 +475,8 @@ k_rhs_kgt(const R* __restrict__ u, const double* __restrict__ u64, const R* __re
 template <typename R, bool Closed>
 __global__ void __launch_bounds__(kThreads)
 k_rhs_at(const R* __restrict__ u, const double* __restrict__ u64, const R* __restrict__ d1,
-         const R* __restrict__ damp, double* __restrict__ k, Geo G, BoxSet S, int nfield) {
+         const R* __restrict__ damp, const double* __restrict__ mat, double* __restrict__ k, Geo G, BoxSet S,
+         int nfield) {
     PointCtx c;
     if (!point(S.b[blockIdx.y], c, G)) return;
     const long long cs = G.cs, p = c.p;
@@ -485,6 +507,13 @@ k_rhs_at(const R* __restrict__ u, const double* __restrict__ u64, const R* __res
         w2_lapse_hessian<R, Closed>(u, d1, G, nfield, c, g, gi, c2, dW, da, W, h);
 #pragma unroll
         for (int s = 0; s < 6; ++s) T[s] = alpha * w2r[s] - h[s];
+        if (mat != nullptr) {
+            // - 8 pi alpha W^2 S_ij before the trace-free part (extrinsic_curvature.py:164-175)
+            const R wf = static_cast<R>(fmax(u64[CW * cs + p], 1.0e-12));
+            const R coef = R(8.0 * kPi) * alpha * (wf * wf);
+#pragma unroll
+            for (int s = 0; s < 6; ++s) T[s] = T[s] - coef * static_cast<R>(mat[(4 + s) * cs + p]);
+        }
         const R tr = contract_sym(gi, T);
 #pragma unroll
         for (int s = 0; s < 6; ++s) T[s] = T[s] - R(1.0 / 3.0) * g[s] * tr;
@@ -557,7 +586,8 @@ k_mom_derived(const R* __restrict__ u, const double* __restrict__ u64, R* __rest
 template <typename R, bool Closed>
 __global__ void __launch_bounds__(kThreads)
 k_mom_damping(const R* __restrict__ u, const double* __restrict__ u64, const R* __restrict__ der,
-              const R* __restrict__ d1, R* __restrict__ damp, Geo G, BoxSet S, int nfield) {
+              const R* __restrict__ d1, const double* __restrict__ mat, R* __restrict__ damp, Geo G, BoxSet S,
+              int nfield) {
     PointCtx c;
     if (!point(S.b[blockIdx.y], c, G)) return;
     const long long cs = G.cs, p = c.p;
@@ -624,6 +654,17 @@ k_mom_damping(const R* __restrict__ u, const double* __restrict__ u64, const R* 
             }
             const R d2K = (l == i) ? D2<R, Closed>(u + CK * cs + p, G, l, c.ix[l]) : mixed<R, Closed>(d1, G, nfield, fK, l, i, c);
             dM[i][l] = divd - R(0.5) * met - R(0.5) * met2 - R(3.0) * conf - R(2.0 / 3.0) * d2K;
+        }
+    }
+    if (mat != nullptr) {
+        // matter momentum: M_i - 8 pi S_i, d_l M_i - 8 pi d_l S_i (constraints.py:233-259)
+#pragma unroll 1
+        for (int i = 0; i < 3; ++i) {
+            const double* Sp = mat + (1 + i) * cs + p;
+            M[i] = M[i] - R(8.0 * kPi) * static_cast<R>(Sp[0]);
+#pragma unroll 1
+            for (int l = 0; l < 3; ++l)
+                dM[i][l] = dM[i][l] - R(8.0 * kPi) * static_cast<R>(D1<double, Closed>(Sp, G, l, c.ix[l]));
         }
     }
     // Christoffels for D_j M_i = d_j M_i - Gamma^k_ij M_k
@@ -901,8 +942,8 @@ cudaError_t launch_constraints(const double* u, const RhsWork& w, const Geo& G, 
 // the shell slabs
 // ---------------------------------------------------------------------------
 template <typename R>
-static void launch_rhs_form(const R* u, const double* u64, double* k, R* d1, R* der, R* damp, const Geo& G,
-                            const Box& box, cudaStream_t stream) {
+static void launch_rhs_form(const R* u, const double* u64, double* k, R* d1, R* der, R* damp, const double* mat,
+                            const Geo& G, const Box& box, cudaStream_t stream) {
     const int with_mom = G.kappa != 0.0;
     const int nfield = with_mom ? NMIX + NMIX_MOM : NMIX;
     const int reach = composition_reach(G);
@@ -921,17 +962,18 @@ static void launch_rhs_form(const R* u, const double* u64, double* k, R* d1, R* 
     const SplitBox sb = split_box(G, box);
     const R* dmp = with_mom ? static_cast<const R*>(damp) : nullptr;
     if (with_mom) {
-        BSSN_LAUNCH_SET(KC_MOM_DAMP, (k_mom_damping<R, false>), sb.interior, stream, u, u64, der, d1, damp, G,
+        BSSN_LAUNCH_SET(KC_MOM_DAMP, (k_mom_damping<R, false>), sb.interior, stream, u, u64, der, d1, mat, damp, G,
                         sb.interior, nfield);
-        BSSN_LAUNCH_SET(KC_MOM_DAMP, (k_mom_damping<R, true>), sb.shell, stream, u, u64, der, d1, damp, G, sb.shell,
-                        nfield);
+        BSSN_LAUNCH_SET(KC_MOM_DAMP, (k_mom_damping<R, true>), sb.shell, stream, u, u64, der, d1, mat, damp, G,
+                        sb.shell, nfield);
     }
     BSSN_LAUNCH_SET(KC_GAUGE, (k_rhs_gauge<R, false>), sb.interior, stream, u, u64, d1, k, G, sb.interior, nfield);
     BSSN_LAUNCH_SET(KC_GAUGE, (k_rhs_gauge<R, true>), sb.shell, stream, u, u64, d1, k, G, sb.shell, nfield);
-    BSSN_LAUNCH_SET(KC_KGT, (k_rhs_kgt<R, false>), sb.interior, stream, u, u64, d1, k, G, sb.interior, nfield);
-    BSSN_LAUNCH_SET(KC_KGT, (k_rhs_kgt<R, true>), sb.shell, stream, u, u64, d1, k, G, sb.shell, nfield);
-    BSSN_LAUNCH_SET(KC_AT, (k_rhs_at<R, false>), sb.interior, stream, u, u64, d1, dmp, k, G, sb.interior, nfield);
-    BSSN_LAUNCH_SET(KC_AT, (k_rhs_at<R, true>), sb.shell, stream, u, u64, d1, dmp, k, G, sb.shell, nfield);
+    BSSN_LAUNCH_SET(KC_KGT, (k_rhs_kgt<R, false>), sb.interior, stream, u, u64, d1, mat, k, G, sb.interior, nfield);
+    BSSN_LAUNCH_SET(KC_KGT, (k_rhs_kgt<R, true>), sb.shell, stream, u, u64, d1, mat, k, G, sb.shell, nfield);
+    BSSN_LAUNCH_SET(KC_AT, (k_rhs_at<R, false>), sb.interior, stream, u, u64, d1, dmp, mat, k, G, sb.interior,
+                    nfield);
+    BSSN_LAUNCH_SET(KC_AT, (k_rhs_at<R, true>), sb.shell, stream, u, u64, d1, dmp, mat, k, G, sb.shell, nfield);
     if (G.any_sommerfeld) {
         const BoxSet S = face_slabs(G, box);
         BSSN_LAUNCH_SET(KC_SOMMERFELD, k_sommerfeld<R>, S, stream, u, k, G, S);
@@ -946,9 +988,9 @@ cudaError_t launch_rhs(const double* u, double* k, const RhsWork& w, const Geo& 
         // upwind stencils reach 4.
         const Box region = grown_box(box, G, 6);
         BSSN_LAUNCH(KC_CONVERT, k_perturb, blocks_for(region.count), kThreads, stream, u, w.uf, G, region);
-        launch_rhs_form<float>(w.uf, u, k, w.d1f, w.derf, w.dampf, G, box, stream);
+        launch_rhs_form<float>(w.uf, u, k, w.d1f, w.derf, w.dampf, w.mat, G, box, stream);
     } else {
-        launch_rhs_form<double>(u, u, k, w.d1, w.der, w.damp, G, box, stream);
+        launch_rhs_form<double>(u, u, k, w.d1, w.der, w.damp, w.mat, G, box, stream);
     }
     return cudaGetLastError();
 }

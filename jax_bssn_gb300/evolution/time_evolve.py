@@ -18,24 +18,49 @@ def _finish(result, host):
     return _device.to_host(result) if host else result
 
 
-def compute_bssn_rhs(vars: BSSNVariables, params: BSSNParameters) -> BSSNVariables:
-    """Bulk BSSN RHS with active Sommerfeld faces (time_evolve.py:41-57)."""
+def _rhs(vars, params, sources, what):
     lib = _native.load()
     state, host = _device.device_state(vars)
     shape = _device.spatial_shape(state)
+    device = state.lapse.device
     p = _device.to_params(params)
-    out = _device.empty_state(shape, state.lapse.device)
-    nbytes = lib.bssn_workspace_bytes(_native.OP_RHS, _device.shape3(shape), p)
-    ws = _device.workspace(nbytes, state.lapse.device)
+    out = _device.empty_state(shape, device)
+    matter = None
+    op = _native.OP_RHS
+    if sources is not None:
+        leads = ((), (3,), (3, 3))
+        names = ("energy_density", "momentum_density", "spatial_stress")
+        tensors = []
+        for value, lead, name in zip(sources, leads, names):
+            if value is None:
+                raise ValueError(f"{name} is required for the matter-coupled RHS")
+            tensors.append(_device.as_device(value, lead + shape, device, name))
+        matter = _native.BssnMatter(*(t.data_ptr() for t in tensors))
+        op = _native.OP_RHS_MATTER
+    nbytes = lib.bssn_workspace_bytes(op, _device.shape3(shape), p)
+    ws = _device.workspace(nbytes, device)
     fin, fout = _device.fields_struct(state), _device.fields_struct(out)
-    _native.check(lib.bssn_rhs(fin, fout, _device.shape3(shape), p, None, ws.data_ptr(), ws.numel(),
-                               _device.stream_handle()), "compute_bssn_rhs")
+    _native.check(lib.bssn_rhs(fin, fout, _device.shape3(shape), p, matter, ws.data_ptr(), ws.numel(),
+                               _device.stream_handle()), what)
     return _finish(out, host)
 
 
-def compute_bssn_rhs_with_matter(vars, params, energy_density, momentum_density, spatial_stress):
-    """Matter-coupled RHS (time_evolve.py:60-91): not provided by this build."""
-    raise NotImplementedError("matter-coupled BSSN RHS is not provided by the GB300 kernels yet")
+def compute_bssn_rhs(vars: BSSNVariables, params: BSSNParameters) -> BSSNVariables:
+    """Bulk BSSN RHS with active Sommerfeld faces (time_evolve.py:41-57)."""
+    return _rhs(vars, params, None, "compute_bssn_rhs")
+
+
+def compute_bssn_rhs_with_matter(vars: BSSNVariables, params: BSSNParameters, energy_density, momentum_density,
+                                 spatial_stress) -> BSSNVariables:
+    """BSSN RHS with Eulerian matter sources (time_evolve.py:60-91).
+
+    Layouts ``rho[nx, ny, nz]``, ``S_i[3, nx, ny, nz]``, ``S_ij[3, 3, nx, ny, nz]``
+    (read from its upper triangle: a symmetric stress).  Sources enter the
+    bulk equations -- +4 pi alpha (rho + S) in dt K, -8 pi alpha W^2 S_ij inside
+    the trace-free part of dt At, -16 pi alpha gt^ij S_j in dt Gt^i and, with
+    kappa != 0, the matter momentum in the damping term -- before the active
+    Sommerfeld faces are imposed."""
+    return _rhs(vars, params, (energy_density, momentum_density, spatial_stress), "compute_bssn_rhs_with_matter")
 
 
 def enforce_algebraic_constraints(vars: BSSNVariables) -> BSSNVariables:

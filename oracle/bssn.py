@@ -230,28 +230,50 @@ def rhs_conformal_factor(geo):
     return out + kreiss_oliger(W, geo.p)
 
 
-def rhs_trace_K(geo, hessian_alpha):
+def rhs_trace_K(geo, hessian_alpha, matter=None):
     alpha, K, A, ginv = geo.alpha, geo.K, geo.A, geo.ginv
     out = (-E('ij...,ij...->...', ginv, hessian_alpha)
            + alpha * E('ij...,kl...,ik...,jl...->...', ginv, ginv, A, A)
            + alpha * K ** 2 / 3.0 + geo.advect(K))
+    if matter is not None:
+        # + 4 pi alpha (rho + W^2 gt^ij S_ij) (extrinsic_curvature.py:78-87)
+        rho, _, S = matter
+        Wf = np.maximum(geo.W, W_FLOOR)
+        stress_trace = E('ij...,ij...->...', Wf ** 2 * ginv, S)
+        out = out + 4.0 * np.pi * alpha * (rho + stress_trace)
     return out + kreiss_oliger(K, geo.p)
 
 
-def rhs_traceless_A(geo, hessian_alpha):
+def rhs_traceless_A(geo, hessian_alpha, matter=None):
     p, alpha, K, A, g, ginv = geo.p, geo.alpha, geo.K, geo.A, geo.g, geo.ginv
     first = alpha * K * A
     second = -2 * alpha * E('ik...,kl...,lj...->ij...', A, ginv, A)
-    third = trace_free(alpha * w2_ricci(geo) - hessian_alpha, g, ginv)
+    source = alpha * w2_ricci(geo) - hessian_alpha
+    if matter is not None:
+        # - 8 pi alpha W^2 S_ij inside the trace-free part (extrinsic_curvature.py:164-175)
+        Wf = np.maximum(geo.W, W_FLOOR)
+        source = source - 8.0 * np.pi * alpha * Wf ** 2 * matter[2]
+    third = trace_free(source, g, ginv)
     fourth = geo.advect(A)
     fifth = E('mi...,mj...->ij...', A, geo.dbeta) + E('mj...,mi...->ij...', A, geo.dbeta)
     sixth = -2.0 / 3.0 * A * geo.div_beta
     out = first + second + third + fourth + fifth + sixth
     if p.kappa != 0:
         M, dM = momentum_constraint_derivative(geo)
+        if matter is not None:
+            # M_i - 8 pi S_i and its derivative (constraints.py:233-259)
+            S_i = matter[1]
+            dS = np.stack([np.stack([D1(S_i[i], l, p) for l in range(3)]) for i in range(3)])
+            M = M - 8.0 * np.pi * S_i
+            dM = dM - 8.0 * np.pi * dS
         DjMi = dM - E('kij...,k...->ij...', geo.chr2, M)
         out = out + p.kappa / 2 * alpha * (DjMi + np.swapaxes(DjMi, 0, 1))
     return out + kreiss_oliger(A, p)
+
+
+def rhs_conformal_connection_with_matter(geo, matter):
+    """Vacuum RHS - 16 pi alpha gt^ij S_j (conformal_connection.py:166-178)."""
+    return rhs_conformal_connection(geo) + -16.0 * np.pi * geo.alpha * E('ij...,j...->i...', geo.ginv, matter[1])
 
 
 def rhs_conformal_connection(geo):
@@ -354,15 +376,21 @@ def apply_sommerfeld(v, rhs, p):
 # assembly, projection and RK4 (time_evolve.py)
 # ----------------------------------------------------------------------------
 
-def compute_rhs(v, p):
+def compute_rhs(v, p, matter=None):
+    """compute_bssn_rhs (time_evolve.py:41-57); with matter = (rho, S_i, S_ij),
+    compute_bssn_rhs_with_matter (time_evolve.py:60-91): sources enter the bulk
+    equations before the Sommerfeld faces are imposed."""
     geo = Geometry(v, p)
     hessian_alpha = w2_lapse_hessian(geo)
+    if matter is not None:
+        matter = tuple(np.asarray(m) for m in matter)
     rhs = BSSNVariables(
         conformal_metric=rhs_conformal_metric(geo),
         conformal_factor=rhs_conformal_factor(geo),
-        traceless_K=rhs_traceless_A(geo, hessian_alpha),
-        trace_K=rhs_trace_K(geo, hessian_alpha),
-        conformal_connection=rhs_conformal_connection(geo),
+        traceless_K=rhs_traceless_A(geo, hessian_alpha, matter),
+        trace_K=rhs_trace_K(geo, hessian_alpha, matter),
+        conformal_connection=(rhs_conformal_connection(geo) if matter is None
+                              else rhs_conformal_connection_with_matter(geo, matter)),
         lapse=rhs_lapse(geo),
         shift=rhs_shift(geo),
     )

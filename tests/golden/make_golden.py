@@ -264,6 +264,44 @@ def cartoon_cases():
     return {"axisymmetric": (axi, axi_params), "spherical": (sph, sph_params)}
 
 
+def matter_fields(shape, seed):
+    """Smooth seeded matter sources rho (n), S_i (3, n), symmetric S_ij (3, 3, n)."""
+    rng = np.random.default_rng(seed)
+    axes = [np.linspace(0.0, 2.0 * np.pi, n, endpoint=False) for n in shape]
+    X, Y, Z = np.meshgrid(*axes, indexing="ij")
+
+    def field(amp):
+        c = rng.normal(size=6)
+        return amp * (c[0] * np.sin(X + c[1]) + c[2] * np.cos(2.0 * Y + c[3]) + c[4] * np.sin(Z + X + c[5]))
+
+    rho = 0.02 + field(0.01) ** 2
+    S_i = np.stack([field(0.01) for _ in range(3)])
+    S_ij = np.zeros((3, 3) + tuple(shape))
+    for i in range(3):
+        for j in range(i, 3):
+            S_ij[i, j] = S_ij[j, i] = (0.01 if i == j else 0.0) + field(0.005)
+    return rho, S_i, S_ij
+
+
+def make_matter(out_dir: Path):
+    """compute_bssn_rhs_with_matter (time_evolve.py:60-91) on three RHS cases:
+    kappa != 0 (momentum-constraint damping with the matter momentum), Sommerfeld
+    faces, and MAD weights."""
+    from JAX_BSSN.evolution.time_evolve import compute_bssn_rhs_with_matter
+    cases = rhs_cases()
+    for name, seed in (("generic_kappa", 71), ("sommerfeld", 72), ("mad_mixed", 73)):
+        state, params = cases[name]
+        shape = np.asarray(state.conformal_factor).shape
+        rho, S_i, S_ij = matter_fields(shape, seed)
+        data = {"params": np.asarray(_params_json(params))}
+        data.update(_state_arrays("input", state))
+        data["matter.energy_density"] = rho
+        data["matter.momentum_density"] = S_i
+        data["matter.spatial_stress"] = S_ij
+        data.update(_state_arrays("rhs", compute_bssn_rhs_with_matter(state, params, rho, S_i, S_ij)))
+        np.savez_compressed(out_dir / f"matter_{name}.npz", **data)
+
+
 def make_cartoon(out_dir: Path):
     from JAX_BSSN.cartoon.axisymmetry import (axisymmetric_rk4_step, compute_axisymmetric_rhs,
                                               compute_axisymmetric_constraints, reconstruct_axisymmetric_support,
@@ -314,6 +352,7 @@ def main(argv):
     only = [part for a in argv if a.startswith("--only=") for part in a.split("=", 1)[1].split(",")]
     parts = {"stencils": lambda: make_stencils(HERE / "stencils.npz"), "rhs": lambda: make_rhs(HERE),
              "fmr": lambda: make_fmr(HERE), "cartoon": lambda: make_cartoon(HERE),
+             "matter": lambda: make_matter(HERE),
              "long": lambda: make_long_runs(HERE)}
     for name, build in parts.items():
         if only and name not in only:

@@ -100,3 +100,21 @@ def test_long_run_first_step_matches_reference(name):
     params = golden_params(data, BSSNParameters)
     one = ob.rk4_step(state, params)
     assert worst(field_errors(one, golden_state(data, "rk4_1", BSSNVariables))) == 0.0
+
+
+MATTER_CASES = ("generic_kappa", "sommerfeld", "mad_mixed")
+
+
+def matter_of(data):
+    return (data["matter.energy_density"], data["matter.momentum_density"], data["matter.spatial_stress"])
+
+
+@pytest.mark.parametrize("name", MATTER_CASES)
+def test_rhs_with_matter_matches_reference(name):
+    """compute_bssn_rhs_with_matter (time_evolve.py:60-91): kappa damping with the
+    matter momentum, Sommerfeld faces after the sources, MAD weights."""
+    data = load_golden(f"matter_{name}")
+    state = golden_state(data, "input", BSSNVariables)
+    params = golden_params(data, BSSNParameters)
+    rhs = ob.compute_rhs(state, params, matter_of(data))
+    assert worst(field_errors(rhs, golden_state(data, "rhs", BSSNVariables))) == 0.0
