@@ -105,6 +105,9 @@ int make_geo(const BssnParams* p, const int S[3], const int org[3], const int P[
     G.inv_dx2 = 1.0 / (dx * dx);
     G.inv_dx6h5 = std::pow(dx, 5.0) / std::pow(dx, 6.0);
     G.nu64 = p->nu / 64.0;
+    G.d1a = (2.0 / 3.0) * G.inv_dx;
+    G.d1b = (-1.0 / 12.0) * G.inv_dx;
+    G.ko_scale = G.nu64 * G.inv_dx6h5;
     G.eta = p->eta;
     G.kappa = p->kappa;
     G.g = p->g;
@@ -121,6 +124,9 @@ int make_geo(const BssnParams* p, const int S[3], const int org[3], const int P[
     G.gf.inv_dx2 = static_cast<float>(G.inv_dx2);
     G.gf.inv_dx6h5 = static_cast<float>(G.inv_dx6h5);
     G.gf.nu64 = static_cast<float>(G.nu64);
+    G.gf.d1a = static_cast<float>(G.d1a);
+    G.gf.d1b = static_cast<float>(G.d1b);
+    G.gf.ko_scale = static_cast<float>(G.ko_scale);
     G.gf.eta = static_cast<float>(G.eta);
     G.gf.kappa = static_cast<float>(G.kappa);
     G.gf.g = static_cast<float>(G.g);

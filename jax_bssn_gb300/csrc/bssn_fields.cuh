@@ -1,9 +1,12 @@
 // Component numbering, point addressing and pointwise tensor algebra.
 //
 // Pointwise algebra follows JAX_BSSN/bssn/tensor_algebra.py: the inverse
-// conformal metric by the explicit Cholesky factor (:20-71), the closed-form
-// 3x3 determinant (:74-96), Christoffel symbols (:148-193) and the trace-free
-// part (:359-381).  The algebraic projection (JAX_BSSN/evolution/time_evolve.py:94-141)
+// conformal metric (:20-71), the closed-form 3x3 determinant (:74-96),
+// Christoffel symbols (:148-193) and the trace-free part (:359-381).  The
+// reference inverts by an explicit Cholesky factor; the RHS kernels invert by
+// cofactors and one reciprocal of the determinant, which agrees to rounding
+// (gt^ij only ever multiplies perturbation-sized derivatives there) and costs
+// one FP64 reciprocal instead of three square roots and three reciprocals.  The algebraic projection (JAX_BSSN/evolution/time_evolve.py:94-141)
 // is written with round-to-nearest intrinsics in the reference's operation
 // order and a correctly rounded det^(-1/3), so a projected conformal metric is
 // bit-identical to the float64 reference: that matters because its second
@@ -60,35 +63,26 @@ __device__ __forceinline__ long long lin(const Geo& G, const int (&ix)[3]) {
 }
 
 // ---------------------------------------------------------------------------
-// inverse metric by explicit Cholesky (tensor_algebra.py:20-71), FMA allowed;
-// a template on the arithmetic type (sqrt and reciprocals in that type)
+// inverse metric by cofactors over the determinant, FMA allowed; a template on
+// the arithmetic type (the reciprocal in that type)
 // ---------------------------------------------------------------------------
 template <typename R>
 __device__ __forceinline__ void inverse_metric(const R (&g)[6], R (&gi)[6]) {
-    const R one = R(1);
-    const R l00 = sqrt(g[0]);
-    const R r00 = one / l00;
-    const R l10 = g[1] * r00;
-    const R l20 = g[2] * r00;
-    const R l11 = sqrt(g[3] - l10 * l10);
-    const R r11 = one / l11;
-    const R l21 = (g[4] - l20 * l10) * r11;
-    const R l22 = sqrt(g[5] - l20 * l20 - l21 * l21);
-    const R r22 = one / l22;
-    const R m00 = r00, m11 = r11, m22 = r22;
-    const R m10 = -l10 * r00 * r11;
-    const R m20 = (l10 * l21 - l20 * l11) * (r00 * r11 * r22);
-    const R m21 = -l21 * r11 * r22;
-    gi[0] = m00 * m00 + m10 * m10 + m20 * m20;
-    gi[1] = m10 * m11 + m20 * m21;
-    gi[2] = m20 * m22;
-    gi[3] = m11 * m11 + m21 * m21;
-    gi[4] = m21 * m22;
-    gi[5] = m22 * m22;
+    const R c00 = g[3] * g[5] - g[4] * g[4];
+    const R c01 = g[2] * g[4] - g[1] * g[5];
+    const R c02 = g[1] * g[4] - g[2] * g[3];
+    const R r = R(1) / (g[0] * c00 + g[1] * c01 + g[2] * c02);
+    gi[0] = c00 * r;
+    gi[1] = c01 * r;
+    gi[2] = c02 * r;
+    gi[3] = (g[0] * g[5] - g[2] * g[2]) * r;
+    gi[4] = (g[1] * g[2] - g[0] * g[4]) * r;
+    gi[5] = (g[0] * g[3] - g[1] * g[1]) * r;
 }
 
-// The same factorisation with every operation rounded in the reference's
-// order (used by the projection, whose output is part of the state).
+// The reference's Cholesky factorisation (tensor_algebra.py:20-71) with every
+// operation rounded in its order (used by the projection, whose output is part
+// of the state).
 __device__ __forceinline__ void inverse_metric_rn(const double (&g)[6], double (&gi)[6]) {
     const double l00 = __dsqrt_rn(g[0]);
     const double l10 = __ddiv_rn(g[1], l00);

@@ -179,11 +179,9 @@ __device__ __forceinline__ void w2_lapse_hessian(const R* __restrict__ u, const 
                                                  R (&out)[6]) {
     R h[6];
     hessian<R, Closed>(u, d1, G, nfield, CALPHA, MIX_ALPHA, c, h);
-    R gw = R(0);
+    R gw = R(0);  // gt^mn d_m W d_n alpha
 #pragma unroll
-    for (int m = 0; m < 3; ++m)
-#pragma unroll
-        for (int n = 0; n < 3; ++n) gw += gi[sym(m, n)] * dW[m] * da[n];
+    for (int n = 0; n < 3; ++n) gw += (gi[sym(0, n)] * dW[0] + gi[sym(1, n)] * dW[1] + gi[sym(2, n)] * dW[2]) * da[n];
     const R W2 = W * W;
 #pragma unroll
     for (int i = 0; i < 3; ++i)
@@ -245,32 +243,28 @@ __device__ __forceinline__ void w2_ricci(const R* __restrict__ u, const R* d1, c
                 ric[sym(i, j)] += R(0.5) * t2 + R(0.5) * t3;
             }
     }
-    // term4 + term5: loop over k to bound live registers.
+    // term4 + term5, one k at a time to bound live registers.  Both contract
+    // X[n][i] = g^mn Gamma^k_mi:
+    //   term4 = X[n][i] Gamma_jkn + X[n][j] Gamma_ikn,  term5 = X[n][i] Gamma_kjn
+    // (term5 = Gamma^k_im g^mn Gamma_kjn with the symmetric Gamma^k_mi).
 #pragma unroll 1
     for (int kk = 0; kk < 3; ++kk) {
-        R X[3][3], Y[3][3];  // X[n][i] = g^mn Gamma^k_mi ; Y[m][j] = g^mn Gamma_kjn
+        R X[3][3];
 #pragma unroll
         for (int a = 0; a < 3; ++a)
 #pragma unroll
-            for (int b = 0; b < 3; ++b) {
+            for (int b = 0; b < 3; ++b)
                 X[a][b] = gi[sym(0, a)] * c2[kk][sym(0, b)] + gi[sym(1, a)] * c2[kk][sym(1, b)]
                           + gi[sym(2, a)] * c2[kk][sym(2, b)];
-                Y[a][b] = gi[sym(a, 0)] * c1[kk][sym(b, 0)] + gi[sym(a, 1)] * c1[kk][sym(b, 1)]
-                          + gi[sym(a, 2)] * c1[kk][sym(b, 2)];
-            }
 #pragma unroll
         for (int i = 0; i < 3; ++i)
 #pragma unroll
             for (int j = i; j < 3; ++j) {
-                R t4 = R(0), t5 = R(0);
+                R acc = ric[sym(i, j)];
 #pragma unroll
-                for (int n = 0; n < 3; ++n) {
-                    // term4: g^mn Gamma^k_mi Gamma_jkn + (i<->j); c1[j][sym(k,n)] = Gamma_jkn
-                    t4 += X[n][i] * c1[j][sym(kk, n)] + X[n][j] * c1[i][sym(kk, n)];
-                    // term5: Gamma^k_im g^mn Gamma_kjn
-                    t5 += c2[kk][sym(i, n)] * Y[n][j];
-                }
-                ric[sym(i, j)] += t4 + t5;
+                for (int n = 0; n < 3; ++n)
+                    acc += X[n][i] * (c1[j][sym(kk, n)] + c1[kk][sym(j, n)]) + X[n][j] * c1[i][sym(kk, n)];
+                ric[sym(i, j)] = acc;
             }
     }
     // --- W terms: W (D_i D_j W + gt_ij lap W) - 2 gt_ij |dW|^2 (geometry.py:84-117) ---
@@ -280,11 +274,10 @@ __device__ __forceinline__ void w2_ricci(const R* __restrict__ u, const R* d1, c
 #pragma unroll
         for (int s = 0; s < 6; ++s) hW[s] -= c2[0][s] * dW[0] + c2[1][s] * dW[1] + c2[2][s] * dW[2];
         const R lap = contract_sym(gi, hW);
-        R grad2 = R(0);
+        R grad2 = R(0);  // gt^mn d_m W d_n W
 #pragma unroll
-        for (int m = 0; m < 3; ++m)
-#pragma unroll
-            for (int n = 0; n < 3; ++n) grad2 += gi[sym(m, n)] * dW[m] * dW[n];
+        for (int n = 0; n < 3; ++n)
+            grad2 += (gi[sym(0, n)] * dW[0] + gi[sym(1, n)] * dW[1] + gi[sym(2, n)] * dW[2]) * dW[n];
         const R W2 = W * W;
 #pragma unroll
         for (int s = 0; s < 6; ++s) w2r[s] = W2 * ric[s] + (W * (hW[s] + g[s] * lap) - R(2) * g[s] * grad2);
@@ -302,6 +295,8 @@ k_rhs_gauge(const R* __restrict__ u, const double* __restrict__ u64, const R* __
     if (!point(S.b[blockIdx.y], c, G)) return;
     const long long cs = G.cs, p = c.p;
     const R beta[3] = {u[BX * cs + p], u[BY * cs + p], u[BZ * cs + p]};
+    R bs[3];
+    shift_over_12dx(G, beta, bs);
     R db[3][3];  // db[i][j] = d_j beta^i
 #pragma unroll
     for (int i = 0; i < 3; ++i)
@@ -314,27 +309,35 @@ k_rhs_gauge(const R* __restrict__ u, const double* __restrict__ u64, const R* __
     R g[6];
     load_sym(u, GXX, G, p, g);
 
+    R P[6];  // pointwise terms: Lie terms - 2/3 gt_ij div beta - 2 alpha At_ij
+    {
+        const R m23div = R(-2.0 / 3.0) * div, m2a = R(-2.0) * alpha;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = i; j < 3; ++j) {
+                R lie = R(0);
+#pragma unroll
+                for (int m = 0; m < 3; ++m) lie += g[sym(m, i)] * db[m][j] + g[sym(m, j)] * db[m][i];
+                const int s = sym(i, j);
+                P[s] = lie + m23div * g[s] + m2a * u[(AXX + s) * cs + p];
+            }
+    }
 #pragma unroll 1
     for (int s = 0; s < 6; ++s) {
-        const int i = s < 3 ? 0 : (s < 5 ? 1 : 2);
-        const int j = s < 3 ? s : (s < 5 ? s - 2 : 2);
         const R* f = u + (GXX + s) * cs + p;
-        R lie = R(0);
-#pragma unroll
-        for (int m = 0; m < 3; ++m) lie += g[sym(m, i)] * db[m][j] + g[sym(m, j)] * db[m][i];
-        const R v = ADV<R, Closed>(f, G, c.ix, beta) + lie + R(-2.0 / 3.0) * g[s] * div
-                    + R(-2.0) * alpha * u[(AXX + s) * cs + p];
+        const R v = ADV<R, Closed>(f, G, c.ix, beta, bs) + P[s];
         k[(GXX + s) * cs + p] = v + KO<R, Closed>(f, G, c.ix);
     }
     {
         const R* f = u + CW * cs + p;
-        const R v = ADV<R, Closed>(f, G, c.ix, beta) + R(1.0 / 3.0) * alpha * W * K - R(1.0 / 3.0) * W * div;
+        const R v = ADV<R, Closed>(f, G, c.ix, beta, bs) + R(1.0 / 3.0) * alpha * W * K - R(1.0 / 3.0) * W * div;
         k[CW * cs + p] = v + KO<R, Closed>(f, G, c.ix);
     }
     {
         const R* f = u + CALPHA * cs + p;
         const R slicing = (G.gauge == 0) ? -(alpha * alpha) * K : R(-2.0) * alpha * K;
-        k[CALPHA * cs + p] = slicing + ADV<R, Closed>(f, G, c.ix, beta) + KO<R, Closed>(f, G, c.ix);
+        k[CALPHA * cs + p] = slicing + ADV<R, Closed>(f, G, c.ix, beta, bs) + KO<R, Closed>(f, G, c.ix);
     }
 #pragma unroll 1
     for (int i = 0; i < 3; ++i) {
@@ -343,7 +346,7 @@ k_rhs_gauge(const R* __restrict__ u, const double* __restrict__ u64, const R* __
         if (G.zero_shift) {
             v = R(0) * beta[i];
         } else {
-            v = BSSN_CO(R, G, g) * u[(GTX + i) * cs + p] + ADV<R, Closed>(f, G, c.ix, beta) + (-BSSN_CO(R, G, eta)) * beta[i];
+            v = BSSN_CO(R, G, g) * u[(GTX + i) * cs + p] + ADV<R, Closed>(f, G, c.ix, beta, bs) + (-BSSN_CO(R, G, eta)) * beta[i];
             v = v + KO<R, Closed>(f, G, c.ix);
         }
         k[(BX + i) * cs + p] = v;
@@ -380,20 +383,24 @@ k_rhs_kgt(const R* __restrict__ u, const double* __restrict__ u64, const R* __re
     const R alpha = full_exact(u, u64, CALPHA, cs, p);
     const R K = u[CK * cs + p];
     const R beta[3] = {u[BX * cs + p], u[BY * cs + p], u[BZ * cs + p]};
+    R bs[3];
+    shift_over_12dx(G, beta, bs);
     R A[6];
     load_sym(u, AXX, G, p, A);
-    R Au[6];  // A^ij = g^ik g^jl A_kl
+    R Au[6];  // A^ij = g^ik (A_kl g^lj)
+    {
+        R M[3][3];  // M[k][j] = A_kl g^lj
 #pragma unroll
-    for (int i = 0; i < 3; ++i)
+        for (int kk = 0; kk < 3; ++kk)
 #pragma unroll
-        for (int j = i; j < 3; ++j) {
-            R acc = R(0);
+            for (int j = 0; j < 3; ++j)
+                M[kk][j] = A[sym(kk, 0)] * gi[sym(0, j)] + A[sym(kk, 1)] * gi[sym(1, j)] + A[sym(kk, 2)] * gi[sym(2, j)];
 #pragma unroll
-            for (int kk = 0; kk < 3; ++kk)
+        for (int i = 0; i < 3; ++i)
 #pragma unroll
-                for (int l = 0; l < 3; ++l) acc += gi[sym(i, kk)] * gi[sym(j, l)] * A[sym(kk, l)];
-            Au[sym(i, j)] = acc;
-        }
+            for (int j = i; j < 3; ++j)
+                Au[sym(i, j)] = gi[sym(i, 0)] * M[0][j] + gi[sym(i, 1)] * M[1][j] + gi[sym(i, 2)] * M[2][j];
+    }
 
     // dt K
     {
@@ -403,7 +410,7 @@ k_rhs_kgt(const R* __restrict__ u, const double* __restrict__ u64, const R* __re
         const R second = alpha * contract_sym(A, Au);
         const R third = alpha * (K * K) / R(3.0);
         const R* f = u + CK * cs + p;
-        R bulk = first + second + third + ADV<R, Closed>(f, G, c.ix, beta);
+        R bulk = first + second + third + ADV<R, Closed>(f, G, c.ix, beta, bs);
         if (mat != nullptr) {
             // + 4 pi alpha (rho + W^2 gt^ij S_ij) (extrinsic_curvature.py:78-87)
             const R wf = static_cast<R>(fmax(u64[CW * cs + p], 1.0e-12));
@@ -455,7 +462,7 @@ k_rhs_kgt(const R* __restrict__ u, const double* __restrict__ u64, const R* __re
         const R t8 = contract_sym(gi, hb[i]);
         const R* f = u + (GTX + i) * cs + p;
         const R v = R(-4.0 / 3.0) * alpha * t1 + R(2.0) * alpha * t2 + six_alpha_over_w * t3
-                    - R(2.0) * t4 + ADV<R, Closed>(f, G, c.ix, beta) + R(2.0 / 3.0) * Gt[i] * div - t7 + t8
+                    - R(2.0) * t4 + ADV<R, Closed>(f, G, c.ix, beta, bs) + R(2.0 / 3.0) * Gt[i] * div - t7 + t8
                     + R(1.0 / 3.0) * t9;
         R out = v + KO<R, Closed>(f, G, c.ix);
         if (mat != nullptr) {
@@ -523,26 +530,42 @@ k_rhs_at(const R* __restrict__ u, const double* __restrict__ u64, const R* __res
     R A[6];
     load_sym(u, AXX, G, p, A);
     const R beta[3] = {u[BX * cs + p], u[BY * cs + p], u[BZ * cs + p]};
+    R bs[3];
+    shift_over_12dx(G, beta, bs);
     R db[3][3];
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
         for (int j = 0; j < 3; ++j) db[i][j] = d1ptr(d1, G, nfield, j, MIX_B + i, p)[0];
     const R div = db[0][0] + db[1][1] + db[2][2];
+    {
+        // Pointwise terms of every component first, with static indices:
+        // alpha K A_ij - 2 alpha A_ik g^kl A_lj + Lie terms - 2/3 A_ij div beta.
+        R M[3][3];  // M[k][j] = g^kl A_lj
+#pragma unroll
+        for (int kk = 0; kk < 3; ++kk)
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+                M[kk][j] = gi[sym(kk, 0)] * A[sym(0, j)] + gi[sym(kk, 1)] * A[sym(1, j)] + gi[sym(kk, 2)] * A[sym(2, j)];
+        const R aK = alpha * K, m2a = R(-2.0) * alpha, m23div = R(-2.0 / 3.0) * div;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = i; j < 3; ++j) {
+                R AgA = R(0), lie = R(0);
+#pragma unroll
+                for (int kk = 0; kk < 3; ++kk) {
+                    AgA += A[sym(i, kk)] * M[kk][j];
+                    lie += A[sym(kk, i)] * db[kk][j] + A[sym(kk, j)] * db[kk][i];
+                }
+                const int s = sym(i, j);
+                T[s] = (aK * A[s] + m2a * AgA) + T[s] + lie + m23div * A[s];
+            }
+    }
 #pragma unroll 1
     for (int s = 0; s < 6; ++s) {
-        const int i = s < 3 ? 0 : (s < 5 ? 1 : 2);
         const R* f = u + (AXX + s) * cs + p;
-        const int j = s < 3 ? s : (s < 5 ? s - 2 : 2);
-        R AgA = R(0), lie = R(0);
-#pragma unroll
-        for (int kk = 0; kk < 3; ++kk) {
-#pragma unroll
-            for (int l = 0; l < 3; ++l) AgA += A[sym(i, kk)] * gi[sym(kk, l)] * A[sym(l, j)];
-            lie += A[sym(kk, i)] * db[kk][j] + A[sym(kk, j)] * db[kk][i];
-        }
-        R v = alpha * K * A[s] - R(2.0) * alpha * AgA + T[s] + ADV<R, Closed>(f, G, c.ix, beta) + lie
-              + R(-2.0 / 3.0) * A[s] * div;
+        R v = T[s] + ADV<R, Closed>(f, G, c.ix, beta, bs);
         if (damp != nullptr) v += damp[s * cs + p];
         k[(AXX + s) * cs + p] = v + KO<R, Closed>(f, G, c.ix);
     }

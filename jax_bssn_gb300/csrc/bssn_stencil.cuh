@@ -15,9 +15,13 @@
 // difference and all one-sided closures) are accumulated with explicit
 // round-to-nearest intrinsics in the reference's term order, so the compiler
 // cannot contract them into FMAs and their rounding matches the float64
-// reference bit for bit (it is not amplified by the 1/dx^2 scaling).  Centred
-// differences of neighbouring pairs carry no such amplification and are left
-// free for FMA contraction.  R = float is the FP32-arithmetic form: the same
+// reference bit for bit (it is not amplified by the 1/dx^2 scaling).  A term
+// whose coefficient is +-1 or an upward power of two is an exact product, so
+// it is added by a plain add or a fused multiply-add with the same bits.
+// Centred differences of neighbouring pairs carry no such amplification, and
+// neither does anything after a numerator is formed (its scaling by 1/dx, the
+// shift factor of the advection term, the KO factor and the sum over axes):
+// those are left free for FMA contraction and regrouping.  R = float is the FP32-arithmetic form: the same
 // operators on float samples (perturbations about a constant background),
 // with every coefficient taken in float so no FP64 instruction is issued, and
 // contraction allowed throughout.
@@ -51,6 +55,7 @@ struct Axis {
 // Float copies of the scalar coefficients (FP32-arithmetic form).
 struct GeoF {
     float inv_dx, inv_12dx, inv_60dx, inv_12dx2, inv_dx2, inv_dx6h5, nu64, eta, kappa, g;
+    float d1a, d1b, ko_scale;
 };
 
 // Per-launch geometry and scalar parameters (passed by value).
@@ -66,6 +71,8 @@ struct Geo {
     double inv_dx2;   // 1/dx^2
     double inv_dx6h5; // h^5 / dx^6 (KO factor on the undivided sixth difference)
     double nu64;      // nu / 64
+    double d1a, d1b;  // 2/(3 dx) and -1/(12 dx): centred D4 weights of the pair differences
+    double ko_scale;  // nu/64 * h^5/dx^6: KO factor on the summed sixth-difference numerators
     double eta, kappa, g, dt;
     int gauge, zero_shift;
     int any_sommerfeld;
@@ -95,6 +102,28 @@ template <> struct Num<float> {
     static __device__ __forceinline__ float mul(float a, float b) { return a * b; }
 };
 
+// |c| in {2, 4, ..., 64}: c*f is exact for every finite f that does not overflow.
+__host__ __device__ constexpr bool upward_pow2(double c) {
+    const double a = c < 0.0 ? -c : c;
+    return a == 2.0 || a == 4.0 || a == 8.0 || a == 16.0 || a == 32.0 || a == 64.0;
+}
+
+// acc + c*f with the product and the sum each rounded (the reference's
+// rounding).  c is a compile-time coefficient after inlining: +-1 needs no
+// product, and an upward power of two makes the product exact, so one fused
+// multiply-add returns the same bits as the rounded product and sum.
+template <typename R>
+__device__ __forceinline__ R mac(R acc, double c, R f) {
+    if constexpr (std::is_same<R, double>::value) {
+        if (c == 1.0) return __dadd_rn(acc, f);
+        if (c == -1.0) return __dadd_rn(acc, -f);
+        if (upward_pow2(c)) return __fma_rn(c, f, acc);
+        return __dadd_rn(acc, __dmul_rn(c, f));
+    } else {
+        return acc + static_cast<float>(c) * f;
+    }
+}
+
 template <typename R>
 __device__ __forceinline__ R ld(const R* __restrict__ p, long long off) {
     return __ldg(p + off);
@@ -106,7 +135,7 @@ __device__ __forceinline__ R ordered(const R* __restrict__ p, long long s, const
                                      const double (&c)[N]) {
     R acc = Num<R>::mul(static_cast<R>(c[0]), ld(p, off[0] * s));
 #pragma unroll
-    for (int t = 1; t < N; ++t) acc = Num<R>::add(acc, Num<R>::mul(static_cast<R>(c[t]), ld(p, off[t] * s)));
+    for (int t = 1; t < N; ++t) acc = mac(acc, c[t], ld(p, off[t] * s));
     return acc;
 }
 
@@ -119,8 +148,7 @@ template <typename R, int N>
 __device__ __forceinline__ R closure(const R* __restrict__ p, long long s, int first, const double (&c)[N]) {
     R acc = Num<R>::mul(static_cast<R>(c[0]), ld(p, (long long)first * s));
 #pragma unroll
-    for (int t = 1; t < N; ++t)
-        acc = Num<R>::add(acc, Num<R>::mul(static_cast<R>(c[t]), ld(p, (long long)(first + t) * s)));
+    for (int t = 1; t < N; ++t) acc = mac(acc, c[t], ld(p, (long long)(first + t) * s));
     return acc;
 }
 
@@ -152,7 +180,7 @@ __device__ __forceinline__ R d1_interior(const R* __restrict__ p, long long s, c
                                          bool mad) {
     const R c1 = ld(p, s) - ld(p, -s);
     const R c2 = ld(p, 2 * s) - ld(p, -2 * s);
-    const R d4 = (static_cast<R>(2.0 / 3.0) * c1 + static_cast<R>(-1.0 / 12.0) * c2) * BSSN_CO(R, G, inv_dx);
+    const R d4 = c1 * BSSN_CO(R, G, d1a) + c2 * BSSN_CO(R, G, d1b);
     if (!mad) return d4;
     const R c3 = ld(p, 3 * s) - ld(p, -3 * s);
     const R d6 = (static_cast<R>(3.0 / 4.0) * c1 - static_cast<R>(3.0 / 20.0) * c2 + static_cast<R>(1.0 / 60.0) * c3)
@@ -216,7 +244,8 @@ __device__ __forceinline__ R D2(const R* __restrict__ p, const Geo& G, int d, in
 }
 
 // ---------------------------------------------------------------------------
-// h^5 * sixth derivative (one KO term, without nu/64)
+// undivided sixth difference along one axis (one KO numerator; the factor
+// nu/64 * h^5/dx^6 is applied once to the sum over axes)
 // ---------------------------------------------------------------------------
 template <typename R, bool Closed = true>
 __device__ __forceinline__ R KO1(const R* __restrict__ p, const Geo& G, int d, int i) {
@@ -245,14 +274,16 @@ __device__ __forceinline__ R KO1(const R* __restrict__ p, const Geo& G, int d, i
             num = ordered(p, s, o, c);
         }
     }
-    return num * BSSN_CO(R, G, inv_dx6h5);
+    return num;
 }
 
-// nu/64 * sum_d h^5 D6_d f  (JAX_BSSN/evolution/spatial_derivatives.py:81-92)
+// nu/64 * sum_d h^5 D6_d f  (JAX_BSSN/evolution/spatial_derivatives.py:81-92);
+// every axis shares h^5/dx^6, so it is applied with nu/64 to the summed
+// numerators.
 template <typename R, bool Closed = true>
 __device__ __forceinline__ R KO(const R* __restrict__ p, const Geo& G, const int (&ix)[3]) {
     const R t = KO1<R, Closed>(p, G, 0, ix[0]) + KO1<R, Closed>(p, G, 1, ix[1]);
-    return BSSN_CO(R, G, nu64) * (t + KO1<R, Closed>(p, G, 2, ix[2]));
+    return BSSN_CO(R, G, ko_scale) * (t + KO1<R, Closed>(p, G, 2, ix[2]));
 }
 
 // ---------------------------------------------------------------------------
@@ -300,11 +331,42 @@ __device__ __forceinline__ R UP1(const R* __restrict__ p, const Geo& G, int d, i
     return d1_interior(p, s, a, G, a.mad != 0);
 }
 
-// beta^d d_d f summed over d (JAX_BSSN/bssn/shift_and_lapse.py:43-63)
+// Interior D4 upwind numerator in units of 1/(12 dx), the side picked by the
+// sign of c.  A zero or NaN coefficient takes the second side: the caller
+// multiplies by c/(12 dx), which gives the zero or NaN that UP1's centred
+// value times c gives.
+template <typename R>
+__device__ __forceinline__ R up1_num(const R* __restrict__ p, long long s, R c) {
+    if (c > R(0)) {
+        constexpr int o[5] = {-1, 0, 1, 2, 3};
+        constexpr double k[5] = {-3.0, -10.0, 18.0, -6.0, 1.0};
+        return ordered(p, s, o, k);
+    }
+    constexpr int o[5] = {-3, -2, -1, 0, 1};
+    constexpr double k[5] = {-1.0, 6.0, -18.0, 10.0, 3.0};
+    return ordered(p, s, o, k);
+}
+
+// Shift over 12 dx: the factor of the interior upwind numerators.
+template <typename R>
+__device__ __forceinline__ void shift_over_12dx(const Geo& G, const R (&beta)[3], R (&bs)[3]) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) bs[d] = beta[d] * BSSN_CO(R, G, inv_12dx);
+}
+
+// beta^d d_d f summed over d (JAX_BSSN/bssn/shift_and_lapse.py:43-63).  bs is
+// beta/(12 dx): closure-free D4 axes multiply it into the bare numerator.
 template <typename R, bool Closed = true>
-__device__ __forceinline__ R ADV(const R* __restrict__ p, const Geo& G, const int (&ix)[3], const R (&beta)[3]) {
-    const R t = beta[0] * UP1<R, Closed>(p, G, 0, ix[0], beta[0]) + beta[1] * UP1<R, Closed>(p, G, 1, ix[1], beta[1]);
-    return t + beta[2] * UP1<R, Closed>(p, G, 2, ix[2], beta[2]);
+__device__ __forceinline__ R ADV(const R* __restrict__ p, const Geo& G, const int (&ix)[3], const R (&beta)[3],
+                                 const R (&bs)[3]) {
+    R t[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const Axis& a = G.ax[d];
+        if (!Closed && !a.mad) t[d] = a.reduced ? R(0) : bs[d] * up1_num(p, G.st[d], beta[d]);
+        else t[d] = beta[d] * UP1<R, Closed>(p, G, d, ix[d], beta[d]);
+    }
+    return (t[0] + t[1]) + t[2];
 }
 
 }  // namespace bssn
