@@ -44,6 +44,14 @@ constexpr double kPi = 3.141592653589793;   // the double nearest pi (numpy.pi)
 template <typename R>
 constexpr bool kPerturbative = std::is_same<R, float>::value;
 
+// Stencil numerators keep the reference's rounding for fields with a unit
+// background (diagonal gt, W, alpha) in the FP64 form; fields with a zero
+// background, and every field of the FP32 form (which stores perturbations),
+// take the regrouped interior numerators.
+template <typename R>
+constexpr bool kExactBg = !kPerturbative<R>;
+__host__ __device__ constexpr bool unit_diagonal(int s) { return s == 0 || s == 3 || s == 5; }
+
 __host__ __device__ constexpr bool has_background(int c) {
     return c == GXX || c == GYY || c == GZZ || c == CW || c == CALPHA;
 }
@@ -154,13 +162,13 @@ __device__ __forceinline__ R mixed(const R* d1, const Geo& G, int nfield, int f,
 
 // Symmetric Hessian of stored field f whose state component is comp:
 // h[sym(i,j)] = d_i d_j f, D2 on the diagonal.
-template <typename R, bool Closed>
+template <typename R, bool Closed, bool Exact = true>
 __device__ __forceinline__ void hessian(const R* __restrict__ u, const R* d1, const Geo& G, int nfield, int comp,
                                         int f, const PointCtx& c, R (&h)[6]) {
     const R* fp = u + comp * G.cs + c.p;
-    h[0] = D2<R, Closed>(fp, G, 0, c.ix[0]);
-    h[3] = D2<R, Closed>(fp, G, 1, c.ix[1]);
-    h[5] = D2<R, Closed>(fp, G, 2, c.ix[2]);
+    h[0] = D2<R, Closed, Exact>(fp, G, 0, c.ix[0]);
+    h[3] = D2<R, Closed, Exact>(fp, G, 1, c.ix[1]);
+    h[5] = D2<R, Closed, Exact>(fp, G, 2, c.ix[2]);
     h[1] = mixed<R, Closed>(d1, G, nfield, f, 0, 1, c);
     h[2] = mixed<R, Closed>(d1, G, nfield, f, 0, 2, c);
     h[4] = mixed<R, Closed>(d1, G, nfield, f, 1, 2, c);
@@ -178,7 +186,7 @@ __device__ __forceinline__ void w2_lapse_hessian(const R* __restrict__ u, const 
                                                  const R (&c2)[3][6], const R (&dW)[3], const R (&da)[3], R W,
                                                  R (&out)[6]) {
     R h[6];
-    hessian<R, Closed>(u, d1, G, nfield, CALPHA, MIX_ALPHA, c, h);
+    hessian<R, Closed, kExactBg<R>>(u, d1, G, nfield, CALPHA, MIX_ALPHA, c, h);
     R gw = R(0);  // gt^mn d_m W d_n alpha
 #pragma unroll
     for (int n = 0; n < 3; ++n) gw += (gi[sym(0, n)] * dW[0] + gi[sym(1, n)] * dW[1] + gi[sym(2, n)] * dW[2]) * da[n];
@@ -220,7 +228,8 @@ __device__ __forceinline__ void w2_ricci(const R* __restrict__ u, const R* d1, c
 #pragma unroll 1
     for (int s = 0; s < 6; ++s) {
         R h[6];
-        hessian<R, Closed>(u, d1, G, nfield, GXX + s, MIX_G + s, c, h);
+        if (unit_diagonal(s)) hessian<R, Closed, kExactBg<R>>(u, d1, G, nfield, GXX + s, MIX_G + s, c, h);
+        else hessian<R, Closed, false>(u, d1, G, nfield, GXX + s, MIX_G + s, c, h);
         ric[s] = R(-0.5) * contract_sym(gi, h);
     }
     {
@@ -270,7 +279,7 @@ __device__ __forceinline__ void w2_ricci(const R* __restrict__ u, const R* d1, c
     // --- W terms: W (D_i D_j W + gt_ij lap W) - 2 gt_ij |dW|^2 (geometry.py:84-117) ---
     {
         R hW[6];
-        hessian<R, Closed>(u, d1, G, nfield, CW, MIX_W, c, hW);
+        hessian<R, Closed, kExactBg<R>>(u, d1, G, nfield, CW, MIX_W, c, hW);
 #pragma unroll
         for (int s = 0; s < 6; ++s) hW[s] -= c2[0][s] * dW[0] + c2[1][s] * dW[1] + c2[2][s] * dW[2];
         const R lap = contract_sym(gi, hW);
@@ -326,18 +335,24 @@ k_rhs_gauge(const R* __restrict__ u, const double* __restrict__ u64, const R* __
 #pragma unroll 1
     for (int s = 0; s < 6; ++s) {
         const R* f = u + (GXX + s) * cs + p;
-        const R v = ADV<R, Closed>(f, G, c.ix, beta, bs) + P[s];
-        k[(GXX + s) * cs + p] = v + KO<R, Closed>(f, G, c.ix);
+        R v;
+        if (unit_diagonal(s))
+            v = (ADV<R, Closed, kExactBg<R>>(f, G, c.ix, beta, bs) + P[s]) + KO<R, Closed, kExactBg<R>>(f, G, c.ix);
+        else
+            v = (ADV<R, Closed, false>(f, G, c.ix, beta, bs) + P[s]) + KO<R, Closed, false>(f, G, c.ix);
+        k[(GXX + s) * cs + p] = v;
     }
     {
         const R* f = u + CW * cs + p;
-        const R v = ADV<R, Closed>(f, G, c.ix, beta, bs) + R(1.0 / 3.0) * alpha * W * K - R(1.0 / 3.0) * W * div;
-        k[CW * cs + p] = v + KO<R, Closed>(f, G, c.ix);
+        const R v = ADV<R, Closed, kExactBg<R>>(f, G, c.ix, beta, bs) + R(1.0 / 3.0) * alpha * W * K
+                    - R(1.0 / 3.0) * W * div;
+        k[CW * cs + p] = v + KO<R, Closed, kExactBg<R>>(f, G, c.ix);
     }
     {
         const R* f = u + CALPHA * cs + p;
         const R slicing = (G.gauge == 0) ? -(alpha * alpha) * K : R(-2.0) * alpha * K;
-        k[CALPHA * cs + p] = slicing + ADV<R, Closed>(f, G, c.ix, beta, bs) + KO<R, Closed>(f, G, c.ix);
+        k[CALPHA * cs + p] = slicing + ADV<R, Closed, kExactBg<R>>(f, G, c.ix, beta, bs)
+                             + KO<R, Closed, kExactBg<R>>(f, G, c.ix);
     }
 #pragma unroll 1
     for (int i = 0; i < 3; ++i) {
@@ -346,8 +361,9 @@ k_rhs_gauge(const R* __restrict__ u, const double* __restrict__ u64, const R* __
         if (G.zero_shift) {
             v = R(0) * beta[i];
         } else {
-            v = BSSN_CO(R, G, g) * u[(GTX + i) * cs + p] + ADV<R, Closed>(f, G, c.ix, beta, bs) + (-BSSN_CO(R, G, eta)) * beta[i];
-            v = v + KO<R, Closed>(f, G, c.ix);
+            v = BSSN_CO(R, G, g) * u[(GTX + i) * cs + p] + ADV<R, Closed, false>(f, G, c.ix, beta, bs)
+                + (-BSSN_CO(R, G, eta)) * beta[i];
+            v = v + KO<R, Closed, false>(f, G, c.ix);
         }
         k[(BX + i) * cs + p] = v;
     }
@@ -410,7 +426,7 @@ k_rhs_kgt(const R* __restrict__ u, const double* __restrict__ u64, const R* __re
         const R second = alpha * contract_sym(A, Au);
         const R third = alpha * (K * K) / R(3.0);
         const R* f = u + CK * cs + p;
-        R bulk = first + second + third + ADV<R, Closed>(f, G, c.ix, beta, bs);
+        R bulk = first + second + third + ADV<R, Closed, false>(f, G, c.ix, beta, bs);
         if (mat != nullptr) {
             // + 4 pi alpha (rho + W^2 gt^ij S_ij) (extrinsic_curvature.py:78-87)
             const R wf = static_cast<R>(fmax(u64[CW * cs + p], 1.0e-12));
@@ -422,7 +438,7 @@ k_rhs_kgt(const R* __restrict__ u, const double* __restrict__ u64, const R* __re
                 for (int j = 0; j < 3; ++j) trace += (wf2 * gi[sym(i, j)]) * static_cast<R>(mat[(4 + sym(i, j)) * cs + p]);
             bulk = bulk + R(4.0 * kPi) * alpha * (static_cast<R>(mat[p]) + trace);
         }
-        k[CK * cs + p] = bulk + KO<R, Closed>(f, G, c.ix);
+        k[CK * cs + p] = bulk + KO<R, Closed, false>(f, G, c.ix);
     }
 
     // dt Gt^i
@@ -442,7 +458,7 @@ k_rhs_kgt(const R* __restrict__ u, const double* __restrict__ u64, const R* __re
     }
     R hb[3][6];  // hb[i][sym(m,n)] = d_m d_n beta^i
 #pragma unroll 1
-    for (int i = 0; i < 3; ++i) hessian<R, Closed>(u, d1, G, nfield, BX + i, MIX_B + i, c, hb[i]);
+    for (int i = 0; i < 3; ++i) hessian<R, Closed, false>(u, d1, G, nfield, BX + i, MIX_B + i, c, hb[i]);
     R graddiv[3];
 #pragma unroll
     for (int m = 0; m < 3; ++m) graddiv[m] = hb[0][sym(m, 0)] + hb[1][sym(m, 1)] + hb[2][sym(m, 2)];
@@ -462,9 +478,9 @@ k_rhs_kgt(const R* __restrict__ u, const double* __restrict__ u64, const R* __re
         const R t8 = contract_sym(gi, hb[i]);
         const R* f = u + (GTX + i) * cs + p;
         const R v = R(-4.0 / 3.0) * alpha * t1 + R(2.0) * alpha * t2 + six_alpha_over_w * t3
-                    - R(2.0) * t4 + ADV<R, Closed>(f, G, c.ix, beta, bs) + R(2.0 / 3.0) * Gt[i] * div - t7 + t8
+                    - R(2.0) * t4 + ADV<R, Closed, false>(f, G, c.ix, beta, bs) + R(2.0 / 3.0) * Gt[i] * div - t7 + t8
                     + R(1.0 / 3.0) * t9;
-        R out = v + KO<R, Closed>(f, G, c.ix);
+        R out = v + KO<R, Closed, false>(f, G, c.ix);
         if (mat != nullptr) {
             // - 16 pi alpha gt^ij S_j (conformal_connection.py:166-178)
             R gs = R(0);
@@ -565,9 +581,9 @@ k_rhs_at(const R* __restrict__ u, const double* __restrict__ u64, const R* __res
 #pragma unroll 1
     for (int s = 0; s < 6; ++s) {
         const R* f = u + (AXX + s) * cs + p;
-        R v = T[s] + ADV<R, Closed>(f, G, c.ix, beta, bs);
+        R v = T[s] + ADV<R, Closed, false>(f, G, c.ix, beta, bs);
         if (damp != nullptr) v += damp[s * cs + p];
-        k[(AXX + s) * cs + p] = v + KO<R, Closed>(f, G, c.ix);
+        k[(AXX + s) * cs + p] = v + KO<R, Closed, false>(f, G, c.ix);
     }
 }
 
@@ -650,7 +666,7 @@ k_mom_damping(const R* __restrict__ u, const double* __restrict__ u64, const R* 
     }
     // d_l M_i (constraints.py:186-213), dM[i][l]
     R hW[6];
-    hessian<R, Closed>(u, d1, G, nfield, CW, MIX_W, c, hW);
+    hessian<R, Closed, kExactBg<R>>(u, d1, G, nfield, CW, MIX_W, c, hW);
     R dM[3][3];
 #pragma unroll 1
     for (int i = 0; i < 3; ++i) {
@@ -661,7 +677,7 @@ k_mom_damping(const R* __restrict__ u, const double* __restrict__ u64, const R* 
             for (int j = 0; j < 3; ++j) {
                 // d_l d_j B_ij
                 const int fb = fB + 3 * i + j;
-                divd += (l == j) ? D2<R, Closed>(der + (6 + 3 * i + j) * cs + p, G, l, c.ix[l])
+                divd += (l == j) ? D2<R, Closed, false>(der + (6 + 3 * i + j) * cs + p, G, l, c.ix[l])
                                  : mixed<R, Closed>(d1, G, nfield, fb, l, j, c);
                 const R dBW = D1<R, Closed>(der + (15 + 3 * i + j) * cs + p, G, l, c.ix[l]);
                 conf += dBW * dW[j] + der[(15 + 3 * i + j) * cs + p] * hW[sym(l, j)];
@@ -671,11 +687,11 @@ k_mom_damping(const R* __restrict__ u, const double* __restrict__ u64, const R* 
                 const R w = (s == 0 || s == 3 || s == 5) ? R(1.0) : R(2.0);
                 const R dgi = D1<R, Closed>(der + s * cs + p, G, l, c.ix[l]);
                 met += w * dgi * d1ptr(d1, G, nfield, i, fA + s, p)[0];
-                const R d2A = (l == i) ? D2<R, Closed>(u + (AXX + s) * cs + p, G, l, c.ix[l])
+                const R d2A = (l == i) ? D2<R, Closed, false>(u + (AXX + s) * cs + p, G, l, c.ix[l])
                                        : mixed<R, Closed>(d1, G, nfield, fA + s, l, i, c);
                 met2 += w * gi[s] * d2A;
             }
-            const R d2K = (l == i) ? D2<R, Closed>(u + CK * cs + p, G, l, c.ix[l]) : mixed<R, Closed>(d1, G, nfield, fK, l, i, c);
+            const R d2K = (l == i) ? D2<R, Closed, false>(u + CK * cs + p, G, l, c.ix[l]) : mixed<R, Closed>(d1, G, nfield, fK, l, i, c);
             dM[i][l] = divd - R(0.5) * met - R(0.5) * met2 - R(3.0) * conf - R(2.0 / 3.0) * d2K;
         }
     }

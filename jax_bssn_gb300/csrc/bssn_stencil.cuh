@@ -216,7 +216,33 @@ __device__ __forceinline__ R D1(const R* __restrict__ p, const Geo& G, int d, in
 // ---------------------------------------------------------------------------
 // pure second derivative
 // ---------------------------------------------------------------------------
-template <typename R, bool Closed = true>
+// Interior numerators of a field without a constant background (zero far
+// value: At, K, Gt, beta, the off-diagonal gt, and every field of the FP32
+// form, which stores perturbations).  Their rounding is relative to the
+// field's own scale rather than to an O(1) offset, so the reference's term
+// order does not have to be kept: the terms are grouped into symmetric pairs
+// and fused multiply-adds.  Template argument Exact = false selects these.
+template <typename R>
+__device__ __forceinline__ R d2_num_pairs(const R* __restrict__ p, long long s) {
+    const R p1 = ld(p, s) + ld(p, -s);
+    const R p2 = ld(p, 2 * s) + ld(p, -2 * s);
+    return (R(16) * p1 - p2) + R(-30) * ld(p, 0);
+}
+template <typename R>
+__device__ __forceinline__ R ko_num_pairs(const R* __restrict__ p, long long s) {
+    const R p1 = ld(p, s) + ld(p, -s);
+    const R p2 = ld(p, 2 * s) + ld(p, -2 * s);
+    const R p3 = ld(p, 3 * s) + ld(p, -3 * s);
+    return ((p3 + R(-6) * p2) + R(15) * p1) + R(-20) * ld(p, 0);
+}
+template <typename R>
+__device__ __forceinline__ R up1_num_fused(const R* __restrict__ p, long long s, R c) {
+    if (c > R(0))
+        return (((R(-3) * ld(p, -s) + R(-10) * ld(p, 0)) + R(18) * ld(p, s)) + R(-6) * ld(p, 2 * s)) + ld(p, 3 * s);
+    return (((-ld(p, -3 * s) + R(6) * ld(p, -2 * s)) + R(-18) * ld(p, -s)) + R(10) * ld(p, 0)) + R(3) * ld(p, s);
+}
+
+template <typename R, bool Closed = true, bool Exact = true>
 __device__ __forceinline__ R D2(const R* __restrict__ p, const Geo& G, int d, int i) {
     const Axis& a = G.ax[d];
     if (a.reduced) return R(0);
@@ -234,7 +260,7 @@ __device__ __forceinline__ R D2(const R* __restrict__ p, const Geo& G, int d, in
     if (r == 1) return closure(p, s, -1, L1) * inv_dx2;
     constexpr int o4[5] = {2, 1, 0, -1, -2};
     constexpr double c4[5] = {-1.0, 16.0, -30.0, 16.0, -1.0};
-    const R d4 = ordered(p, s, o4, c4) * BSSN_CO(R, G, inv_12dx2);
+    const R d4 = (!Closed && !Exact ? d2_num_pairs(p, s) : ordered(p, s, o4, c4)) * BSSN_CO(R, G, inv_12dx2);
     if (!a.mad) return d4;
     constexpr int o6[7] = {3, 2, 1, 0, -1, -2, -3};
     constexpr double c6[7] = {1.0 / 90.0, -3.0 / 20.0, 3.0 / 2.0, -49.0 / 18.0,
@@ -280,8 +306,14 @@ __device__ __forceinline__ R KO1(const R* __restrict__ p, const Geo& G, int d, i
 // nu/64 * sum_d h^5 D6_d f  (JAX_BSSN/evolution/spatial_derivatives.py:81-92);
 // every axis shares h^5/dx^6, so it is applied with nu/64 to the summed
 // numerators.
-template <typename R, bool Closed = true>
+template <typename R, bool Closed = true, bool Exact = true>
 __device__ __forceinline__ R KO(const R* __restrict__ p, const Geo& G, const int (&ix)[3]) {
+    if constexpr (!Closed && !Exact) {
+        R t[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) t[d] = G.ax[d].reduced ? R(0) : ko_num_pairs(p, G.st[d]);
+        return BSSN_CO(R, G, ko_scale) * ((t[0] + t[1]) + t[2]);
+    }
     const R t = KO1<R, Closed>(p, G, 0, ix[0]) + KO1<R, Closed>(p, G, 1, ix[1]);
     return BSSN_CO(R, G, ko_scale) * (t + KO1<R, Closed>(p, G, 2, ix[2]));
 }
@@ -356,15 +388,18 @@ __device__ __forceinline__ void shift_over_12dx(const Geo& G, const R (&beta)[3]
 
 // beta^d d_d f summed over d (JAX_BSSN/bssn/shift_and_lapse.py:43-63).  bs is
 // beta/(12 dx): closure-free D4 axes multiply it into the bare numerator.
-template <typename R, bool Closed = true>
+template <typename R, bool Closed = true, bool Exact = true>
 __device__ __forceinline__ R ADV(const R* __restrict__ p, const Geo& G, const int (&ix)[3], const R (&beta)[3],
                                  const R (&bs)[3]) {
     R t[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         const Axis& a = G.ax[d];
-        if (!Closed && !a.mad) t[d] = a.reduced ? R(0) : bs[d] * up1_num(p, G.st[d], beta[d]);
-        else t[d] = beta[d] * UP1<R, Closed>(p, G, d, ix[d], beta[d]);
+        if (!Closed && !a.mad)
+            t[d] = a.reduced ? R(0)
+                             : bs[d] * (Exact ? up1_num(p, G.st[d], beta[d]) : up1_num_fused(p, G.st[d], beta[d]));
+        else
+            t[d] = beta[d] * UP1<R, Closed>(p, G, d, ix[d], beta[d]);
     }
     return (t[0] + t[1]) + t[2];
 }
