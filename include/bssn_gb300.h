@@ -258,6 +258,12 @@ int bssn_cartoon_constraints(int32_t axisymmetric, const double* compact, const 
  * (synchronous; the denominator of the RHS kernels' compute roofline). */
 int bssn_probe_fma_peak(int32_t precision, double* gflops);
 
+/* No reference counterpart.  Self-check of the final RK4 division: for the n
+ * device doubles a, fast[i] = the three-operation correctly rounded a[i]/6 the
+ * RK4 stage kernel uses and hw[i] = the hardware-rounded division a[i]/6.0.
+ * Asynchronous on `stream`. */
+int bssn_check_div6(const double* a, double* fast, double* hw, int64_t n, void* stream);
+
 /* Kernel launches issued by this library since load (all threads). */
 long long bssn_launch_count(void);
 /* Per-kernel-class device-time accounting with CUDA events on each launch's

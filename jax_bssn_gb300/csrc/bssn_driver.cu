@@ -396,10 +396,10 @@ __global__ void k_rk4_stage(const double* __restrict__ u0, const double* __restr
         } else {
             if (stage < 4) {
                 v[c] = __dadd_rn(u0[q], __dmul_rn(h, kv));
-                acc[q] = (stage == 1) ? kv : __dadd_rn(acc[q], __dmul_rn(2.0, kv));
+                acc[q] = (stage == 1) ? kv : __fma_rn(2.0, kv, acc[q]);  // 2k is exact: same bits as mul + add
             } else {
                 const double s = __dadd_rn(acc[q], kv);
-                const double inc = final_form ? __ddiv_rn(__dmul_rn(dt, s), 6.0) : __dmul_rn(dt / 6.0, s);
+                const double inc = final_form ? div6_rn(__dmul_rn(dt, s)) : __dmul_rn(dt / 6.0, s);
                 v[c] = __dadd_rn(u0[q], inc);
             }
         }

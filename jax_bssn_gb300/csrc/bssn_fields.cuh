@@ -80,6 +80,22 @@ __device__ __forceinline__ void inverse_metric(const R (&g)[6], R (&gi)[6]) {
     gi[5] = (g[0] * g[3] - g[1] * g[1]) * r;
 }
 
+// Correctly rounded a/6, the final RK4 division of the reference
+// (time_evolve.py:144-217), in three FP64 operations by Markstein's theorem
+// (P. Markstein, IBM J. Res. Dev. 34(1), 1990, 111-119): y = RN(1/6) is within
+// half an ulp of 1/6 and q = RN(a*y) within one ulp of a/6, so the remainder
+// r = a - 6q is exact under an FMA and RN(q + r*y) = RN(a/6).  The theorem
+// assumes no underflow or overflow; outside that range, and for zeros, infinities
+// and NaN, the hardware division is used.
+__device__ __forceinline__ double div6_rn(double a) {
+    const double m = fabs(a);
+    if (!(m >= 0x1p-960 && m <= 0x1p1020)) return __ddiv_rn(a, 6.0);
+    constexpr double y = 1.0 / 6.0;
+    const double q = __dmul_rn(a, y);
+    const double r = __fma_rn(-6.0, q, a);
+    return __fma_rn(r, y, q);
+}
+
 // The reference's Cholesky factorisation (tensor_algebra.py:20-71) with every
 // operation rounded in its order (used by the projection, whose output is part
 // of the state).

@@ -11,6 +11,7 @@
 
 #include "../../include/bssn_gb300.h"
 #include "bssn_driver.h"
+#include "bssn_fields.cuh"
 
 namespace bssn {
 namespace {
@@ -66,6 +67,14 @@ int probe(double* gflops, int iters) {
     return BSSN_OK;
 }
 
+__global__ void k_check_div6(const double* __restrict__ a, double* __restrict__ fast, double* __restrict__ hw,
+                             long long n) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    fast[i] = div6_rn(a[i]);
+    hw[i] = __ddiv_rn(a[i], 6.0);
+}
+
 }  // namespace
 }  // namespace bssn
 
@@ -74,4 +83,12 @@ extern "C" int bssn_probe_fma_peak(int32_t precision, double* gflops) {
     if (precision == BSSN_PRECISION_F64) return bssn::probe<double>(gflops, 4096);
     if (precision == BSSN_PRECISION_F32) return bssn::probe<float>(gflops, 65536);
     return bssn::fail(BSSN_ERR_INVALID, "precision must be BSSN_PRECISION_F64 or BSSN_PRECISION_F32");
+}
+
+extern "C" int bssn_check_div6(const double* a, double* fast, double* hw, int64_t n, void* stream) {
+    if (n < 0 || (n > 0 && (!a || !fast || !hw))) return bssn::fail(BSSN_ERR_INVALID, "bssn_check_div6: bad arguments");
+    if (n == 0) return BSSN_OK;
+    const long long blocks = (n + 255) / 256;
+    bssn::k_check_div6<<<(unsigned)blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(a, fast, hw, n);
+    return bssn::cuda_status(cudaGetLastError(), "bssn_check_div6");
 }
