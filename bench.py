@@ -51,13 +51,14 @@ UNIT = "updates/s"
 BYTES_PER_UPDATE = 2856          # algorithmic HBM bytes per point per RK4 step (21 comps, 357 doubles)
 # Algorithmic HBM bytes per point of one launch, per kernel class (values read + written x 8 B).
 CLASS_BYTES = {
+    "rhs_curv": 512,       # 21 state + 33 first derivatives read, 10 written (K, Gt, At in one pass)
     "rhs_at": 480,         # 21 state + 33 first derivatives read, 6 written
     "rhs_kgt": 464,        # 21 state + 33 first derivatives read, 4 written
     "rhs_gauge": 328,      # 21 state + 9 first derivatives read, 11 written
     "first_derivs": 352,   # 11 fields read, 33 derivatives written
     "rk4_stage": 714,      # mean of 63, 105, 105, 84 values over the four stages
 }
-RHS_CLASSES = ("rhs_at", "rhs_kgt", "rhs_gauge", "first_derivs")
+RHS_CLASSES = ("rhs_curv", "rhs_at", "rhs_kgt", "rhs_gauge", "first_derivs")
 # FP32 form: float state and derivatives (4 B), FP64 RHS written (8 B), W and alpha read from the FP64 state
 CLASS_BYTES_F32 = {
     "rhs_at": (21 + 33) * 4 + 2 * 8 + 6 * 8,
@@ -65,10 +66,12 @@ CLASS_BYTES_F32 = {
     "rhs_gauge": (21 + 9) * 4 + 2 * 8 + 11 * 8,
     "first_derivs": 11 * 4 + 33 * 4,
 }
-# Executed flops per point of one k_rhs_at launch (FMA = 2), from an ncu count
-# of the 96^3 Teukolsky configuration's interior launch (DADD + DMUL + 2 DFMA,
-# resp. FADD + FMUL + 2 FFMA over the launch's threads).
-RHS_AT_FLOPS_PER_POINT = {"fp64": 2512, "fp32": 2395}
+# The compute-roofline kernel of each form and its executed flops per point
+# (FMA = 2), from an ncu count of the 96^3 Teukolsky configuration's interior
+# launch (DADD + DMUL + 2 DFMA, resp. FADD + FMUL + 2 FFMA over the launch's
+# threads): the one-pass K/Gt/At kernel of the FP64 form, the At kernel of the
+# FP32 form.
+COMPUTE_KERNEL = {"fp64": ("rhs_curv", 2512), "fp32": ("rhs_at", 2395)}
 LEAVES = ("conformal_metric", "conformal_factor", "traceless_K", "trace_K", "conformal_connection", "lapse",
           "shift")
 
@@ -362,16 +365,18 @@ def _max_over_ranks(ms, world, device):
 
 
 def compute_roofline_of(prof, points, profiled_steps, peak_gflops, precision):
-    """FP64 / FP32 pipe roofline of k_rhs_at: executed flops of its launches in
-    the profiled steps over their summed device time, against the live FMA peak."""
-    if "rhs_at" not in prof or not peak_gflops:
+    """FP64 / FP32 pipe roofline of the form's curvature kernel: executed flops
+    of its launches in the profiled steps over their summed device time, against
+    the live FMA peak."""
+    name, per_point = COMPUTE_KERNEL[precision]
+    if name not in prof or not peak_gflops:
         return None
-    ms, launches = prof["rhs_at"]
-    flops = RHS_AT_FLOPS_PER_POINT[precision] * points * 4 * profiled_steps
+    ms, launches = prof[name]
+    flops = per_point * points * 4 * profiled_steps
     achieved = flops / (ms / 1e3) / 1e12
     peak = peak_gflops / 1e3
-    return {"bound": precision, "kernel": "k_rhs_at", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-            "frac": achieved / peak, "flops_per_point": RHS_AT_FLOPS_PER_POINT[precision],
+    return {"bound": precision, "kernel": f"k_{name}", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak, "flops_per_point": per_point,
             "peak_source": "measured live by bssn_probe_fma_peak"}
 
 

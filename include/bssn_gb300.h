@@ -270,7 +270,7 @@ long long bssn_launch_count(void);
  * stream; off by default.  Classes: fill, first derivatives, gauge RHS, K/Gt
  * RHS, At RHS, momentum derived fields, momentum damping, Sommerfeld, RK4
  * stage, projection, import, export, constraints, FMR transfer, Cartoon,
- * other.  bssn_profile_read synchronises the recorded events, accumulates and
+ * FP32 conversion, other, K/Gt/At RHS in one pass (FP64 form).  bssn_profile_read synchronises the recorded events, accumulates and
  * returns the number of classes. */
 void bssn_profile_enable(int on);
 void bssn_profile_reset(void);

@@ -139,9 +139,9 @@ SIGNATURES = {
     "bssn_profile_read": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
 }
 
-KERNEL_CLASSES = ("fill", "first_derivs", "rhs_gauge", "rhs_k_gamma", "rhs_at", "mom_derived", "mom_damping",
+KERNEL_CLASSES = ("fill", "first_derivs", "rhs_gauge", "rhs_kgt", "rhs_at", "mom_derived", "mom_damping",
                   "sommerfeld", "rk4_stage", "project", "import", "export", "constraints", "fmr_transfer",
-                  "cartoon", "convert", "other")
+                  "cartoon", "convert", "other", "rhs_curv")
 
 
 def profile_read() -> dict:

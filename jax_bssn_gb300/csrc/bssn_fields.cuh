@@ -221,13 +221,22 @@ __device__ __forceinline__ double inv_cbrt_cr(double x) {
 // ---------------------------------------------------------------------------
 template <typename R>
 __device__ __forceinline__ void christoffel(const R (&dg)[3][6], const R (&gi)[6], R (&c1)[3][6], R (&c2)[3][6]) {
+    // Index patterns whose terms cancel are written out: Gamma_iii = d_i g_ii / 2,
+    // Gamma_ijj = d_j g_ij - d_i g_jj / 2, Gamma_iik = Gamma_iki = d_k g_ii / 2.
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
         for (int j = 0; j < 3; ++j)
 #pragma unroll
-            for (int k = j; k < 3; ++k)
-                c1[i][sym(j, k)] = R(0.5) * (dg[k][sym(i, j)] + dg[j][sym(i, k)] - dg[i][sym(j, k)]);
+            for (int k = j; k < 3; ++k) {
+                R v;
+                if (j == k && i == j) v = R(0.5) * dg[i][sym(i, i)];
+                else if (j == k) v = dg[j][sym(i, j)] + R(-0.5) * dg[i][sym(j, j)];
+                else if (i == j) v = R(0.5) * dg[k][sym(i, i)];
+                else if (i == k) v = R(0.5) * dg[j][sym(i, i)];
+                else v = R(0.5) * (dg[k][sym(i, j)] + dg[j][sym(i, k)] - dg[i][sym(j, k)]);
+                c1[i][sym(j, k)] = v;
+            }
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll

@@ -223,14 +223,24 @@ __device__ __forceinline__ void w2_ricci(const R* __restrict__ u, const R* d1, c
                                          const PointCtx& c, const R (&g)[6], const R (&gi)[6], const R (&c1)[3][6],
                                          const R (&c2)[3][6], const R (&dW)[3], R W, R (&w2r)[6]) {
     const long long cs = G.cs, p = c.p;
+    // The FP64 form is bound by FP64 instructions, not loads: it re-reads the
+    // metric derivatives d_m gt_ij and uses d_m gt_jk = Gamma_jkm + Gamma_kjm,
+    // which needs fewer operations than the Christoffel sums.
+    constexpr bool reload = !kPerturbative<R>;
+    auto dgm = [&](int m, int s) { return d1ptr(d1, G, nfield, m, MIX_G + s, p)[0]; };
     // --- conformal Ricci tensor (geometry.py:44-81) ---
     R ric[6];
+    {
+        // -1/2 gt^mn with the off-diagonal entries doubled: -1/2 gt^mn d_m d_n gt_ij
+        // as a six-term sum over the symmetric Hessian
+        const R hg[6] = {R(-0.5) * gi[0], -gi[1], -gi[2], R(-0.5) * gi[3], -gi[4], R(-0.5) * gi[5]};
 #pragma unroll 1
-    for (int s = 0; s < 6; ++s) {
-        R h[6];
-        if (unit_diagonal(s)) hessian<R, Closed, kExactBg<R>>(u, d1, G, nfield, GXX + s, MIX_G + s, c, h);
-        else hessian<R, Closed, false>(u, d1, G, nfield, GXX + s, MIX_G + s, c, h);
-        ric[s] = R(-0.5) * contract_sym(gi, h);
+        for (int s = 0; s < 6; ++s) {
+            R h[6];
+            if (unit_diagonal(s)) hessian<R, Closed, kExactBg<R>>(u, d1, G, nfield, GXX + s, MIX_G + s, c, h);
+            else hessian<R, Closed, false>(u, d1, G, nfield, GXX + s, MIX_G + s, c, h);
+            ric[s] = hg[0] * h[0] + hg[1] * h[1] + hg[2] * h[2] + hg[3] * h[3] + hg[4] * h[4] + hg[5] * h[5];
+        }
     }
     {
         const R Gt[3] = {u[GTX * cs + p], u[GTY * cs + p], u[GTZ * cs + p]};
@@ -243,13 +253,14 @@ __device__ __forceinline__ void w2_ricci(const R* __restrict__ u, const R* d1, c
         for (int i = 0; i < 3; ++i)
 #pragma unroll
             for (int j = i; j < 3; ++j) {
-                R t2 = R(0), t3 = R(0);
+                R t2 = R(0), t3 = R(0);  // t3 = Gt^m (Gamma_ijm + Gamma_jim) = Gt^m d_m gt_ij
 #pragma unroll
                 for (int m = 0; m < 3; ++m) {
                     t2 += g[sym(m, i)] * dG[j][m] + g[sym(m, j)] * dG[i][m];
-                    t3 += Gt[m] * (c1[i][sym(j, m)] + c1[j][sym(i, m)]);
+                    if constexpr (reload) t3 += Gt[m] * dgm(m, sym(i, j));
+                    else t3 += Gt[m] * (c1[i][sym(j, m)] + c1[j][sym(i, m)]);
                 }
-                ric[sym(i, j)] += R(0.5) * t2 + R(0.5) * t3;
+                ric[sym(i, j)] += R(0.5) * (t2 + t3);
             }
     }
     // term4 + term5, one k at a time to bound live registers.  Both contract
@@ -271,8 +282,10 @@ __device__ __forceinline__ void w2_ricci(const R* __restrict__ u, const R* d1, c
             for (int j = i; j < 3; ++j) {
                 R acc = ric[sym(i, j)];
 #pragma unroll
-                for (int n = 0; n < 3; ++n)
-                    acc += X[n][i] * (c1[j][sym(kk, n)] + c1[kk][sym(j, n)]) + X[n][j] * c1[i][sym(kk, n)];
+                for (int n = 0; n < 3; ++n) {
+                    if constexpr (reload) acc += X[n][i] * dgm(n, sym(j, kk)) + X[n][j] * c1[i][sym(kk, n)];
+                    else acc += X[n][i] * (c1[j][sym(kk, n)] + c1[kk][sym(j, n)]) + X[n][j] * c1[i][sym(kk, n)];
+                }
                 ric[sym(i, j)] = acc;
             }
     }
@@ -584,6 +597,165 @@ k_rhs_at(const R* __restrict__ u, const double* __restrict__ u64, const R* __res
         R v = T[s] + ADV<R, Closed, false>(f, G, c.ix, beta, bs);
         if (damp != nullptr) v += damp[s * cs + p];
         k[(AXX + s) * cs + p] = v + KO<R, Closed, false>(f, G, c.ix);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// dt K, dt Gt^i and dt At_ij in one pass (the FP64 form).  The two curvature
+// kernels above share the inverse metric, the Christoffel symbols, the lapse
+// Hessian and the products of At with gt^ij; the FP64 form is bound by its
+// FP64 instruction count, not by occupancy, so it computes those once.
+// ---------------------------------------------------------------------------
+template <typename R, bool Closed>
+__global__ void __launch_bounds__(kThreads)
+k_rhs_curv(const R* __restrict__ u, const double* __restrict__ u64, const R* __restrict__ d1,
+           const R* __restrict__ damp, const double* __restrict__ mat, double* __restrict__ k, Geo G, BoxSet S,
+           int nfield) {
+    PointCtx c;
+    if (!point(S.b[blockIdx.y], c, G)) return;
+    const long long cs = G.cs, p = c.p;
+    R g[6], gi[6];
+    load_sym(u, GXX, G, p, g);
+    inverse_metric(g, gi);
+    R c1[3][6], c2[3][6];
+    {
+        R dg[3][6];
+        load_metric_derivs(d1, G, nfield, p, dg);
+        christoffel(dg, gi, c1, c2);
+    }
+    R dW[3], da[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        dW[d] = d1ptr(d1, G, nfield, d, MIX_W, p)[0];
+        da[d] = d1ptr(d1, G, nfield, d, MIX_ALPHA, p)[0];
+    }
+    const R W = full_exact(u, u64, CW, cs, p);
+    const R alpha = full_exact(u, u64, CALPHA, cs, p);
+
+    // [alpha W^2 R_ij - W^2 D_i D_j alpha]^TF and gt^ij W^2 D_i D_j alpha
+    R T[6], lapse_lap;
+    {
+        R w2r[6];
+        w2_ricci<R, Closed>(u, d1, G, nfield, c, g, gi, c1, c2, dW, W, w2r);
+        R h[6];
+        w2_lapse_hessian<R, Closed>(u, d1, G, nfield, c, g, gi, c2, dW, da, W, h);
+        lapse_lap = contract_sym(gi, h);
+#pragma unroll
+        for (int s = 0; s < 6; ++s) T[s] = alpha * w2r[s] - h[s];
+        if (mat != nullptr) {
+            const R wf = static_cast<R>(fmax(u64[CW * cs + p], 1.0e-12));
+            const R coef = R(8.0 * kPi) * alpha * (wf * wf);
+#pragma unroll
+            for (int s = 0; s < 6; ++s) T[s] = T[s] - coef * static_cast<R>(mat[(4 + s) * cs + p]);
+        }
+        const R tr = contract_sym(gi, T);
+#pragma unroll
+        for (int s = 0; s < 6; ++s) T[s] = T[s] - R(1.0 / 3.0) * g[s] * tr;
+    }
+    const R K = u[CK * cs + p];
+    R A[6];
+    load_sym(u, AXX, G, p, A);
+    const R beta[3] = {u[BX * cs + p], u[BY * cs + p], u[BZ * cs + p]};
+    R bs[3];
+    shift_over_12dx(G, beta, bs);
+    R db[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) db[i][j] = d1ptr(d1, G, nfield, j, MIX_B + i, p)[0];
+    const R div = db[0][0] + db[1][1] + db[2][2];
+    R Au[6];  // A^ij = g^ik (g^jl A_lk)
+    {
+        R M[3][3];  // M[k][j] = g^kl A_lj
+#pragma unroll
+        for (int kk = 0; kk < 3; ++kk)
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+                M[kk][j] = gi[sym(kk, 0)] * A[sym(0, j)] + gi[sym(kk, 1)] * A[sym(1, j)] + gi[sym(kk, 2)] * A[sym(2, j)];
+        const R aK = alpha * K, m2a = R(-2.0) * alpha, m23div = R(-2.0 / 3.0) * div;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = i; j < 3; ++j) {
+                R AgA = R(0), lie = R(0);
+#pragma unroll
+                for (int kk = 0; kk < 3; ++kk) {
+                    AgA += A[sym(i, kk)] * M[kk][j];
+                    lie += A[sym(kk, i)] * db[kk][j] + A[sym(kk, j)] * db[kk][i];
+                }
+                const int s = sym(i, j);
+                T[s] = (aK * A[s] + m2a * AgA) + T[s] + lie + m23div * A[s];
+                Au[s] = gi[sym(i, 0)] * M[j][0] + gi[sym(i, 1)] * M[j][1] + gi[sym(i, 2)] * M[j][2];
+            }
+    }
+    // dt At_ij (extrinsic_curvature.py:100-175)
+#pragma unroll 1
+    for (int s = 0; s < 6; ++s) {
+        const R* f = u + (AXX + s) * cs + p;
+        R v = T[s] + ADV<R, Closed, false>(f, G, c.ix, beta, bs);
+        if (damp != nullptr) v += damp[s * cs + p];
+        k[(AXX + s) * cs + p] = v + KO<R, Closed, false>(f, G, c.ix);
+    }
+    // dt K (extrinsic_curvature.py:20-87)
+    {
+        const R* f = u + CK * cs + p;
+        R bulk = -lapse_lap + alpha * contract_sym(A, Au) + alpha * (K * K) / R(3.0)
+                 + ADV<R, Closed, false>(f, G, c.ix, beta, bs);
+        if (mat != nullptr) {
+            const R wf = static_cast<R>(fmax(u64[CW * cs + p], 1.0e-12));
+            const R wf2 = wf * wf;
+            R trace = R(0);
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) trace += (wf2 * gi[sym(i, j)]) * static_cast<R>(mat[(4 + sym(i, j)) * cs + p]);
+            bulk = bulk + R(4.0 * kPi) * alpha * (static_cast<R>(mat[p]) + trace);
+        }
+        k[CK * cs + p] = bulk + KO<R, Closed, false>(f, G, c.ix);
+    }
+    // dt Gt^i (conformal_connection.py:20-178)
+    R dK[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) dK[d] = D1<R, Closed>(u + CK * cs + p, G, d, c.ix[d]);
+    R six_alpha_over_w;
+    if constexpr (kPerturbative<R>) {
+        six_alpha_over_w = R(-6.0) * alpha * static_cast<R>(1.0 / fmax(u64[CW * cs + p], 1.0e-12));
+    } else {
+        const R Wf = fmax(W, 1.0e-12);
+        six_alpha_over_w = -6.0 * alpha / Wf;
+    }
+    R hb[3][6];  // hb[i][sym(m,n)] = d_m d_n beta^i
+#pragma unroll 1
+    for (int i = 0; i < 3; ++i) hessian<R, Closed, false>(u, d1, G, nfield, BX + i, MIX_B + i, c, hb[i]);
+    R graddiv[3];
+#pragma unroll
+    for (int m = 0; m < 3; ++m) graddiv[m] = hb[0][sym(m, 0)] + hb[1][sym(m, 1)] + hb[2][sym(m, 2)];
+    const R Gt[3] = {u[GTX * cs + p], u[GTY * cs + p], u[GTZ * cs + p]};
+#pragma unroll 1
+    for (int i = 0; i < 3; ++i) {
+        R t1 = R(0), t3 = R(0), t4 = R(0), t7 = R(0), t9 = R(0);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            t1 += gi[sym(i, j)] * dK[j];
+            t3 += Au[sym(i, j)] * dW[j];
+            t4 += Au[sym(i, j)] * da[j];
+            t7 += Gt[j] * db[i][j];
+            t9 += gi[sym(i, j)] * graddiv[j];
+        }
+        const R t2 = contract_sym(c2[i], Au);
+        const R t8 = contract_sym(gi, hb[i]);
+        const R* f = u + (GTX + i) * cs + p;
+        const R v = R(-4.0 / 3.0) * alpha * t1 + R(2.0) * alpha * t2 + six_alpha_over_w * t3
+                    - R(2.0) * t4 + ADV<R, Closed, false>(f, G, c.ix, beta, bs) + R(2.0 / 3.0) * Gt[i] * div - t7 + t8
+                    + R(1.0 / 3.0) * t9;
+        R out = v + KO<R, Closed, false>(f, G, c.ix);
+        if (mat != nullptr) {
+            R gs = R(0);
+#pragma unroll
+            for (int j = 0; j < 3; ++j) gs += gi[sym(i, j)] * static_cast<R>(mat[(1 + j) * cs + p]);
+            out = out + R(-16.0 * kPi) * alpha * gs;
+        }
+        k[(GTX + i) * cs + p] = out;
     }
 }
 
@@ -1008,11 +1180,21 @@ static void launch_rhs_form(const R* u, const double* u64, double* k, R* d1, R* 
     }
     BSSN_LAUNCH_SET(KC_GAUGE, (k_rhs_gauge<R, false>), sb.interior, stream, u, u64, d1, k, G, sb.interior, nfield);
     BSSN_LAUNCH_SET(KC_GAUGE, (k_rhs_gauge<R, true>), sb.shell, stream, u, u64, d1, k, G, sb.shell, nfield);
-    BSSN_LAUNCH_SET(KC_KGT, (k_rhs_kgt<R, false>), sb.interior, stream, u, u64, d1, mat, k, G, sb.interior, nfield);
-    BSSN_LAUNCH_SET(KC_KGT, (k_rhs_kgt<R, true>), sb.shell, stream, u, u64, d1, mat, k, G, sb.shell, nfield);
-    BSSN_LAUNCH_SET(KC_AT, (k_rhs_at<R, false>), sb.interior, stream, u, u64, d1, dmp, mat, k, G, sb.interior,
-                    nfield);
-    BSSN_LAUNCH_SET(KC_AT, (k_rhs_at<R, true>), sb.shell, stream, u, u64, d1, dmp, mat, k, G, sb.shell, nfield);
+    if constexpr (kPerturbative<R>) {
+        // FP32 form: issue- and latency-bound, so the smaller split kernels run
+        // at higher occupancy.
+        BSSN_LAUNCH_SET(KC_KGT, (k_rhs_kgt<R, false>), sb.interior, stream, u, u64, d1, mat, k, G, sb.interior,
+                        nfield);
+        BSSN_LAUNCH_SET(KC_KGT, (k_rhs_kgt<R, true>), sb.shell, stream, u, u64, d1, mat, k, G, sb.shell, nfield);
+        BSSN_LAUNCH_SET(KC_AT, (k_rhs_at<R, false>), sb.interior, stream, u, u64, d1, dmp, mat, k, G, sb.interior,
+                        nfield);
+        BSSN_LAUNCH_SET(KC_AT, (k_rhs_at<R, true>), sb.shell, stream, u, u64, d1, dmp, mat, k, G, sb.shell, nfield);
+    } else {
+        BSSN_LAUNCH_SET(KC_CURV, (k_rhs_curv<R, false>), sb.interior, stream, u, u64, d1, dmp, mat, k, G,
+                        sb.interior, nfield);
+        BSSN_LAUNCH_SET(KC_CURV, (k_rhs_curv<R, true>), sb.shell, stream, u, u64, d1, dmp, mat, k, G, sb.shell,
+                        nfield);
+    }
     if (G.any_sommerfeld) {
         const BoxSet S = face_slabs(G, box);
         BSSN_LAUNCH_SET(KC_SOMMERFELD, k_sommerfeld<R>, S, stream, u, k, G, S);

@@ -260,7 +260,7 @@ __device__ __forceinline__ R D2(const R* __restrict__ p, const Geo& G, int d, in
     if (r == 1) return closure(p, s, -1, L1) * inv_dx2;
     constexpr int o4[5] = {2, 1, 0, -1, -2};
     constexpr double c4[5] = {-1.0, 16.0, -30.0, 16.0, -1.0};
-    const R d4 = (!Closed && !Exact ? d2_num_pairs(p, s) : ordered(p, s, o4, c4)) * BSSN_CO(R, G, inv_12dx2);
+    const R d4 = (Exact ? ordered(p, s, o4, c4) : d2_num_pairs(p, s)) * BSSN_CO(R, G, inv_12dx2);
     if (!a.mad) return d4;
     constexpr int o6[7] = {3, 2, 1, 0, -1, -2, -3};
     constexpr double c6[7] = {1.0 / 90.0, -3.0 / 20.0, 3.0 / 2.0, -49.0 / 18.0,
@@ -273,7 +273,7 @@ __device__ __forceinline__ R D2(const R* __restrict__ p, const Geo& G, int d, in
 // undivided sixth difference along one axis (one KO numerator; the factor
 // nu/64 * h^5/dx^6 is applied once to the sum over axes)
 // ---------------------------------------------------------------------------
-template <typename R, bool Closed = true>
+template <typename R, bool Closed = true, bool Exact = true>
 __device__ __forceinline__ R KO1(const R* __restrict__ p, const Geo& G, int d, int i) {
     const Axis& a = G.ax[d];
     if (a.reduced) return R(0);
@@ -294,10 +294,12 @@ __device__ __forceinline__ R KO1(const R* __restrict__ p, const Geo& G, int d, i
         if (r == 0) num = closure(p, s, 0, L0);
         else if (r == 1) num = closure(p, s, -1, L1);
         else if (r == 2) num = closure(p, s, -2, L2);
-        else {
+        else if (Exact) {
             constexpr int o[7] = {3, 2, 1, 0, -1, -2, -3};
             constexpr double c[7] = {1.0, -6.0, 15.0, -20.0, 15.0, -6.0, 1.0};
             num = ordered(p, s, o, c);
+        } else {
+            num = ko_num_pairs(p, s);
         }
     }
     return num;
@@ -314,14 +316,14 @@ __device__ __forceinline__ R KO(const R* __restrict__ p, const Geo& G, const int
         for (int d = 0; d < 3; ++d) t[d] = G.ax[d].reduced ? R(0) : ko_num_pairs(p, G.st[d]);
         return BSSN_CO(R, G, ko_scale) * ((t[0] + t[1]) + t[2]);
     }
-    const R t = KO1<R, Closed>(p, G, 0, ix[0]) + KO1<R, Closed>(p, G, 1, ix[1]);
-    return BSSN_CO(R, G, ko_scale) * (t + KO1<R, Closed>(p, G, 2, ix[2]));
+    const R t = KO1<R, Closed, Exact>(p, G, 0, ix[0]) + KO1<R, Closed, Exact>(p, G, 1, ix[1]);
+    return BSSN_CO(R, G, ko_scale) * (t + KO1<R, Closed, Exact>(p, G, 2, ix[2]));
 }
 
 // ---------------------------------------------------------------------------
 // upwind first derivative selected by the sign of the RHS coefficient c
 // ---------------------------------------------------------------------------
-template <typename R, bool Closed = true>
+template <typename R, bool Closed = true, bool Exact = true>
 __device__ __forceinline__ R UP1(const R* __restrict__ p, const Geo& G, int d, int i, R c) {
     const Axis& a = G.ax[d];
     if (a.reduced) return R(0);
@@ -344,7 +346,7 @@ __device__ __forceinline__ R UP1(const R* __restrict__ p, const Geo& G, int d, i
     if (c > R(0)) {
         constexpr int o[5] = {-1, 0, 1, 2, 3};
         constexpr double k[5] = {-3.0, -10.0, 18.0, -6.0, 1.0};
-        const R d4 = ordered(p, s, o, k) * inv_12dx;
+        const R d4 = (Exact ? ordered(p, s, o, k) : up1_num_fused(p, s, c)) * inv_12dx;
         if (!a.mad) return d4;
         constexpr int o6[7] = {-2, -1, 0, 1, 2, 3, 4};
         constexpr double k6[7] = {2.0, -24.0, -35.0, 80.0, -30.0, 8.0, -1.0};
@@ -353,7 +355,7 @@ __device__ __forceinline__ R UP1(const R* __restrict__ p, const Geo& G, int d, i
     if (c < R(0)) {
         constexpr int o[5] = {-3, -2, -1, 0, 1};
         constexpr double k[5] = {-1.0, 6.0, -18.0, 10.0, 3.0};
-        const R d4 = ordered(p, s, o, k) * inv_12dx;
+        const R d4 = (Exact ? ordered(p, s, o, k) : up1_num_fused(p, s, c)) * inv_12dx;
         if (!a.mad) return d4;
         constexpr int o6[7] = {-4, -3, -2, -1, 0, 1, 2};
         constexpr double k6[7] = {1.0, -8.0, 30.0, -80.0, 35.0, 24.0, -2.0};
@@ -399,7 +401,7 @@ __device__ __forceinline__ R ADV(const R* __restrict__ p, const Geo& G, const in
             t[d] = a.reduced ? R(0)
                              : bs[d] * (Exact ? up1_num(p, G.st[d], beta[d]) : up1_num_fused(p, G.st[d], beta[d]));
         else
-            t[d] = beta[d] * UP1<R, Closed>(p, G, d, ix[d], beta[d]);
+            t[d] = beta[d] * UP1<R, Closed, Exact>(p, G, d, ix[d], beta[d]);
     }
     return (t[0] + t[1]) + t[2];
 }
