@@ -42,19 +42,29 @@ __host__ __device__ constexpr int mix_source(int f) {
 // derived-field buffer.  Indexed after the NMIX base set.
 constexpr int NMIX_MOM = 16;
 
-// Compute box: linear thread index -> padded (x, y, z), z fastest.
+// Compute box: linear thread index -> padded (x, y, z).  `fast` names the
+// fastest-varying axis: z (2, the default and the memory order), y (1, then z,
+// then x) or x (0, then z, then y).  Shell slabs thin in z or y run with
+// another fast axis so that the samples of a warp share their closure rows.
 struct Box {
     int lo[3];
     int n[3];
     long long count;
+    int fast = 2;
     __device__ __forceinline__ void coords(long long t, int (&ix)[3]) const {
-        const long long yz = (long long)n[1] * n[2];
-        const int x = (int)(t / yz);
-        const long long r = t - (long long)x * yz;
-        const int y = (int)(r / n[2]);
-        ix[0] = lo[0] + x;
-        ix[1] = lo[1] + y;
-        ix[2] = lo[2] + (int)(r - (long long)y * n[2]);
+        int a, b, c;  // slowest, middle, fastest extents' indices
+        if (fast == 2) { a = 0; b = 1; c = 2; }
+        else if (fast == 1) { a = 0; b = 2; c = 1; }
+        else { a = 1; b = 2; c = 0; }
+        const int nb = n[b], nc = n[c];
+        const long long bc = (long long)nb * nc;
+        const int ia = (int)(t / bc);
+        const long long r = t - (long long)ia * bc;
+        const int ib = (int)(r / nc);
+        const int ic = (int)(r - (long long)ib * nc);
+        if (fast == 2) { ix[0] = lo[0] + ia; ix[1] = lo[1] + ib; ix[2] = lo[2] + ic; }
+        else if (fast == 1) { ix[0] = lo[0] + ia; ix[2] = lo[2] + ib; ix[1] = lo[1] + ic; }
+        else { ix[1] = lo[1] + ia; ix[2] = lo[2] + ib; ix[0] = lo[0] + ic; }
     }
 };
 

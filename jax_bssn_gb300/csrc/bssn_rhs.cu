@@ -60,7 +60,7 @@ __device__ __forceinline__ bool in_range(const Axis& a, int i) { return i >= a.l
 
 // Up to six boxes covered by one launch; blockIdx.y selects the box.
 struct BoxSet {
-    Box b[6];
+    Box b[10];
     int n;
 };
 
@@ -1039,8 +1039,9 @@ static int composition_reach(const Geo& G) {
 
 static inline unsigned blocks_for(long long n) { return (unsigned)((n + kThreads - 1) / kThreads); }
 
-static Box make_box(const int lo[3], const int hi[3]) {
+static Box make_box(const int lo[3], const int hi[3], int fast = 2) {
     Box b;
+    b.fast = fast;
     b.count = 1;
     for (int d = 0; d < 3; ++d) {
         b.lo[d] = lo[d];
@@ -1062,12 +1063,12 @@ static long long largest(const BoxSet& S) {
 
 // A box split into its interior -- samples at least kClosureRows from every
 // closed (Sommerfeld) owned face, where no stencil needs a one-sided closure --
-// and the rest of the box as up to six slabs.
+// and the rest of the box as up to ten slabs.
 struct SplitBox {
     BoxSet interior, shell;
 };
 
-static SplitBox split_box(const Geo& G, const Box& box) {
+static SplitBox split_box(const Geo& G, const Box& box, bool coalesced) {
     int blo[3], bhi[3], lo[3], hi[3];
     for (int d = 0; d < 3; ++d) {
         const Axis& a = G.ax[d];
@@ -1084,18 +1085,51 @@ static SplitBox split_box(const Geo& G, const Box& box) {
     S.interior.n = 0;
     S.shell.n = 0;
     add_box(S.interior, make_box(lo, hi));
-    // x slabs over the whole box in y and z; y slabs inside x; z slabs inside x and y
-    for (int d = 0; d < 3; ++d) {
-        int l0[3], h0[3], l1[3], h1[3];
-        for (int e = 0; e < 3; ++e) {
-            const bool inner = e < d;   // axes already sliced take the interior range
-            l0[e] = l1[e] = inner ? lo[e] : blo[e];
-            h0[e] = h1[e] = inner ? hi[e] : bhi[e];
+    if (coalesced) {
+        // z fastest everywhere (coalesced loads, for the load-bound FP32
+        // form): x slabs over the whole box in y and z, y slabs inside x, z
+        // slabs inside x and y.
+        for (int d = 0; d < 3; ++d) {
+            int l0[3], h0[3], l1[3], h1[3];
+            for (int e = 0; e < 3; ++e) {
+                const bool inner = e < d;   // axes already sliced take the interior range
+                l0[e] = l1[e] = inner ? lo[e] : blo[e];
+                h0[e] = h1[e] = inner ? hi[e] : bhi[e];
+            }
+            l0[d] = blo[d]; h0[d] = lo[d];
+            l1[d] = hi[d];  h1[d] = bhi[d];
+            add_box(S.shell, make_box(l0, h0));
+            add_box(S.shell, make_box(l1, h1));
         }
-        l0[d] = blo[d]; h0[d] = lo[d];
-        l1[d] = hi[d];  h1[d] = bhi[d];
-        add_box(S.shell, make_box(l0, h0));
-        add_box(S.shell, make_box(l1, h1));
+        return S;
+    }
+    // The shell (for the FP64 form, bound by FP64 instructions), cut so that the fast axis of every slab runs through the
+    // interior range of its axis: the 32 samples of a warp then share their
+    // closure rows (no divergent closure branches), except where a warp wraps
+    // to the next row.
+    //   z rows:  z in the closure rows, y interior, x whole box; y fastest
+    //   y rows:  y in the closure rows, z interior, x whole box; z fastest
+    //   yz rows: y and z in the closure rows, x whole box; x fastest
+    //   x rows:  x in the closure rows, y and z interior; z fastest
+    const int E0[2] = {blo[0], hi[0]}, E1[2] = {lo[0], bhi[0]};  // x closure ranges [E0, E1)
+    const int Y0[2] = {blo[1], hi[1]}, Y1[2] = {lo[1], bhi[1]};
+    const int Z0[2] = {blo[2], hi[2]}, Z1[2] = {lo[2], bhi[2]};
+    for (int f = 0; f < 2; ++f) {
+        const int l[3] = {blo[0], lo[1], Z0[f]}, h[3] = {bhi[0], hi[1], Z1[f]};
+        add_box(S.shell, make_box(l, h, 1));
+    }
+    for (int f = 0; f < 2; ++f) {
+        const int l[3] = {blo[0], Y0[f], lo[2]}, h[3] = {bhi[0], Y1[f], hi[2]};
+        add_box(S.shell, make_box(l, h, 2));
+    }
+    for (int f = 0; f < 2; ++f)
+        for (int e = 0; e < 2; ++e) {
+            const int l[3] = {blo[0], Y0[f], Z0[e]}, h[3] = {bhi[0], Y1[f], Z1[e]};
+            add_box(S.shell, make_box(l, h, 0));
+        }
+    for (int f = 0; f < 2; ++f) {
+        const int l[3] = {E0[f], lo[1], lo[2]}, h[3] = {E1[f], hi[1], hi[2]};
+        add_box(S.shell, make_box(l, h, 2));
     }
     return S;
 }
@@ -1167,10 +1201,13 @@ static void launch_rhs_form(const R* u, const double* u64, double* k, R* d1, R* 
         BSSN_LAUNCH(KC_MOM_DERIVED, k_mom_derived<R>, blocks_for(region.count), kThreads, stream, u, u64, der, G,
                     region);
     }
-    const SplitBox se = split_box(G, ext);
+    // The FP64 form is bound by FP64 instructions, so its shell slabs avoid
+    // divergent closure branches; the FP32 form keeps coalesced slabs.
+    const bool coalesced = kPerturbative<R>;
+    const SplitBox se = split_box(G, ext, coalesced);
     BSSN_LAUNCH_SET(KC_FIRST, (k_first_derivs<R, false>), se.interior, stream, u, der, d1, G, se.interior, with_mom);
     BSSN_LAUNCH_SET(KC_FIRST, (k_first_derivs<R, true>), se.shell, stream, u, der, d1, G, se.shell, with_mom);
-    const SplitBox sb = split_box(G, box);
+    const SplitBox sb = split_box(G, box, coalesced);
     const R* dmp = with_mom ? static_cast<const R*>(damp) : nullptr;
     if (with_mom) {
         BSSN_LAUNCH_SET(KC_MOM_DAMP, (k_mom_damping<R, false>), sb.interior, stream, u, u64, der, d1, mat, damp, G,
