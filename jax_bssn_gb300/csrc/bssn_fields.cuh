@@ -51,7 +51,21 @@ struct Box {
     int n[3];
     long long count;
     int fast = 2;
+    // z fastest (interior boxes always are)
+    __device__ __forceinline__ void coords_z(long long t, int (&ix)[3]) const {
+        const long long yz = (long long)n[1] * n[2];
+        const int x = (int)(t / yz);
+        const long long r = t - (long long)x * yz;
+        const int y = (int)(r / n[2]);
+        ix[0] = lo[0] + x;
+        ix[1] = lo[1] + y;
+        ix[2] = lo[2] + (int)(r - (long long)y * n[2]);
+    }
     __device__ __forceinline__ void coords(long long t, int (&ix)[3]) const {
+        if (fast == 2) {
+            coords_z(t, ix);
+            return;
+        }
         int a, b, c;  // slowest, middle, fastest extents' indices
         if (fast == 2) { a = 0; b = 1; c = 2; }
         else if (fast == 1) { a = 0; b = 2; c = 1; }

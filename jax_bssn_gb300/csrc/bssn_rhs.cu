@@ -50,6 +50,14 @@ constexpr bool kPerturbative = std::is_same<R, float>::value;
 // take the regrouped interior numerators.
 template <typename R>
 constexpr bool kExactBg = !kPerturbative<R>;
+
+// Unrolling of the gauge kernel's per-component loops: the FP32 form is
+// issue-bound there, and full unrolling turns runtime component indices into
+// constants (the larger curvature kernels lose more to occupancy and
+// instruction fetch than they gain); the FP64 form is bound by FP64
+// instructions and keeps compact loops.
+template <typename R>
+constexpr int kUnroll = kPerturbative<R> ? 8 : 1;
 __host__ __device__ constexpr bool unit_diagonal(int s) { return s == 0 || s == 3 || s == 5; }
 
 __host__ __device__ constexpr bool has_background(int c) {
@@ -111,7 +119,8 @@ k_first_derivs(const R* __restrict__ u, const R* __restrict__ der, R* __restrict
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ext.count) return;
     int ix[3];
-    ext.coords(t, ix);
+    if constexpr (Closed) ext.coords(t, ix);
+    else ext.coords_z(t, ix);
     const long long p = lin(G, ix);
     const long long cs = G.cs;
     const int nfield = with_mom ? NMIX + NMIX_MOM : NMIX;
@@ -137,10 +146,13 @@ struct PointCtx {
     long long p;
 };
 
+// AnyOrder = false: the box is known to run z fastest (closure-free interior boxes).
+template <bool AnyOrder = true>
 __device__ __forceinline__ bool point(const Box& B, PointCtx& c, const Geo& G) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= B.count) return false;
-    B.coords(t, c.ix);
+    if constexpr (AnyOrder) B.coords(t, c.ix);
+    else B.coords_z(t, c.ix);
     c.p = lin(G, c.ix);
     return true;
 }
@@ -314,7 +326,7 @@ __global__ void __launch_bounds__(kThreads)
 k_rhs_gauge(const R* __restrict__ u, const double* __restrict__ u64, const R* __restrict__ d1,
             double* __restrict__ k, Geo G, BoxSet S, int nfield) {
     PointCtx c;
-    if (!point(S.b[blockIdx.y], c, G)) return;
+    if (!point<Closed>(S.b[blockIdx.y], c, G)) return;
     const long long cs = G.cs, p = c.p;
     const R beta[3] = {u[BX * cs + p], u[BY * cs + p], u[BZ * cs + p]};
     R bs[3];
@@ -345,7 +357,7 @@ k_rhs_gauge(const R* __restrict__ u, const double* __restrict__ u64, const R* __
                 P[s] = lie + m23div * g[s] + m2a * u[(AXX + s) * cs + p];
             }
     }
-#pragma unroll 1
+#pragma unroll (kUnroll<R>)
     for (int s = 0; s < 6; ++s) {
         const R* f = u + (GXX + s) * cs + p;
         R v;
@@ -367,7 +379,7 @@ k_rhs_gauge(const R* __restrict__ u, const double* __restrict__ u64, const R* __
         k[CALPHA * cs + p] = slicing + ADV<R, Closed, kExactBg<R>>(f, G, c.ix, beta, bs)
                              + KO<R, Closed, kExactBg<R>>(f, G, c.ix);
     }
-#pragma unroll 1
+#pragma unroll (kUnroll<R>)
     for (int i = 0; i < 3; ++i) {
         const R* f = u + (BX + i) * cs + p;
         R v;
@@ -390,7 +402,7 @@ __global__ void __launch_bounds__(kThreads)
 k_rhs_kgt(const R* __restrict__ u, const double* __restrict__ u64, const R* __restrict__ d1,
           const double* __restrict__ mat, double* __restrict__ k, Geo G, BoxSet S, int nfield) {
     PointCtx c;
-    if (!point(S.b[blockIdx.y], c, G)) return;
+    if (!point<Closed>(S.b[blockIdx.y], c, G)) return;
     const long long cs = G.cs, p = c.p;
     R g[6], gi[6];
     load_sym(u, GXX, G, p, g);
@@ -514,7 +526,7 @@ k_rhs_at(const R* __restrict__ u, const double* __restrict__ u64, const R* __res
          const R* __restrict__ damp, const double* __restrict__ mat, double* __restrict__ k, Geo G, BoxSet S,
          int nfield) {
     PointCtx c;
-    if (!point(S.b[blockIdx.y], c, G)) return;
+    if (!point<Closed>(S.b[blockIdx.y], c, G)) return;
     const long long cs = G.cs, p = c.p;
     R g[6], gi[6];
     load_sym(u, GXX, G, p, g);
@@ -612,7 +624,7 @@ k_rhs_curv(const R* __restrict__ u, const double* __restrict__ u64, const R* __r
            const R* __restrict__ damp, const double* __restrict__ mat, double* __restrict__ k, Geo G, BoxSet S,
            int nfield) {
     PointCtx c;
-    if (!point(S.b[blockIdx.y], c, G)) return;
+    if (!point<Closed>(S.b[blockIdx.y], c, G)) return;
     const long long cs = G.cs, p = c.p;
     R g[6], gi[6];
     load_sym(u, GXX, G, p, g);
@@ -800,7 +812,7 @@ k_mom_damping(const R* __restrict__ u, const double* __restrict__ u64, const R* 
               const R* __restrict__ d1, const double* __restrict__ mat, R* __restrict__ damp, Geo G, BoxSet S,
               int nfield) {
     PointCtx c;
-    if (!point(S.b[blockIdx.y], c, G)) return;
+    if (!point<Closed>(S.b[blockIdx.y], c, G)) return;
     const long long cs = G.cs, p = c.p;
     const int fA = NMIX, fK = NMIX + 6, fB = NMIX + 7;
     R gi[6];
