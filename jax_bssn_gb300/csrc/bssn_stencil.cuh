@@ -235,6 +235,22 @@ __device__ __forceinline__ R ko_num_pairs(const R* __restrict__ p, long long s) 
     const R p3 = ld(p, 3 * s) + ld(p, -3 * s);
     return ((p3 + R(-6) * p2) + R(15) * p1) + R(-20) * ld(p, 0);
 }
+// Sixth-order D2 numerator (MAD blend) in symmetric pairs.
+template <typename R>
+__device__ __forceinline__ R d2_6_num_pairs(const R* __restrict__ p, long long s) {
+    const R p1 = ld(p, s) + ld(p, -s);
+    const R p2 = ld(p, 2 * s) + ld(p, -2 * s);
+    const R p3 = ld(p, 3 * s) + ld(p, -3 * s);
+    return ((R(1.0 / 90.0) * p3 + R(-3.0 / 20.0) * p2) + R(3.0 / 2.0) * p1) + R(-49.0 / 18.0) * ld(p, 0);
+}
+// Any numerator as a fused multiply-add chain.
+template <typename R, int N>
+__device__ __forceinline__ R fused(const R* __restrict__ p, long long s, const int (&off)[N], const double (&c)[N]) {
+    R acc = static_cast<R>(c[0]) * ld(p, off[0] * s);
+#pragma unroll
+    for (int t = 1; t < N; ++t) acc = acc + static_cast<R>(c[t]) * ld(p, off[t] * s);
+    return acc;
+}
 template <typename R>
 __device__ __forceinline__ R up1_num_fused(const R* __restrict__ p, long long s, R c) {
     if (c > R(0))
@@ -265,7 +281,7 @@ __device__ __forceinline__ R D2(const R* __restrict__ p, const Geo& G, int d, in
     constexpr int o6[7] = {3, 2, 1, 0, -1, -2, -3};
     constexpr double c6[7] = {1.0 / 90.0, -3.0 / 20.0, 3.0 / 2.0, -49.0 / 18.0,
                               3.0 / 2.0, -3.0 / 20.0, 1.0 / 90.0};
-    const R d6 = ordered(p, s, o6, c6) * inv_dx2;
+    const R d6 = (Exact ? ordered(p, s, o6, c6) : d2_6_num_pairs(p, s)) * inv_dx2;
     return BSSN_AQ(R, a) * d4 + BSSN_AOMQ(R, a) * d6;
 }
 
@@ -350,7 +366,8 @@ __device__ __forceinline__ R UP1(const R* __restrict__ p, const Geo& G, int d, i
         if (!a.mad) return d4;
         constexpr int o6[7] = {-2, -1, 0, 1, 2, 3, 4};
         constexpr double k6[7] = {2.0, -24.0, -35.0, 80.0, -30.0, 8.0, -1.0};
-        return BSSN_AQ(R, a) * d4 + BSSN_AOMQ(R, a) * (ordered(p, s, o6, k6) * BSSN_CO(R, G, inv_60dx));
+        const R n6 = Exact ? ordered(p, s, o6, k6) : fused(p, s, o6, k6);
+        return BSSN_AQ(R, a) * d4 + BSSN_AOMQ(R, a) * (n6 * BSSN_CO(R, G, inv_60dx));
     }
     if (c < R(0)) {
         constexpr int o[5] = {-3, -2, -1, 0, 1};
@@ -359,7 +376,8 @@ __device__ __forceinline__ R UP1(const R* __restrict__ p, const Geo& G, int d, i
         if (!a.mad) return d4;
         constexpr int o6[7] = {-4, -3, -2, -1, 0, 1, 2};
         constexpr double k6[7] = {1.0, -8.0, 30.0, -80.0, 35.0, 24.0, -2.0};
-        return BSSN_AQ(R, a) * d4 + BSSN_AOMQ(R, a) * (ordered(p, s, o6, k6) * BSSN_CO(R, G, inv_60dx));
+        const R n6 = Exact ? ordered(p, s, o6, k6) : fused(p, s, o6, k6);
+        return BSSN_AQ(R, a) * d4 + BSSN_AOMQ(R, a) * (n6 * BSSN_CO(R, G, inv_60dx));
     }
     // zero coefficient (or NaN): centred (JAX_BSSN/evolution/derivatives.py:238-241,272-276)
     return d1_interior(p, s, a, G, a.mad != 0);
