@@ -66,19 +66,16 @@ struct Box {
             coords_z(t, ix);
             return;
         }
-        int a, b, c;  // slowest, middle, fastest extents' indices
-        if (fast == 2) { a = 0; b = 1; c = 2; }
-        else if (fast == 1) { a = 0; b = 2; c = 1; }
-        else { a = 1; b = 2; c = 0; }
-        const int nb = n[b], nc = n[c];
-        const long long bc = (long long)nb * nc;
+        // fast = 1: order (x, z, y); fast = 0: order (y, z, x) -- z is the middle axis
+        const int nc = n[fast];
+        const long long bc = (long long)n[2] * nc;
         const int ia = (int)(t / bc);
         const long long r = t - (long long)ia * bc;
         const int ib = (int)(r / nc);
         const int ic = (int)(r - (long long)ib * nc);
-        if (fast == 2) { ix[0] = lo[0] + ia; ix[1] = lo[1] + ib; ix[2] = lo[2] + ic; }
-        else if (fast == 1) { ix[0] = lo[0] + ia; ix[2] = lo[2] + ib; ix[1] = lo[1] + ic; }
-        else { ix[1] = lo[1] + ia; ix[2] = lo[2] + ib; ix[0] = lo[0] + ic; }
+        ix[2] = lo[2] + ib;
+        if (fast == 1) { ix[0] = lo[0] + ia; ix[1] = lo[1] + ic; }
+        else { ix[1] = lo[1] + ia; ix[0] = lo[0] + ic; }
     }
 };
 
