@@ -20,16 +20,23 @@
 //   k_sommerfeld     radial Sommerfeld replacement on active owned faces
 //                    (JAX_BSSN/evolution/boundaries.py:150-171)
 // Operators commute along different axes, so each mixed derivative is formed
-// once (outer axis = the larger index) and used for both orderings.
+// once (outer axis = the larger index, as in the reference's upper triangle)
+// and used for both orderings.  (The reference also forms the other ordering;
+// on the second row from a Sommerfeld face that one applies the one-sided
+// closure to O(1) samples, so its lower-triangle entries differ from the
+// upper ones by that closure's rounding.)
 //
 // Two arithmetic forms share this source (template parameter R):
 //   double  the plain FP64 form; kernels read the FP64 state directly.
 //   float   the FP32-arithmetic form: k_perturb first writes the state as
-//           float perturbations about the constant background (1 for the
-//           conformal-metric diagonal, W and alpha; 0 otherwise), so small
+//           float perturbations about a constant background (1 for the
+//           conformal-metric diagonal, W and alpha; the state's own value at
+//           the box's first sample for the shift and K, so a uniform shift or
+//           a constant-K slice is removed too; 0 otherwise), so small
 //           deviations keep float's relative precision through every
-//           stencil; the algebra then runs in float.  W and alpha enter the
-//           pointwise terms as full values read from the FP64 state, and 1/W
+//           stencil; the algebra then runs in float.  W, alpha, the shift and
+//           K enter the pointwise terms as full values read from the FP64
+//           state, and 1/W
 //           (large near punctures) is formed in FP64.  The RHS is written in
 //           FP64, and the RK4 combination stays FP64.
 #include "bssn_fields.cuh"
@@ -44,10 +51,11 @@ constexpr double kPi = 3.141592653589793;   // the double nearest pi (numpy.pi)
 template <typename R>
 constexpr bool kPerturbative = std::is_same<R, float>::value;
 
-// Stencil numerators keep the reference's rounding for fields with a unit
-// background (diagonal gt, W, alpha) in the FP64 form; fields with a zero
-// background, and every field of the FP32 form (which stores perturbations),
-// take the regrouped interior numerators.
+// Stencil numerators keep the reference's rounding, in the FP64 form, for the
+// fields that can carry a constant background: the unit diagonal of gt, W and
+// alpha, and the shift (a uniform shift is a constant background too).  Fields
+// whose background is zero (At, K, Gt, the off-diagonal gt), and every field of
+// the FP32 form (which stores perturbations), take the regrouped numerators.
 template <typename R>
 constexpr bool kExactBg = !kPerturbative<R>;
 
@@ -63,6 +71,11 @@ __host__ __device__ constexpr bool unit_diagonal(int s) { return s == 0 || s == 
 __host__ __device__ constexpr bool has_background(int c) {
     return c == GXX || c == GYY || c == GZZ || c == CW || c == CALPHA;
 }
+// FP32 form: components whose perturbation is taken about their own value at
+// one sample of the state (a uniform shift, a constant-K slice).
+__host__ __device__ constexpr bool state_background(int c) {
+    return c == BX || c == BY || c == BZ || c == CK;
+}
 
 __device__ __forceinline__ bool in_range(const Axis& a, int i) { return i >= a.lo && i < a.hi; }
 
@@ -72,12 +85,21 @@ struct BoxSet {
     int n;
 };
 
-// Full value of component c at sample p of the R-typed state.
+// The point a thread works on.
+struct PointCtx {
+    int ix[3];
+    long long p;
+};
+
+// Full value of component comp at the point of the R-typed state: the FP32
+// form adds back the unit background of the metric diagonal, W and alpha
+// (the shift and K, whose background is taken from the state, are read in
+// FP64 by full_exact).
 template <typename R>
-__device__ __forceinline__ R full(const R* __restrict__ u, int c, long long cs, long long p) {
-    R v = u[c * cs + p];
+__device__ __forceinline__ R full(const R* __restrict__ u, int comp, const Geo& G, const PointCtx& c) {
+    R v = u[comp * G.cs + c.p];
     if constexpr (kPerturbative<R>) {
-        if (has_background(c)) v += R(1);
+        if (has_background(comp)) v += R(1);
     }
     return v;
 }
@@ -95,7 +117,7 @@ __device__ __forceinline__ R full_exact(const R* __restrict__ u, const double* _
 // FP32 form: float perturbations of the state on a region
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kThreads)
-k_perturb(const double* __restrict__ u, float* __restrict__ uf, Geo G, Box region) {
+k_perturb(const double* __restrict__ u, float* __restrict__ uf, Geo G, Box region, long long p0) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= region.count) return;
     int ix[3];
@@ -103,8 +125,8 @@ k_perturb(const double* __restrict__ u, float* __restrict__ uf, Geo G, Box regio
     const long long p = lin(G, ix), cs = G.cs;
 #pragma unroll
     for (int c = 0; c < NCOMP; ++c) {
-        const double v = u[c * cs + p];
-        uf[c * cs + p] = static_cast<float>(has_background(c) ? v - 1.0 : v);
+        const double b = has_background(c) ? 1.0 : (state_background(c) ? u[c * cs + p0] : 0.0);
+        uf[c * cs + p] = static_cast<float>(u[c * cs + p] - b);
     }
 }
 
@@ -140,11 +162,6 @@ k_first_derivs(const R* __restrict__ u, const R* __restrict__ der, R* __restrict
         }
     }
 }
-
-struct PointCtx {
-    int ix[3];
-    long long p;
-};
 
 // AnyOrder = false: the box is known to run z fastest (closure-free interior boxes).
 template <bool AnyOrder = true>
@@ -215,9 +232,10 @@ __device__ __forceinline__ void w2_lapse_hessian(const R* __restrict__ u, const 
 }
 
 template <typename R>
-__device__ __forceinline__ void load_sym(const R* __restrict__ u, int base, const Geo& G, long long p, R (&v)[6]) {
+__device__ __forceinline__ void load_sym(const R* __restrict__ u, int base, const Geo& G, const PointCtx& c,
+                                         R (&v)[6]) {
 #pragma unroll
-    for (int s = 0; s < 6; ++s) v[s] = full(u, base + s, G.cs, p);
+    for (int s = 0; s < 6; ++s) v[s] = full(u, base + s, G, c);
 }
 
 template <typename R>
@@ -255,7 +273,7 @@ __device__ __forceinline__ void w2_ricci(const R* __restrict__ u, const R* d1, c
         }
     }
     {
-        const R Gt[3] = {u[GTX * cs + p], u[GTY * cs + p], u[GTZ * cs + p]};
+        const R Gt[3] = {full(u, GTX, G, c), full(u, GTY, G, c), full(u, GTZ, G, c)};
         R dG[3][3];  // dG[d][i] = d_d Gt^i
 #pragma unroll 1
         for (int d = 0; d < 3; ++d)
@@ -328,7 +346,7 @@ k_rhs_gauge(const R* __restrict__ u, const double* __restrict__ u64, const R* __
     PointCtx c;
     if (!point<Closed>(S.b[blockIdx.y], c, G)) return;
     const long long cs = G.cs, p = c.p;
-    const R beta[3] = {u[BX * cs + p], u[BY * cs + p], u[BZ * cs + p]};
+    const R beta[3] = {full_exact(u, u64, BX, cs, p), full_exact(u, u64, BY, cs, p), full_exact(u, u64, BZ, cs, p)};
     R bs[3];
     shift_over_12dx(G, beta, bs);
     R db[3][3];  // db[i][j] = d_j beta^i
@@ -338,10 +356,10 @@ k_rhs_gauge(const R* __restrict__ u, const double* __restrict__ u64, const R* __
         for (int j = 0; j < 3; ++j) db[i][j] = d1ptr(d1, G, nfield, j, MIX_B + i, p)[0];
     const R div = db[0][0] + db[1][1] + db[2][2];
     const R alpha = full_exact(u, u64, CALPHA, cs, p);
-    const R K = u[CK * cs + p];
+    const R K = full_exact(u, u64, CK, cs, p);
     const R W = full_exact(u, u64, CW, cs, p);
     R g[6];
-    load_sym(u, GXX, G, p, g);
+    load_sym(u, GXX, G, c, g);
 
     R P[6];  // pointwise terms: Lie terms - 2/3 gt_ij div beta - 2 alpha At_ij
     {
@@ -354,7 +372,7 @@ k_rhs_gauge(const R* __restrict__ u, const double* __restrict__ u64, const R* __
 #pragma unroll
                 for (int m = 0; m < 3; ++m) lie += g[sym(m, i)] * db[m][j] + g[sym(m, j)] * db[m][i];
                 const int s = sym(i, j);
-                P[s] = lie + m23div * g[s] + m2a * u[(AXX + s) * cs + p];
+                P[s] = lie + m23div * g[s] + m2a * full(u, AXX + s, G, c);
             }
     }
 #pragma unroll (kUnroll<R>)
@@ -386,9 +404,9 @@ k_rhs_gauge(const R* __restrict__ u, const double* __restrict__ u64, const R* __
         if (G.zero_shift) {
             v = R(0) * beta[i];
         } else {
-            v = BSSN_CO(R, G, g) * u[(GTX + i) * cs + p] + ADV<R, Closed, false>(f, G, c.ix, beta, bs)
+            v = BSSN_CO(R, G, g) * full(u, GTX + i, G, c) + ADV<R, Closed, kExactBg<R>>(f, G, c.ix, beta, bs)
                 + (-BSSN_CO(R, G, eta)) * beta[i];
-            v = v + KO<R, Closed, false>(f, G, c.ix);
+            v = v + KO<R, Closed, kExactBg<R>>(f, G, c.ix);
         }
         k[(BX + i) * cs + p] = v;
     }
@@ -405,7 +423,7 @@ k_rhs_kgt(const R* __restrict__ u, const double* __restrict__ u64, const R* __re
     if (!point<Closed>(S.b[blockIdx.y], c, G)) return;
     const long long cs = G.cs, p = c.p;
     R g[6], gi[6];
-    load_sym(u, GXX, G, p, g);
+    load_sym(u, GXX, G, c, g);
     inverse_metric(g, gi);
     R c1[3][6], c2[3][6];
     {
@@ -422,12 +440,12 @@ k_rhs_kgt(const R* __restrict__ u, const double* __restrict__ u64, const R* __re
     }
     const R W = full_exact(u, u64, CW, cs, p);
     const R alpha = full_exact(u, u64, CALPHA, cs, p);
-    const R K = u[CK * cs + p];
-    const R beta[3] = {u[BX * cs + p], u[BY * cs + p], u[BZ * cs + p]};
+    const R K = full_exact(u, u64, CK, cs, p);
+    const R beta[3] = {full_exact(u, u64, BX, cs, p), full_exact(u, u64, BY, cs, p), full_exact(u, u64, BZ, cs, p)};
     R bs[3];
     shift_over_12dx(G, beta, bs);
     R A[6];
-    load_sym(u, AXX, G, p, A);
+    load_sym(u, AXX, G, c, A);
     R Au[6];  // A^ij = g^ik (A_kl g^lj)
     {
         R M[3][3];  // M[k][j] = A_kl g^lj
@@ -483,11 +501,11 @@ k_rhs_kgt(const R* __restrict__ u, const double* __restrict__ u64, const R* __re
     }
     R hb[3][6];  // hb[i][sym(m,n)] = d_m d_n beta^i
 #pragma unroll 1
-    for (int i = 0; i < 3; ++i) hessian<R, Closed, false>(u, d1, G, nfield, BX + i, MIX_B + i, c, hb[i]);
+    for (int i = 0; i < 3; ++i) hessian<R, Closed, kExactBg<R>>(u, d1, G, nfield, BX + i, MIX_B + i, c, hb[i]);
     R graddiv[3];
 #pragma unroll
     for (int m = 0; m < 3; ++m) graddiv[m] = hb[0][sym(m, 0)] + hb[1][sym(m, 1)] + hb[2][sym(m, 2)];
-    const R Gt[3] = {u[GTX * cs + p], u[GTY * cs + p], u[GTZ * cs + p]};
+    const R Gt[3] = {full(u, GTX, G, c), full(u, GTY, G, c), full(u, GTZ, G, c)};
 #pragma unroll 1
     for (int i = 0; i < 3; ++i) {
         R t1 = R(0), t3 = R(0), t4 = R(0), t7 = R(0), t9 = R(0);
@@ -529,7 +547,7 @@ k_rhs_at(const R* __restrict__ u, const double* __restrict__ u64, const R* __res
     if (!point<Closed>(S.b[blockIdx.y], c, G)) return;
     const long long cs = G.cs, p = c.p;
     R g[6], gi[6];
-    load_sym(u, GXX, G, p, g);
+    load_sym(u, GXX, G, c, g);
     inverse_metric(g, gi);
     R c1[3][6], c2[3][6];
     {
@@ -567,10 +585,10 @@ k_rhs_at(const R* __restrict__ u, const double* __restrict__ u64, const R* __res
         for (int s = 0; s < 6; ++s) T[s] = T[s] - R(1.0 / 3.0) * g[s] * tr;
     }
     // --- remaining terms ---
-    const R K = u[CK * cs + p];
+    const R K = full_exact(u, u64, CK, cs, p);
     R A[6];
-    load_sym(u, AXX, G, p, A);
-    const R beta[3] = {u[BX * cs + p], u[BY * cs + p], u[BZ * cs + p]};
+    load_sym(u, AXX, G, c, A);
+    const R beta[3] = {full_exact(u, u64, BX, cs, p), full_exact(u, u64, BY, cs, p), full_exact(u, u64, BZ, cs, p)};
     R bs[3];
     shift_over_12dx(G, beta, bs);
     R db[3][3];
@@ -627,7 +645,7 @@ k_rhs_curv(const R* __restrict__ u, const double* __restrict__ u64, const R* __r
     if (!point<Closed>(S.b[blockIdx.y], c, G)) return;
     const long long cs = G.cs, p = c.p;
     R g[6], gi[6];
-    load_sym(u, GXX, G, p, g);
+    load_sym(u, GXX, G, c, g);
     inverse_metric(g, gi);
     R c1[3][6], c2[3][6];
     {
@@ -664,10 +682,10 @@ k_rhs_curv(const R* __restrict__ u, const double* __restrict__ u64, const R* __r
 #pragma unroll
         for (int s = 0; s < 6; ++s) T[s] = T[s] - R(1.0 / 3.0) * g[s] * tr;
     }
-    const R K = u[CK * cs + p];
+    const R K = full_exact(u, u64, CK, cs, p);
     R A[6];
-    load_sym(u, AXX, G, p, A);
-    const R beta[3] = {u[BX * cs + p], u[BY * cs + p], u[BZ * cs + p]};
+    load_sym(u, AXX, G, c, A);
+    const R beta[3] = {full_exact(u, u64, BX, cs, p), full_exact(u, u64, BY, cs, p), full_exact(u, u64, BZ, cs, p)};
     R bs[3];
     shift_over_12dx(G, beta, bs);
     R db[3][3];
@@ -738,11 +756,11 @@ k_rhs_curv(const R* __restrict__ u, const double* __restrict__ u64, const R* __r
     }
     R hb[3][6];  // hb[i][sym(m,n)] = d_m d_n beta^i
 #pragma unroll 1
-    for (int i = 0; i < 3; ++i) hessian<R, Closed, false>(u, d1, G, nfield, BX + i, MIX_B + i, c, hb[i]);
+    for (int i = 0; i < 3; ++i) hessian<R, Closed, kExactBg<R>>(u, d1, G, nfield, BX + i, MIX_B + i, c, hb[i]);
     R graddiv[3];
 #pragma unroll
     for (int m = 0; m < 3; ++m) graddiv[m] = hb[0][sym(m, 0)] + hb[1][sym(m, 1)] + hb[2][sym(m, 2)];
-    const R Gt[3] = {u[GTX * cs + p], u[GTY * cs + p], u[GTZ * cs + p]};
+    const R Gt[3] = {full(u, GTX, G, c), full(u, GTY, G, c), full(u, GTZ, G, c)};
 #pragma unroll 1
     for (int i = 0; i < 3; ++i) {
         R t1 = R(0), t3 = R(0), t4 = R(0), t7 = R(0), t9 = R(0);
@@ -783,8 +801,8 @@ k_mom_derived(const R* __restrict__ u, const double* __restrict__ u64, R* __rest
     if (!point(all, c, G)) return;
     const long long cs = G.cs, p = c.p;
     R g[6], gi[6], A[6];
-    load_sym(u, GXX, G, p, g);
-    load_sym(u, AXX, G, p, A);
+    load_sym(u, GXX, G, c, g);
+    load_sym(u, AXX, G, c, A);
     inverse_metric(g, gi);
     R inv_w;
     if constexpr (kPerturbative<R>) inv_w = static_cast<R>(1.0 / fmax(u64[CW * cs + p], 1.0e-12));
@@ -892,7 +910,7 @@ k_mom_damping(const R* __restrict__ u, const double* __restrict__ u64, const R* 
     }
     // Christoffels for D_j M_i = d_j M_i - Gamma^k_ij M_k
     R g[6], gl[6];
-    load_sym(u, GXX, G, p, g);
+    load_sym(u, GXX, G, c, g);
     inverse_metric(g, gl);
     R c1[3][6], c2[3][6];
     {
@@ -921,7 +939,7 @@ k_mom_damping(const R* __restrict__ u, const double* __restrict__ u64, const R* 
 // sample in two slabs is computed twice with the same result.
 template <typename R>
 __global__ void __launch_bounds__(kThreads)
-k_sommerfeld(const R* __restrict__ u, double* __restrict__ k, Geo G, BoxSet S) {
+k_sommerfeld(const R* __restrict__ u, const double* __restrict__ u64, double* __restrict__ k, Geo G, BoxSet S) {
     PointCtx c;
     if (!point(S.b[blockIdx.y], c, G)) return;
     bool face = false;
@@ -949,7 +967,7 @@ k_sommerfeld(const R* __restrict__ u, double* __restrict__ k, Geo G, BoxSet S) {
                           + xr[2] * D1<R, true>(f, G, 2, c.ix[2])) / rr;
         R offset;
         if constexpr (kPerturbative<R>) {
-            offset = f[0];
+            offset = static_cast<R>(u64[comp * cs + p] - (has_background(comp) ? 1.0 : 0.0));
         } else {
             const R asym = has_background(comp) ? 1.0 : 0.0;
             offset = f[0] - asym;
@@ -973,8 +991,8 @@ k_constraints(const double* __restrict__ u, const double* __restrict__ d1, const
     const long long n = B.count;
     const long long cs = G.cs, p = c.p;
     double g[6], gi[6], A[6];
-    load_sym(u, GXX, G, p, g);
-    load_sym(u, AXX, G, p, A);
+    load_sym(u, GXX, G, c, g);
+    load_sym(u, AXX, G, c, A);
     inverse_metric(g, gi);
     double c1[3][6], c2[3][6];
     {
@@ -1246,7 +1264,7 @@ static void launch_rhs_form(const R* u, const double* u64, double* k, R* d1, R* 
     }
     if (G.any_sommerfeld) {
         const BoxSet S = face_slabs(G, box);
-        BSSN_LAUNCH_SET(KC_SOMMERFELD, k_sommerfeld<R>, S, stream, u, k, G, S);
+        BSSN_LAUNCH_SET(KC_SOMMERFELD, k_sommerfeld<R>, S, stream, u, u64, k, G, S);
     }
 }
 
@@ -1257,7 +1275,9 @@ cudaError_t launch_rhs(const double* u, double* k, const RhsWork& w, const Geo& 
         // derivatives on the box grown by 3 with a 3-sample reach; KO and
         // upwind stencils reach 4.
         const Box region = grown_box(box, G, 6);
-        BSSN_LAUNCH(KC_CONVERT, k_perturb, blocks_for(region.count), kThreads, stream, u, w.uf, G, region);
+        // background: each component's value at the box's first sample
+        const long long p0 = (long long)box.lo[0] * G.st[0] + (long long)box.lo[1] * G.st[1] + box.lo[2];
+        BSSN_LAUNCH(KC_CONVERT, k_perturb, blocks_for(region.count), kThreads, stream, u, w.uf, G, region, p0);
         launch_rhs_form<float>(w.uf, u, k, w.d1f, w.derf, w.dampf, w.mat, G, box, stream);
     } else {
         launch_rhs_form<double>(u, u, k, w.d1, w.der, w.damp, w.mat, G, box, stream);

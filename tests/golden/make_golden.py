@@ -87,6 +87,16 @@ def rhs_cases():
     cases["mad_periodic_zero_shift"] = (random_smooth_state((10, 10, 10), seed=9, shift=False),
                                         P(eta=1.0, kappa=0.0, nu=0.02, g=0.75, dx=0.1, dt=0.02, gauge=0,
                                           mad_q=1.0 / 16.0, zero_shift=1))
+    # A 1e-6 wave on the flat background carried by a uniform O(1) shift, with
+    # no shift damping: the advection of the unit-background fields dominates
+    # their RHS, and the shift's own RHS is as small as the wave, so the
+    # numerators of every field with a constant background (diagonal metric,
+    # W, alpha and the shift) must round as the reference's do.
+    weak = random_smooth_state((12, 11, 10), seed=11, amplitude=1e-6)
+    beta = np.asarray(weak.shift) + np.array([0.5, -0.3, 0.2])[:, None, None, None]
+    cases["boosted_weak_wave"] = (weak._replace(shift=beta),
+                                  P(eta=0.0, kappa=0.0, nu=0.02, g=0.75, dx=0.1, dt=0.02, gauge=1,
+                                    x_min=-0.55, y_min=-0.5, z_min=-0.45))
     return cases
 
 

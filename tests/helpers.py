@@ -44,7 +44,8 @@ def worst(errors: dict) -> float:
     return max(errors.values())
 
 
-RHS_CASES = ("gauge_wave", "generic_kappa", "sommerfeld", "mad_mixed", "mad_periodic_zero_shift")
+RHS_CASES = ("gauge_wave", "generic_kappa", "sommerfeld", "mad_mixed", "mad_periodic_zero_shift",
+             "boosted_weak_wave")
 
 
 def assert_norms_match(got: dict, ref: dict, rel: float = 1e-9) -> None:
