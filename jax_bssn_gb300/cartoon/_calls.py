@@ -11,6 +11,7 @@ from __future__ import annotations
 import torch
 
 from .. import _device, _native
+from .._graph import GraphSteps
 from ..bssn.constraints import ConstraintViolations
 from ..bssn.variables import BSSNParameters, BSSNVariables
 
@@ -106,7 +107,7 @@ def constraints(vars: BSSNVariables, params: BSSNParameters, axi: bool) -> Const
     return v
 
 
-class CartoonEvolution:
+class CartoonEvolution(GraphSteps):
     """A compact Cartoon state kept resident in the 21-component layout.
 
     ``step(n)`` runs n classical RK4 steps (one C-ABI call) with no layout
@@ -126,7 +127,7 @@ class CartoonEvolution:
             _native.check(_native.BSSN_ERR_INVALID, "bssn_cartoon_workspace_bytes")
         self.ws = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
 
-    def step(self, steps: int = 1) -> None:
+    def _advance(self, steps: int) -> None:
         _native.check(self.lib.bssn_cartoon_rk4_step(int(self.axi), self.u.data_ptr(), _device.shape3(self.shape),
                                                      self.cparams, int(steps), self.ws.data_ptr(), self.ws.numel(),
                                                      _device.stream_handle()), "bssn_cartoon_rk4_step")

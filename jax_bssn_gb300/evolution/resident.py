@@ -13,12 +13,13 @@ from __future__ import annotations
 import torch
 
 from .. import _device, _native
+from .._graph import GraphSteps
 from ..bssn.variables import BSSNParameters, BSSNVariables
 
 NCOMP = 21
 
 
-class PatchEvolution:
+class PatchEvolution(GraphSteps):
     def __init__(self, vars: BSSNVariables, params: BSSNParameters, ghost: int = 4, precision: str | None = None):
         if params.guard_cells or params.owned_shape is not None:
             raise ValueError("PatchEvolution evolves a whole unpadded grid (guard_cells=0, owned_shape=None)")
@@ -42,7 +43,7 @@ class PatchEvolution:
         _native.check(self.lib.bssn_patch_import(_device.fields_struct(state), self.u.data_ptr(), self.patch,
                                                  _device.stream_handle()), "bssn_patch_import")
 
-    def step(self, steps: int = 1) -> None:
+    def _advance(self, steps: int) -> None:
         _native.check(self.lib.bssn_patch_rk4(self.u.data_ptr(), self.patch, self.cparams, int(steps),
                                               self.ws.data_ptr(), self.ws.numel(), _device.stream_handle()),
                       "bssn_patch_rk4")

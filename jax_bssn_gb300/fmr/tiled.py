@@ -20,6 +20,7 @@ import numpy as np
 import torch
 
 from .. import _device, _native
+from .._graph import GraphSteps
 from ..bssn.variables import BSSNParameters, BSSNVariables
 from .refinement import fine_active_shape, hierarchy_parents
 
@@ -341,7 +342,7 @@ def _stats(buffers, parameters, hierarchy, shapes, device):
     return _norms_from_stats(stats.cpu().numpy(), parameters, hierarchy, shapes)
 
 
-class FMREvolution:
+class FMREvolution(GraphSteps):
     """All patches resident in the 21-component layout; ``step(n)`` runs n
     stage-synchronous RK4 steps without leaving the device."""
 
@@ -362,7 +363,7 @@ class FMREvolution:
     def points(self) -> int:
         return sum(math.prod(shape) for shape in self.shapes)
 
-    def step(self, steps: int = 1) -> None:
+    def _advance(self, steps: int) -> None:
         _native.check(self.lib.bssn_fmr_rk4_step(self.ptrs, self.patches, self.cparams, len(self.shapes),
                                                  int(steps), self.ws.data_ptr(), self.ws.numel(),
                                                  _device.stream_handle()), "fmr_rk4_step")
