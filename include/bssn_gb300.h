@@ -250,6 +250,28 @@ int bssn_cartoon_constraints(int32_t axisymmetric, const double* compact, const 
                              const BssnParams* params, double* out, void* workspace, size_t workspace_bytes,
                              void* stream);
 
+/* ---------------- wave diagnostics ---------------- */
+
+/* h_plus (JAX_BSSN/diagnostics/waves.py:11-20): 0.5 (gt_yy - gt_zz) / W^2 on
+ * the reference layout of `shape`, bit-identical to the float64 reference.
+ * Asynchronous on `stream`. */
+int bssn_h_plus(const BssnFields* state, const int32_t shape[3], double* h_plus, void* stream);
+
+/* Scratch needed by bssn_wave_norm_sums. */
+size_t bssn_wave_norm_workspace_bytes(void);
+
+/* One level of composite_wave_diagnostics (waves.py:43-91): over the vertices of
+ * the C-ordered `shape` arrays not inside any of the `ncovered` (<= 8) boxes
+ * `covered` (6 int32 each: lo[3], hi[3], inclusive), writes to the 5 device
+ * doubles `sums`: sum of (h_plus - amplitude sin(2 pi (x - time)/wavelength))^2
+ * with x = `coordinates`, max |that error|, sum of H^2, sum over vertices of
+ * |M|^2 (`momentum` = three blocks), and the vertex count.  Deterministic
+ * block partials in `workspace`.  Asynchronous on `stream`. */
+int bssn_wave_norm_sums(const double* h_plus, const double* coordinates, const double* hamiltonian,
+                        const double* momentum, const int32_t shape[3], const int32_t* covered,
+                        int32_t ncovered, double time, double amplitude, double wavelength, double* sums,
+                        void* workspace, size_t workspace_bytes, void* stream);
+
 /* ---------------- instrumentation ---------------- */
 
 /* No reference counterpart.  FMA throughput of this GPU in GFLOP/s (FMA = 2

@@ -133,6 +133,12 @@ SIGNATURES = {
     "bssn_probe_fma_peak": (ctypes.c_int, [ctypes.c_int32, ctypes.POINTER(ctypes.c_double)]),
     "bssn_check_div6": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
                                        ctypes.c_void_p]),
+    "bssn_h_plus": (ctypes.c_int, [ctypes.POINTER(BssnFields), Shape3, ctypes.c_void_p, ctypes.c_void_p]),
+    "bssn_wave_norm_workspace_bytes": (ctypes.c_size_t, []),
+    "bssn_wave_norm_sums": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                           Shape3, ctypes.c_void_p, ctypes.c_int32, ctypes.c_double,
+                                           ctypes.c_double, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.c_size_t, ctypes.c_void_p]),
     "bssn_launch_count": (ctypes.c_longlong, []),
     "bssn_profile_enable": (None, [ctypes.c_int]),
     "bssn_profile_reset": (None, []),

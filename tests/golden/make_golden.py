@@ -312,6 +312,65 @@ def make_matter(out_dir: Path):
         np.savez_compressed(out_dir / f"matter_{name}.npz", **data)
 
 
+def wave_tree():
+    """A branching patch tree with synthetic level fields for the composite
+    wave norms: two siblings under the root and a grandchild under the first."""
+    from JAX_BSSN.fmr import FMRHierarchySpec, FMRPatchSpec
+    hierarchy = FMRHierarchySpec((FMRPatchSpec((2, 2, 2), (5, 5, 4), parent=0),
+                                  FMRPatchSpec((7, 2, 2), (9, 5, 5), parent=0),
+                                  FMRPatchSpec((1, 1, 1), (3, 3, 3), parent=1)))
+    rng = np.random.default_rng(2024)
+    shapes = [(12, 10, 9)] + [tuple(2 * (h - l) + 1 for l, h in zip(s.coarse_lo, s.coarse_hi))
+                              for s in hierarchy.patches]
+    amplitude, wavelength, time = 1.0e-3, 2.0, 0.3
+    levels, coords = [], []
+    for shape in shapes:
+        x = np.broadcast_to(rng.uniform(-1.0, 1.0, shape[0])[:, None, None], shape).copy()
+        h = amplitude * np.sin(2.0 * np.pi * (x - time) / wavelength) + 1e-6 * rng.normal(size=shape)
+        levels.append({"h_plus": h, "hamiltonian_constraint": rng.normal(size=shape),
+                       "momentum_constraint": tuple(rng.normal(size=shape) for _ in range(3))})
+        coords.append(x)
+    return hierarchy, levels, coords, time, amplitude, wavelength
+
+
+def make_waves(out_dir: Path):
+    """h_plus and diagnostic_fields (diagnostics/waves.py:11-39) on the
+    Sommerfeld RHS case, and composite_wave_diagnostics (:43-91) on a branching
+    tree, with active and guard-padded level fields."""
+    from JAX_BSSN.diagnostics.waves import composite_wave_diagnostics, diagnostic_fields, h_plus
+    state, params = rhs_cases()["sommerfeld"]
+    data = {"params": np.asarray(_params_json(params))}
+    data.update(_state_arrays("input", state))
+    data["h_plus"] = np.asarray(h_plus(state))
+    fields = diagnostic_fields(state, params)
+    data["hamiltonian"] = np.asarray(fields["hamiltonian_constraint"])
+    data["momentum"] = np.stack([np.asarray(m) for m in fields["momentum_constraint"]])
+    hierarchy, levels, coords, time, amplitude, wavelength = wave_tree()
+    for i, (lv, x) in enumerate(zip(levels, coords)):
+        data[f"tree.{i}.h_plus"] = lv["h_plus"]
+        data[f"tree.{i}.hamiltonian"] = lv["hamiltonian_constraint"]
+        data[f"tree.{i}.momentum"] = np.stack(lv["momentum_constraint"])
+        data[f"tree.{i}.x"] = x
+    data["tree.hierarchy"] = np.asarray(json.dumps([[list(s.coarse_lo), list(s.coarse_hi), s.parent]
+                                                    for s in hierarchy.patches]))
+    data["tree.scalars"] = np.array([time, amplitude, wavelength])
+    active = composite_wave_diagnostics(tuple(levels), tuple(coords), hierarchy, time, amplitude, wavelength,
+                                        active_fields=True)
+    data["tree.active"] = np.array([active[k] for k in sorted(active)])
+    # the same fields inside guard-padded arrays for every level below the root
+    padded, padded_x = [levels[0]], [coords[0]]
+    for lv, x, spec in zip(levels[1:], coords[1:], hierarchy.patches):
+        g = spec.ghost_width
+        pad = lambda a: np.pad(a, g, constant_values=999.0)  # noqa: E731
+        padded.append({"h_plus": pad(lv["h_plus"]), "hamiltonian_constraint": pad(lv["hamiltonian_constraint"]),
+                       "momentum_constraint": tuple(pad(m) for m in lv["momentum_constraint"])})
+        padded_x.append(pad(x))
+    guarded = composite_wave_diagnostics(tuple(padded), tuple(padded_x), hierarchy, time, amplitude, wavelength)
+    data["tree.guarded"] = np.array([guarded[k] for k in sorted(guarded)])
+    data["tree.keys"] = np.asarray(json.dumps(sorted(active)))
+    np.savez_compressed(out_dir / "waves.npz", **data)
+
+
 def make_cartoon(out_dir: Path):
     from JAX_BSSN.cartoon.axisymmetry import (axisymmetric_rk4_step, compute_axisymmetric_rhs,
                                               compute_axisymmetric_constraints, reconstruct_axisymmetric_support,
@@ -362,7 +421,7 @@ def main(argv):
     only = [part for a in argv if a.startswith("--only=") for part in a.split("=", 1)[1].split(",")]
     parts = {"stencils": lambda: make_stencils(HERE / "stencils.npz"), "rhs": lambda: make_rhs(HERE),
              "fmr": lambda: make_fmr(HERE), "cartoon": lambda: make_cartoon(HERE),
-             "matter": lambda: make_matter(HERE),
+             "matter": lambda: make_matter(HERE), "waves": lambda: make_waves(HERE),
              "long": lambda: make_long_runs(HERE)}
     for name, build in parts.items():
         if only and name not in only:
