@@ -68,6 +68,13 @@ template <typename R>
 constexpr int kUnroll = kPerturbative<R> ? 8 : 1;
 __host__ __device__ constexpr bool unit_diagonal(int s) { return s == 0 || s == 3 || s == 5; }
 
+// Resident blocks per SM asked of the FP32 curvature kernels: 8 blocks of 128
+// caps them at 64 registers.  They are latency-bound on stencil loads, and the
+// extra warps outweigh the spills (measured: the At kernel 14% and the K/Gt
+// kernel 3% faster than at 96 and 80 registers; 7 or 9 blocks do less well).
+template <typename R>
+constexpr int kMinBlocks = kPerturbative<R> ? 8 : 1;
+
 __host__ __device__ constexpr bool has_background(int c) {
     return c == GXX || c == GYY || c == GZZ || c == CW || c == CALPHA;
 }
@@ -416,7 +423,7 @@ k_rhs_gauge(const R* __restrict__ u, const double* __restrict__ u64, const R* __
 // dt K and dt Gt^i
 // ---------------------------------------------------------------------------
 template <typename R, bool Closed>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, kMinBlocks<R>)
 k_rhs_kgt(const R* __restrict__ u, const double* __restrict__ u64, const R* __restrict__ d1,
           const double* __restrict__ mat, double* __restrict__ k, Geo G, BoxSet S, int nfield) {
     PointCtx c;
@@ -539,7 +546,7 @@ k_rhs_kgt(const R* __restrict__ u, const double* __restrict__ u64, const R* __re
 // dt At_ij
 // ---------------------------------------------------------------------------
 template <typename R, bool Closed>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, kMinBlocks<R>)
 k_rhs_at(const R* __restrict__ u, const double* __restrict__ u64, const R* __restrict__ d1,
          const R* __restrict__ damp, const double* __restrict__ mat, double* __restrict__ k, Geo G, BoxSet S,
          int nfield) {
