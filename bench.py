@@ -71,7 +71,7 @@ CLASS_BYTES_F32 = {
 # launch (DADD + DMUL + 2 DFMA, resp. FADD + FMUL + 2 FFMA over the launch's
 # threads): the one-pass K/Gt/At kernel of the FP64 form, the At kernel of the
 # FP32 form.
-COMPUTE_KERNEL = {"fp64": ("rhs_curv", 2572), "fp32": ("rhs_at", 1905)}
+COMPUTE_KERNEL = {"fp64": ("rhs_curv", 2590), "fp32": ("rhs_at", 1890)}
 LEAVES = ("conformal_metric", "conformal_factor", "traceless_K", "trace_K", "conformal_connection", "lapse",
           "shift")
 
