@@ -11,9 +11,11 @@
 //                    JAX_BSSN/bssn/constraints.py:165-184)
 //   k_rhs_gauge      dt gt_ij, dt W, dt alpha, dt beta^i
 //                    (JAX_BSSN/bssn/spatial_metric.py:17-106, shift_and_lapse.py:65-132)
-//   k_rhs_kgt        dt K, dt Gt^i (JAX_BSSN/bssn/extrinsic_curvature.py:31-92,
+//   k_rhs_curv       FP64 form: dt K, dt Gt^i and dt At_ij in one pass
+//                    (sharing the inverse metric, Christoffels, lapse Hessian)
+//   k_rhs_kgt        FP32 form: dt K, dt Gt^i (JAX_BSSN/bssn/extrinsic_curvature.py:31-92,
 //                    conformal_connection.py:19-162)
-//   k_rhs_at         dt At_ij incl. W^2 R_ij, W^2 D_i D_j alpha
+//   k_rhs_at         FP32 form: dt At_ij incl. W^2 R_ij, W^2 D_i D_j alpha
 //                    (JAX_BSSN/bssn/extrinsic_curvature.py:119-224, geometry.py:21-186)
 //   k_mom_*          kappa != 0 only: M_i, d_l M_i and the constraint-damping
 //                    term (JAX_BSSN/bssn/constraints.py:22-213)
@@ -86,7 +88,7 @@ __host__ __device__ constexpr bool state_background(int c) {
 
 __device__ __forceinline__ bool in_range(const Axis& a, int i) { return i >= a.lo && i < a.hi; }
 
-// Up to six boxes covered by one launch; blockIdx.y selects the box.
+// Up to ten boxes covered by one launch; blockIdx.y selects the box.
 struct BoxSet {
     Box b[10];
     int n;
