@@ -256,8 +256,12 @@ __global__ void k_import_matter(const double* __restrict__ rho, const double* __
 
 // Periodic wrap of the array region [lo, lo+n) into every other padded sample
 // (np.roll semantics of the reference on an unpadded array, and the self-wrap
-// of a single tile, JAX_BSSN/parallel/communication.py:45-52).
-__global__ void k_fill_periodic(double* __restrict__ u, int ncomp, Geo G, Box region, Box all) {
+// of a single tile, JAX_BSSN/parallel/communication.py:45-52).  Samples beyond
+// an axis whose two faces are both Sommerfeld-closed (bit d of `closed`) are
+// left alone: on such an axis the one-sided closures cover the three outer
+// rows and every interior stencil stays inside the region, so nothing reads
+// them.
+__global__ void k_fill_periodic(double* __restrict__ u, int ncomp, Geo G, Box region, Box all, int closed) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= all.count) return;
     int ix[3];
@@ -267,7 +271,9 @@ __global__ void k_fill_periodic(double* __restrict__ u, int ncomp, Geo G, Box re
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         int rel = ix[d] - region.lo[d];
-        if (rel < 0 || rel >= region.n[d]) inside = false;
+        const bool out = rel < 0 || rel >= region.n[d];
+        if (out && ((closed >> d) & 1)) return;
+        if (out) inside = false;
         rel %= region.n[d];
         if (rel < 0) rel += region.n[d];
         src[d] = region.lo[d] + rel;
@@ -439,7 +445,14 @@ __global__ void k_zero(double* __restrict__ u, long long n) {
 cudaError_t launch_fill_periodic(double* u, int ncomp, const Geo& G, cudaStream_t s) {
     const Box region = box_of(G);
     const Box all = full_box(G);
-    BSSN_LAUNCH(KC_FILL, k_fill_periodic, nblocks(all.count), kThreads, s, u, ncomp, G, region, all);
+    int closed = 0;
+    for (int d = 0; d < 3; ++d) {
+        const Axis& a = G.ax[d];
+        // both faces closed and owned by this region: no stencil leaves it
+        if (!a.reduced && a.lbc && a.rbc && a.lo == a.start && a.hi == a.end) closed |= 1 << d;
+    }
+    if (closed == 7) return cudaSuccess;
+    BSSN_LAUNCH(KC_FILL, k_fill_periodic, nblocks(all.count), kThreads, s, u, ncomp, G, region, all, closed);
     return cudaGetLastError();
 }
 
