@@ -1058,7 +1058,14 @@ static Box grown_box(const Box& box, const Geo& G, int by) {
     Box b;
     b.count = 1;
     for (int d = 0; d < 3; ++d) {
-        int lo = box.lo[d] - by, hi = box.lo[d] + box.n[d] + by;
+        // An axis whose two owned faces are Sommerfeld-closed and which the box
+        // spans is not grown: its closures cover the three outer rows and every
+        // interior stencil stays inside the owned samples, so nothing beyond
+        // them is read.
+        const Axis& a = G.ax[d];
+        const bool closed = !a.reduced && a.lbc && a.rbc && box.lo[d] == a.start && box.lo[d] + box.n[d] == a.end;
+        const int g = closed ? 0 : by;
+        int lo = box.lo[d] - g, hi = box.lo[d] + box.n[d] + g;
         if (lo < 0) lo = 0;
         if (hi > G.ax[d].P) hi = G.ax[d].P;
         b.lo[d] = lo;
