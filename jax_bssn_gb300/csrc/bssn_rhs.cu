@@ -1189,6 +1189,20 @@ static BoxSet single(const Box& b) {
 
 // The box's samples on each active Sommerfeld face (owned face index on that
 // axis, the box's range on the others).
+// The box without its samples on active Sommerfeld face planes (the planes
+// face_slabs lists).
+static Box without_faces(const Geo& G, const Box& box) {
+    int lo[3], hi[3];
+    for (int d = 0; d < 3; ++d) {
+        const Axis& a = G.ax[d];
+        lo[d] = box.lo[d];
+        hi[d] = box.lo[d] + box.n[d];
+        if (a.slo && lo[d] == a.start && lo[d] < hi[d]) ++lo[d];
+        if (a.shi && hi[d] == a.end && hi[d] > lo[d]) --hi[d];
+    }
+    return make_box(lo, hi);
+}
+
 static BoxSet face_slabs(const Geo& G, const Box& box) {
     BoxSet S;
     S.n = 0;
@@ -1253,7 +1267,9 @@ static void launch_rhs_form(const R* u, const double* u64, double* k, R* d1, R* 
     const SplitBox se = split_box(G, ext, coalesced);
     BSSN_LAUNCH_SET(KC_FIRST, (k_first_derivs<R, false>), se.interior, stream, u, der, d1, G, se.interior, with_mom);
     BSSN_LAUNCH_SET(KC_FIRST, (k_first_derivs<R, true>), se.shell, stream, u, der, d1, G, se.shell, with_mom);
-    const SplitBox sb = split_box(G, box, coalesced);
+    // k_sommerfeld replaces every component's RHS on the active Sommerfeld face
+    // planes, so the stencil kernels skip those planes.
+    const SplitBox sb = split_box(G, G.any_sommerfeld ? without_faces(G, box) : box, coalesced);
     const R* dmp = with_mom ? static_cast<const R*>(damp) : nullptr;
     if (with_mom) {
         BSSN_LAUNCH_SET(KC_MOM_DAMP, (k_mom_damping<R, false>), sb.interior, stream, u, u64, der, d1, mat, damp, G,
