@@ -946,6 +946,9 @@ k_mom_damping(const R* __restrict__ u, const double* __restrict__ u64, const R* 
 // ---------------------------------------------------------------------------
 // Sommerfeld replacement on one-sample slabs at the active faces; an edge
 // sample in two slabs is computed twice with the same result.
+constexpr int kSommerfeldGroup = 3;   // 7 groups of 3 components
+static_assert(NCOMP % kSommerfeldGroup == 0, "component groups must tile the state");
+
 template <typename R>
 __global__ void __launch_bounds__(kThreads)
 k_sommerfeld(const R* __restrict__ u, const double* __restrict__ u64, double* __restrict__ k, Geo G, BoxSet S) {
@@ -969,8 +972,10 @@ k_sommerfeld(const R* __restrict__ u, const double* __restrict__ u64, double* __
     const long long cs = G.cs, p = c.p;
     const R xr[3] = {static_cast<R>(X[0]), static_cast<R>(X[1]), static_cast<R>(X[2])};
     const R rr = static_cast<R>(rs);
+    // blockIdx.z picks a group of kSommerfeldGroup components: short per-thread
+    // chains and enough threads for the few face samples
 #pragma unroll 1
-    for (int comp = 0; comp < NCOMP; ++comp) {
+    for (int comp = blockIdx.z * kSommerfeldGroup; comp < (int)(blockIdx.z + 1) * kSommerfeldGroup; ++comp) {
         const R* f = u + comp * cs + p;
         const R radial = (xr[0] * D1<R, true>(f, G, 0, c.ix[0]) + xr[1] * D1<R, true>(f, G, 1, c.ix[1])
                           + xr[2] * D1<R, true>(f, G, 2, c.ix[2])) / rr;
@@ -1296,7 +1301,9 @@ static void launch_rhs_form(const R* u, const double* u64, double* k, R* d1, R* 
     }
     if (G.any_sommerfeld) {
         const BoxSet S = face_slabs(G, box);
-        BSSN_LAUNCH_SET(KC_SOMMERFELD, k_sommerfeld<R>, S, stream, u, u64, k, G, S);
+        if (S.n > 0)
+            BSSN_LAUNCH(KC_SOMMERFELD, k_sommerfeld<R>, dim3(blocks_for(largest(S)), S.n, NCOMP / kSommerfeldGroup),
+                        kThreads, stream, u, u64, k, G, S);
     }
 }
 
