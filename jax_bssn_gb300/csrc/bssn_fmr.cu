@@ -291,6 +291,143 @@ cudaError_t launch_fmr_prolong(const double* parent, const PatchDims& Dp, double
 }
 
 // ---------------------------------------------------------------------------
+// FP32 form: the same prolongation in float on perturbations.  Interpolation
+// is linear with weights summing to one, so interpolating u - b and adding b
+// back gives the interpolant of u for any constant b.  The parent window the
+// child's stencils reach is converted once to float perturbations about each
+// component's value at the window's first sample (a uniform shift or any
+// other offset drops out), interpolated in float, and written to the FP64
+// child guards as b + result.  Node shortcuts and enumeration as above.
+// ---------------------------------------------------------------------------
+struct Window {
+    int lo[3], n[3];
+    long long cs;   // samples per component block
+    __host__ __device__ long long at(int x, int y, int z) const {
+        return ((long long)(x - lo[0]) * n[1] + (y - lo[1])) * n[2] + (z - lo[2]);
+    }
+};
+
+__global__ void k_fmr_window_f32(const double* __restrict__ parent, PatchDims Dp, Window Wn, float* __restrict__ out) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = blockIdx.y;
+    if (t >= Wn.cs) return;
+    const int x = Wn.lo[0] + (int)(t / ((long long)Wn.n[1] * Wn.n[2]));
+    const long long r = t % ((long long)Wn.n[1] * Wn.n[2]);
+    const int y = Wn.lo[1] + (int)(r / Wn.n[2]);
+    const int z = Wn.lo[2] + (int)(r % Wn.n[2]);
+    const double* f = parent + (long long)c * Dp.cs;
+    const double b = f[Dp.at(Wn.lo[0], Wn.lo[1], Wn.lo[2])];
+    out[(long long)c * Wn.cs + t] = static_cast<float>(f[Dp.at(x, y, z)] - b);
+}
+
+__global__ void k_fmr_prolong_f32(const double* __restrict__ parent, PatchDims Dp, const float* __restrict__ win,
+                                  Window Wn, double* __restrict__ child, PatchDims Dc, int lo0, int lo1, int lo2,
+                                  ProlongWeights W, ShellSlabs S) {
+    const int slab = blockIdx.y;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= S.count[slab]) return;
+    const int np0 = S.pair_n[slab][0], npairs = np0 + S.pair_n[slab][1];
+    const int ny = set_count(S.y[slab]);
+    const long long row = t / npairs;
+    const int k = (int)(t - row * npairs);
+    const int x = set_pick(S.x[slab], (int)(row / ny));
+    const int y = set_pick(S.y[slab], (int)(row - (row / ny) * ny));
+    const int pr = k < np0 ? S.pair_lo[slab][0] + k : S.pair_lo[slab][1] + (k - np0);
+    const int z0 = 2 * pr, z1 = z0 + 1;
+    const int g = kFmrGuard;
+    const bool xy_shell = x < g || x >= g + Dc.n[0] || y < g || y >= g + Dc.n[1];
+    const bool s0 = xy_shell || z0 < g || z0 >= g + Dc.n[2];
+    const bool s1 = z1 < Dc.P[2] && (xy_shell || z1 < g || z1 >= g + Dc.n[2]);
+    if (!s0 && !s1) return;
+    const int lo[3] = {lo0, lo1, lo2};
+    const int ix[3] = {x, y, z0};
+    int node0[3], frac[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const int twice = 2 * (lo[a] + g) + (ix[a] - g);
+        const int fl = twice >= 0 ? twice / 2 : -((-twice + 1) / 2);
+        frac[a] = twice - 2 * fl;
+        node0[a] = fl - 2;
+    }
+    float w[6];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) w[q] = static_cast<float>(W.w[1][q]);
+    const long long sx = (long long)Wn.n[1] * Wn.n[2];
+    const bool fx = frac[0] != 0, fy = frac[1] != 0;
+    const int c = blockIdx.z;
+    const float* f = win + (long long)c * Wn.cs;
+    const double b = parent[(long long)c * Dp.cs + Dp.at(Wn.lo[0], Wn.lo[1], Wn.lo[2])];
+    auto xval = [&](int py, int pz) -> float {
+        const float* rowp = f + Wn.at(node0[0], py, pz);
+        if (!fx) return rowp[2 * sx];
+        float v = rowp[0] * w[0];
+#pragma unroll
+        for (int q = 1; q < 6; ++q) v += rowp[q * sx] * w[q];
+        return v;
+    };
+    auto yval = [&](int pz) -> float {
+        if (!fy) return xval(node0[1] + 2, pz);
+        float v = xval(node0[1], pz) * w[0];
+#pragma unroll
+        for (int q = 1; q < 6; ++q) v += xval(node0[1] + q, pz) * w[q];
+        return v;
+    };
+    double* out = child + (long long)c * Dc.cs;
+    if (s1) {
+        float line[6];
+#pragma unroll
+        for (int q = 0; q < 6; ++q) line[q] = yval(node0[2] + q);
+        if (s0) out[Dc.at(x, y, z0)] = b + static_cast<double>(line[2]);
+        float acc = line[0] * w[0];
+#pragma unroll
+        for (int q = 1; q < 6; ++q) acc += line[q] * w[q];
+        out[Dc.at(x, y, z1)] = b + static_cast<double>(acc);
+    } else {
+        out[Dc.at(x, y, z0)] = b + static_cast<double>(yval(node0[2] + 2));
+    }
+}
+
+// The parent samples the child's guard shell reaches: six nodes around every
+// target lo + (i - g)/2 + g, i over the child's padded extent.  A child
+// strictly inside its parent keeps the window inside the parent's padded
+// array; `ok` is false otherwise or when the window outgrows the child's
+// float scratch, and the caller then takes the FP64 prolongation.
+static Window prolong_window(const PatchDims& Dp, const PatchDims& Dc, const int lo[3], bool& ok) {
+    const int g = kFmrGuard;
+    auto floor_half = [](int twice) { return twice >= 0 ? twice / 2 : -((-twice + 1) / 2); };
+    Window Wn;
+    Wn.cs = 1;
+    ok = true;
+    for (int a = 0; a < 3; ++a) {
+        const int first = floor_half(2 * (lo[a] + g) + (0 - g)) - 2;
+        const int last = floor_half(2 * (lo[a] + g) + (Dc.P[a] - 1 - g)) + 3;
+        ok = ok && first >= 0 && last <= Dp.P[a] - 1;
+        Wn.lo[a] = first;
+        Wn.n[a] = last - first + 1;
+        Wn.cs *= Wn.n[a];
+    }
+    ok = ok && Wn.cs <= Dc.cs;
+    return Wn;
+}
+
+// FP32-form prolongation; `scratch` holds NCOMP * Dc.cs floats.
+cudaError_t launch_fmr_prolong_f32(const double* parent, const PatchDims& Dp, double* child, const PatchDims& Dc,
+                                   const int lo[3], float* scratch, cudaStream_t s) {
+    bool ok = false;
+    const Window Wn = prolong_window(Dp, Dc, lo, ok);
+    if (!ok) return launch_fmr_prolong(parent, Dp, child, Dc, lo, s);
+    BSSN_LAUNCH(KC_TRANSFER, k_fmr_window_f32, dim3(fmr_blocks(Wn.cs), NCOMP), kFmrThreads, s, parent, Dp, Wn,
+                scratch);
+    const ShellSlabs S = shell_slabs(Dc);
+    long long most = 0;
+    for (int k = 0; k < 3; ++k) most = S.count[k] > most ? S.count[k] : most;
+    const dim3 grid(fmr_blocks(most), 3, NCOMP);
+    BSSN_LAUNCH(KC_TRANSFER, k_fmr_prolong_f32, grid, kFmrThreads, s, parent, Dp, scratch, Wn, child, Dc, lo[0],
+                lo[1], lo[2], prolong_weights(), S);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // injection of coincident owned fine vertices (transfer.py:145-171)
 // ---------------------------------------------------------------------------
 __global__ void k_fmr_inject(double* __restrict__ parent, PatchDims Dp, const double* __restrict__ child,
@@ -500,16 +637,25 @@ std::vector<PatchWork> carve(const FmrPlan& plan, double* base) {
 
 Box owned_box(const Geo& G) { return box_of(G); }
 
+// Prolongation into child p: the bitwise FP64 form, or (FP32 form, with the
+// patch work available) the float form using the child's float RHS scratch,
+// which is free between RHS evaluations.
+cudaError_t prolong_child(const FmrPlan& plan, double* const* u, int p, const std::vector<PatchWork>* w,
+                          cudaStream_t s) {
+    const int q = plan.parent[p];
+    if (w && plan.geo[p].precision == kPrecisionF32)
+        return launch_fmr_prolong_f32(u[q], plan.dims[q], u[p], plan.dims[p], plan.lo[p].data(), (*w)[p].rw.uf, s);
+    return launch_fmr_prolong(u[q], plan.dims[q], u[p], plan.dims[p], plan.lo[p].data(), s);
+}
+
 // prepare: (project owned), refresh, prolong from the prepared parent -- parent first
-cudaError_t prepare(const FmrPlan& plan, double* const* u, bool project, cudaStream_t s) {
+cudaError_t prepare(const FmrPlan& plan, double* const* u, bool project, cudaStream_t s,
+                    const std::vector<PatchWork>* w = nullptr) {
     cudaError_t e = cudaSuccess;
     for (int p = 0; p < plan.npatch && e == cudaSuccess; ++p) {
         if (project) e = launch_project(u[p], plan.geo[p], owned_box(plan.geo[p]), s);
         if (e == cudaSuccess) e = launch_fmr_refresh(u[p], plan.dims[p], plan.codes[p].data(), s);
-        if (e == cudaSuccess && p > 0) {
-            const int q = plan.parent[p];
-            e = launch_fmr_prolong(u[q], plan.dims[q], u[p], plan.dims[p], plan.lo[p].data(), s);
-        }
+        if (e == cudaSuccess && p > 0) e = prolong_child(plan, u, p, w, s);
     }
     return e;
 }
@@ -519,7 +665,7 @@ cudaError_t fmr_step(const FmrPlan& plan, double* const* u, const std::vector<Pa
     const int np = plan.npatch;
     std::vector<double*> us(np);
     for (int p = 0; p < np; ++p) us[p] = w[p].us;
-    cudaError_t e = prepare(plan, u, true, s);  // s0
+    cudaError_t e = prepare(plan, u, true, s, &w);  // s0
     for (int stage = 1; stage <= 4 && e == cudaSuccess; ++stage) {
         double* const* src = stage == 1 ? u : us.data();
         for (int p = 0; p < np && e == cudaSuccess; ++p)
@@ -534,10 +680,7 @@ cudaError_t fmr_step(const FmrPlan& plan, double* const* u, const std::vector<Pa
             // refresh + prolong of the next stage state (projection already applied)
             for (int p = 0; p < np && e == cudaSuccess; ++p) {
                 e = launch_fmr_refresh(us[p], plan.dims[p], plan.codes[p].data(), s);
-                if (e == cudaSuccess && p > 0) {
-                    const int q = plan.parent[p];
-                    e = launch_fmr_prolong(us[q], plan.dims[q], us[p], plan.dims[p], plan.lo[p].data(), s);
-                }
+                if (e == cudaSuccess && p > 0) e = prolong_child(plan, us.data(), p, &w, s);
             }
         }
     }
@@ -547,7 +690,7 @@ cudaError_t fmr_step(const FmrPlan& plan, double* const* u, const std::vector<Pa
         e = launch_fmr_inject(u[q], plan.dims[q], u[c], plan.dims[c], plan.lo[c].data(), s);
         if (e == cudaSuccess) e = launch_project(u[q], plan.geo[q], owned_box(plan.geo[q]), s);
     }
-    if (e == cudaSuccess) e = prepare(plan, u, false, s);
+    if (e == cudaSuccess) e = prepare(plan, u, false, s, &w);
     return e;
 }
 
