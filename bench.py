@@ -15,6 +15,11 @@ Other workloads (--workload):
   axisymmetric  two zero-momentum punctures (Brill-Lindquist, m=0.5 at z=+-1) on
                 the compact Cartoon plane 256 x 512, dx=1/32, kappa=0.002, CFL 0.2;
                 updates count the 256 x 512 evolved samples.
+  puncture      Bowen-York binary initial data: Newton + conjugate gradients on a
+                128^3 cell-centred grid (a "step" is one complete solve; the
+                metric counts unknowns x Krylov iterations per second).
+  puncture_axi  the axisymmetric collision's initial data: Newton + BiCGSTAB on
+                the 128 x 256 meridional grid, tolerances 1e-12.
 All inputs are synthetic (analytic initial data generated on the host).
 
 Arms:
@@ -90,7 +95,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
-    ap.add_argument("--workload", choices=("teukolsky", "fmr", "axisymmetric"), default="teukolsky")
+    ap.add_argument("--workload", choices=("teukolsky", "fmr", "axisymmetric", "puncture", "puncture_axi"),
+                    default="teukolsky")
     ap.add_argument("--n", type=int, default=None, help="grid size (teukolsky n, fmr root n, axisymmetric Nrho)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -290,6 +296,270 @@ class Axisymmetric:
 
 
 WORKLOADS = {w.name: w for w in (Teukolsky, NestedFMR, Axisymmetric)}
+
+
+# ----------------------------------------------------------------------------
+# puncture initial data (Newton-Krylov solves)
+# ----------------------------------------------------------------------------
+
+PUNCTURE_METRIC = "Bowen-York Newton-Krylov unknown-iterations/s"
+PUNCTURE_UNIT = "unknown-iterations/s"
+# Algorithmic HBM bytes per unknown of one Krylov iteration, per kernel class.
+PUNCTURE_BYTES = {
+    False: {"solve_apply": 40,    # CG apply: r, p_prev, dS/du read; p, Ap written
+            "solve_update": 48},  # CG update: x, r, p, Ap read; x, r written
+    True: {"solve_apply": 96,     # BiCGSTAB p/q (r, rhat, p, q, dS/du read; p, q written) + s/t (r, q, dS/du; s, t)
+           "solve_update": 56},   # BiCGSTAB x/r: x, rhat, p, s, t read; x, r written
+}
+
+
+class Puncture:
+    """Cartesian Bowen-York binary: 128^3 cell-centred grid on [-12,12]^3 (the
+    reference's cell_centered_grid at 128 points), m=0.5 at z=-+1.5 with
+    momenta -+0.2 along x, the reference's default tolerances."""
+    name = "puncture"
+    axisymmetric = False
+
+    def __init__(self, n=None):
+        self.n = n or 128
+        self.masses = [0.5, 0.5]
+        self.positions = [[0.0, 0.0, -1.5], [0.0, 0.0, 1.5]]
+        self.momenta = [[0.2, 0.0, 0.0], [-0.2, 0.0, 0.0]]
+        self.tol = dict(newton_tolerance=1e-10, max_newton_iterations=12, linear_tolerance=1e-10,
+                        max_linear_iterations=1000)
+
+    def config(self):
+        return {"workload": f"Bowen-York binary puncture data, Newton + conjugate gradients on a {self.n}^3 "
+                            "cell-centred grid over [-12,12]^3, FP64",
+                "masses": self.masses, "positions": self.positions, "momenta": self.momenta,
+                "tolerances": self.tol, "unknowns": (self.n - 2) ** 3,
+                "l2": "each timed solve re-derives its vectors; 10 grid vectors exceed the 129 MB L2 above ~110^3",
+                "parallelism": "replicas"}
+
+    def grid(self, device):
+        from jax_bssn_gb300.utilities import bowen_york_solver as by
+        return by.cell_centered_grid(self.n, 12.0)
+
+    def unknowns(self):
+        return (self.n - 2) ** 3
+
+    def cpu_grid(self, n):
+        from oracle import puncture as op
+        return op.cell_centered_grid(n, 12.0)
+
+    def cpu_solve(self, grid, dx, counts):
+        from oracle import puncture as op
+        t = self.tol
+        return op.solve_conformal_factor(self.masses, self.positions, self.momenta, grid, dx,
+                                         t["newton_tolerance"], t["max_newton_iterations"],
+                                         t["linear_tolerance"], t["max_linear_iterations"], counts=counts)
+
+    def cpu_unknowns(self, n):
+        return (n - 2) ** 3
+
+
+class PunctureAxi(Puncture):
+    """The axisymmetric head-on collision's initial data
+    (demos/axisymmetric_blackhole_collision): meridional 128 x 256 grid,
+    r_max 12, m=0.5 at z=-+3 with inward momenta 0.05, tolerances 1e-12 and up
+    to 100 Newton steps."""
+    name = "puncture_axi"
+    axisymmetric = True
+
+    def __init__(self, n=None):
+        self.n = n or 128
+        self.masses = [0.5, 0.5]
+        self.positions = [[0.0, 0.0, -3.0], [0.0, 0.0, 3.0]]
+        self.momenta = [[0.0, 0.0, 0.05], [0.0, 0.0, -0.05]]
+        self.tol = dict(newton_tolerance=1e-12, max_newton_iterations=100, linear_tolerance=1e-12,
+                        max_linear_iterations=1000)
+
+    def config(self):
+        return {"workload": f"axisymmetric Bowen-York head-on data, Newton + BiCGSTAB on the {self.n} x "
+                            f"{2 * self.n} meridional grid, r_max 12, FP64",
+                "masses": self.masses, "positions": self.positions, "momenta": self.momenta,
+                "tolerances": self.tol, "unknowns": (self.n - 1) * (2 * self.n - 2),
+                "l2": "working set (~2.6 MB) stays in L2: the solve is latency bound", "parallelism": "replicas"}
+
+    def grid(self, device):
+        from jax_bssn_gb300.utilities import bowen_york_solver as by
+        return by.axisymmetric_cell_centered_grid(self.n, 12.0)
+
+    def unknowns(self):
+        return (self.n - 1) * (2 * self.n - 2)
+
+    def cpu_grid(self, n):
+        from oracle import puncture as op
+        return op.axisymmetric_cell_centered_grid(n, 12.0)
+
+    def cpu_solve(self, grid, dx, counts):
+        from oracle import puncture as op
+        t = self.tol
+        return op.solve_axisymmetric_conformal_factor(self.masses, self.positions, self.momenta, grid, dx,
+                                                      t["newton_tolerance"], t["max_newton_iterations"],
+                                                      t["linear_tolerance"], t["max_linear_iterations"],
+                                                      counts=counts)
+
+    def cpu_unknowns(self, n):
+        return (n - 1) * (2 * n - 2)
+
+
+PUNCTURES = {w.name: w for w in (Puncture, PunctureAxi)}
+PUNCTURE_CPU_N = {"puncture": 48, "puncture_axi": 64}
+
+
+def puncture_cpu(wl, solves=1, n=None):
+    """The reference algorithm (NumPy restatement with SciPy's Krylov solvers)
+    on a smaller grid of the same problem."""
+    n = n or PUNCTURE_CPU_N[wl.name]
+    grid, dx = wl.cpu_grid(n)
+    counts = []
+    t = time.perf_counter()
+    for _ in range(solves):
+        wl.cpu_solve(grid, dx, counts)
+    dt = time.perf_counter() - t
+    work = wl.cpu_unknowns(n) * sum(counts)
+    shape = f"{n}^3" if not wl.axisymmetric else f"{n} x {2 * n}"
+    cores = os.cpu_count() or 1
+    return {"value": work / dt, "unit": PUNCTURE_UNIT, "cores": cores, "kind": "port",
+            "sample": f"{solves} Newton-Krylov solve(s) of the same punctures on the {shape} grid "
+                      f"({sum(counts)} Krylov iterations; NumPy restatement with SciPy's Krylov solvers: "
+                      f"elementwise work on one thread, dot products through the threaded BLAS on up to {cores} "
+                      "cores; JAX not installed)", "seconds": dt}
+
+
+def run_puncture(args, world, rank, local):
+    import numpy as np
+    import torch
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=device)
+    from jax_bssn_gb300 import _native, build
+    if not build.LIBRARY.exists():
+        build.build()
+    lib = _native.load()
+    from jax_bssn_gb300.utilities import bowen_york_solver as by
+    wl = PUNCTURES[args.workload](args.n)
+    grid, dx = wl.grid(device)
+    unknowns = wl.unknowns()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    def solve(g):
+        return by.puncture_solve(wl.masses, wl.positions, wl.momenta, g, dx, axisymmetric=wl.axisymmetric, **wl.tol)
+
+    peaks = {}
+    peaks_path = ROOT / "MEASURED_PEAKS.json"
+    if peaks_path.exists():
+        peaks = json.loads(peaks_path.read_text())
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        r = solve(grid)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    torch.cuda.synchronize()
+    launches0 = lib.bssn_launch_count()
+    iterations = 0
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for _ in range(args.steps):
+        r = solve(grid)
+        iterations += sum(r.linear_iterations)
+    t1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    launches = lib.bssn_launch_count() - launches0
+    clock_info = clocks.stop()
+    ms = _max_over_ranks(t0.elapsed_time(t1), world, device)
+    value = world * unknowns * iterations / (ms / 1e3)
+    # per-kernel device time of one profiled solve
+    lib.bssn_profile_reset()
+    lib.bssn_profile_enable(1)
+    rp = solve(grid)
+    torch.cuda.synchronize()
+    lib.bssn_profile_enable(0)
+    prof = _native.profile_read()
+    lib.bssn_profile_reset()
+    its = sum(rp.linear_iterations)
+    total = sum(v[0] for v in prof.values()) or 1.0
+    kernels = {k: {"ms": round(v[0], 3), "launches": v[1], "share": round(v[0] / total, 4)}
+               for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}
+    name = max(PUNCTURE_BYTES[wl.axisymmetric], key=lambda k: prof.get(k, (0.0, 0))[0])
+    kms, klaunch = prof.get(name, (0.0, 0))
+    per = PUNCTURE_BYTES[wl.axisymmetric][name]
+    achieved = per * unknowns * its / (kms / 1e3) / 1e9 if kms > 0 else None
+    roofline = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved / hbm_peak if achieved else None, "traffic": None, "peak_source": peak_src,
+                "kernel_share": kms / total, "kernel_ms_per_launch": kms / max(klaunch, 1),
+                "algorithmic_bytes_per_unknown_iteration": per,
+                "note": "launches after convergence inside a chunk return at once and are included in the time"}
+    e2e = None
+    if not args.no_e2e:
+        host_grid = grid.cpu().pin_memory()
+        host_psi = torch.empty(tuple(grid.shape[:-1]), dtype=torch.float64).pin_memory()
+        dev_grid = torch.empty_like(grid)
+        h2d = host_grid.numel() * 8
+        d2h = host_psi.numel() * 8
+        torch.cuda.synchronize()
+        barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e_its = 0
+        e0.record(stream)
+        for _ in range(args.steps):
+            dev_grid.copy_(host_grid, non_blocking=True)
+            re = solve(dev_grid)
+            host_psi.copy_(re.psi, non_blocking=True)
+            e_its += sum(re.linear_iterations)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        ems = _max_over_ranks(e0.elapsed_time(e1), world, device)
+        e2e = {"value": world * unknowns * e_its / (ems / 1e3), "unit": PUNCTURE_UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "ms_per_step": ems / args.steps}
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = puncture_cpu(wl)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    if rank != 0:
+        return None
+    return {
+        "metric": PUNCTURE_METRIC, "value": value, "unit": PUNCTURE_UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (analytic puncture parameters)",
+        "config": {**wl.config(), "step": "one complete Newton-Krylov solve",
+                   "newton_steps": len(r.residual_history), "krylov_iterations": r.linear_iterations,
+                   "final_residual": r.residual_history[-1]},
+        "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clock_info,
+        "kernels": kernels,
+    }
+
+
+def run_puncture_reference(args, world, rank):
+    if rank != 0:
+        return None
+    wl = PUNCTURES[args.workload](args.n)
+    n = {"puncture": 32, "puncture_axi": 32}[wl.name]
+    puncture_cpu(wl, max(args.warmup, 1), n)
+    base = puncture_cpu(wl, args.steps, n)
+    value = base["value"]
+    return {"metric": PUNCTURE_METRIC, "value": value, "unit": PUNCTURE_UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": base["seconds"] * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": wl.config(),
+            "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": PUNCTURE_UNIT, "cores": base["cores"], "kind": "port",
+                             "sample": "each step " + base["sample"]},
+            "e2e": {"value": value, "unit": PUNCTURE_UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
 # ----------------------------------------------------------------------------
@@ -607,7 +877,10 @@ def run_reference(args, world, rank):
 def main():
     args = parse()
     world, rank, local = dist_setup()
-    if args.impl == "reference":
+    if args.workload in PUNCTURES:
+        out = (run_puncture_reference(args, world, rank) if args.impl == "reference"
+               else run_puncture(args, world, rank, local))
+    elif args.impl == "reference":
         out = run_reference(args, world, rank)
     else:
         out = run_gb300(args, world, rank, local)

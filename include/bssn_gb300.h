@@ -42,6 +42,7 @@ extern "C" {
 #define BSSN_ERR_CUDA 3         /* a CUDA launch or runtime call failed */
 #define BSSN_ERR_NONFINITE 4    /* non-finite value detected in the state */
 #define BSSN_ERR_TIMEOUT 5      /* a bounded device wait gave up */
+#define BSSN_ERR_NOT_CONVERGED 6 /* an iterative solve ran out of iterations */
 
 #define BSSN_NCOMP 21           /* independent evolved components */
 #define BSSN_NLEAF_VALUES 27    /* stored values per point in the reference layout */
@@ -274,6 +275,68 @@ int bssn_wave_norm_sums(const double* h_plus, const double* coordinates, const d
 
 /* ---------------- instrumentation ---------------- */
 
+/* ---------------------------------------------------------------------------
+ * Bowen-York puncture initial data (JAX_BSSN/utilities/bowen_york_solver.py).
+ * Grids are the reference's cell-centred grids: Cartesian (n0, n1, n2), or the
+ * meridional (Nrho, 1, Nz) grid with axisymmetric = 1.  Arrays are C-ordered
+ * float64 on the device.
+ * ------------------------------------------------------------------------- */
+#define BSSN_MAX_PUNCTURES 16
+
+/* brill_lindquist_conformal_factor (:52-63), bowen_york_extrinsic_curvature
+ * (:66-91) and contract_conformal_curvature (:93-101) at npoints coordinates
+ * grid[npoints][3].  masses[np], positions[np][3], momenta[np][3] are HOST
+ * arrays.  Any of psi_bl[npoints], curvature[npoints][3][3] and
+ * curvature_squared[npoints] may be NULL. */
+int bssn_puncture_fields(const double* grid, int64_t npoints, const double* masses, const double* positions,
+                         const double* momenta, int32_t npunctures, double* psi_bl, double* curvature,
+                         double* curvature_squared, void* stream);
+
+/* Operators of bowen_york_solver.py, in the reference's operation order:
+ *   CONTRACT              out = K_ij K_ij of a = K[n][3][3]; shape = (n, 1, 1)      (:93-101)
+ *   SOURCE                out = 1/8 b psi^-7, a = psi, b = A^2 (pointwise, shape = any) (:151-155)
+ *   LINEARIZED_SOURCE     out = -7/8 c b^-8 a, a = delta, b = psi, c = A^2 (pointwise)  (:158-162)
+ *   LAPLACIAN             seven-point / axisymmetric Laplacian of the interior-shaped a (:104-148)
+ *   LINEARIZED_OPERATOR   Laplacian(a) + LINEARIZED_SOURCE(a, b, c), all interior-shaped (:165-198)
+ *   RESIDUAL              Laplacian(u) + SOURCE(psi_bl + u, A^2) at the interior, with
+ *                         full-grid a = u, b = psi_bl, c = A^2; out interior-shaped (:201-230)
+ * For the last three, shape is the FULL grid's; the interior of a Cartesian
+ * grid is (n0-2, n1-2, n2-2), of a meridional grid (Nrho-1, Nz-2).  LAPLACIAN
+ * and LINEARIZED_OPERATOR need a workspace of one full-grid array. */
+#define BSSN_PUNCTURE_CONTRACT 0
+#define BSSN_PUNCTURE_SOURCE 1
+#define BSSN_PUNCTURE_LINEARIZED_SOURCE 2
+#define BSSN_PUNCTURE_LAPLACIAN 3
+#define BSSN_PUNCTURE_LINEARIZED_OPERATOR 4
+#define BSSN_PUNCTURE_RESIDUAL 5
+int bssn_puncture_operator(int32_t op, const double* a, const double* b, const double* c, const int32_t shape[3],
+                           double dx, int32_t axisymmetric, double* out, void* workspace, size_t workspace_bytes,
+                           void* stream);
+
+/* Bytes of device workspace bssn_puncture_solve needs on a grid (0 if the
+ * grid is invalid). */
+size_t bssn_puncture_workspace_bytes(const int32_t shape[3], int32_t axisymmetric);
+
+/* solve_conformal_factor (:283-366; conjugate gradients) or, with
+ * axisymmetric = 1, solve_axisymmetric_conformal_factor (:369-479; BiCGSTAB):
+ * Newton iterations on the regular correction u, fixed to zero on the outer
+ * cells, each correction from a matrix-free Krylov solve of the negative
+ * linearised operator.  Inputs psi_bl and curvature_squared and outputs u and
+ * psi = psi_bl + u span the full grid.  residual_history (HOST, room for
+ * max_newton_iterations + 1 values) receives the interior RMS residual before
+ * each correction and after the last; *history_length its count;
+ * linear_iterations (HOST, optional, max_newton_iterations entries) the Krylov
+ * iterations of each correction.  Synchronises `stream` once per Newton step
+ * and once per 16 Krylov iterations.  Returns BSSN_ERR_NOT_CONVERGED when the
+ * Newton iterations run out, and (axisymmetric) BSSN_ERR_NONFINITE for a
+ * nonfinite residual or correction or a nonpositive psi, each with the
+ * reference's message in bssn_last_error(). */
+int bssn_puncture_solve(const double* psi_bl, const double* curvature_squared, const int32_t shape[3], double dx,
+                        int32_t axisymmetric, double newton_tolerance, int32_t max_newton_iterations,
+                        double linear_tolerance, int32_t max_linear_iterations, double* u, double* psi,
+                        double* residual_history, int32_t* history_length, int32_t* linear_iterations,
+                        void* workspace, size_t workspace_bytes, void* stream);
+
 /* No reference counterpart.  FMA throughput of this GPU in GFLOP/s (FMA = 2
  * flops) for BSSN_PRECISION_F64 or BSSN_PRECISION_F32: sixteen independent FMA
  * chains per thread, 8 x 256 threads per SM, one timed launch after a warm-up
@@ -292,7 +355,9 @@ long long bssn_launch_count(void);
  * stream; off by default.  Classes: fill, first derivatives, gauge RHS, K/Gt
  * RHS, At RHS, momentum derived fields, momentum damping, Sommerfeld, RK4
  * stage, projection, import, export, constraints, FMR transfer, Cartoon,
- * FP32 conversion, other, K/Gt/At RHS in one pass (FP64 form).  bssn_profile_read synchronises the recorded events, accumulates and
+ * FP32 conversion, other, K/Gt/At RHS in one pass (FP64 form), puncture
+ * Newton-level kernels, puncture Krylov operator kernels, puncture Krylov
+ * vector updates.  bssn_profile_read synchronises the recorded events, accumulates and
  * returns the number of classes. */
 void bssn_profile_enable(int on);
 void bssn_profile_reset(void);

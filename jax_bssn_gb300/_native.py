@@ -24,6 +24,7 @@ BSSN_ERR_WORKSPACE = 2
 BSSN_ERR_CUDA = 3
 BSSN_ERR_NONFINITE = 4
 BSSN_ERR_TIMEOUT = 5
+BSSN_ERR_NOT_CONVERGED = 6
 
 PRECISION_F64 = 0
 PRECISION_F32 = 1
@@ -139,6 +140,18 @@ SIGNATURES = {
                                            Shape3, ctypes.c_void_p, ctypes.c_int32, ctypes.c_double,
                                            ctypes.c_double, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p,
                                            ctypes.c_size_t, ctypes.c_void_p]),
+    "bssn_puncture_fields": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, c_double_p, c_double_p, c_double_p,
+                                            ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                            ctypes.c_void_p]),
+    "bssn_puncture_operator": (ctypes.c_int, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                              Shape3, ctypes.c_double, ctypes.c_int32, ctypes.c_void_p,
+                                              ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    "bssn_puncture_workspace_bytes": (ctypes.c_size_t, [Shape3, ctypes.c_int32]),
+    "bssn_puncture_solve": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, Shape3, ctypes.c_double, ctypes.c_int32,
+                                           ctypes.c_double, ctypes.c_int32, ctypes.c_double, ctypes.c_int32,
+                                           ctypes.c_void_p, ctypes.c_void_p, c_double_p,
+                                           ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32),
+                                           ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     "bssn_launch_count": (ctypes.c_longlong, []),
     "bssn_profile_enable": (None, [ctypes.c_int]),
     "bssn_profile_reset": (None, []),
@@ -147,7 +160,7 @@ SIGNATURES = {
 
 KERNEL_CLASSES = ("fill", "first_derivs", "rhs_gauge", "rhs_kgt", "rhs_at", "mom_derived", "mom_damping",
                   "sommerfeld", "rk4_stage", "project", "import", "export", "constraints", "fmr_transfer",
-                  "cartoon", "convert", "other", "rhs_curv")
+                  "cartoon", "convert", "other", "rhs_curv", "solve_newton", "solve_apply", "solve_update")
 
 
 def profile_read() -> dict:

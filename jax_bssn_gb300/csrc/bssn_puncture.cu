@@ -1,0 +1,816 @@
+// Bowen-York puncture initial data (JAX_BSSN/utilities/bowen_york_solver.py):
+//   puncture fields     Brill-Lindquist psi (:52-63), the conformal Bowen-York
+//                       curvature (:66-91) and its flat contraction (:93-101)
+//                       at given grid coordinates, in the reference's operation
+//                       order;
+//   pointwise/stencil   the seven-point and axisymmetric Laplacians (:104-148),
+//   operators           the Hamiltonian source and its linearisation (:151-162),
+//                       the linearised operators (:165-198) and the residuals
+//                       (:201-230), each in the reference's operation order;
+//   Newton solve        solve_conformal_factor (:283-366) with conjugate
+//                       gradients on the Cartesian grid, and
+//                       solve_axisymmetric_conformal_factor (:369-479) with
+//                       BiCGSTAB on the meridional grid.
+//
+// The Krylov iterations of the reference come from jax.scipy.sparse.linalg
+// (JAX >= 0.9.2, not part of the reference checkout): textbook conjugate
+// gradients (Hestenes-Stiefel) and BiCGSTAB (van der Vorst 1992), started from
+// zero, stopping once r.r <= max(tol^2 b.b, atol^2) or after maxiter
+// iterations; BiCGSTAB also stops early when s.s < that bound and on
+// breakdown (rho, alpha or omega zero).  Here every iteration is a few
+// kernels on the caller's stream with no host round trip: each kernel's blocks
+// write partial dot products, the last block to finish (a ticket counter, no
+// waiting) folds them in a fixed order and updates a small control record that
+// the next kernel reads; kernels launched after convergence return at once.
+// The host reads the control record once per chunk of iterations and once per
+// Newton step (the residual history).  Dot products are folded in a fixed
+// order, so a solve is deterministic run to run.
+//
+// Storage: every vector spans the full grid (the reference's padded shape);
+// unknowns live at the interior cells and the fixed outer cells hold zero, so
+// stencils read zero-valued neighbours with no branches.  Inside the Krylov
+// loop the Laplacian multiplies by 1/dx^2 instead of dividing; the operators
+// exported on their own keep the reference's divisions.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/bssn_gb300.h"
+#include "bssn_driver.h"
+#include "bssn_profile.h"
+
+namespace bssn {
+namespace {
+
+constexpr int kPunctThreads = 256;
+constexpr int kMaxPunctures = BSSN_MAX_PUNCTURES;
+constexpr int kMaxSums = 3;              // dot products folded per kernel
+constexpr int kUpdateBlocks = 152 * 4;   // grid of the vector-update kernels
+constexpr int kChunk = 16;               // Krylov iterations enqueued between host checks (even)
+
+static inline unsigned pblocks(long long n) { return (unsigned)((n + kPunctThreads - 1) / kPunctThreads); }
+
+struct Punctures {
+    int n;
+    double m[kMaxPunctures];
+    double x[kMaxPunctures][3];
+    double p[kMaxPunctures][3];
+};
+
+// ---------------------------------------------------------------------------
+// puncture fields (bowen_york_solver.py:52-101)
+// ---------------------------------------------------------------------------
+__global__ void k_puncture_fields(const double* __restrict__ grid, long long npts, Punctures P,
+                                  double* __restrict__ psi_bl, double* __restrict__ curvature,
+                                  double* __restrict__ curvature_squared) {
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < npts;
+         t += (long long)gridDim.x * blockDim.x) {
+        const double g[3] = {grid[3 * t], grid[3 * t + 1], grid[3 * t + 2]};
+        double bl = 0.0;
+        double K[9] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        for (int a = 0; a < P.n; ++a) {
+            double d[3];
+#pragma unroll
+            for (int i = 0; i < 3; ++i) d[i] = __dadd_rn(g[i], -P.x[a][i]);
+            const double rsq = __dadd_rn(__dadd_rn(__dmul_rn(d[0], d[0]), __dmul_rn(d[1], d[1])), __dmul_rn(d[2], d[2]));
+            const double r = __dsqrt_rn(rsq);
+            const double term = __ddiv_rn(P.m[a], __dmul_rn(2.0, r));
+            bl = a == 0 ? term : __dadd_rn(bl, term);
+            double nrm[3];
+#pragma unroll
+            for (int i = 0; i < 3; ++i) nrm[i] = __ddiv_rn(d[i], r);
+            const double pdn =
+                __dadd_rn(__dadd_rn(__dmul_rn(P.p[a][0], nrm[0]), __dmul_rn(P.p[a][1], nrm[1])), __dmul_rn(P.p[a][2], nrm[2]));
+            const double c = __ddiv_rn(3.0, __dmul_rn(2.0, __dmul_rn(r, r)));
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) {
+                    const double pn = __dadd_rn(__dmul_rn(P.p[a][i], nrm[j]), __dmul_rn(nrm[i], P.p[a][j]));
+                    const double tr = __dadd_rn(i == j ? 1.0 : 0.0, -__dmul_rn(nrm[i], nrm[j]));
+                    const double v = __dmul_rn(c, __dadd_rn(pn, -__dmul_rn(tr, pdn)));
+                    K[3 * i + j] = a == 0 ? v : __dadd_rn(K[3 * i + j], v);
+                }
+        }
+        if (psi_bl) psi_bl[t] = __dadd_rn(1.0, bl);
+        if (curvature)
+#pragma unroll
+            for (int q = 0; q < 9; ++q) curvature[9 * t + q] = K[q];
+        if (curvature_squared) {
+            double s = __dmul_rn(K[0], K[0]);
+#pragma unroll
+            for (int q = 1; q < 9; ++q) s = __dadd_rn(s, __dmul_rn(K[q], K[q]));
+            curvature_squared[t] = s;
+        }
+    }
+}
+
+__global__ void k_contract(const double* __restrict__ curvature, long long npts, double* __restrict__ out) {
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < npts;
+         t += (long long)gridDim.x * blockDim.x) {
+        double s = __dmul_rn(curvature[9 * t], curvature[9 * t]);
+#pragma unroll
+        for (int q = 1; q < 9; ++q) s = __dadd_rn(s, __dmul_rn(curvature[9 * t + q], curvature[9 * t + q]));
+        out[t] = s;
+    }
+}
+
+// psi^-7 and psi^-8 as integer powers: binary powering, then one reciprocal
+__device__ __forceinline__ double inv_pow7(double x) {
+    const double x2 = __dmul_rn(x, x), x3 = __dmul_rn(x2, x), x4 = __dmul_rn(x2, x2);
+    return __ddiv_rn(1.0, __dmul_rn(x3, x4));
+}
+__device__ __forceinline__ double inv_pow8(double x) {
+    const double x2 = __dmul_rn(x, x), x4 = __dmul_rn(x2, x2);
+    return __ddiv_rn(1.0, __dmul_rn(x4, x4));
+}
+
+// S = 1/8 A^2 psi^-7 and dS = -7/8 A^2 psi^-8 (:151-162), left to right
+__device__ __forceinline__ double source_of(double psi, double a2) {
+    return __dmul_rn(__dmul_rn(0.125, a2), inv_pow7(psi));
+}
+__device__ __forceinline__ double lin_coefficient(double psi, double a2) {
+    return __dmul_rn(__dmul_rn(-0.875, a2), inv_pow8(psi));
+}
+
+// ---------------------------------------------------------------------------
+// Grids.  Cartesian: full extent n[0] x n[1] x n[2], unknowns at 1..n-2 on
+// every axis.  Axisymmetric: n = (Nrho, 1, Nz), unknowns at rho 0..Nrho-2 and
+// z 1..Nz-2; the regular ghost u(-dx/2) = u(dx/2) closes the axis.
+// ---------------------------------------------------------------------------
+struct SolveGrid {
+    int n[3];
+    int axi;
+    double dx, dx2, inv_dx2;
+    __host__ __device__ long long size() const { return (long long)n[0] * n[1] * n[2]; }
+    __host__ __device__ bool interior(int i, int j, int k) const {
+        if (axi) return i <= n[0] - 2 && k >= 1 && k <= n[2] - 2;
+        return i >= 1 && i <= n[0] - 2 && j >= 1 && j <= n[1] - 2 && k >= 1 && k <= n[2] - 2;
+    }
+    __host__ __device__ long long unknowns() const {
+        if (axi) return (long long)(n[0] - 1) * (n[2] - 2);
+        return (long long)(n[0] - 2) * (n[1] - 2) * (n[2] - 2);
+    }
+};
+
+__device__ __forceinline__ void decompose(const SolveGrid& G, long long t, int& i, int& j, int& k) {
+    const long long plane = (long long)G.n[1] * G.n[2];
+    i = (int)(t / plane);
+    const long long r = t - (long long)i * plane;
+    j = (int)(r / G.n[2]);
+    k = (int)(r - (long long)j * G.n[2]);
+}
+
+// Reference-order Laplacians at an interior cell of a full-grid vector whose
+// fixed cells are zero (exported operators and the Newton residual).
+template <class F>
+__device__ __forceinline__ double laplacian_exact(const SolveGrid& G, int i, int j, int k, F f) {
+    if (G.axi) {
+        const double c = f(i, 0, k);
+        const double rp = f(i + 1, 0, k);
+        const double rm = i == 0 ? c : f(i - 1, 0, k);
+        const double rho = __dmul_rn(__dadd_rn((double)i, 0.5), G.dx);
+        const double c2 = __dmul_rn(2.0, c);
+        const double radial_second = __ddiv_rn(__dadd_rn(__dadd_rn(rp, -c2), rm), G.dx2);
+        const double radial_first = __ddiv_rn(__dadd_rn(rp, -rm), __dmul_rn(__dmul_rn(2.0, rho), G.dx));
+        const double axial_second = __ddiv_rn(__dadd_rn(__dadd_rn(f(i, 0, k + 1), f(i, 0, k - 1)), -c2), G.dx2);
+        return __dadd_rn(__dadd_rn(radial_second, radial_first), axial_second);
+    }
+    double s = __dadd_rn(f(i + 1, j, k), f(i - 1, j, k));
+    s = __dadd_rn(s, f(i, j + 1, k));
+    s = __dadd_rn(s, f(i, j - 1, k));
+    s = __dadd_rn(s, f(i, j, k + 1));
+    s = __dadd_rn(s, f(i, j, k - 1));
+    return __ddiv_rn(__dadd_rn(s, -__dmul_rn(6.0, f(i, j, k))), G.dx2);
+}
+
+// ---------------------------------------------------------------------------
+// Exported operators (:104-230) on the reference's shapes.  Inputs/outputs of
+// the Laplacian and linearised operators are interior-shaped; they are
+// evaluated on a zero-padded full-grid copy.
+// ---------------------------------------------------------------------------
+__global__ void k_pad_interior(const double* __restrict__ in, SolveGrid G, double* __restrict__ full) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= G.size()) return;
+    int i, j, k;
+    decompose(G, t, i, j, k);
+    double v = 0.0;
+    if (G.interior(i, j, k)) {
+        if (G.axi) v = in[(long long)i * (G.n[2] - 2) + (k - 1)];
+        else v = in[((long long)(i - 1) * (G.n[1] - 2) + (j - 1)) * (G.n[2] - 2) + (k - 1)];
+    }
+    full[t] = v;
+}
+
+// op 0: Laplacian; op 1: linearised operator Lap(d) + dS(psi, A2) d;
+// op 2: residual Lap(u) + S(psi_bl + u, A2) with full-grid psi_bl and A2.
+// For ops 0/1, psi and A2 are interior-shaped.
+__global__ void k_operator(const double* __restrict__ full, const double* __restrict__ b, const double* __restrict__ c,
+                           SolveGrid G, int op, double* __restrict__ out) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= G.size()) return;
+    int i, j, k;
+    decompose(G, t, i, j, k);
+    if (!G.interior(i, j, k)) return;
+    const long long plane = (long long)G.n[1] * G.n[2];
+    auto f = [&](int x, int y, int z) { return full[(long long)x * plane + (long long)y * G.n[2] + z]; };
+    const long long o = G.axi ? (long long)i * (G.n[2] - 2) + (k - 1)
+                              : ((long long)(i - 1) * (G.n[1] - 2) + (j - 1)) * (G.n[2] - 2) + (k - 1);
+    const double lap = laplacian_exact(G, i, j, k, f);
+    double v = lap;
+    if (op == 1) v = __dadd_rn(lap, __dmul_rn(lin_coefficient(b[o], c[o]), f(i, j, k)));
+    if (op == 2) v = __dadd_rn(lap, source_of(__dadd_rn(b[t], f(i, j, k)), c[t]));
+    out[o] = v;
+}
+
+__global__ void k_pointwise(const double* __restrict__ a, const double* __restrict__ b, const double* __restrict__ c,
+                            long long n, int op, double* __restrict__ out) {
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        out[t] = op == 0 ? source_of(a[t], b[t]) : __dmul_rn(lin_coefficient(b[t], c[t]), a[t]);
+}
+
+// ---------------------------------------------------------------------------
+// Solver control record and deterministic block folds
+// ---------------------------------------------------------------------------
+struct SolveCtrl {
+    double gamma;        // r.r of the current iterate
+    double alpha, beta, omega, rho;
+    double atol2;        // stopping bound on r.r
+    double bb;           // b.b of the Newton residual
+    double rms;          // Newton residual RMS
+    int k, maxiter, done, first;
+    int bad_psi, bad_u;  // Newton-level checks (axisymmetric solve)
+    unsigned ticket;
+    int pad;
+};
+
+// Block sum of NS values in a fixed order (warp shuffles, then warp 0).
+template <int NS>
+__device__ __forceinline__ void block_sums(double (&v)[NS], double (*shared)[32]) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nwarps = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int q = 0; q < NS; ++q) {
+        double s = v[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (lane == 0) shared[q][warp] = s;
+    }
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int q = 0; q < NS; ++q) {
+            double s = lane < nwarps ? shared[q][lane] : 0.0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+            v[q] = s;
+        }
+    }
+}
+
+// Writes this block's partials; returns true in the one block that finishes
+// last, in which every thread then holds the fixed-order fold of all blocks'
+// partials in `tot` (thread 0's copy is the one used).
+template <int NS>
+__device__ bool fold_last(double (&v)[NS], double* __restrict__ partial, unsigned* ticket, double (&tot)[NS]) {
+    __shared__ double sh[NS][32];
+    __shared__ bool last;
+    const unsigned nblocks = gridDim.x * gridDim.y * gridDim.z;
+    const unsigned bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    const int tid = threadIdx.x;
+    block_sums<NS>(v, sh);
+    if (tid == 0) {
+#pragma unroll
+        for (int q = 0; q < NS; ++q) partial[(long long)bid * NS + q] = v[q];
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == nblocks - 1;
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    double s[NS];
+#pragma unroll
+    for (int q = 0; q < NS; ++q) s[q] = 0.0;
+    for (unsigned b = tid; b < nblocks; b += blockDim.x)
+#pragma unroll
+        for (int q = 0; q < NS; ++q) s[q] += __ldcg(partial + (long long)b * NS + q);
+    __syncthreads();
+    block_sums<NS>(s, sh);
+#pragma unroll
+    for (int q = 0; q < NS; ++q) tot[q] = s[q];
+    if (tid == 0) *ticket = 0u;
+    return true;
+}
+
+__device__ __forceinline__ SolveCtrl read_ctrl(const SolveCtrl* c) {
+    SolveCtrl r;
+    const double* d = reinterpret_cast<const double*>(c);
+#pragma unroll
+    for (int q = 0; q < (int)(sizeof(SolveCtrl) / sizeof(double)); ++q)
+        reinterpret_cast<double*>(&r)[q] = __ldcg(d + q);
+    return r;
+}
+
+// ---------------------------------------------------------------------------
+// Newton level: residual F(u) = Lap(u) + S(psi_bl + u) at the interior (zero at
+// fixed cells), the Jacobian's source coefficient dS/du, the residual RMS, and
+// the Krylov start: x = 0 follows from a memset; r = b = F; r.r = b.b.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kPunctThreads)
+k_newton_residual(const double* __restrict__ u, const double* __restrict__ psi_bl, const double* __restrict__ a2,
+                  SolveGrid G, double* __restrict__ r, double* __restrict__ rhat, double* __restrict__ lin,
+                  double* __restrict__ partial, SolveCtrl* ctrl, double tol2, int maxiter) {
+    double acc[3] = {0.0, 0.0, 0.0};   // F.F, nonpositive psi, nonfinite u
+    const long long plane = (long long)G.n[1] * G.n[2];
+    auto f = [&](int x, int y, int z) { return u[(long long)x * plane + (long long)y * G.n[2] + z]; };
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < G.size();
+         t += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        decompose(G, t, i, j, k);
+        double res = 0.0, coef = 0.0;
+        if (G.interior(i, j, k)) {
+            const double psi = __dadd_rn(psi_bl[t], u[t]);
+            res = __dadd_rn(laplacian_exact(G, i, j, k, f), source_of(psi, a2[t]));
+            coef = lin_coefficient(psi, a2[t]);
+            acc[0] += res * res;
+            if (!(psi > 0.0)) acc[1] += 1.0;
+            if (!isfinite(u[t])) acc[2] += 1.0;
+        }
+        r[t] = res;
+        if (rhat) rhat[t] = res;
+        lin[t] = coef;
+    }
+    double tot[3];
+    if (!fold_last<3>(acc, partial, &ctrl->ticket, tot)) return;
+    if (threadIdx.x == 0) {
+        const double bb = tot[0];
+        ctrl->bb = bb;
+        ctrl->gamma = bb;
+        ctrl->rms = sqrt(bb / (double)G.unknowns());
+        ctrl->atol2 = tol2 * bb;
+        ctrl->k = 0;
+        ctrl->maxiter = maxiter;
+        ctrl->first = 1;
+        ctrl->alpha = ctrl->omega = 1.0;
+        ctrl->rho = bb;   // rhat.r with rhat = r = b
+        ctrl->beta = 0.0;
+        ctrl->done = !(bb > ctrl->atol2 && maxiter > 0);
+        ctrl->bad_psi = tot[1] > 0.0;
+        ctrl->bad_u = tot[2] > 0.0;
+    }
+}
+
+__global__ void k_newton_update(double* __restrict__ u, const double* __restrict__ x, long long n) {
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        u[t] = u[t] + x[t];
+}
+
+__global__ void k_psi_total(const double* __restrict__ psi_bl, const double* __restrict__ u, double* __restrict__ psi,
+                            long long n) {
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        psi[t] = psi_bl[t] + u[t];
+}
+
+// ---------------------------------------------------------------------------
+// Conjugate gradients on A = -(Lap + dS) (Cartesian).  One iteration:
+//   k_cg_apply   p = r + beta p_prev (p = r at the first), Ap, p.Ap
+//                -> alpha = gamma / p.Ap
+//   k_cg_update  x += alpha p, r -= alpha Ap, r.r -> beta, gamma, k, done
+// The apply kernel stages p of one x plane of a 32 x 8 (z, y) tile in shared
+// memory, with its one-cell halo, and marches along x over a chunk of planes,
+// carrying the x neighbours in registers: each p value is formed once per
+// tile (plus the halo) instead of once per stencil tap.  p ping-pongs between
+// two buffers, since neighbouring tiles still read the previous p.
+// ---------------------------------------------------------------------------
+constexpr int kTz = 32, kTy = 8, kXc = 16;
+
+__global__ void __launch_bounds__(kTz* kTy)
+k_cg_apply(const double* __restrict__ r, const double* __restrict__ pin, double* __restrict__ pout,
+           const double* __restrict__ lin, double* __restrict__ ap, SolveGrid G, SolveCtrl* ctrl,
+           double* __restrict__ partial) {
+    __shared__ double tile[kTy + 2][kTz + 2];
+    const SolveCtrl C = read_ctrl(ctrl);
+    if (C.done) return;
+    const bool first = C.first != 0;
+    const double beta = C.beta;
+    const int tz = threadIdx.x % kTz, ty = threadIdx.x / kTz;
+    const int tiles_z = (G.n[2] - 2 + kTz - 1) / kTz;
+    const int z = 1 + (blockIdx.x % tiles_z) * kTz + tz;
+    const int y = 1 + (blockIdx.x / tiles_z) * kTy + ty;
+    const int x0 = 1 + blockIdx.y * kXc;
+    const int x1 = min(x0 + kXc, G.n[0] - 1);
+    const long long sx = (long long)G.n[1] * G.n[2], sy = G.n[2];
+    const bool in_yz = y <= G.n[1] - 1 && z <= G.n[2] - 1;   // y, z >= 1 by construction
+    const bool interior = y <= G.n[1] - 2 && z <= G.n[2] - 2;
+    auto pnew = [&](long long idx) { return first ? r[idx] : fma(beta, pin[idx], r[idx]); };
+    const long long own = (long long)y * sy + z;
+    double pm = in_yz ? pnew((long long)(x0 - 1) * sx + own) : 0.0;
+    double pc = in_yz ? pnew((long long)x0 * sx + own) : 0.0;
+    double dot[1] = {0.0};
+    for (int x = x0; x < x1; ++x) {
+        const long long base = (long long)x * sx;
+        const double pn = in_yz ? pnew(base + sx + own) : 0.0;
+        tile[ty + 1][tz + 1] = pc;
+        if (ty == 0) tile[0][tz + 1] = z <= G.n[2] - 1 ? pnew(base + own - sy) : 0.0;
+        if (ty == kTy - 1) tile[kTy + 1][tz + 1] = (y + 1 <= G.n[1] - 1 && z <= G.n[2] - 1) ? pnew(base + own + sy) : 0.0;
+        if (tz == 0) tile[ty + 1][0] = y <= G.n[1] - 1 ? pnew(base + own - 1) : 0.0;
+        if (tz == kTz - 1) tile[ty + 1][kTz + 1] = (y <= G.n[1] - 1 && z + 1 <= G.n[2] - 1) ? pnew(base + own + 1) : 0.0;
+        __syncthreads();
+        if (interior) {
+            double s = pn + pm;
+            s += tile[ty + 2][tz + 1];
+            s += tile[ty][tz + 1];
+            s += tile[ty + 1][tz + 2];
+            s += tile[ty + 1][tz];
+            const double lap = fma(-6.0, pc, s) * G.inv_dx2;
+            const double a = -fma(lin[base + own], pc, lap);
+            pout[base + own] = pc;
+            ap[base + own] = a;
+            dot[0] = fma(pc, a, dot[0]);
+        }
+        __syncthreads();
+        pm = pc;
+        pc = pn;
+    }
+    double tot[1];
+    if (!fold_last<1>(dot, partial, &ctrl->ticket, tot)) return;
+    if (threadIdx.x == 0) ctrl->alpha = C.gamma / tot[0];
+}
+
+__global__ void __launch_bounds__(kPunctThreads)
+k_cg_update(double* __restrict__ x, double* __restrict__ r, const double* __restrict__ p, const double* __restrict__ ap,
+            long long n, SolveCtrl* ctrl, double* __restrict__ partial) {
+    const SolveCtrl C = read_ctrl(ctrl);
+    if (C.done) return;
+    const double alpha = C.alpha;
+    double rr[1] = {0.0};
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        x[t] = fma(alpha, p[t], x[t]);
+        const double rn = fma(-alpha, ap[t], r[t]);
+        r[t] = rn;
+        rr[0] = fma(rn, rn, rr[0]);
+    }
+    double tot[1];
+    if (!fold_last<1>(rr, partial, &ctrl->ticket, tot)) return;
+    if (threadIdx.x == 0) {
+        ctrl->beta = tot[0] / C.gamma;
+        ctrl->gamma = tot[0];
+        ctrl->k = C.k + 1;
+        ctrl->first = 0;
+        ctrl->done = !(tot[0] > C.atol2 && C.k + 1 < C.maxiter);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// BiCGSTAB on A = -(Lap_axi + dS) (meridional grid, small: one thread per cell,
+// vector combinations formed at each stencil tap).  One iteration:
+//   k_bicg_p   p = r + beta (p_prev - omega q_prev) (p = r at the first),
+//              q = A p, rhat.q -> alpha = rho / rhat.q
+//   k_bicg_s   s = r - alpha q, t = A s, s.s, t.s, t.t -> omega, early exit
+//   k_bicg_x   x += alpha p (+ omega s), r = s (- omega t), r.r, rhat.r
+//              -> beta, rho, k, done (convergence, maxiter or breakdown)
+// ---------------------------------------------------------------------------
+template <class F>
+__device__ __forceinline__ double axi_operator(const SolveGrid& G, int i, int k, double lin_c, F f) {
+    const double c = f(i, k);
+    const double rp = f(i + 1, k);
+    const double rm = i == 0 ? c : f(i - 1, k);
+    const double inv_2rho_dx = 1.0 / (2.0 * ((i + 0.5) * G.dx) * G.dx);
+    const double radial_second = (rp - 2.0 * c + rm) * G.inv_dx2;
+    const double radial_first = (rp - rm) * inv_2rho_dx;
+    const double axial_second = (f(i, k + 1) + f(i, k - 1) - 2.0 * c) * G.inv_dx2;
+    return -(radial_second + radial_first + axial_second + lin_c * c);
+}
+
+__global__ void __launch_bounds__(kPunctThreads)
+k_bicg_p(const double* __restrict__ r, const double* __restrict__ rhat, const double* __restrict__ pin,
+         const double* __restrict__ qin, double* __restrict__ pout, double* __restrict__ qout,
+         const double* __restrict__ lin, SolveGrid G, SolveCtrl* ctrl, double* __restrict__ partial) {
+    const SolveCtrl C = read_ctrl(ctrl);
+    if (C.done) return;
+    const bool first = C.first != 0;
+    const double beta = C.beta, omega = C.omega;
+    const int nz = G.n[2];
+    auto pv = [&](int i, int k) {
+        const long long o = (long long)i * nz + k;
+        return first ? r[o] : fma(beta, fma(-omega, qin[o], pin[o]), r[o]);
+    };
+    double acc[1] = {0.0};
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < G.size();
+         t += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(t / nz), k = (int)(t - (long long)i * nz);
+        if (!G.interior(i, 0, k)) continue;
+        const double q = axi_operator(G, i, k, lin[t], pv);
+        pout[t] = pv(i, k);
+        qout[t] = q;
+        acc[0] = fma(rhat[t], q, acc[0]);
+    }
+    double tot[1];
+    if (!fold_last<1>(acc, partial, &ctrl->ticket, tot)) return;
+    if (threadIdx.x == 0) ctrl->alpha = C.rho / tot[0];
+}
+
+__global__ void __launch_bounds__(kPunctThreads)
+k_bicg_s(const double* __restrict__ r, const double* __restrict__ q, double* __restrict__ s, double* __restrict__ tv,
+         const double* __restrict__ lin, SolveGrid G, SolveCtrl* ctrl, double* __restrict__ partial) {
+    const SolveCtrl C = read_ctrl(ctrl);
+    if (C.done) return;
+    const double alpha = C.alpha;
+    const int nz = G.n[2];
+    auto sv = [&](int i, int k) {
+        const long long o = (long long)i * nz + k;
+        return fma(-alpha, q[o], r[o]);
+    };
+    double acc[3] = {0.0, 0.0, 0.0};   // s.s, t.s, t.t
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < G.size();
+         t += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(t / nz), k = (int)(t - (long long)i * nz);
+        if (!G.interior(i, 0, k)) continue;
+        const double sc = sv(i, k);
+        const double tt = axi_operator(G, i, k, lin[t], sv);
+        s[t] = sc;
+        tv[t] = tt;
+        acc[0] = fma(sc, sc, acc[0]);
+        acc[1] = fma(tt, sc, acc[1]);
+        acc[2] = fma(tt, tt, acc[2]);
+    }
+    double tot[3];
+    if (!fold_last<3>(acc, partial, &ctrl->ticket, tot)) return;
+    if (threadIdx.x == 0) {
+        const bool early = tot[0] < C.atol2;
+        ctrl->omega = early ? 0.0 : tot[1] / tot[2];
+        ctrl->first = early ? -1 : 0;   // -1 marks the early exit for k_bicg_x
+    }
+}
+
+__global__ void __launch_bounds__(kPunctThreads)
+k_bicg_x(double* __restrict__ x, double* __restrict__ r, const double* __restrict__ rhat, const double* __restrict__ p,
+         const double* __restrict__ s, const double* __restrict__ tv, long long n, SolveCtrl* ctrl,
+         double* __restrict__ partial) {
+    const SolveCtrl C = read_ctrl(ctrl);
+    if (C.done) return;
+    const bool early = C.first == -1;
+    const double alpha = C.alpha, omega = C.omega;
+    double acc[2] = {0.0, 0.0};   // r.r, rhat.r
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        const double xa = fma(alpha, p[t], x[t]);
+        double rn;
+        if (early) {
+            x[t] = xa;
+            rn = s[t];
+        } else {
+            x[t] = fma(omega, s[t], xa);
+            rn = fma(-omega, tv[t], s[t]);
+        }
+        r[t] = rn;
+        acc[0] = fma(rn, rn, acc[0]);
+        acc[1] = fma(rhat[t], rn, acc[1]);
+    }
+    double tot[2];
+    if (!fold_last<2>(acc, partial, &ctrl->ticket, tot)) return;
+    if (threadIdx.x == 0) {
+        const int k = C.k + 1;
+        const double rho = tot[1];
+        const bool breakdown = (!early && (omega == 0.0 || alpha == 0.0)) || rho == 0.0;
+        ctrl->beta = (rho / C.rho) * (alpha / omega);
+        ctrl->rho = rho;
+        ctrl->gamma = tot[0];
+        ctrl->k = k;
+        ctrl->first = 0;
+        ctrl->done = early || breakdown || !(tot[0] > C.atol2 && k < C.maxiter);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// workspace: 10 full-grid vectors, the partial sums, the control record
+// ---------------------------------------------------------------------------
+enum { V_R, V_RHAT, V_LIN, V_X, V_P0, V_P1, V_Q, V_S, V_T, V_SPARE, V_COUNT };
+
+int grid_of(const int32_t shape[3], int axi, double dx, SolveGrid& G) {
+    if (!shape) return fail(BSSN_ERR_INVALID, "null shape");
+    for (int a = 0; a < 3; ++a) G.n[a] = shape[a];
+    G.axi = axi ? 1 : 0;
+    if (G.axi) {
+        if (shape[1] != 1 || shape[0] < 2 || shape[2] < 3)
+            return fail(BSSN_ERR_INVALID, "grid requires at least two rho and three z cells");
+    } else if (shape[0] < 3 || shape[1] < 3 || shape[2] < 3) {
+        return fail(BSSN_ERR_INVALID, "every grid axis needs at least three cells");
+    }
+    if (!(dx > 0.0) || !std::isfinite(dx)) return fail(BSSN_ERR_INVALID, "dx must be finite and positive");
+    G.dx = dx;
+    G.dx2 = dx * dx;
+    G.inv_dx2 = 1.0 / G.dx2;
+    return BSSN_OK;
+}
+
+long long max_blocks(const SolveGrid& G) {
+    long long apply = 0;
+    if (!G.axi) {
+        const long long tz = (G.n[2] - 2 + kTz - 1) / kTz, ty = (G.n[1] - 2 + kTy - 1) / kTy;
+        const long long tx = (G.n[0] - 2 + kXc - 1) / kXc;
+        apply = tz * ty * tx;
+    }
+    return std::max<long long>(apply, kUpdateBlocks);
+}
+
+size_t workspace_bytes(const SolveGrid& G) {
+    const size_t vec = (size_t)G.size() * sizeof(double);
+    const size_t vec_al = (vec + 255) & ~(size_t)255;
+    return V_COUNT * vec_al + (size_t)max_blocks(G) * kMaxSums * sizeof(double) + 256 + sizeof(SolveCtrl);
+}
+
+unsigned update_blocks(long long n) { return (unsigned)std::min<long long>(pblocks(n), kUpdateBlocks); }
+
+}  // namespace
+}  // namespace bssn
+
+using namespace bssn;
+
+extern "C" {
+
+int bssn_puncture_fields(const double* grid, int64_t npoints, const double* masses, const double* positions,
+                         const double* momenta, int32_t npunctures, double* psi_bl, double* curvature,
+                         double* curvature_squared, void* stream) {
+    if (!grid || !masses || !positions || !momenta) return fail(BSSN_ERR_INVALID, "bssn_puncture_fields: null pointer");
+    if (npunctures < 1 || npunctures > kMaxPunctures)
+        return fail(BSSN_ERR_INVALID, "between 1 and " + std::to_string(kMaxPunctures) + " punctures");
+    if (npoints < 0) return fail(BSSN_ERR_INVALID, "npoints must be non-negative");
+    Punctures P;
+    std::memset(&P, 0, sizeof(P));
+    P.n = npunctures;
+    for (int a = 0; a < npunctures; ++a) {
+        P.m[a] = masses[a];
+        for (int i = 0; i < 3; ++i) {
+            P.x[a][i] = positions[3 * a + i];
+            P.p[a][i] = momenta[3 * a + i];
+        }
+    }
+    if (npoints == 0) return BSSN_OK;
+    const unsigned blocks = (unsigned)std::min<long long>(pblocks(npoints), 152 * 16);
+    BSSN_LAUNCH(KC_SOLVE_NEWTON, k_puncture_fields, blocks, kPunctThreads, (cudaStream_t)stream, grid, npoints, P,
+                psi_bl, curvature, curvature_squared);
+    return cuda_status(cudaGetLastError(), "bssn_puncture_fields");
+}
+
+int bssn_puncture_operator(int32_t op, const double* a, const double* b, const double* c, const int32_t shape[3],
+                           double dx, int32_t axisymmetric, double* out, void* workspace, size_t workspace_bytes_,
+                           void* stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!a || !out) return fail(BSSN_ERR_INVALID, "bssn_puncture_operator: null pointer");
+    if (op == BSSN_PUNCTURE_CONTRACT || op == BSSN_PUNCTURE_SOURCE || op == BSSN_PUNCTURE_LINEARIZED_SOURCE) {
+        if (!shape || shape[0] < 0 || shape[1] < 0 || shape[2] < 0)
+            return fail(BSSN_ERR_INVALID, "array extents must be non-negative");
+        const long long n = (long long)shape[0] * shape[1] * shape[2];
+        if (n == 0) return BSSN_OK;
+        const unsigned blocks = (unsigned)std::min<long long>(pblocks(n), 152 * 16);
+        if (op == BSSN_PUNCTURE_CONTRACT) {
+            BSSN_LAUNCH(KC_SOLVE_NEWTON, k_contract, blocks, kPunctThreads, s, a, n, out);
+        } else {
+            if (!b || (op == BSSN_PUNCTURE_LINEARIZED_SOURCE && !c))
+                return fail(BSSN_ERR_INVALID, "bssn_puncture_operator: null pointer");
+            BSSN_LAUNCH(KC_SOLVE_NEWTON, k_pointwise, blocks, kPunctThreads, s, a, b, c, n,
+                        op == BSSN_PUNCTURE_SOURCE ? 0 : 1, out);
+        }
+        return cuda_status(cudaGetLastError(), "bssn_puncture_operator");
+    }
+    if (op != BSSN_PUNCTURE_LAPLACIAN && op != BSSN_PUNCTURE_LINEARIZED_OPERATOR && op != BSSN_PUNCTURE_RESIDUAL)
+        return fail(BSSN_ERR_INVALID, "unknown puncture operator");
+    SolveGrid G;
+    if (int e = grid_of(shape, axisymmetric, dx, G)) return e;
+    if (op != BSSN_PUNCTURE_LAPLACIAN && (!b || !c)) return fail(BSSN_ERR_INVALID, "bssn_puncture_operator: null pointer");
+    const long long n = G.size();
+    const double* full = a;
+    if (op != BSSN_PUNCTURE_RESIDUAL) {
+        if (!workspace || workspace_bytes_ < (size_t)n * sizeof(double))
+            return fail(BSSN_ERR_WORKSPACE, "workspace must hold one full-grid array");
+        double* pad = static_cast<double*>(workspace);
+        BSSN_LAUNCH(KC_SOLVE_NEWTON, k_pad_interior, pblocks(n), kPunctThreads, s, a, G, pad);
+        full = pad;
+    }
+    const int code = op == BSSN_PUNCTURE_LAPLACIAN ? 0 : op == BSSN_PUNCTURE_LINEARIZED_OPERATOR ? 1 : 2;
+    BSSN_LAUNCH(KC_SOLVE_NEWTON, k_operator, pblocks(n), kPunctThreads, s, full, b, c, G, code, out);
+    return cuda_status(cudaGetLastError(), "bssn_puncture_operator");
+}
+
+size_t bssn_puncture_workspace_bytes(const int32_t shape[3], int32_t axisymmetric) {
+    SolveGrid G;
+    if (grid_of(shape, axisymmetric, 1.0, G)) return 0;
+    return workspace_bytes(G);
+}
+
+int bssn_puncture_solve(const double* psi_bl, const double* curvature_squared, const int32_t shape[3], double dx,
+                        int32_t axisymmetric, double newton_tolerance, int32_t max_newton_iterations,
+                        double linear_tolerance, int32_t max_linear_iterations, double* u, double* psi,
+                        double* residual_history, int32_t* history_length, int32_t* linear_iterations,
+                        void* workspace, size_t workspace_bytes_, void* stream) {
+    if (!psi_bl || !curvature_squared || !u || !psi || !residual_history || !history_length)
+        return fail(BSSN_ERR_INVALID, "bssn_puncture_solve: null pointer");
+    SolveGrid G;
+    if (int e = grid_of(shape, axisymmetric, dx, G)) return e;
+    if (!(newton_tolerance > 0.0) || !std::isfinite(newton_tolerance))
+        return fail(BSSN_ERR_INVALID, "newton_tolerance must be finite and positive");
+    if (!(linear_tolerance > 0.0) || !std::isfinite(linear_tolerance))
+        return fail(BSSN_ERR_INVALID, "linear_tolerance must be finite and positive");
+    if (max_newton_iterations < 0) return fail(BSSN_ERR_INVALID, "max_newton_iterations must be a nonnegative integer");
+    if (max_linear_iterations < 1) return fail(BSSN_ERR_INVALID, "max_linear_iterations must be a positive integer");
+    if (!workspace || workspace_bytes_ < workspace_bytes(G))
+        return fail(BSSN_ERR_WORKSPACE, "workspace missing or smaller than bssn_puncture_workspace_bytes()");
+
+    cudaStream_t s = (cudaStream_t)stream;
+    const long long n = G.size();
+    const size_t vec_al = ((size_t)n * sizeof(double) + 255) & ~(size_t)255;
+    char* base = static_cast<char*>(workspace);
+    double* v[V_COUNT];
+    for (int q = 0; q < V_COUNT; ++q) v[q] = reinterpret_cast<double*>(base + q * vec_al);
+    double* partial = reinterpret_cast<double*>(base + V_COUNT * vec_al);
+    const size_t pbytes = (size_t)max_blocks(G) * kMaxSums * sizeof(double);
+    SolveCtrl* ctrl = reinterpret_cast<SolveCtrl*>(base + V_COUNT * vec_al + ((pbytes + 255) & ~(size_t)255));
+
+    cudaError_t e = cudaMemsetAsync(base, 0, V_COUNT * vec_al, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctrl, 0, sizeof(SolveCtrl), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(u, 0, (size_t)n * sizeof(double), s);
+    if (e != cudaSuccess) return cuda_status(e, "bssn_puncture_solve");
+
+    const unsigned ub = update_blocks(n);
+    dim3 apply_grid(1, 1, 1);
+    if (!G.axi) {
+        const int tz = (G.n[2] - 2 + kTz - 1) / kTz, ty = (G.n[1] - 2 + kTy - 1) / kTy;
+        apply_grid = dim3(tz * ty, (G.n[0] - 2 + kXc - 1) / kXc, 1);
+    }
+    const double tol2 = linear_tolerance * linear_tolerance;
+    SolveCtrl host;
+    int count = 0;
+    for (int it = 0; it <= max_newton_iterations; ++it) {
+        BSSN_LAUNCH(KC_SOLVE_NEWTON, k_newton_residual, ub, kPunctThreads, s, u, psi_bl, curvature_squared, G, v[V_R],
+                    G.axi ? v[V_RHAT] : nullptr, v[V_LIN], partial, ctrl, tol2, max_linear_iterations);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&host, ctrl, sizeof(SolveCtrl), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return cuda_status(e, "bssn_puncture_solve");
+        if (G.axi && it > 0) {
+            // checks of the previous correction (bowen_york_solver.py:471-474)
+            if (host.bad_u) {
+                *history_length = count;
+                return fail(BSSN_ERR_NONFINITE, "Newton-Raphson correction is nonfinite");
+            }
+            if (host.bad_psi) {
+                *history_length = count;
+                return fail(BSSN_ERR_NONFINITE, "Newton-Raphson correction made psi nonpositive");
+            }
+        }
+        residual_history[count++] = host.rms;
+        *history_length = count;
+        if (G.axi && !std::isfinite(host.rms))
+            return fail(BSSN_ERR_NONFINITE, "Newton-Raphson solve produced a nonfinite residual");
+        if (host.rms <= newton_tolerance) break;
+        if (it == max_newton_iterations) {
+            char msg[160];
+            std::snprintf(msg, sizeof(msg), "Newton-Raphson solve did not converge: RMS residual %.3e exceeds %.3e.",
+                          host.rms, newton_tolerance);
+            return fail(BSSN_ERR_NOT_CONVERGED, msg);
+        }
+        e = cudaMemsetAsync(v[V_X], 0, (size_t)n * sizeof(double), s);
+        if (e != cudaSuccess) return cuda_status(e, "bssn_puncture_solve");
+        bool done = host.done != 0;
+        while (!done) {
+            for (int j = 0; j < kChunk; ++j) {
+                if (!G.axi) {
+                    double* pin = v[j % 2 ? V_P1 : V_P0];
+                    double* pout = v[j % 2 ? V_P0 : V_P1];
+                    BSSN_LAUNCH(KC_SOLVE_APPLY, k_cg_apply, apply_grid, kTz * kTy, s, v[V_R], pin, pout, v[V_LIN],
+                                v[V_Q], G, ctrl, partial);
+                    BSSN_LAUNCH(KC_SOLVE_UPDATE, k_cg_update, ub, kPunctThreads, s, v[V_X], v[V_R], pout, v[V_Q], n,
+                                ctrl, partial);
+                } else {
+                    // p and q both ping-pong: the apply kernel reads the previous p and q at stencil taps
+                    double* pin = v[j % 2 ? V_P1 : V_P0];
+                    double* pout = v[j % 2 ? V_P0 : V_P1];
+                    double* qin = v[j % 2 ? V_SPARE : V_Q];
+                    double* qout = v[j % 2 ? V_Q : V_SPARE];
+                    BSSN_LAUNCH(KC_SOLVE_APPLY, k_bicg_p, ub, kPunctThreads, s, v[V_R], v[V_RHAT], pin, qin, pout,
+                                qout, v[V_LIN], G, ctrl, partial);
+                    BSSN_LAUNCH(KC_SOLVE_APPLY, k_bicg_s, ub, kPunctThreads, s, v[V_R], qout, v[V_S], v[V_T],
+                                v[V_LIN], G, ctrl, partial);
+                    BSSN_LAUNCH(KC_SOLVE_UPDATE, k_bicg_x, ub, kPunctThreads, s, v[V_X], v[V_R], v[V_RHAT], pout,
+                                v[V_S], v[V_T], n, ctrl, partial);
+                }
+            }
+            e = cudaGetLastError();
+            if (e == cudaSuccess) e = cudaMemcpyAsync(&host, ctrl, sizeof(SolveCtrl), cudaMemcpyDeviceToHost, s);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+            if (e != cudaSuccess) return cuda_status(e, "bssn_puncture_solve");
+            done = host.done != 0;
+        }
+        if (linear_iterations) linear_iterations[it] = host.k;
+        BSSN_LAUNCH(KC_SOLVE_UPDATE, k_newton_update, ub, kPunctThreads, s, u, v[V_X], n);
+    }
+    BSSN_LAUNCH(KC_SOLVE_UPDATE, k_psi_total, ub, kPunctThreads, s, psi_bl, u, psi, n);
+    return cuda_status(cudaGetLastError(), "bssn_puncture_solve");
+}
+
+}  // extern "C"

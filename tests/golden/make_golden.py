@@ -371,6 +371,84 @@ def make_waves(out_dir: Path):
     np.savez_compressed(out_dir / "waves.npz", **data)
 
 
+def puncture_cases():
+    """Bowen-York solves: the reference suite's two boosted single punctures
+    (tests/test_bowen_york.py:57-110), a generic boosted binary on a Cartesian
+    grid, the axisymmetric collision's setup at reduced resolution
+    (demos/axisymmetric_blackhole_collision, tolerances 1e-12) and a
+    zero-momentum meridional grid (analytic Brill-Lindquist data)."""
+    return {
+        "cart_single": dict(axi=False, grid=(10, 5.0), masses=[1.0], positions=[[0.0, 0.0, 0.0]],
+                            momenta=[[0.0, 0.0, 0.2]], tol=(1.0e-9, 12, 1.0e-11, 1000)),
+        "cart_binary": dict(axi=False, grid=(20, 6.0), masses=[0.5, 0.4],
+                            positions=[[0.05, -0.12, -1.07], [-0.08, 0.11, 1.21]],
+                            momenta=[[0.1, -0.05, 0.2], [-0.1, 0.03, -0.15]], tol=(1.0e-10, 12, 1.0e-10, 1000)),
+        "axi_single": dict(axi=True, grid=(12, 5.0), masses=[1.0], positions=[[0.0, 0.0, 0.0]],
+                           momenta=[[0.0, 0.0, 0.2]], tol=(1.0e-9, 12, 1.0e-11, 1000)),
+        "axi_binary": dict(axi=True, grid=(32, 8.0), masses=[0.5, 0.5], positions=[[0.0, 0.0, -1.5], [0.0, 0.0, 1.5]],
+                           momenta=[[0.0, 0.0, 0.05], [0.0, 0.0, -0.05]], tol=(1.0e-12, 100, 1.0e-12, 1000)),
+        "axi_zero": dict(axi=True, grid=(8, 4.0), masses=[1.0], positions=[[0.0, 0.0, 0.0]],
+                         momenta=[[0.0, 0.0, 0.0]], tol=(1.0e-10, 12, 1.0e-10, 1000)),
+    }
+
+
+def make_puncture(out_dir: Path):
+    """utilities/bowen_york_solver.py: grids, Brill-Lindquist psi, Bowen-York
+    curvature, operators on seeded fields, and the Newton solves."""
+    import jax.numpy as jnp
+    from JAX_BSSN.utilities import bowen_york_solver as by
+    data = {}
+    for name, case in puncture_cases().items():
+        n, extent = case["grid"]
+        if case["axi"]:
+            grid, dx = by.axisymmetric_cell_centered_grid(n, extent)
+            solve = by.solve_axisymmetric_conformal_factor
+            kw = dict(newton_tolerance=case["tol"][0], max_newton_iterations=case["tol"][1],
+                      linear_tolerance=case["tol"][2], max_linear_iterations=case["tol"][3])
+        else:
+            grid, dx = by.cell_centered_grid(n, extent)
+            solve = by.solve_conformal_factor
+            kw = dict(newton_tolerance=case["tol"][0], max_newton_iterations=case["tol"][1],
+                      cg_tolerance=case["tol"][2], max_cg_iterations=case["tol"][3])
+        masses, positions, momenta = (jnp.asarray(case[k]) for k in ("masses", "positions", "momenta"))
+        psi, u, history = solve(masses, positions, momenta, grid, dx, **kw)
+        data[f"{name}.case"] = np.asarray(json.dumps(case))
+        data[f"{name}.grid"] = np.asarray(grid)
+        data[f"{name}.dx"] = np.asarray(dx)
+        data[f"{name}.psi_bl"] = np.asarray(by.brill_lindquist_conformal_factor(masses, positions, grid))
+        data[f"{name}.curvature"] = np.asarray(by.bowen_york_extrinsic_curvature(momenta, positions, grid))
+        data[f"{name}.psi"] = np.asarray(psi)
+        data[f"{name}.u"] = np.asarray(u)
+        data[f"{name}.history"] = np.asarray(history, dtype=np.float64)
+    # operators on seeded fields of the binary cases' grids
+    rng = np.random.default_rng(11)
+    for name in ("cart_binary", "axi_binary"):
+        grid = data[f"{name}.grid"]
+        dx = float(data[f"{name}.dx"])
+        axi = name.startswith("axi")
+        inner = (slice(None, -1), 0, slice(1, -1)) if axi else (slice(1, -1),) * 3
+        curvature = jnp.asarray(data[f"{name}.curvature"])
+        psi_bl = jnp.asarray(data[f"{name}.psi_bl"])
+        a2 = np.asarray(by.contract_conformal_curvature(curvature))
+        delta = rng.standard_normal(psi_bl[inner].shape)
+        u = np.zeros(psi_bl.shape)
+        u[inner] = 0.01 * rng.standard_normal(psi_bl[inner].shape)
+        psi = np.asarray(psi_bl)[inner] + u[inner]
+        data[f"{name}.a2"] = a2
+        data[f"{name}.delta"] = delta
+        data[f"{name}.u_probe"] = u
+        lap = by.axisymmetric_laplacian if axi else by.laplacian
+        lin = by.axisymmetric_linearized_hamiltonian_operator if axi else by.linearized_hamiltonian_operator
+        res = by.axisymmetric_hamiltonian_residual if axi else by.hamiltonian_residual
+        data[f"{name}.laplacian"] = np.asarray(lap(jnp.asarray(delta), dx))
+        data[f"{name}.linearized"] = np.asarray(lin(jnp.asarray(delta), jnp.asarray(psi), jnp.asarray(a2[inner]), dx))
+        data[f"{name}.residual"] = np.asarray(res(jnp.asarray(u), psi_bl, curvature, dx))
+        data[f"{name}.source"] = np.asarray(by.hamiltonian_source(jnp.asarray(psi), jnp.asarray(a2[inner])))
+        data[f"{name}.linearized_source"] = np.asarray(
+            by.linearized_hamiltonian_source(jnp.asarray(delta), jnp.asarray(psi), jnp.asarray(a2[inner])))
+    np.savez_compressed(out_dir / "puncture.npz", **data)
+
+
 def make_cartoon(out_dir: Path):
     from JAX_BSSN.cartoon.axisymmetry import (axisymmetric_rk4_step, compute_axisymmetric_rhs,
                                               compute_axisymmetric_constraints, reconstruct_axisymmetric_support,
@@ -422,6 +500,7 @@ def main(argv):
     parts = {"stencils": lambda: make_stencils(HERE / "stencils.npz"), "rhs": lambda: make_rhs(HERE),
              "fmr": lambda: make_fmr(HERE), "cartoon": lambda: make_cartoon(HERE),
              "matter": lambda: make_matter(HERE), "waves": lambda: make_waves(HERE),
+             "puncture": lambda: make_puncture(HERE),
              "long": lambda: make_long_runs(HERE)}
     for name, build in parts.items():
         if only and name not in only:
