@@ -45,6 +45,10 @@ void prof_begin(int cls, cudaStream_t s) {
     cudaEventRecord(t_start, s);
 }
 
+bool profiling_enabled() { return g_enabled.load(std::memory_order_relaxed) != 0; }
+
+void count_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
 void prof_end(int cls, cudaStream_t s) {
     if (!g_enabled.load(std::memory_order_relaxed) || t_start == nullptr) return;
     std::lock_guard<std::mutex> lock(g_mu);

@@ -16,6 +16,11 @@ enum KernelClass {
 };
 
 void prof_begin(int cls, cudaStream_t s);
+// Per-launch event timing is on (bssn_profile_enable).
+bool profiling_enabled();
+// Adds n (may be negative) to the launch counter: kernels replayed from a
+// CUDA graph, or recorded during a capture without running.
+void count_launches(long long n);
 void prof_end(int cls, cudaStream_t s);
 
 }  // namespace bssn

@@ -44,12 +44,15 @@
 #include "bssn_driver.h"
 #include "bssn_profile.h"
 
+#include <map>
+
 namespace bssn {
 namespace {
 
 constexpr int kPunctThreads = 256;
 constexpr int kMaxPunctures = BSSN_MAX_PUNCTURES;
-constexpr int kMaxSums = 3;              // dot products folded per kernel
+constexpr int kMaxSums = 4;              // dot products folded per kernel
+constexpr int kMaxApplyBlocks = 152 * 16; // cap of the persistent operator grid
 constexpr int kUpdateBlocks = 152 * 4;   // grid of the vector-update kernels
 constexpr int kChunk = 16;               // Krylov iterations enqueued between host checks (even)
 
@@ -318,40 +321,47 @@ __device__ __forceinline__ SolveCtrl read_ctrl(const SolveCtrl* c) {
 
 // ---------------------------------------------------------------------------
 // Newton level: residual F(u) = Lap(u) + S(psi_bl + u) at the interior (zero at
-// fixed cells), the Jacobian's source coefficient dS/du, the residual RMS, and
-// the Krylov start: x = 0 follows from a memset; r = b = F; r.r = b.b.
+// fixed cells), its RMS, and the Krylov start.  The Krylov solve runs on the
+// system scaled by dx^2 (the same solution; every stopping test is scale
+// free): b = dx^2 F, and the operator's centre coefficient dx^2 dS/du - 6
+// (Cartesian) or dx^2 dS/du - 4 (meridional) is stored per cell, so that one
+// operator application is a neighbour sum and one FMA.  x = 0 comes from a
+// memset; r = rhat = b.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kPunctThreads)
 k_newton_residual(const double* __restrict__ u, const double* __restrict__ psi_bl, const double* __restrict__ a2,
-                  SolveGrid G, double* __restrict__ r, double* __restrict__ rhat, double* __restrict__ lin,
+                  SolveGrid G, double* __restrict__ r, double* __restrict__ rhat, double* __restrict__ centre,
                   double* __restrict__ partial, SolveCtrl* ctrl, double tol2, int maxiter) {
-    double acc[3] = {0.0, 0.0, 0.0};   // F.F, nonpositive psi, nonfinite u
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};   // F.F, nonpositive psi, nonfinite u, b.b
     const long long plane = (long long)G.n[1] * G.n[2];
+    const double diag = G.axi ? 4.0 : 6.0;
     auto f = [&](int x, int y, int z) { return u[(long long)x * plane + (long long)y * G.n[2] + z]; };
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < G.size();
          t += (long long)gridDim.x * blockDim.x) {
         int i, j, k;
         decompose(G, t, i, j, k);
-        double res = 0.0, coef = 0.0;
+        double res = 0.0, b = 0.0, c = 0.0;
         if (G.interior(i, j, k)) {
             const double psi = __dadd_rn(psi_bl[t], u[t]);
             res = __dadd_rn(laplacian_exact(G, i, j, k, f), source_of(psi, a2[t]));
-            coef = lin_coefficient(psi, a2[t]);
+            b = G.dx2 * res;
+            c = fma(G.dx2, lin_coefficient(psi, a2[t]), -diag);
             acc[0] += res * res;
             if (!(psi > 0.0)) acc[1] += 1.0;
             if (!isfinite(u[t])) acc[2] += 1.0;
+            acc[3] += b * b;
         }
-        r[t] = res;
-        if (rhat) rhat[t] = res;
-        lin[t] = coef;
+        r[t] = b;
+        if (rhat) rhat[t] = b;
+        centre[t] = c;
     }
-    double tot[3];
-    if (!fold_last<3>(acc, partial, &ctrl->ticket, tot)) return;
+    double tot[4];
+    if (!fold_last<4>(acc, partial, &ctrl->ticket, tot)) return;
     if (threadIdx.x == 0) {
-        const double bb = tot[0];
+        const double bb = tot[3];
         ctrl->bb = bb;
         ctrl->gamma = bb;
-        ctrl->rms = sqrt(bb / (double)G.unknowns());
+        ctrl->rms = sqrt(tot[0] / (double)G.unknowns());
         ctrl->atol2 = tol2 * bb;
         ctrl->k = 0;
         ctrl->maxiter = maxiter;
@@ -377,21 +387,24 @@ __global__ void k_psi_total(const double* __restrict__ psi_bl, const double* __r
 }
 
 // ---------------------------------------------------------------------------
-// Conjugate gradients on A = -(Lap + dS) (Cartesian).  One iteration:
+// Conjugate gradients on A = -dx^2 (Lap + dS) (Cartesian).  One iteration:
 //   k_cg_apply   p = r + beta p_prev (p = r at the first), Ap, p.Ap
 //                -> alpha = gamma / p.Ap
 //   k_cg_update  x += alpha p, r -= alpha Ap, r.r -> beta, gamma, k, done
 // The apply kernel stages p of one x plane of a 32 x 8 (z, y) tile in shared
-// memory, with its one-cell halo, and marches along x over a chunk of planes,
-// carrying the x neighbours in registers: each p value is formed once per
-// tile (plus the halo) instead of once per stencil tap.  p ping-pongs between
-// two buffers, since neighbouring tiles still read the previous p.
+// memory, with its one-cell halo, and marches along x carrying the x
+// neighbours in registers, so each p value is formed once per tile (plus the
+// halo) rather than once per stencil tap.  Its grid is persistent (the
+// resident blocks of every SM): the (tile, plane) steps are split evenly
+// between blocks, a block's range possibly continuing into the next tile, so
+// that every SM gets the same FP64 work.  p ping-pongs between two buffers,
+// since neighbouring tiles still read the previous p.
 // ---------------------------------------------------------------------------
-constexpr int kTz = 32, kTy = 8, kXc = 16;
+constexpr int kTz = 32, kTy = 8;
 
 __global__ void __launch_bounds__(kTz* kTy)
 k_cg_apply(const double* __restrict__ r, const double* __restrict__ pin, double* __restrict__ pout,
-           const double* __restrict__ lin, double* __restrict__ ap, SolveGrid G, SolveCtrl* ctrl,
+           const double* __restrict__ centre, double* __restrict__ ap, SolveGrid G, SolveCtrl* ctrl,
            double* __restrict__ partial) {
     __shared__ double tile[kTy + 2][kTz + 2];
     const SolveCtrl C = read_ctrl(ctrl);
@@ -400,48 +413,58 @@ k_cg_apply(const double* __restrict__ r, const double* __restrict__ pin, double*
     const double beta = C.beta;
     const int tz = threadIdx.x % kTz, ty = threadIdx.x / kTz;
     const int tiles_z = (G.n[2] - 2 + kTz - 1) / kTz;
-    const int z = 1 + (blockIdx.x % tiles_z) * kTz + tz;
-    const int y = 1 + (blockIdx.x / tiles_z) * kTy + ty;
-    const int x0 = 1 + blockIdx.y * kXc;
-    const int x1 = min(x0 + kXc, G.n[0] - 1);
+    const int tiles_y = (G.n[1] - 2 + kTy - 1) / kTy;
+    const int planes = G.n[0] - 2;
+    const long long steps = (long long)tiles_z * tiles_y * planes;
+    const long long w0 = steps * blockIdx.x / gridDim.x, w1 = steps * (blockIdx.x + 1) / gridDim.x;
     const long long sx = (long long)G.n[1] * G.n[2], sy = G.n[2];
-    const bool in_yz = y <= G.n[1] - 1 && z <= G.n[2] - 1;   // y, z >= 1 by construction
-    const bool interior = y <= G.n[1] - 2 && z <= G.n[2] - 2;
     auto pnew = [&](long long idx) { return first ? r[idx] : fma(beta, pin[idx], r[idx]); };
-    const long long own = (long long)y * sy + z;
-    double pm = in_yz ? pnew((long long)(x0 - 1) * sx + own) : 0.0;
-    double pc = in_yz ? pnew((long long)x0 * sx + own) : 0.0;
     double dot[1] = {0.0};
-    for (int x = x0; x < x1; ++x) {
-        const long long base = (long long)x * sx;
-        const double pn = in_yz ? pnew(base + sx + own) : 0.0;
-        tile[ty + 1][tz + 1] = pc;
-        if (ty == 0) tile[0][tz + 1] = z <= G.n[2] - 1 ? pnew(base + own - sy) : 0.0;
-        if (ty == kTy - 1) tile[kTy + 1][tz + 1] = (y + 1 <= G.n[1] - 1 && z <= G.n[2] - 1) ? pnew(base + own + sy) : 0.0;
-        if (tz == 0) tile[ty + 1][0] = y <= G.n[1] - 1 ? pnew(base + own - 1) : 0.0;
-        if (tz == kTz - 1) tile[ty + 1][kTz + 1] = (y <= G.n[1] - 1 && z + 1 <= G.n[2] - 1) ? pnew(base + own + 1) : 0.0;
-        __syncthreads();
-        if (interior) {
-            double s = pn + pm;
-            s += tile[ty + 2][tz + 1];
-            s += tile[ty][tz + 1];
-            s += tile[ty + 1][tz + 2];
-            s += tile[ty + 1][tz];
-            const double lap = fma(-6.0, pc, s) * G.inv_dx2;
-            const double a = -fma(lin[base + own], pc, lap);
-            pout[base + own] = pc;
-            ap[base + own] = a;
-            dot[0] = fma(pc, a, dot[0]);
+    for (long long w = w0; w < w1;) {
+        const int t = (int)(w / planes);
+        const int xs = 1 + (int)(w - (long long)t * planes);
+        const int xe = 1 + (int)min((long long)planes, (long long)(xs - 1) + (w1 - w));   // exclusive
+        w += xe - xs;
+        const int z = 1 + (t % tiles_z) * kTz + tz;
+        const int y = 1 + (t / tiles_z) * kTy + ty;
+        const bool in_yz = y <= G.n[1] - 1 && z <= G.n[2] - 1;   // y, z >= 1 by construction
+        const bool interior = y <= G.n[1] - 2 && z <= G.n[2] - 2;
+        const long long own = (long long)y * sy + z;
+        double pm = in_yz ? pnew((long long)(xs - 1) * sx + own) : 0.0;
+        double pc = in_yz ? pnew((long long)xs * sx + own) : 0.0;
+        for (int x = xs; x < xe; ++x) {
+            const long long base = (long long)x * sx;
+            const double pn = in_yz ? pnew(base + sx + own) : 0.0;
+            tile[ty + 1][tz + 1] = pc;
+            if (ty == 0) tile[0][tz + 1] = z <= G.n[2] - 1 ? pnew(base + own - sy) : 0.0;
+            if (ty == kTy - 1)
+                tile[kTy + 1][tz + 1] = (y + 1 <= G.n[1] - 1 && z <= G.n[2] - 1) ? pnew(base + own + sy) : 0.0;
+            if (tz == 0) tile[ty + 1][0] = y <= G.n[1] - 1 ? pnew(base + own - 1) : 0.0;
+            if (tz == kTz - 1)
+                tile[ty + 1][kTz + 1] = (y <= G.n[1] - 1 && z + 1 <= G.n[2] - 1) ? pnew(base + own + 1) : 0.0;
+            __syncthreads();
+            if (interior) {
+                double s = pn + pm;
+                s += tile[ty + 2][tz + 1];
+                s += tile[ty][tz + 1];
+                s += tile[ty + 1][tz + 2];
+                s += tile[ty + 1][tz];
+                const double a = -fma(centre[base + own], pc, s);
+                pout[base + own] = pc;
+                ap[base + own] = a;
+                dot[0] = fma(pc, a, dot[0]);
+            }
+            __syncthreads();
+            pm = pc;
+            pc = pn;
         }
-        __syncthreads();
-        pm = pc;
-        pc = pn;
     }
     double tot[1];
     if (!fold_last<1>(dot, partial, &ctrl->ticket, tot)) return;
     if (threadIdx.x == 0) ctrl->alpha = C.gamma / tot[0];
 }
 
+// Two samples per thread and step (16-byte loads), two steps in flight.
 __global__ void __launch_bounds__(kPunctThreads)
 k_cg_update(double* __restrict__ x, double* __restrict__ r, const double* __restrict__ p, const double* __restrict__ ap,
             long long n, SolveCtrl* ctrl, double* __restrict__ partial) {
@@ -449,12 +472,33 @@ k_cg_update(double* __restrict__ x, double* __restrict__ r, const double* __rest
     if (C.done) return;
     const double alpha = C.alpha;
     double rr[1] = {0.0};
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    double rr1 = 0.0;
+    const long long pairs = n / 2;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    double2* x2 = reinterpret_cast<double2*>(x);
+    double2* r2 = reinterpret_cast<double2*>(r);
+    const double2* p2 = reinterpret_cast<const double2*>(p);
+    const double2* a2 = reinterpret_cast<const double2*>(ap);
+#pragma unroll 2
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < pairs; t += stride) {
+        const double2 pv = p2[t], av = a2[t], rv = r2[t];
+        double2 xv = x2[t];
+        xv.x = fma(alpha, pv.x, xv.x);
+        xv.y = fma(alpha, pv.y, xv.y);
+        const double rx = fma(-alpha, av.x, rv.x), ry = fma(-alpha, av.y, rv.y);
+        x2[t] = xv;
+        r2[t] = make_double2(rx, ry);
+        rr[0] = fma(rx, rx, rr[0]);
+        rr1 = fma(ry, ry, rr1);
+    }
+    if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+        const long long t = n - 1;
         x[t] = fma(alpha, p[t], x[t]);
         const double rn = fma(-alpha, ap[t], r[t]);
         r[t] = rn;
-        rr[0] = fma(rn, rn, rr[0]);
+        rr1 = fma(rn, rn, rr1);
     }
+    rr[0] += rr1;
     double tot[1];
     if (!fold_last<1>(rr, partial, &ctrl->ticket, tot)) return;
     if (threadIdx.x == 0) {
@@ -467,77 +511,102 @@ k_cg_update(double* __restrict__ x, double* __restrict__ r, const double* __rest
 }
 
 // ---------------------------------------------------------------------------
-// BiCGSTAB on A = -(Lap_axi + dS) (meridional grid, small: one thread per cell,
-// vector combinations formed at each stencil tap).  One iteration:
+// BiCGSTAB on A = -dx^2 (Lap_axi + dS) (meridional grid).  With h_i = 1/(2i+1)
+// = dx / (2 rho_i), A v = -((1 + h_i) v[i+1] + (1 - h_i) v[i-1] + v[k+1] +
+// v[k-1] + c v), c the stored centre coefficient; 1 - h_0 = 0 closes the axis.
+// One iteration:
 //   k_bicg_p   p = r + beta (p_prev - omega q_prev) (p = r at the first),
 //              q = A p, rhat.q -> alpha = rho / rhat.q
 //   k_bicg_s   s = r - alpha q, t = A s, s.s, t.s, t.t -> omega, early exit
 //   k_bicg_x   x += alpha p (+ omega s), r = s (- omega t), r.r, rhat.r
 //              -> beta, rho, k, done (convergence, maxiter or breakdown)
+// The two operator kernels stage the combined vector of a 32 x 8 (z, rho)
+// tile plus halo in shared memory, one tile per block.
 // ---------------------------------------------------------------------------
-template <class F>
-__device__ __forceinline__ double axi_operator(const SolveGrid& G, int i, int k, double lin_c, F f) {
-    const double c = f(i, k);
-    const double rp = f(i + 1, k);
-    const double rm = i == 0 ? c : f(i - 1, k);
-    const double inv_2rho_dx = 1.0 / (2.0 * ((i + 0.5) * G.dx) * G.dx);
-    const double radial_second = (rp - 2.0 * c + rm) * G.inv_dx2;
-    const double radial_first = (rp - rm) * inv_2rho_dx;
-    const double axial_second = (f(i, k + 1) + f(i, k - 1) - 2.0 * c) * G.inv_dx2;
-    return -(radial_second + radial_first + axial_second + lin_c * c);
+constexpr int kAz = 32, kAr = 8;
+
+__device__ __forceinline__ double axi_apply_tile(double (*tile)[kAz + 2], const double* rows, int i, int ti, int tk,
+                                                 double centre) {
+    const double c = tile[ti + 1][tk + 1];
+    const double rp = tile[ti + 2][tk + 1];
+    const double rm = i == 0 ? c : tile[ti][tk + 1];
+    const double zs = tile[ti + 1][tk + 2] + tile[ti + 1][tk];
+    return -fma(rows[2 * ti], rp, fma(rows[2 * ti + 1], rm, fma(centre, c, zs)));
 }
 
-__global__ void __launch_bounds__(kPunctThreads)
+// 1 + h_i and 1 - h_i of the block's rows
+__device__ __forceinline__ void axi_rows(double* rows, int i0) {
+    if (threadIdx.x < kAr) {
+        const double h = 1.0 / (double)(2 * (i0 + (int)threadIdx.x) + 1);
+        rows[2 * threadIdx.x] = 1.0 + h;
+        rows[2 * threadIdx.x + 1] = 1.0 - h;
+    }
+}
+
+// Fills the (kAr + 2) x (kAz + 2) tile of vec(i, k) around the block's cells;
+// cells outside the array read as zero.
+template <class V>
+__device__ __forceinline__ void axi_fill_tile(const SolveGrid& G, double (*tile)[kAz + 2], int i0, int k0, V vec) {
+    for (int q = threadIdx.x; q < (kAr + 2) * (kAz + 2); q += blockDim.x) {
+        const int ti = q / (kAz + 2), tk = q - ti * (kAz + 2);
+        const int i = i0 - 1 + ti, k = k0 - 1 + tk;
+        tile[ti][tk] = (i >= 0 && i <= G.n[0] - 1 && k >= 0 && k <= G.n[2] - 1) ? vec((long long)i * G.n[2] + k) : 0.0;
+    }
+}
+
+__global__ void __launch_bounds__(kAz* kAr)
 k_bicg_p(const double* __restrict__ r, const double* __restrict__ rhat, const double* __restrict__ pin,
          const double* __restrict__ qin, double* __restrict__ pout, double* __restrict__ qout,
-         const double* __restrict__ lin, SolveGrid G, SolveCtrl* ctrl, double* __restrict__ partial) {
+         const double* __restrict__ centre, SolveGrid G, SolveCtrl* ctrl, double* __restrict__ partial) {
+    __shared__ double tile[kAr + 2][kAz + 2];
+    __shared__ double rows[2 * kAr];
     const SolveCtrl C = read_ctrl(ctrl);
     if (C.done) return;
     const bool first = C.first != 0;
     const double beta = C.beta, omega = C.omega;
-    const int nz = G.n[2];
-    auto pv = [&](int i, int k) {
-        const long long o = (long long)i * nz + k;
-        return first ? r[o] : fma(beta, fma(-omega, qin[o], pin[o]), r[o]);
-    };
+    const int tk = threadIdx.x % kAz, ti = threadIdx.x / kAz;
+    const int i0 = blockIdx.y * kAr, k0 = 1 + blockIdx.x * kAz;
+    axi_rows(rows, i0);
+    axi_fill_tile(G, tile, i0, k0, [&](long long o) { return first ? r[o] : fma(beta, fma(-omega, qin[o], pin[o]), r[o]); });
+    __syncthreads();
+    const int i = i0 + ti, k = k0 + tk;
     double acc[1] = {0.0};
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < G.size();
-         t += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(t / nz), k = (int)(t - (long long)i * nz);
-        if (!G.interior(i, 0, k)) continue;
-        const double q = axi_operator(G, i, k, lin[t], pv);
-        pout[t] = pv(i, k);
-        qout[t] = q;
-        acc[0] = fma(rhat[t], q, acc[0]);
+    if (G.interior(i, 0, k)) {
+        const long long o = (long long)i * G.n[2] + k;
+        const double q = axi_apply_tile(tile, rows, i, ti, tk, centre[o]);
+        pout[o] = tile[ti + 1][tk + 1];
+        qout[o] = q;
+        acc[0] = rhat[o] * q;
     }
     double tot[1];
     if (!fold_last<1>(acc, partial, &ctrl->ticket, tot)) return;
     if (threadIdx.x == 0) ctrl->alpha = C.rho / tot[0];
 }
 
-__global__ void __launch_bounds__(kPunctThreads)
+__global__ void __launch_bounds__(kAz* kAr)
 k_bicg_s(const double* __restrict__ r, const double* __restrict__ q, double* __restrict__ s, double* __restrict__ tv,
-         const double* __restrict__ lin, SolveGrid G, SolveCtrl* ctrl, double* __restrict__ partial) {
+         const double* __restrict__ centre, SolveGrid G, SolveCtrl* ctrl, double* __restrict__ partial) {
+    __shared__ double tile[kAr + 2][kAz + 2];
+    __shared__ double rows[2 * kAr];
     const SolveCtrl C = read_ctrl(ctrl);
     if (C.done) return;
     const double alpha = C.alpha;
-    const int nz = G.n[2];
-    auto sv = [&](int i, int k) {
-        const long long o = (long long)i * nz + k;
-        return fma(-alpha, q[o], r[o]);
-    };
+    const int tk = threadIdx.x % kAz, ti = threadIdx.x / kAz;
+    const int i0 = blockIdx.y * kAr, k0 = 1 + blockIdx.x * kAz;
+    axi_rows(rows, i0);
+    axi_fill_tile(G, tile, i0, k0, [&](long long o) { return fma(-alpha, q[o], r[o]); });
+    __syncthreads();
+    const int i = i0 + ti, k = k0 + tk;
     double acc[3] = {0.0, 0.0, 0.0};   // s.s, t.s, t.t
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < G.size();
-         t += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(t / nz), k = (int)(t - (long long)i * nz);
-        if (!G.interior(i, 0, k)) continue;
-        const double sc = sv(i, k);
-        const double tt = axi_operator(G, i, k, lin[t], sv);
-        s[t] = sc;
-        tv[t] = tt;
-        acc[0] = fma(sc, sc, acc[0]);
-        acc[1] = fma(tt, sc, acc[1]);
-        acc[2] = fma(tt, tt, acc[2]);
+    if (G.interior(i, 0, k)) {
+        const long long o = (long long)i * G.n[2] + k;
+        const double sc = tile[ti + 1][tk + 1];
+        const double tt = axi_apply_tile(tile, rows, i, ti, tk, centre[o]);
+        s[o] = sc;
+        tv[o] = tt;
+        acc[0] = sc * sc;
+        acc[1] = tt * sc;
+        acc[2] = tt * tt;
     }
     double tot[3];
     if (!fold_last<3>(acc, partial, &ctrl->ticket, tot)) return;
@@ -589,7 +658,7 @@ k_bicg_x(double* __restrict__ x, double* __restrict__ r, const double* __restric
 // ---------------------------------------------------------------------------
 // workspace: 10 full-grid vectors, the partial sums, the control record
 // ---------------------------------------------------------------------------
-enum { V_R, V_RHAT, V_LIN, V_X, V_P0, V_P1, V_Q, V_S, V_T, V_SPARE, V_COUNT };
+enum { V_R, V_RHAT, V_CENTRE, V_X, V_P0, V_P1, V_Q, V_S, V_T, V_Q1, V_COUNT };
 
 int grid_of(const int32_t shape[3], int axi, double dx, SolveGrid& G) {
     if (!shape) return fail(BSSN_ERR_INVALID, "null shape");
@@ -609,12 +678,8 @@ int grid_of(const int32_t shape[3], int axi, double dx, SolveGrid& G) {
 }
 
 long long max_blocks(const SolveGrid& G) {
-    long long apply = 0;
-    if (!G.axi) {
-        const long long tz = (G.n[2] - 2 + kTz - 1) / kTz, ty = (G.n[1] - 2 + kTy - 1) / kTy;
-        const long long tx = (G.n[0] - 2 + kXc - 1) / kXc;
-        apply = tz * ty * tx;
-    }
+    long long apply = kMaxApplyBlocks;
+    if (G.axi) apply = (long long)((G.n[2] - 2 + kAz - 1) / kAz) * ((G.n[0] - 1 + kAr - 1) / kAr);
     return std::max<long long>(apply, kUpdateBlocks);
 }
 
@@ -625,6 +690,42 @@ size_t workspace_bytes(const SolveGrid& G) {
 }
 
 unsigned update_blocks(long long n) { return (unsigned)std::min<long long>(pblocks(n), kUpdateBlocks); }
+
+// A non-blocking stream per device and thread for the solve, ordered after
+// and before the caller's stream with events (stream capture of the Krylov
+// chunks needs a stream other than the legacy default stream).
+struct SolveStream {
+    cudaStream_t s = nullptr;
+    cudaEvent_t in = nullptr, out = nullptr;
+};
+
+cudaError_t solve_stream(SolveStream*& out) {
+    thread_local std::map<int, SolveStream> streams;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    SolveStream& ss = streams[dev];
+    if (!ss.s) {
+        e = cudaStreamCreateWithFlags(&ss.s, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ss.in, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ss.out, cudaEventDisableTiming);
+        if (e != cudaSuccess) return e;
+    }
+    out = &ss;
+    return cudaSuccess;
+}
+
+// Persistent grid of the Cartesian operator kernel: its resident blocks on
+// every SM, at most one block per (tile, plane) step.
+unsigned cg_apply_blocks(const SolveGrid& G) {
+    int dev = 0, sms = 152, per_sm = 4;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg_apply, kTz * kTy, 0);
+    const long long steps = (long long)((G.n[2] - 2 + kTz - 1) / kTz) * ((G.n[1] - 2 + kTy - 1) / kTy) * (G.n[0] - 2);
+    const long long want = (long long)sms * std::max(per_sm, 1);
+    return (unsigned)std::min<long long>(std::min<long long>(want, steps), kMaxApplyBlocks);
+}
 
 }  // namespace
 }  // namespace bssn
@@ -720,8 +821,17 @@ int bssn_puncture_solve(const double* psi_bl, const double* curvature_squared, c
     if (max_linear_iterations < 1) return fail(BSSN_ERR_INVALID, "max_linear_iterations must be a positive integer");
     if (!workspace || workspace_bytes_ < workspace_bytes(G))
         return fail(BSSN_ERR_WORKSPACE, "workspace missing or smaller than bssn_puncture_workspace_bytes()");
+    *history_length = 0;
 
-    cudaStream_t s = (cudaStream_t)stream;
+    SolveStream* ss = nullptr;
+    cudaError_t e = solve_stream(ss);
+    if (e != cudaSuccess) return cuda_status(e, "bssn_puncture_solve");
+    cudaStream_t caller = (cudaStream_t)stream;
+    cudaStream_t s = ss->s;
+    e = cudaEventRecord(ss->in, caller);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, ss->in, 0);
+    if (e != cudaSuccess) return cuda_status(e, "bssn_puncture_solve");
+
     const long long n = G.size();
     const size_t vec_al = ((size_t)n * sizeof(double) + 255) & ~(size_t)255;
     char* base = static_cast<char*>(workspace);
@@ -731,86 +841,115 @@ int bssn_puncture_solve(const double* psi_bl, const double* curvature_squared, c
     const size_t pbytes = (size_t)max_blocks(G) * kMaxSums * sizeof(double);
     SolveCtrl* ctrl = reinterpret_cast<SolveCtrl*>(base + V_COUNT * vec_al + ((pbytes + 255) & ~(size_t)255));
 
-    cudaError_t e = cudaMemsetAsync(base, 0, V_COUNT * vec_al, s);
+    e = cudaMemsetAsync(base, 0, V_COUNT * vec_al, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(ctrl, 0, sizeof(SolveCtrl), s);
     if (e == cudaSuccess) e = cudaMemsetAsync(u, 0, (size_t)n * sizeof(double), s);
     if (e != cudaSuccess) return cuda_status(e, "bssn_puncture_solve");
 
     const unsigned ub = update_blocks(n);
-    dim3 apply_grid(1, 1, 1);
-    if (!G.axi) {
-        const int tz = (G.n[2] - 2 + kTz - 1) / kTz, ty = (G.n[1] - 2 + kTy - 1) / kTy;
-        apply_grid = dim3(tz * ty, (G.n[0] - 2 + kXc - 1) / kXc, 1);
+    const unsigned cg_blocks = G.axi ? 0u : cg_apply_blocks(G);
+    const dim3 axi_grid(G.axi ? (G.n[2] - 2 + kAz - 1) / kAz : 1, G.axi ? (G.n[0] - 1 + kAr - 1) / kAr : 1, 1);
+
+    // one chunk of kChunk Krylov iterations (kChunk is even, so the ping-pong
+    // buffers line up from chunk to chunk)
+    int chunk_launches = 0;
+    auto enqueue_chunk = [&]() {
+        for (int j = 0; j < kChunk; ++j) {
+            double* pin = v[j % 2 ? V_P1 : V_P0];
+            double* pout = v[j % 2 ? V_P0 : V_P1];
+            if (!G.axi) {
+                BSSN_LAUNCH(KC_SOLVE_APPLY, k_cg_apply, cg_blocks, kTz * kTy, s, v[V_R], pin, pout, v[V_CENTRE],
+                            v[V_Q], G, ctrl, partial);
+                BSSN_LAUNCH(KC_SOLVE_UPDATE, k_cg_update, ub, kPunctThreads, s, v[V_X], v[V_R], pout, v[V_Q], n,
+                            ctrl, partial);
+                chunk_launches += 2;
+            } else {
+                // q ping-pongs as well: the p kernel reads the previous p and q around each cell
+                double* qin = v[j % 2 ? V_Q1 : V_Q];
+                double* qout = v[j % 2 ? V_Q : V_Q1];
+                BSSN_LAUNCH(KC_SOLVE_APPLY, k_bicg_p, axi_grid, kAz * kAr, s, v[V_R], v[V_RHAT], pin, qin, pout, qout,
+                            v[V_CENTRE], G, ctrl, partial);
+                BSSN_LAUNCH(KC_SOLVE_APPLY, k_bicg_s, axi_grid, kAz * kAr, s, v[V_R], qout, v[V_S], v[V_T],
+                            v[V_CENTRE], G, ctrl, partial);
+                BSSN_LAUNCH(KC_SOLVE_UPDATE, k_bicg_x, ub, kPunctThreads, s, v[V_X], v[V_R], v[V_RHAT], pout, v[V_S],
+                            v[V_T], n, ctrl, partial);
+                chunk_launches += 3;
+            }
+        }
+    };
+    cudaGraphExec_t exec = nullptr;
+    auto finish = [&](int code) {
+        if (exec) cudaGraphExecDestroy(exec);
+        cudaEventRecord(ss->out, s);
+        cudaStreamWaitEvent(caller, ss->out, 0);
+        return code;
+    };
+    // Replay the chunk as a CUDA graph unless per-kernel profiling is on
+    // (which times every launch with events of its own).
+    if (!profiling_enabled() && cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+        cudaGraph_t graph = nullptr;
+        enqueue_chunk();
+        count_launches(-chunk_launches);   // recorded, not run
+        e = cudaStreamEndCapture(s, &graph);
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+            exec = nullptr;
+            return finish(cuda_status(e, "bssn_puncture_solve (graph capture)"));
+        }
     }
+    auto run_chunk = [&]() -> cudaError_t {
+        if (!exec) {
+            chunk_launches = 0;
+            enqueue_chunk();
+            return cudaGetLastError();
+        }
+        count_launches(chunk_launches);
+        return cudaGraphLaunch(exec, s);
+    };
+
     const double tol2 = linear_tolerance * linear_tolerance;
     SolveCtrl host;
     int count = 0;
     for (int it = 0; it <= max_newton_iterations; ++it) {
         BSSN_LAUNCH(KC_SOLVE_NEWTON, k_newton_residual, ub, kPunctThreads, s, u, psi_bl, curvature_squared, G, v[V_R],
-                    G.axi ? v[V_RHAT] : nullptr, v[V_LIN], partial, ctrl, tol2, max_linear_iterations);
+                    G.axi ? v[V_RHAT] : nullptr, v[V_CENTRE], partial, ctrl, tol2, max_linear_iterations);
         e = cudaGetLastError();
         if (e == cudaSuccess) e = cudaMemcpyAsync(&host, ctrl, sizeof(SolveCtrl), cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-        if (e != cudaSuccess) return cuda_status(e, "bssn_puncture_solve");
+        if (e != cudaSuccess) return finish(cuda_status(e, "bssn_puncture_solve"));
         if (G.axi && it > 0) {
             // checks of the previous correction (bowen_york_solver.py:471-474)
-            if (host.bad_u) {
-                *history_length = count;
-                return fail(BSSN_ERR_NONFINITE, "Newton-Raphson correction is nonfinite");
-            }
-            if (host.bad_psi) {
-                *history_length = count;
-                return fail(BSSN_ERR_NONFINITE, "Newton-Raphson correction made psi nonpositive");
-            }
+            if (host.bad_u) return finish(fail(BSSN_ERR_NONFINITE, "Newton-Raphson correction is nonfinite"));
+            if (host.bad_psi)
+                return finish(fail(BSSN_ERR_NONFINITE, "Newton-Raphson correction made psi nonpositive"));
         }
         residual_history[count++] = host.rms;
         *history_length = count;
         if (G.axi && !std::isfinite(host.rms))
-            return fail(BSSN_ERR_NONFINITE, "Newton-Raphson solve produced a nonfinite residual");
+            return finish(fail(BSSN_ERR_NONFINITE, "Newton-Raphson solve produced a nonfinite residual"));
         if (host.rms <= newton_tolerance) break;
         if (it == max_newton_iterations) {
             char msg[160];
             std::snprintf(msg, sizeof(msg), "Newton-Raphson solve did not converge: RMS residual %.3e exceeds %.3e.",
                           host.rms, newton_tolerance);
-            return fail(BSSN_ERR_NOT_CONVERGED, msg);
+            return finish(fail(BSSN_ERR_NOT_CONVERGED, msg));
         }
         e = cudaMemsetAsync(v[V_X], 0, (size_t)n * sizeof(double), s);
-        if (e != cudaSuccess) return cuda_status(e, "bssn_puncture_solve");
+        if (e != cudaSuccess) return finish(cuda_status(e, "bssn_puncture_solve"));
         bool done = host.done != 0;
         while (!done) {
-            for (int j = 0; j < kChunk; ++j) {
-                if (!G.axi) {
-                    double* pin = v[j % 2 ? V_P1 : V_P0];
-                    double* pout = v[j % 2 ? V_P0 : V_P1];
-                    BSSN_LAUNCH(KC_SOLVE_APPLY, k_cg_apply, apply_grid, kTz * kTy, s, v[V_R], pin, pout, v[V_LIN],
-                                v[V_Q], G, ctrl, partial);
-                    BSSN_LAUNCH(KC_SOLVE_UPDATE, k_cg_update, ub, kPunctThreads, s, v[V_X], v[V_R], pout, v[V_Q], n,
-                                ctrl, partial);
-                } else {
-                    // p and q both ping-pong: the apply kernel reads the previous p and q at stencil taps
-                    double* pin = v[j % 2 ? V_P1 : V_P0];
-                    double* pout = v[j % 2 ? V_P0 : V_P1];
-                    double* qin = v[j % 2 ? V_SPARE : V_Q];
-                    double* qout = v[j % 2 ? V_Q : V_SPARE];
-                    BSSN_LAUNCH(KC_SOLVE_APPLY, k_bicg_p, ub, kPunctThreads, s, v[V_R], v[V_RHAT], pin, qin, pout,
-                                qout, v[V_LIN], G, ctrl, partial);
-                    BSSN_LAUNCH(KC_SOLVE_APPLY, k_bicg_s, ub, kPunctThreads, s, v[V_R], qout, v[V_S], v[V_T],
-                                v[V_LIN], G, ctrl, partial);
-                    BSSN_LAUNCH(KC_SOLVE_UPDATE, k_bicg_x, ub, kPunctThreads, s, v[V_X], v[V_R], v[V_RHAT], pout,
-                                v[V_S], v[V_T], n, ctrl, partial);
-                }
-            }
-            e = cudaGetLastError();
+            e = run_chunk();
             if (e == cudaSuccess) e = cudaMemcpyAsync(&host, ctrl, sizeof(SolveCtrl), cudaMemcpyDeviceToHost, s);
             if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-            if (e != cudaSuccess) return cuda_status(e, "bssn_puncture_solve");
+            if (e != cudaSuccess) return finish(cuda_status(e, "bssn_puncture_solve"));
             done = host.done != 0;
         }
         if (linear_iterations) linear_iterations[it] = host.k;
         BSSN_LAUNCH(KC_SOLVE_UPDATE, k_newton_update, ub, kPunctThreads, s, u, v[V_X], n);
     }
     BSSN_LAUNCH(KC_SOLVE_UPDATE, k_psi_total, ub, kPunctThreads, s, psi_bl, u, psi, n);
-    return cuda_status(cudaGetLastError(), "bssn_puncture_solve");
+    return finish(cuda_status(cudaGetLastError(), "bssn_puncture_solve"));
 }
 
 }  // extern "C"
