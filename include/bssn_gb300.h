@@ -275,6 +275,21 @@ int bssn_wave_norm_sums(const double* h_plus, const double* coordinates, const d
 
 /* ---------------- instrumentation ---------------- */
 
+/* Output staging (diagnostics/openpmd.py:51-71 _strip_ghost_cells,
+ * :254-285 tiled_output_fields): copies the box [lo, lo + extent) of each
+ * C-ordered float64 device array src (extents `shape`) into dst, box after
+ * box, each box C-ordered, so a writer gathers every owned sample of a level
+ * with one launch and one device-to-host copy.  At most
+ * BSSN_MAX_GATHER_BOXES boxes per call. */
+#define BSSN_MAX_GATHER_BOXES 32
+typedef struct BssnBox {
+    const double* src;
+    int32_t shape[3];
+    int32_t lo[3];
+    int32_t extent[3];
+} BssnBox;
+int bssn_gather_boxes(int32_t count, const BssnBox* boxes, double* dst, void* stream);
+
 /* ---------------------------------------------------------------------------
  * Bowen-York puncture initial data (JAX_BSSN/utilities/bowen_york_solver.py).
  * Grids are the reference's cell-centred grids: Cartesian (n0, n1, n2), or the

@@ -51,6 +51,14 @@ class BssnParams(ctypes.Structure):
     ]
 
 
+class BssnBox(ctypes.Structure):
+    _fields_ = [("src", ctypes.c_void_p), ("shape", ctypes.c_int32 * 3), ("lo", ctypes.c_int32 * 3),
+                ("extent", ctypes.c_int32 * 3)]
+
+
+MAX_GATHER_BOXES = 32
+
+
 class BssnFields(ctypes.Structure):
     _fields_ = [(name, ctypes.c_void_p) for name in (
         "conformal_metric", "conformal_factor", "traceless_K", "trace_K",
@@ -152,6 +160,7 @@ SIGNATURES = {
                                            ctypes.c_void_p, ctypes.c_void_p, c_double_p,
                                            ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32),
                                            ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    "bssn_gather_boxes": (ctypes.c_int, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "bssn_launch_count": (ctypes.c_longlong, []),
     "bssn_profile_enable": (None, [ctypes.c_int]),
     "bssn_profile_reset": (None, []),

@@ -8,7 +8,9 @@
 //                                  of H^2 and of |M|^2, and the vertex count
 //                                  (waves.py:43-91).  Block partials in a fixed
 //                                  order, folded by one block (deterministic).
+#include <algorithm>
 #include <cstring>
+#include <string>
 
 #include <cuda_runtime.h>
 
@@ -146,3 +148,73 @@ int bssn_wave_norm_sums(const double* h_plus, const double* coordinates, const d
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Output staging (JAX_BSSN/diagnostics/openpmd.py:51-71, 254-285): the owned
+// (ghost-stripped) box of every field copied, box after box, into one
+// contiguous buffer, so that a writer needs a single device-to-host transfer.
+// ---------------------------------------------------------------------------
+namespace bssn {
+namespace {
+
+constexpr int kMaxGatherBoxes = BSSN_MAX_GATHER_BOXES;
+
+struct GatherTable {
+    int count;
+    const double* src[kMaxGatherBoxes];
+    int shape[kMaxGatherBoxes][3];
+    int lo[kMaxGatherBoxes][3];
+    int ext[kMaxGatherBoxes][3];
+    long long offset[kMaxGatherBoxes];
+};
+
+__global__ void k_gather_boxes(GatherTable T, double* __restrict__ dst) {
+    const int b = blockIdx.y;
+    const long long n = (long long)T.ext[b][0] * T.ext[b][1] * T.ext[b][2];
+    const double* src = T.src[b];
+    double* out = dst + T.offset[b];
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        const long long plane = (long long)T.ext[b][1] * T.ext[b][2];
+        const int i = (int)(t / plane);
+        const long long r = t - (long long)i * plane;
+        const int j = (int)(r / T.ext[b][2]);
+        const int k = (int)(r - (long long)j * T.ext[b][2]);
+        out[t] = src[((long long)(T.lo[b][0] + i) * T.shape[b][1] + (T.lo[b][1] + j)) * T.shape[b][2] + T.lo[b][2] + k];
+    }
+}
+
+}  // namespace
+}  // namespace bssn
+
+extern "C" int bssn_gather_boxes(int32_t count, const BssnBox* boxes, double* dst, void* stream) {
+    using namespace bssn;
+    if (count < 0 || count > kMaxGatherBoxes)
+        return fail(BSSN_ERR_INVALID, "bssn_gather_boxes: between 0 and " + std::to_string(kMaxGatherBoxes) + " boxes");
+    if (count == 0) return BSSN_OK;
+    if (!boxes || !dst) return fail(BSSN_ERR_INVALID, "bssn_gather_boxes: null pointer");
+    GatherTable T;
+    std::memset(&T, 0, sizeof(T));
+    T.count = count;
+    long long offset = 0, largest = 0;
+    for (int b = 0; b < count; ++b) {
+        const BssnBox& x = boxes[b];
+        if (!x.src) return fail(BSSN_ERR_INVALID, "bssn_gather_boxes: null source");
+        long long n = 1;
+        for (int a = 0; a < 3; ++a) {
+            if (x.shape[a] < 1 || x.extent[a] < 0 || x.lo[a] < 0 || x.lo[a] + x.extent[a] > x.shape[a])
+                return fail(BSSN_ERR_INVALID, "bssn_gather_boxes: box outside its array");
+            T.shape[b][a] = x.shape[a];
+            T.lo[b][a] = x.lo[a];
+            T.ext[b][a] = x.extent[a];
+            n *= x.extent[a];
+        }
+        T.src[b] = x.src;
+        T.offset[b] = offset;
+        offset += n;
+        largest = n > largest ? n : largest;
+    }
+    if (largest == 0) return BSSN_OK;
+    const unsigned bx = (unsigned)std::min<long long>((largest + 255) / 256, 1024);
+    BSSN_LAUNCH(KC_EXPORT, k_gather_boxes, dim3(bx, count), 256, (cudaStream_t)stream, T, dst);
+    return cuda_status(cudaGetLastError(), "bssn_gather_boxes");
+}
