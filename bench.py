@@ -62,6 +62,9 @@ CLASS_BYTES = {
     "rhs_gauge": 328,      # 21 state + 9 first derivatives read, 11 written
     "first_derivs": 352,   # 11 fields read, 33 derivatives written
     "rk4_stage": 714,      # mean of 63, 105, 105, 84 values over the four stages
+    # Cartoon class per evolved point: the reconstruction reads 21 compact values and
+    # writes the 9-plane support (21 x 9), the collection reads and writes 21 each
+    "cartoon": 21 * 8 + 21 * 9 * 8 + 2 * 21 * 8,
 }
 RHS_CLASSES = ("rhs_curv", "rhs_at", "rhs_kgt", "rhs_gauge", "first_derivs")
 # FP32 form: float state and derivatives (4 B), FP64 RHS written (8 B), W and alpha read from the FP64 state
