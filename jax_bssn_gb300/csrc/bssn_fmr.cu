@@ -654,7 +654,9 @@ cudaError_t prepare(const FmrPlan& plan, double* const* u, bool project, cudaStr
     cudaError_t e = cudaSuccess;
     for (int p = 0; p < plan.npatch && e == cudaSuccess; ++p) {
         if (project) e = launch_project(u[p], plan.geo[p], owned_box(plan.geo[p]), s);
-        if (e == cudaSuccess) e = launch_fmr_refresh(u[p], plan.dims[p], plan.codes[p].data(), s);
+        // a child's guard shell is overwritten whole by the prolongation, so
+        // only the root's guards take the halo refresh
+        if (e == cudaSuccess && p == 0) e = launch_fmr_refresh(u[p], plan.dims[p], plan.codes[p].data(), s);
         if (e == cudaSuccess && p > 0) e = prolong_child(plan, u, p, w, s);
     }
     return e;
@@ -679,8 +681,8 @@ cudaError_t fmr_step(const FmrPlan& plan, double* const* u, const std::vector<Pa
         if (stage < 4 && e == cudaSuccess) {
             // refresh + prolong of the next stage state (projection already applied)
             for (int p = 0; p < np && e == cudaSuccess; ++p) {
-                e = launch_fmr_refresh(us[p], plan.dims[p], plan.codes[p].data(), s);
-                if (e == cudaSuccess && p > 0) e = prolong_child(plan, us.data(), p, &w, s);
+                e = p == 0 ? launch_fmr_refresh(us[p], plan.dims[p], plan.codes[p].data(), s)
+                           : prolong_child(plan, us.data(), p, &w, s);
             }
         }
     }

@@ -406,7 +406,9 @@ __global__ void __launch_bounds__(kTz* kTy)
 k_cg_apply(const double* __restrict__ r, const double* __restrict__ pin, double* __restrict__ pout,
            const double* __restrict__ centre, double* __restrict__ ap, SolveGrid G, SolveCtrl* ctrl,
            double* __restrict__ partial) {
-    __shared__ double tile[kTy + 2][kTz + 2];
+    // two plane buffers: plane x+1 is written while plane x may still be read,
+    // so each plane step needs one barrier
+    __shared__ double tile[2][kTy + 2][kTz + 2];
     const SolveCtrl C = read_ctrl(ctrl);
     if (C.done) return;
     const bool first = C.first != 0;
@@ -419,6 +421,9 @@ k_cg_apply(const double* __restrict__ r, const double* __restrict__ pin, double*
     const long long w0 = steps * blockIdx.x / gridDim.x, w1 = steps * (blockIdx.x + 1) / gridDim.x;
     const long long sx = (long long)G.n[1] * G.n[2], sy = G.n[2];
     auto pnew = [&](long long idx) { return first ? r[idx] : fma(beta, pin[idx], r[idx]); };
+    // halo roles: a row of the tile's y halo and/or a column of its z halo
+    const int hy_row = ty == 0 ? 0 : ty == kTy - 1 ? kTy + 1 : -1;
+    const int hz_col = tz == 0 ? 0 : tz == kTz - 1 ? kTz + 1 : -1;
     double dot[1] = {0.0};
     for (long long w = w0; w < w1;) {
         const int t = (int)(w / planes);
@@ -430,34 +435,52 @@ k_cg_apply(const double* __restrict__ r, const double* __restrict__ pin, double*
         const bool in_yz = y <= G.n[1] - 1 && z <= G.n[2] - 1;   // y, z >= 1 by construction
         const bool interior = y <= G.n[1] - 2 && z <= G.n[2] - 2;
         const long long own = (long long)y * sy + z;
-        double pm = in_yz ? pnew((long long)(xs - 1) * sx + own) : 0.0;
-        double pc = in_yz ? pnew((long long)xs * sx + own) : 0.0;
+        // in-array halo cells of this thread (offset from `own`), or none
+        const long long hy_off = hy_row == 0 ? -sy : sy;
+        const bool hy_ok = hy_row >= 0 && z <= G.n[2] - 1 && (hy_row == 0 || y + 1 <= G.n[1] - 1);
+        const long long hz_off = hz_col == 0 ? -1 : 1;
+        const bool hz_ok = hz_col >= 0 && y <= G.n[1] - 1 && (hz_col == 0 || z + 1 <= G.n[2] - 1);
+        auto own_at = [&](int x) { return in_yz ? pnew((long long)x * sx + own) : 0.0; };
+        auto hy_at = [&](int x) { return hy_ok ? pnew((long long)x * sx + own + hy_off) : 0.0; };
+        auto hz_at = [&](int x) { return hz_ok ? pnew((long long)x * sx + own + hz_off) : 0.0; };
+        auto centre_at = [&](int x) { return interior ? centre[(long long)x * sx + own] : 0.0; };
+        double pm = own_at(xs - 1), pc = own_at(xs), pn = own_at(xs + 1);
+        double hy = hy_at(xs), hz = hz_at(xs), cc = centre_at(xs);
+        int buf = 0;
         for (int x = xs; x < xe; ++x) {
-            const long long base = (long long)x * sx;
-            const double pn = in_yz ? pnew(base + sx + own) : 0.0;
-            tile[ty + 1][tz + 1] = pc;
-            if (ty == 0) tile[0][tz + 1] = z <= G.n[2] - 1 ? pnew(base + own - sy) : 0.0;
-            if (ty == kTy - 1)
-                tile[kTy + 1][tz + 1] = (y + 1 <= G.n[1] - 1 && z <= G.n[2] - 1) ? pnew(base + own + sy) : 0.0;
-            if (tz == 0) tile[ty + 1][0] = y <= G.n[1] - 1 ? pnew(base + own - 1) : 0.0;
-            if (tz == kTz - 1)
-                tile[ty + 1][kTz + 1] = (y <= G.n[1] - 1 && z + 1 <= G.n[2] - 1) ? pnew(base + own + 1) : 0.0;
-            __syncthreads();
-            if (interior) {
-                double s = pn + pm;
-                s += tile[ty + 2][tz + 1];
-                s += tile[ty][tz + 1];
-                s += tile[ty + 1][tz + 2];
-                s += tile[ty + 1][tz];
-                const double a = -fma(centre[base + own], pc, s);
-                pout[base + own] = pc;
-                ap[base + own] = a;
-                dot[0] = fma(pc, a, dot[0]);
+            tile[buf][ty + 1][tz + 1] = pc;
+            if (hy_row >= 0) tile[buf][hy_row][tz + 1] = hy;
+            if (hz_col >= 0) tile[buf][ty + 1][hz_col] = hz;
+            // loads of the next plane step, in flight across the barrier and the stencil
+            double pnn = 0.0, hyn = 0.0, hzn = 0.0, ccn = 0.0;
+            if (x + 1 < xe) {
+                pnn = x + 2 <= G.n[0] - 1 ? own_at(x + 2) : 0.0;
+                hyn = hy_at(x + 1);
+                hzn = hz_at(x + 1);
+                ccn = centre_at(x + 1);
             }
             __syncthreads();
+            if (interior) {
+                const long long o = (long long)x * sx + own;
+                double s = pn + pm;
+                s += tile[buf][ty + 2][tz + 1];
+                s += tile[buf][ty][tz + 1];
+                s += tile[buf][ty + 1][tz + 2];
+                s += tile[buf][ty + 1][tz];
+                const double a = -fma(cc, pc, s);
+                pout[o] = pc;
+                ap[o] = a;
+                dot[0] = fma(pc, a, dot[0]);
+            }
             pm = pc;
             pc = pn;
+            pn = pnn;
+            hy = hyn;
+            hz = hzn;
+            cc = ccn;
+            buf ^= 1;
         }
+        __syncthreads();   // the next segment starts over in buffer 0
     }
     double tot[1];
     if (!fold_last<1>(dot, partial, &ctrl->ticket, tot)) return;
