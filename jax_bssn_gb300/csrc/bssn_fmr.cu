@@ -320,7 +320,8 @@ __global__ void k_fmr_window_f32(const double* __restrict__ parent, PatchDims Dp
     out[(long long)c * Wn.cs + t] = static_cast<float>(f[Dp.at(x, y, z)] - b);
 }
 
-__global__ void k_fmr_prolong_f32(const double* __restrict__ parent, PatchDims Dp, const float* __restrict__ win,
+__global__ void __launch_bounds__(kFmrThreads, 4)
+k_fmr_prolong_f32(const double* __restrict__ parent, PatchDims Dp, const float* __restrict__ win,
                                   Window Wn, double* __restrict__ child, PatchDims Dc, int lo0, int lo1, int lo2,
                                   ProlongWeights W, ShellSlabs S) {
     const int slab = blockIdx.y;

@@ -41,6 +41,8 @@
 //           state, and 1/W
 //           (large near punctures) is formed in FP64.  The RHS is written in
 //           FP64, and the RK4 combination stays FP64.
+#include <map>
+
 #include "bssn_fields.cuh"
 #include "bssn_kernels.h"
 #include "bssn_profile.h"
@@ -1247,9 +1249,56 @@ cudaError_t launch_constraints(const double* u, const RhsWork& w, const Geo& G, 
 }
 
 // ---------------------------------------------------------------------------
+// Independent RHS kernels run on two auxiliary streams (per device and host
+// thread), forked from and joined back to the caller's stream with events, so
+// the block scheduler can fill one kernel's tail with another's blocks; under
+// stream capture the forks become parallel graph branches.  Per-kernel
+// profiling times each launch on its own, so it runs them serially; so does a
+// call that is already being captured before the streams exist (creating them
+// is not a capturable operation).
+// ---------------------------------------------------------------------------
+struct RhsStreams {
+    cudaStream_t b = nullptr, c = nullptr;
+    cudaEvent_t fork = nullptr, d1 = nullptr, join_b = nullptr, join_c = nullptr;
+};
+
+static RhsStreams* rhs_streams(cudaStream_t s) {
+    if (profiling_enabled()) return nullptr;
+    thread_local std::map<int, RhsStreams> all;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    auto it = all.find(dev);
+    if (it != all.end()) return &it->second;
+    cudaStreamCaptureStatus status = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &status) != cudaSuccess || status != cudaStreamCaptureStatusNone) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    RhsStreams X;
+    bool ok = cudaStreamCreateWithFlags(&X.b, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaStreamCreateWithFlags(&X.c, cudaStreamNonBlocking) == cudaSuccess;
+    for (cudaEvent_t* e : {&X.fork, &X.d1, &X.join_b, &X.join_c})
+        ok = ok && cudaEventCreateWithFlags(e, cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return &(all[dev] = X);
+}
+
+// ---------------------------------------------------------------------------
 // host-side launch sequence of one RHS evaluation: every stencil kernel runs
 // as a closure-free instantiation on the box interior and a general one on
-// the shell slabs
+// the shell slabs.  Stream use (with the auxiliary streams b and c):
+//   c: Sommerfeld face planes (reads only the state)
+//   main: [momentum derived fields], first derivatives
+//   b: gauge RHS (FP64) or K/Gt RHS (FP32); c: gauge RHS (FP32)
+//   main: [momentum damping], K/Gt/At RHS (FP64) or At RHS (FP32)
+// The stencil kernels skip the Sommerfeld face planes, and each writes its
+// own components, so the branches write disjoint parts of k.
 // ---------------------------------------------------------------------------
 template <typename R>
 static void launch_rhs_form(const R* u, const double* u64, double* k, R* d1, R* der, R* damp, const double* mat,
@@ -1258,6 +1307,18 @@ static void launch_rhs_form(const R* u, const double* u64, double* k, R* d1, R* 
     const int nfield = with_mom ? NMIX + NMIX_MOM : NMIX;
     const int reach = composition_reach(G);
     const Box ext = grown_box(box, G, reach);
+    RhsStreams* X = rhs_streams(stream);
+    const cudaStream_t stb = X ? X->b : stream, stc = X ? X->c : stream;
+    if (X) {
+        cudaEventRecord(X->fork, stream);
+        cudaStreamWaitEvent(stc, X->fork, 0);
+    }
+    if (G.any_sommerfeld) {
+        const BoxSet S = face_slabs(G, box);
+        if (S.n > 0)
+            BSSN_LAUNCH(KC_SOMMERFELD, k_sommerfeld<R>, dim3(blocks_for(largest(S)), S.n, NCOMP / kSommerfeldGroup),
+                        kThreads, stc, u, u64, k, G, S);
+    }
     if (with_mom) {
         // The derived fields are differentiated on ext, so they must be valid
         // on ext grown by the first-derivative reach (3); being pointwise, they
@@ -1276,20 +1337,26 @@ static void launch_rhs_form(const R* u, const double* u64, double* k, R* d1, R* 
     // planes, so the stencil kernels skip those planes.
     const SplitBox sb = split_box(G, G.any_sommerfeld ? without_faces(G, box) : box, coalesced);
     const R* dmp = with_mom ? static_cast<const R*>(damp) : nullptr;
+    if (X) {
+        cudaEventRecord(X->d1, stream);
+        cudaStreamWaitEvent(stb, X->d1, 0);
+        cudaStreamWaitEvent(stc, X->d1, 0);
+    }
+    // gauge: its own branch (b in the FP64 form, c in the FP32 form)
+    const cudaStream_t stg = kPerturbative<R> ? stc : stb;
+    BSSN_LAUNCH_SET(KC_GAUGE, (k_rhs_gauge<R, false>), sb.interior, stg, u, u64, d1, k, G, sb.interior, nfield);
+    BSSN_LAUNCH_SET(KC_GAUGE, (k_rhs_gauge<R, true>), sb.shell, stg, u, u64, d1, k, G, sb.shell, nfield);
     if (with_mom) {
         BSSN_LAUNCH_SET(KC_MOM_DAMP, (k_mom_damping<R, false>), sb.interior, stream, u, u64, der, d1, mat, damp, G,
                         sb.interior, nfield);
         BSSN_LAUNCH_SET(KC_MOM_DAMP, (k_mom_damping<R, true>), sb.shell, stream, u, u64, der, d1, mat, damp, G,
                         sb.shell, nfield);
     }
-    BSSN_LAUNCH_SET(KC_GAUGE, (k_rhs_gauge<R, false>), sb.interior, stream, u, u64, d1, k, G, sb.interior, nfield);
-    BSSN_LAUNCH_SET(KC_GAUGE, (k_rhs_gauge<R, true>), sb.shell, stream, u, u64, d1, k, G, sb.shell, nfield);
     if constexpr (kPerturbative<R>) {
         // FP32 form: issue- and latency-bound, so the smaller split kernels run
         // at higher occupancy.
-        BSSN_LAUNCH_SET(KC_KGT, (k_rhs_kgt<R, false>), sb.interior, stream, u, u64, d1, mat, k, G, sb.interior,
-                        nfield);
-        BSSN_LAUNCH_SET(KC_KGT, (k_rhs_kgt<R, true>), sb.shell, stream, u, u64, d1, mat, k, G, sb.shell, nfield);
+        BSSN_LAUNCH_SET(KC_KGT, (k_rhs_kgt<R, false>), sb.interior, stb, u, u64, d1, mat, k, G, sb.interior, nfield);
+        BSSN_LAUNCH_SET(KC_KGT, (k_rhs_kgt<R, true>), sb.shell, stb, u, u64, d1, mat, k, G, sb.shell, nfield);
         BSSN_LAUNCH_SET(KC_AT, (k_rhs_at<R, false>), sb.interior, stream, u, u64, d1, dmp, mat, k, G, sb.interior,
                         nfield);
         BSSN_LAUNCH_SET(KC_AT, (k_rhs_at<R, true>), sb.shell, stream, u, u64, d1, dmp, mat, k, G, sb.shell, nfield);
@@ -1299,11 +1366,11 @@ static void launch_rhs_form(const R* u, const double* u64, double* k, R* d1, R* 
         BSSN_LAUNCH_SET(KC_CURV, (k_rhs_curv<R, true>), sb.shell, stream, u, u64, d1, dmp, mat, k, G, sb.shell,
                         nfield);
     }
-    if (G.any_sommerfeld) {
-        const BoxSet S = face_slabs(G, box);
-        if (S.n > 0)
-            BSSN_LAUNCH(KC_SOMMERFELD, k_sommerfeld<R>, dim3(blocks_for(largest(S)), S.n, NCOMP / kSommerfeldGroup),
-                        kThreads, stream, u, u64, k, G, S);
+    if (X) {
+        cudaEventRecord(X->join_b, stb);
+        cudaEventRecord(X->join_c, stc);
+        cudaStreamWaitEvent(stream, X->join_b, 0);
+        cudaStreamWaitEvent(stream, X->join_c, 0);
     }
 }
 
