@@ -121,9 +121,11 @@ struct AxiGeom {
 constexpr int kAxiThreads = 128;
 constexpr int kAxiPairs = kCenter + 1;   // planes (j, 8 - j) for j = 0..3, and the centre plane
 
+// With w_only set (the FP32 form, whose support is reconstructed in float),
+// the off-centre plane pairs receive W alone.
 __global__ void __launch_bounds__(kAxiThreads) k_axi_reconstruct(const double* __restrict__ u, Compact C, AxiGeom A,
                                                                  double* __restrict__ dst, long long dcs, long long sx,
-                                                                 long long sy, int ox, int oy, int oz) {
+                                                                 long long sy, int ox, int oy, int oz, int w_only) {
     __shared__ double s_w[6];
     __shared__ double s_cs, s_sn;
     __shared__ int s_start, s_valid;
@@ -166,10 +168,12 @@ __global__ void __launch_bounds__(kAxiThreads) k_axi_reconstruct(const double* _
     }
     const double par3[3] = {-1.0, -1.0, 1.0};
     const double nan = __longlong_as_double(0x7ff8000000000000LL);
+    const bool only_w = w_only && j != kCenter;
     // six-node sum of every component (reflected plane, then the buffer)
     double val[NCOMP];
 #pragma unroll
     for (int c = 0; c < NCOMP; ++c) {
+        if (only_w && c != CW) continue;
         const double* f = u + (long long)c * C.cs;
         const double par = comp_parity(c, par3);
         const double asym = comp_asymptote(c);
@@ -196,6 +200,7 @@ __global__ void __launch_bounds__(kAxiThreads) k_axi_reconstruct(const double* _
         const double L[3][3] = {{s_cs, -sn, 0.0}, {sn, s_cs, 0.0}, {0.0, 0.0, 1.0}};
         const long long d = (long long)(ox + x) * sx + (long long)(oy + plane) * sy + (oz + z);
         dst[(long long)CW * dcs + d] = val[CW];
+        if (only_w) return;
         dst[(long long)CK * dcs + d] = val[CK];
         dst[(long long)CALPHA * dcs + d] = val[CALPHA];
 #pragma unroll
@@ -222,6 +227,140 @@ __global__ void __launch_bounds__(kAxiThreads) k_axi_reconstruct(const double* _
                         const double term = RN_MUL(RN_MUL(L[i][a2], L[jj][b2]), val[off + sym(a2, b2)]);
                         acc = first ? term : RN_ADD(acc, term);
                         first = false;
+                    }
+                    dst[(long long)(off + sym(i, jj)) * dcs + d] = acc;
+                }
+        }
+    };
+    rotate_write(j, s_sn);
+    if (j != kCenter) rotate_write(kSup - 1 - j, -s_sn);
+}
+
+// ---------------------------------------------------------------------------
+// FP32 form: the axisymmetric support in float.  The FP32 RHS reads float
+// perturbations of the support about fixed backgrounds (1 for the metric
+// diagonal, W and alpha; the value at the first positive sample of z row 0
+// for the shift and K; 0 else).  Interpolation weights sum to one, so the
+// perturbation of an interpolated profile is the interpolated perturbation;
+// the reflected ghosts and the 1/r buffer add the background terms their
+// parity and asymptote produce; the rotation preserves the identity metric,
+// and a uniform shift background b gains R b - b.  So the support is
+// reconstructed from float perturbations of the compact state, in float, and
+// only the centre plane (full values at the points) and W (1/W of the
+// derived fields) stay FP64 (k_axi_reconstruct with w_only).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double axi_background(const double* __restrict__ u, const Compact& C, int c) {
+    if (comp_asymptote(c) != 0.0) return 1.0;
+    if (c == BX || c == BY || c == BZ || c == CK) return u[(long long)c * C.cs + (long long)kCG * C.nz];
+    return 0.0;
+}
+
+__global__ void k_compact_f32(const double* __restrict__ u, Compact C, float* __restrict__ cf) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= C.cs * NCOMP) return;
+    const int c = (int)(t / C.cs);
+    cf[t] = static_cast<float>(u[t] - axi_background(u, C, c));
+}
+
+__global__ void __launch_bounds__(kAxiThreads)
+k_axi_reconstruct_f32(const float* __restrict__ cf, const double* __restrict__ u, Compact C, AxiGeom A,
+                      float* __restrict__ dst, long long dcs, long long sx, long long sy, int ox, int oy, int oz) {
+    __shared__ float s_w[6];
+    __shared__ float s_cs, s_sn;
+    __shared__ int s_start, s_valid;
+    __shared__ float s_b[NCOMP];
+    const int col = blockIdx.x;
+    const int x = col / kAxiPairs, j = col - (col / kAxiPairs) * kAxiPairs;
+    if (threadIdx.x == 0) {
+        const double X = RN_MUL((double)x - 3.5, A.dx);
+        const double Y = RN_MUL((double)j - 4.0, A.dx);
+        const double rho = __dsqrt_rn(RN_ADD(RN_MUL(X, X), RN_MUL(Y, Y)));
+        const double q = RN_ADD(RN_ADD(RN_DIV(rho, A.dx), 4.0), -0.5);
+        int start;
+        double w[6];
+        s_valid = lagrange_nodes(q, C.nx + 3, start, w) ? 1 : 0;
+        s_start = start;
+        for (int k = 0; k < 6; ++k) s_w[k] = static_cast<float>(w[k]);
+        s_cs = static_cast<float>(rho <= 0.0 ? 1.0 : RN_DIV(X, rho));
+        s_sn = static_cast<float>(rho <= 0.0 ? 0.0 : RN_DIV(Y, rho));
+    }
+    if (threadIdx.x < NCOMP) s_b[threadIdx.x] = static_cast<float>(axi_background(u, C, threadIdx.x));
+    __syncthreads();
+    const int z = blockIdx.y * kAxiThreads + threadIdx.x;
+    if (z >= C.nz) return;
+    const int start = s_start;
+    const bool valid = s_valid != 0;
+    float w[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) w[k] = s_w[k];
+    float ratio[3] = {0.f, 0.f, 0.f};
+    if (start + 5 >= C.nx) {
+        const double rho_edge = RN_MUL((double)(C.nx - kCG) - 0.5, A.dx);
+        const double zc = RN_ADD(A.zmin, RN_MUL(A.dx, (double)z));
+        const double zz = RN_MUL(zc, zc);
+        const double r_edge = __dsqrt_rn(RN_ADD(RN_MUL(rho_edge, rho_edge), zz));
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            const double rho_b = RN_ADD(rho_edge, RN_MUL(A.dx, (double)(b + 1)));
+            ratio[b] = static_cast<float>(RN_DIV(r_edge, __dsqrt_rn(RN_ADD(RN_MUL(rho_b, rho_b), zz))));
+        }
+    }
+    const double par3[3] = {-1.0, -1.0, 1.0};
+    const float nan = __int_as_float(0x7fc00000);
+    float val[NCOMP];
+#pragma unroll
+    for (int c = 0; c < NCOMP; ++c) {
+        const float* f = cf + (long long)c * C.cs;
+        const float par = static_cast<float>(comp_parity(c, par3));
+        const float b = s_b[c];
+        const float asym = static_cast<float>(comp_asymptote(c));
+        float acc = 0.f;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            const int src = start + k;
+            float v;
+            // perturbations: the reflection par (d + b) - b, the buffer
+            // asym + (d_edge + b - asym) r - b
+            if (src < kCG) v = fmaf(par, f[(long long)(2 * kCG - 1 - src) * C.nz + z], (par - 1.f) * b);
+            else if (src < C.nx) v = f[(long long)src * C.nz + z];
+            else {
+                const float r = ratio[src - C.nx];
+                v = fmaf(f[(long long)(C.nx - 1) * C.nz + z], r, (asym - b) * (1.f - r));
+            }
+            acc = fmaf(v, w[k], acc);
+        }
+        val[c] = valid ? acc : nan;
+    }
+    auto rotate_write = [&](int plane, float sn) {
+        const float cs = s_cs;
+        const float L[3][3] = {{cs, -sn, 0.f}, {sn, cs, 0.f}, {0.f, 0.f, 1.f}};
+        const long long d = (long long)(ox + x) * sx + (long long)(oy + plane) * sy + (oz + z);
+        dst[(long long)CW * dcs + d] = val[CW];
+        dst[(long long)CK * dcs + d] = val[CK];
+        dst[(long long)CALPHA * dcs + d] = val[CALPHA];
+        // connection functions: background 0
+        dst[(long long)GTX * dcs + d] = L[0][0] * val[GTX] + L[0][1] * val[GTY];
+        dst[(long long)GTY * dcs + d] = L[1][0] * val[GTX] + L[1][1] * val[GTY];
+        dst[(long long)GTZ * dcs + d] = val[GTZ];
+        // shift: R (b + d) - b = R d + (R b - b)
+        const float bx = s_b[BX], by = s_b[BY];
+        dst[(long long)BX * dcs + d] = L[0][0] * val[BX] + L[0][1] * val[BY] + ((cs - 1.f) * bx - sn * by);
+        dst[(long long)BY * dcs + d] = L[1][0] * val[BX] + L[1][1] * val[BY] + (sn * bx + (cs - 1.f) * by);
+        dst[(long long)BZ * dcs + d] = val[BZ];
+        // metric (background I, preserved) and At (background 0): R T R^T
+#pragma unroll
+        for (int base = 0; base < 2; ++base) {
+            const int off = base == 0 ? GXX : AXX;
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int jj = i; jj < 3; ++jj) {
+                    float acc = 0.f;
+#pragma unroll
+                    for (int ab = 0; ab < 9; ++ab) {
+                        const int a2 = ab / 3, b2 = ab % 3;
+                        if ((i == 2) != (a2 == 2) || (jj == 2) != (b2 == 2)) continue;   // literal zero of L
+                        acc = fmaf(L[i][a2] * L[jj][b2], val[off + sym(a2, b2)], acc);
                     }
                     dst[(long long)(off + sym(i, jj)) * dcs + d] = acc;
                 }
@@ -481,7 +620,7 @@ cudaError_t reconstruct(const CartoonPlan& P, const BssnParams* p, const double*
     if (P.axi) {
         const AxiGeom A{p->dx, p->xmin[2]};
         const dim3 grid((unsigned)(P.C.nx * kAxiPairs), (unsigned)((P.C.nz + kAxiThreads - 1) / kAxiThreads));
-        BSSN_LAUNCH(KC_CARTOON, k_axi_reconstruct, grid, kAxiThreads, s, u, P.C, A, us, P.scs, sx, sy, 4, 4, 4);
+        BSSN_LAUNCH(KC_CARTOON, k_axi_reconstruct, grid, kAxiThreads, s, u, P.C, A, us, P.scs, sx, sy, 4, 4, 4, 0);
     } else {
         const long long n = (long long)P.C.nx * kSup * kSup;
         BSSN_LAUNCH(KC_CARTOON, k_sph_reconstruct, blocks(n), kThr, s, u, P.C.nx, p->dx, us, P.scs, sx, sy, 4, 4, 4);
@@ -489,13 +628,36 @@ cudaError_t reconstruct(const CartoonPlan& P, const BssnParams* p, const double*
     return launch_fill_periodic(us, NCOMP, P.Gs, s);
 }
 
+// FP32 form, axisymmetric: FP64 support only on the centre plane and for W,
+// float support from float perturbations of the compact state (staged in the
+// first-derivative scratch, which the RHS overwrites afterwards).
+cudaError_t reconstruct_f32(const CartoonPlan& P, const BssnParams* p, const double* u, double* us, const RhsWork& w,
+                            cudaStream_t s) {
+    const long long sx = P.Gs.st[0], sy = P.Gs.st[1];
+    const AxiGeom A{p->dx, p->xmin[2]};
+    const dim3 grid((unsigned)(P.C.nx * kAxiPairs), (unsigned)((P.C.nz + kAxiThreads - 1) / kAxiThreads));
+    BSSN_LAUNCH(KC_CARTOON, k_axi_reconstruct, grid, kAxiThreads, s, u, P.C, A, us, P.scs, sx, sy, 4, 4, 4, 1);
+    cudaError_t e = launch_fill_periodic(us, NCOMP, P.Gs, s);
+    if (e != cudaSuccess) return e;
+    float* cf = w.d1f;
+    BSSN_LAUNCH(KC_CONVERT, k_compact_f32, blocks(P.C.cs * NCOMP), kThr, s, u, P.C, cf);
+    BSSN_LAUNCH(KC_CARTOON, k_axi_reconstruct_f32, grid, kAxiThreads, s, cf, u, P.C, A, w.uf, P.scs, sx, sy, 4, 4, 4);
+    return launch_fill_periodic(w.uf, NCOMP, P.Gs, s);
+}
+
 cudaError_t compact_rhs(const CartoonPlan& P, const BssnParams* p, const double* u, double* kc, double* base,
                         cudaStream_t s) {
     double* us = base;
     double* ks = us + NCOMP * P.scs;
     const RhsWork w = carve_rhs_work(ks + NCOMP * P.scs, P.scs, P.with_mom);
-    cudaError_t e = reconstruct(P, p, u, us, s);
-    if (e == cudaSuccess) e = launch_rhs(us, ks, w, P.Gs, P.centre, s);
+    cudaError_t e;
+    if (P.axi && P.Gs.precision == kPrecisionF32) {
+        e = reconstruct_f32(P, p, u, us, w, s);
+        if (e == cudaSuccess) e = launch_rhs_f32_prepared(us, ks, w, P.Gs, P.centre, s);
+    } else {
+        e = reconstruct(P, p, u, us, s);
+        if (e == cudaSuccess) e = launch_rhs(us, ks, w, P.Gs, P.centre, s);
+    }
     if (e == cudaSuccess) {
         const long long n = (long long)(P.C.nx - kCG) * P.C.nz * NCOMP;
         BSSN_LAUNCH(KC_CARTOON, k_collect, blocks(n), kThr, s, ks, P.scs, P.Gs.st[0], P.Gs.st[1], 4 + kCenter,
@@ -582,7 +744,7 @@ int bssn_cartoon_reconstruct(int32_t axisymmetric, const double* compact, double
         const long long dcs = (long long)P.C.nx * kSup * P.C.nz;
         const dim3 grid((unsigned)(P.C.nx * kAxiPairs), (unsigned)((P.C.nz + kAxiThreads - 1) / kAxiThreads));
         BSSN_LAUNCH(KC_CARTOON, k_axi_reconstruct, grid, kAxiThreads, s, compact, P.C, A, support, dcs,
-                    (long long)kSup * P.C.nz, (long long)P.C.nz, 0, 0, 0);
+                    (long long)kSup * P.C.nz, (long long)P.C.nz, 0, 0, 0, 0);
     } else {
         const long long n = (long long)P.C.nx * kSup * kSup;
         BSSN_LAUNCH(KC_CARTOON, k_sph_reconstruct, blocks(n), kThr, s, compact, P.C.nx, params->dx, support, n,

@@ -261,7 +261,8 @@ __global__ void k_import_matter(const double* __restrict__ rho, const double* __
 // left alone: on such an axis the one-sided closures cover the three outer
 // rows and every interior stencil stays inside the region, so nothing reads
 // them.
-__global__ void k_fill_periodic(double* __restrict__ u, int ncomp, Geo G, Box region, Box all, int closed) {
+template <typename T>
+__global__ void k_fill_periodic(T* __restrict__ u, int ncomp, Geo G, Box region, Box all, int closed) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= all.count) return;
     int ix[3];
@@ -442,7 +443,8 @@ __global__ void k_zero(double* __restrict__ u, long long n) {
 // ---------------------------------------------------------------------------
 // launchers shared by the C ABI, FMR and Cartoon drivers
 // ---------------------------------------------------------------------------
-cudaError_t launch_fill_periodic(double* u, int ncomp, const Geo& G, cudaStream_t s) {
+template <typename T>
+static cudaError_t fill_periodic(T* u, int ncomp, const Geo& G, cudaStream_t s) {
     const Box region = box_of(G);
     const Box all = full_box(G);
     int closed = 0;
@@ -452,8 +454,16 @@ cudaError_t launch_fill_periodic(double* u, int ncomp, const Geo& G, cudaStream_
         if (!a.reduced && a.lbc && a.rbc && a.lo == a.start && a.hi == a.end) closed |= 1 << d;
     }
     if (closed == 7) return cudaSuccess;
-    BSSN_LAUNCH(KC_FILL, k_fill_periodic, nblocks(all.count), kThreads, s, u, ncomp, G, region, all, closed);
+    BSSN_LAUNCH(KC_FILL, k_fill_periodic<T>, nblocks(all.count), kThreads, s, u, ncomp, G, region, all, closed);
     return cudaGetLastError();
+}
+
+cudaError_t launch_fill_periodic(double* u, int ncomp, const Geo& G, cudaStream_t s) {
+    return fill_periodic(u, ncomp, G, s);
+}
+
+cudaError_t launch_fill_periodic(float* u, int ncomp, const Geo& G, cudaStream_t s) {
+    return fill_periodic(u, ncomp, G, s);
 }
 
 cudaError_t launch_project(double* u, const Geo& G, const Box& B, cudaStream_t s) {

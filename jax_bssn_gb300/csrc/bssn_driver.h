@@ -20,6 +20,7 @@ Box box_of(const Geo& G);
 Box full_box(const Geo& G);
 
 cudaError_t launch_fill_periodic(double* u, int ncomp, const Geo& G, cudaStream_t s);
+cudaError_t launch_fill_periodic(float* u, int ncomp, const Geo& G, cudaStream_t s);
 cudaError_t launch_project(double* u, const Geo& G, const Box& B, cudaStream_t s);
 cudaError_t launch_rk4_stage(const double* u0, const double* k, double* acc, double* out, const Geo& G,
                              const Box& B, int stage, double dt, int final_form, int project, cudaStream_t s);

@@ -32,6 +32,14 @@ RhsWork carve_rhs_work(double* base, long long cs, bool with_mom);
 cudaError_t launch_rhs(const double* u, double* k, const RhsWork& w, const Geo& G, const Box& box,
                        cudaStream_t stream);
 
+// FP32 form with w.uf already holding the float perturbations of the whole
+// padded block, about the backgrounds the FP32 RHS assumes (1 for the metric
+// diagonal, W and alpha; one sample's value for the shift and K; 0 else).
+// u supplies the FP64 values the FP32 kernels read: every component on the
+// box, W wherever the momentum-constraint derived fields are formed.
+cudaError_t launch_rhs_f32_prepared(const double* u, double* k, const RhsWork& w, const Geo& G, const Box& box,
+                                    cudaStream_t stream);
+
 // H, M_i (3 blocks), det-1, tr At, Gamma constraint (3 blocks) on the box,
 // each block box.count long in the box's linear order.  Uses w.d1 (NMIX set)
 // and w.der.

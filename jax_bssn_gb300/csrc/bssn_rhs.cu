@@ -1374,6 +1374,12 @@ static void launch_rhs_form(const R* u, const double* u64, double* k, R* d1, R* 
     }
 }
 
+cudaError_t launch_rhs_f32_prepared(const double* u, double* k, const RhsWork& w, const Geo& G, const Box& box,
+                                    cudaStream_t stream) {
+    launch_rhs_form<float>(w.uf, u, k, w.d1f, w.derf, w.dampf, w.mat, G, box, stream);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_rhs(const double* u, double* k, const RhsWork& w, const Geo& G, const Box& box,
                        cudaStream_t stream) {
     if (G.precision == kPrecisionF32) {
