@@ -637,7 +637,8 @@ cudaError_t reconstruct_f32(const CartoonPlan& P, const BssnParams* p, const dou
     const AxiGeom A{p->dx, p->xmin[2]};
     const dim3 grid((unsigned)(P.C.nx * kAxiPairs), (unsigned)((P.C.nz + kAxiThreads - 1) / kAxiThreads));
     BSSN_LAUNCH(KC_CARTOON, k_axi_reconstruct, grid, kAxiThreads, s, u, P.C, A, us, P.scs, sx, sy, 4, 4, 4, 1);
-    cudaError_t e = launch_fill_periodic(us, NCOMP, P.Gs, s);
+    // FP64 values outside the centre box are read for W only
+    cudaError_t e = launch_fill_periodic(us + (long long)CW * P.scs, 1, P.Gs, s);
     if (e != cudaSuccess) return e;
     float* cf = w.d1f;
     BSSN_LAUNCH(KC_CONVERT, k_compact_f32, blocks(P.C.cs * NCOMP), kThr, s, u, P.C, cf);

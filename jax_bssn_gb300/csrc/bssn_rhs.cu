@@ -1114,6 +1114,18 @@ static long long largest(const BoxSet& S) {
     return m;
 }
 
+// Block size of a box-set launch: kThreads, or fewer (down to one warp) when
+// kThreads would leave under four blocks per SM.  With GB300's two FP64 lanes
+// per SM per cycle, a small launch (a Cartoon plane, the shell of a small box)
+// otherwise runs a few FP64-heavy blocks on a few SMs while the rest idle.
+static inline int set_threads(const BoxSet& S) {
+    long long total = 0;
+    for (int i = 0; i < S.n; ++i) total += S.b[i].count;
+    for (int t = kThreads; t > 32; t /= 2)
+        if ((total + t - 1) / t >= 152LL * 4) return t;
+    return 32;
+}
+
 // A box split into its interior -- samples at least kClosureRows from every
 // closed (Sommerfeld) owned face, where no stencil needs a one-sided closure --
 // and the rest of the box as up to ten slabs.
@@ -1160,16 +1172,20 @@ static SplitBox split_box(const Geo& G, const Box& box, bool coalesced) {
     // interior range of its axis: the 32 samples of a warp then share their
     // closure rows (no divergent closure branches), except where a warp wraps
     // to the next row.
-    //   z rows:  z in the closure rows, y interior, x whole box; y fastest
+    //   z rows:  z in the closure rows, y interior, x whole box; y fastest,
+    //            or x fastest when the y range is shorter than a warp and
+    //            than the x range (a single-plane Cartoon box)
     //   y rows:  y in the closure rows, z interior, x whole box; z fastest
     //   yz rows: y and z in the closure rows, x whole box; x fastest
     //   x rows:  x in the closure rows, y and z interior; z fastest
     const int E0[2] = {blo[0], hi[0]}, E1[2] = {lo[0], bhi[0]};  // x closure ranges [E0, E1)
     const int Y0[2] = {blo[1], hi[1]}, Y1[2] = {lo[1], bhi[1]};
     const int Z0[2] = {blo[2], hi[2]}, Z1[2] = {lo[2], bhi[2]};
+    const int ny = hi[1] - lo[1], nx = bhi[0] - blo[0];
+    const int zrow_fast = (ny >= 32 || ny >= nx) ? 1 : 0;
     for (int f = 0; f < 2; ++f) {
         const int l[3] = {blo[0], lo[1], Z0[f]}, h[3] = {bhi[0], hi[1], Z1[f]};
-        add_box(S.shell, make_box(l, h, 1));
+        add_box(S.shell, make_box(l, h, zrow_fast));
     }
     for (int f = 0; f < 2; ++f) {
         const int l[3] = {blo[0], Y0[f], lo[2]}, h[3] = {bhi[0], Y1[f], hi[2]};
@@ -1232,8 +1248,11 @@ static BoxSet face_slabs(const Geo& G, const Box& box) {
 
 #define BSSN_LAUNCH_SET(cls, kernel, set, stream, ...)                                                     \
     do {                                                                                                  \
-        if ((set).n > 0)                                                                                  \
-            BSSN_LAUNCH(cls, kernel, dim3(blocks_for(largest(set)), (set).n), kThreads, stream, __VA_ARGS__); \
+        if ((set).n > 0) {                                                                                \
+            const int threads_ = set_threads(set);                                                        \
+            BSSN_LAUNCH(cls, kernel, dim3((unsigned)((largest(set) + threads_ - 1) / threads_), (set).n),   \
+                        threads_, stream, __VA_ARGS__);                                                    \
+        }                                                                                                 \
     } while (0)
 
 cudaError_t launch_constraints(const double* u, const RhsWork& w, const Geo& G, const Box& box, double* H,
@@ -1295,8 +1314,9 @@ static RhsStreams* rhs_streams(cudaStream_t s) {
 // the shell slabs.  Stream use (with the auxiliary streams b and c):
 //   c: Sommerfeld face planes (reads only the state)
 //   main: [momentum derived fields], first derivatives
-//   b: gauge RHS (FP64) or K/Gt RHS (FP32); c: gauge RHS (FP32)
-//   main: [momentum damping], K/Gt/At RHS (FP64) or At RHS (FP32)
+//   b: gauge RHS (FP64) or K/Gt RHS (FP32); c: gauge RHS (FP32), or the
+//      shell's [momentum damping] and K/Gt/At RHS (FP64)
+//   main: [momentum damping], K/Gt/At RHS (FP64, interior) or At RHS (FP32)
 // The stencil kernels skip the Sommerfeld face planes, and each writes its
 // own components, so the branches write disjoint parts of k.
 // ---------------------------------------------------------------------------
@@ -1346,10 +1366,13 @@ static void launch_rhs_form(const R* u, const double* u64, double* k, R* d1, R* 
     const cudaStream_t stg = kPerturbative<R> ? stc : stb;
     BSSN_LAUNCH_SET(KC_GAUGE, (k_rhs_gauge<R, false>), sb.interior, stg, u, u64, d1, k, G, sb.interior, nfield);
     BSSN_LAUNCH_SET(KC_GAUGE, (k_rhs_gauge<R, true>), sb.shell, stg, u, u64, d1, k, G, sb.shell, nfield);
+    // FP64 form: the shell's damping and curvature (each pointwise in damp)
+    // run on c beside the interior's
+    const cudaStream_t sts = kPerturbative<R> ? stream : stc;
     if (with_mom) {
         BSSN_LAUNCH_SET(KC_MOM_DAMP, (k_mom_damping<R, false>), sb.interior, stream, u, u64, der, d1, mat, damp, G,
                         sb.interior, nfield);
-        BSSN_LAUNCH_SET(KC_MOM_DAMP, (k_mom_damping<R, true>), sb.shell, stream, u, u64, der, d1, mat, damp, G,
+        BSSN_LAUNCH_SET(KC_MOM_DAMP, (k_mom_damping<R, true>), sb.shell, sts, u, u64, der, d1, mat, damp, G,
                         sb.shell, nfield);
     }
     if constexpr (kPerturbative<R>) {
@@ -1363,7 +1386,7 @@ static void launch_rhs_form(const R* u, const double* u64, double* k, R* d1, R* 
     } else {
         BSSN_LAUNCH_SET(KC_CURV, (k_rhs_curv<R, false>), sb.interior, stream, u, u64, d1, dmp, mat, k, G,
                         sb.interior, nfield);
-        BSSN_LAUNCH_SET(KC_CURV, (k_rhs_curv<R, true>), sb.shell, stream, u, u64, d1, dmp, mat, k, G, sb.shell,
+        BSSN_LAUNCH_SET(KC_CURV, (k_rhs_curv<R, true>), sb.shell, sts, u, u64, d1, dmp, mat, k, G, sb.shell,
                         nfield);
     }
     if (X) {
