@@ -1278,7 +1278,7 @@ cudaError_t launch_constraints(const double* u, const RhsWork& w, const Geo& G, 
 // ---------------------------------------------------------------------------
 struct RhsStreams {
     cudaStream_t b = nullptr, c = nullptr;
-    cudaEvent_t fork = nullptr, d1 = nullptr, join_b = nullptr, join_c = nullptr;
+    cudaEvent_t fork = nullptr, pre = nullptr, fd = nullptr, d1 = nullptr, join_b = nullptr, join_c = nullptr;
 };
 
 static RhsStreams* rhs_streams(cudaStream_t s) {
@@ -1299,7 +1299,7 @@ static RhsStreams* rhs_streams(cudaStream_t s) {
     RhsStreams X;
     bool ok = cudaStreamCreateWithFlags(&X.b, cudaStreamNonBlocking) == cudaSuccess &&
               cudaStreamCreateWithFlags(&X.c, cudaStreamNonBlocking) == cudaSuccess;
-    for (cudaEvent_t* e : {&X.fork, &X.d1, &X.join_b, &X.join_c})
+    for (cudaEvent_t* e : {&X.fork, &X.pre, &X.fd, &X.d1, &X.join_b, &X.join_c})
         ok = ok && cudaEventCreateWithFlags(e, cudaEventDisableTiming) == cudaSuccess;
     if (!ok) {
         cudaGetLastError();
@@ -1313,10 +1313,13 @@ static RhsStreams* rhs_streams(cudaStream_t s) {
 // as a closure-free instantiation on the box interior and a general one on
 // the shell slabs.  Stream use (with the auxiliary streams b and c):
 //   c: Sommerfeld face planes (reads only the state)
-//   main: [momentum derived fields], first derivatives
-//   b: gauge RHS (FP64) or K/Gt RHS (FP32); c: gauge RHS (FP32), or the
-//      shell's [momentum damping] and K/Gt/At RHS (FP64)
-//   main: [momentum damping], K/Gt/At RHS (FP64, interior) or At RHS (FP32)
+//   main: [momentum derived fields], first derivatives (interior); b: the
+//      shell's first derivatives
+//   b: gauge RHS (FP64) or K/Gt RHS and the shell's [momentum damping] and
+//      At RHS (FP32); c: gauge RHS (FP32), or the shell's [momentum damping]
+//      and K/Gt/At RHS (FP64)
+//   main: the interior's [momentum damping] and K/Gt/At (FP64) or At (FP32)
+// (the damping term enters the curvature RHS at its own point only).
 // The stencil kernels skip the Sommerfeld face planes, and each writes its
 // own components, so the branches write disjoint parts of k.
 // ---------------------------------------------------------------------------
@@ -1351,8 +1354,16 @@ static void launch_rhs_form(const R* u, const double* u64, double* k, R* d1, R* 
     // divergent closure branches; the FP32 form keeps coalesced slabs.
     const bool coalesced = kPerturbative<R>;
     const SplitBox se = split_box(G, ext, coalesced);
+    if (X) {
+        cudaEventRecord(X->pre, stream);
+        cudaStreamWaitEvent(stb, X->pre, 0);
+    }
+    BSSN_LAUNCH_SET(KC_FIRST, (k_first_derivs<R, true>), se.shell, stb, u, der, d1, G, se.shell, with_mom);
     BSSN_LAUNCH_SET(KC_FIRST, (k_first_derivs<R, false>), se.interior, stream, u, der, d1, G, se.interior, with_mom);
-    BSSN_LAUNCH_SET(KC_FIRST, (k_first_derivs<R, true>), se.shell, stream, u, der, d1, G, se.shell, with_mom);
+    if (X) {
+        cudaEventRecord(X->fd, stb);
+        cudaStreamWaitEvent(stream, X->fd, 0);
+    }
     // k_sommerfeld replaces every component's RHS on the active Sommerfeld face
     // planes, so the stencil kernels skip those planes.
     const SplitBox sb = split_box(G, G.any_sommerfeld ? without_faces(G, box) : box, coalesced);
@@ -1366,9 +1377,9 @@ static void launch_rhs_form(const R* u, const double* u64, double* k, R* d1, R* 
     const cudaStream_t stg = kPerturbative<R> ? stc : stb;
     BSSN_LAUNCH_SET(KC_GAUGE, (k_rhs_gauge<R, false>), sb.interior, stg, u, u64, d1, k, G, sb.interior, nfield);
     BSSN_LAUNCH_SET(KC_GAUGE, (k_rhs_gauge<R, true>), sb.shell, stg, u, u64, d1, k, G, sb.shell, nfield);
-    // FP64 form: the shell's damping and curvature (each pointwise in damp)
-    // run on c beside the interior's
-    const cudaStream_t sts = kPerturbative<R> ? stream : stc;
+    // the shell's damping and curvature (pointwise in damp) run beside the
+    // interior's: on c (FP64) or after the K/Gt RHS on b (FP32)
+    const cudaStream_t sts = kPerturbative<R> ? stb : stc;
     if (with_mom) {
         BSSN_LAUNCH_SET(KC_MOM_DAMP, (k_mom_damping<R, false>), sb.interior, stream, u, u64, der, d1, mat, damp, G,
                         sb.interior, nfield);
@@ -1382,7 +1393,7 @@ static void launch_rhs_form(const R* u, const double* u64, double* k, R* d1, R* 
         BSSN_LAUNCH_SET(KC_KGT, (k_rhs_kgt<R, true>), sb.shell, stb, u, u64, d1, mat, k, G, sb.shell, nfield);
         BSSN_LAUNCH_SET(KC_AT, (k_rhs_at<R, false>), sb.interior, stream, u, u64, d1, dmp, mat, k, G, sb.interior,
                         nfield);
-        BSSN_LAUNCH_SET(KC_AT, (k_rhs_at<R, true>), sb.shell, stream, u, u64, d1, dmp, mat, k, G, sb.shell, nfield);
+        BSSN_LAUNCH_SET(KC_AT, (k_rhs_at<R, true>), sb.shell, sts, u, u64, d1, dmp, mat, k, G, sb.shell, nfield);
     } else {
         BSSN_LAUNCH_SET(KC_CURV, (k_rhs_curv<R, false>), sb.interior, stream, u, u64, d1, dmp, mat, k, G,
                         sb.interior, nfield);
