@@ -17,6 +17,7 @@
 #include <array>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <vector>
 
 #include "../../include/bssn_gb300.h"
@@ -663,22 +664,78 @@ cudaError_t prepare(const FmrPlan& plan, double* const* u, bool project, cudaStr
     return e;
 }
 
+// Streams for the children's stage work (per device and host thread), so
+// that every patch's RHS and stage combination run concurrently: they touch
+// only their own patch.  Profiling and calls captured before the streams exist
+// run serially on the caller's stream.
+struct PatchStreams {
+    std::vector<cudaStream_t> s;
+    std::vector<cudaEvent_t> join;
+    cudaEvent_t fork = nullptr;
+};
+
+PatchStreams* patch_streams(int n, cudaStream_t caller) {
+    if (n <= 0 || profiling_enabled()) return nullptr;
+    thread_local std::map<int, PatchStreams> all;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    PatchStreams& P = all[dev];
+    if ((int)P.s.size() >= n && P.fork) return &P;
+    cudaStreamCaptureStatus status = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(caller, &status) != cudaSuccess || status != cudaStreamCaptureStatusNone) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (!P.fork && cudaEventCreateWithFlags(&P.fork, cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError();
+        P.fork = nullptr;
+        return nullptr;
+    }
+    while ((int)P.s.size() < n) {
+        cudaStream_t st = nullptr;
+        cudaEvent_t ev = nullptr;
+        if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        P.s.push_back(st);
+        P.join.push_back(ev);
+    }
+    return &P;
+}
+
 cudaError_t fmr_step(const FmrPlan& plan, double* const* u, const std::vector<PatchWork>& w, double dt,
                      cudaStream_t s) {
     const int np = plan.npatch;
     std::vector<double*> us(np);
     for (int p = 0; p < np; ++p) us[p] = w[p].us;
+    PatchStreams* PS = patch_streams(np - 1, s);
     cudaError_t e = prepare(plan, u, true, s, &w);  // s0
     for (int stage = 1; stage <= 4 && e == cudaSuccess; ++stage) {
         double* const* src = stage == 1 ? u : us.data();
-        for (int p = 0; p < np && e == cudaSuccess; ++p)
-            e = launch_rhs(src[p], w[p].k, w[p].rw, plan.geo[p], owned_box(plan.geo[p]), s);
-        // stage combination on owned samples with projection (= project_owned of the next prepare)
-        for (int p = 0; p < np && e == cudaSuccess; ++p) {
-            double* out = stage == 4 ? u[p] : us[p];
-            e = launch_rk4_stage(u[p], w[p].k, w[p].acc, out, plan.geo[p], owned_box(plan.geo[p]), stage, dt,
-                                 /*final_form=*/1, /*project=*/1, s);
+        if (PS) {
+            cudaEventRecord(PS->fork, s);
+            for (int p = 1; p < np; ++p) cudaStreamWaitEvent(PS->s[p - 1], PS->fork, 0);
         }
+        // each patch's RHS, then its stage combination on owned samples with
+        // projection (= project_owned of the next prepare), on its own stream
+        for (int p = 0; p < np && e == cudaSuccess; ++p) {
+            const cudaStream_t sp = (PS && p > 0) ? PS->s[p - 1] : s;
+            e = launch_rhs(src[p], w[p].k, w[p].rw, plan.geo[p], owned_box(plan.geo[p]), sp);
+            double* out = stage == 4 ? u[p] : us[p];
+            if (e == cudaSuccess)
+                e = launch_rk4_stage(u[p], w[p].k, w[p].acc, out, plan.geo[p], owned_box(plan.geo[p]), stage, dt,
+                                     /*final_form=*/1, /*project=*/1, sp);
+        }
+        if (PS)
+            for (int p = 1; p < np; ++p) {
+                cudaEventRecord(PS->join[p - 1], PS->s[p - 1]);
+                cudaStreamWaitEvent(s, PS->join[p - 1], 0);
+            }
         if (stage < 4 && e == cudaSuccess) {
             // refresh + prolong of the next stage state (projection already applied)
             for (int p = 0; p < np && e == cudaSuccess; ++p) {
