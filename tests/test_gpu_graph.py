@@ -69,3 +69,44 @@ def test_axisymmetric_evolution_graph(cuda, native, precision):
     def snapshot(evo):
         return [evo.components().flatten()]
     _check(lambda: AxisymmetricEvolution(state, params, precision=precision), snapshot)
+
+
+def _serial(lib, fn):
+    """Run fn with per-kernel profiling on: every launch then goes to the
+    caller's stream in order, with no auxiliary-stream branches."""
+    lib.bssn_profile_reset()
+    lib.bssn_profile_enable(1)
+    try:
+        return fn()
+    finally:
+        torch.cuda.synchronize()
+        lib.bssn_profile_enable(0)
+        lib.bssn_profile_reset()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_stream_branches_equal_serial_launches(cuda, native, precision):
+    """The RHS kernels' auxiliary-stream branches and the FMR children's
+    streams give the same bits as one in-order stream."""
+    from jax_bssn_gb300.cartoon.axisymmetry import AxisymmetricEvolution
+    from jax_bssn_gb300.evolution import PatchEvolution
+    from jax_bssn_gb300.fmr import FMREvolution, initialize_tiled_fmr
+    from jax_bssn_gb300.initial_data import (brill_lindquist_config, fmr_linear_wave_hierarchy,
+                                             fmr_linear_wave_root, linear_wave_callback, teukolsky_config)
+    state, params = teukolsky_config(n=20)
+    hierarchy = fmr_linear_wave_hierarchy(32)
+    states, parameters, layouts = initialize_tiled_fmr(linear_wave_callback(), fmr_linear_wave_root(32), (32,) * 3,
+                                                       hierarchy)
+    bl_state, bl_params = brill_lindquist_config(num_radial_points=32, r_max=1.0)
+    cases = [
+        (lambda: PatchEvolution(state, params, precision=precision), lambda e: [e.components().flatten()]),
+        (lambda: FMREvolution(states, parameters, hierarchy, layouts, precision=precision),
+         lambda e: [leaf.flatten() for s in e.states() for leaf in s]),
+        (lambda: AxisymmetricEvolution(bl_state, bl_params, precision=precision), lambda e: [e.components().flatten()]),
+    ]
+    for make, snapshot in cases:
+        branched, serial = make(), make()
+        branched.step(3)
+        _serial(native, lambda: serial.step(3))
+        torch.cuda.synchronize()
+        _bitwise_equal(snapshot(branched), snapshot(serial))

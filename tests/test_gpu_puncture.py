@@ -217,3 +217,24 @@ def test_newton_not_converged_raises(by):
         by.solve_axisymmetric_conformal_factor([1.0], np.zeros((1, 3)), [[0.0, 0.0, 0.2]],
                                                by.axisymmetric_cell_centered_grid(8, 4.0)[0], 0.5,
                                                max_newton_iterations=1, max_linear_iterations=1)
+
+
+@pytest.mark.parametrize("name", ["cart_binary", "axi_binary"])
+def test_graph_replay_equals_direct_launches(by, gold, native, name):
+    """Krylov chunks replayed as a CUDA graph give the bits of direct launches
+    (per-kernel profiling launches them directly)."""
+    case = _case(gold, name)
+    grid = torch.as_tensor(gold[f"{name}.grid"], device="cuda")
+    dx = float(gold[f"{name}.dx"])
+    graphed = _solve(by, case, grid, dx)
+    native.bssn_profile_reset()
+    native.bssn_profile_enable(1)
+    try:
+        direct = _solve(by, case, grid, dx)
+    finally:
+        torch.cuda.synchronize()
+        native.bssn_profile_enable(0)
+        native.bssn_profile_reset()
+    assert torch.equal(graphed.u.view(torch.int64), direct.u.view(torch.int64))
+    assert graphed.residual_history == direct.residual_history
+    assert graphed.linear_iterations == direct.linear_iterations
