@@ -76,3 +76,7 @@ def test_staging_errors(op):
         op.stage_output_fields({"a": np.zeros((4, 4, 4))}, -1)
     with pytest.raises(ValueError, match="empty axis"):
         op.stage_output_fields({"a": np.zeros((4, 4, 4))}, 2)
+
+
+def test_empty_field_map(op):
+    assert op.stage_output_fields({}, 2) == {}

@@ -238,3 +238,39 @@ def test_graph_replay_equals_direct_launches(by, gold, native, name):
     assert torch.equal(graphed.u.view(torch.int64), direct.u.view(torch.int64))
     assert graphed.residual_history == direct.residual_history
     assert graphed.linear_iterations == direct.linear_iterations
+
+
+def test_smallest_grids(by, gold):
+    """One unknown on the Cartesian (3^3) and the meridional (2 x 1 x 3) grid:
+    the operator kernels' tiles and the fixed cells around a single cell."""
+    masses, positions, momenta = [0.4], [[0.05, -0.02, 0.11]], [[0.1, 0.0, 0.2]]
+    axes = [(np.arange(3) + 0.5) * 0.7 - 1.05] * 3
+    grid = np.stack(np.meshgrid(*axes, indexing="ij"), axis=-1)
+    psi, u, hist = by.solve_conformal_factor(masses, positions, momenta, torch.as_tensor(grid, device="cuda"), 0.7)
+    rpsi, ru, rhist = op.solve_conformal_factor(masses, positions, momenta, grid, 0.7)
+    assert len(hist) == len(rhist)
+    np.testing.assert_allclose(_np(u), ru, rtol=0, atol=1e-12 * max(np.abs(ru).max(), 1e-300))
+    agrid, adx = by.axisymmetric_cell_centered_grid(2, 1.0)
+    assert tuple(agrid.shape) == (2, 1, 4, 3)
+    psi, u, hist = by.solve_axisymmetric_conformal_factor([0.5], [[0.0, 0.0, 0.1]], [[0.0, 0.0, 0.3]], agrid, adx)
+    rpsi, ru, rhist = op.solve_axisymmetric_conformal_factor([0.5], [[0.0, 0.0, 0.1]], [[0.0, 0.0, 0.3]],
+                                                             _np(agrid), adx)
+    assert len(hist) == len(rhist)
+    np.testing.assert_allclose(_np(u), ru, rtol=0, atol=1e-12 * max(np.abs(ru).max(), 1e-300))
+
+
+def test_cartesian_zero_momentum_is_brill_lindquist(by):
+    grid, dx = by.cell_centered_grid(num_points=8, half_width=4.0)
+    psi, u, history = by.solve_conformal_factor([1.0], np.zeros((1, 3)), np.zeros((1, 3)), grid, dx)
+    np.testing.assert_array_equal(_np(u), 0.0)
+    assert history == [0.0]
+
+
+def test_invalid_inputs(by):
+    grid, dx = by.cell_centered_grid(num_points=8, half_width=4.0)
+    with pytest.raises(ValueError, match="punctures"):
+        by.brill_lindquist_conformal_factor(np.ones(17), np.zeros((17, 3)), grid)
+    with pytest.raises(ValueError, match="three cells"):
+        by.solve_conformal_factor([1.0], np.zeros((1, 3)), np.zeros((1, 3)), grid[:2], dx)
+    with pytest.raises(ValueError, match="share one shape"):
+        by.hamiltonian_source(np.ones((3, 3, 3)), np.ones((3, 3, 4)))
