@@ -326,12 +326,14 @@ __device__ __forceinline__ SolveCtrl read_ctrl(const SolveCtrl* c) {
 // free): b = dx^2 F, and the operator's centre coefficient dx^2 dS/du - 6
 // (Cartesian) or dx^2 dS/du - 4 (meridional) is stored per cell, so that one
 // operator application is a neighbour sum and one FMA.  x = 0 comes from a
-// memset; r = rhat = b.
+// memset; r = rhat = b.  Conjugate gradients run on the negated system
+// (-A) x = -b: every iterate is the exact negation of the standard one (x
+// itself is unchanged, bit for bit), and the operator needs no negation.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kPunctThreads)
 k_newton_residual(const double* __restrict__ u, const double* __restrict__ psi_bl, const double* __restrict__ a2,
                   SolveGrid G, double* __restrict__ r, double* __restrict__ rhat, double* __restrict__ centre,
-                  double* __restrict__ partial, SolveCtrl* ctrl, double tol2, int maxiter) {
+                  double* __restrict__ partial, SolveCtrl* ctrl, double tol2, int maxiter, int negate) {
     double acc[4] = {0.0, 0.0, 0.0, 0.0};   // F.F, nonpositive psi, nonfinite u, b.b
     const long long plane = (long long)G.n[1] * G.n[2];
     const double diag = G.axi ? 4.0 : 6.0;
@@ -345,6 +347,7 @@ k_newton_residual(const double* __restrict__ u, const double* __restrict__ psi_b
             const double psi = __dadd_rn(psi_bl[t], u[t]);
             res = __dadd_rn(laplacian_exact(G, i, j, k, f), source_of(psi, a2[t]));
             b = G.dx2 * res;
+            if (negate) b = -b;
             c = fma(G.dx2, lin_coefficient(psi, a2[t]), -diag);
             acc[0] += res * res;
             if (!(psi > 0.0)) acc[1] += 1.0;
@@ -388,9 +391,9 @@ __global__ void k_psi_total(const double* __restrict__ psi_bl, const double* __r
 
 // ---------------------------------------------------------------------------
 // Conjugate gradients on A = -dx^2 (Lap + dS) (Cartesian).  One iteration:
-//   k_cg_apply   p = r + beta p_prev (p = r at the first), Ap, p.Ap
-//                -> alpha = gamma / p.Ap
-//   k_cg_update  x += alpha p, r -= alpha Ap, r.r -> beta, gamma, k, done
+//   k_cg_apply   p = r + beta p_prev (p = r at the first), Bp, p.Bp with
+//                B = -A = dx^2 (Lap + dS)  -> alpha = gamma / p.Bp
+//   k_cg_update  x += alpha p, r -= alpha Bp, r.r -> beta, gamma, k, done
 // The apply kernel stages p of one x plane of a 32 x 8 (z, y) tile in shared
 // memory, with its one-cell halo, and marches along x carrying the x
 // neighbours in registers, so each p value is formed once per tile (plus the
@@ -467,7 +470,7 @@ k_cg_apply(const double* __restrict__ r, const double* __restrict__ pin, double*
                 s += tile[buf][ty][tz + 1];
                 s += tile[buf][ty + 1][tz + 2];
                 s += tile[buf][ty + 1][tz];
-                const double a = -fma(cc, pc, s);
+                const double a = fma(cc, pc, s);
                 pout[o] = pc;
                 ap[o] = a;
                 dot[0] = fma(pc, a, dot[0]);
@@ -936,7 +939,8 @@ int bssn_puncture_solve(const double* psi_bl, const double* curvature_squared, c
     int count = 0;
     for (int it = 0; it <= max_newton_iterations; ++it) {
         BSSN_LAUNCH(KC_SOLVE_NEWTON, k_newton_residual, ub, kPunctThreads, s, u, psi_bl, curvature_squared, G, v[V_R],
-                    G.axi ? v[V_RHAT] : nullptr, v[V_CENTRE], partial, ctrl, tol2, max_linear_iterations);
+                    G.axi ? v[V_RHAT] : nullptr, v[V_CENTRE], partial, ctrl, tol2, max_linear_iterations,
+                    G.axi ? 0 : 1);
         e = cudaGetLastError();
         if (e == cudaSuccess) e = cudaMemcpyAsync(&host, ctrl, sizeof(SolveCtrl), cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
