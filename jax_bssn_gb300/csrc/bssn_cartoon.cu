@@ -121,29 +121,59 @@ struct AxiGeom {
 constexpr int kAxiThreads = 128;
 constexpr int kAxiPairs = kCenter + 1;   // planes (j, 8 - j) for j = 0..3, and the centre plane
 
+// Node window, six weights and rotation of one (x, plane pair) column.  They
+// depend on the geometry only, so a stepping driver computes the table once
+// and every reconstruction of the step reads it (the alternative, thread 0 of
+// every block computing its column's chain of FP64 divisions while the block
+// waits, dominates the float reconstruction).
+struct AxiCol {
+    double w[6];
+    double cs, sn;
+    int start, valid;
+};
+
+__device__ __forceinline__ void axi_column(int x, int j, const Compact& C, const AxiGeom& A, AxiCol& out) {
+    const double X = RN_MUL((double)x - 3.5, A.dx);
+    const double Y = RN_MUL((double)j - 4.0, A.dx);
+    const double rho = __dsqrt_rn(RN_ADD(RN_MUL(X, X), RN_MUL(Y, Y)));
+    const double q = RN_ADD(RN_ADD(RN_DIV(rho, A.dx), 4.0), -0.5);
+    int start;
+    double w[6];
+    out.valid = lagrange_nodes(q, C.nx + 3, start, w) ? 1 : 0;
+    out.start = start;
+    for (int k = 0; k < 6; ++k) out.w[k] = w[k];
+    // rotation by phi about z: L = [[c,-s,0],[s,c,0],[0,0,1]]
+    out.cs = rho <= 0.0 ? 1.0 : RN_DIV(X, rho);
+    out.sn = rho <= 0.0 ? 0.0 : RN_DIV(Y, rho);
+}
+
+__global__ void k_axi_columns(Compact C, AxiGeom A, AxiCol* __restrict__ T) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= C.nx * kAxiPairs) return;
+    axi_column(t / kAxiPairs, t - (t / kAxiPairs) * kAxiPairs, C, A, T[t]);
+}
+
 // With w_only set (the FP32 form, whose support is reconstructed in float),
-// the off-centre plane pairs receive W alone.
+// the off-centre plane pairs receive W alone.  T: the column table, or null
+// (each block then computes its column).
 __global__ void __launch_bounds__(kAxiThreads) k_axi_reconstruct(const double* __restrict__ u, Compact C, AxiGeom A,
                                                                  double* __restrict__ dst, long long dcs, long long sx,
-                                                                 long long sy, int ox, int oy, int oz, int w_only) {
+                                                                 long long sy, int ox, int oy, int oz, int w_only,
+                                                                 const AxiCol* __restrict__ T) {
     __shared__ double s_w[6];
     __shared__ double s_cs, s_sn;
     __shared__ int s_start, s_valid;
     const int col = blockIdx.x;            // x * kAxiPairs + j
     const int x = col / kAxiPairs, j = col - (col / kAxiPairs) * kAxiPairs;
     if (threadIdx.x == 0) {
-        const double X = RN_MUL((double)x - 3.5, A.dx);
-        const double Y = RN_MUL((double)j - 4.0, A.dx);
-        const double rho = __dsqrt_rn(RN_ADD(RN_MUL(X, X), RN_MUL(Y, Y)));
-        const double q = RN_ADD(RN_ADD(RN_DIV(rho, A.dx), 4.0), -0.5);
-        int start;
-        double w[6];
-        s_valid = lagrange_nodes(q, C.nx + 3, start, w) ? 1 : 0;
-        s_start = start;
-        for (int k = 0; k < 6; ++k) s_w[k] = w[k];
-        // rotation by phi about z: L = [[c,-s,0],[s,c,0],[0,0,1]]
-        s_cs = rho <= 0.0 ? 1.0 : RN_DIV(X, rho);
-        s_sn = rho <= 0.0 ? 0.0 : RN_DIV(Y, rho);
+        AxiCol K;
+        if (T) K = T[col];
+        else axi_column(x, j, C, A, K);
+        s_valid = K.valid;
+        s_start = K.start;
+        for (int k = 0; k < 6; ++k) s_w[k] = K.w[k];
+        s_cs = K.cs;
+        s_sn = K.sn;
     }
     __syncthreads();
     const int z = blockIdx.y * kAxiThreads + threadIdx.x;
@@ -264,27 +294,30 @@ __global__ void k_compact_f32(const double* __restrict__ u, Compact C, float* __
 
 __global__ void __launch_bounds__(kAxiThreads)
 k_axi_reconstruct_f32(const float* __restrict__ cf, const double* __restrict__ u, Compact C, AxiGeom A,
-                      float* __restrict__ dst, long long dcs, long long sx, long long sy, int ox, int oy, int oz) {
+                      float* __restrict__ dst, long long dcs, long long sx, long long sy, int ox, int oy, int oz,
+                      const AxiCol* __restrict__ T) {
     __shared__ float s_w[6];
     __shared__ float s_cs, s_sn;
     __shared__ int s_start, s_valid;
-    __shared__ float s_b[NCOMP];
+    __shared__ float s_b[NCOMP], s_par[NCOMP], s_asym[NCOMP];
     const int col = blockIdx.x;
     const int x = col / kAxiPairs, j = col - (col / kAxiPairs) * kAxiPairs;
     if (threadIdx.x == 0) {
-        const double X = RN_MUL((double)x - 3.5, A.dx);
-        const double Y = RN_MUL((double)j - 4.0, A.dx);
-        const double rho = __dsqrt_rn(RN_ADD(RN_MUL(X, X), RN_MUL(Y, Y)));
-        const double q = RN_ADD(RN_ADD(RN_DIV(rho, A.dx), 4.0), -0.5);
-        int start;
-        double w[6];
-        s_valid = lagrange_nodes(q, C.nx + 3, start, w) ? 1 : 0;
-        s_start = start;
-        for (int k = 0; k < 6; ++k) s_w[k] = static_cast<float>(w[k]);
-        s_cs = static_cast<float>(rho <= 0.0 ? 1.0 : RN_DIV(X, rho));
-        s_sn = static_cast<float>(rho <= 0.0 ? 0.0 : RN_DIV(Y, rho));
+        AxiCol K;
+        if (T) K = T[col];
+        else axi_column(x, j, C, A, K);
+        s_valid = K.valid;
+        s_start = K.start;
+        for (int k = 0; k < 6; ++k) s_w[k] = static_cast<float>(K.w[k]);
+        s_cs = static_cast<float>(K.cs);
+        s_sn = static_cast<float>(K.sn);
     }
-    if (threadIdx.x < NCOMP) s_b[threadIdx.x] = static_cast<float>(axi_background(u, C, threadIdx.x));
+    if (threadIdx.x < NCOMP) {
+        const double par3[3] = {-1.0, -1.0, 1.0};
+        s_b[threadIdx.x] = static_cast<float>(axi_background(u, C, threadIdx.x));
+        s_par[threadIdx.x] = static_cast<float>(comp_parity(threadIdx.x, par3));
+        s_asym[threadIdx.x] = static_cast<float>(comp_asymptote(threadIdx.x));
+    }
     __syncthreads();
     const int z = blockIdx.y * kAxiThreads + threadIdx.x;
     if (z >= C.nz) return;
@@ -305,15 +338,14 @@ k_axi_reconstruct_f32(const float* __restrict__ cf, const double* __restrict__ u
             ratio[b] = static_cast<float>(RN_DIV(r_edge, __dsqrt_rn(RN_ADD(RN_MUL(rho_b, rho_b), zz))));
         }
     }
-    const double par3[3] = {-1.0, -1.0, 1.0};
     const float nan = __int_as_float(0x7fc00000);
     float val[NCOMP];
 #pragma unroll
     for (int c = 0; c < NCOMP; ++c) {
         const float* f = cf + (long long)c * C.cs;
-        const float par = static_cast<float>(comp_parity(c, par3));
+        const float par = s_par[c];
         const float b = s_b[c];
-        const float asym = static_cast<float>(comp_asymptote(c));
+        const float asym = s_asym[c];
         float acc = 0.f;
 #pragma unroll
         for (int k = 0; k < 6; ++k) {
@@ -601,8 +633,14 @@ int cartoon_plan(bool axi, const int32_t shape[3], const BssnParams* p, CartoonP
 }
 
 // support state + support RHS + RHS work + compact stage, RHS, accumulator
+// doubles of the axisymmetric column table
+size_t axi_table_values(const CartoonPlan& P) {
+    return P.axi ? ((size_t)P.C.nx * kAxiPairs * sizeof(AxiCol) + sizeof(double) - 1) / sizeof(double) : 0;
+}
+
 size_t cartoon_step_values(const CartoonPlan& P) {
-    return (size_t)(2 * NCOMP + rhs_work_blocks(P.with_mom)) * (size_t)P.scs + 3 * NCOMP * (size_t)P.C.cs;
+    return (size_t)(2 * NCOMP + rhs_work_blocks(P.with_mom)) * (size_t)P.scs + 3 * NCOMP * (size_t)P.C.cs +
+           axi_table_values(P);
 }
 
 // support state + first derivatives + derived blocks + nine constraint blocks of the centre box
@@ -615,12 +653,13 @@ size_t cartoon_work_values(const CartoonPlan& P) {
     return a > b ? a : b;
 }
 
-cudaError_t reconstruct(const CartoonPlan& P, const BssnParams* p, const double* u, double* us, cudaStream_t s) {
+cudaError_t reconstruct(const CartoonPlan& P, const BssnParams* p, const double* u, double* us, cudaStream_t s,
+                        const AxiCol* T = nullptr) {
     const long long sx = P.Gs.st[0], sy = P.Gs.st[1];
     if (P.axi) {
         const AxiGeom A{p->dx, p->xmin[2]};
         const dim3 grid((unsigned)(P.C.nx * kAxiPairs), (unsigned)((P.C.nz + kAxiThreads - 1) / kAxiThreads));
-        BSSN_LAUNCH(KC_CARTOON, k_axi_reconstruct, grid, kAxiThreads, s, u, P.C, A, us, P.scs, sx, sy, 4, 4, 4, 0);
+        BSSN_LAUNCH(KC_CARTOON, k_axi_reconstruct, grid, kAxiThreads, s, u, P.C, A, us, P.scs, sx, sy, 4, 4, 4, 0, T);
     } else {
         const long long n = (long long)P.C.nx * kSup * kSup;
         BSSN_LAUNCH(KC_CARTOON, k_sph_reconstruct, blocks(n), kThr, s, u, P.C.nx, p->dx, us, P.scs, sx, sy, 4, 4, 4);
@@ -632,31 +671,32 @@ cudaError_t reconstruct(const CartoonPlan& P, const BssnParams* p, const double*
 // float support from float perturbations of the compact state (staged in the
 // first-derivative scratch, which the RHS overwrites afterwards).
 cudaError_t reconstruct_f32(const CartoonPlan& P, const BssnParams* p, const double* u, double* us, const RhsWork& w,
-                            cudaStream_t s) {
+                            cudaStream_t s, const AxiCol* T) {
     const long long sx = P.Gs.st[0], sy = P.Gs.st[1];
     const AxiGeom A{p->dx, p->xmin[2]};
     const dim3 grid((unsigned)(P.C.nx * kAxiPairs), (unsigned)((P.C.nz + kAxiThreads - 1) / kAxiThreads));
-    BSSN_LAUNCH(KC_CARTOON, k_axi_reconstruct, grid, kAxiThreads, s, u, P.C, A, us, P.scs, sx, sy, 4, 4, 4, 1);
+    BSSN_LAUNCH(KC_CARTOON, k_axi_reconstruct, grid, kAxiThreads, s, u, P.C, A, us, P.scs, sx, sy, 4, 4, 4, 1, T);
     // FP64 values outside the centre box are read for W only
     cudaError_t e = launch_fill_periodic(us + (long long)CW * P.scs, 1, P.Gs, s);
     if (e != cudaSuccess) return e;
     float* cf = w.d1f;
     BSSN_LAUNCH(KC_CONVERT, k_compact_f32, blocks(P.C.cs * NCOMP), kThr, s, u, P.C, cf);
-    BSSN_LAUNCH(KC_CARTOON, k_axi_reconstruct_f32, grid, kAxiThreads, s, cf, u, P.C, A, w.uf, P.scs, sx, sy, 4, 4, 4);
+    BSSN_LAUNCH(KC_CARTOON, k_axi_reconstruct_f32, grid, kAxiThreads, s, cf, u, P.C, A, w.uf, P.scs, sx, sy, 4, 4, 4,
+                T);
     return launch_fill_periodic(w.uf, NCOMP, P.Gs, s);
 }
 
 cudaError_t compact_rhs(const CartoonPlan& P, const BssnParams* p, const double* u, double* kc, double* base,
-                        cudaStream_t s) {
+                        cudaStream_t s, const AxiCol* T = nullptr) {
     double* us = base;
     double* ks = us + NCOMP * P.scs;
     const RhsWork w = carve_rhs_work(ks + NCOMP * P.scs, P.scs, P.with_mom);
     cudaError_t e;
     if (P.axi && P.Gs.precision == kPrecisionF32) {
-        e = reconstruct_f32(P, p, u, us, w, s);
+        e = reconstruct_f32(P, p, u, us, w, s, T);
         if (e == cudaSuccess) e = launch_rhs_f32_prepared(us, ks, w, P.Gs, P.centre, s);
     } else {
-        e = reconstruct(P, p, u, us, s);
+        e = reconstruct(P, p, u, us, s, T);
         if (e == cudaSuccess) e = launch_rhs(us, ks, w, P.Gs, P.centre, s);
     }
     if (e == cudaSuccess) {
@@ -693,10 +733,17 @@ cudaError_t cartoon_step(const CartoonPlan& P, const BssnParams* p, double* u, d
     double* us = comp;
     double* kc = us + NCOMP * P.C.cs;
     double* acc = kc + NCOMP * P.C.cs;
+    AxiCol* T = nullptr;
+    if (P.axi) {
+        // the geometry of every (x, plane pair) column, once for the four stages
+        T = reinterpret_cast<AxiCol*>(acc + NCOMP * P.C.cs);
+        const AxiGeom A{p->dx, p->xmin[2]};
+        BSSN_LAUNCH(KC_CARTOON, k_axi_columns, blocks((long long)P.C.nx * kAxiPairs), kThr, s, P.C, A, T);
+    }
     cudaError_t e = prepare_compact(P, u, s);
     for (int stage = 1; stage <= 4 && e == cudaSuccess; ++stage) {
         const double* src = stage == 1 ? u : us;
-        e = compact_rhs(P, p, src, kc, base, s);
+        e = compact_rhs(P, p, src, kc, base, s, T);
         double* out = stage == 4 ? u : us;
         if (e == cudaSuccess)
             e = launch_rk4_stage(u, kc, acc, out, P.Gc, P.positive, stage, p->dt, 0, /*project=*/0, s);
@@ -745,7 +792,7 @@ int bssn_cartoon_reconstruct(int32_t axisymmetric, const double* compact, double
         const long long dcs = (long long)P.C.nx * kSup * P.C.nz;
         const dim3 grid((unsigned)(P.C.nx * kAxiPairs), (unsigned)((P.C.nz + kAxiThreads - 1) / kAxiThreads));
         BSSN_LAUNCH(KC_CARTOON, k_axi_reconstruct, grid, kAxiThreads, s, compact, P.C, A, support, dcs,
-                    (long long)kSup * P.C.nz, (long long)P.C.nz, 0, 0, 0, 0);
+                    (long long)kSup * P.C.nz, (long long)P.C.nz, 0, 0, 0, 0, nullptr);
     } else {
         const long long n = (long long)P.C.nx * kSup * kSup;
         BSSN_LAUNCH(KC_CARTOON, k_sph_reconstruct, blocks(n), kThr, s, compact, P.C.nx, params->dx, support, n,
