@@ -154,8 +154,9 @@ __global__ void k_axi_columns(Compact C, AxiGeom A, AxiCol* __restrict__ T) {
 }
 
 // With w_only set (the FP32 form, whose support is reconstructed in float),
-// the off-centre plane pairs receive W alone.  T: the column table, or null
-// (each block then computes its column).
+// only W is written, on the off-centre plane pairs (the centre plane comes
+// from k_copy_centre).  T: the column table, or null (each block then
+// computes its column).
 __global__ void __launch_bounds__(kAxiThreads) k_axi_reconstruct(const double* __restrict__ u, Compact C, AxiGeom A,
                                                                  double* __restrict__ dst, long long dcs, long long sx,
                                                                  long long sy, int ox, int oy, int oz, int w_only,
@@ -165,6 +166,7 @@ __global__ void __launch_bounds__(kAxiThreads) k_axi_reconstruct(const double* _
     __shared__ int s_start, s_valid;
     const int col = blockIdx.x;            // x * kAxiPairs + j
     const int x = col / kAxiPairs, j = col - (col / kAxiPairs) * kAxiPairs;
+    if (w_only && j == kCenter) return;    // block-uniform
     if (threadIdx.x == 0) {
         AxiCol K;
         if (T) K = T[col];
@@ -198,7 +200,7 @@ __global__ void __launch_bounds__(kAxiThreads) k_axi_reconstruct(const double* _
     }
     const double par3[3] = {-1.0, -1.0, 1.0};
     const double nan = __longlong_as_double(0x7ff8000000000000LL);
-    const bool only_w = w_only && j != kCenter;
+    const bool only_w = w_only != 0;
     // six-node sum of every component (reflected plane, then the buffer)
     double val[NCOMP];
 #pragma unroll
@@ -283,6 +285,21 @@ __device__ __forceinline__ double axi_background(const double* __restrict__ u, c
     if (comp_asymptote(c) != 0.0) return 1.0;
     if (c == BX || c == BY || c == BZ || c == CK) return u[(long long)c * C.cs + (long long)kCG * C.nz];
     return 0.0;
+}
+
+// The support's centre plane is the compact state itself: there every column
+// sits on a node (weights 0, 0, 1, 0, 0, 0) and the rotation is the identity
+// (x >= 4) or by pi (the ghost columns, which hold exactly the parity images
+// it produces), so for finite values the reconstruction returns the compact
+// samples bit for bit.
+__global__ void k_copy_centre(const double* __restrict__ u, Compact C, double* __restrict__ dst, long long dcs,
+                              long long sx, long long sy, int ox, int oy, int oz) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= C.cs * NCOMP) return;
+    const int c = (int)(t / C.cs);
+    const long long r = t - (long long)c * C.cs;
+    const int x = (int)(r / C.nz), z = (int)(r - (long long)x * C.nz);
+    dst[(long long)c * dcs + (long long)(ox + x) * sx + (long long)(oy + kCenter) * sy + (oz + z)] = u[t];
 }
 
 __global__ void k_compact_f32(const double* __restrict__ u, Compact C, float* __restrict__ cf) {
@@ -675,6 +692,7 @@ cudaError_t reconstruct_f32(const CartoonPlan& P, const BssnParams* p, const dou
     const long long sx = P.Gs.st[0], sy = P.Gs.st[1];
     const AxiGeom A{p->dx, p->xmin[2]};
     const dim3 grid((unsigned)(P.C.nx * kAxiPairs), (unsigned)((P.C.nz + kAxiThreads - 1) / kAxiThreads));
+    BSSN_LAUNCH(KC_CARTOON, k_copy_centre, blocks(P.C.cs * NCOMP), kThr, s, u, P.C, us, P.scs, sx, sy, 4, 4, 4);
     BSSN_LAUNCH(KC_CARTOON, k_axi_reconstruct, grid, kAxiThreads, s, u, P.C, A, us, P.scs, sx, sy, 4, 4, 4, 1, T);
     // FP64 values outside the centre box are read for W only
     cudaError_t e = launch_fill_periodic(us + (long long)CW * P.scs, 1, P.Gs, s);
