@@ -153,20 +153,21 @@ __global__ void k_axi_columns(Compact C, AxiGeom A, AxiCol* __restrict__ T) {
     axi_column(t / kAxiPairs, t - (t / kAxiPairs) * kAxiPairs, C, A, T[t]);
 }
 
-// With w_only set (the FP32 form, whose support is reconstructed in float),
-// only W is written, on the off-centre plane pairs (the centre plane comes
-// from k_copy_centre).  T: the column table, or null (each block then
+// mode 0: every plane.  mode 1 (the FP32 form, whose support is
+// reconstructed in float): W alone, on the off-centre plane pairs.  mode 2:
+// every component on the off-centre pairs.  In modes 1 and 2 the centre plane
+// comes from k_copy_centre.  T: the column table, or null (each block then
 // computes its column).
 __global__ void __launch_bounds__(kAxiThreads) k_axi_reconstruct(const double* __restrict__ u, Compact C, AxiGeom A,
                                                                  double* __restrict__ dst, long long dcs, long long sx,
-                                                                 long long sy, int ox, int oy, int oz, int w_only,
+                                                                 long long sy, int ox, int oy, int oz, int mode,
                                                                  const AxiCol* __restrict__ T) {
     __shared__ double s_w[6];
     __shared__ double s_cs, s_sn;
     __shared__ int s_start, s_valid;
     const int col = blockIdx.x;            // x * kAxiPairs + j
     const int x = col / kAxiPairs, j = col - (col / kAxiPairs) * kAxiPairs;
-    if (w_only && j == kCenter) return;    // block-uniform
+    if (mode != 0 && j == kCenter) return;    // block-uniform
     if (threadIdx.x == 0) {
         AxiCol K;
         if (T) K = T[col];
@@ -200,7 +201,7 @@ __global__ void __launch_bounds__(kAxiThreads) k_axi_reconstruct(const double* _
     }
     const double par3[3] = {-1.0, -1.0, 1.0};
     const double nan = __longlong_as_double(0x7ff8000000000000LL);
-    const bool only_w = w_only != 0;
+    const bool only_w = mode == 1;
     // six-node sum of every component (reflected plane, then the buffer)
     double val[NCOMP];
 #pragma unroll
@@ -676,7 +677,17 @@ cudaError_t reconstruct(const CartoonPlan& P, const BssnParams* p, const double*
     if (P.axi) {
         const AxiGeom A{p->dx, p->xmin[2]};
         const dim3 grid((unsigned)(P.C.nx * kAxiPairs), (unsigned)((P.C.nz + kAxiThreads - 1) / kAxiThreads));
-        BSSN_LAUNCH(KC_CARTOON, k_axi_reconstruct, grid, kAxiThreads, s, u, P.C, A, us, P.scs, sx, sy, 4, 4, 4, 0, T);
+        if (T) {
+            // the stepping driver: centre plane copied (bit-identical for finite
+            // values, up to the sign of zeros), the plane pairs reconstructed
+            BSSN_LAUNCH(KC_CARTOON, k_copy_centre, blocks(P.C.cs * NCOMP), kThr, s, u, P.C, us, P.scs, sx, sy, 4, 4,
+                        4);
+            BSSN_LAUNCH(KC_CARTOON, k_axi_reconstruct, grid, kAxiThreads, s, u, P.C, A, us, P.scs, sx, sy, 4, 4, 4, 2,
+                        T);
+        } else {
+            BSSN_LAUNCH(KC_CARTOON, k_axi_reconstruct, grid, kAxiThreads, s, u, P.C, A, us, P.scs, sx, sy, 4, 4, 4, 0,
+                        T);
+        }
     } else {
         const long long n = (long long)P.C.nx * kSup * kSup;
         BSSN_LAUNCH(KC_CARTOON, k_sph_reconstruct, blocks(n), kThr, s, u, P.C.nx, p->dx, us, P.scs, sx, sy, 4, 4, 4);
