@@ -408,6 +408,9 @@ class PunctureAxi(Puncture):
 
 
 PUNCTURES = {w.name: w for w in (Puncture, PunctureAxi)}
+# Executed FP64 flops per unknown of one CG operator launch (DADD + 2 DFMA, from an
+# ncu op count of the 128^3 solve: 5.5 DADD, 3.5 DFMA)
+CG_APPLY_FLOPS = 12.5
 PUNCTURE_CPU_N = {"puncture": 48, "puncture_axi": 64}
 
 
@@ -505,6 +508,13 @@ def run_puncture(args, world, rank, local):
                 "kernel_share": kms / total, "kernel_ms_per_launch": kms / max(klaunch, 1),
                 "algorithmic_bytes_per_unknown_iteration": per,
                 "note": "launches after convergence inside a chunk return at once and are included in the time"}
+    compute = None
+    if not wl.axisymmetric and kms > 0:
+        peak = _native.fma_peak_gflops(_native.PRECISION_F64) / 1e3
+        achieved = CG_APPLY_FLOPS * unknowns * its / (kms / 1e3) / 1e12
+        compute = {"bound": "fp64", "kernel": "k_cg_apply", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                   "frac": achieved / peak, "flops_per_unknown": CG_APPLY_FLOPS,
+                   "peak_source": "measured live by bssn_probe_fma_peak"}
     e2e = None
     if not args.no_e2e:
         host_grid = grid.cpu().pin_memory()
@@ -543,8 +553,8 @@ def run_puncture(args, world, rank, local):
         "config": {**wl.config(), "step": "one complete Newton-Krylov solve",
                    "newton_steps": len(r.residual_history), "krylov_iterations": r.linear_iterations,
                    "final_residual": r.residual_history[-1]},
-        "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clock_info,
-        "kernels": kernels,
+        "roofline": roofline, "roofline_compute": compute, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+        "clocks": clock_info, "kernels": kernels,
     }
 
 
