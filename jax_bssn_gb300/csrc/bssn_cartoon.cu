@@ -310,14 +310,60 @@ __global__ void k_compact_f32(const double* __restrict__ u, Compact C, float* __
     cf[t] = static_cast<float>(u[t] - axi_background(u, C, c));
 }
 
+// Float-float accumulation of products: s + c carries a sum of products v w
+// (w given as a float pair hi + lo) to about 2^-46 of its size, so the
+// interpolation and rotation round once, at the final float, like the FP64
+// path's final conversion.
+struct FF {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add_prod(float v, float whi, float wlo) {
+        // _rn intrinsics: no contraction may merge the product into the sums
+        const float p = __fmul_rn(v, whi);
+        const float pe = fmaf(v, whi, -p);   // exact error of the product
+        const float t = __fadd_rn(s, p);
+        const float z = __fsub_rn(t, s);
+        const float te = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z));   // TwoSum error
+        c += te + pe + v * wlo;
+        s = t;
+    }
+    __device__ __forceinline__ float value() const { return s + c; }
+};
+
+// The rotation coefficients L_ia L_jb (tensors) and L_ia (vectors) of one
+// plane, as float pairs: index q over the tensor terms that are not literal
+// zeros (xx 4, xy 4, xz 2, yy 4, yz 2, zz 1), then the four vector entries.
+constexpr int kRotTensorTerms = 17;
+constexpr int kRotTerms = kRotTensorTerms + 4;
+
+__device__ void rotation_pairs(double cs, double sn, float* hi, float* lo) {
+    const double L[3][3] = {{cs, -sn, 0.0}, {sn, cs, 0.0}, {0.0, 0.0, 1.0}};
+    int q = 0;
+    for (int i = 0; i < 3; ++i)
+        for (int jj = i; jj < 3; ++jj)
+            for (int ab = 0; ab < 9; ++ab) {
+                const int a2 = ab / 3, b2 = ab % 3;
+                if ((i == 2) != (a2 == 2) || (jj == 2) != (b2 == 2)) continue;
+                const double v = L[i][a2] * L[jj][b2];
+                hi[q] = static_cast<float>(v);
+                lo[q] = static_cast<float>(v - (double)hi[q]);
+                ++q;
+            }
+    const double vec[4] = {L[0][0], L[0][1], L[1][0], L[1][1]};
+    for (int k = 0; k < 4; ++k, ++q) {
+        hi[q] = static_cast<float>(vec[k]);
+        lo[q] = static_cast<float>(vec[k] - (double)hi[q]);
+    }
+}
+
 __global__ void __launch_bounds__(kAxiThreads)
 k_axi_reconstruct_f32(const float* __restrict__ cf, const double* __restrict__ u, Compact C, AxiGeom A,
                       float* __restrict__ dst, long long dcs, long long sx, long long sy, int ox, int oy, int oz,
                       const AxiCol* __restrict__ T) {
-    __shared__ float s_w[6];
+    __shared__ float s_w[6], s_wlo[6];
     __shared__ float s_cs, s_sn;
     __shared__ int s_start, s_valid;
     __shared__ float s_b[NCOMP], s_par[NCOMP], s_asym[NCOMP];
+    __shared__ float s_rhi[2][kRotTerms], s_rlo[2][kRotTerms];   // plane j, mirrored plane
     const int col = blockIdx.x;
     const int x = col / kAxiPairs, j = col - (col / kAxiPairs) * kAxiPairs;
     if (threadIdx.x == 0) {
@@ -326,9 +372,14 @@ k_axi_reconstruct_f32(const float* __restrict__ cf, const double* __restrict__ u
         else axi_column(x, j, C, A, K);
         s_valid = K.valid;
         s_start = K.start;
-        for (int k = 0; k < 6; ++k) s_w[k] = static_cast<float>(K.w[k]);
+        for (int k = 0; k < 6; ++k) {
+            s_w[k] = static_cast<float>(K.w[k]);
+            s_wlo[k] = static_cast<float>(K.w[k] - (double)s_w[k]);
+        }
         s_cs = static_cast<float>(K.cs);
         s_sn = static_cast<float>(K.sn);
+        rotation_pairs(K.cs, K.sn, s_rhi[0], s_rlo[0]);
+        rotation_pairs(K.cs, -K.sn, s_rhi[1], s_rlo[1]);
     }
     if (threadIdx.x < NCOMP) {
         const double par3[3] = {-1.0, -1.0, 1.0};
@@ -341,9 +392,12 @@ k_axi_reconstruct_f32(const float* __restrict__ cf, const double* __restrict__ u
     if (z >= C.nz) return;
     const int start = s_start;
     const bool valid = s_valid != 0;
-    float w[6];
+    float w[6], wlo[6];
 #pragma unroll
-    for (int k = 0; k < 6; ++k) w[k] = s_w[k];
+    for (int k = 0; k < 6; ++k) {
+        w[k] = s_w[k];
+        wlo[k] = s_wlo[k];
+    }
     float ratio[3] = {0.f, 0.f, 0.f};
     if (start + 5 >= C.nx) {
         const double rho_edge = RN_MUL((double)(C.nx - kCG) - 0.5, A.dx);
@@ -364,7 +418,7 @@ k_axi_reconstruct_f32(const float* __restrict__ cf, const double* __restrict__ u
         const float par = s_par[c];
         const float b = s_b[c];
         const float asym = s_asym[c];
-        float acc = 0.f;
+        FF acc;
 #pragma unroll
         for (int k = 0; k < 6; ++k) {
             const int src = start + k;
@@ -377,47 +431,60 @@ k_axi_reconstruct_f32(const float* __restrict__ cf, const double* __restrict__ u
                 const float r = ratio[src - C.nx];
                 v = fmaf(f[(long long)(C.nx - 1) * C.nz + z], r, (asym - b) * (1.f - r));
             }
-            acc = fmaf(v, w[k], acc);
+            acc.add_prod(v, w[k], wlo[k]);
         }
-        val[c] = valid ? acc : nan;
+        val[c] = valid ? acc.value() : nan;
     }
-    auto rotate_write = [&](int plane, float sn) {
-        const float cs = s_cs;
-        const float L[3][3] = {{cs, -sn, 0.f}, {sn, cs, 0.f}, {0.f, 0.f, 1.f}};
+    auto rotate_write = [&](int plane, int mirror) {
+        const float* rh = s_rhi[mirror];
+        const float* rl = s_rlo[mirror];
+        const float cs = s_cs, sn = mirror ? -s_sn : s_sn;
         const long long d = (long long)(ox + x) * sx + (long long)(oy + plane) * sy + (oz + z);
         dst[(long long)CW * dcs + d] = val[CW];
         dst[(long long)CK * dcs + d] = val[CK];
         dst[(long long)CALPHA * dcs + d] = val[CALPHA];
-        // connection functions: background 0
-        dst[(long long)GTX * dcs + d] = L[0][0] * val[GTX] + L[0][1] * val[GTY];
-        dst[(long long)GTY * dcs + d] = L[1][0] * val[GTX] + L[1][1] * val[GTY];
-        dst[(long long)GTZ * dcs + d] = val[GTZ];
-        // shift: R (b + d) - b = R d + (R b - b)
-        const float bx = s_b[BX], by = s_b[BY];
-        dst[(long long)BX * dcs + d] = L[0][0] * val[BX] + L[0][1] * val[BY] + ((cs - 1.f) * bx - sn * by);
-        dst[(long long)BY * dcs + d] = L[1][0] * val[BX] + L[1][1] * val[BY] + (sn * bx + (cs - 1.f) * by);
-        dst[(long long)BZ * dcs + d] = val[BZ];
+        // vectors: rows (L_00, L_01), (L_10, L_11) are terms 17-20
+#pragma unroll
+        for (int base = 0; base < 2; ++base) {
+            const int off = base == 0 ? GTX : BX;
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                FF a;
+                a.add_prod(val[off], rh[kRotTensorTerms + 2 * i], rl[kRotTensorTerms + 2 * i]);
+                a.add_prod(val[off + 1], rh[kRotTensorTerms + 2 * i + 1], rl[kRotTensorTerms + 2 * i + 1]);
+                float v = a.value();
+                // shift: R (b + d) - b = R d + (R b - b)
+                if (base == 1) {
+                    const float bx = s_b[BX], by = s_b[BY];
+                    v += i == 0 ? (cs - 1.f) * bx - sn * by : sn * bx + (cs - 1.f) * by;
+                }
+                dst[(long long)(off + i) * dcs + d] = v;
+            }
+            dst[(long long)(off + 2) * dcs + d] = val[off + 2];
+        }
         // metric (background I, preserved) and At (background 0): R T R^T
 #pragma unroll
         for (int base = 0; base < 2; ++base) {
             const int off = base == 0 ? GXX : AXX;
+            int q = 0;
 #pragma unroll
             for (int i = 0; i < 3; ++i)
 #pragma unroll
                 for (int jj = i; jj < 3; ++jj) {
-                    float acc = 0.f;
+                    FF a;
 #pragma unroll
                     for (int ab = 0; ab < 9; ++ab) {
                         const int a2 = ab / 3, b2 = ab % 3;
                         if ((i == 2) != (a2 == 2) || (jj == 2) != (b2 == 2)) continue;   // literal zero of L
-                        acc = fmaf(L[i][a2] * L[jj][b2], val[off + sym(a2, b2)], acc);
+                        a.add_prod(val[off + sym(a2, b2)], rh[q], rl[q]);
+                        ++q;
                     }
-                    dst[(long long)(off + sym(i, jj)) * dcs + d] = acc;
+                    dst[(long long)(off + sym(i, jj)) * dcs + d] = a.value();
                 }
         }
     };
-    rotate_write(j, s_sn);
-    if (j != kCenter) rotate_write(kSup - 1 - j, -s_sn);
+    rotate_write(j, 0);
+    if (j != kCenter) rotate_write(kSup - 1 - j, 1);
 }
 
 // ---------------------------------------------------------------------------
