@@ -174,3 +174,60 @@ def test_device_cube_root_is_correctly_rounded(gb):
                               np.zeros((3, n, 1, 1)))
     got = np.asarray(te.enforce_algebraic_constraints(state).conformal_metric)[1, 1, :, 0, 0]
     np.testing.assert_array_equal(got, exact_pow_minus_third(x))
+
+
+def _gauge_wave_errors(n, steps_per_unit=1, final_time=1.0, precision="fp64"):
+    """RMS errors of gt_xx, gt_yy, gt_zz and W against the exact gauge wave at
+    t = final_time, dt = dx, nu = 0 (tests/test_gauge_wave.py:67-111)."""
+    from jax_bssn_gb300.bssn.variables import BSSNParameters
+    from jax_bssn_gb300.evolution import PatchEvolution
+    from jax_bssn_gb300.initial_data import gauge_wave_state, mesh, periodic_axis
+    x = periodic_axis(n, 1.0)
+    X, Y, Z = mesh(x)
+    dx = 1.0 / n
+    state = gauge_wave_state(X, Y, Z, 0.0)
+    params = BSSNParameters(eta=0.0, kappa=0.0, nu=0.0, g=0.0, dx=dx, dt=dx / steps_per_unit, zero_shift=1,
+                            gauge=0, x_min=float(x[0]), y_min=float(x[0]), z_min=float(x[0]))
+    evo = PatchEvolution(state, params, precision=precision)
+    evo.step(round(final_time / params.dt))
+    got = evo.state()
+    exact = gauge_wave_state(X, Y, Z, final_time)
+    g = got.conformal_metric.detach().cpu().numpy()
+    w = got.conformal_factor.detach().cpu().numpy()
+    return np.array([np.sqrt(np.mean((g[i, i] - exact.conformal_metric[i, i]) ** 2)) for i in range(3)]
+                    + [np.sqrt(np.mean((w - exact.conformal_factor) ** 2))])
+
+
+def test_gauge_wave_fourth_order_convergence(gb):
+    """The reference suite's convergence check: 16^3 and 32^3 to t = 1 with
+    dt = dx, order above 3.8 in every checked field."""
+    coarse, fine = _gauge_wave_errors(16), _gauge_wave_errors(32)
+    orders = np.log2(coarse / fine)
+    print("gauge-wave convergence orders", orders, "errors", coarse, fine)
+    assert np.all(orders > 3.8), orders
+
+
+def test_gauge_wave_60_fifty_steps(gb):
+    """tests/test_gauge_wave.py:16-64: 60^3, dt = dx, 50 steps; relative RMS
+    errors below 5e-5 (metric) and 1e-4 (W)."""
+    from jax_bssn_gb300.bssn.variables import BSSNParameters
+    from jax_bssn_gb300.evolution import PatchEvolution
+    from jax_bssn_gb300.initial_data import gauge_wave_state, mesh, periodic_axis
+    n = 60
+    x = periodic_axis(n, 1.0)
+    X, Y, Z = mesh(x)
+    dx = 1.0 / n
+    params = BSSNParameters(eta=0.0, kappa=0.0, g=0.0, dx=dx, dt=dx, x_min=float(x[0]), y_min=float(x[0]),
+                            z_min=float(x[0]))
+    evo = PatchEvolution(gauge_wave_state(X, Y, Z, 0.0), params)
+    evo.step(50)
+    got = evo.state()
+    exact = gauge_wave_state(X, Y, Z, 50 * dx)
+    g = got.conformal_metric.detach().cpu().numpy()
+    w = got.conformal_factor.detach().cpu().numpy()
+    rel = [np.sqrt(np.mean(((g[i, i] - exact.conformal_metric[i, i]) / exact.conformal_metric[i, i]) ** 2))
+           for i in range(3)]
+    rel.append(np.sqrt(np.mean(((w - exact.conformal_factor) / exact.conformal_factor) ** 2)))
+    print("gauge wave 60^3 relative errors", rel)
+    for err, tol in zip(rel, (5e-5, 5e-5, 5e-5, 1e-4)):
+        assert err < tol
