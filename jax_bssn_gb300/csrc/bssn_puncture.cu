@@ -393,7 +393,11 @@ __global__ void k_psi_total(const double* __restrict__ psi_bl, const double* __r
 // Conjugate gradients on A = -dx^2 (Lap + dS) (Cartesian).  One iteration:
 //   k_cg_apply   p = r + beta p_prev (p = r at the first), Bp, p.Bp with
 //                B = -A = dx^2 (Lap + dS)  -> alpha = gamma / p.Bp
-//   k_cg_update  x += alpha p, r -= alpha Bp, r.r -> beta, gamma, k, done
+//   k_cg_update  r -= alpha Bp, r.r -> beta, gamma, k, done
+// x += alpha p of an iteration is applied by the next iteration's operator
+// kernel, which reads that p anyway (the same FMA on the same values, so x is
+// unchanged bit for bit), and after the last iteration by k_cg_finish; the
+// update kernel then streams 24 bytes per unknown instead of 48.
 // The apply kernel stages p of one x plane of a 32 x 8 (z, y) tile in shared
 // memory, with its one-cell halo, and marches along x carrying the x
 // neighbours in registers, so each p value is formed once per tile (plus the
@@ -407,8 +411,8 @@ constexpr int kTz = 32, kTy = 8;
 
 __global__ void __launch_bounds__(kTz* kTy)
 k_cg_apply(const double* __restrict__ r, const double* __restrict__ pin, double* __restrict__ pout,
-           const double* __restrict__ centre, double* __restrict__ ap, SolveGrid G, SolveCtrl* ctrl,
-           double* __restrict__ partial) {
+           const double* __restrict__ centre, double* __restrict__ ap, double* __restrict__ sol, SolveGrid G,
+           SolveCtrl* ctrl, double* __restrict__ partial) {
     // two plane buffers: plane x+1 is written while plane x may still be read,
     // so each plane step needs one barrier
     __shared__ double tile[2][kTy + 2][kTz + 2];
@@ -471,6 +475,7 @@ k_cg_apply(const double* __restrict__ r, const double* __restrict__ pin, double*
                 s += tile[buf][ty + 1][tz + 2];
                 s += tile[buf][ty + 1][tz];
                 const double a = fma(cc, pc, s);
+                if (!first) sol[o] = fma(C.alpha, pin[o], sol[o]);   // x += alpha p of the previous iteration
                 pout[o] = pc;
                 ap[o] = a;
                 dot[0] = fma(pc, a, dot[0]);
@@ -492,8 +497,8 @@ k_cg_apply(const double* __restrict__ r, const double* __restrict__ pin, double*
 
 // Two samples per thread and step (16-byte loads), two steps in flight.
 __global__ void __launch_bounds__(kPunctThreads)
-k_cg_update(double* __restrict__ x, double* __restrict__ r, const double* __restrict__ p, const double* __restrict__ ap,
-            long long n, SolveCtrl* ctrl, double* __restrict__ partial) {
+k_cg_update(double* __restrict__ r, const double* __restrict__ ap, long long n, SolveCtrl* ctrl,
+            double* __restrict__ partial) {
     const SolveCtrl C = read_ctrl(ctrl);
     if (C.done) return;
     const double alpha = C.alpha;
@@ -501,25 +506,18 @@ k_cg_update(double* __restrict__ x, double* __restrict__ r, const double* __rest
     double rr1 = 0.0;
     const long long pairs = n / 2;
     const long long stride = (long long)gridDim.x * blockDim.x;
-    double2* x2 = reinterpret_cast<double2*>(x);
     double2* r2 = reinterpret_cast<double2*>(r);
-    const double2* p2 = reinterpret_cast<const double2*>(p);
     const double2* a2 = reinterpret_cast<const double2*>(ap);
 #pragma unroll 2
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < pairs; t += stride) {
-        const double2 pv = p2[t], av = a2[t], rv = r2[t];
-        double2 xv = x2[t];
-        xv.x = fma(alpha, pv.x, xv.x);
-        xv.y = fma(alpha, pv.y, xv.y);
+        const double2 av = a2[t], rv = r2[t];
         const double rx = fma(-alpha, av.x, rv.x), ry = fma(-alpha, av.y, rv.y);
-        x2[t] = xv;
         r2[t] = make_double2(rx, ry);
         rr[0] = fma(rx, rx, rr[0]);
         rr1 = fma(ry, ry, rr1);
     }
     if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
         const long long t = n - 1;
-        x[t] = fma(alpha, p[t], x[t]);
         const double rn = fma(-alpha, ap[t], r[t]);
         r[t] = rn;
         rr1 = fma(rn, rn, rr1);
@@ -534,6 +532,14 @@ k_cg_update(double* __restrict__ x, double* __restrict__ r, const double* __rest
         ctrl->first = 0;
         ctrl->done = !(tot[0] > C.atol2 && C.k + 1 < C.maxiter);
     }
+}
+
+// x += alpha p of the last conjugate-gradient iteration
+__global__ void k_cg_finish(double* __restrict__ x, const double* __restrict__ p, long long n,
+                            const SolveCtrl* ctrl) {
+    const double alpha = __ldcg(&ctrl->alpha);
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        x[t] = fma(alpha, p[t], x[t]);
 }
 
 // ---------------------------------------------------------------------------
@@ -885,9 +891,8 @@ int bssn_puncture_solve(const double* psi_bl, const double* curvature_squared, c
             double* pout = v[j % 2 ? V_P0 : V_P1];
             if (!G.axi) {
                 BSSN_LAUNCH(KC_SOLVE_APPLY, k_cg_apply, cg_blocks, kTz * kTy, s, v[V_R], pin, pout, v[V_CENTRE],
-                            v[V_Q], G, ctrl, partial);
-                BSSN_LAUNCH(KC_SOLVE_UPDATE, k_cg_update, ub, kPunctThreads, s, v[V_X], v[V_R], pout, v[V_Q], n,
-                            ctrl, partial);
+                            v[V_Q], v[V_X], G, ctrl, partial);
+                BSSN_LAUNCH(KC_SOLVE_UPDATE, k_cg_update, ub, kPunctThreads, s, v[V_R], v[V_Q], n, ctrl, partial);
                 chunk_launches += 2;
             } else {
                 // q ping-pongs as well: the p kernel reads the previous p and q around each cell
@@ -971,6 +976,11 @@ int bssn_puncture_solve(const double* psi_bl, const double* curvature_squared, c
             if (e == cudaSuccess) e = cudaStreamSynchronize(s);
             if (e != cudaSuccess) return finish(cuda_status(e, "bssn_puncture_solve"));
             done = host.done != 0;
+        }
+        if (!G.axi && host.k > 0) {
+            // iteration k - 1 wrote its p to P0 when odd, P1 when even
+            const double* p_last = v[(host.k - 1) % 2 ? V_P0 : V_P1];
+            BSSN_LAUNCH(KC_SOLVE_UPDATE, k_cg_finish, ub, kPunctThreads, s, v[V_X], p_last, n, ctrl);
         }
         if (linear_iterations) linear_iterations[it] = host.k;
         BSSN_LAUNCH(KC_SOLVE_UPDATE, k_newton_update, ub, kPunctThreads, s, u, v[V_X], n);
