@@ -352,6 +352,74 @@ int bssn_puncture_solve(const double* psi_bl, const double* curvature_squared, c
                         double* residual_history, int32_t* history_length, int32_t* linear_iterations,
                         void* workspace, size_t workspace_bytes, void* stream);
 
+/* ---------------------------------------------------------------------------
+ * Apparent-horizon finder (JAX_BSSN/utilities/apparent_horizon.py,
+ * hermite_interpolation.py).  The geometry is the physical metric and extrinsic
+ * curvature, each (3, 3, *grid) C-ordered float64 on the device, on a radial
+ * line (dims 1, axis r), a signed x-z plane (dims 2, axes x and z) or a
+ * Cartesian volume (dims 3): build_geometry (:22-98).  Surfaces are radii
+ * h[n_theta][n_phi] on the cell-centred polar and periodic azimuthal grid of
+ * angular_grid (:101-117), n_theta, n_phi >= 6, n_phi even.
+ * ------------------------------------------------------------------------- */
+typedef struct BssnHorizonGeometry {
+    const double* gamma;
+    const double* curvature;
+    int32_t dims;
+    int32_t size[3];     /* points per axis (entries past dims ignored) */
+    double origin[3];    /* first coordinate of each axis */
+    double spacing[3];
+    int32_t margin;      /* resolved region: [margin, size - 1 - margin] */
+} BssnHorizonGeometry;
+
+/* sample (:91-98) at points[n][3]: gamma[n][3][3], d_gamma[n][3][3][3]
+ * (derivative index first), curvature[n][3][3] and valid[n] (int32); any
+ * output may be NULL.  Reads the upper triangle of each tensor. */
+int bssn_horizon_sample(const BssnHorizonGeometry* geometry, const double* points, int64_t npoints,
+                        double* gamma, double* d_gamma, double* curvature, int32_t* valid, void* stream);
+
+/* angular_derivatives (:125-144): out[5][n_theta][n_phi] = h_theta,
+ * h_thetatheta, h_phi, h_phiphi, h_thetaphi. */
+int bssn_horizon_angular_derivatives(const double* radius, int32_t n_theta, int32_t n_phi, double* out,
+                                     void* stream);
+
+/* Bytes of device workspace for the surface, Jacobian and Newton-direction
+ * calls on an (n_theta, n_phi) surface (0 if the surface is invalid). */
+size_t bssn_horizon_workspace_bytes(int32_t n_theta, int32_t n_phi);
+
+/* surface (:160-236) of h = radius, or (direction not NULL) of the trial
+ * surface h = radius + step * direction, which is written to trial.
+ * expansion[n] and density[n] (may be NULL) per node; summary[4] (device) =
+ * sum of h, max |expansion|, count of unusable nodes (outside the resolved
+ * region, non-positive-definite metric, nonfinite expansion or density, or
+ * h <= 0) and the area sum_theta weights[theta] sum_phi density * 2 pi / n_phi
+ * (0 when area_weights is NULL).  center is a HOST triple. */
+int bssn_horizon_surface(const BssnHorizonGeometry* geometry, const double center[3], const double* radius,
+                         const double* direction, double step, int32_t n_theta, int32_t n_phi,
+                         const double* area_weights, double* trial, double* expansion, double* density,
+                         double* summary, void* workspace, size_t workspace_bytes, void* stream);
+
+/* The Jacobian d expansion / d radius (N x N, N = n_theta n_phi, row-major)
+ * that dense_jacobian (:239-250) forms with jax.linearize; here from central
+ * differences of relative step fd_step in each node's radius and angular
+ * derivatives, assembled in band storage and expanded. */
+int bssn_horizon_jacobian(const BssnHorizonGeometry* geometry, const double center[3], const double* radius,
+                          int32_t n_theta, int32_t n_phi, double fd_step, double* dense, void* workspace,
+                          size_t workspace_bytes, void* stream);
+
+/* Newton direction delta = -J^-1 expansion of find_apparent_horizon (:296-299):
+ * the band Jacobian as above, factorised by band LU with partial pivoting.
+ * summary[2] (device) = max |delta| over finite entries and the count of
+ * nonfinite entries. */
+int bssn_horizon_newton_direction(const BssnHorizonGeometry* geometry, const double center[3],
+                                  const double* radius, const double* expansion, int32_t n_theta, int32_t n_phi,
+                                  double fd_step, double* delta, double* summary, void* workspace,
+                                  size_t workspace_bytes, void* stream);
+
+/* interpolate_angular (:147-157): out[n_theta_out][n_phi_out] at polar angles
+ * theta[n_theta_out] and azimuths phi[n_phi_out] (device arrays). */
+int bssn_horizon_regrid(const double* radius, int32_t n_theta, int32_t n_phi, const double* theta,
+                        int32_t n_theta_out, const double* phi, int32_t n_phi_out, double* out, void* stream);
+
 /* No reference counterpart.  FMA throughput of this GPU in GFLOP/s (FMA = 2
  * flops) for BSSN_PRECISION_F64 or BSSN_PRECISION_F32: sixteen independent FMA
  * chains per thread, 8 x 256 threads per SM, one timed launch after a warm-up
@@ -372,7 +440,7 @@ long long bssn_launch_count(void);
  * stage, projection, import, export, constraints, FMR transfer, Cartoon,
  * FP32 conversion, other, K/Gt/At RHS in one pass (FP64 form), puncture
  * Newton-level kernels, puncture Krylov operator kernels, puncture Krylov
- * vector updates.  bssn_profile_read synchronises the recorded events, accumulates and
+ * vector updates, horizon surface kernels, horizon band solve.  bssn_profile_read synchronises the recorded events, accumulates and
  * returns the number of classes. */
 void bssn_profile_enable(int on);
 void bssn_profile_reset(void);

@@ -81,6 +81,12 @@ class BssnPatch(ctypes.Structure):
 
 Shape3 = ctypes.c_int32 * 3
 
+class BssnHorizonGeometry(ctypes.Structure):
+    _fields_ = [("gamma", ctypes.c_void_p), ("curvature", ctypes.c_void_p), ("dims", ctypes.c_int32),
+                ("size", ctypes.c_int32 * 3), ("origin", ctypes.c_double * 3), ("spacing", ctypes.c_double * 3),
+                ("margin", ctypes.c_int32)]
+
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "bssn_last_error": (ctypes.c_char_p, []),
@@ -160,6 +166,27 @@ SIGNATURES = {
                                            ctypes.c_void_p, ctypes.c_void_p, c_double_p,
                                            ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32),
                                            ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    "bssn_horizon_sample": (ctypes.c_int, [ctypes.POINTER(BssnHorizonGeometry), ctypes.c_void_p, ctypes.c_int64,
+                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.c_void_p]),
+    "bssn_horizon_angular_derivatives": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
+                                                        ctypes.c_void_p, ctypes.c_void_p]),
+    "bssn_horizon_workspace_bytes": (ctypes.c_size_t, [ctypes.c_int32, ctypes.c_int32]),
+    "bssn_horizon_surface": (ctypes.c_int, [ctypes.POINTER(BssnHorizonGeometry), c_double_p, ctypes.c_void_p,
+                                            ctypes.c_void_p, ctypes.c_double, ctypes.c_int32, ctypes.c_int32,
+                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    "bssn_horizon_jacobian": (ctypes.c_int, [ctypes.POINTER(BssnHorizonGeometry), c_double_p, ctypes.c_void_p,
+                                             ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_void_p,
+                                             ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    "bssn_horizon_newton_direction": (ctypes.c_int, [ctypes.POINTER(BssnHorizonGeometry), c_double_p,
+                                                     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
+                                                     ctypes.c_int32, ctypes.c_double, ctypes.c_void_p,
+                                                     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                                     ctypes.c_void_p]),
+    "bssn_horizon_regrid": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p,
+                                           ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
+                                           ctypes.c_void_p]),
     "bssn_gather_boxes": (ctypes.c_int, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "bssn_launch_count": (ctypes.c_longlong, []),
     "bssn_profile_enable": (None, [ctypes.c_int]),
@@ -169,7 +196,8 @@ SIGNATURES = {
 
 KERNEL_CLASSES = ("fill", "first_derivs", "rhs_gauge", "rhs_kgt", "rhs_at", "mom_derived", "mom_damping",
                   "sommerfeld", "rk4_stage", "project", "import", "export", "constraints", "fmr_transfer",
-                  "cartoon", "convert", "other", "rhs_curv", "solve_newton", "solve_apply", "solve_update")
+                  "cartoon", "convert", "other", "rhs_curv", "solve_newton", "solve_apply", "solve_update", "horizon_surface",
+                  "horizon_solve")
 
 
 def profile_read() -> dict:

@@ -1,4 +1,4 @@
-"""Puncture initial data on the GPU (mirrors JAX_BSSN/utilities, the Bowen-York part)."""
+"""Puncture initial data and the apparent-horizon finder on the GPU (mirrors JAX_BSSN/utilities)."""
 
 from .bowen_york_solver import (  # noqa: F401
     PunctureSolve,
@@ -18,4 +18,15 @@ from .bowen_york_solver import (  # noqa: F401
     puncture_solve,
     solve_axisymmetric_conformal_factor,
     solve_conformal_factor,
+)
+from .apparent_horizon import (  # noqa: F401
+    ExpansionResidual,
+    angular_derivatives,
+    angular_grid,
+    build_geometry,
+    dense_jacobian,
+    find_apparent_horizon,
+    interpolate_angular,
+    surface,
+    theta_ghosts,
 )
