@@ -20,6 +20,10 @@ Other workloads (--workload):
                 metric counts unknowns x Krylov iterations per second).
   puncture_axi  the axisymmetric collision's initial data: Newton + BiCGSTAB on
                 the 128 x 256 meridional grid, tolerances 1e-12.
+  horizon       apparent-horizon finder on a triaxially stretched Schwarzschild
+                slice (M=2, scales 1, 1.25, 1.5, isotropic) stored as a 124^3
+                Cartesian volume (dx=0.04): the finder's defaults (12 x 24
+                start, refinement to 24 x 48); a "step" is one complete find.
 All inputs are synthetic (analytic initial data generated on the host).
 
 Arms:
@@ -98,7 +102,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
-    ap.add_argument("--workload", choices=("teukolsky", "fmr", "axisymmetric", "puncture", "puncture_axi"),
+    ap.add_argument("--workload", choices=("teukolsky", "fmr", "axisymmetric", "puncture", "puncture_axi",
+                                           "horizon"),
                     default="teukolsky")
     ap.add_argument("--n", type=int, default=None, help="grid size (teukolsky n, fmr root n, axisymmetric Nrho)")
     ap.add_argument("--no-e2e", action="store_true")
@@ -576,6 +581,212 @@ def run_puncture_reference(args, world, rank):
 
 
 # ----------------------------------------------------------------------------
+# apparent-horizon finder
+# ----------------------------------------------------------------------------
+
+HORIZON_METRIC = "apparent-horizon finds/s"
+HORIZON_UNIT = "finds/s"
+
+
+class Horizon:
+    """The reference suite's triaxial case (tests/test_apparent_horizon.py:118-129):
+    Schwarzschild M=2 in isotropic slicing pulled back by scales (1, 1.25, 1.5),
+    a 124^3 volume with dx=0.04 about the origin, initial radius 0.9 and the
+    finder's defaults."""
+    name = "horizon"
+
+    def __init__(self, n=None):
+        self.dx = 0.04
+        self.count = n or 124
+        self.scale = (1.0, 1.25, 1.5)
+        self.mass = 2.0
+        self.initial = 0.9
+
+    def config(self):
+        return {"workload": f"apparent-horizon find on a triaxial Schwarzschild slice (M=2, scales 1/1.25/1.5, "
+                            f"isotropic) stored as a {self.count}^3 Cartesian volume, dx={self.dx}, FP64",
+                "finder": {"n_theta": 12, "n_phi": 24, "max_angular": 48, "tolerance": 1e-8,
+                           "initial_radius": self.initial},
+                "l2": f"geometry 18 x {self.count}^3 doubles ({18 * 8 * self.count ** 3 / 1e6:.0f} MB) exceeds "
+                      "the 129 MB L2", "parallelism": "replicas"}
+
+    def fields(self, count=None):
+        import numpy as np
+        count = count or self.count
+        axis = (np.arange(count) - (count - 1) / 2) * self.dx
+        pos = np.meshgrid(axis, axis, axis, indexing="ij")
+        st = [f * q for q, f in zip(pos, self.scale)]
+        r = np.sqrt(sum(q ** 2 for q in st))
+        gamma = np.eye(3).reshape(3, 3, 1, 1, 1) * (1 + self.mass / (2 * r)) ** 4
+        f = np.asarray(self.scale)
+        gamma = gamma * (f[:, None] * f[None, :]).reshape(3, 3, 1, 1, 1)
+        return (axis, axis, axis), np.ascontiguousarray(gamma), np.zeros_like(gamma)
+
+
+def band_lu_work(n_theta, n_phi):
+    """Algorithmic FP64 flops and bytes of one band LU factorisation with the
+    right-hand side carried along (the kernel's band widths)."""
+    n = n_theta * n_phi
+    kl = min(3 * n_phi - 1, n - 1)
+    ku2 = min(2 * kl, n - 1)
+    flops = 0
+    nbytes = 0
+    for k in range(n):
+        rows = min(n - 1, k + kl) - k          # rows eliminated below the pivot
+        cols = min(n - 1, k + ku2) - k + 1     # trailing columns plus the right-hand side
+        flops += 2 * rows * cols
+        nbytes += 16 * (rows + 1) * cols + 8 * (rows + 1)
+    return flops, nbytes
+
+
+def horizon_cpu(wl, finds=1, count=None):
+    """The oracle finder (NumPy; dense Jacobian and LAPACK solve) on the same
+    kind of slice."""
+    from oracle import horizon as oh
+    axes, gamma, kij = wl.fields(count)
+    t = time.perf_counter()
+    for _ in range(finds):
+        res = oh.find_apparent_horizon(axes, gamma, kij, center=(0, 0, 0), initial_radius=wl.initial)
+    dt = time.perf_counter() - t
+    cores = os.cpu_count() or 1
+    return {"value": finds / dt, "unit": HORIZON_UNIT, "cores": cores, "kind": "port",
+            "sample": f"{finds} find(s) on the {count or wl.count}^3 volume ({int(res['iterations'])} Newton "
+                      f"iterations; NumPy restatement, dense Jacobian and LAPACK solve through the threaded BLAS on "
+                      f"up to {cores} cores; JAX not installed)", "seconds": dt, "mass": res["mass"]}
+
+
+def run_horizon(args, world, rank, local):
+    import torch
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=device)
+    from jax_bssn_gb300 import _native, build
+    if not build.LIBRARY.exists():
+        build.build()
+    lib = _native.load()
+    from jax_bssn_gb300.utilities import apparent_horizon as ah
+    wl = Horizon(args.n)
+    axes, gamma_h, kij_h = wl.fields()
+    gamma = torch.as_tensor(gamma_h, device=device)
+    kij = torch.as_tensor(kij_h, device=device)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    def find(g, k):
+        return ah.find_apparent_horizon(axes, g, k, center=(0, 0, 0), initial_radius=wl.initial)
+
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        res = find(gamma, kij)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    torch.cuda.synchronize()
+    launches0 = lib.bssn_launch_count()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for _ in range(args.steps):
+        res = find(gamma, kij)
+    t1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    launches = lib.bssn_launch_count() - launches0
+    clock_info = clocks.stop()
+    ms = _max_over_ranks(t0.elapsed_time(t1), world, device)
+    value = world * args.steps / (ms / 1e3)
+    # per-kernel-class device time of one profiled find
+    lib.bssn_profile_reset()
+    lib.bssn_profile_enable(1)
+    rp = find(gamma, kij)
+    torch.cuda.synchronize()
+    lib.bssn_profile_enable(0)
+    prof = _native.profile_read()
+    lib.bssn_profile_reset()
+    total = sum(v[0] for v in prof.values()) or 1.0
+    kernels = {k: {"ms": round(v[0], 3), "launches": v[1], "share": round(v[0] / total, 4)}
+               for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}
+    # Newton iterations per resolution: one band factorisation each
+    flops = nbytes = 0
+    for row in rp["convergence"]:
+        f, b = band_lu_work(int(row[0]), int(row[1]))
+        flops += f * int(row[5])
+        nbytes += b * int(row[5])
+    sms, slaunch = prof.get("horizon_solve", (0.0, 0))
+    hbm_peak, peak_src = 6800.0, "fallback"
+    peaks_path = ROOT / "MEASURED_PEAKS.json"
+    if peaks_path.exists():
+        peaks = json.loads(peaks_path.read_text())
+        if "hbm_gbs" in peaks:
+            hbm_peak, peak_src = float(peaks["hbm_gbs"]), "measured"
+    achieved = nbytes / (sms / 1e3) / 1e9 if sms > 0 else None
+    roofline = {"bound": "hbm", "kernel": "k_band_step", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved / hbm_peak if achieved else None, "traffic": None, "peak_source": peak_src,
+                "kernel_share": sms / total, "kernel_ms_per_launch": sms / max(slaunch, 1),
+                "algorithmic_bytes_per_find": nbytes,
+                "note": "one launch per band column; the band (at most 32 MB) stays in L2, so the factorisation is "
+                        "bound by launch latency, not by HBM or the FP64 pipe"}
+    peak = _native.fma_peak_gflops(_native.PRECISION_F64) / 1e3
+    fl = flops / (sms / 1e3) / 1e12 if sms > 0 else None
+    compute = {"bound": "fp64", "kernel": "k_band_step", "achieved": fl, "peak": peak, "unit": "TFLOP/s",
+               "frac": fl / peak if fl else None, "flops_per_find": flops,
+               "peak_source": "measured live by bssn_probe_fma_peak"}
+    e2e = None
+    if not args.no_e2e:
+        torch.cuda.synchronize()
+        barrier()
+        e0 = time.perf_counter()
+        for _ in range(args.steps):
+            re = find(gamma_h, kij_h)
+        torch.cuda.synchronize()
+        ems = (time.perf_counter() - e0) * 1e3
+        ems = _max_over_ranks(ems, world, device)
+        e2e = {"value": world * args.steps / (ems / 1e3), "unit": HORIZON_UNIT,
+               "h2d_bytes_per_step": gamma_h.nbytes + kij_h.nbytes,
+               "d2h_bytes_per_step": re["radius"].nbytes + re["expansion"].nbytes, "ms_per_step": ems / args.steps,
+               "note": "host NumPy geometry through find_apparent_horizon (pageable copies); host wall clock"}
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = horizon_cpu(wl, 1)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    if rank != 0:
+        return None
+    return {
+        "metric": HORIZON_METRIC, "value": value, "unit": HORIZON_UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (analytic Schwarzschild slice)",
+        "config": {**wl.config(), "step": "one complete find_apparent_horizon call",
+                   "mass": res["mass"], "mass_error": abs(res["mass"] / wl.mass - 1),
+                   "convergence": [[int(r[0]), int(r[1]), int(r[5])] for r in res["convergence"]],
+                   "residual": res["residual"], "audit_residual": res["audit_residual"]},
+        "roofline": roofline, "roofline_compute": compute, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+        "clocks": clock_info, "kernels": kernels,
+    }
+
+
+def run_horizon_reference(args, world, rank):
+    if rank != 0:
+        return None
+    wl = Horizon(args.n)
+    horizon_cpu(wl, 1)
+    base = horizon_cpu(wl, args.steps)
+    value = base["value"]
+    return {"metric": HORIZON_METRIC, "value": value, "unit": HORIZON_UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": base["seconds"] * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": wl.config(),
+            "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": HORIZON_UNIT, "cores": base["cores"], "kind": "port",
+                             "sample": "each step " + base["sample"]},
+            "e2e": {"value": value, "unit": HORIZON_UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+# ----------------------------------------------------------------------------
 # clocks
 # ----------------------------------------------------------------------------
 
@@ -893,6 +1104,9 @@ def main():
     if args.workload in PUNCTURES:
         out = (run_puncture_reference(args, world, rank) if args.impl == "reference"
                else run_puncture(args, world, rank, local))
+    elif args.workload == "horizon":
+        out = (run_horizon_reference(args, world, rank) if args.impl == "reference"
+               else run_horizon(args, world, rank, local))
     elif args.impl == "reference":
         out = run_reference(args, world, rank)
     else:
