@@ -774,11 +774,12 @@ def run_horizon_reference(args, world, rank):
     if rank != 0:
         return None
     wl = Horizon(args.n)
+    finds = max(1, min(args.steps, 2))  # about 15 s per find on the host cores
     horizon_cpu(wl, 1)
-    base = horizon_cpu(wl, args.steps)
+    base = horizon_cpu(wl, finds)
     value = base["value"]
-    return {"metric": HORIZON_METRIC, "value": value, "unit": HORIZON_UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": base["seconds"] * 1e3 / args.steps, "higher_is_better": True,
+    return {"metric": HORIZON_METRIC, "value": value, "unit": HORIZON_UNIT, "n_gpus": world, "steps": finds,
+            "warmup": 1, "ms_per_step": base["seconds"] * 1e3 / finds, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": wl.config(),
             "impl": "reference",
             "cpu_baseline": {"value": value, "unit": HORIZON_UNIT, "cores": base["cores"], "kind": "port",

@@ -34,7 +34,9 @@
 //                        in phi on the wrapped field, in the reference's order.
 #include <algorithm>
 #include <cmath>
+#include <map>
 #include <string>
+#include <tuple>
 
 #include <cuda_runtime.h>
 
@@ -46,8 +48,9 @@ namespace bssn {
 namespace {
 
 constexpr int kHThreads = 128;
+constexpr int kSurfThreads = 32;  // one node per thread; small blocks spread a surface over the SMs
 constexpr int kSumThreads = 1024;
-constexpr int kStepWarps = 8;      // columns per block of a factorisation step
+constexpr int kStepWarps = 2;      // columns per block of a factorisation step (spread over the SMs)
 constexpr int kBackThreads = 1024;
 constexpr double kPi = 3.141592653589793;
 
@@ -64,6 +67,13 @@ struct HGeom {
 __device__ __forceinline__ double rmul(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double radd(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double rdiv(double a, double b) { return __ddiv_rn(a, b); }
+
+// Programmatic dependent launch: a step kernel waits for its predecessor's
+// completion (and the visibility of its writes) before touching the band, and
+// lets the next one be scheduled once its own stores are issued.  Without the
+// launch attribute both instructions are no-ops.
+__device__ __forceinline__ void pdl_enter() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_release() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
 // ---------------------------------------------------------------------------
 // Hermite weights and their index derivatives (hermite_interpolation.py:12-24)
@@ -379,7 +389,7 @@ __device__ __forceinline__ double& band_at(const Band& B, int i, int j) {
 
 // One node per thread: the surface, the node's bad flag, and (band != null)
 // the node's Jacobian row.
-__global__ void __launch_bounds__(kHThreads)
+__global__ void __launch_bounds__(kSurfThreads)
 k_surface(HGeom G, Sphere S, double cx, double cy, double cz, double* __restrict__ trial,
           double* __restrict__ expansion, double* __restrict__ density, int* __restrict__ bad, Band B,
           double fd_step) {
@@ -496,20 +506,30 @@ k_surface_summary(const double* __restrict__ radius, const double* __restrict__ 
 // to the right-hand side.  Column k is only read during step k; its pivot goes
 // to diag[k].
 // ---------------------------------------------------------------------------
+constexpr int kRowsPerLane = 12;  // rows per lane per pass: loads issued together
+
 __global__ void __launch_bounds__(kStepWarps * 32)
 k_band_step(Band B, int k, double* __restrict__ rhs, double* __restrict__ diag) {
+    pdl_enter();
     const int lane = threadIdx.x & 31;
     const int col = k + 1 + blockIdx.x * kStepWarps + (threadIdx.x >> 5);
     const int last = min(B.n - 1, k + B.ku2);
     const bool is_rhs = col == last + 1;
     if (col > last + 1) return;
     const int rmax = min(B.n - 1, k + B.kl);
-    const double* ck = B.a + (long long)k * B.ld + B.ku2;  // ck[r - k] = A(r, k)
+    const double* __restrict__ ck = B.a + (long long)k * B.ld + B.ku2 - k;  // ck[r] = A(r, k)
     double best = -1.0;
     int arg = k;
-    for (int r = k + lane; r <= rmax; r += 32) {
-        const double v = fabs(ck[r - k]);
-        if (v > best) { best = v; arg = r; }
+    for (int base = k; base <= rmax; base += 32 * kRowsPerLane) {
+        double v[kRowsPerLane];
+#pragma unroll
+        for (int q = 0; q < kRowsPerLane; ++q) {
+            const int r = base + lane + 32 * q;
+            v[q] = r <= rmax ? fabs(ck[r]) : -1.0;
+        }
+#pragma unroll
+        for (int q = 0; q < kRowsPerLane; ++q)
+            if (v[q] > best) { best = v[q]; arg = base + lane + 32 * q; }
     }
     for (int o = 16; o > 0; o >>= 1) {
         const double ob = __shfl_xor_sync(0xffffffffu, best, o);
@@ -517,24 +537,187 @@ k_band_step(Band B, int k, double* __restrict__ rhs, double* __restrict__ diag) 
         if (ob > best || (ob == best && oa < arg)) { best = ob; arg = oa; }
     }
     const int pr = arg;
-    const double piv = ck[pr - k], akk = ck[0];
-    double* cj = is_rhs ? rhs : B.a + (long long)col * B.ld + (B.ku2 - col);  // cj[r] = A(r, col)
-    const double xk = cj[k], xp = cj[pr];
-    for (int r = k + 1 + lane; r <= rmax; r += 32) {
-        const double l = (r == pr ? akk : ck[r - k]) / piv;
-        const double old = r == pr ? xk : cj[r];
-        cj[r] = old - l * xp;
+    double* __restrict__ cj = is_rhs ? rhs : B.a + (long long)col * B.ld + (B.ku2 - col);  // cj[r] = A(r, col)
+    const double piv = ck[pr], akk = ck[k], xk = cj[k], xp = cj[pr];
+    const double rpiv = 1.0 / piv;  // multipliers scaled by the reciprocal, as getf2 does
+    __syncwarp();  // every lane holds rows k and pr before any lane rewrites them
+    for (int base = k + 1; base <= rmax; base += 32 * kRowsPerLane) {
+        double a[kRowsPerLane], x[kRowsPerLane];
+#pragma unroll
+        for (int q = 0; q < kRowsPerLane; ++q) {
+            const int r = base + lane + 32 * q;
+            a[q] = r <= rmax ? ck[r] : 0.0;
+            x[q] = r <= rmax ? cj[r] : 0.0;
+        }
+#pragma unroll
+        for (int q = 0; q < kRowsPerLane; ++q) {
+            const int r = base + lane + 32 * q;
+            if (r <= rmax) {
+                const double l = (r == pr ? akk : a[q]) * rpiv;
+                cj[r] = (r == pr ? xk : x[q]) - l * xp;
+            }
+        }
     }
+    __syncwarp();
     if (lane == 0) {
         cj[k] = xp;
         if (is_rhs) diag[k] = piv;
     }
 }
 
+// The same step with the pivot search of the next column folded in: the warp
+// that updates column k + 1 holds its new entries in registers, finds their
+// first largest modulus and leaves the row in piv_row[k + 1], so every step
+// makes one round trip to memory (the pivot row's entries come from the lane
+// that loaded them).  Step 0 searches its own column (search = 1).  Needs
+// kl + 2 <= 32 * kRowsPerLane.
+__global__ void __launch_bounds__(kStepWarps * 32)
+k_band_step_fused(Band B, int k, int search, double* __restrict__ rhs, double* __restrict__ diag,
+                  int* __restrict__ piv_row) {
+    pdl_enter();
+    const int lane = threadIdx.x & 31;
+    const int col = k + 1 + blockIdx.x * kStepWarps + (threadIdx.x >> 5);
+    const int last = min(B.n - 1, k + B.ku2);
+    const bool is_rhs = col == last + 1;
+    if (col > last + 1) return;
+    const bool next = !is_rhs && col == k + 1;  // this warp searches the next pivot
+    const int rmax = min(B.n - 1, k + B.kl);
+    const int rext = next ? min(B.n - 1, col + B.kl) : rmax;  // rows of column k + 1 to search
+    const double* __restrict__ ck = B.a + (long long)k * B.ld + B.ku2 - k;  // ck[r] = A(r, k)
+    double* __restrict__ cj = is_rhs ? rhs : B.a + (long long)col * B.ld + (B.ku2 - col);
+    const int pre = search ? -1 : piv_row[k];
+    double a[kRowsPerLane], x[kRowsPerLane];
+#pragma unroll
+    for (int q = 0; q < kRowsPerLane; ++q) {
+        const int r = k + lane + 32 * q;
+        a[q] = r <= rmax ? ck[r] : 0.0;
+        x[q] = r <= rext ? cj[r] : 0.0;
+    }
+    int pr = pre;
+    if (search) {
+        double best = -1.0;
+        int arg = k;
+#pragma unroll
+        for (int q = 0; q < kRowsPerLane; ++q) {
+            const int r = k + lane + 32 * q;
+            const double v = r <= rmax ? fabs(a[q]) : -1.0;
+            if (v > best) { best = v; arg = r; }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+            const int oa = __shfl_xor_sync(0xffffffffu, arg, o);
+            if (ob > best || (ob == best && oa < arg)) { best = ob; arg = oa; }
+        }
+        pr = arg;
+    }
+    // rows k and pr of both columns from the lanes that hold them
+    const int qp = (pr - k) >> 5, lp = (pr - k) & 31;
+    double ap = 0.0, xpv = 0.0;
+#pragma unroll
+    for (int q = 0; q < kRowsPerLane; ++q)
+        if (q == qp) { ap = a[q]; xpv = x[q]; }
+    const double piv = __shfl_sync(0xffffffffu, ap, lp);
+    const double xp = __shfl_sync(0xffffffffu, xpv, lp);
+    const double akk = __shfl_sync(0xffffffffu, a[0], 0);
+    const double xk = __shfl_sync(0xffffffffu, x[0], 0);
+    const double rpiv = 1.0 / piv;  // multipliers scaled by the reciprocal, as getf2 does
+    double best = -1.0;
+    int arg = col;
+#pragma unroll
+    for (int q = 0; q < kRowsPerLane; ++q) {
+        const int r = k + lane + 32 * q;
+        if (r > k && r <= rmax) {
+            const double l = (r == pr ? akk : a[q]) * rpiv;
+            x[q] = (r == pr ? xk : x[q]) - l * xp;
+            cj[r] = x[q];
+        }
+        if (next && r > k && r <= rext) {
+            const double v = fabs(x[q]);
+            if (v > best) { best = v; arg = r; }
+        }
+    }
+    if (lane == 0) {
+        cj[k] = xp;
+        if (is_rhs) diag[k] = piv;
+    }
+    if (next) {
+        for (int o = 16; o > 0; o >>= 1) {
+            const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+            const int oa = __shfl_xor_sync(0xffffffffu, arg, o);
+            if (ob > best || (ob == best && oa < arg)) { best = ob; arg = oa; }
+        }
+        if (lane == 0) piv_row[col] = arg;
+    }
+    pdl_release();
+}
+
+// Back substitution with y and 1/U_kk in shared memory: thread t owns the row
+// k - 1 - t of column k, whose U entries stream in kPrefetch steps ahead.
+constexpr int kPrefetch = 8;
+constexpr int kBackSmemMax = 200 * 1024;
+
+__global__ void __launch_bounds__(kBackThreads)
+k_band_back_shared(Band B, double* __restrict__ y, const double* __restrict__ diag, double* __restrict__ out) {
+    pdl_enter();
+    extern __shared__ double sm[];
+    double* sy = sm;
+    double* srd = sm + B.n;
+    __shared__ double s_x;
+    __shared__ double s_max[kBackThreads], s_bad[kBackThreads];
+    for (int i = threadIdx.x; i < B.n; i += blockDim.x) {
+        sy[i] = y[i];
+        srd[i] = 1.0 / diag[i];
+    }
+    const int t = threadIdx.x;
+    const bool active = t < B.ku2;
+    double pre[kPrefetch];
+#pragma unroll
+    for (int d = 0; d < kPrefetch; ++d) {
+        const int k = B.n - 1 - d;
+        pre[d] = (active && k >= 0 && k - 1 - t >= 0) ? B.a[(long long)k * B.ld + (B.ku2 - 1 - t)] : 0.0;
+    }
+    __syncthreads();
+    for (int k = B.n - 1; k >= 0; --k) {
+        if (t == 0) {
+            const double x = sy[k] * srd[k];
+            sy[k] = x;
+            s_x = x;
+        }
+        const double a = pre[0];
+#pragma unroll
+        for (int d = 0; d + 1 < kPrefetch; ++d) pre[d] = pre[d + 1];
+        const int kn = k - kPrefetch;
+        pre[kPrefetch - 1] = (active && kn >= 0 && kn - 1 - t >= 0) ? B.a[(long long)kn * B.ld + (B.ku2 - 1 - t)] : 0.0;
+        __syncthreads();
+        const int r = k - 1 - t;
+        if (active && r >= 0) sy[r] -= a * s_x;
+        __syncthreads();
+    }
+    double mx = 0.0, nb = 0.0;
+    for (int i = threadIdx.x; i < B.n; i += blockDim.x) {
+        const double v = sy[i];
+        y[i] = v;
+        if (!isfinite(v)) nb += 1.0;
+        else mx = fmax(mx, fabs(v));
+    }
+    s_max[threadIdx.x] = mx;
+    s_bad[threadIdx.x] = nb;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            s_max[threadIdx.x] = fmax(s_max[threadIdx.x], s_max[threadIdx.x + w]);
+            s_bad[threadIdx.x] += s_bad[threadIdx.x + w];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) { out[0] = s_max[0]; out[1] = s_bad[0]; }
+}
+
 // x = U^-1 y by columns: x_k = y_k / U_kk, then y_r -= U_rk x_k above it.
 // One block; also writes max |x| and the nonfinite count.
 __global__ void __launch_bounds__(kBackThreads)
 k_band_back(Band B, double* __restrict__ y, const double* __restrict__ diag, double* __restrict__ out) {
+    pdl_enter();
     __shared__ double s_x;
     __shared__ double s_max[kBackThreads], s_bad[kBackThreads];
     for (int k = B.n - 1; k >= 0; --k) {
@@ -710,13 +893,123 @@ size_t band_bytes(int nt, int np) {
     return (size_t)B.n * B.ld * sizeof(double);
 }
 
+// Workspace of the Newton direction: the band, then the pivots (U's
+// diagonal), the right-hand side / solution, its two-number summary and the
+// nodes' bad flags.
+struct Factor {
+    Band B;
+    double *diag, *rhs, *sum;
+    int *bad, *piv;
+};
+
+Factor factor_of(void* ws, int nt, int np) {
+    Factor F;
+    F.B = band_of(ws, nt, np);
+    char* rest = static_cast<char*>(ws) + band_bytes(nt, np);
+    F.diag = reinterpret_cast<double*>(rest);
+    F.rhs = F.diag + F.B.n;
+    F.sum = F.rhs + F.B.n;
+    F.bad = reinterpret_cast<int*>(F.sum + 2);
+    F.piv = F.bad + F.B.n;
+    return F;
+}
+
+// Launch with the programmatic-stream-serialisation attribute (dependent
+// launch), counted and timed like every other launch.
+template <typename... P, typename... A>
+void launch_dependent(void (*kernel)(P...), unsigned blocks, unsigned threads, size_t smem, cudaStream_t s,
+                      A... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(blocks);
+    cfg.blockDim = dim3(threads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    prof_begin(KC_HORIZON_SOLVE, s);
+    cudaLaunchKernelEx(&cfg, kernel, args...);
+    prof_end(KC_HORIZON_SOLVE, s);
+}
+
+// The factorisation and back substitution: one launch per band column, then
+// one for the back substitution, each a dependent launch of the one before.
+int enqueue_factor(const Factor& F, cudaStream_t s) {
+    const Band& B = F.B;
+    const bool fused = B.kl + 2 <= 32 * kRowsPerLane;
+    for (int k = 0; k < B.n; ++k) {
+        const int cols = std::min(B.n - 1, k + B.ku2) - k + 1;  // trailing columns plus the right-hand side
+        const unsigned blocks = (unsigned)((cols + kStepWarps - 1) / kStepWarps);
+        if (fused)
+            launch_dependent(k_band_step_fused, blocks, kStepWarps * 32, 0, s, B, k, k == 0 ? 1 : 0, F.rhs, F.diag,
+                             F.piv);
+        else
+            launch_dependent(k_band_step, blocks, kStepWarps * 32, 0, s, B, k, F.rhs, F.diag);
+    }
+    const size_t smem = 2 * (size_t)B.n * sizeof(double);
+    if (smem <= (size_t)kBackSmemMax && B.ku2 <= kBackThreads) {
+        static bool configured = false;
+        if (!configured) {
+            cudaFuncSetAttribute(k_band_back_shared, cudaFuncAttributeMaxDynamicSharedMemorySize, kBackSmemMax);
+            configured = true;
+        }
+        launch_dependent(k_band_back_shared, 1, kBackThreads, smem, s, B, F.rhs, F.diag, F.sum);
+    } else {
+        launch_dependent(k_band_back, 1, kBackThreads, 0, s, B, F.rhs, F.diag, F.sum);
+    }
+    return B.n + 1;
+}
+
+// Instantiated factorisation graphs per thread, keyed by device, workspace
+// and surface shape (the kernels' pointers all live in the workspace).
+struct FactorGraphs {
+    cudaStream_t capture = nullptr;
+    std::map<std::tuple<int, void*, int, int>, cudaGraphExec_t> execs;
+};
+
+cudaError_t factor_graph(const Factor& F, void* ws, int nt, int np, cudaGraphExec_t& out) {
+    thread_local FactorGraphs graphs;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const auto key = std::make_tuple(dev, ws, nt, np);
+    auto it = graphs.execs.find(key);
+    if (it != graphs.execs.end()) {
+        out = it->second;
+        return cudaSuccess;
+    }
+    if (graphs.execs.size() >= 16) {
+        for (auto& kv : graphs.execs) cudaGraphExecDestroy(kv.second);
+        graphs.execs.clear();
+    }
+    if (!graphs.capture) {
+        e = cudaStreamCreateWithFlags(&graphs.capture, cudaStreamNonBlocking);
+        if (e != cudaSuccess) return e;
+    }
+    e = cudaStreamBeginCapture(graphs.capture, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    const int launches = enqueue_factor(F, graphs.capture);
+    count_launches(-launches);  // recorded, not run
+    cudaGraph_t graph = nullptr;
+    e = cudaStreamEndCapture(graphs.capture, &graph);
+    cudaGraphExec_t exec = nullptr;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return e;
+    graphs.execs[key] = exec;
+    out = exec;
+    return cudaSuccess;
+}
+
 int assemble(const HGeom& G, const double center[3], const double* radius, int nt, int np, double fd_step,
              const Band& B, double* expansion, int* bad, cudaStream_t s) {
     Sphere S{nt, np, radius, nullptr, 0.0};
     cudaError_t e = cudaMemsetAsync(B.a, 0, (size_t)B.n * B.ld * sizeof(double), s);
     if (e != cudaSuccess) return cuda_status(e, "bssn_horizon: band clear");
-    const unsigned blocks = (unsigned)((B.n + kHThreads - 1) / kHThreads);
-    BSSN_LAUNCH(KC_HORIZON_SURFACE, k_surface, blocks, kHThreads, s, G, S, center[0], center[1], center[2],
+    const unsigned blocks = (unsigned)((B.n + kSurfThreads - 1) / kSurfThreads);
+    BSSN_LAUNCH(KC_HORIZON_SURFACE, k_surface, blocks, kSurfThreads, s, G, S, center[0], center[1], center[2],
                 (double*)nullptr, expansion, (double*)nullptr, bad, B, fd_step);
     return cuda_status(cudaGetLastError(), "bssn_horizon: jacobian");
 }
@@ -754,7 +1047,7 @@ extern "C" int bssn_horizon_angular_derivatives(const double* radius, int32_t n_
 extern "C" size_t bssn_horizon_workspace_bytes(int32_t n_theta, int32_t n_phi) {
     if (n_theta < 6 || n_phi < 6 || n_phi % 2 || (long long)n_theta * n_phi > (1 << 22)) return 0;
     const size_t n = (size_t)n_theta * n_phi;
-    return band_bytes(n_theta, n_phi) + n * sizeof(double) + n * sizeof(int) + 8 * sizeof(double);
+    return band_bytes(n_theta, n_phi) + 2 * n * sizeof(double) + 2 * sizeof(double) + 2 * n * sizeof(int);
 }
 
 extern "C" int bssn_horizon_surface(const BssnHorizonGeometry* geometry, const double center[3],
@@ -776,7 +1069,7 @@ extern "C" int bssn_horizon_surface(const BssnHorizonGeometry* geometry, const d
     int* bad = static_cast<int*>(workspace);
     Sphere S{n_theta, n_phi, radius, direction, step};
     Band none{nullptr, 0, 0, 0, 0};
-    BSSN_LAUNCH(KC_HORIZON_SURFACE, k_surface, (n + kHThreads - 1) / kHThreads, kHThreads, s, G, S, center[0],
+    BSSN_LAUNCH(KC_HORIZON_SURFACE, k_surface, (n + kSurfThreads - 1) / kSurfThreads, kSurfThreads, s, G, S, center[0],
                 center[1], center[2], trial, expansion, density, bad, none, 0.0);
     BSSN_LAUNCH(KC_HORIZON_SURFACE, k_surface_summary, 1, kSumThreads, s, direction ? (const double*)trial : radius,
                 expansion, density, bad, area_weights, n_theta, n_phi, summary);
@@ -794,13 +1087,10 @@ extern "C" int bssn_horizon_jacobian(const BssnHorizonGeometry* geometry, const 
     if (!workspace || workspace_bytes < bssn_horizon_workspace_bytes(n_theta, n_phi))
         return fail(BSSN_ERR_WORKSPACE, "bssn_horizon_jacobian: workspace too small");
     cudaStream_t s = (cudaStream_t)stream;
-    Band B = band_of(workspace, n_theta, n_phi);
-    char* rest = static_cast<char*>(workspace) + band_bytes(n_theta, n_phi);
-    double* expansion = reinterpret_cast<double*>(rest);
-    int* bad = reinterpret_cast<int*>(rest + (size_t)B.n * sizeof(double));
-    if ((st = assemble(G, center, radius, n_theta, n_phi, fd_step, B, expansion, bad, s)) != BSSN_OK) return st;
-    const long long total = (long long)B.n * B.n;
-    BSSN_LAUNCH(KC_HORIZON_SOLVE, k_band_dense, (unsigned)((total + 255) / 256), 256, s, B, dense);
+    const Factor F = factor_of(workspace, n_theta, n_phi);
+    if ((st = assemble(G, center, radius, n_theta, n_phi, fd_step, F.B, F.rhs, F.bad, s)) != BSSN_OK) return st;
+    const long long total = (long long)F.B.n * F.B.n;
+    BSSN_LAUNCH(KC_HORIZON_SOLVE, k_band_dense, (unsigned)((total + 255) / 256), 256, s, F.B, dense);
     return cuda_status(cudaGetLastError(), "bssn_horizon_jacobian");
 }
 
@@ -817,21 +1107,26 @@ extern "C" int bssn_horizon_newton_direction(const BssnHorizonGeometry* geometry
     if (!workspace || workspace_bytes < bssn_horizon_workspace_bytes(n_theta, n_phi))
         return fail(BSSN_ERR_WORKSPACE, "bssn_horizon_newton_direction: workspace too small");
     cudaStream_t s = (cudaStream_t)stream;
-    Band B = band_of(workspace, n_theta, n_phi);
-    char* rest = static_cast<char*>(workspace) + band_bytes(n_theta, n_phi);
-    double* diag = reinterpret_cast<double*>(rest);
-    int* bad = reinterpret_cast<int*>(rest + (size_t)B.n * sizeof(double));
-    // the band assembly writes its own copy of the expansion into delta, then
-    // the right-hand side -Theta replaces it
-    if ((st = assemble(G, center, radius, n_theta, n_phi, fd_step, B, delta, bad, s)) != BSSN_OK) return st;
-    BSSN_LAUNCH(KC_HORIZON_SOLVE, k_negate, (B.n + 255) / 256, 256, s, expansion, delta, B.n);
-    for (int k = 0; k < B.n; ++k) {
-        const int cols = std::min(B.n - 1, k + B.ku2) - k + 1;  // trailing columns plus the right-hand side
-        const unsigned blocks = (unsigned)((cols + kStepWarps - 1) / kStepWarps);
-        BSSN_LAUNCH(KC_HORIZON_SOLVE, k_band_step, blocks, kStepWarps * 32, s, B, k, delta, diag);
+    const Factor F = factor_of(workspace, n_theta, n_phi);
+    // the assembly's own expansion lands in rhs, which -Theta then replaces
+    if ((st = assemble(G, center, radius, n_theta, n_phi, fd_step, F.B, F.rhs, F.bad, s)) != BSSN_OK) return st;
+    BSSN_LAUNCH(KC_HORIZON_SOLVE, k_negate, (F.B.n + 255) / 256, 256, s, expansion, F.rhs, F.B.n);
+    cudaError_t e = cudaSuccess;
+    cudaGraphExec_t exec = nullptr;
+    // Replay the per-column launches as a CUDA graph unless per-kernel
+    // profiling is on (which times every launch with events of its own).
+    if (!profiling_enabled()) e = factor_graph(F, workspace, n_theta, n_phi, exec);
+    if (e != cudaSuccess) return cuda_status(e, "bssn_horizon_newton_direction (graph capture)");
+    if (exec) {
+        count_launches(F.B.n + 1);
+        e = cudaGraphLaunch(exec, s);
+    } else {
+        enqueue_factor(F, s);
+        e = cudaGetLastError();
     }
-    BSSN_LAUNCH(KC_HORIZON_SOLVE, k_band_back, 1, kBackThreads, s, B, delta, diag, summary);
-    return cuda_status(cudaGetLastError(), "bssn_horizon_newton_direction");
+    if (e == cudaSuccess) e = cudaMemcpyAsync(delta, F.rhs, (size_t)F.B.n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(summary, F.sum, 2 * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    return cuda_status(e, "bssn_horizon_newton_direction");
 }
 
 extern "C" int bssn_horizon_regrid(const double* radius, int32_t n_theta, int32_t n_phi, const double* theta,
