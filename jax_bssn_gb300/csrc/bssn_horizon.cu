@@ -48,7 +48,7 @@ namespace bssn {
 namespace {
 
 constexpr int kHThreads = 128;
-constexpr int kSurfThreads = 32;  // one node per thread; small blocks spread a surface over the SMs
+constexpr int kSurfWarps = 4;     // nodes (one warp each) per block of the surface kernel
 constexpr int kSumThreads = 1024;
 constexpr int kStepWarps = 2;      // columns per block of a factorisation step (spread over the SMs)
 constexpr int kBackThreads = 1024;
@@ -110,10 +110,19 @@ __device__ inline void unpack(const double (&v)[6], double (&M)[3][3]) {
     M[1][1] = v[3]; M[1][2] = M[2][1] = v[4]; M[2][2] = v[5];
 }
 
+__device__ __forceinline__ void warp_sum(double& v) {
+    // butterfly: every lane ends with the same, order-independent sum of pairs
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+}
+
 // gamma, d_gamma[k][i][j] = d_k gamma_ij, K and the resolved flag at a point
 // (apparent_horizon.py:65-98).  The upper triangle of each tensor is read.
+// S = 1: one thread samples the point; S = 32: the lanes of a warp split the
+// Hermite stencil and every lane ends with the whole result.
+template <int S>
 __device__ void sample_point(const HGeom& G, const double (&p)[3], double (&gam)[3][3], double (&dg)[3][3][3],
                              double (&K)[3][3], bool& inside) {
+    const int l0 = S == 1 ? 0 : (int)(threadIdx.x & 31);
     double idx[3], coord0 = 0.0;
     if (G.dims == 1) {
         coord0 = sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
@@ -121,13 +130,17 @@ __device__ void sample_point(const HGeom& G, const double (&p)[3], double (&gam)
         double w[6], dw[6];
         const int b = hermite(idx[0], G.n[0], w, dw);
         double v[4] = {0, 0, 0, 0}, d[2] = {0, 0};
-#pragma unroll
-        for (int a = 0; a < 6; ++a) {
+        for (int a = l0; a < 6; a += S) {
             const long long o = b + a;
             const double grr = G.g[o], gtt = G.g[4 * G.cs + o];
             v[0] += w[a] * grr; v[1] += w[a] * gtt;
             d[0] += dw[a] * grr; d[1] += dw[a] * gtt;
             v[2] += w[a] * G.k[o]; v[3] += w[a] * G.k[4 * G.cs + o];
+        }
+        if (S > 1) {
+            for (int q = 0; q < 4; ++q) warp_sum(v[q]);
+            warp_sum(d[0]);
+            warp_sum(d[1]);
         }
         d[0] /= G.spacing[0];
         d[1] /= G.spacing[0];
@@ -157,8 +170,9 @@ __device__ void sample_point(const HGeom& G, const double (&p)[3], double (&gam)
         const int b0 = hermite(idx[0], G.n[0], w0, d0);
         const int b1 = hermite(idx[1], G.n[1], w1, d1);
         double gv[6] = {0}, gr[6] = {0}, gz[6] = {0}, kv[6] = {0};
-        for (int a = 0; a < 6; ++a)
-            for (int c = 0; c < 6; ++c) {
+        for (int t = l0; t < 36; t += S) {
+            const int a = t / 6, c = t % 6;
+            {
                 const long long o = (long long)(b0 + a) * G.n[1] + (b1 + c);
                 const double ww = w0[a] * w1[c], wr = d0[a] * w1[c], wz = w0[a] * d1[c];
 #pragma unroll
@@ -168,6 +182,9 @@ __device__ void sample_point(const HGeom& G, const double (&p)[3], double (&gam)
                     kv[q] += ww * G.k[kSym[q] * G.cs + o];
                 }
             }
+        }
+        if (S > 1)
+            for (int q = 0; q < 6; ++q) { warp_sum(gv[q]); warp_sum(gr[q]); warp_sum(gz[q]); warp_sum(kv[q]); }
 #pragma unroll
         for (int q = 0; q < 6; ++q) { gr[q] /= G.spacing[0]; gz[q] /= G.spacing[1]; }
         double M[3][3], Mr[3][3], Mz[3][3], Kp[3][3];
@@ -206,11 +223,12 @@ __device__ void sample_point(const HGeom& G, const double (&p)[3], double (&gam)
         const int b1 = hermite(idx[1], G.n[1], w1, d1);
         const int b2 = hermite(idx[2], G.n[2], w2, d2);
         double gv[6] = {0}, gx[6] = {0}, gy[6] = {0}, gz[6] = {0}, kv[6] = {0};
-        for (int a = 0; a < 6; ++a)
-            for (int b = 0; b < 6; ++b) {
+        for (int t = l0; t < 216; t += S) {
+            const int a = t / 36, b = (t / 6) % 6, c = t % 6;
+            {
                 const long long row = ((long long)(b0 + a) * G.n[1] + (b1 + b)) * G.n[2] + b2;
                 const double wab = w0[a] * w1[b], xab = d0[a] * w1[b], yab = w0[a] * d1[b];
-                for (int c = 0; c < 6; ++c) {
+                {
                     const long long o = row + c;
                     const double ww = wab * w2[c], wx = xab * w2[c], wy = yab * w2[c], wz = wab * d2[c];
 #pragma unroll
@@ -220,6 +238,11 @@ __device__ void sample_point(const HGeom& G, const double (&p)[3], double (&gam)
                         kv[q] += ww * G.k[kSym[q] * G.cs + o];
                     }
                 }
+            }
+        }
+        if (S > 1)
+            for (int q = 0; q < 6; ++q) {
+                warp_sum(gv[q]); warp_sum(gx[q]); warp_sum(gy[q]); warp_sum(gz[q]); warp_sum(kv[q]);
             }
         double Dx[6], Dy[6], Dz[6];
 #pragma unroll
@@ -387,34 +410,50 @@ __device__ __forceinline__ double& band_at(const Band& B, int i, int j) {
     return B.a[(long long)j * B.ld + (i - j + B.ku2)];
 }
 
-// One node per thread: the surface, the node's bad flag, and (band != null)
-// the node's Jacobian row.
-__global__ void __launch_bounds__(kSurfThreads)
+// One warp per node: the surface, the node's bad flag, and (band != null) the
+// node's Jacobian row.  The lanes share each geometry sample; for the row,
+// lanes 1-10 evaluate the expansion with one angular derivative moved by -+ its
+// step (lane 0 the unmoved one) in a single pass, then two more samples give
+// the radial partial.
+__global__ void __launch_bounds__(kSurfWarps * 32)
 k_surface(HGeom G, Sphere S, double cx, double cy, double cz, double* __restrict__ trial,
           double* __restrict__ expansion, double* __restrict__ density, int* __restrict__ bad, Band B,
           double fd_step) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= S.nt * S.np) return;
+    const int lane = threadIdx.x & 31;
+    const int i = blockIdx.x * kSurfWarps + (threadIdx.x >> 5);
+    if (i >= S.nt * S.np) return;  // whole warp
     const int t = i / S.np, p = i % S.np;
     const double h = hval(S, t, p);
-    if (trial) trial[i] = h;
     double D[5];
     ang_derivs(S, t, p, D);
     const Frame F = frame(t, p, S.nt, S.np);
     double gam[3][3], dg[3][3][3], K[3][3];
     bool inside;
     double pt[3] = {cx + h * F.radial[0], cy + h * F.radial[1], cz + h * F.radial[2]};
-    sample_point(G, pt, gam, dg, K, inside);
+    sample_point<32>(G, pt, gam, dg, K, inside);
+    // lane 1 + 2m: D[m] + step, lane 2 + 2m: D[m] - step (m = 0..4)
+    double Dl[5] = {D[0], D[1], D[2], D[3], D[4]};
+    const int m = (lane - 1) >> 1;
+    if (B.a && lane >= 1 && lane <= 10) {
+        const double sc = fd_step * fmax(fabs(D[m]), 1.0);
+        Dl[m] = (lane & 1) ? D[m] + sc : D[m] - sc;
+    }
     double th, dens;
-    pointwise(h, D, F, gam, dg, K, th, &dens);
-    expansion[i] = th;
-    if (density) density[i] = dens;
-    const bool ok = inside && positive(gam) && isfinite(th) && isfinite(dens) && h > 0.0;
-    bad[i] = ok ? 0 : 1;
+    pointwise(h, Dl, F, gam, dg, K, th, &dens);
+    const double th0 = __shfl_sync(0xffffffffu, th, 0);
+    const double dens0 = __shfl_sync(0xffffffffu, dens, 0);
+    double tpm[10];
+#pragma unroll
+    for (int q = 0; q < 10; ++q) tpm[q] = __shfl_sync(0xffffffffu, th, q + 1);
+    if (lane == 0) {
+        if (trial) trial[i] = h;
+        expansion[i] = th0;
+        if (density) density[i] = dens0;
+        const bool ok = inside && positive(gam) && isfinite(th0) && isfinite(dens0) && h > 0.0;
+        bad[i] = ok ? 0 : 1;
+    }
     if (!B.a) return;
 
-    // pointwise partials (central differences): h with the geometry resampled,
-    // each angular derivative with the geometry fixed
     double part[6];
     {
         const double dh = fd_step * fmax(fabs(h), 1.0);
@@ -422,24 +461,19 @@ k_surface(HGeom G, Sphere S, double cx, double cy, double cz, double* __restrict
         bool in2;
         const double hp_ = h + dh, hm_ = h - dh;
         double q[3] = {cx + hp_ * F.radial[0], cy + hp_ * F.radial[1], cz + hp_ * F.radial[2]};
-        sample_point(G, q, gp, dgp, Kp, in2);
+        sample_point<32>(G, q, gp, dgp, Kp, in2);
         pointwise(hp_, D, F, gp, dgp, Kp, tp, nullptr);
         q[0] = cx + hm_ * F.radial[0]; q[1] = cy + hm_ * F.radial[1]; q[2] = cz + hm_ * F.radial[2];
-        sample_point(G, q, gp, dgp, Kp, in2);
+        sample_point<32>(G, q, gp, dgp, Kp, in2);
         pointwise(hm_, D, F, gp, dgp, Kp, tm, nullptr);
         part[0] = (tp - tm) / (2.0 * dh);
     }
-    for (int m = 0; m < 5; ++m) {
-        const double sc = fd_step * fmax(fabs(D[m]), 1.0);
-        double Dp[5], Dm[5];
-        for (int q = 0; q < 5; ++q) { Dp[q] = D[q]; Dm[q] = D[q]; }
-        Dp[m] = D[m] + sc;
-        Dm[m] = D[m] - sc;
-        double tp, tm;
-        pointwise(h, Dp, F, gam, dg, K, tp, nullptr);
-        pointwise(h, Dm, F, gam, dg, K, tm, nullptr);
-        part[m + 1] = (tp - tm) / (2.0 * sc);
+#pragma unroll
+    for (int mm = 0; mm < 5; ++mm) {
+        const double sc = fd_step * fmax(fabs(D[mm]), 1.0);
+        part[mm + 1] = (tpm[2 * mm] - tpm[2 * mm + 1]) / (2.0 * sc);
     }
+    if (lane != 0) return;
 
     // row i of the Jacobian: diagonal plus the partials times the stencils
     const double dth = rdiv(kPi, (double)S.nt), dph = rdiv(2.0 * kPi, (double)S.np);
@@ -651,6 +685,171 @@ k_band_step_fused(Band B, int k, int search, double* __restrict__ rhs, double* _
     pdl_release();
 }
 
+// Blocked form: one launch factors kPanel columns.  Every block factors the
+// panel (rows c0 .. c0 + kl + kPanel - 1 of columns c0 .. c0 + kPanel - 1) in
+// shared memory from a copy the previous launch left in `pin` (the same pivot
+// rule, swaps and eliminations as the column steps, in the same order), then
+// each warp applies the panel's swaps and eliminations to one trailing column
+// (or the right-hand side) held in shared memory.  The warps whose columns
+// form the next panel also write them to `pout`; block 0 writes the panel's U
+// rows and pivots back.  Needs kl + kPanel <= kPanelRows.
+constexpr int kPanel = 8;
+constexpr int kPanelWarps = 4;
+constexpr int kPanelRows = 384;
+
+__global__ void __launch_bounds__(kPanelWarps * 32)
+k_band_panel(Band B, int c0, const double* __restrict__ pin, double* __restrict__ pout, double* __restrict__ rhs,
+             double* __restrict__ diag) {
+    pdl_enter();
+    __shared__ double Ps[kPanel][kPanelRows];
+    __shared__ double Cs[kPanelWarps][kPanelRows];
+    __shared__ int s_po[kPanel];
+    __shared__ double s_rp[kPanel], s_akk[kPanel], s_piv[kPanel], s_xk[kPanel], s_xp[kPanel];
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int P = B.kl + kPanel;
+    const int nrow = min(P, B.n - c0);
+    const int ncol = min(kPanel, B.n - c0);
+    {
+        constexpr int kQ = (kPanelRows + kPanelWarps * 32 - 1) / (kPanelWarps * 32);
+        double v[kPanel][kQ];  // every load issued before any is used
+#pragma unroll
+        for (int jj = 0; jj < kPanel; ++jj)
+#pragma unroll
+            for (int q = 0; q < kQ; ++q) {
+                const int o = tid + q * kPanelWarps * 32;
+                v[jj][q] = (jj < ncol && o < nrow) ? pin[jj * P + o] : 0.0;
+            }
+#pragma unroll
+        for (int jj = 0; jj < kPanel; ++jj)
+#pragma unroll
+            for (int q = 0; q < kQ; ++q) {
+                const int o = tid + q * kPanelWarps * 32;
+                if (o < P) Ps[jj][o] = v[jj][q];
+            }
+    }
+    __syncthreads();
+    for (int jj = 0; jj < ncol; ++jj) {
+        const int omax = min(nrow - 1, jj + B.kl);
+        if (w == 0) {
+            double best = -1.0;
+            int arg = jj;
+            for (int o = jj + lane; o <= omax; o += 32) {
+                const double v = fabs(Ps[jj][o]);
+                if (v > best) { best = v; arg = o; }
+            }
+            for (int sh = 16; sh > 0; sh >>= 1) {
+                const double ob = __shfl_xor_sync(0xffffffffu, best, sh);
+                const int oa = __shfl_xor_sync(0xffffffffu, arg, sh);
+                if (ob > best || (ob == best && oa < arg)) { best = ob; arg = oa; }
+            }
+            if (lane == 0) {
+                s_po[jj] = arg;
+                s_piv[jj] = Ps[jj][arg];
+                s_akk[jj] = Ps[jj][jj];
+                s_rp[jj] = 1.0 / Ps[jj][arg];
+            }
+            // rows jj and po of the later panel columns, before any is rewritten
+            if (lane > jj && lane < ncol) {
+                s_xk[lane] = Ps[lane][jj];
+                s_xp[lane] = Ps[lane][arg];
+            }
+        }
+        __syncthreads();
+        const int po = s_po[jj];
+        const double rp = s_rp[jj], akk = s_akk[jj];
+        // per row: the multiplier into column jj, then the swap and elimination
+        // of the later panel columns
+        for (int o = jj + 1 + tid; o <= omax; o += blockDim.x) {
+            const double l = (o == po ? akk : Ps[jj][o]) * rp;
+            Ps[jj][o] = l;
+            for (int jc = jj + 1; jc < ncol; ++jc) Ps[jc][o] = (o == po ? s_xk[jc] : Ps[jc][o]) - l * s_xp[jc];
+        }
+        if (tid == 0) {
+            Ps[jj][jj] = s_piv[jj];
+            for (int jc = jj + 1; jc < ncol; ++jc) Ps[jc][jj] = s_xp[jc];
+        }
+        __syncthreads();
+    }
+
+    // trailing columns (and the right-hand side)
+    const int first = c0 + ncol;
+    const int lastc = min(B.n - 1, c0 + ncol - 1 + B.ku2);
+    const int ntrail = lastc >= first ? lastc - first + 1 : 0;
+    const int idx = blockIdx.x * kPanelWarps + w;
+    if (idx <= ntrail) {
+        const bool is_rhs = idx == ntrail;
+        const int j = first + idx;
+        double* col = is_rhs ? rhs : B.a + (long long)j * B.ld + (B.ku2 - j);  // col[r] = A(r, j)
+        const int rlo = is_rhs ? 0 : j - B.ku2;                                 // rows inside the band
+        const int rhi = is_rhs ? B.n - 1 : min(B.n - 1, j + B.kl);
+        double* cs = Cs[w];
+        {
+            constexpr int kQ = kPanelRows / 32;
+            double v[kQ];
+#pragma unroll
+            for (int q = 0; q < kQ; ++q) {
+                const int o = lane + 32 * q, r = c0 + o;
+                v[q] = (o < nrow && r >= rlo && r <= rhi) ? col[r] : 0.0;
+            }
+#pragma unroll
+            for (int q = 0; q < kQ; ++q) {
+                const int o = lane + 32 * q;
+                if (o < nrow) cs[o] = v[q];
+            }
+        }
+        __syncwarp();
+        for (int jj = 0; jj < ncol; ++jj) {
+            const int po = s_po[jj];
+            if (lane == 0 && po != jj) {
+                const double t = cs[jj];
+                cs[jj] = cs[po];
+                cs[po] = t;
+            }
+            __syncwarp();
+            const double xc = cs[jj];
+            const int omax = min(nrow - 1, jj + B.kl);
+            for (int o = jj + 1 + lane; o <= omax; o += 32) cs[o] -= Ps[jj][o] * xc;
+            __syncwarp();
+        }
+        for (int o = lane; o < nrow; o += 32) {
+            const int r = c0 + o;
+            if (r >= rlo && r <= rhi) col[r] = cs[o];
+        }
+        // the next panel's copy
+        const int nc0 = first;
+        if (!is_rhs && j < nc0 + kPanel) {
+            const int nrow2 = min(P, B.n - nc0);
+            double* dst = pout + (long long)(j - nc0) * P;
+            for (int o = lane; o < nrow2; o += 32) {
+                const int r = nc0 + o;
+                const int local = r - c0;
+                double v = 0.0;
+                if (r >= rlo && r <= rhi) v = local < nrow ? cs[local] : col[r];
+                dst[o] = v;
+            }
+        }
+    }
+    if (blockIdx.x == 0) {
+        // U rows c0 .. c of each panel column c, and its pivot
+        if (tid < ncol)
+            for (int o = 0; o <= tid; ++o) B.a[(long long)(c0 + tid) * B.ld + (o - tid + B.ku2)] = Ps[tid][o];
+        if (tid < ncol) diag[c0 + tid] = s_piv[tid];
+    }
+    pdl_release();
+}
+
+// Copy of the first panel (columns 0 .. kPanel - 1, rows 0 .. kl + kPanel - 1).
+__global__ void k_panel_init(Band B, double* __restrict__ pout) {
+    const int P = B.kl + kPanel;
+    const int nrow = min(P, B.n), ncol = min(kPanel, B.n);
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < kPanel * P; e += gridDim.x * blockDim.x) {
+        const int jj = e / P, o = e % P;
+        double v = 0.0;
+        if (jj < ncol && o < nrow && o - jj <= B.kl) v = B.a[(long long)jj * B.ld + (o - jj + B.ku2)];
+        pout[e] = v;
+    }
+}
+
 // Back substitution with y and 1/U_kk in shared memory: thread t owns the row
 // k - 1 - t of column k, whose U entries stream in kPrefetch steps ahead.
 constexpr int kPrefetch = 8;
@@ -775,7 +974,7 @@ __global__ void k_sample(HGeom G, const double* __restrict__ points, long long n
     const double p[3] = {points[3 * t], points[3 * t + 1], points[3 * t + 2]};
     double gam[3][3], dg[3][3][3], K[3][3];
     bool inside;
-    sample_point(G, p, gam, dg, K, inside);
+    sample_point<1>(G, p, gam, dg, K, inside);
     for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j) {
             if (gamma) gamma[9 * t + 3 * i + j] = gam[i][j];
@@ -900,7 +1099,10 @@ struct Factor {
     Band B;
     double *diag, *rhs, *sum;
     int *bad, *piv;
+    double* panel[2];  // double-buffered copies of the next panel (blocked form)
 };
+
+size_t panel_doubles(const Band& B) { return (size_t)kPanel * (B.kl + kPanel); }
 
 Factor factor_of(void* ws, int nt, int np) {
     Factor F;
@@ -911,6 +1113,9 @@ Factor factor_of(void* ws, int nt, int np) {
     F.sum = F.rhs + F.B.n;
     F.bad = reinterpret_cast<int*>(F.sum + 2);
     F.piv = F.bad + F.B.n;
+    const size_t off = ((size_t)(reinterpret_cast<char*>(F.piv + F.B.n) - static_cast<char*>(ws)) + 15) & ~(size_t)15;
+    F.panel[0] = reinterpret_cast<double*>(static_cast<char*>(ws) + off);
+    F.panel[1] = F.panel[0] + panel_doubles(F.B);
     return F;
 }
 
@@ -939,7 +1144,24 @@ void launch_dependent(void (*kernel)(P...), unsigned blocks, unsigned threads, s
 int enqueue_factor(const Factor& F, cudaStream_t s) {
     const Band& B = F.B;
     const bool fused = B.kl + 2 <= 32 * kRowsPerLane;
-    for (int k = 0; k < B.n; ++k) {
+    const bool blocked = B.kl + kPanel <= kPanelRows;
+    int launches = 0;
+    if (blocked) {
+        const int P = B.kl + kPanel;
+        BSSN_LAUNCH(KC_HORIZON_SOLVE, k_panel_init, (kPanel * P + 255) / 256, 256, s, B, F.panel[0]);
+        ++launches;
+        for (int c0 = 0, p = 0; c0 < B.n; c0 += kPanel, ++p) {
+            const int ncol = std::min(kPanel, B.n - c0);
+            const int first = c0 + ncol;
+            const int lastc = std::min(B.n - 1, c0 + ncol - 1 + B.ku2);
+            const int ntrail = lastc >= first ? lastc - first + 1 : 0;
+            const unsigned blocks = (unsigned)((ntrail + 1 + kPanelWarps - 1) / kPanelWarps);
+            launch_dependent(k_band_panel, blocks, kPanelWarps * 32, 0, s, B, c0, (const double*)F.panel[p % 2],
+                             F.panel[(p + 1) % 2], F.rhs, F.diag);
+            ++launches;
+        }
+    }
+    for (int k = 0; !blocked && k < B.n; ++k) {
         const int cols = std::min(B.n - 1, k + B.ku2) - k + 1;  // trailing columns plus the right-hand side
         const unsigned blocks = (unsigned)((cols + kStepWarps - 1) / kStepWarps);
         if (fused)
@@ -947,6 +1169,7 @@ int enqueue_factor(const Factor& F, cudaStream_t s) {
                              F.piv);
         else
             launch_dependent(k_band_step, blocks, kStepWarps * 32, 0, s, B, k, F.rhs, F.diag);
+        ++launches;
     }
     const size_t smem = 2 * (size_t)B.n * sizeof(double);
     if (smem <= (size_t)kBackSmemMax && B.ku2 <= kBackThreads) {
@@ -959,7 +1182,7 @@ int enqueue_factor(const Factor& F, cudaStream_t s) {
     } else {
         launch_dependent(k_band_back, 1, kBackThreads, 0, s, B, F.rhs, F.diag, F.sum);
     }
-    return B.n + 1;
+    return launches + 1;
 }
 
 // Instantiated factorisation graphs per thread, keyed by device, workspace
@@ -967,9 +1190,10 @@ int enqueue_factor(const Factor& F, cudaStream_t s) {
 struct FactorGraphs {
     cudaStream_t capture = nullptr;
     std::map<std::tuple<int, void*, int, int>, cudaGraphExec_t> execs;
+    std::map<std::tuple<int, void*, int, int>, int> launches;
 };
 
-cudaError_t factor_graph(const Factor& F, void* ws, int nt, int np, cudaGraphExec_t& out) {
+cudaError_t factor_graph(const Factor& F, void* ws, int nt, int np, cudaGraphExec_t& out, int& launches) {
     thread_local FactorGraphs graphs;
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -978,11 +1202,13 @@ cudaError_t factor_graph(const Factor& F, void* ws, int nt, int np, cudaGraphExe
     auto it = graphs.execs.find(key);
     if (it != graphs.execs.end()) {
         out = it->second;
+        launches = graphs.launches[key];
         return cudaSuccess;
     }
     if (graphs.execs.size() >= 16) {
         for (auto& kv : graphs.execs) cudaGraphExecDestroy(kv.second);
         graphs.execs.clear();
+        graphs.launches.clear();
     }
     if (!graphs.capture) {
         e = cudaStreamCreateWithFlags(&graphs.capture, cudaStreamNonBlocking);
@@ -990,8 +1216,9 @@ cudaError_t factor_graph(const Factor& F, void* ws, int nt, int np, cudaGraphExe
     }
     e = cudaStreamBeginCapture(graphs.capture, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return e;
-    const int launches = enqueue_factor(F, graphs.capture);
-    count_launches(-launches);  // recorded, not run
+    const int recorded = enqueue_factor(F, graphs.capture);
+    count_launches(-recorded);  // recorded, not run
+    graphs.launches[key] = recorded;
     cudaGraph_t graph = nullptr;
     e = cudaStreamEndCapture(graphs.capture, &graph);
     cudaGraphExec_t exec = nullptr;
@@ -1000,6 +1227,7 @@ cudaError_t factor_graph(const Factor& F, void* ws, int nt, int np, cudaGraphExe
     if (e != cudaSuccess) return e;
     graphs.execs[key] = exec;
     out = exec;
+    launches = graphs.launches[key];
     return cudaSuccess;
 }
 
@@ -1008,8 +1236,8 @@ int assemble(const HGeom& G, const double center[3], const double* radius, int n
     Sphere S{nt, np, radius, nullptr, 0.0};
     cudaError_t e = cudaMemsetAsync(B.a, 0, (size_t)B.n * B.ld * sizeof(double), s);
     if (e != cudaSuccess) return cuda_status(e, "bssn_horizon: band clear");
-    const unsigned blocks = (unsigned)((B.n + kSurfThreads - 1) / kSurfThreads);
-    BSSN_LAUNCH(KC_HORIZON_SURFACE, k_surface, blocks, kSurfThreads, s, G, S, center[0], center[1], center[2],
+    const unsigned blocks = (unsigned)((B.n + kSurfWarps - 1) / kSurfWarps);
+    BSSN_LAUNCH(KC_HORIZON_SURFACE, k_surface, blocks, kSurfWarps * 32, s, G, S, center[0], center[1], center[2],
                 (double*)nullptr, expansion, (double*)nullptr, bad, B, fd_step);
     return cuda_status(cudaGetLastError(), "bssn_horizon: jacobian");
 }
@@ -1047,7 +1275,8 @@ extern "C" int bssn_horizon_angular_derivatives(const double* radius, int32_t n_
 extern "C" size_t bssn_horizon_workspace_bytes(int32_t n_theta, int32_t n_phi) {
     if (n_theta < 6 || n_phi < 6 || n_phi % 2 || (long long)n_theta * n_phi > (1 << 22)) return 0;
     const size_t n = (size_t)n_theta * n_phi;
-    return band_bytes(n_theta, n_phi) + 2 * n * sizeof(double) + 2 * sizeof(double) + 2 * n * sizeof(int);
+    return band_bytes(n_theta, n_phi) + 2 * n * sizeof(double) + 2 * sizeof(double) + 2 * n * sizeof(int) + 16 +
+           2 * panel_doubles(band_of(nullptr, n_theta, n_phi)) * sizeof(double);
 }
 
 extern "C" int bssn_horizon_surface(const BssnHorizonGeometry* geometry, const double center[3],
@@ -1069,7 +1298,7 @@ extern "C" int bssn_horizon_surface(const BssnHorizonGeometry* geometry, const d
     int* bad = static_cast<int*>(workspace);
     Sphere S{n_theta, n_phi, radius, direction, step};
     Band none{nullptr, 0, 0, 0, 0};
-    BSSN_LAUNCH(KC_HORIZON_SURFACE, k_surface, (n + kSurfThreads - 1) / kSurfThreads, kSurfThreads, s, G, S, center[0],
+    BSSN_LAUNCH(KC_HORIZON_SURFACE, k_surface, (n + kSurfWarps - 1) / kSurfWarps, kSurfWarps * 32, s, G, S, center[0],
                 center[1], center[2], trial, expansion, density, bad, none, 0.0);
     BSSN_LAUNCH(KC_HORIZON_SURFACE, k_surface_summary, 1, kSumThreads, s, direction ? (const double*)trial : radius,
                 expansion, density, bad, area_weights, n_theta, n_phi, summary);
@@ -1113,12 +1342,13 @@ extern "C" int bssn_horizon_newton_direction(const BssnHorizonGeometry* geometry
     BSSN_LAUNCH(KC_HORIZON_SOLVE, k_negate, (F.B.n + 255) / 256, 256, s, expansion, F.rhs, F.B.n);
     cudaError_t e = cudaSuccess;
     cudaGraphExec_t exec = nullptr;
-    // Replay the per-column launches as a CUDA graph unless per-kernel
+    int launches = 0;
+    // Replay the factorisation's launches as a CUDA graph unless per-kernel
     // profiling is on (which times every launch with events of its own).
-    if (!profiling_enabled()) e = factor_graph(F, workspace, n_theta, n_phi, exec);
+    if (!profiling_enabled()) e = factor_graph(F, workspace, n_theta, n_phi, exec, launches);
     if (e != cudaSuccess) return cuda_status(e, "bssn_horizon_newton_direction (graph capture)");
     if (exec) {
-        count_launches(F.B.n + 1);
+        count_launches(launches);
         e = cudaGraphLaunch(exec, s);
     } else {
         enqueue_factor(F, s);
