@@ -850,9 +850,13 @@ __global__ void k_panel_init(Band B, double* __restrict__ pout) {
     }
 }
 
-// Back substitution with y and 1/U_kk in shared memory: thread t owns the row
-// k - 1 - t of column k, whose U entries stream in kPrefetch steps ahead.
-constexpr int kPrefetch = 8;
+// Back substitution with y and 1/U_kk in shared memory, eight columns per
+// pair of barriers: warp 0 solves the block's 8 x 8 triangle in registers
+// (lane l holds row kl0 + l), then thread t subtracts the block's unknowns
+// from row kl0 - 1 - t.  Every row receives its column terms in the same
+// (descending) order as one column at a time.  The next block's U entries
+// are loaded while the current one is solved.
+constexpr int kBackBlock = 8;
 constexpr int kBackSmemMax = 200 * 1024;
 
 __global__ void __launch_bounds__(kBackThreads)
@@ -861,55 +865,82 @@ k_band_back_shared(Band B, double* __restrict__ y, const double* __restrict__ di
     extern __shared__ double sm[];
     double* sy = sm;
     double* srd = sm + B.n;
-    __shared__ double s_x;
+    __shared__ double sx[kBackBlock];
     __shared__ double s_max[kBackThreads], s_bad[kBackThreads];
-    for (int i = threadIdx.x; i < B.n; i += blockDim.x) {
+    const int t = threadIdx.x, lane = t & 31;
+    for (int i = t; i < B.n; i += blockDim.x) {
         sy[i] = y[i];
         srd[i] = 1.0 / diag[i];
     }
-    const int t = threadIdx.x;
-    const bool active = t < B.ku2;
-    double pre[kPrefetch];
+    // U entries of the block ending at column kh: pd[cl] = U(kl0 + lane, kl0 + cl)
+    // above the diagonal (warp 0), pu[j] = U(kl0 - 1 - t, kh - j)
+    auto load = [&](int kh, double (&pd)[kBackBlock], double (&pu)[kBackBlock]) {
+        const int kl0 = max(0, kh - kBackBlock + 1);
 #pragma unroll
-    for (int d = 0; d < kPrefetch; ++d) {
-        const int k = B.n - 1 - d;
-        pre[d] = (active && k >= 0 && k - 1 - t >= 0) ? B.a[(long long)k * B.ld + (B.ku2 - 1 - t)] : 0.0;
-    }
-    __syncthreads();
-    for (int k = B.n - 1; k >= 0; --k) {
-        if (t == 0) {
-            const double x = sy[k] * srd[k];
-            sy[k] = x;
-            s_x = x;
+        for (int cl = 0; cl < kBackBlock; ++cl) {
+            const int r = kl0 + lane, c = kl0 + cl;
+            pd[cl] = (t < 32 && c > r && c <= kh) ? B.a[(long long)c * B.ld + (r - c + B.ku2)] : 0.0;
         }
-        const double a = pre[0];
 #pragma unroll
-        for (int d = 0; d + 1 < kPrefetch; ++d) pre[d] = pre[d + 1];
-        const int kn = k - kPrefetch;
-        pre[kPrefetch - 1] = (active && kn >= 0 && kn - 1 - t >= 0) ? B.a[(long long)kn * B.ld + (B.ku2 - 1 - t)] : 0.0;
+        for (int j = 0; j < kBackBlock; ++j) {
+            const int r = kl0 - 1 - t, c = kh - j;
+            pu[j] = (t < B.ku2 && r >= 0 && c >= kl0 && c - r <= B.ku2) ? B.a[(long long)c * B.ld + (r - c + B.ku2)]
+                                                                       : 0.0;
+        }
+    };
+    double pd[kBackBlock], pu[kBackBlock], nd[kBackBlock], nu[kBackBlock];
+    int kh = B.n - 1;
+    load(kh, pd, pu);
+    __syncthreads();
+    while (kh >= 0) {
+        const int kl0 = max(0, kh - kBackBlock + 1), nb = kh - kl0 + 1, khn = kl0 - 1;
+        if (khn >= 0) load(khn, nd, nu);
+        if (t < 32) {
+            double yv = lane < nb ? sy[kl0 + lane] : 0.0;
+#pragma unroll
+            for (int cl = kBackBlock - 1; cl >= 0; --cl) {
+                if (cl >= nb) continue;
+                const double x = __shfl_sync(0xffffffffu, yv, cl) * srd[kl0 + cl];
+                if (lane == cl) yv = x;
+                else if (lane < cl) yv -= pd[cl] * x;
+            }
+            if (lane < nb) {
+                sy[kl0 + lane] = yv;
+                sx[lane] = yv;
+            }
+        }
         __syncthreads();
-        const int r = k - 1 - t;
-        if (active && r >= 0) sy[r] -= a * s_x;
+        const int r = kl0 - 1 - t;
+        if (t < B.ku2 && r >= 0) {
+            double v = sy[r];
+#pragma unroll
+            for (int j = 0; j < kBackBlock; ++j)
+                if (j < nb) v -= pu[j] * sx[nb - 1 - j];
+            sy[r] = v;
+        }
         __syncthreads();
+        kh = khn;
+#pragma unroll
+        for (int q = 0; q < kBackBlock; ++q) { pd[q] = nd[q]; pu[q] = nu[q]; }
     }
-    double mx = 0.0, nb = 0.0;
-    for (int i = threadIdx.x; i < B.n; i += blockDim.x) {
+    double mx = 0.0, nbad = 0.0;
+    for (int i = t; i < B.n; i += blockDim.x) {
         const double v = sy[i];
         y[i] = v;
-        if (!isfinite(v)) nb += 1.0;
+        if (!isfinite(v)) nbad += 1.0;
         else mx = fmax(mx, fabs(v));
     }
-    s_max[threadIdx.x] = mx;
-    s_bad[threadIdx.x] = nb;
+    s_max[t] = mx;
+    s_bad[t] = nbad;
     __syncthreads();
     for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if (threadIdx.x < w) {
-            s_max[threadIdx.x] = fmax(s_max[threadIdx.x], s_max[threadIdx.x + w]);
-            s_bad[threadIdx.x] += s_bad[threadIdx.x + w];
+        if (t < w) {
+            s_max[t] = fmax(s_max[t], s_max[t + w]);
+            s_bad[t] += s_bad[t + w];
         }
         __syncthreads();
     }
-    if (threadIdx.x == 0) { out[0] = s_max[0]; out[1] = s_bad[0]; }
+    if (t == 0) { out[0] = s_max[0]; out[1] = s_bad[0]; }
 }
 
 // x = U^-1 y by columns: x_k = y_k / U_kk, then y_r -= U_rk x_k above it.
