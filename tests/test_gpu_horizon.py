@@ -237,9 +237,10 @@ def test_jacobian_matches_oracle(ah, layout):
     assert not np.any(got[~pattern])
 
 
-# (6, 130): band too wide for the fused pivot step; (6, 200): upper band too
-# wide for the shared-memory back substitution
-@pytest.mark.parametrize("shape", [(6, 12), (8, 16), (12, 24), (24, 48), (6, 130), (6, 200)])
+# (6, 126): band too wide for the panel kernel (column steps with the folded
+# pivot search); (6, 130): too wide for those too (plain column steps);
+# (6, 200): upper band too wide for the shared-memory back substitution
+@pytest.mark.parametrize("shape", [(6, 12), (8, 16), (12, 24), (24, 48), (6, 126), (6, 130), (6, 200)])
 def test_band_solve_matches_dense_solve(ah, shape):
     axes, gamma, kij, _, exact = layout_case("plane", "kerr_schild")
     table, _ = ah.build_geometry(axes, gamma, kij)
@@ -275,3 +276,17 @@ def test_surface_summary(ah):
     assert total == pytest.approx(h.sum(), rel=1.e-14)
     assert peak == pytest.approx(np.max(np.abs(exp)), rel=1.e-11)
     assert area == pytest.approx(float(np.sum(weights[:, None] * dens) * (2 * np.pi / 24)), rel=1.e-12)
+
+
+def test_invalid_surfaces_raise(ah):
+    dev = torch.device("cuda")
+    with pytest.raises(ValueError, match="six nodes"):
+        ah.angular_derivatives(torch.ones((5, 12), dtype=torch.float64, device=dev))
+    with pytest.raises(ValueError, match="even n_phi"):
+        ah.angular_derivatives(torch.ones((6, 13), dtype=torch.float64, device=dev))
+    with pytest.raises(ValueError, match="output grid"):
+        ah.interpolate_angular(torch.ones((6, 12), dtype=torch.float64, device=dev), np.zeros(0), np.zeros(3))
+    r, gamma, kij = schwarzschild_line()
+    table, _ = ah.build_geometry((r,), gamma, kij)
+    with pytest.raises(ValueError, match="six nodes"):
+        ah.surface(torch.ones((6, 7), dtype=torch.float64, device=dev), np.zeros(3), table)
