@@ -13,10 +13,13 @@ KEYS = ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "
         "vs_baseline", "dtype", "data", "config", "impl", "cpu_baseline", "e2e")
 
 
-@pytest.mark.parametrize("workload", ["teukolsky", "puncture", "puncture_axi"])
-def test_reference_arm_line(workload):
+# the horizon case runs on a 64^3 volume: the find's cost does not depend on it
+@pytest.mark.parametrize("workload,extra", [("teukolsky", []), ("puncture", []), ("puncture_axi", []),
+                                            ("horizon", ["--n", "64"])])
+def test_reference_arm_line(workload, extra):
     out = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--workload", workload, "--steps", "1",
-                          "--warmup", "1"], cwd=ROOT, capture_output=True, text=True, timeout=600, check=True)
+                          "--warmup", "1", *extra], cwd=ROOT, capture_output=True, text=True, timeout=600,
+                         check=True)
     lines = [line for line in out.stdout.splitlines() if line.startswith("{")]
     assert len(lines) == 1
     d = json.loads(lines[0])
