@@ -725,15 +725,16 @@ def run_horizon(args, world, rank, local):
         if "hbm_gbs" in peaks:
             hbm_peak, peak_src = float(peaks["hbm_gbs"]), "measured"
     achieved = nbytes / (sms / 1e3) / 1e9 if sms > 0 else None
-    roofline = {"bound": "hbm", "kernel": "k_band_step", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+    roofline = {"bound": "hbm", "kernel": "k_band_panel", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved / hbm_peak if achieved else None, "traffic": None, "peak_source": peak_src,
                 "kernel_share": sms / total, "kernel_ms_per_launch": sms / max(slaunch, 1),
                 "algorithmic_bytes_per_find": nbytes,
-                "note": "one launch per band column; the band (at most 32 MB) stays in L2, so the factorisation is "
-                        "bound by launch latency, not by HBM or the FP64 pipe"}
+                "note": "band LU in 8-column panels, one dependent launch each (the horizon_solve class also holds "
+                        "the back substitution); the band (at most 32 MB) stays in L2, so the factorisation is bound "
+                        "by the per-column latency of the panel factorisation, not by HBM or the FP64 pipe"}
     peak = _native.fma_peak_gflops(_native.PRECISION_F64) / 1e3
     fl = flops / (sms / 1e3) / 1e12 if sms > 0 else None
-    compute = {"bound": "fp64", "kernel": "k_band_step", "achieved": fl, "peak": peak, "unit": "TFLOP/s",
+    compute = {"bound": "fp64", "kernel": "k_band_panel", "achieved": fl, "peak": peak, "unit": "TFLOP/s",
                "frac": fl / peak if fl else None, "flops_per_find": flops,
                "peak_source": "measured live by bssn_probe_fma_peak"}
     e2e = None
