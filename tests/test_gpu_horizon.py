@@ -290,3 +290,33 @@ def test_invalid_surfaces_raise(ah):
     table, _ = ah.build_geometry((r,), gamma, kij)
     with pytest.raises(ValueError, match="six nodes"):
         ah.surface(torch.ones((6, 7), dtype=torch.float64, device=dev), np.zeros(3), table)
+
+
+def test_horizon_of_puncture_data_matches_oracle(ah):
+    """Brill-Lindquist data from the GPU puncture kernels, physical metric
+    psi^4 delta_ij and K = 0, searched about one of two punctures; the oracle
+    runs the same finder on the oracle's own puncture data."""
+    from jax_bssn_gb300.utilities import bowen_york_solver as by
+    from oracle import puncture as op
+    masses, positions = [0.5, 0.5], [[0.0, 0.0, -1.0], [0.0, 0.0, 1.0]]
+    grid, dx = by.cell_centered_grid(96, 1.5)
+    psi = by.brill_lindquist_conformal_factor(masses, positions, grid)
+    gamma = psi[None, None] ** 4 * torch.eye(3, dtype=torch.float64, device=psi.device)[:, :, None, None, None]
+    kij = torch.zeros_like(gamma)
+    axis = grid[:, 0, 0, 0].cpu().numpy()
+    # the horizon sits 8 cells from a 1/r puncture: the C1 geometry limits the
+    # angular audit to a few 1e-4, so its tolerance is loosened
+    options = dict(center=(0.0, 0.0, -1.0), initial_radius=0.3, n_theta=6, n_phi=12, max_angular=24,
+                   audit_tolerance=2.e-3)
+    got = ah.find_apparent_horizon((axis, axis, axis), gamma.contiguous(), kij, **options)
+    hgrid, _ = op.cell_centered_grid(96, 1.5)
+    hpsi = op.brill_lindquist_conformal_factor(masses, positions, hgrid)
+    hgamma = hpsi[None, None] ** 4 * np.eye(3)[:, :, None, None, None]
+    want = H.find_apparent_horizon((axis, axis, axis), hgamma, np.zeros_like(hgamma), **options)
+    assert got["residual"] < 1.e-8 and got["audit_residual"] < 2.e-3
+    assert got["radius"].shape == want["radius"].shape
+    np.testing.assert_allclose(got["radius"], want["radius"], rtol=0, atol=1.e-7)
+    np.testing.assert_allclose(got["mass"], want["mass"], rtol=1.e-7)
+    # an isolated hole of mass 0.5 would have area mass 0.5 at coordinate radius 0.25;
+    # the companion raises both a little
+    assert 0.5 < got["mass"] < 0.6 and 0.2 < got["radius"].mean() < 0.35
