@@ -122,8 +122,11 @@ int bssn_rhs(const BssnFields* in, BssnFields* out, const int32_t shape[3],
  * Limit: (nx+8)*(ny+8)*(nz+8) <= 21952 samples (e.g. 20x20x20); larger arrays
  * return BSSN_ERR_INVALID.  The first call on each device looks up the
  * array's device address with that device current; make that first call
- * before any stream capture.  All calls share the one array, so calls that
- * overlap on the GPU (different streams or threads) race; serialise them. */
+ * before any stream capture.  The looked-up address is kept per device index
+ * and belongs to the device's primary context (the CUDA runtime's): it does
+ * not survive cudaDeviceReset, and a caller's own driver context must not be
+ * current.  All calls share the one array, so calls that overlap on the GPU
+ * (different streams or threads) race; serialise them. */
 int bssn_rhs_noalloc(const BssnFields* in, BssnFields* out, const int32_t shape[3],
                      const BssnParams* params, void* stream);
 
@@ -185,7 +188,8 @@ typedef struct BssnFmrPatch {
 /* Workspace for bssn_fmr_rk4_step / bssn_fmr_stage_rhs on this hierarchy. */
 size_t bssn_fmr_workspace_bytes(const BssnFmrPatch* patches, const BssnParams* params, int32_t npatch);
 /* refresh_bssn_halos of one single-tile patch: periodic self-wrap, linear
- * exterior on Sommerfeld faces (JAX_BSSN/parallel/communication.py:144-214). */
+ * exterior on Sommerfeld faces (refresh_bssn_halos, JAX_BSSN/parallel/evolution.py:74-92;
+ * the single-tile sweep of JAX_BSSN/parallel/communication.py:36-106). */
 int bssn_fmr_refresh(double* state, const int32_t n[3], const int32_t codes[6], void* stream);
 /* fill_tiled_fine_ghosts (JAX_BSSN/fmr/transfer.py:237-244): six-node Lagrange
  * prolongation of the prepared parent into the child's exterior shell. */
@@ -195,20 +199,20 @@ int bssn_fmr_prolong(const double* parent, const int32_t parent_n[3], double* ch
  * coincident owned fine vertices into the parent. */
 int bssn_fmr_inject(double* parent, const int32_t parent_n[3], const double* child,
                     const int32_t child_n[3], const int32_t coarse_lo[3], void* stream);
-/* prepare_fmr_states (JAX_BSSN/fmr/tiled.py:230-250): project owned samples
+/* prepare_fmr_states (JAX_BSSN/fmr/tiled.py:146-166): project owned samples
  * (when project != 0), refresh halos and prolong child shells, parent first. */
 int bssn_fmr_prepare(double* const* states, const BssnFmrPatch* patches, const BssnParams* params,
                      int32_t npatch, int32_t project, void* stream);
-/* fmr_stage (JAX_BSSN/fmr/tiled.py:253-263): prepare in place, then the RHS of
+/* fmr_stage (JAX_BSSN/fmr/tiled.py:169-179): prepare in place, then the RHS of
  * every patch on its owned samples into rhs[p] (resident layout). */
 int bssn_fmr_stage_rhs(double* const* states, double* const* rhs, const BssnFmrPatch* patches,
                        const BssnParams* params, int32_t npatch, void* workspace,
                        size_t workspace_bytes, void* stream);
-/* fmr_rk4_step (JAX_BSSN/fmr/tiled.py:266-293), `steps` times, in place.
+/* fmr_rk4_step (JAX_BSSN/fmr/tiled.py:182-209), `steps` times, in place.
  * params[p] are the per-patch evolution parameters (MAD weight, child faces periodic). */
 int bssn_fmr_rk4_step(double* const* states, const BssnFmrPatch* patches, const BssnParams* params,
                       int32_t npatch, int32_t steps, void* workspace, size_t workspace_bytes, void* stream);
-/* fmr_constraint_norms statistics (JAX_BSSN/fmr/tiled.py:296-330): prepares the
+/* fmr_constraint_norms statistics (JAX_BSSN/fmr/tiled.py:212-246): prepares the
  * states (no projection) and accumulates, over owned samples not covered by a
  * child, the sum of squares and max |.| of H, M, det-1, tr A, Gamma into
  * stats[10] (device, pairs per constraint).  Workspace: see the implementation. */

@@ -6,7 +6,7 @@
 // Stage combinations are evaluated with round-to-nearest intrinsics in the
 // reference's order: u0 + (c*dt)*k for the stages, the accumulator
 // ((k1 + 2 k2) + 2 k3) + k4 and u0 + (dt/6)*sum (serial, tiled and Cartoon
-// steppers) or u0 + (dt*sum)/6 (JAX_BSSN/fmr/tiled.py:279-280).  Together
+// steppers) or u0 + (dt*sum)/6 (JAX_BSSN/fmr/tiled.py:195-196).  Together
 // with the bit-exact projection this keeps the evolved state identical to the
 // float64 reference wherever the RHS agrees to the last bit.
 #include <cmath>
@@ -153,10 +153,6 @@ Box full_box(const Geo& G) {
         b.count *= b.n[d];
     }
     return b;
-}
-
-size_t rhs_work_blocks(bool with_mom) {
-    return with_mom ? (size_t)(3 * (NMIX + NMIX_MOM) + 24 + 6) : (size_t)(3 * NMIX);
 }
 
 RhsWork carve_rhs_work(double* base, long long cs, bool with_mom) {

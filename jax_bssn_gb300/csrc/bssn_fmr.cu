@@ -4,11 +4,12 @@
 // Every patch lives in the working layout (21 components, padded by G = 4
 // guards, owned samples at [4, 4+n)).  Algorithms follow uwplasma/JAX_BSSN for
 // a single-tile topology:
-//   halo refresh: self-wrap + linear exterior  JAX_BSSN/parallel/communication.py:144-214
+//   halo refresh: self-wrap + linear exterior  JAX_BSSN/parallel/evolution.py:74-92,
+//                                              JAX_BSSN/parallel/communication.py:36-106
 //   prolongation into the exterior shell       JAX_BSSN/fmr/transfer.py:57-142, 197-244
 //   injection of coincident vertices           JAX_BSSN/fmr/transfer.py:145-171, 247-252
-//   prepare / stage / RK4 / injection order    JAX_BSSN/fmr/tiled.py:230-293
-//   composite point-count norms                JAX_BSSN/fmr/tiled.py:296-330,
+//   prepare / stage / RK4 / injection order    JAX_BSSN/fmr/tiled.py:146-209
+//   composite point-count norms                JAX_BSSN/fmr/tiled.py:212-246,
 //                                              JAX_BSSN/parallel/evolution.py:145-170
 // The six-node interpolation is separable and is evaluated in the
 // reference's order -- along x for each of the 6x6 (y, z) source lines, then
@@ -54,7 +55,7 @@ static PatchDims dims_of(const int32_t n[3]) {
 }
 
 // ---------------------------------------------------------------------------
-// halo refresh along one axis (communication.py:153-213): guards take the
+// halo refresh along one axis (communication.py:39-106): guards take the
 // periodic image of owned samples; on a Sommerfeld face they take the linear
 // extrapolation base + (i - boundary) * slope instead.
 // ---------------------------------------------------------------------------

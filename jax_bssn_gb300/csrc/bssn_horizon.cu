@@ -35,6 +35,8 @@
 #include <algorithm>
 #include <cmath>
 #include <map>
+#include <mutex>
+#include <set>
 #include <string>
 #include <tuple>
 
@@ -1153,8 +1155,8 @@ Factor factor_of(void* ws, int nt, int np) {
 // Launch with the programmatic-stream-serialisation attribute (dependent
 // launch), counted and timed like every other launch.
 template <typename... P, typename... A>
-void launch_dependent(void (*kernel)(P...), unsigned blocks, unsigned threads, size_t smem, cudaStream_t s,
-                      A... args) {
+cudaError_t launch_dependent(void (*kernel)(P...), unsigned blocks, unsigned threads, size_t smem, cudaStream_t s,
+                             A... args) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(blocks);
     cfg.blockDim = dim3(threads);
@@ -1166,14 +1168,34 @@ void launch_dependent(void (*kernel)(P...), unsigned blocks, unsigned threads, s
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     prof_begin(KC_HORIZON_SOLVE, s);
-    cudaLaunchKernelEx(&cfg, kernel, args...);
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, kernel, args...);
     prof_end(KC_HORIZON_SOLVE, s);
+    return e;
+}
+
+// The dynamic shared-memory opt-in of k_band_back_shared is an attribute of
+// the kernel in the current device's context, so it is set once per device
+// (under a lock: several host threads may solve at once).
+cudaError_t configure_back_shared() {
+    static std::mutex lock;
+    static std::set<int> configured;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> guard(lock);
+    if (configured.count(dev)) return cudaSuccess;
+    e = cudaFuncSetAttribute(k_band_back_shared, cudaFuncAttributeMaxDynamicSharedMemorySize, kBackSmemMax);
+    if (e == cudaSuccess) configured.insert(dev);
+    return e;
 }
 
 // The factorisation and back substitution: one launch per band column, then
 // one for the back substitution, each a dependent launch of the one before.
-int enqueue_factor(const Factor& F, cudaStream_t s) {
+// Returns the number of launches; *err receives the first launch error.
+int enqueue_factor(const Factor& F, cudaStream_t s, cudaError_t* err) {
     const Band& B = F.B;
+    cudaError_t first = cudaSuccess;
+    auto keep = [&first](cudaError_t e) { if (first == cudaSuccess) first = e; };
     const bool fused = B.kl + 2 <= 32 * kRowsPerLane;
     const bool blocked = B.kl + kPanel <= kPanelRows;
     int launches = 0;
@@ -1187,8 +1209,8 @@ int enqueue_factor(const Factor& F, cudaStream_t s) {
             const int lastc = std::min(B.n - 1, c0 + ncol - 1 + B.ku2);
             const int ntrail = lastc >= first ? lastc - first + 1 : 0;
             const unsigned blocks = (unsigned)((ntrail + 1 + kPanelWarps - 1) / kPanelWarps);
-            launch_dependent(k_band_panel, blocks, kPanelWarps * 32, 0, s, B, c0, (const double*)F.panel[p % 2],
-                             F.panel[(p + 1) % 2], F.rhs, F.diag);
+            keep(launch_dependent(k_band_panel, blocks, kPanelWarps * 32, 0, s, B, c0,
+                                  (const double*)F.panel[p % 2], F.panel[(p + 1) % 2], F.rhs, F.diag));
             ++launches;
         }
     }
@@ -1196,23 +1218,20 @@ int enqueue_factor(const Factor& F, cudaStream_t s) {
         const int cols = std::min(B.n - 1, k + B.ku2) - k + 1;  // trailing columns plus the right-hand side
         const unsigned blocks = (unsigned)((cols + kStepWarps - 1) / kStepWarps);
         if (fused)
-            launch_dependent(k_band_step_fused, blocks, kStepWarps * 32, 0, s, B, k, k == 0 ? 1 : 0, F.rhs, F.diag,
-                             F.piv);
+            keep(launch_dependent(k_band_step_fused, blocks, kStepWarps * 32, 0, s, B, k, k == 0 ? 1 : 0, F.rhs,
+                                  F.diag, F.piv));
         else
-            launch_dependent(k_band_step, blocks, kStepWarps * 32, 0, s, B, k, F.rhs, F.diag);
+            keep(launch_dependent(k_band_step, blocks, kStepWarps * 32, 0, s, B, k, F.rhs, F.diag));
         ++launches;
     }
     const size_t smem = 2 * (size_t)B.n * sizeof(double);
     if (smem <= (size_t)kBackSmemMax && B.ku2 <= kBackThreads) {
-        static bool configured = false;
-        if (!configured) {
-            cudaFuncSetAttribute(k_band_back_shared, cudaFuncAttributeMaxDynamicSharedMemorySize, kBackSmemMax);
-            configured = true;
-        }
-        launch_dependent(k_band_back_shared, 1, kBackThreads, smem, s, B, F.rhs, F.diag, F.sum);
+        keep(configure_back_shared());
+        keep(launch_dependent(k_band_back_shared, 1, kBackThreads, smem, s, B, F.rhs, F.diag, F.sum));
     } else {
-        launch_dependent(k_band_back, 1, kBackThreads, 0, s, B, F.rhs, F.diag, F.sum);
+        keep(launch_dependent(k_band_back, 1, kBackThreads, 0, s, B, F.rhs, F.diag, F.sum));
     }
+    if (err) *err = first;
     return launches + 1;
 }
 
@@ -1245,17 +1264,24 @@ cudaError_t factor_graph(const Factor& F, void* ws, int nt, int np, cudaGraphExe
         e = cudaStreamCreateWithFlags(&graphs.capture, cudaStreamNonBlocking);
         if (e != cudaSuccess) return e;
     }
+    e = configure_back_shared();
+    if (e != cudaSuccess) return e;
     e = cudaStreamBeginCapture(graphs.capture, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return e;
-    const int recorded = enqueue_factor(F, graphs.capture);
+    cudaError_t launched = cudaSuccess;
+    const int recorded = enqueue_factor(F, graphs.capture, &launched);
     count_launches(-recorded);  // recorded, not run
     graphs.launches[key] = recorded;
     cudaGraph_t graph = nullptr;
     e = cudaStreamEndCapture(graphs.capture, &graph);
+    if (e == cudaSuccess && launched != cudaSuccess) e = launched;
     cudaGraphExec_t exec = nullptr;
     if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
     if (graph) cudaGraphDestroy(graph);
-    if (e != cudaSuccess) return e;
+    if (e != cudaSuccess) {
+        graphs.launches.erase(key);
+        return e;
+    }
     graphs.execs[key] = exec;
     out = exec;
     launches = graphs.launches[key];
@@ -1382,8 +1408,8 @@ extern "C" int bssn_horizon_newton_direction(const BssnHorizonGeometry* geometry
         count_launches(launches);
         e = cudaGraphLaunch(exec, s);
     } else {
-        enqueue_factor(F, s);
-        e = cudaGetLastError();
+        enqueue_factor(F, s, &e);
+        if (e == cudaSuccess) e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(delta, F.rhs, (size_t)F.B.n * sizeof(double), cudaMemcpyDeviceToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(summary, F.sum, 2 * sizeof(double), cudaMemcpyDeviceToDevice, s);

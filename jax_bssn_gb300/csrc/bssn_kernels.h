@@ -3,7 +3,7 @@
 
 #include <cuda_runtime.h>
 
-#include "bssn_stencil.cuh"
+#include "bssn_fields.cuh"
 
 namespace bssn {
 
@@ -26,7 +26,12 @@ struct RhsWork {
 
 constexpr int kMatterComps = 10;
 
-size_t rhs_work_blocks(bool with_mom);
+// Padded blocks of RHS scratch (RhsWork): the inner first derivatives of the
+// NMIX base fields, plus, when kappa != 0, those of the NMIX_MOM momentum
+// fields, 24 derived-field blocks and 6 damping blocks.
+constexpr size_t rhs_work_blocks(bool with_mom) {
+    return with_mom ? (size_t)(3 * (NMIX + NMIX_MOM) + 24 + 6) : (size_t)(3 * NMIX);
+}
 RhsWork carve_rhs_work(double* base, long long cs, bool with_mom);
 
 cudaError_t launch_rhs(const double* u, double* k, const RhsWork& w, const Geo& G, const Box& box,

@@ -28,12 +28,17 @@ namespace {
 // Largest array served: (nx+8)*(ny+8)*(nz+8) <= 21952 samples, e.g. 20x20x20.
 constexpr size_t kMaxPaddedSamples = 21952;
 // Work blocks bssn_rhs uses in its larger (kappa != 0) form: the padded
-// state and RHS (21 each), 81 first-derivative blocks, 24 derived-field
-// blocks and 6 damping-term blocks.
-constexpr size_t kBlocks = 21 + 21 + 81 + 24 + 6;
+// state and RHS (21 each) and the RHS scratch (81 first-derivative blocks,
+// 24 derived-field blocks and 6 damping-term blocks), from the same
+// constants bssn_workspace_bytes uses.
+constexpr size_t kBlocks = 2 * bssn::NCOMP + bssn::rhs_work_blocks(true);
+static_assert(kBlocks == 153, "the stated size of the array (26.9 MB) assumes 153 blocks");
 constexpr size_t kScratchValues = kBlocks * kMaxPaddedSamples;  // 26.9 MB of float64
 
-// One array shared by every call on a device.  Host code must not pass the
+// One array shared by every call on a device.  The address cache below is
+// keyed by device index and assumes the device's primary context (the one the
+// CUDA runtime uses); after cudaDeviceReset, or under a caller's own driver
+// context, the cached address would be stale.  Host code must not pass the
 // name of this array to a kernel: on the host it only stands in for the
 // device symbol; its device address comes from cudaGetSymbolAddress.
 static __device__ __align__(256) double g_rhs_scratch[kScratchValues];

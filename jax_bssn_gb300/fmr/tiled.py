@@ -67,7 +67,7 @@ def _layout_shape(layout):
 
 
 def evolution_parameters(parameters, hierarchy):
-    """Finest spacing for MAD, bulk equations on children (tiled.py:123-132)."""
+    """Finest spacing for MAD, bulk equations on children (tiled.py:39-48)."""
     finest = min(p.dx for p in parameters)
     out = []
     for patch, p in enumerate(parameters):
@@ -79,7 +79,7 @@ def evolution_parameters(parameters, hierarchy):
 
 
 def validate_hierarchy(states, parameters, hierarchy, layouts):
-    """Host-side checks of the reference (tiled.py:135-186), before any launch."""
+    """Host-side checks of the reference (tiled.py:51-102), before any launch."""
     parents = hierarchy_parents(hierarchy)
     if not parameters or not len(parameters) == len(layouts) == len(parents):
         raise ValueError("FMR requires one parameter tuple and one layout per patch")
@@ -198,7 +198,7 @@ def _finish(states, host):
 # ----------------------------------------------------------------------------
 
 def initialize_tiled_fmr(initial, root_params, root_shape, hierarchy, *, mesh=None):
-    """Patches from a common ``initial(coordinates, params)`` callback (tiled.py:189-227).
+    """Patches from a common ``initial(coordinates, params)`` callback (tiled.py:105-143).
 
     The callback receives broadcast Cartesian coordinates of a patch's owned
     samples and parameters describing that patch, and returns BSSNVariables
@@ -247,7 +247,7 @@ def initialize_tiled_fmr(initial, root_params, root_shape, hierarchy, *, mesh=No
 
 
 def prepare_fmr_states(states, parameters, hierarchy, *, layouts, project=True):
-    """Project owned samples, refresh halos, prolong child shells (tiled.py:230-250)."""
+    """Project owned samples, refresh halos, prolong child shells (tiled.py:146-166)."""
     shapes = validate_hierarchy(states, parameters, hierarchy, layouts)
     host = _is_host(states)
     device = _device.require_cuda()
@@ -260,7 +260,7 @@ def prepare_fmr_states(states, parameters, hierarchy, *, layouts, project=True):
 
 
 def fmr_stage(states, parameters, hierarchy, *, layouts):
-    """Matching stage states and RHS values (tiled.py:253-263).
+    """Matching stage states and RHS values (tiled.py:169-179).
 
     The RHS is defined on owned samples; its guard samples are zero."""
     parameters = evolution_parameters(parameters, hierarchy)
@@ -281,7 +281,7 @@ def fmr_stage(states, parameters, hierarchy, *, layouts):
 
 
 def fmr_rk4_step(states, parameters, hierarchy, *, layouts):
-    """Advance every patch with the same four RK stages and timestep (tiled.py:266-293)."""
+    """Advance every patch with the same four RK stages and timestep (tiled.py:182-209)."""
     return fmr_rk4_steps(states, parameters, hierarchy, 1, layouts=layouts)
 
 
@@ -319,7 +319,7 @@ def _norms_from_stats(stats, parameters, hierarchy, shapes):
 
 
 def fmr_constraint_norms(states, parameters, hierarchy, *, layouts):
-    """Composite point-count norms over uncovered owned vertices (tiled.py:296-330)."""
+    """Composite point-count norms over uncovered owned vertices (tiled.py:212-246)."""
     parameters = evolution_parameters(parameters, hierarchy)
     shapes = validate_hierarchy(states, parameters, hierarchy, layouts)
     device = _device.require_cuda()

@@ -2,13 +2,13 @@
 
 Follows uwplasma/JAX_BSSN for a (1, 1, 1) tile topology -- every patch is a
 single padded array of (n + 2g)^3 samples with g = 4 guards:
-  patch spacing/origin/MAD policy       JAX_BSSN/fmr/tiled.py:106-132, 189-227
-  halo refresh (self-wrap, linear exterior)   JAX_BSSN/parallel/communication.py:144-214
+  patch spacing/origin/MAD policy       JAX_BSSN/fmr/tiled.py:39-48, 105-143
+  halo refresh (self-wrap, linear exterior)   JAX_BSSN/parallel/evolution.py:74-92, communication.py:36-106
   tile-local parameters                 JAX_BSSN/parallel/evolution.py:19-38
   six-node Lagrange prolongation        JAX_BSSN/fmr/transfer.py:57-142, 197-244
   injection                             JAX_BSSN/fmr/transfer.py:145-171, 247-252
-  prepare / stage / RK4 step            JAX_BSSN/fmr/tiled.py:230-293
-  composite constraint norms            JAX_BSSN/fmr/tiled.py:296-330
+  prepare / stage / RK4 step            JAX_BSSN/fmr/tiled.py:146-209
+  composite constraint norms            JAX_BSSN/fmr/tiled.py:212-246
 Fields are BSSNVariables whose leaves have shape (..., n+2g, n+2g, n+2g); the
 reference's three singleton tile axes are dropped.
 """
@@ -52,7 +52,7 @@ def fine_active_shape(spec):
 
 
 def evolution_parameters(parameters, hierarchy):
-    """mad_q = (dx_finest/dx)^4 per patch; child faces periodic (tiled.py:123-132)."""
+    """mad_q = (dx_finest/dx)^4 per patch; child faces periodic (tiled.py:39-48)."""
     finest = min(p.dx for p in parameters)
     out = []
     for patch, p in enumerate(parameters):
@@ -64,7 +64,7 @@ def evolution_parameters(parameters, hierarchy):
 
 
 def patch_parameters(root_params, root_shape, hierarchy):
-    """Per-patch spacing and active origins (tiled.py:189-212)."""
+    """Per-patch spacing and active origins (tiled.py:120-127)."""
     parents = parents_of(hierarchy)
     reduced = (tuple(n == 1 for n in root_shape) if root_params.reduced_axes is None
                else root_params.reduced_axes)
@@ -89,7 +89,7 @@ def local_parameters(p, shape):
 
 
 # ----------------------------------------------------------------------------
-# halo refresh of one patch (communication.py:144-214, count == 1)
+# halo refresh of one patch (parallel/evolution.py:74-92; communication.py:36-106, count == 1)
 # ----------------------------------------------------------------------------
 
 def _plane(axis, index):
@@ -205,7 +205,7 @@ def inject(parent, child, spec, child_n):
 
 
 # ----------------------------------------------------------------------------
-# stages and the RK4 step (tiled.py:230-293)
+# stages and the RK4 step (tiled.py:146-209)
 # ----------------------------------------------------------------------------
 
 def _owned(shape_n):
@@ -269,7 +269,7 @@ def rk4_step(states, params, shapes, hierarchy):
 
 
 def constraint_norms(states, params, shapes, hierarchy):
-    """Composite point-count L2/Linf over uncovered owned vertices (tiled.py:296-330)."""
+    """Composite point-count L2/Linf over uncovered owned vertices (tiled.py:212-246)."""
     prepared = prepare(states, params, shapes, hierarchy, project=False)
     parents = parents_of(hierarchy)
     names = ("hamiltonian", "momentum", "det_gamma", "trace_A", "gamma")

@@ -46,6 +46,10 @@ def test_noalloc_matches_workspace_entry_point_on_two_calls(cuda, native):
                         xl_bc=1, xr_bc=1, x_min=-0.5, y_min=0.1, z_min=-0.6)),
         (random_smooth_state((20, 20, 20), seed=32),
          BSSNParameters(eta=2.0, kappa=0.0, nu=0.05, g=0.75, dx=0.05, dt=0.01, gauge=0, mad_q=1.0 / 16.0)),
+        # the largest array served, with the damping branch: all 153 blocks
+        (random_smooth_state((20, 20, 20), seed=33),
+         BSSNParameters(eta=1.0, kappa=0.1, nu=0.04, g=0.75, dx=0.06, dt=0.01, gauge=1,
+                        zl_bc=1, zr_bc=1, x_min=-0.6, y_min=-0.6, z_min=-0.6)),
     ]
     for state, params in cases:
         status, got = _call_noalloc(native, state, params)
