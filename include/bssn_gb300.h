@@ -168,6 +168,67 @@ int bssn_patch_rk4(double* patch_state, const BssnPatch* patch, const BssnParams
 int bssn_patch_check_finite(const double* patch_state, const BssnPatch* patch,
                             int32_t* device_flag, void* stream);
 
+/* ---------------- instance batches ----------------
+ * No reference counterpart: the reference evolves one state per call (a vmap
+ * over rk4_step would batch it).  ninst independent instances of the same
+ * patch and parameters advance in the same launches.  Layout [component]
+ * [instance][padded block]: component c of instance i starts at
+ * (c * ninst + i) * prod(n + 2G) doubles.  Results are bit-identical to
+ * ninst separate single-patch calls.  The bssn_patch_* calls above are the
+ * one-instance batch. */
+size_t bssn_batch_values(const BssnPatch* patch, int32_t ninst);
+size_t bssn_batch_workspace_bytes(const BssnPatch* patch, int32_t ninst, const BssnParams* params);
+/* Reference layout -> owned samples of instance `instance` (ghosts untouched). */
+int bssn_batch_import(const BssnFields* in, double* states, const BssnPatch* patch, int32_t ninst, int32_t instance,
+                      void* stream);
+/* Owned samples of instance `instance` -> reference layout. */
+int bssn_batch_export(const double* states, BssnFields* out, const BssnPatch* patch, int32_t ninst,
+                      int32_t instance, void* stream);
+int bssn_batch_fill_periodic(double* states, const BssnPatch* patch, int32_t ninst, void* stream);
+/* `steps` RK4 steps of every instance, in place (time_evolve.py:144-217 per instance). */
+int bssn_batch_rk4(double* states, const BssnPatch* patch, int32_t ninst, const BssnParams* params, int32_t steps,
+                   void* workspace, size_t workspace_bytes, void* stream);
+int bssn_batch_check_finite(const double* states, const BssnPatch* patch, int32_t ninst, int32_t* device_flag,
+                            void* stream);
+
+/* ---------------- adjoint (reverse mode) ----------------
+ * Gradients of periodic evolutions.  The reference has no hand-written
+ * adjoint: differentiating its rk4_step (JAX_BSSN/evolution/time_evolve.py:144-217)
+ * means jax.grad / jax.vjp through XLA.  These entry points are the
+ * vector-Jacobian products of the same forward path, on instance batches
+ * (layout of bssn_batch_*).  Scope: every face periodic (bc all 0),
+ * kappa = 0, no matter sources, BSSN_PRECISION_F64, at least 8 samples per
+ * axis; anything else returns BSSN_ERR_INVALID.  Adjoint arrays have the
+ * batch layout; only their owned samples carry values (ghosts are scratch).
+ * Gradients are with respect to the 21 independent components. */
+
+/* Bytes of workspace bssn_rhs_vjp needs (111 + 33 padded blocks per instance). */
+size_t bssn_rhs_vjp_workspace_bytes(const BssnPatch* patch, int32_t ninst);
+/* state_adjoint = (d RHS / d state)^T rhs_adjoint at `states`
+ * (compute_bssn_rhs, time_evolve.py:41-57).  Fills the ghosts of `states`
+ * and `rhs_adjoint` (periodic wrap) in place. */
+int bssn_rhs_vjp(double* states, double* rhs_adjoint, double* state_adjoint, const BssnPatch* patch, int32_t ninst,
+                 const BssnParams* params, void* workspace, size_t workspace_bytes, void* stream);
+
+/* Checkpointed evolution for reverse mode.  `segment` <= 0 selects
+ * ceil(sqrt(steps)) steps between checkpoints; store_stages != 0 keeps, while
+ * a segment is re-run backward, every step's four stage RHS values (one
+ * forward re-run in total instead of two, at 4 more states per segment step).
+ * The workspace holds ceil(steps / segment) checkpoints, segment step states
+ * (x5 with store_stages) and about 20 working states. */
+size_t bssn_adjoint_workspace_bytes(const BssnPatch* patch, int32_t ninst, const BssnParams* params, int32_t steps,
+                                    int32_t segment, int32_t store_stages);
+/* `steps` RK4 steps of every instance in place (bit-identical to
+ * bssn_batch_rk4), recording the checkpoints in the workspace. */
+int bssn_adjoint_forward(double* states, const BssnPatch* patch, int32_t ninst, const BssnParams* params,
+                         int32_t steps, int32_t segment, int32_t store_stages, void* workspace, size_t workspace_bytes,
+                         void* stream);
+/* After bssn_adjoint_forward with the same arguments and workspace: on entry
+ * `adjoint` holds d loss / d (final state), on exit d loss / d (initial state). */
+int bssn_adjoint_backward(double* adjoint, const BssnPatch* patch, int32_t ninst, const BssnParams* params,
+                          int32_t steps, int32_t segment, int32_t store_stages, void* workspace, size_t workspace_bytes,
+                          void* stream);
+
 /* Whole-array conversion between the reference layout (seven leaves) and the
  * 21-component layout, over all samples of an array of the given extent
  * (e.g. a padded FMR patch, whose guards are part of the array). */
@@ -444,7 +505,8 @@ long long bssn_launch_count(void);
  * stage, projection, import, export, constraints, FMR transfer, Cartoon,
  * FP32 conversion, other, K/Gt/At RHS in one pass (FP64 form), puncture
  * Newton-level kernels, puncture Krylov operator kernels, puncture Krylov
- * vector updates, horizon surface kernels, horizon band solve.  bssn_profile_read synchronises the recorded events, accumulates and
+ * vector updates, horizon surface kernels, horizon band solve, adjoint point
+ * kernel, adjoint stencil transposes, adjoint stage and projection kernels.  bssn_profile_read synchronises the recorded events, accumulates and
  * returns the number of classes. */
 void bssn_profile_enable(int on);
 void bssn_profile_reset(void);

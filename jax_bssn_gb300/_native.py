@@ -114,6 +114,33 @@ SIGNATURES = {
                                       ctypes.c_int32, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     "bssn_patch_check_finite": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BssnPatch),
                                                ctypes.c_void_p, ctypes.c_void_p]),
+    "bssn_batch_values": (ctypes.c_size_t, [ctypes.POINTER(BssnPatch), ctypes.c_int32]),
+    "bssn_batch_workspace_bytes": (ctypes.c_size_t, [ctypes.POINTER(BssnPatch), ctypes.c_int32,
+                                                      ctypes.POINTER(BssnParams)]),
+    "bssn_batch_import": (ctypes.c_int, [ctypes.POINTER(BssnFields), ctypes.c_void_p, ctypes.POINTER(BssnPatch),
+                                         ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p]),
+    "bssn_batch_export": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BssnFields), ctypes.POINTER(BssnPatch),
+                                         ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p]),
+    "bssn_batch_fill_periodic": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BssnPatch), ctypes.c_int32,
+                                                ctypes.c_void_p]),
+    "bssn_batch_rk4": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BssnPatch), ctypes.c_int32,
+                                      ctypes.POINTER(BssnParams), ctypes.c_int32, ctypes.c_void_p,
+                                      ctypes.c_size_t, ctypes.c_void_p]),
+    "bssn_batch_check_finite": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BssnPatch), ctypes.c_int32,
+                                               ctypes.c_void_p, ctypes.c_void_p]),
+    "bssn_rhs_vjp_workspace_bytes": (ctypes.c_size_t, [ctypes.POINTER(BssnPatch), ctypes.c_int32]),
+    "bssn_rhs_vjp": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(BssnPatch),
+                                    ctypes.c_int32, ctypes.POINTER(BssnParams), ctypes.c_void_p, ctypes.c_size_t,
+                                    ctypes.c_void_p]),
+    "bssn_adjoint_workspace_bytes": (ctypes.c_size_t, [ctypes.POINTER(BssnPatch), ctypes.c_int32,
+                                                        ctypes.POINTER(BssnParams), ctypes.c_int32, ctypes.c_int32,
+                                                        ctypes.c_int32]),
+    "bssn_adjoint_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BssnPatch), ctypes.c_int32,
+                                            ctypes.POINTER(BssnParams), ctypes.c_int32, ctypes.c_int32,
+                                            ctypes.c_int32, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    "bssn_adjoint_backward": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BssnPatch), ctypes.c_int32,
+                                             ctypes.POINTER(BssnParams), ctypes.c_int32, ctypes.c_int32,
+                                             ctypes.c_int32, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     "bssn_fields_to_components": (ctypes.c_int, [ctypes.POINTER(BssnFields), ctypes.c_void_p, Shape3,
                                                  ctypes.c_void_p]),
     "bssn_components_to_fields": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BssnFields), Shape3,
@@ -197,7 +224,7 @@ SIGNATURES = {
 KERNEL_CLASSES = ("fill", "first_derivs", "rhs_gauge", "rhs_kgt", "rhs_at", "mom_derived", "mom_damping",
                   "sommerfeld", "rk4_stage", "project", "import", "export", "constraints", "fmr_transfer",
                   "cartoon", "convert", "other", "rhs_curv", "solve_newton", "solve_apply", "solve_update", "horizon_surface",
-                  "horizon_solve")
+                  "horizon_solve", "adjoint_point", "adjoint_stencil", "adjoint_stage")
 
 
 def profile_read() -> dict:

@@ -1,0 +1,629 @@
+// Reverse-mode (adjoint) kernels of the periodic BSSN evolution on GB300.
+//
+// The forward path is rk4_step (JAX_BSSN/evolution/time_evolve.py:144-217)
+// with its RHS compute_bssn_rhs (time_evolve.py:41-57).  The reference never
+// differentiates it; jax.grad through it would be XLA's reverse mode.  Here
+// the vector-Jacobian products are written as kernels:
+//
+//   RHS.  At every point the RHS is F(x) + advection + dissipation, where x
+//   holds the 21 state values and their first and second finite-difference
+//   derivatives (132 inputs) and F is algebraic.  For an adjoint kbar of the
+//   RHS:
+//     k_adj_point   recomputes x from the state (the forward's own stencil
+//                   helpers), runs the generated reverse sweep of F
+//                   (bssn_adjoint_point.cuh) and writes the 21 value
+//                   coefficients into the state adjoint and the 111
+//                   derivative coefficients into their own blocks;
+//     k_adj_mixed   folds each composed mixed derivative D1_n(D1_m f) (m < n)
+//                   into the first-derivative coefficient of axis m:
+//                   on a periodic grid the centred D1 is antisymmetric
+//                   (D1^T = -D1) and D2 and the sixth difference symmetric,
+//                   so  m_a = -c1_a + sum_{b>a} D1_b(c2_ab);
+//     k_adj_field   applies the transposed stencils: sum_a D1_a(m_a) +
+//                   D2_a(c2_aa), the (symmetric) Kreiss-Oliger term of kbar,
+//                   and the transposed upwind advection -- at each neighbour
+//                   the stencil side is the one the sign of that neighbour's
+//                   shift selected in the forward -- plus the shift's own
+//                   adjoint from the advection terms, sum_f kbar_f U_a(f).
+//   Projection and stage combination.  k_adj_final, k_adj_stage and
+//   k_adj_initial run the generated reverse sweep of the algebraic projection
+//   (time_evolve.py:94-141) on the pre-projection values and distribute the
+//   result over the RK4 combination's inputs.
+//
+// Evolutions are differentiated with sqrt(N) checkpointing: the forward pass
+// stores the state every `segment` steps; the backward pass re-runs each
+// segment from its checkpoint, either keeping every step's four stage RHS
+// values (store_stages = 1: one extra forward pass, more memory) or only the
+// step-start states (then each step's stages are recomputed once more).
+// Everything runs on instance batches (layout [component][instance][block]).
+// Scope: all faces periodic, kappa = 0, no matter, FP64 arithmetic.
+#include <cmath>
+#include <cstring>
+#include <string>
+
+#include "../../include/bssn_gb300.h"
+#include "bssn_adjoint_point.cuh"
+#include "bssn_driver.h"
+#include "bssn_profile.h"
+
+namespace bssn {
+namespace adjoint {
+namespace {
+
+constexpr int kThreads = 128;
+constexpr int NC1 = 45;            // first-derivative coefficient blocks
+constexpr int NC2 = 66;            // second-derivative coefficient blocks
+constexpr int NCOEF = NC1 + NC2;   // 111
+constexpr int I_DG = 21, I_DW = 39, I_DAL = 42, I_DK = 45, I_DB = 48, I_DGT = 57;
+constexpr int I_D2G = 66, I_D2W = 102, I_D2AL = 108, I_D2B = 114;
+
+inline unsigned blocks_of(long long n) { return (unsigned)((n + kThreads - 1) / kThreads); }
+
+// Coefficient block (index into the 111) of d_a of state component f, or -1.
+__host__ __device__ constexpr int c1_block(int f, int a) {
+    return f < 6 ? I_DG - 21 + 6 * a + f
+         : f == CW ? I_DW - 21 + a
+         : f == CK ? I_DK - 21 + a
+         : (f >= GTX && f <= GTZ) ? I_DGT - 21 + 3 * a + (f - GTX)
+         : f == CALPHA ? I_DAL - 21 + a
+         : (f >= BX) ? I_DB - 21 + 3 * (f - BX) + a
+         : -1;
+}
+
+// Coefficient block of d_m d_n of the NMIX field mf (pair slot pr), f's slot
+// in the 111.
+__host__ __device__ constexpr int c2_block(int mf, int pr) {
+    return mf < 6 ? I_D2G - 21 + 6 * pr + mf
+         : mf == MIX_W ? I_D2W - 21 + pr
+         : mf == MIX_ALPHA ? I_D2AL - 21 + pr
+         : I_D2B - 21 + 6 * (mf - MIX_B) + pr;
+}
+
+// NMIX field index of state component f (gt, W, alpha, beta), or -1.
+__host__ __device__ constexpr int mix_of(int f) {
+    return f < 6 ? f : f == CW ? MIX_W : f == CALPHA ? MIX_ALPHA : (f >= BX ? MIX_B + (f - BX) : -1);
+}
+
+PointParams point_params(const Geo& G) {
+    PointParams pp;
+    pp.eta = G.eta;
+    pp.gdrv = G.g;
+    pp.c_harm = G.gauge == 0 ? 1.0 : 0.0;
+    pp.c_log = G.gauge == 1 ? 1.0 : 0.0;
+    pp.shift_on = G.zero_shift ? 0.0 : 1.0;
+    return pp;
+}
+
+struct Pt {
+    int ix[3];
+    long long p;
+};
+
+__device__ __forceinline__ bool owned_point(const Geo& G, const Box& B, Pt& c) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= box_threads(G, B)) return false;
+    const long long off = instance_offset(G, B, t);
+    B.coords(t, c.ix);
+    c.p = lin(G, c.ix) + off;
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// point kernel: inputs of F by the forward's stencil helpers, reverse sweep
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads)
+k_adj_point(const double* __restrict__ u, const double* __restrict__ d1, const double* __restrict__ kbar,
+            double* __restrict__ ubar, double* __restrict__ coef, Geo G, Box B, PointParams pp, int accumulate) {
+    Pt c;
+    if (!owned_point(G, B, c)) return;
+    const long long cs = G.cs, p = c.p;
+    double x[kPointInputs];
+#pragma unroll
+    for (int f = 0; f < NCOMP; ++f) x[f] = u[f * cs + p];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+#pragma unroll
+        for (int s = 0; s < 6; ++s) x[I_DG + 6 * a + s] = D1<double, false>(u + (GXX + s) * cs + p, G, a, c.ix[a]);
+        x[I_DW + a] = D1<double, false>(u + CW * cs + p, G, a, c.ix[a]);
+        x[I_DAL + a] = D1<double, false>(u + CALPHA * cs + p, G, a, c.ix[a]);
+        x[I_DK + a] = D1<double, false>(u + CK * cs + p, G, a, c.ix[a]);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            x[I_DB + 3 * i + a] = D1<double, false>(u + (BX + i) * cs + p, G, a, c.ix[a]);
+            x[I_DGT + 3 * a + i] = D1<double, false>(u + (GTX + i) * cs + p, G, a, c.ix[a]);
+        }
+    }
+    // second derivatives: D2 on the diagonal, D1 along the larger axis of the
+    // stored first derivative along the smaller one off it (the forward's order)
+#pragma unroll
+    for (int m = 0; m < 3; ++m)
+#pragma unroll
+        for (int n = m; n < 3; ++n) {
+            const int pr = sym(m, n);
+#pragma unroll
+            for (int f = 0; f < NMIX; ++f) {
+                const double v = m == n
+                    ? D2<double, false, false>(u + mix_source(f) * cs + p, G, m, c.ix[m])
+                    : D1<double, false>(d1 + (long long)(m * NMIX + f) * cs + p, G, n, c.ix[n]);
+                x[21 + c2_block(f, pr)] = v;
+            }
+        }
+    double kb[NCOMP];
+#pragma unroll
+    for (int f = 0; f < NCOMP; ++f) kb[f] = kbar[f * cs + p];
+    double xb[kPointInputs];
+    rhs_point_vjp(x, kb, pp, xb);
+#pragma unroll
+    for (int f = 0; f < NCOMP; ++f) ubar[f * cs + p] = accumulate ? ubar[f * cs + p] + xb[f] : xb[f];
+#pragma unroll
+    for (int k = 0; k < NCOEF; ++k) coef[(long long)k * cs + p] = xb[21 + k];
+}
+
+// m_a = -c1_a + sum_{b > a} D1_b(c2_ab) for the NMIX fields, into mbuf
+// (layout of the inner-derivative buffer: block a * NMIX + f).
+__global__ void __launch_bounds__(kThreads)
+k_adj_mixed(const double* __restrict__ coef, double* __restrict__ mbuf, Geo G, Box B) {
+    Pt c;
+    if (!owned_point(G, B, c)) return;
+    const long long cs = G.cs, p = c.p;
+#pragma unroll 1
+    for (int f = 0; f < NMIX; ++f) {
+        const int comp = mix_source(f);
+        const double* c01 = coef + (long long)c2_block(f, sym(0, 1)) * cs + p;
+        const double* c02 = coef + (long long)c2_block(f, sym(0, 2)) * cs + p;
+        const double* c12 = coef + (long long)c2_block(f, sym(1, 2)) * cs + p;
+        const double m0 = -coef[(long long)c1_block(comp, 0) * cs + p] + D1<double, false>(c01, G, 1, c.ix[1])
+                          + D1<double, false>(c02, G, 2, c.ix[2]);
+        const double m1 = -coef[(long long)c1_block(comp, 1) * cs + p] + D1<double, false>(c12, G, 2, c.ix[2]);
+        const double m2 = -coef[(long long)c1_block(comp, 2) * cs + p];
+        mbuf[(long long)(0 * NMIX + f) * cs + p] = m0;
+        mbuf[(long long)(1 * NMIX + f) * cs + p] = m1;
+        mbuf[(long long)(2 * NMIX + f) * cs + p] = m2;
+    }
+}
+
+// Upwind weights of offset k (index k + 4, k in [-4, 4]) for a positive and a
+// negative coefficient: D4 in units of 1/(12 dx), the sixth-order side
+// stencils in units of 1/(60 dx) (JAX_BSSN/evolution/derivatives.py:166-338).
+__constant__ double kUp4[2][9] = {{0, 0, 0, -3, -10, 18, -6, 1, 0}, {0, -1, 6, -18, 10, 3, 0, 0, 0}};
+__constant__ double kUp6[2][9] = {{0, 0, 2, -24, -35, 80, -30, 8, -1}, {1, -8, 30, -80, 35, 24, -2, 0, 0}};
+
+// Transposed stencils of every component at one point, the dissipation and
+// advection transposes, and the shift's adjoint from the advection terms.
+__global__ void __launch_bounds__(kThreads)
+k_adj_field(const double* __restrict__ u, const double* __restrict__ kbar, const double* __restrict__ coef,
+            const double* __restrict__ mbuf, double* __restrict__ ubar, Geo G, Box B) {
+    Pt c;
+    if (!owned_point(G, B, c)) return;
+    const long long cs = G.cs, p = c.p;
+    // w[a][k + 4]: weight of kbar_f at q - k e_a in the transposed advection
+    double w[3][9];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const Axis& ax = G.ax[a];
+        const long long s = G.st[a];
+#pragma unroll
+        for (int k = -4; k <= 4; ++k) {
+            const double b = u[(BX + a) * cs + p - k * s];
+            const int side = b > 0.0 ? 0 : 1;
+            double c4 = kUp4[side][k + 4] * G.inv_12dx;
+            if (ax.mad) c4 = ax.q * c4 + ax.omq * (kUp6[side][k + 4] * G.inv_60dx);
+            w[a][k + 4] = (b == 0.0 || ax.reduced) ? 0.0 : b * c4;
+        }
+    }
+    double shift_bar[3] = {0.0, 0.0, 0.0};
+    double beta[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) beta[a] = u[(BX + a) * cs + p];
+#pragma unroll 1
+    for (int f = 0; f < NCOMP; ++f) {
+        double r = ubar[f * cs + p];
+        const int mf = mix_of(f);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            if (mf >= 0) {
+                r += D1<double, false>(mbuf + (long long)(a * NMIX + mf) * cs + p, G, a, c.ix[a]);
+                r += D2<double, false, false>(coef + (long long)c2_block(mf, sym(a, a)) * cs + p, G, a, c.ix[a]);
+            } else {
+                const int cb = c1_block(f, a);
+                if (cb >= 0) r -= D1<double, false>(coef + (long long)cb * cs + p, G, a, c.ix[a]);
+            }
+        }
+        const bool row_on = !(f >= BX && G.zero_shift);
+        if (row_on) {
+            const double* kf = kbar + f * cs + p;
+            r += KO<double, false, false>(kf, G, c.ix);
+            double adv = 0.0;
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                const long long s = G.st[a];
+#pragma unroll
+                for (int k = -4; k <= 4; ++k) adv = fma(w[a][k + 4], kf[-k * s], adv);
+            }
+            r += adv;
+            const double kq = kf[0];
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+                shift_bar[a] = fma(kq, UP1<double, false, false>(u + f * cs + p, G, a, c.ix[a], beta[a]), shift_bar[a]);
+        }
+        ubar[f * cs + p] = r;
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) ubar[(BX + a) * cs + p] += shift_bar[a];
+}
+
+// ---------------------------------------------------------------------------
+// projection and stage combination
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void project_vjp(const double (&b)[12], const double (&yb)[12], double (&bb)[12]) {
+    project_point_vjp(b, yb, bb);
+}
+
+// Final combination a = v0 + (dt/6)(((k1 + 2 k2) + 2 k3) + k4), u' = P(a):
+// from ubar' (in adj) writes v0bar and kbar_i = (dt/6){1,2,2,1} abar.
+__global__ void __launch_bounds__(kThreads)
+k_adj_final(const double* __restrict__ v0, const double* __restrict__ k1, const double* __restrict__ k2,
+            const double* __restrict__ k3, const double* __restrict__ k4, const double* __restrict__ adj,
+            double* __restrict__ v0bar, double* __restrict__ kb1, double* __restrict__ kb2, double* __restrict__ kb3,
+            double* __restrict__ kb4, Geo G, Box B) {
+    Pt c;
+    if (!owned_point(G, B, c)) return;
+    const long long cs = G.cs, p = c.p;
+    const double h6 = G.dt / 6.0, h3 = G.dt / 3.0;
+    double b[12], yb[12], bb[12];
+#pragma unroll
+    for (int s = 0; s < 12; ++s) {
+        const int f = s < 6 ? GXX + s : AXX + (s - 6);
+        const long long q = f * cs + p;
+        b[s] = v0[q] + h6 * (((k1[q] + 2.0 * k2[q]) + 2.0 * k3[q]) + k4[q]);
+        yb[s] = adj[q];
+    }
+    project_vjp(b, yb, bb);
+#pragma unroll
+    for (int f = 0; f < NCOMP; ++f) {
+        const long long q = f * cs + p;
+        const int s = f < 6 ? f : ((f >= AXX && f <= AZZ) ? 6 + (f - AXX) : -1);
+        const double a = s >= 0 ? bb[s] : adj[q];
+        v0bar[q] = a;
+        kb1[q] = h6 * a;
+        kb2[q] = h3 * a;
+        kb3[q] = h3 * a;
+        kb4[q] = h6 * a;
+    }
+}
+
+// Stage v = P(v0 + h k): from vbar adds bbar to v0bar and h bbar to kbar.
+__global__ void __launch_bounds__(kThreads)
+k_adj_stage(const double* __restrict__ v0, const double* __restrict__ k, double h, const double* __restrict__ vbar,
+            double* __restrict__ v0bar, double* __restrict__ kbar, Geo G, Box B) {
+    Pt c;
+    if (!owned_point(G, B, c)) return;
+    const long long cs = G.cs, p = c.p;
+    double b[12], yb[12], bb[12];
+#pragma unroll
+    for (int s = 0; s < 12; ++s) {
+        const int f = s < 6 ? GXX + s : AXX + (s - 6);
+        const long long q = f * cs + p;
+        b[s] = v0[q] + h * k[q];
+        yb[s] = vbar[q];
+    }
+    project_vjp(b, yb, bb);
+#pragma unroll
+    for (int f = 0; f < NCOMP; ++f) {
+        const long long q = f * cs + p;
+        const int s = f < 6 ? f : ((f >= AXX && f <= AZZ) ? 6 + (f - AXX) : -1);
+        const double a = s >= 0 ? bb[s] : vbar[q];
+        v0bar[q] += a;
+        kbar[q] += h * a;
+    }
+}
+
+// Initial projection v0 = P(u): ubar = P^T v0bar (in place on the adjoint).
+__global__ void __launch_bounds__(kThreads)
+k_adj_initial(const double* __restrict__ u, const double* __restrict__ v0bar, double* __restrict__ adj, Geo G,
+              Box B) {
+    Pt c;
+    if (!owned_point(G, B, c)) return;
+    const long long cs = G.cs, p = c.p;
+    double b[12], yb[12], bb[12];
+#pragma unroll
+    for (int s = 0; s < 12; ++s) {
+        const int f = s < 6 ? GXX + s : AXX + (s - 6);
+        b[s] = u[f * cs + p];
+        yb[s] = v0bar[f * cs + p];
+    }
+    project_vjp(b, yb, bb);
+#pragma unroll
+    for (int f = 0; f < NCOMP; ++f) {
+        const int s = f < 6 ? f : ((f >= AXX && f <= AZZ) ? 6 + (f - AXX) : -1);
+        adj[f * cs + p] = s >= 0 ? bb[s] : v0bar[f * cs + p];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+struct Plan {
+    Geo G;
+    Box B;
+    long long cs;        // component stride of a batch state
+    size_t state;        // doubles per batch state (21 * cs)
+    int steps, segment, nseg, store;
+};
+
+int validate(const BssnParams* p, const char* where) {
+    int st = validate_params(p);
+    if (st) return st;
+    for (int f = 0; f < 6; ++f)
+        if (p->bc[f] != 0) return fail(BSSN_ERR_INVALID, std::string(where) + ": the adjoint needs periodic faces");
+    if (p->kappa != 0.0) return fail(BSSN_ERR_INVALID, std::string(where) + ": the adjoint needs kappa = 0");
+    if (p->precision != BSSN_PRECISION_F64)
+        return fail(BSSN_ERR_INVALID, std::string(where) + ": the adjoint runs in FP64 arithmetic");
+    return BSSN_OK;
+}
+
+int make_plan(const BssnPatch* patch, int32_t ninst, const BssnParams* params, int32_t steps, int32_t segment,
+              int32_t store, const char* where, Plan& P) {
+    int st = validate(params, where);
+    if (st) return st;
+    if (!patch || patch->ghost < 4) return fail(BSSN_ERR_INVALID, std::string(where) + ": patch ghost must be >= 4");
+    if (ninst < 1) return fail(BSSN_ERR_INVALID, std::string(where) + ": instance count must be positive");
+    if (steps < 0) return fail(BSSN_ERR_INVALID, std::string(where) + ": steps must be non-negative");
+    int S[3], org[3], Pd[3];
+    for (int d = 0; d < 3; ++d) {
+        if (patch->n[d] < 8) return fail(BSSN_ERR_INVALID, std::string(where) + ": the adjoint needs 8+ samples per axis");
+        S[d] = patch->n[d];
+        org[d] = patch->ghost;
+        Pd[d] = patch->n[d] + 2 * patch->ghost;
+    }
+    BssnParams q = *params;
+    q.guard_cells = 0;
+    for (int d = 0; d < 3; ++d) { q.owned_shape[d] = -1; q.reduced_axes[d] = 0; }
+    for (int f = 0; f < 6; ++f) q.owned_faces[f] = 1;
+    if ((st = make_geo(&q, S, org, Pd, P.G))) return st;
+    P.G.ninst = ninst;
+    P.G.istride = P.G.cs;
+    P.G.cs *= ninst;
+    P.cs = P.G.cs;
+    P.state = (size_t)NCOMP * (size_t)P.cs;
+    P.B = box_of(P.G);
+    P.steps = steps;
+    P.segment = segment > 0 ? segment : (steps > 0 ? (int)std::ceil(std::sqrt((double)steps)) : 1);
+    if (P.segment > (steps > 0 ? steps : 1)) P.segment = steps > 0 ? steps : 1;
+    P.nseg = steps > 0 ? (steps + P.segment - 1) / P.segment : 0;
+    P.store = store ? 1 : 0;
+    return BSSN_OK;
+}
+
+// Work buffers of one RHS VJP (in units of cs): coefficients and the
+// inner-derivative / folded-coefficient blocks.
+constexpr size_t kVjpBlocks = NCOEF + 3 * NMIX;
+
+struct Layout {
+    double* ckpt;      // nseg states
+    double* seg;       // segment states (step starts)
+    double* segk;      // store: segment x 4 stage RHS states
+    double* V[4];      // stage states (ghost-filled)
+    double* K[4];      // stage RHS values (recompute mode)
+    double* KB[4];     // stage RHS adjoints
+    double* v0bar;
+    double* vb;
+    double* acc;
+    double* coef;      // NCOEF blocks
+    double* d1;        // 3 NMIX blocks: inner derivatives, then the folded coefficients
+    size_t doubles;
+};
+
+Layout layout_of(const Plan& P, double* base) {
+    Layout L;
+    double* q = base;
+    auto take = [&](size_t n) { double* r = q; q += n; return r; };
+    L.ckpt = take(P.nseg * P.state);
+    L.seg = take((size_t)P.segment * P.state);
+    L.segk = take(P.store ? (size_t)P.segment * 4 * P.state : 0);
+    for (int i = 0; i < 4; ++i) L.V[i] = take(P.state);
+    for (int i = 0; i < 4; ++i) L.K[i] = P.store ? nullptr : take(P.state);
+    for (int i = 0; i < 4; ++i) L.KB[i] = take(P.state);
+    L.v0bar = take(P.state);
+    L.vb = take(P.state);
+    L.acc = take(P.state);
+    L.coef = take((size_t)NCOEF * P.cs);
+    L.d1 = take((size_t)3 * NMIX * P.cs);
+    L.doubles = (size_t)(q - base);
+    return L;
+}
+
+cudaError_t fill(double* a, int ncomp, const Geo& G, cudaStream_t s) { return launch_fill_periodic(a, ncomp, G, s); }
+
+// RHS VJP: ubar (= or +=) (dRHS/du)^T kbar at state u; u and kbar ghost-filled.
+cudaError_t rhs_vjp(const double* u, const double* kbar, double* ubar, int accumulate, double* coef, double* d1,
+                    const Geo& G, const Box& B, cudaStream_t s) {
+    cudaError_t e = launch_inner_derivs(u, d1, G, B, s);
+    if (e != cudaSuccess) return e;
+    const unsigned nb = blocks_of(box_threads(G, B));
+    BSSN_LAUNCH(KC_ADJ_POINT, k_adj_point, nb, kThreads, s, u, d1, kbar, ubar, coef, G, B, point_params(G),
+                accumulate);
+    if ((e = fill(coef, NCOEF, G, s)) != cudaSuccess) return e;
+    BSSN_LAUNCH(KC_ADJ_STENCIL, k_adj_mixed, nb, kThreads, s, coef, d1, G, B);
+    if ((e = fill(d1, 3 * NMIX, G, s)) != cudaSuccess) return e;
+    BSSN_LAUNCH(KC_ADJ_STENCIL, k_adj_field, nb, kThreads, s, u, kbar, coef, d1, ubar, G, B);
+    return cudaGetLastError();
+}
+
+// One forward RK4 step from u_n (owned values) recording the stage states V
+// (ghost-filled) and the stage RHS values K; the new state goes to next.
+// The kernels and their order are the production step's, so the recorded
+// values are the forward's own.
+cudaError_t record_step(const double* un, double* const V[4], double* const K[4], double* acc, double* next,
+                        double* d1, const Plan& P, cudaStream_t s) {
+    const Geo& G = P.G;
+    const Box& B = P.B;
+    RhsWork w;
+    w.d1 = d1;
+    cudaError_t e = cudaMemcpyAsync(V[0], un, P.state * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) e = launch_project(V[0], G, B, s);
+    for (int i = 0; i < 4 && e == cudaSuccess; ++i) {
+        if ((e = fill(V[i], NCOMP, G, s)) != cudaSuccess) break;
+        if ((e = launch_rhs(V[i], K[i], w, G, B, s)) != cudaSuccess) break;
+        double* out = i < 3 ? V[i + 1] : next;
+        e = launch_rk4_stage(V[0], K[i], acc, out, G, B, i + 1, G.dt, 0, 1, s);
+    }
+    return e;
+}
+
+// The stage states of a recorded step from u_n and its stage RHS values.
+cudaError_t replay_stages(const double* un, double* const K[4], double* const V[4], double* acc, const Plan& P,
+                          cudaStream_t s) {
+    const Geo& G = P.G;
+    const Box& B = P.B;
+    cudaError_t e = cudaMemcpyAsync(V[0], un, P.state * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) e = launch_project(V[0], G, B, s);
+    if (e == cudaSuccess) e = fill(V[0], NCOMP, G, s);
+    for (int i = 1; i < 4 && e == cudaSuccess; ++i) {
+        e = launch_rk4_stage(V[0], K[i - 1], acc, V[i], G, B, i, G.dt, 0, 1, s);
+        if (e == cudaSuccess) e = fill(V[i], NCOMP, G, s);
+    }
+    return e;
+}
+
+// Reverse of one RK4 step: adj holds ubar_{n+1} on entry and ubar_n on exit.
+cudaError_t backward_step(const double* un, double* const V[4], double* const K[4], double* adj, const Layout& L,
+                          const Plan& P, cudaStream_t s) {
+    const Geo& G = P.G;
+    const Box& B = P.B;
+    const unsigned nb = blocks_of(box_threads(G, B));
+    BSSN_LAUNCH(KC_ADJ_STAGE, k_adj_final, nb, kThreads, s, V[0], K[0], K[1], K[2], K[3], adj, L.v0bar, L.KB[0],
+                L.KB[1], L.KB[2], L.KB[3], G, B);
+    cudaError_t e = cudaGetLastError();
+    const double h[3] = {0.5 * G.dt, 0.5 * G.dt, G.dt};
+    for (int i = 3; i >= 1 && e == cudaSuccess; --i) {
+        // v_i = P(v0 + h k_i) with k_i = RHS(v_{i-1}) ... the RHS of v_i is K[i]
+        if ((e = fill(L.KB[i], NCOMP, G, s)) != cudaSuccess) break;
+        if ((e = rhs_vjp(V[i], L.KB[i], L.vb, 0, L.coef, L.d1, G, B, s)) != cudaSuccess) break;
+        BSSN_LAUNCH(KC_ADJ_STAGE, k_adj_stage, nb, kThreads, s, V[0], K[i - 1], h[i - 1], L.vb, L.v0bar,
+                    L.KB[i - 1], G, B);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = fill(L.KB[0], NCOMP, G, s);
+    if (e == cudaSuccess) e = rhs_vjp(V[0], L.KB[0], L.v0bar, 1, L.coef, L.d1, G, B, s);
+    if (e == cudaSuccess) {
+        BSSN_LAUNCH(KC_ADJ_STAGE, k_adj_initial, nb, kThreads, s, un, L.v0bar, adj, G, B);
+        e = cudaGetLastError();
+    }
+    return e;
+}
+
+}  // namespace
+}  // namespace adjoint
+}  // namespace bssn
+
+using namespace bssn;
+using namespace bssn::adjoint;
+
+extern "C" {
+
+size_t bssn_rhs_vjp_workspace_bytes(const BssnPatch* patch, int32_t ninst) {
+    if (!patch || ninst < 1) return 0;
+    size_t block = 1;
+    for (int d = 0; d < 3; ++d) block *= (size_t)(patch->n[d] + 2 * patch->ghost);
+    return kVjpBlocks * (size_t)ninst * block * sizeof(double);
+}
+
+int bssn_rhs_vjp(double* states, double* rhs_adjoint, double* state_adjoint, const BssnPatch* patch, int32_t ninst,
+                 const BssnParams* params, void* workspace, size_t workspace_bytes, void* stream) {
+    if (!states || !rhs_adjoint || !state_adjoint) return fail(BSSN_ERR_INVALID, "bssn_rhs_vjp: null pointer");
+    Plan P;
+    int st = make_plan(patch, ninst, params, 0, 1, 0, "bssn_rhs_vjp", P);
+    if (st) return st;
+    if (!workspace || workspace_bytes < bssn_rhs_vjp_workspace_bytes(patch, ninst))
+        return fail(BSSN_ERR_WORKSPACE, "bssn_rhs_vjp: workspace missing or smaller than bssn_rhs_vjp_workspace_bytes");
+    cudaStream_t s = (cudaStream_t)stream;
+    double* coef = (double*)workspace;
+    double* d1 = coef + (size_t)NCOEF * P.cs;
+    cudaError_t e = fill(states, NCOMP, P.G, s);
+    if (e == cudaSuccess) e = fill(rhs_adjoint, NCOMP, P.G, s);
+    if (e == cudaSuccess) e = rhs_vjp(states, rhs_adjoint, state_adjoint, 0, coef, d1, P.G, P.B, s);
+    return cuda_status(e, "bssn_rhs_vjp");
+}
+
+size_t bssn_adjoint_workspace_bytes(const BssnPatch* patch, int32_t ninst, const BssnParams* params, int32_t steps,
+                                    int32_t segment, int32_t store_stages) {
+    Plan P;
+    if (make_plan(patch, ninst, params, steps, segment, store_stages, "bssn_adjoint_workspace_bytes", P)) return 0;
+    return layout_of(P, nullptr).doubles * sizeof(double);
+}
+
+int bssn_adjoint_forward(double* states, const BssnPatch* patch, int32_t ninst, const BssnParams* params,
+                         int32_t steps, int32_t segment, int32_t store_stages, void* workspace, size_t workspace_bytes,
+                         void* stream) {
+    if (!states) return fail(BSSN_ERR_INVALID, "bssn_adjoint_forward: null pointer");
+    Plan P;
+    int st = make_plan(patch, ninst, params, steps, segment, store_stages, "bssn_adjoint_forward", P);
+    if (st) return st;
+    const Layout L = layout_of(P, (double*)workspace);
+    if (!workspace || workspace_bytes < L.doubles * sizeof(double))
+        return fail(BSSN_ERR_WORKSPACE, "bssn_adjoint_forward: workspace smaller than bssn_adjoint_workspace_bytes");
+    cudaStream_t s = (cudaStream_t)stream;
+    RhsWork w;
+    w.d1 = L.d1;
+    cudaError_t e = cudaSuccess;
+    for (int j = 0; j < P.nseg && e == cudaSuccess; ++j) {
+        e = cudaMemcpyAsync(L.ckpt + (size_t)j * P.state, states, P.state * sizeof(double), cudaMemcpyDeviceToDevice, s);
+        const int len = std::min(P.segment, P.steps - j * P.segment);
+        for (int n = 0; n < len && e == cudaSuccess; ++n) {
+            e = launch_project(states, P.G, P.B, s);
+            if (e == cudaSuccess) e = rk4_step_patch(states, L.V[0], L.V[1], L.acc, w, P.G, P.B, true, 0, s);
+        }
+    }
+    return cuda_status(e, "bssn_adjoint_forward");
+}
+
+int bssn_adjoint_backward(double* adjoint, const BssnPatch* patch, int32_t ninst, const BssnParams* params,
+                          int32_t steps, int32_t segment, int32_t store_stages, void* workspace, size_t workspace_bytes,
+                          void* stream) {
+    if (!adjoint) return fail(BSSN_ERR_INVALID, "bssn_adjoint_backward: null pointer");
+    Plan P;
+    int st = make_plan(patch, ninst, params, steps, segment, store_stages, "bssn_adjoint_backward", P);
+    if (st) return st;
+    const Layout L = layout_of(P, (double*)workspace);
+    if (!workspace || workspace_bytes < L.doubles * sizeof(double))
+        return fail(BSSN_ERR_WORKSPACE, "bssn_adjoint_backward: workspace smaller than bssn_adjoint_workspace_bytes");
+    cudaStream_t s = (cudaStream_t)stream;
+    RhsWork w;
+    w.d1 = L.d1;
+    cudaError_t e = cudaSuccess;
+    for (int j = P.nseg - 1; j >= 0 && e == cudaSuccess; --j) {
+        const int len = std::min(P.segment, P.steps - j * P.segment);
+        // re-run the segment from its checkpoint, keeping step starts (and stages)
+        e = cudaMemcpyAsync(L.seg, L.ckpt + (size_t)j * P.state, P.state * sizeof(double), cudaMemcpyDeviceToDevice, s);
+        for (int n = 0; n + 1 < len + (P.store ? 1 : 0) && e == cudaSuccess; ++n) {
+            double* un = L.seg + (size_t)n * P.state;
+            if (P.store) {
+                double* K[4];
+                for (int i = 0; i < 4; ++i) K[i] = L.segk + ((size_t)n * 4 + i) * P.state;
+                double* next = n + 1 < len ? L.seg + (size_t)(n + 1) * P.state : L.vb;
+                e = record_step(un, L.V, K, L.acc, next, L.d1, P, s);
+            } else {
+                double* next = L.seg + (size_t)(n + 1) * P.state;
+                e = cudaMemcpyAsync(next, un, P.state * sizeof(double), cudaMemcpyDeviceToDevice, s);
+                if (e == cudaSuccess) e = launch_project(next, P.G, P.B, s);
+                if (e == cudaSuccess) e = rk4_step_patch(next, L.V[0], L.V[1], L.acc, w, P.G, P.B, true, 0, s);
+            }
+        }
+        for (int n = len - 1; n >= 0 && e == cudaSuccess; --n) {
+            double* un = L.seg + (size_t)n * P.state;
+            double* K[4];
+            if (P.store) {
+                for (int i = 0; i < 4; ++i) K[i] = L.segk + ((size_t)n * 4 + i) * P.state;
+                e = replay_stages(un, K, L.V, L.acc, P, s);
+            } else {
+                for (int i = 0; i < 4; ++i) K[i] = L.K[i];
+                e = record_step(un, L.V, K, L.acc, L.vb, L.d1, P, s);
+            }
+            if (e == cudaSuccess) e = backward_step(un, L.V, K, adjoint, L, P, s);
+        }
+    }
+    return cuda_status(e, "bssn_adjoint_backward");
+}
+
+}  // extern "C"

@@ -706,6 +706,8 @@ int cartoon_plan(bool axi, const int32_t shape[3], const BssnParams* p, CartoonP
     P.Gc.st[1] = P.C.nz;
     P.Gc.st[0] = P.C.nz;
     P.Gc.cs = P.C.cs;
+    P.Gc.ninst = 1;
+    P.Gc.istride = P.C.cs;
     P.positive.lo[0] = kCG;
     P.positive.n[0] = nx - kCG;
     P.positive.lo[1] = 0;

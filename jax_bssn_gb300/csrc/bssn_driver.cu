@@ -96,6 +96,8 @@ int make_geo(const BssnParams* p, const int S[3], const int org[3], const int P[
     G.st[1] = P[2];
     G.st[0] = (long long)P[1] * P[2];
     G.cs = (long long)P[0] * P[1] * P[2];
+    G.ninst = 1;
+    G.istride = G.cs;
     const double dx = p->dx;
     G.dx = dx;
     G.inv_dx = 1.0 / dx;
@@ -259,8 +261,9 @@ __global__ void k_import_matter(const double* __restrict__ rho, const double* __
 // them.
 template <typename T>
 __global__ void k_fill_periodic(T* __restrict__ u, int ncomp, Geo G, Box region, Box all, int closed) {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= all.count) return;
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= box_threads(G, all)) return;
+    const long long off = instance_offset(G, all, t);
     int ix[3];
     all.coords(t, ix);
     bool inside = true;
@@ -276,7 +279,7 @@ __global__ void k_fill_periodic(T* __restrict__ u, int ncomp, Geo G, Box region,
         src[d] = region.lo[d] + rel;
     }
     if (inside) return;
-    const long long dst = lin(G, ix), s = lin(G, src);
+    const long long dst = lin(G, ix) + off, s = lin(G, src) + off;
     for (int c = 0; c < ncomp; ++c) u[c * G.cs + dst] = u[c * G.cs + s];
 }
 
@@ -335,11 +338,12 @@ __device__ __forceinline__ void project_form(double (&g)[6], double (&A)[6], int
 }
 
 __global__ void k_project(double* __restrict__ u, Geo G, Box B) {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= B.count) return;
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= box_threads(G, B)) return;
+    const long long off = instance_offset(G, B, t);
     int ix[3];
     B.coords(t, ix);
-    const long long p = lin(G, ix), cs = G.cs;
+    const long long p = lin(G, ix) + off, cs = G.cs;
     double g[6], A[6];
 #pragma unroll
     for (int c = 0; c < 6; ++c) { g[c] = u[(GXX + c) * cs + p]; A[c] = u[(AXX + c) * cs + p]; }
@@ -379,11 +383,12 @@ template <bool Light>
 __global__ void k_rk4_stage(const double* __restrict__ u0, const double* __restrict__ k,
                             double* __restrict__ acc, double* __restrict__ out, Geo G, Box B,
                             int stage, double h, double dt, int final_form, int project) {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= B.count) return;
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= box_threads(G, B)) return;
+    const long long off = instance_offset(G, B, t);
     int ix[3];
     B.coords(t, ix);
-    const long long p = lin(G, ix), cs = G.cs;
+    const long long p = lin(G, ix) + off, cs = G.cs;
     double v[NCOMP];
 #pragma unroll
     for (int c = 0; c < NCOMP; ++c) {
@@ -421,11 +426,12 @@ __global__ void k_rk4_stage(const double* __restrict__ u0, const double* __restr
 }
 
 __global__ void k_count_nonfinite(const double* __restrict__ u, Geo G, Box B, int* flag) {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= B.count) return;
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= box_threads(G, B)) return;
+    const long long off = instance_offset(G, B, t);
     int ix[3];
     B.coords(t, ix);
-    const long long p = lin(G, ix);
+    const long long p = lin(G, ix) + off;
     int bad = 0;
     for (int c = 0; c < NCOMP; ++c) bad += !isfinite(u[c * G.cs + p]);
     if (bad) atomicAdd(flag, bad);
@@ -450,7 +456,8 @@ static cudaError_t fill_periodic(T* u, int ncomp, const Geo& G, cudaStream_t s) 
         if (!a.reduced && a.lbc && a.rbc && a.lo == a.start && a.hi == a.end) closed |= 1 << d;
     }
     if (closed == 7) return cudaSuccess;
-    BSSN_LAUNCH(KC_FILL, k_fill_periodic<T>, nblocks(all.count), kThreads, s, u, ncomp, G, region, all, closed);
+    BSSN_LAUNCH(KC_FILL, k_fill_periodic<T>, nblocks(box_threads(G, all)), kThreads, s, u, ncomp, G, region, all,
+                closed);
     return cudaGetLastError();
 }
 
@@ -463,7 +470,7 @@ cudaError_t launch_fill_periodic(float* u, int ncomp, const Geo& G, cudaStream_t
 }
 
 cudaError_t launch_project(double* u, const Geo& G, const Box& B, cudaStream_t s) {
-    BSSN_LAUNCH(KC_PROJECT, k_project, nblocks(B.count), kThreads, s, u, G, B);
+    BSSN_LAUNCH(KC_PROJECT, k_project, nblocks(box_threads(G, B)), kThreads, s, u, G, B);
     return cudaGetLastError();
 }
 
@@ -472,10 +479,10 @@ cudaError_t launch_rk4_stage(const double* u0, const double* k, double* acc, dou
                              cudaStream_t s) {
     const double h = stage == 3 ? dt : 0.5 * dt;
     if (G.precision == kPrecisionF32)
-        BSSN_LAUNCH(KC_STAGE, k_rk4_stage<true>, nblocks(B.count), kThreads, s, u0, k, acc, out, G, B, stage, h, dt,
+        BSSN_LAUNCH(KC_STAGE, k_rk4_stage<true>, nblocks(box_threads(G, B)), kThreads, s, u0, k, acc, out, G, B, stage, h, dt,
                     final_form, project);
     else
-        BSSN_LAUNCH(KC_STAGE, k_rk4_stage<false>, nblocks(B.count), kThreads, s, u0, k, acc, out, G, B, stage, h, dt,
+        BSSN_LAUNCH(KC_STAGE, k_rk4_stage<false>, nblocks(box_threads(G, B)), kThreads, s, u0, k, acc, out, G, B, stage, h, dt,
                     final_form, project);
     return cudaGetLastError();
 }
@@ -694,6 +701,8 @@ static Geo plain_geo(const int32_t extent[3]) {
     G.st[1] = extent[2];
     G.st[0] = (long long)extent[1] * extent[2];
     G.cs = (long long)extent[0] * extent[1] * extent[2];
+    G.ninst = 1;
+    G.istride = G.cs;
     return G;
 }
 
@@ -745,62 +754,85 @@ static int patch_geo(const BssnPatch* patch, const BssnParams* params, Geo& G) {
     return make_geo(&p, S, org, P, G);
 }
 
-size_t bssn_patch_values(const BssnPatch* patch) {
-    if (!patch) return 0;
-    size_t n = NCOMP;
-    for (int d = 0; d < 3; ++d) n *= (size_t)(patch->n[d] + 2 * patch->ghost);
-    return n;
+// A batch: ninst instances of one patch, laid out [component][instance][padded block].
+static int batch_geo(const BssnPatch* patch, int32_t ninst, const BssnParams* params, Geo& G) {
+    if (ninst < 1) return fail(BSSN_ERR_INVALID, "instance count must be positive");
+    const int st = patch_geo(patch, params, G);
+    if (st) return st;
+    G.ninst = ninst;
+    G.istride = G.cs;
+    G.cs *= ninst;
+    return BSSN_OK;
 }
 
-size_t bssn_patch_workspace_bytes(const BssnPatch* patch, const BssnParams* params) {
-    if (!patch) return 0;
+static size_t patch_block(const BssnPatch* patch) {
     size_t cs = 1;
     for (int d = 0; d < 3; ++d) cs *= (size_t)(patch->n[d] + 2 * patch->ghost);
+    return cs;
+}
+
+size_t bssn_batch_values(const BssnPatch* patch, int32_t ninst) {
+    if (!patch || ninst < 1) return 0;
+    return (size_t)NCOMP * (size_t)ninst * patch_block(patch);
+}
+
+size_t bssn_batch_workspace_bytes(const BssnPatch* patch, int32_t ninst, const BssnParams* params) {
+    if (!patch || ninst < 1) return 0;
     const bool with_mom = params && params->kappa != 0.0;
-    return (3 * NCOMP + rhs_work_blocks(with_mom)) * cs * sizeof(double);
+    return (3 * NCOMP + rhs_work_blocks(with_mom)) * (size_t)ninst * patch_block(patch) * sizeof(double);
 }
 
-int bssn_patch_import(const BssnFields* in, double* patch_state, const BssnPatch* patch, void* stream) {
-    if (!fields_ok(in) || !patch_state) return fail(BSSN_ERR_INVALID, "null pointer");
-    Geo G;
-    int st = patch_geo(patch, nullptr, G);
+static int instance_ok(int32_t ninst, int32_t instance) {
+    if (ninst < 1 || instance < 0 || instance >= ninst)
+        return fail(BSSN_ERR_INVALID, "instance index outside [0, instance count)");
+    return BSSN_OK;
+}
+
+int bssn_batch_import(const BssnFields* in, double* states, const BssnPatch* patch, int32_t ninst, int32_t instance,
+                      void* stream) {
+    if (!fields_ok(in) || !states) return fail(BSSN_ERR_INVALID, "null pointer");
+    int st = instance_ok(ninst, instance);
     if (st) return st;
+    Geo G;
+    if ((st = batch_geo(patch, ninst, nullptr, G))) return st;
     const Box region = box_of(G);
-    BSSN_LAUNCH(KC_IMPORT, k_import, nblocks(region.count * NCOMP), kThreads, (cudaStream_t)stream, leaves_in(in), patch_state, G,
-                                                                                  region, region.count);
-    return cuda_status(cudaGetLastError(), "bssn_patch_import");
+    BSSN_LAUNCH(KC_IMPORT, k_import, nblocks(region.count * NCOMP), kThreads, (cudaStream_t)stream, leaves_in(in),
+                states + (long long)instance * G.istride, G, region, region.count);
+    return cuda_status(cudaGetLastError(), "bssn_batch_import");
 }
 
-int bssn_patch_export(const double* patch_state, BssnFields* out, const BssnPatch* patch, void* stream) {
-    if (!fields_ok(out) || !patch_state) return fail(BSSN_ERR_INVALID, "null pointer");
-    Geo G;
-    int st = patch_geo(patch, nullptr, G);
+int bssn_batch_export(const double* states, BssnFields* out, const BssnPatch* patch, int32_t ninst,
+                      int32_t instance, void* stream) {
+    if (!fields_ok(out) || !states) return fail(BSSN_ERR_INVALID, "null pointer");
+    int st = instance_ok(ninst, instance);
     if (st) return st;
+    Geo G;
+    if ((st = batch_geo(patch, ninst, nullptr, G))) return st;
     const Box region = box_of(G);
-    BSSN_LAUNCH(KC_EXPORT, k_export, nblocks(region.count * NCOMP), kThreads, (cudaStream_t)stream, patch_state, leaves_out(out), G,
-                                                                                  region, region.count);
-    return cuda_status(cudaGetLastError(), "bssn_patch_export");
+    BSSN_LAUNCH(KC_EXPORT, k_export, nblocks(region.count * NCOMP), kThreads, (cudaStream_t)stream,
+                states + (long long)instance * G.istride, leaves_out(out), G, region, region.count);
+    return cuda_status(cudaGetLastError(), "bssn_batch_export");
 }
 
-int bssn_patch_fill_periodic(double* patch_state, const BssnPatch* patch, void* stream) {
-    if (!patch_state) return fail(BSSN_ERR_INVALID, "null pointer");
+int bssn_batch_fill_periodic(double* states, const BssnPatch* patch, int32_t ninst, void* stream) {
+    if (!states) return fail(BSSN_ERR_INVALID, "null pointer");
     Geo G;
-    int st = patch_geo(patch, nullptr, G);
+    const int st = batch_geo(patch, ninst, nullptr, G);
     if (st) return st;
-    return cuda_status(launch_fill_periodic(patch_state, NCOMP, G, (cudaStream_t)stream), "bssn_patch_fill_periodic");
+    return cuda_status(launch_fill_periodic(states, NCOMP, G, (cudaStream_t)stream), "bssn_batch_fill_periodic");
 }
 
-int bssn_patch_rk4(double* patch_state, const BssnPatch* patch, const BssnParams* params, int32_t steps,
+int bssn_batch_rk4(double* states, const BssnPatch* patch, int32_t ninst, const BssnParams* params, int32_t steps,
                    void* workspace, size_t workspace_bytes, void* stream) {
-    if (!patch_state) return fail(BSSN_ERR_INVALID, "null pointer");
+    if (!states) return fail(BSSN_ERR_INVALID, "null pointer");
     if (steps < 0) return fail(BSSN_ERR_INVALID, "steps must be non-negative");
     int st = validate_params(params);
     if (st) return st;
     Geo G;
-    if ((st = patch_geo(patch, params, G))) return st;
+    if ((st = batch_geo(patch, ninst, params, G))) return st;
     const bool with_mom = params->kappa != 0.0;
-    if (!workspace || workspace_bytes < bssn_patch_workspace_bytes(patch, params))
-        return fail(BSSN_ERR_WORKSPACE, "workspace missing or smaller than bssn_patch_workspace_bytes");
+    if (!workspace || workspace_bytes < bssn_batch_workspace_bytes(patch, ninst, params))
+        return fail(BSSN_ERR_WORKSPACE, "workspace missing or smaller than bssn_batch_workspace_bytes");
     cudaStream_t s = (cudaStream_t)stream;
     double* us = (double*)workspace;
     double* k = us + NCOMP * G.cs;
@@ -809,22 +841,51 @@ int bssn_patch_rk4(double* patch_state, const BssnPatch* patch, const BssnParams
     const Box region = box_of(G);
     cudaError_t e = cudaSuccess;
     for (int n = 0; n < steps && e == cudaSuccess; ++n) {
-        e = launch_project(patch_state, G, region, s);
-        if (e == cudaSuccess) e = rk4_step_patch(patch_state, us, k, acc, w, G, region, true, 0, s);
+        e = launch_project(states, G, region, s);
+        if (e == cudaSuccess) e = rk4_step_patch(states, us, k, acc, w, G, region, true, 0, s);
     }
-    return cuda_status(e, "bssn_patch_rk4");
+    return cuda_status(e, "bssn_batch_rk4");
+}
+
+int bssn_batch_check_finite(const double* states, const BssnPatch* patch, int32_t ninst, int32_t* device_flag,
+                            void* stream) {
+    if (!states || !device_flag) return fail(BSSN_ERR_INVALID, "null pointer");
+    Geo G;
+    const int st = batch_geo(patch, ninst, nullptr, G);
+    if (st) return st;
+    const Box region = box_of(G);
+    BSSN_LAUNCH(KC_OTHER, k_count_nonfinite, nblocks(box_threads(G, region)), kThreads, (cudaStream_t)stream, states,
+                G, region, (int*)device_flag);
+    return cuda_status(cudaGetLastError(), "bssn_batch_check_finite");
+}
+
+// The single-patch calls are the one-instance batch.
+size_t bssn_patch_values(const BssnPatch* patch) { return bssn_batch_values(patch, 1); }
+
+size_t bssn_patch_workspace_bytes(const BssnPatch* patch, const BssnParams* params) {
+    return bssn_batch_workspace_bytes(patch, 1, params);
+}
+
+int bssn_patch_import(const BssnFields* in, double* patch_state, const BssnPatch* patch, void* stream) {
+    return bssn_batch_import(in, patch_state, patch, 1, 0, stream);
+}
+
+int bssn_patch_export(const double* patch_state, BssnFields* out, const BssnPatch* patch, void* stream) {
+    return bssn_batch_export(patch_state, out, patch, 1, 0, stream);
+}
+
+int bssn_patch_fill_periodic(double* patch_state, const BssnPatch* patch, void* stream) {
+    return bssn_batch_fill_periodic(patch_state, patch, 1, stream);
+}
+
+int bssn_patch_rk4(double* patch_state, const BssnPatch* patch, const BssnParams* params, int32_t steps,
+                   void* workspace, size_t workspace_bytes, void* stream) {
+    return bssn_batch_rk4(patch_state, patch, 1, params, steps, workspace, workspace_bytes, stream);
 }
 
 int bssn_patch_check_finite(const double* patch_state, const BssnPatch* patch, int32_t* device_flag,
                             void* stream) {
-    if (!patch_state || !device_flag) return fail(BSSN_ERR_INVALID, "null pointer");
-    Geo G;
-    int st = patch_geo(patch, nullptr, G);
-    if (st) return st;
-    const Box region = box_of(G);
-    BSSN_LAUNCH(KC_OTHER, k_count_nonfinite, nblocks(region.count), kThreads, (cudaStream_t)stream, patch_state, G, region,
-                                                                                   (int*)device_flag);
-    return cuda_status(cudaGetLastError(), "bssn_patch_check_finite");
+    return bssn_batch_check_finite(patch_state, patch, 1, device_flag, stream);
 }
 
 }  // extern "C"

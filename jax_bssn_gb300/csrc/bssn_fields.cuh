@@ -83,6 +83,20 @@ __device__ __forceinline__ long long lin(const Geo& G, const int (&ix)[3]) {
     return (long long)ix[0] * G.st[0] + (long long)ix[1] * G.st[1] + ix[2];
 }
 
+// Threads of a launch over box B: count per instance times the instances.
+__host__ __device__ __forceinline__ long long box_threads(const Geo& G, const Box& B) {
+    return B.count * G.ninst;
+}
+
+// Split a launch's linear thread index into the index within one instance's
+// box (t, updated) and that instance's sample offset (returned).
+__device__ __forceinline__ long long instance_offset(const Geo& G, const Box& B, long long& t) {
+    if (G.ninst == 1) return 0;
+    const long long i = t / B.count;
+    t -= i * B.count;
+    return i * G.istride;
+}
+
 // ---------------------------------------------------------------------------
 // inverse metric by cofactors over the determinant, FMA allowed; a template on
 // the arithmetic type (the reciprocal in that type)

@@ -37,6 +37,12 @@ RhsWork carve_rhs_work(double* base, long long cs, bool with_mom);
 cudaError_t launch_rhs(const double* u, double* k, const RhsWork& w, const Geo& G, const Box& box,
                        cudaStream_t stream);
 
+// First derivatives of the NMIX fields (3 * NMIX blocks of d1, layout
+// d1[(d * NMIX + f) * cs + p]) on the box grown by the reach of the composed
+// mixed derivatives, for an all-periodic FP64 geometry: the inner factors the
+// RHS kernels differentiate again.
+cudaError_t launch_inner_derivs(const double* u, double* d1, const Geo& G, const Box& box, cudaStream_t stream);
+
 // FP32 form with w.uf already holding the float perturbations of the whole
 // padded block, about the backgrounds the FP32 RHS assumes (1 for the metric
 // diagonal, W and alpha; one sample's value for the shift and K; 0 else).

@@ -12,6 +12,7 @@ enum KernelClass {
     KC_FILL = 0, KC_FIRST, KC_GAUGE, KC_KGT, KC_AT, KC_MOM_DERIVED, KC_MOM_DAMP, KC_SOMMERFELD,
     KC_STAGE, KC_PROJECT, KC_IMPORT, KC_EXPORT, KC_CONSTRAINTS, KC_TRANSFER, KC_CARTOON, KC_CONVERT, KC_OTHER,
     KC_CURV, KC_SOLVE_NEWTON, KC_SOLVE_APPLY, KC_SOLVE_UPDATE, KC_HORIZON_SURFACE, KC_HORIZON_SOLVE,
+    KC_ADJ_POINT, KC_ADJ_STENCIL, KC_ADJ_STAGE,
     KC_COUNT
 };
 

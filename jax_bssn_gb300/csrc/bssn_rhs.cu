@@ -129,14 +129,15 @@ __device__ __forceinline__ R full_exact(const R* __restrict__ u, const double* _
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kThreads)
 k_perturb(const double* __restrict__ u, float* __restrict__ uf, Geo G, Box region, long long p0) {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= region.count) return;
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= box_threads(G, region)) return;
+    const long long off = instance_offset(G, region, t);
     int ix[3];
     region.coords(t, ix);
-    const long long p = lin(G, ix), cs = G.cs;
+    const long long p = lin(G, ix) + off, cs = G.cs;
 #pragma unroll
     for (int c = 0; c < NCOMP; ++c) {
-        const double b = has_background(c) ? 1.0 : (state_background(c) ? u[c * cs + p0] : 0.0);
+        const double b = has_background(c) ? 1.0 : (state_background(c) ? u[c * cs + p0 + off] : 0.0);
         uf[c * cs + p] = static_cast<float>(u[c * cs + p] - b);
     }
 }
@@ -149,12 +150,13 @@ __global__ void __launch_bounds__(kThreads)
 k_first_derivs(const R* __restrict__ u, const R* __restrict__ der, R* __restrict__ d1, Geo G, BoxSet S,
                int with_mom) {
     const Box& ext = S.b[blockIdx.y];
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= ext.count) return;
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= box_threads(G, ext)) return;
+    const long long off = instance_offset(G, ext, t);
     int ix[3];
     if constexpr (Closed) ext.coords(t, ix);
     else ext.coords_z(t, ix);
-    const long long p = lin(G, ix);
+    const long long p = lin(G, ix) + off;
     const long long cs = G.cs;
     const int nfield = with_mom ? NMIX + NMIX_MOM : NMIX;
 #pragma unroll 1
@@ -177,11 +179,12 @@ k_first_derivs(const R* __restrict__ u, const R* __restrict__ der, R* __restrict
 // AnyOrder = false: the box is known to run z fastest (closure-free interior boxes).
 template <bool AnyOrder = true>
 __device__ __forceinline__ bool point(const Box& B, PointCtx& c, const Geo& G) {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= B.count) return false;
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= box_threads(G, B)) return false;
+    const long long off = instance_offset(G, B, t);
     if constexpr (AnyOrder) B.coords(t, c.ix);
     else B.coords_z(t, c.ix);
-    c.p = lin(G, c.ix);
+    c.p = lin(G, c.ix) + off;
     return true;
 }
 
@@ -1118,9 +1121,9 @@ static long long largest(const BoxSet& S) {
 // kThreads would leave under four blocks per SM.  With GB300's two FP64 lanes
 // per SM per cycle, a small launch (a Cartoon plane, the shell of a small box)
 // otherwise runs a few FP64-heavy blocks on a few SMs while the rest idle.
-static inline int set_threads(const BoxSet& S) {
+static inline int set_threads(const BoxSet& S, int ninst) {
     long long total = 0;
-    for (int i = 0; i < S.n; ++i) total += S.b[i].count;
+    for (int i = 0; i < S.n; ++i) total += S.b[i].count * ninst;
     for (int t = kThreads; t > 32; t /= 2)
         if ((total + t - 1) / t >= 152LL * 4) return t;
     return 32;
@@ -1246,11 +1249,14 @@ static BoxSet face_slabs(const Geo& G, const Box& box) {
     return S;
 }
 
+// Launch over a box set; the launch's geometry must be in scope as G (its
+// instance count multiplies the threads).
 #define BSSN_LAUNCH_SET(cls, kernel, set, stream, ...)                                                     \
     do {                                                                                                  \
         if ((set).n > 0) {                                                                                \
-            const int threads_ = set_threads(set);                                                        \
-            BSSN_LAUNCH(cls, kernel, dim3((unsigned)((largest(set) + threads_ - 1) / threads_), (set).n),   \
+            const int threads_ = set_threads(set, G.ninst);                                               \
+            const long long cover_ = largest(set) * G.ninst;                                              \
+            BSSN_LAUNCH(cls, kernel, dim3((unsigned)((cover_ + threads_ - 1) / threads_), (set).n),         \
                         threads_, stream, __VA_ARGS__);                                                    \
         }                                                                                                 \
     } while (0)
@@ -1259,7 +1265,8 @@ cudaError_t launch_constraints(const double* u, const RhsWork& w, const Geo& G, 
                                double* M, double* detm1, double* trA, double* gam, cudaStream_t stream) {
     const Box ext = grown_box(box, G, composition_reach(G));
     // derived fields are pointwise and read on the box only
-    BSSN_LAUNCH(KC_MOM_DERIVED, k_mom_derived<double>, blocks_for(ext.count), kThreads, stream, u, u, w.der, G, ext);
+    BSSN_LAUNCH(KC_MOM_DERIVED, k_mom_derived<double>, blocks_for(box_threads(G, ext)), kThreads, stream, u, u, w.der,
+                G, ext);
     const BoxSet es = single(ext);
     BSSN_LAUNCH_SET(KC_FIRST, (k_first_derivs<double, true>), es, stream, u, w.der, w.d1, G, es, 0);
     BSSN_LAUNCH(KC_CONSTRAINTS, k_constraints, blocks_for(box.count), kThreads, stream, u, w.d1, w.der, G, box,
@@ -1339,7 +1346,8 @@ static void launch_rhs_form(const R* u, const double* u64, double* k, R* d1, R* 
     if (G.any_sommerfeld) {
         const BoxSet S = face_slabs(G, box);
         if (S.n > 0)
-            BSSN_LAUNCH(KC_SOMMERFELD, k_sommerfeld<R>, dim3(blocks_for(largest(S)), S.n, NCOMP / kSommerfeldGroup),
+            BSSN_LAUNCH(KC_SOMMERFELD, k_sommerfeld<R>,
+                        dim3(blocks_for(largest(S) * G.ninst), S.n, NCOMP / kSommerfeldGroup),
                         kThreads, stc, u, u64, k, G, S);
     }
     if (with_mom) {
@@ -1347,7 +1355,8 @@ static void launch_rhs_form(const R* u, const double* u64, double* k, R* d1, R* 
         // on ext grown by the first-derivative reach (3); being pointwise, they
         // take the same values there whatever region is computed.
         const Box region = grown_box(box, G, reach + 3);
-        BSSN_LAUNCH(KC_MOM_DERIVED, k_mom_derived<R>, blocks_for(region.count), kThreads, stream, u, u64, der, G,
+        BSSN_LAUNCH(KC_MOM_DERIVED, k_mom_derived<R>, blocks_for(box_threads(G, region)), kThreads, stream, u, u64,
+                    der, G,
                     region);
     }
     // The FP64 form is bound by FP64 instructions, so its shell slabs avoid
@@ -1408,6 +1417,14 @@ static void launch_rhs_form(const R* u, const double* u64, double* k, R* d1, R* 
     }
 }
 
+cudaError_t launch_inner_derivs(const double* u, double* d1, const Geo& G, const Box& box, cudaStream_t stream) {
+    // periodic boxes have no closure rows: the closure-free instantiation
+    // covers the box grown by the composition reach
+    const BoxSet es = single(grown_box(box, G, composition_reach(G)));
+    BSSN_LAUNCH_SET(KC_FIRST, (k_first_derivs<double, false>), es, stream, u, (const double*)nullptr, d1, G, es, 0);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_rhs_f32_prepared(const double* u, double* k, const RhsWork& w, const Geo& G, const Box& box,
                                     cudaStream_t stream) {
     launch_rhs_form<float>(w.uf, u, k, w.d1f, w.derf, w.dampf, w.mat, G, box, stream);
@@ -1423,7 +1440,8 @@ cudaError_t launch_rhs(const double* u, double* k, const RhsWork& w, const Geo& 
         const Box region = grown_box(box, G, 6);
         // background: each component's value at the box's first sample
         const long long p0 = (long long)box.lo[0] * G.st[0] + (long long)box.lo[1] * G.st[1] + box.lo[2];
-        BSSN_LAUNCH(KC_CONVERT, k_perturb, blocks_for(region.count), kThreads, stream, u, w.uf, G, region, p0);
+        BSSN_LAUNCH(KC_CONVERT, k_perturb, blocks_for(box_threads(G, region)), kThreads, stream, u, w.uf, G, region,
+                    p0);
         launch_rhs_form<float>(w.uf, u, k, w.d1f, w.derf, w.dampf, w.mat, G, box, stream);
     } else {
         launch_rhs_form<double>(u, u, k, w.d1, w.der, w.damp, w.mat, G, box, stream);

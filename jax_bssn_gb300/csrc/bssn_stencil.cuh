@@ -77,6 +77,11 @@ struct Geo {
     int gauge, zero_shift;
     int any_sommerfeld;
     int precision;    // kPrecisionF64 or kPrecisionF32
+    // Independent instances of the same patch in one launch: buffers are laid
+    // out [component][instance][padded block], so cs = ninst * istride and an
+    // instance starts istride samples after the previous one.
+    int ninst;
+    long long istride;
     GeoF gf;
 };
 

@@ -63,3 +63,72 @@ class PatchEvolution(GraphSteps):
         _native.check(self.lib.bssn_patch_check_finite(self.u.data_ptr(), self.patch, flag.data_ptr(),
                                                        _device.stream_handle()), "bssn_patch_check_finite")
         return int(flag.item())
+
+
+class BatchEvolution(GraphSteps):
+    """Many independent instances of one grid, advanced by the same launches.
+
+    Every instance has the same shape and parameters (a seed ensemble, a set
+    of replicas); each is the reference's ``rk4_step`` repeated on its own
+    state.  The resident layout is [component][instance][padded block], so a
+    kernel launch covers every instance and one captured graph advances them
+    all.  Results equal separate ``PatchEvolution`` runs bit for bit.
+    """
+
+    def __init__(self, states, params: BSSNParameters, ghost: int = 4, precision: str | None = None):
+        states = list(states)
+        if not states:
+            raise ValueError("BatchEvolution needs at least one instance")
+        if params.guard_cells or params.owned_shape is not None:
+            raise ValueError("BatchEvolution evolves whole unpadded grids (guard_cells=0, owned_shape=None)")
+        self.lib = _native.load()
+        first, _ = _device.device_state(states[0])
+        self.device = first.lapse.device
+        self.shape = _device.spatial_shape(first)
+        self.params = params
+        self.instances = len(states)
+        self.patch = _native.BssnPatch()
+        for d in range(3):
+            self.patch.n[d] = self.shape[d]
+        self.patch.ghost = int(ghost)
+        self.cparams = _device.to_params(params, precision)
+        values = self.lib.bssn_batch_values(self.patch, self.instances)
+        if values == 0:
+            raise ValueError("invalid patch description")
+        self.padded = tuple(n + 2 * ghost for n in self.shape)
+        self.u = torch.zeros(values, dtype=torch.float64, device=self.device)
+        nbytes = self.lib.bssn_batch_workspace_bytes(self.patch, self.instances, self.cparams)
+        self.ws = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
+        for i, vars in enumerate(states):
+            state, _ = _device.device_state(vars)
+            if _device.spatial_shape(state) != self.shape:
+                raise ValueError("every instance must have the same grid shape")
+            _native.check(self.lib.bssn_batch_import(_device.fields_struct(state), self.u.data_ptr(), self.patch,
+                                                     self.instances, i, _device.stream_handle()),
+                          "bssn_batch_import")
+
+    def _advance(self, steps: int) -> None:
+        _native.check(self.lib.bssn_batch_rk4(self.u.data_ptr(), self.patch, self.instances, self.cparams,
+                                              int(steps), self.ws.data_ptr(), self.ws.numel(),
+                                              _device.stream_handle()), "bssn_batch_rk4")
+
+    def state(self, instance: int = 0) -> BSSNVariables:
+        out = _device.empty_state(self.shape, self.device)
+        _native.check(self.lib.bssn_batch_export(self.u.data_ptr(), _device.fields_struct(out), self.patch,
+                                                 self.instances, int(instance), _device.stream_handle()),
+                      "bssn_batch_export")
+        return out
+
+    def states(self) -> list:
+        return [self.state(i) for i in range(self.instances)]
+
+    def components(self) -> torch.Tensor:
+        """View of the resident state as (21, instances, nx+2G, ny+2G, nz+2G)."""
+        return self.u.view(NCOMP, self.instances, *self.padded)
+
+    def nonfinite_count(self) -> int:
+        flag = torch.zeros(1, dtype=torch.int32, device=self.device)
+        _native.check(self.lib.bssn_batch_check_finite(self.u.data_ptr(), self.patch, self.instances,
+                                                       flag.data_ptr(), _device.stream_handle()),
+                      "bssn_batch_check_finite")
+        return int(flag.item())

@@ -67,6 +67,45 @@ def _inverse_sym(g):
     return inv, det
 
 
+# Platform-independent elementary functions.  NumPy's exp and pow may differ
+# by an ulp between CPU builds (x86-64 and Arm use different vector
+# libraries); the functions below use only IEEE-rounded +, -, *, /, rint and
+# ldexp in a fixed order, so the initial data they build are the same bits on
+# every host -- which lets parity pins made on one machine be checked on
+# another.  Accuracy is within a few ulp of the exact values.
+
+_LN2_HI = 0.693145751953125            # 16 significant bits: k * _LN2_HI is exact for |k| < 2^37
+_LN2_LO = 1.4286068203094173e-06       # ln 2 - _LN2_HI
+_INV_LN2 = 1.4426950408889634
+
+
+def _exp_portable(x):
+    """exp(x) by Cody-Waite reduction x = k ln 2 + r, |r| <= ln 2 / 2, and the
+    degree-20 Taylor polynomial of exp(r) in Horner form."""
+    x = np.asarray(x, dtype=np.float64)
+    k = np.rint(x * _INV_LN2)
+    r = (x - k * _LN2_HI) - k * _LN2_LO
+    acc = np.ones_like(r)
+    for n in range(20, 0, -1):
+        acc = 1.0 + (r / float(n)) * acc
+    return np.ldexp(acc, k.astype(np.int64))
+
+
+def _power_near_one(x, exponent, terms=24):
+    """x ** exponent for |x - 1| < 0.01 by the binomial series in Horner form."""
+    x = np.asarray(x, dtype=np.float64)
+    e = x - 1.0
+    if np.max(np.abs(e)) >= 0.01:
+        raise ValueError("_power_near_one needs |x - 1| < 0.01")
+    coef = [1.0]
+    for k in range(1, terms + 1):
+        coef.append(coef[-1] * (exponent - (k - 1)) / k)
+    acc = np.full_like(e, coef[terms])
+    for k in range(terms - 1, -1, -1):
+        acc = coef[k] + e * acc
+    return acc
+
+
 def _d1_closed(f, axis, dx, closed):
     """Fourth-order centred derivative; one-sided 5-point closures at both
     ends when ``closed`` (otherwise periodic)."""
@@ -82,21 +121,35 @@ def _d1_closed(f, axis, dx, closed):
     return out
 
 
+def _ordered_sum(terms):
+    acc = None
+    for t in terms:
+        acc = t if acc is None else acc + t
+    return acc
+
+
 def discrete_connection(conformal_metric, dx, closed):
-    """Gamma^i = g^mn Gamma^i_mn from discrete D4 derivatives of gt."""
+    """Gamma^i = g^mn Gamma^i_mn from discrete D4 derivatives of gt (sums in a
+    fixed order, so the result does not depend on the host's BLAS/einsum)."""
     dg = np.stack([_d1_closed(conformal_metric, 2 + d, dx, closed) for d in range(3)])  # [k,i,j]
     gi, _ = _inverse_sym(conformal_metric)
-    c1 = 0.5 * (np.einsum("kij...->ijk...", dg) + np.einsum("jik...->ijk...", dg) - dg)
-    c2 = np.einsum("im...,mjk...->ijk...", gi, c1)
-    return np.einsum("mn...,imn...->i...", gi, c2)
+    R3 = range(3)
+    c1 = [[[0.5 * ((dg[k, i, j] + dg[j, i, k]) - dg[i, j, k]) for k in R3] for j in R3] for i in R3]
+    c2 = [[[_ordered_sum(gi[i, m] * c1[m][j][k] for m in R3) for k in R3] for j in R3] for i in R3]
+    return np.stack([_ordered_sum(gi[m, n] * c2[i][m][n] for m in R3 for n in R3) for i in R3])
 
 
 def bssn_from_adm(gamma, Kij, alpha, beta, connection=None, dx=None, closed=False):
-    """Physical (gamma_ij, K_ij) -> BSSN W-formulation variables."""
+    """Physical (gamma_ij, K_ij) -> BSSN W-formulation variables.  Metrics
+    within 1% of unit determinant use the portable power series for
+    det^(-1/6), so the result is host-independent."""
     gi, det = _inverse_sym(gamma)
-    W = det ** (-1.0 / 6.0)
+    if np.max(np.abs(det - 1.0)) < 0.01:
+        W = _power_near_one(det, -1.0 / 6.0)
+    else:
+        W = det ** (-1.0 / 6.0)
     gt = W * W * gamma
-    K = np.einsum("ij...,ij...->...", gi, Kij)
+    K = _ordered_sum(gi[i, j] * Kij[i, j] for i in range(3) for j in range(3))
     At = W * W * (Kij - gamma * K / 3.0)
     if connection is None:
         connection = discrete_connection(gt, dx, closed)
@@ -178,12 +231,16 @@ def linear_wave_state(X, Y, Z, amplitude=1.0e-8, wavelength=1.0) -> BSSNVariable
 def _gauss_odd_derivatives(r, a, w):
     """F(x) = a x exp(-x^2/w^2) and its first four derivatives at x = r."""
     u = r / w
-    e = np.exp(-u * u)
+    u2 = u * u
+    u3 = u2 * u
+    u4 = u2 * u2
+    u5 = u4 * u
+    e = _exp_portable(-u2)
     F0 = a * r * e
-    F1 = a * e * (1.0 - 2.0 * u * u)
-    F2 = a * e * (-6.0 * u + 4.0 * u ** 3) / w
-    F3 = a * e * (-6.0 + 24.0 * u * u - 8.0 * u ** 4) / (w * w)
-    F4 = a * e * (60.0 * u - 80.0 * u ** 3 + 16.0 * u ** 5) / w ** 3
+    F1 = a * e * (1.0 - 2.0 * u2)
+    F2 = a * e * (-6.0 * u + 4.0 * u3) / w
+    F3 = a * e * (-6.0 + 24.0 * u2 - 8.0 * u4) / (w * w)
+    F4 = a * e * (60.0 * u - 80.0 * u3 + 16.0 * u5) / (w * w * w)
     return F0, F1, F2, F3, F4
 
 
@@ -195,10 +252,14 @@ def teukolsky_radial(r, a, w):
     powers with odd n; all others vanish.
     """
     F0, F1, F2, F3, F4 = _gauss_odd_derivatives(r, a, w)
-    A = 3.0 * (-2.0 * F2 / r ** 3 + 3.0 * 2.0 * F1 / r ** 4 + 3.0 * (-2.0) * F0 / r ** 5)
-    B = -(2.0 * F3 / r ** 2 + 3.0 * (-2.0) * F2 / r ** 3 + 6.0 * 2.0 * F1 / r ** 4 + 6.0 * (-2.0) * F0 / r ** 5)
-    C = 0.25 * (-2.0 * F4 / r + 2.0 * 2.0 * F3 / r ** 2 + 9.0 * (-2.0) * F2 / r ** 3
-                + 21.0 * 2.0 * F1 / r ** 4 + 21.0 * (-2.0) * F0 / r ** 5)
+    r2 = r * r
+    r3 = r2 * r
+    r4 = r2 * r2
+    r5 = r4 * r
+    A = 3.0 * (-2.0 * F2 / r3 + 3.0 * 2.0 * F1 / r4 + 3.0 * (-2.0) * F0 / r5)
+    B = -(2.0 * F3 / r2 + 3.0 * (-2.0) * F2 / r3 + 6.0 * 2.0 * F1 / r4 + 6.0 * (-2.0) * F0 / r5)
+    C = 0.25 * (-2.0 * F4 / r + 2.0 * 2.0 * F3 / r2 + 9.0 * (-2.0) * F2 / r3
+                + 21.0 * 2.0 * F1 / r4 + 21.0 * (-2.0) * F0 / r5)
     return A, B, C
 
 
@@ -297,7 +358,7 @@ def brill_lindquist_plane_state(masses=(0.5, 0.5), separation=2.0, num_radial_po
     psi = np.ones_like(R)
     for m, zc in zip(masses, (-separation / 2.0, separation / 2.0)):
         psi = psi + m / (2.0 * np.sqrt(R * R + (Z - zc) ** 2))
-    W = psi ** -2
+    W = 1.0 / (psi * psi)
     full = np.concatenate((W[3::-1], W), axis=0)[:, None, :]       # even parity ghosts
     shape = full.shape
     g = np.broadcast_to(np.eye(3)[:, :, None, None, None], (3, 3) + shape).copy()
