@@ -211,11 +211,13 @@ int bssn_rhs_vjp(double* states, double* rhs_adjoint, double* state_adjoint, con
                  const BssnParams* params, void* workspace, size_t workspace_bytes, void* stream);
 
 /* Checkpointed evolution for reverse mode.  `segment` <= 0 selects
- * ceil(sqrt(steps)) steps between checkpoints; store_stages != 0 keeps, while
- * a segment is re-run backward, every step's four stage RHS values (one
- * forward re-run in total instead of two, at 4 more states per segment step).
- * The workspace holds ceil(steps / segment) checkpoints, segment step states
- * (x5 with store_stages) and about 20 working states. */
+ * ceil(sqrt(steps)) steps between checkpoints.  While the backward pass re-runs
+ * a segment it keeps, by store_stages: 0 the step-start states only (each
+ * step's stages are then recomputed: two forward re-runs in total); 1 also
+ * every step's four stage RHS values (one re-run; 4 more states per segment
+ * step); 2 also the four stage states (8 more).  With 1 or 2 the forward pass
+ * records the last segment itself.  The workspace holds ceil(steps / segment)
+ * checkpoints, the segment's states and about 20 working states. */
 size_t bssn_adjoint_workspace_bytes(const BssnPatch* patch, int32_t ninst, const BssnParams* params, int32_t steps,
                                     int32_t segment, int32_t store_stages);
 /* `steps` RK4 steps of every instance in place (bit-identical to
@@ -224,7 +226,9 @@ int bssn_adjoint_forward(double* states, const BssnPatch* patch, int32_t ninst, 
                          int32_t steps, int32_t segment, int32_t store_stages, void* workspace, size_t workspace_bytes,
                          void* stream);
 /* After bssn_adjoint_forward with the same arguments and workspace: on entry
- * `adjoint` holds d loss / d (final state), on exit d loss / d (initial state). */
+ * `adjoint` holds d loss / d (final state), on exit d loss / d (initial state).
+ * One backward pass per forward pass: with store_stages the forward pass
+ * records the last segment's stages, which the backward pass then overwrites. */
 int bssn_adjoint_backward(double* adjoint, const BssnPatch* patch, int32_t ninst, const BssnParams* params,
                           int32_t steps, int32_t segment, int32_t store_stages, void* workspace, size_t workspace_bytes,
                           void* stream);

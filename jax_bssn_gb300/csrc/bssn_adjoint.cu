@@ -32,11 +32,14 @@
 //
 // Evolutions are differentiated with sqrt(N) checkpointing: the forward pass
 // stores the state every `segment` steps; the backward pass re-runs each
-// segment from its checkpoint, either keeping every step's four stage RHS
-// values (store_stages = 1: one extra forward pass, more memory) or only the
-// step-start states (then each step's stages are recomputed once more).
+// segment from its checkpoint, keeping the step-start states and, by
+// store_stages: 0 nothing more (each step's stages are recomputed once more),
+// 1 every step's four stage RHS values (the stage states are then re-formed by
+// the cheap stage kernels), 2 the stage states as well.  With 1 or 2 the
+// forward pass records the last segment itself.
 // Everything runs on instance batches (layout [component][instance][block]).
 // Scope: all faces periodic, kappa = 0, no matter, FP64 arithmetic.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -113,7 +116,8 @@ __device__ __forceinline__ bool owned_point(const Geo& G, const Box& B, Pt& c) {
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kThreads)
 k_adj_point(const double* __restrict__ u, const double* __restrict__ d1, const double* __restrict__ kbar,
-            double* __restrict__ ubar, double* __restrict__ coef, Geo G, Box B, PointParams pp, int accumulate) {
+            double kscale, double* __restrict__ ubar, double* __restrict__ coef, Geo G, Box B, PointParams pp,
+            int accumulate) {
     Pt c;
     if (!owned_point(G, B, c)) return;
     const long long cs = G.cs, p = c.p;
@@ -150,7 +154,7 @@ k_adj_point(const double* __restrict__ u, const double* __restrict__ d1, const d
         }
     double kb[NCOMP];
 #pragma unroll
-    for (int f = 0; f < NCOMP; ++f) kb[f] = kbar[f * cs + p];
+    for (int f = 0; f < NCOMP; ++f) kb[f] = kscale * kbar[f * cs + p];
     double xb[kPointInputs];
     rhs_point_vjp(x, kb, pp, xb);
 #pragma unroll
@@ -191,8 +195,9 @@ __constant__ double kUp6[2][9] = {{0, 0, 2, -24, -35, 80, -30, 8, -1}, {1, -8, 3
 // Transposed stencils of every component at one point, the dissipation and
 // advection transposes, and the shift's adjoint from the advection terms.
 __global__ void __launch_bounds__(kThreads)
-k_adj_field(const double* __restrict__ u, const double* __restrict__ kbar, const double* __restrict__ coef,
-            const double* __restrict__ mbuf, double* __restrict__ ubar, Geo G, Box B) {
+k_adj_field(const double* __restrict__ u, const double* __restrict__ kbar, double kscale,
+            const double* __restrict__ coef, const double* __restrict__ mbuf, double* __restrict__ ubar, Geo G,
+            Box B) {
     Pt c;
     if (!owned_point(G, B, c)) return;
     const long long cs = G.cs, p = c.p;
@@ -211,6 +216,14 @@ k_adj_field(const double* __restrict__ u, const double* __restrict__ kbar, const
             w[a][k + 4] = (b == 0.0 || ax.reduced) ? 0.0 : b * c4;
         }
     }
+    // Where the shift vanishes on every tap of every lane of the warp the
+    // transposed advection is exactly zero: skip its taps (warp-uniform).
+    bool moving = false;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int k = 0; k < 9; ++k) moving = moving || w[a][k] != 0.0;
+    moving = __any_sync(__activemask(), moving);
     double shift_bar[3] = {0.0, 0.0, 0.0};
     double beta[3];
 #pragma unroll
@@ -232,16 +245,19 @@ k_adj_field(const double* __restrict__ u, const double* __restrict__ kbar, const
         const bool row_on = !(f >= BX && G.zero_shift);
         if (row_on) {
             const double* kf = kbar + f * cs + p;
-            r += KO<double, false, false>(kf, G, c.ix);
-            double adv = 0.0;
+            double lin = KO<double, false, false>(kf, G, c.ix);
+            if (moving) {
+                double adv = 0.0;
 #pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                const long long s = G.st[a];
+                for (int a = 0; a < 3; ++a) {
+                    const long long s = G.st[a];
 #pragma unroll
-                for (int k = -4; k <= 4; ++k) adv = fma(w[a][k + 4], kf[-k * s], adv);
+                    for (int k = -4; k <= 4; ++k) adv = fma(w[a][k + 4], kf[-k * s], adv);
+                }
+                lin += adv;
             }
-            r += adv;
-            const double kq = kf[0];
+            r = fma(kscale, lin, r);
+            const double kq = kscale * kf[0];
 #pragma unroll
             for (int a = 0; a < 3; ++a)
                 shift_bar[a] = fma(kq, UP1<double, false, false>(u + f * cs + p, G, a, c.ix[a], beta[a]), shift_bar[a]);
@@ -260,16 +276,16 @@ __device__ __forceinline__ void project_vjp(const double (&b)[12], const double 
 }
 
 // Final combination a = v0 + (dt/6)(((k1 + 2 k2) + 2 k3) + k4), u' = P(a):
-// from ubar' (in adj) writes v0bar and kbar_i = (dt/6){1,2,2,1} abar.
+// from ubar' (in adj) writes abar to v0bar and to abar; the stage RHS
+// adjoints are (dt/6){1,2,2,1} abar plus the stage terms, formed later.
 __global__ void __launch_bounds__(kThreads)
 k_adj_final(const double* __restrict__ v0, const double* __restrict__ k1, const double* __restrict__ k2,
             const double* __restrict__ k3, const double* __restrict__ k4, const double* __restrict__ adj,
-            double* __restrict__ v0bar, double* __restrict__ kb1, double* __restrict__ kb2, double* __restrict__ kb3,
-            double* __restrict__ kb4, Geo G, Box B) {
+            double* __restrict__ v0bar, double* __restrict__ abar, Geo G, Box B) {
     Pt c;
     if (!owned_point(G, B, c)) return;
     const long long cs = G.cs, p = c.p;
-    const double h6 = G.dt / 6.0, h3 = G.dt / 3.0;
+    const double h6 = G.dt / 6.0;
     double b[12], yb[12], bb[12];
 #pragma unroll
     for (int s = 0; s < 12; ++s) {
@@ -285,17 +301,17 @@ k_adj_final(const double* __restrict__ v0, const double* __restrict__ k1, const 
         const int s = f < 6 ? f : ((f >= AXX && f <= AZZ) ? 6 + (f - AXX) : -1);
         const double a = s >= 0 ? bb[s] : adj[q];
         v0bar[q] = a;
-        kb1[q] = h6 * a;
-        kb2[q] = h3 * a;
-        kb3[q] = h3 * a;
-        kb4[q] = h6 * a;
+        abar[q] = a;
     }
 }
 
-// Stage v = P(v0 + h k): from vbar adds bbar to v0bar and h bbar to kbar.
+// Stage v = P(v0 + h k): from vbar adds bbar to v0bar and writes the
+// adjoint of k, weight abar + h bbar (weight: k's factor in the final
+// combination).
 __global__ void __launch_bounds__(kThreads)
 k_adj_stage(const double* __restrict__ v0, const double* __restrict__ k, double h, const double* __restrict__ vbar,
-            double* __restrict__ v0bar, double* __restrict__ kbar, Geo G, Box B) {
+            double* __restrict__ v0bar, const double* __restrict__ abar, double weight, double* __restrict__ kbar,
+            Geo G, Box B) {
     Pt c;
     if (!owned_point(G, B, c)) return;
     const long long cs = G.cs, p = c.p;
@@ -314,7 +330,7 @@ k_adj_stage(const double* __restrict__ v0, const double* __restrict__ k, double 
         const int s = f < 6 ? f : ((f >= AXX && f <= AZZ) ? 6 + (f - AXX) : -1);
         const double a = s >= 0 ? bb[s] : vbar[q];
         v0bar[q] += a;
-        kbar[q] += h * a;
+        kbar[q] = fma(h, a, weight * abar[q]);
     }
 }
 
@@ -349,6 +365,10 @@ struct Plan {
     long long cs;        // component stride of a batch state
     size_t state;        // doubles per batch state (21 * cs)
     int steps, segment, nseg, store;
+    // Segment j holds len(j) steps, in order: the first takes the remainder,
+    // so the last -- recorded by the forward pass when stages are stored --
+    // is a full one.
+    int len(int j) const { return j == 0 ? steps - (nseg - 1) * segment : segment; }
 };
 
 int validate(const BssnParams* p, const char* where) {
@@ -391,7 +411,7 @@ int make_plan(const BssnPatch* patch, int32_t ninst, const BssnParams* params, i
     P.segment = segment > 0 ? segment : (steps > 0 ? (int)std::ceil(std::sqrt((double)steps)) : 1);
     if (P.segment > (steps > 0 ? steps : 1)) P.segment = steps > 0 ? steps : 1;
     P.nseg = steps > 0 ? (steps + P.segment - 1) / P.segment : 0;
-    P.store = store ? 1 : 0;
+    P.store = store < 0 ? 0 : (store > 2 ? 2 : store);
     return BSSN_OK;
 }
 
@@ -402,7 +422,8 @@ constexpr size_t kVjpBlocks = NCOEF + 3 * NMIX;
 struct Layout {
     double* ckpt;      // nseg states
     double* seg;       // segment states (step starts)
-    double* segk;      // store: segment x 4 stage RHS states
+    double* segk;      // store >= 1: segment x 4 stage RHS states
+    double* segv;      // store == 2: segment x 4 stage states (ghost-filled)
     double* V[4];      // stage states (ghost-filled)
     double* K[4];      // stage RHS values (recompute mode)
     double* KB[4];     // stage RHS adjoints
@@ -421,6 +442,7 @@ Layout layout_of(const Plan& P, double* base) {
     L.ckpt = take(P.nseg * P.state);
     L.seg = take((size_t)P.segment * P.state);
     L.segk = take(P.store ? (size_t)P.segment * 4 * P.state : 0);
+    L.segv = take(P.store == 2 ? (size_t)P.segment * 4 * P.state : 0);
     for (int i = 0; i < 4; ++i) L.V[i] = take(P.state);
     for (int i = 0; i < 4; ++i) L.K[i] = P.store ? nullptr : take(P.state);
     for (int i = 0; i < 4; ++i) L.KB[i] = take(P.state);
@@ -435,18 +457,32 @@ Layout layout_of(const Plan& P, double* base) {
 
 cudaError_t fill(double* a, int ncomp, const Geo& G, cudaStream_t s) { return launch_fill_periodic(a, ncomp, G, s); }
 
+// Stage RHS values and stage states of segment step n (the working buffers
+// when the mode does not keep them).
+void step_buffers(const Layout& L, const Plan& P, int n, double* K[4], double* V[4]) {
+    for (int i = 0; i < 4; ++i) {
+        K[i] = P.store ? L.segk + ((size_t)n * 4 + i) * P.state : L.K[i];
+        V[i] = P.store == 2 ? L.segv + ((size_t)n * 4 + i) * P.state : L.V[i];
+    }
+}
+
 // RHS VJP: ubar (= or +=) (dRHS/du)^T kbar at state u; u and kbar ghost-filled.
-cudaError_t rhs_vjp(const double* u, const double* kbar, double* ubar, int accumulate, double* coef, double* d1,
-                    const Geo& G, const Box& B, cudaStream_t s) {
+cudaError_t rhs_vjp(const double* u, const double* kbar, double kscale, double* ubar, int accumulate, double* coef,
+                    double* d1, const Geo& G, const Box& B, cudaStream_t s) {
     cudaError_t e = launch_inner_derivs(u, d1, G, B, s);
     if (e != cudaSuccess) return e;
     const unsigned nb = blocks_of(box_threads(G, B));
-    BSSN_LAUNCH(KC_ADJ_POINT, k_adj_point, nb, kThreads, s, u, d1, kbar, ubar, coef, G, B, point_params(G),
+    BSSN_LAUNCH(KC_ADJ_POINT, k_adj_point, nb, kThreads, s, u, d1, kbar, kscale, ubar, coef, G, B, point_params(G),
                 accumulate);
-    if ((e = fill(coef, NCOEF, G, s)) != cudaSuccess) return e;
+    // Stencils read the neighbours of the first-derivative coefficients of K
+    // and Gt (blocks 24..26 and 36..44) and of every second-derivative
+    // coefficient (45..110); the NMIX fields' first-derivative coefficients
+    // are read at their own point only.
+    if ((e = fill(coef + (long long)(I_DK - 21) * G.cs, 3, G, s)) != cudaSuccess) return e;
+    if ((e = fill(coef + (long long)(I_DGT - 21) * G.cs, NCOEF - (I_DGT - 21), G, s)) != cudaSuccess) return e;
     BSSN_LAUNCH(KC_ADJ_STENCIL, k_adj_mixed, nb, kThreads, s, coef, d1, G, B);
     if ((e = fill(d1, 3 * NMIX, G, s)) != cudaSuccess) return e;
-    BSSN_LAUNCH(KC_ADJ_STENCIL, k_adj_field, nb, kThreads, s, u, kbar, coef, d1, ubar, G, B);
+    BSSN_LAUNCH(KC_ADJ_STENCIL, k_adj_field, nb, kThreads, s, u, kbar, kscale, coef, d1, ubar, G, B);
     return cudaGetLastError();
 }
 
@@ -492,20 +528,25 @@ cudaError_t backward_step(const double* un, double* const V[4], double* const K[
     const Geo& G = P.G;
     const Box& B = P.B;
     const unsigned nb = blocks_of(box_threads(G, B));
-    BSSN_LAUNCH(KC_ADJ_STAGE, k_adj_final, nb, kThreads, s, V[0], K[0], K[1], K[2], K[3], adj, L.v0bar, L.KB[0],
-                L.KB[1], L.KB[2], L.KB[3], G, B);
+    // abar lives in KB[3]; the adjoints of k1..k3 go to KB[0..2]
+    double* abar = L.KB[3];
+    BSSN_LAUNCH(KC_ADJ_STAGE, k_adj_final, nb, kThreads, s, V[0], K[0], K[1], K[2], K[3], adj, L.v0bar, abar, G, B);
     cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = fill(abar, NCOMP, G, s);
+    // k4's adjoint is (dt/6) abar: the VJP scales abar as it reads it
     const double h[3] = {0.5 * G.dt, 0.5 * G.dt, G.dt};
+    const double weight[3] = {G.dt / 6.0, G.dt / 3.0, G.dt / 3.0};   // of k1, k2, k3 in the final combination
     for (int i = 3; i >= 1 && e == cudaSuccess; --i) {
-        // v_i = P(v0 + h k_i) with k_i = RHS(v_{i-1}) ... the RHS of v_i is K[i]
-        if ((e = fill(L.KB[i], NCOMP, G, s)) != cudaSuccess) break;
-        if ((e = rhs_vjp(V[i], L.KB[i], L.vb, 0, L.coef, L.d1, G, B, s)) != cudaSuccess) break;
-        BSSN_LAUNCH(KC_ADJ_STAGE, k_adj_stage, nb, kThreads, s, V[0], K[i - 1], h[i - 1], L.vb, L.v0bar,
-                    L.KB[i - 1], G, B);
+        // V[i] = P(V[0] + h[i-1] K[i-1]); its RHS is K[i]
+        const double* kin = i == 3 ? abar : L.KB[i];
+        const double scale = i == 3 ? G.dt / 6.0 : 1.0;
+        if ((e = rhs_vjp(V[i], kin, scale, L.vb, 0, L.coef, L.d1, G, B, s)) != cudaSuccess) break;
+        BSSN_LAUNCH(KC_ADJ_STAGE, k_adj_stage, nb, kThreads, s, V[0], K[i - 1], h[i - 1], L.vb, L.v0bar, abar,
+                    weight[i - 1], L.KB[i - 1], G, B);
         e = cudaGetLastError();
+        if (e == cudaSuccess) e = fill(L.KB[i - 1], NCOMP, G, s);
     }
-    if (e == cudaSuccess) e = fill(L.KB[0], NCOMP, G, s);
-    if (e == cudaSuccess) e = rhs_vjp(V[0], L.KB[0], L.v0bar, 1, L.coef, L.d1, G, B, s);
+    if (e == cudaSuccess) e = rhs_vjp(V[0], L.KB[0], 1.0, L.v0bar, 1, L.coef, L.d1, G, B, s);
     if (e == cudaSuccess) {
         BSSN_LAUNCH(KC_ADJ_STAGE, k_adj_initial, nb, kThreads, s, un, L.v0bar, adj, G, B);
         e = cudaGetLastError();
@@ -542,7 +583,7 @@ int bssn_rhs_vjp(double* states, double* rhs_adjoint, double* state_adjoint, con
     double* d1 = coef + (size_t)NCOEF * P.cs;
     cudaError_t e = fill(states, NCOMP, P.G, s);
     if (e == cudaSuccess) e = fill(rhs_adjoint, NCOMP, P.G, s);
-    if (e == cudaSuccess) e = rhs_vjp(states, rhs_adjoint, state_adjoint, 0, coef, d1, P.G, P.B, s);
+    if (e == cudaSuccess) e = rhs_vjp(states, rhs_adjoint, 1.0, state_adjoint, 0, coef, d1, P.G, P.B, s);
     return cuda_status(e, "bssn_rhs_vjp");
 }
 
@@ -569,7 +610,19 @@ int bssn_adjoint_forward(double* states, const BssnPatch* patch, int32_t ninst, 
     cudaError_t e = cudaSuccess;
     for (int j = 0; j < P.nseg && e == cudaSuccess; ++j) {
         e = cudaMemcpyAsync(L.ckpt + (size_t)j * P.state, states, P.state * sizeof(double), cudaMemcpyDeviceToDevice, s);
-        const int len = std::min(P.segment, P.steps - j * P.segment);
+        const int len = P.len(j);
+        if (P.store && j == P.nseg - 1) {
+            // the last segment is recorded now (step starts and stage RHS
+            // values), so the backward pass starts without re-running it
+            for (int n = 0; n < len && e == cudaSuccess; ++n) {
+                double* un = L.seg + (size_t)n * P.state;
+                e = cudaMemcpyAsync(un, states, P.state * sizeof(double), cudaMemcpyDeviceToDevice, s);
+                double *K[4], *V[4];
+                step_buffers(L, P, n, K, V);
+                if (e == cudaSuccess) e = record_step(un, V, K, L.acc, states, L.d1, P, s);
+            }
+            break;
+        }
         for (int n = 0; n < len && e == cudaSuccess; ++n) {
             e = launch_project(states, P.G, P.B, s);
             if (e == cudaSuccess) e = rk4_step_patch(states, L.V[0], L.V[1], L.acc, w, P.G, P.B, true, 0, s);
@@ -593,16 +646,20 @@ int bssn_adjoint_backward(double* adjoint, const BssnPatch* patch, int32_t ninst
     w.d1 = L.d1;
     cudaError_t e = cudaSuccess;
     for (int j = P.nseg - 1; j >= 0 && e == cudaSuccess; --j) {
-        const int len = std::min(P.segment, P.steps - j * P.segment);
-        // re-run the segment from its checkpoint, keeping step starts (and stages)
-        e = cudaMemcpyAsync(L.seg, L.ckpt + (size_t)j * P.state, P.state * sizeof(double), cudaMemcpyDeviceToDevice, s);
-        for (int n = 0; n + 1 < len + (P.store ? 1 : 0) && e == cudaSuccess; ++n) {
+        const int len = P.len(j);
+        // re-run the segment from its checkpoint, keeping step starts (and
+        // stages); with stored stages the forward pass recorded the last one
+        const bool recorded = P.store && j == P.nseg - 1;
+        if (!recorded)
+            e = cudaMemcpyAsync(L.seg, L.ckpt + (size_t)j * P.state, P.state * sizeof(double), cudaMemcpyDeviceToDevice,
+                                s);
+        for (int n = 0; !recorded && n + 1 < len + (P.store ? 1 : 0) && e == cudaSuccess; ++n) {
             double* un = L.seg + (size_t)n * P.state;
             if (P.store) {
-                double* K[4];
-                for (int i = 0; i < 4; ++i) K[i] = L.segk + ((size_t)n * 4 + i) * P.state;
+                double *K[4], *V[4];
+                step_buffers(L, P, n, K, V);
                 double* next = n + 1 < len ? L.seg + (size_t)(n + 1) * P.state : L.vb;
-                e = record_step(un, L.V, K, L.acc, next, L.d1, P, s);
+                e = record_step(un, V, K, L.acc, next, L.d1, P, s);
             } else {
                 double* next = L.seg + (size_t)(n + 1) * P.state;
                 e = cudaMemcpyAsync(next, un, P.state * sizeof(double), cudaMemcpyDeviceToDevice, s);
@@ -612,15 +669,11 @@ int bssn_adjoint_backward(double* adjoint, const BssnPatch* patch, int32_t ninst
         }
         for (int n = len - 1; n >= 0 && e == cudaSuccess; --n) {
             double* un = L.seg + (size_t)n * P.state;
-            double* K[4];
-            if (P.store) {
-                for (int i = 0; i < 4; ++i) K[i] = L.segk + ((size_t)n * 4 + i) * P.state;
-                e = replay_stages(un, K, L.V, L.acc, P, s);
-            } else {
-                for (int i = 0; i < 4; ++i) K[i] = L.K[i];
-                e = record_step(un, L.V, K, L.acc, L.vb, L.d1, P, s);
-            }
-            if (e == cudaSuccess) e = backward_step(un, L.V, K, adjoint, L, P, s);
+            double *K[4], *V[4];
+            step_buffers(L, P, n, K, V);
+            if (P.store == 1) e = replay_stages(un, K, V, L.acc, P, s);
+            else if (P.store == 0) e = record_step(un, V, K, L.acc, L.vb, L.d1, P, s);
+            if (e == cudaSuccess) e = backward_step(un, V, K, adjoint, L, P, s);
         }
     }
     return cuda_status(e, "bssn_adjoint_backward");

@@ -495,14 +495,15 @@ def emit_function(P, outs, fname, nin, nout, vjp, param_names=()):
         sig = (f"__device__ __forceinline__ void {fname}(const double (&x)[{nin}]"
                + (", const PointParams& pp" if param_names else "") + f", double (&y)[{nout}])")
     lines.append(sig + " {")
-    for n, (op, args, payload) in enumerate(P.nodes):
-        if need[n] and op not in ("in", "param", "const"):
-            lines.append(f"    const double t{n} = {_expr(P, n, name)};")
     if not vjp:
+        for n, (op, args, payload) in enumerate(P.nodes):
+            if need[n] and op not in ("in", "param", "const"):
+                lines.append(f"    const double t{n} = {_expr(P, n, name)};")
         for k, o in enumerate(outs):
             lines.append(f"    y[{k}] = {name(o.n)};")
         lines.append("}")
         return "\n".join(lines)
+    forward_at = len(lines)
     # reverse sweep: node adjoints as sums of their contributions, each
     # emitted once all users of the node (which come later) are processed;
     # input adjoints accumulate into xbar.
@@ -520,6 +521,8 @@ def emit_function(P, outs, fname, nin, nout, vjp, param_names=()):
         if not need[n] or op in ("in", "param", "const") or n not in contrib:
             continue
         terms = contrib.pop(n)
+        if all(P.nodes[k][0] in ("const", "param") for k in args):
+            continue   # nothing upstream takes an adjoint
         lines.append(f"    const double a{n} = {' + '.join(terms)};")
         a = f"a{n}"
         if op == "add":
@@ -547,6 +550,19 @@ def emit_function(P, outs, fname, nin, nout, vjp, param_names=()):
         k = int(name_[1:])
         lines.append(f"    xbar[{k}] = {' + '.join(terms) if terms else '0.0'};")
     lines.append("}")
+    # forward values the reverse sweep reads, and what they depend on
+    import re
+    used = {int(m) for line in lines[forward_at:] for m in re.findall(r"\bt(\d+)\b", line)}
+    keep = set()
+    stack = list(used)
+    while stack:
+        n = stack.pop()
+        if n in keep or P.nodes[n][0] in ("in", "param", "const"):
+            continue
+        keep.add(n)
+        stack.extend(P.nodes[n][1])
+    forward = [f"    const double t{n} = {_expr(P, n, name)};" for n in range(len(P.nodes)) if n in keep]
+    lines[forward_at:forward_at] = forward
     return "\n".join(lines)
 
 

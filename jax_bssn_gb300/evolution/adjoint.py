@@ -113,14 +113,17 @@ def rhs_vjp(u: torch.Tensor, rhs_adjoint: torch.Tensor, params: BSSNParameters) 
 class CheckpointedEvolution:
     """`steps` RK4 steps of a component batch with sqrt(N) checkpoints kept
     for a later ``backward``.  ``segment`` (default ceil(sqrt(steps))) steps
-    separate checkpoints; ``store_stages`` keeps each re-run segment's stage
-    RHS values so the backward pass runs the forward once more instead of
-    twice."""
+    separate checkpoints.  ``store_stages`` sets what a re-run segment keeps:
+    0 step-start states only (stages recomputed: two forward re-runs), 1 (or
+    True) also the stage RHS values (one re-run), 2 also the stage states
+    (one re-run, no stage replay; the most memory)."""
 
     def __init__(self, u0: torch.Tensor, params: BSSNParameters, steps: int, segment: int = 0,
-                 store_stages: bool = True):
+                 store_stages: int = 1):
         self.B = _batch_for(u0, params)
-        self.steps, self.segment, self.store = int(steps), int(segment), int(bool(store_stages))
+        self.steps, self.segment, self.store = int(steps), int(segment), int(store_stages)
+        if self.store not in (0, 1, 2):
+            raise ValueError("store_stages must be 0, 1 or 2")
         if self.steps < 0:
             raise ValueError("steps must be non-negative")
         nbytes = self.B.lib.bssn_adjoint_workspace_bytes(self.B.patch, self.B.instances, self.B.cparams, self.steps,
@@ -142,11 +145,12 @@ class CheckpointedEvolution:
         return self.B.owned(self.state)
 
     def backward(self, final_adjoint: torch.Tensor) -> torch.Tensor:
-        """d loss / d initial state from d loss / d final state."""
+        """d loss / d initial state from d loss / d final state (once per forward)."""
         if not self.forward_done:
-            raise RuntimeError("backward needs the recorded forward pass")
+            raise RuntimeError("backward needs a recorded forward pass (one backward per forward)")
         adj = self.B.load(final_adjoint)
         _native.check(self.B.lib.bssn_adjoint_backward(adj.data_ptr(), *self._args()), "bssn_adjoint_backward")
+        self.forward_done = False   # the backward pass reuses the recorded segment's memory
         return self.B.owned(adj).clone()
 
 
@@ -155,7 +159,7 @@ class RK4Evolve(torch.autograd.Function):
     the adjoint kernels (torch.autograd.Function over the C ABI)."""
 
     @staticmethod
-    def forward(ctx, u0, params, steps, segment=0, store_stages=True):
+    def forward(ctx, u0, params, steps, segment=0, store_stages=1):
         run = CheckpointedEvolution(u0.detach(), params, steps, segment, store_stages)
         out = run.forward().clone()
         ctx.run = run
@@ -169,6 +173,6 @@ class RK4Evolve(torch.autograd.Function):
 
 
 def evolve(u0: torch.Tensor, params: BSSNParameters, steps: int, segment: int = 0,
-           store_stages: bool = True) -> torch.Tensor:
+           store_stages: int = 1) -> torch.Tensor:
     """Differentiable ``steps`` RK4 steps of a (21, instances, nx, ny, nz) batch."""
     return RK4Evolve.apply(u0, params, steps, segment, store_stages)

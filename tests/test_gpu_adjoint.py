@@ -189,7 +189,7 @@ def test_checkpoint_schedules_and_batching_are_bitwise(cuda, native):
     ybar = torch.randn(u0.shape, generator=gen, device="cuda", dtype=torch.float64)
     grads = []
     finals = []
-    for segment, store in ((0, True), (0, False), (1, True), (3, False), (7, True)):
+    for segment, store in ((0, 1), (0, 0), (1, 1), (3, 0), (7, 1), (0, 2), (2, 2)):
         run = CheckpointedEvolution(u0, params, steps, segment=segment, store_stages=store)
         finals.append(run.forward().clone())
         grads.append(run.backward(ybar))
