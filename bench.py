@@ -86,6 +86,15 @@ CLASS_BYTES_F32 = {
 COMPUTE_KERNEL = {"fp64": ("rhs_curv", 2590), "fp32": ("rhs_at", 1890)}
 LEAVES = ("conformal_metric", "conformal_factor", "traceless_K", "trace_K", "conformal_connection", "lapse",
           "shift")
+# DRAM bytes per evolved point of the dominant kernel class in one RHS
+# evaluation (dram__bytes_read.sum + dram__bytes_write.sum over its launches
+# divided by the points), from the ncu captures summarised in profiles/
+# (workload, form, class) -> (bytes per point, capture).  Traffic grows with
+# the points of a launch, so a launch's traffic is this times its points.
+MEASURED_TRAFFIC = {
+    ("teukolsky", "fp64", "rhs_curv"): (936, "profiles/k_rhs_curv_teukolsky96_fp64.md (96^3)"),
+    ("teukolsky", "fp32", "rhs_at"): (564, "profiles/k_rhs_at_teukolsky96_fp32.md (96^3)"),
+}
 
 
 def background(leaf, t):
@@ -103,12 +112,14 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
     ap.add_argument("--workload", choices=("teukolsky", "fmr", "axisymmetric", "puncture", "puncture_axi",
-                                           "horizon"),
+                                           "horizon", "adjoint", "batch"),
                     default="teukolsky")
     ap.add_argument("--n", type=int, default=None, help="grid size (teukolsky n, fmr root n, axisymmetric Nrho)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-graph", action="store_true", help="launch each step's kernels directly (no CUDA graph)")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="default workload only: skip the FMR and axisymmetric measurements on the same line")
     return ap.parse_args()
 
 
@@ -877,7 +888,7 @@ def compute_roofline_of(prof, points, profiled_steps, peak_gflops, precision):
             "peak_source": "measured live by bssn_probe_fma_peak"}
 
 
-def roofline_of(prof, points, profiled_steps, hbm_peak, peak_src, value_per_gpu, precision="fp64"):
+def roofline_of(prof, points, profiled_steps, hbm_peak, peak_src, value_per_gpu, precision="fp64", workload=None):
     """Live roofline of the dominant kernel class from the per-launch CUDA-event
     accounting: algorithmic bytes of all its launches in the profiled steps
     divided by their summed device time."""
@@ -890,9 +901,15 @@ def roofline_of(prof, points, profiled_steps, hbm_peak, peak_src, value_per_gpu,
     if per_point is not None and ms > 0:
         alg = per_point * points * 4 * profiled_steps
         achieved = alg / (ms / 1e3) / 1e9
+    measured = MEASURED_TRAFFIC.get((workload, precision, name))
+    traffic = {}
+    if measured:
+        traffic = {"traffic_bytes_per_point": measured[0], "traffic_source": measured[1],
+                   "traffic_over_algorithmic": measured[0] / per_point if per_point else None}
     return {
         "bound": "hbm", "kernel": f"k_{name}", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-        "frac": (achieved / hbm_peak) if achieved else None, "traffic": None, "peak_source": peak_src,
+        "frac": (achieved / hbm_peak) if achieved else None,
+        "traffic": measured[0] * points if measured else None, **traffic, "peak_source": peak_src,
         "kernel_share": ms / total, "kernel_ms_per_launch": ms / max(launches, 1),
         "algorithmic_bytes_per_point": per_point,
         "step_hbm_frac": value_per_gpu * BYTES_PER_UPDATE / (hbm_peak * 1e9),
@@ -933,9 +950,10 @@ def run_gb300(args, world, rank, local):
     fma_peaks = {"fp64": _native.fma_peak_gflops(_native.PRECISION_F64),
                  "fp32": _native.fma_peak_gflops(_native.PRECISION_F32)}
 
-    def measure(precision):
+    def measure(wl, precision, steps):
         """Device-resident throughput of one arithmetic form, its per-kernel
         profile and live roofline, and end-to-end public-API throughput."""
+        points = wl.points
         evo = wl.resident(precision)
         for _ in range(args.warmup):
             evo.step(1)
@@ -952,7 +970,7 @@ def run_gb300(args, world, rank, local):
         t0 = torch.cuda.Event(enable_timing=True)
         t1 = torch.cuda.Event(enable_timing=True)
         t0.record(stream)
-        for _ in range(args.steps):
+        for _ in range(steps):
             evo.step(1)
         t1.record(stream)
         torch.cuda.synchronize()
@@ -960,11 +978,11 @@ def run_gb300(args, world, rank, local):
         launches = lib.bssn_launch_count() - launches0
         if evo.captured:
             # replays bypass the host-side counter: each runs the captured launches
-            launches += evo.graph_launches * args.steps
+            launches += evo.graph_launches * steps
             evo.release_graph()
         clock_info = clocks.stop()
         ms = _max_over_ranks(t0.elapsed_time(t1), world, device)
-        value = world * points * args.steps / (ms / 1e3)
+        value = world * points * steps / (ms / 1e3)
         # per-kernel device time (profiled pass, not part of `value`)
         profiled_steps = 2
         lib.bssn_profile_reset()
@@ -974,7 +992,7 @@ def run_gb300(args, world, rank, local):
         lib.bssn_profile_enable(0)
         prof = _native.profile_read()
         lib.bssn_profile_reset()
-        roofline = roofline_of(prof, points, profiled_steps, hbm_peak, peak_src, value / world, precision)
+        roofline = roofline_of(prof, points, profiled_steps, hbm_peak, peak_src, value / world, precision, wl.name)
         compute = compute_roofline_of(prof, points, profiled_steps, fma_peaks.get(precision), precision)
         total_prof = sum(v[0] for v in prof.values()) or 1.0
         kernels = {k: {"ms": round(v[0], 3), "launches": v[1], "share": round(v[0] / total_prof, 4)}
@@ -993,7 +1011,7 @@ def run_gb300(args, world, rank, local):
                 e0 = torch.cuda.Event(enable_timing=True)
                 e1 = torch.cuda.Event(enable_timing=True)
                 e0.record(stream)
-                for _ in range(args.steps):
+                for _ in range(steps):
                     for d, h in zip(dev, host):
                         d.copy_(h, non_blocking=True)
                     out = wl.public_step(dev)
@@ -1003,13 +1021,65 @@ def run_gb300(args, world, rank, local):
                 torch.cuda.synchronize()
                 barrier()
             ems = _max_over_ranks(e0.elapsed_time(e1), world, device)
-            e2e = {"value": world * points * args.steps / (ems / 1e3), "unit": UNIT,
-                   "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d, "ms_per_step": ems / args.steps}
+            e2e = {"value": world * points * steps / (ems / 1e3), "unit": UNIT,
+                   "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d, "ms_per_step": ems / steps}
         return {"evo": evo, "value": value, "ms": ms, "launches": launches, "clocks": clock_info,
                 "roofline": roofline, "compute": compute, "kernels": kernels, "e2e": e2e}
 
-    plain = measure("fp64")
-    chosen = measure("fp32")
+    def both_forms(wl, steps):
+        plain, chosen = measure(wl, "fp64", steps), measure(wl, "fp32", steps)
+        return plain, chosen, form_comparison(wl, plain, chosen, steps)
+
+    def form_comparison(wl, plain, chosen, steps):
+        return compare_forms(wl, plain, chosen, steps, args.warmup + steps + 2)
+
+    plain, chosen, chosen_form = both_forms(wl, args.steps)
+    value, ms, launches, clock_info = plain["value"], plain["ms"], plain["launches"], plain["clocks"]
+    roofline, kernel_table, e2e = plain["roofline"], plain["kernels"], plain["e2e"]
+
+    # The nested-FMR and axisymmetric workloads ride along on the default line
+    # (each a few seconds), so every evolution configuration is measured by
+    # the same run.
+    extra = {}
+    if args.workload == "teukolsky" and args.n is None and not args.no_extra:
+        for name in ("fmr", "axisymmetric"):
+            other = WORKLOADS[name](None)
+            other.setup(device)
+            p64, p32, form = both_forms(other, args.steps)
+            extra[name] = {"config": other.config(), "value": p64["value"], "unit": UNIT,
+                           "ms_per_step": p64["ms"] / args.steps, "roofline": p64["roofline"],
+                           "roofline_compute": p64["compute"], "e2e": p64["e2e"], "gpu_launches": p64["launches"],
+                           "clocks": p64["clocks"], "kernels": p64["kernels"], "chosen_form": form}
+            launches += p64["launches"] + p32["launches"]
+            del p64, p32, other
+            torch.cuda.empty_cache()
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(wl)
+
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    if rank != 0:
+        return None
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (analytic initial data generated on the host)",
+        "config": {**wl.config(), "execution": ("direct kernel launches" if args.no_graph else
+                                                "each timed step replays one RK4 step captured as a CUDA graph")},
+        "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+        "gpu_launches": launches, "clocks": clock_info, "kernels": kernel_table,
+        "roofline_compute": plain["compute"], "fma_peaks_gflops": fma_peaks, "chosen_form": chosen_form,
+    }
+    if extra:
+        line["workloads"] = extra
+    return line
+
+
+def compare_forms(wl, plain, chosen, steps, steps_run):
+    """The FP32 form against the FP64 run after the same number of steps."""
+    import torch
     # error of the FP32 form against the FP64 run after the same number of steps,
     # relative to each leaf's deviation from the flat background
     # (signal = that deviation's maximum, abs = the maximum difference; a leaf
@@ -1026,56 +1096,112 @@ def run_gb300(args, world, rank, local):
             e["abs"], e["signal"] = max(e["abs"], err), max(e["signal"], scale)
     n64, n32 = wl.norms(plain["evo"]), wl.norms(chosen["evo"])
     norm_keys = [k for k in ("hamiltonian_l2", "momentum_l2") if k in n64]
-    chosen_form = {
+    return {
         "arithmetic": "FP32 RHS stencils and algebra on perturbations about the flat background; "
                       "FP64 state, RK4 combination, projection, W/alpha/1/W and constraints",
-        "dtype": "f32 (f64 state)", "value": chosen["value"], "unit": UNIT, "ms_per_step": chosen["ms"] / args.steps,
+        "dtype": "f32 (f64 state)", "value": chosen["value"], "unit": UNIT,
+        "ms_per_step": chosen["ms"] / steps,
         "speedup_vs_fp64": chosen["value"] / plain["value"], "roofline": chosen["roofline"],
         "roofline_compute": chosen["compute"],
         "e2e": chosen["e2e"], "gpu_launches": chosen["launches"], "clocks": chosen["clocks"],
         "kernels": chosen["kernels"],
         "error_vs_fp64": {"metric": "per leaf rel = abs / signal, abs = max|fp32 - fp64|, signal = "
-                                    "max|fp64 - background|, after "
-                                    f"{args.warmup + args.steps + 2} steps", "per_leaf": errors},
+                                    f"max|fp64 - background|, after {steps_run} steps", "per_leaf": errors},
         "constraint_norms": {k: {"fp64": n64[k], "fp32": n32[k], "rel_diff": abs(n32[k] - n64[k]) / abs(n64[k])
                                  if n64[k] else None} for k in norm_keys},
     }
-    value, ms, launches, clock_info = plain["value"], plain["ms"], plain["launches"], plain["clocks"]
-    roofline, kernel_table, e2e = plain["roofline"], plain["kernels"], plain["e2e"]
-
-    cpu = None
-    if rank == 0 and not args.no_cpu:
-        cpu = cpu_baseline(wl)
-
-    if world > 1:
-        torch.distributed.destroy_process_group()
-    if rank != 0:
-        return None
-    return {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (analytic initial data generated on the host)",
-        "config": {**wl.config(), "execution": ("direct kernel launches" if args.no_graph else
-                                                "each timed step replays one RK4 step captured as a CUDA graph")},
-        "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-        "gpu_launches": launches, "clocks": clock_info, "kernels": kernel_table,
-        "roofline_compute": plain["compute"], "fma_peaks_gflops": fma_peaks, "chosen_form": chosen_form,
-    }
-
-
 # ----------------------------------------------------------------------------
 # CPU baseline / reference arm
 # ----------------------------------------------------------------------------
 
-def cpu_baseline(wl, steps=1):
-    """The reference algorithm on the host (NumPy restatement, one thread) on a
-    bounded sample of the same workload."""
-    run, pts, what = wl.cpu_sample()
+# The reference's CPU path is the NumPy restatement (JAX cannot be installed
+# here; the restatement reproduces the reference source's goldens bit for
+# bit).  NumPy runs one thread per process, so the host's cores run one
+# independent instance of a smaller grid of the same configuration each, in
+# processes started with `spawn` (no CUDA state is inherited).
+_POOL_STATE = {}
+
+
+def _pool_init(workload, kwargs):
+    os.environ.setdefault("OMP_NUM_THREADS", "1")
+    sys.path.insert(0, str(ROOT))
+    wl = WORKLOADS[workload](None)
+    run, pts, what = wl.cpu_sample(**kwargs)
+    _POOL_STATE.update(run=run, pts=pts, what=what)
+
+
+def _pool_step(steps):
     t = time.perf_counter()
-    run(steps)
-    dt = time.perf_counter() - t
-    return {"value": pts * steps / dt, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"{steps} {what} (NumPy restatement of the reference, single thread; JAX not installed)",
+    _POOL_STATE["run"](steps)
+    return time.perf_counter() - t, _POOL_STATE["pts"], _POOL_STATE["what"]
+
+
+CPU_SAMPLE = {"teukolsky": {"n": 40}, "fmr": {"root": 24}, "axisymmetric": {"nrho": 32}}
+
+
+class HostInstances:
+    """One oracle instance per host core; `step(k)` advances all of them k
+    RK4 steps at once and returns (wall seconds, points per instance, what)."""
+
+    def __init__(self, workload, cores=None):
+        import multiprocessing as mp
+        self.cores = cores or os.cpu_count() or 1
+        env_threads = {k: os.environ.get(k) for k in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")}
+        for k in env_threads:
+            os.environ[k] = "1"
+        ctx = mp.get_context("spawn")
+        self.pool = ctx.Pool(self.cores, initializer=_pool_init, initargs=(workload, CPU_SAMPLE[workload]))
+        for k, v in env_threads.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+
+    def step(self, steps=1):
+        t = time.perf_counter()
+        out = self.pool.map(_pool_step, [steps] * self.cores, chunksize=1)
+        return time.perf_counter() - t, out[0][1], out[0][2]
+
+    def close(self):
+        self.pool.close()
+        self.pool.join()
+
+
+def sample_config(wl, cores, what):
+    """The configuration that ran on the host: the workload's own keys, with
+    the sample's grid in place of the benchmarked one."""
+    cfg = dict(wl.config())
+    small = CPU_SAMPLE[wl.name]
+    if wl.name == "teukolsky":
+        cfg["grid"] = [small["n"]] * 3
+    elif wl.name == "fmr":
+        from jax_bssn_gb300.fmr import fine_active_shape
+        from jax_bssn_gb300.initial_data import fmr_linear_wave_hierarchy
+        root = small["root"]
+        cfg["patch_shapes"] = [[root] * 3] + [list(fine_active_shape(s))
+                                              for s in fmr_linear_wave_hierarchy(root).patches]
+    elif wl.name == "axisymmetric":
+        cfg["evolved"] = [small["nrho"], 2 * small["nrho"]]
+    cfg["workload"] = (f"host sample of the benchmarked configuration: {cores} concurrent instances, one per core, "
+                       f"each {what}")
+    cfg["instances"] = cores
+    cfg["sample_of"] = wl.config()["workload"]
+    return cfg
+
+
+def cpu_baseline(wl, steps=1):
+    """The reference algorithm (NumPy restatement) on every host core, one
+    instance of a smaller grid of the same configuration per core: one warm-up
+    and one timed RK4 step."""
+    host = HostInstances(wl.name)
+    try:
+        host.step(1)
+        dt, pts, what = host.step(steps)
+    finally:
+        host.close()
+    return {"value": host.cores * pts * steps / dt, "unit": UNIT, "cores": host.cores, "kind": "port",
+            "sample": f"{steps} RK4 step(s) of {host.cores} concurrent instances, one per core, each {what} "
+                      "(NumPy restatement of the reference; JAX not installed)",
             "seconds": dt}
 
 
@@ -1083,21 +1209,248 @@ def run_reference(args, world, rank):
     if rank != 0:
         return None
     wl = WORKLOADS[args.workload](args.n)
-    small = {"teukolsky": {"n": 24}, "fmr": {"root": 16}, "axisymmetric": {"nrho": 16}}[wl.name]
-    run, pts, what = wl.cpu_sample(**small)
-    run(args.warmup)
-    t = time.perf_counter()
-    run(args.steps)
-    dt = time.perf_counter() - t
-    value = pts * args.steps / dt
-    sample = (f"each step one of the {what}, NumPy restatement of the reference (the reference's JAX CPU "
-              "path cannot be installed here), single thread")
+    host = HostInstances(wl.name)
+    try:
+        for _ in range(args.warmup):
+            host.step(1)
+        dt = 0.0
+        for _ in range(args.steps):
+            step_dt, pts, what = host.step(1)
+            dt += step_dt
+    finally:
+        host.close()
+    value = host.cores * pts * args.steps / dt
+    sample = (f"each step one RK4 step of {host.cores} concurrent instances, one per host core, each {what}; "
+              "NumPy restatement of the reference (its JAX CPU path cannot be installed here)")
     return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": wl.config(), "impl": "reference",
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
+            "config": sample_config(wl, host.cores, what), "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": host.cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+# ----------------------------------------------------------------------------
+# adjoint (reverse-mode gradient) and instance batches
+# ----------------------------------------------------------------------------
+
+ADJOINT_METRIC = "BSSN reverse-mode gradient, grid-point RK4 steps/s (forward + adjoint)"
+# Executed FP64 flops per point of one k_adj_point launch (DFMA x 2 + DMUL + DADD,
+# ncu on the 32^3 x 4 gauge-wave case, profiles/k_adj_point_gauge_wave.md) and its
+# algorithmic bytes (21 state + 33 inner derivatives + 21 RHS adjoint read;
+# 21 state adjoint + 111 coefficients written).
+ADJ_POINT_FLOPS = 4762
+ADJ_POINT_BYTES = 8 * (21 + 33 + 21 + 21 + 111)
+
+
+def _gauge_wave_batch(n, seeds, device):
+    """C5 inputs: the periodic gauge wave with a seeded symmetric 1e-3 Gaussian
+    perturbation of gt_ij per seed (numpy default_rng(seed)), component form."""
+    import numpy as np
+    import torch
+    from jax_bssn_gb300.evolution.adjoint import components
+    from jax_bssn_gb300.initial_data import gauge_wave_config
+    state, params = gauge_wave_config(n=n)
+    base = components(state).to(device)
+    batch = []
+    for seed in range(seeds):
+        rng = np.random.default_rng(seed)
+        u = base.clone()
+        u[0:6] += torch.as_tensor(1e-3 * rng.standard_normal((6, n, n, n)), device=device)
+        batch.append(u)
+    return torch.stack(batch, dim=1).contiguous(), base, params
+
+
+def run_adjoint(args, world, rank, local):
+    import torch
+    from jax_bssn_gb300 import _native
+    from jax_bssn_gb300.evolution import BatchEvolution
+    from jax_bssn_gb300.evolution.adjoint import CheckpointedEvolution, leaves
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    lib = _native.load()
+    n, seeds, nsteps = args.n or 64, 16, 200
+    u0, base, params = _gauge_wave_batch(n, seeds, device)
+    points = seeds * n ** 3
+    stream = torch.cuda.current_stream()
+
+    def ev():
+        return torch.cuda.Event(enable_timing=True)
+
+    # the plain forward: the same batch, one captured RK4 step replayed
+    plain = BatchEvolution([leaves(u0[:, i]) for i in range(seeds)], params)
+    plain.step(1)
+    plain.capture(1)
+    plain.step(1)
+    target = BatchEvolution([leaves(base)], params)
+    target.step(nsteps)
+    from jax_bssn_gb300.evolution.adjoint import components
+    w_target = components(target.state(0))[6]
+    del target
+
+    def loss_adjoint(final):
+        ybar = torch.zeros_like(final)
+        ybar[6] = final[6] - w_target
+        return ybar
+
+    for _ in range(args.warmup):          # short gradients warm every kernel
+        run = CheckpointedEvolution(u0, params, 4, store_stages=2)
+        run.backward(loss_adjoint(run.forward()))
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    t = [ev() for _ in range(3)]
+    t[0].record(stream)
+    plain.step(nsteps)
+    t[1].record(stream)
+    torch.cuda.synchronize()
+    plain_ms = t[0].elapsed_time(t[1])
+    fwd_ms = bwd_ms = 0.0
+    launches0 = lib.bssn_launch_count()
+    run = None
+    for _ in range(args.steps):
+        run = None                        # one workspace at a time (~170 GB at 64^3 x 16)
+        run = CheckpointedEvolution(u0, params, nsteps, store_stages=2)
+        t[0].record(stream)
+        final = run.forward()
+        t[1].record(stream)
+        grad = run.backward(loss_adjoint(final))
+        t[2].record(stream)
+        torch.cuda.synchronize()
+        fwd_ms += t[0].elapsed_time(t[1])
+        bwd_ms += t[1].elapsed_time(t[2])
+    launches = lib.bssn_launch_count() - launches0
+    clock_info = clocks.stop()
+    memory_gb = run.ws.numel() / 1e9
+    run = final = None
+    torch.cuda.empty_cache()
+    value = points * nsteps * args.steps / ((fwd_ms + bwd_ms) / 1e3)
+    # roofline of the dominant adjoint kernel, from a profiled VJP pass
+    from jax_bssn_gb300.evolution.adjoint import rhs_vjp
+    lib.bssn_profile_reset()
+    lib.bssn_profile_enable(1)
+    rhs_vjp(u0, torch.randn_like(u0), params)
+    torch.cuda.synchronize()
+    lib.bssn_profile_enable(0)
+    prof = _native.profile_read()
+    lib.bssn_profile_reset()
+    point_ms = prof.get("adjoint_point", (0.0, 1))[0]
+    fma = _native.fma_peak_gflops(_native.PRECISION_F64)
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    roofline = {"bound": "hbm", "kernel": "k_adj_point", "achieved": ADJ_POINT_BYTES * points / (point_ms / 1e3) / 1e9,
+                "peak": hbm_peak, "unit": "GB/s", "frac": ADJ_POINT_BYTES * points / (point_ms / 1e3) / 1e9 / hbm_peak,
+                "traffic": None, "algorithmic_bytes_per_point": ADJ_POINT_BYTES,
+                "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
+                "note": "FP64-pipe bound; see roofline_compute"}
+    roofline_compute = {"bound": "fp64", "kernel": "k_adj_point",
+                        "achieved": ADJ_POINT_FLOPS * points / (point_ms / 1e3) / 1e12, "peak": fma / 1e3,
+                        "unit": "TFLOP/s", "frac": ADJ_POINT_FLOPS * points / (point_ms / 1e3) / 1e12 / (fma / 1e3),
+                        "flops_per_point": ADJ_POINT_FLOPS, "peak_source": "measured live by bssn_probe_fma_peak"}
+    # gradient check: central differences (h = 1e-6) along smooth directions
+    # of the metric perturbation, on the full configuration
+    import numpy as np
+
+    def loss_of(u):
+        run_ = BatchEvolution([leaves(u[:, i]) for i in range(seeds)], params)
+        run_.step(nsteps)
+        final_ = torch.stack([components(run_.state(i)) for i in range(seeds)], dim=1)
+        return 0.5 * float(((final_[6] - w_target) ** 2).sum())
+
+    axes = [torch.arange(n, device=device, dtype=torch.float64) * (2 * np.pi / n)] * 3
+    X, Y, Z = torch.meshgrid(*axes, indexing="ij")
+    checks = []
+    for k in range(2):
+        d = torch.zeros_like(u0)
+        for c in range(6):
+            d[c] = torch.sin(X + 0.7 * c + k) + 0.5 * torch.cos(2 * Y - c) + 0.3 * torch.sin(Z + X + 1.3 * k)
+        h = 1e-6
+        fd = (loss_of(u0 + h * d) - loss_of(u0 - h * d)) / (2 * h)
+        ad = float((grad * d).sum())
+        checks.append({"adjoint": ad, "central_difference": fd, "rel_diff": abs(ad - fd) / abs(fd)})
+    # end to end: the initial batch from pinned host memory, the gradient back
+    host_u = u0.cpu().pin_memory()
+    host_g = torch.empty_like(host_u).pin_memory()
+    e0, e1 = ev(), ev()
+    e0.record(stream)
+    dev_u = host_u.to(device, non_blocking=True)
+    run = CheckpointedEvolution(dev_u, params, nsteps, store_stages=2)
+    g = run.backward(loss_adjoint(run.forward()))
+    run = None
+    host_g.copy_(g, non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1)
+    nbytes = host_u.numel() * 8
+    return {
+        "metric": ADJOINT_METRIC, "value": value, "unit": "point-steps/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": (fwd_ms + bwd_ms) / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded perturbations)",
+        "config": {"workload": f"adjoint of the {n}^3 periodic gauge wave (A=0.1, nu=0.1, CFL 0.25), "
+                               f"{seeds} seeds in one batch, {nsteps} RK4 steps; loss 1/2 |W_N - W_target|^2 "
+                               "with W_target from the unperturbed run; gradient w.r.t. the seeded 1e-3 Gaussian "
+                               "perturbation of gt_ij",
+                   "grid": [n, n, n], "instances": seeds, "evolution_steps": nsteps,
+                   "checkpointing": f"sqrt(N): segments of ceil(sqrt({nsteps})) steps, stage RHS values and "
+                                    "stage states kept while a segment is re-run",
+                   "workspace_gb": memory_gb, "step": "one complete gradient (forward + backward)",
+                   "l2": "working set > 129 MB L2; no flush"},
+        "forward_ms": plain_ms, "recorded_forward_ms": fwd_ms / args.steps, "backward_ms": bwd_ms / args.steps,
+        "adjoint_over_forward": (bwd_ms / args.steps) / plain_ms,
+        "gradient_over_forward": ((fwd_ms + bwd_ms) / args.steps) / plain_ms,
+        "fd_check": checks, "roofline": roofline, "roofline_compute": roofline_compute,
+        "kernels_rhs_vjp": {k: {"ms": round(v[0], 3), "launches": v[1]} for k, v in prof.items()},
+        "e2e": {"value": points * nsteps / (e2e_ms / 1e3), "unit": "point-steps/s", "h2d_bytes_per_step": nbytes,
+                "d2h_bytes_per_step": nbytes, "ms_per_step": e2e_ms},
+        "gpu_launches": launches, "clocks": clock_info, "cpu_baseline": None,
+    }
+
+
+def run_batch(args, world, rank, local):
+    """Updates/s against batch size: the periodic gauge wave (64^3 and 32^3),
+    each timed step one captured RK4 step of the whole batch."""
+    import torch
+    from jax_bssn_gb300 import _native
+    from jax_bssn_gb300.evolution import BatchEvolution
+    from jax_bssn_gb300.initial_data import gauge_wave_config
+    torch.cuda.set_device(local)
+    lib = _native.load()
+    stream = torch.cuda.current_stream()
+    table, headline = {}, None
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches = 0
+    for n in (32, 64):
+        state, params = gauge_wave_config(n=n)
+        table[n] = {}
+        for b in (1, 2, 4, 8, 16):
+            evo = BatchEvolution([state] * b, params)
+            for _ in range(args.warmup):
+                evo.step(1)
+            evo.capture(1)
+            evo.step(1)
+            torch.cuda.synchronize()
+            t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            t0.record(stream)
+            evo.step(args.steps)
+            t1.record(stream)
+            torch.cuda.synchronize()
+            ms = t0.elapsed_time(t1)
+            launches += evo.graph_launches * args.steps
+            table[n][b] = {"updates_per_s": b * n ** 3 * args.steps / (ms / 1e3), "ms_per_step": ms / args.steps,
+                           "launches_per_step": evo.graph_launches}
+            del evo
+            torch.cuda.empty_cache()
+        headline = table[64][16]
+    return {"metric": METRIC, "value": headline["updates_per_s"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": headline["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "instance batches of the periodic gauge wave (A=0.1, harmonic, zero shift, "
+                                   "nu=0.1, CFL 0.25); value at 64^3 x 16 instances",
+                       "grids": [32, 64], "batches": [1, 2, 4, 8, 16],
+                       "execution": "each timed step replays one captured RK4 step of the whole batch"},
+            "by_grid_and_batch": table, "gpu_launches": launches, "clocks": clocks.stop(), "e2e": None,
+            "cpu_baseline": None}
 
 
 def main():
@@ -1109,6 +1462,14 @@ def main():
     elif args.workload == "horizon":
         out = (run_horizon_reference(args, world, rank) if args.impl == "reference"
                else run_horizon(args, world, rank, local))
+    elif args.workload in ("adjoint", "batch"):
+        if args.impl == "reference":
+            why = ("the reference never differentiates its evolution (jax.grad would need JAX, absent here)"
+                   if args.workload == "adjoint" else
+                   "instance batching has no reference counterpart (its per-instance arm is --workload teukolsky)")
+            out = {"impl": "reference", "unavailable": why} if rank == 0 else None
+        else:
+            out = (run_adjoint if args.workload == "adjoint" else run_batch)(args, world, rank, local)
     elif args.impl == "reference":
         out = run_reference(args, world, rank)
     else:

@@ -41,7 +41,7 @@ extern "C" {
 #define BSSN_ERR_WORKSPACE 2    /* workspace pointer null or too small */
 #define BSSN_ERR_CUDA 3         /* a CUDA launch or runtime call failed */
 #define BSSN_ERR_NONFINITE 4    /* non-finite value detected in the state */
-#define BSSN_ERR_TIMEOUT 5      /* a bounded device wait gave up */
+/* 5 is unused: no entry point waits on the device */
 #define BSSN_ERR_NOT_CONVERGED 6 /* an iterative solve ran out of iterations */
 
 #define BSSN_NCOMP 21           /* independent evolved components */
@@ -190,6 +190,17 @@ int bssn_batch_rk4(double* states, const BssnPatch* patch, int32_t ninst, const 
                    void* workspace, size_t workspace_bytes, void* stream);
 int bssn_batch_check_finite(const double* states, const BssnPatch* patch, int32_t ninst, int32_t* device_flag,
                             void* stream);
+/* bssn_batch_rk4 with a failure monitor (no reference counterpart: the
+ * reference lets NaN propagate).  Before the first step and after every
+ * `check_every` steps (and the last) it counts the non-finite owned values of
+ * all instances into *device_counter (one caller-provided device int32) and
+ * reads the count back, synchronising `stream`.  A nonzero count stops the
+ * run: BSSN_ERR_NONFINITE, with the count and the step in bssn_last_error();
+ * *steps_done (host) receives the steps completed before the check that
+ * failed, or `steps`. */
+int bssn_batch_rk4_monitored(double* states, const BssnPatch* patch, int32_t ninst, const BssnParams* params,
+                             int32_t steps, int32_t check_every, int32_t* device_counter, int32_t* steps_done,
+                             void* workspace, size_t workspace_bytes, void* stream);
 
 /* ---------------- adjoint (reverse mode) ----------------
  * Gradients of periodic evolutions.  The reference has no hand-written

@@ -23,7 +23,6 @@ BSSN_ERR_INVALID = 1
 BSSN_ERR_WORKSPACE = 2
 BSSN_ERR_CUDA = 3
 BSSN_ERR_NONFINITE = 4
-BSSN_ERR_TIMEOUT = 5
 BSSN_ERR_NOT_CONVERGED = 6
 
 PRECISION_F64 = 0
@@ -141,6 +140,10 @@ SIGNATURES = {
     "bssn_adjoint_backward": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BssnPatch), ctypes.c_int32,
                                              ctypes.POINTER(BssnParams), ctypes.c_int32, ctypes.c_int32,
                                              ctypes.c_int32, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    "bssn_batch_rk4_monitored": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BssnPatch), ctypes.c_int32,
+                                                ctypes.POINTER(BssnParams), ctypes.c_int32, ctypes.c_int32,
+                                                ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32), ctypes.c_void_p,
+                                                ctypes.c_size_t, ctypes.c_void_p]),
     "bssn_fields_to_components": (ctypes.c_int, [ctypes.POINTER(BssnFields), ctypes.c_void_p, Shape3,
                                                  ctypes.c_void_p]),
     "bssn_components_to_fields": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BssnFields), Shape3,

@@ -9,6 +9,7 @@
 // steppers) or u0 + (dt*sum)/6 (JAX_BSSN/fmr/tiled.py:195-196).  Together
 // with the bit-exact projection this keeps the evolved state identical to the
 // float64 reference wherever the RHS agrees to the last bit.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -857,6 +858,43 @@ int bssn_batch_check_finite(const double* states, const BssnPatch* patch, int32_
     BSSN_LAUNCH(KC_OTHER, k_count_nonfinite, nblocks(box_threads(G, region)), kThreads, (cudaStream_t)stream, states,
                 G, region, (int*)device_flag);
     return cuda_status(cudaGetLastError(), "bssn_batch_check_finite");
+}
+
+int bssn_batch_rk4_monitored(double* states, const BssnPatch* patch, int32_t ninst, const BssnParams* params,
+                             int32_t steps, int32_t check_every, int32_t* device_counter, int32_t* steps_done,
+                             void* workspace, size_t workspace_bytes, void* stream) {
+    if (!states || !device_counter || !steps_done) return fail(BSSN_ERR_INVALID, "null pointer");
+    if (check_every < 1) return fail(BSSN_ERR_INVALID, "check_every must be positive");
+    *steps_done = 0;
+    Geo G;
+    int st = batch_geo(patch, ninst, nullptr, G);
+    if (st) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    const Box region = box_of(G);
+    int done = 0;
+    for (;;) {
+        cudaError_t e = cudaMemsetAsync(device_counter, 0, sizeof(int32_t), s);
+        if (e == cudaSuccess) {
+            BSSN_LAUNCH(KC_OTHER, k_count_nonfinite, nblocks(box_threads(G, region)), kThreads, s, states, G, region,
+                        (int*)device_counter);
+            e = cudaGetLastError();
+        }
+        int32_t count = 0;
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&count, device_counter, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return cuda_status(e, "bssn_batch_rk4_monitored");
+        if (count > 0)
+            return fail(BSSN_ERR_NONFINITE, std::to_string(count) + " non-finite owned values " +
+                                                (done == 0 ? std::string("in the state before step 1")
+                                                           : "after step " + std::to_string(done)));
+        if (done >= steps) break;
+        const int chunk = std::min(check_every, steps - done);
+        if ((st = bssn_batch_rk4(states, patch, ninst, params, chunk, workspace, workspace_bytes, stream)))
+            return st;
+        done += chunk;
+        *steps_done = done;
+    }
+    return BSSN_OK;
 }
 
 // The single-patch calls are the one-instance batch.

@@ -2,7 +2,7 @@
 
 from .time_evolve import (compute_bssn_rhs, compute_bssn_rhs_with_matter,
                           enforce_algebraic_constraints, rk4_step, rk4_steps)
-from .resident import BatchEvolution, PatchEvolution
+from .resident import BatchEvolution, NonFiniteStateError, PatchEvolution
 
 __all__ = ["compute_bssn_rhs", "compute_bssn_rhs_with_matter", "enforce_algebraic_constraints",
-           "rk4_step", "rk4_steps", "PatchEvolution", "BatchEvolution"]
+           "rk4_step", "rk4_steps", "PatchEvolution", "BatchEvolution", "NonFiniteStateError"]

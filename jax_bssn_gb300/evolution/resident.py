@@ -65,6 +65,15 @@ class PatchEvolution(GraphSteps):
         return int(flag.item())
 
 
+class NonFiniteStateError(FloatingPointError):
+    """A monitored evolution found NaN or infinite values; ``steps_done`` RK4
+    steps had completed before the check that found them."""
+
+    def __init__(self, message: str, steps_done: int):
+        super().__init__(message)
+        self.steps_done = steps_done
+
+
 class BatchEvolution(GraphSteps):
     """Many independent instances of one grid, advanced by the same launches.
 
@@ -118,6 +127,22 @@ class BatchEvolution(GraphSteps):
                                                  self.instances, int(instance), _device.stream_handle()),
                       "bssn_batch_export")
         return out
+
+    def step_monitored(self, steps: int, check_every: int = 1) -> int:
+        """``steps`` RK4 steps, counting non-finite values before the first and
+        every ``check_every`` steps; raises ``NonFiniteStateError`` (carrying
+        the steps completed) at the first check that finds any."""
+        import ctypes
+        counter = torch.zeros(1, dtype=torch.int32, device=self.device)
+        done = ctypes.c_int32(0)
+        status = self.lib.bssn_batch_rk4_monitored(self.u.data_ptr(), self.patch, self.instances, self.cparams,
+                                                   int(steps), int(check_every), counter.data_ptr(),
+                                                   ctypes.byref(done), self.ws.data_ptr(), self.ws.numel(),
+                                                   _device.stream_handle())
+        if status == _native.BSSN_ERR_NONFINITE:
+            raise NonFiniteStateError(_native.last_error(), done.value)
+        _native.check(status, "bssn_batch_rk4_monitored")
+        return done.value
 
     def states(self) -> list:
         return [self.state(i) for i in range(self.instances)]

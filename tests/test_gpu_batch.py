@@ -64,3 +64,32 @@ def test_batch_rejects_mismatched_instances(cuda, native):
     with pytest.raises(ValueError, match="same grid shape"):
         BatchEvolution([random_smooth_state((10, 10, 10)), random_smooth_state((10, 10, 12))],
                        BSSNParameters(dx=0.1, dt=0.01))
+
+
+def test_monitored_run_reports_non_finite_values(cuda, native):
+    """Failure detection: a NaN planted in one instance's host-prepared input
+    stops the monitored run before the first step with BSSN_ERR_NONFINITE; an
+    overflow planted in K turns non-finite during the run and is caught at the
+    next check; a finite batch runs through and equals the unmonitored run."""
+    import numpy as np
+    from jax_bssn_gb300.evolution import BatchEvolution, NonFiniteStateError
+    from jax_bssn_gb300.initial_data import gauge_wave_config
+    state, params = gauge_wave_config(n=12)
+    clean = BatchEvolution([state, state], params)
+    assert clean.step_monitored(6, check_every=2) == 6
+    plain = BatchEvolution([state, state], params)
+    plain.step(6)
+    for i in range(2):
+        assert worst(field_errors(clean.state(i), plain.state(i))) == 0.0
+    bad = state._replace(lapse=np.array(state.lapse, copy=True))
+    bad.lapse[3, 4, 5] = np.nan
+    evo = BatchEvolution([state, bad], params)
+    with pytest.raises(NonFiniteStateError, match="before step 1") as info:
+        evo.step_monitored(4, check_every=1)
+    assert info.value.steps_done == 0
+    hot = state._replace(trace_K=np.array(state.trace_K, copy=True))
+    hot.trace_K[6, 6, 6] = 1.0e200          # finite, but K^2 overflows in the first RHS
+    evo = BatchEvolution([hot, state], params)
+    with pytest.raises(NonFiniteStateError, match="after step") as info:
+        evo.step_monitored(6, check_every=2)
+    assert info.value.steps_done == 2
