@@ -92,8 +92,12 @@ LEAVES = ("conformal_metric", "conformal_factor", "traceless_K", "trace_K", "con
 # (workload, form, class) -> (bytes per point, capture).  Traffic grows with
 # the points of a launch, so a launch's traffic is this times its points.
 MEASURED_TRAFFIC = {
-    ("teukolsky", "fp64", "rhs_curv"): (936, "profiles/k_rhs_curv_teukolsky96_fp64.md (96^3)"),
-    ("teukolsky", "fp32", "rhs_at"): (564, "profiles/k_rhs_at_teukolsky96_fp32.md (96^3)"),
+    ("teukolsky", "fp64", "rhs_curv"): (1221, "profiles/traffic_full_size.md (one RK4 step at 128^3)"),
+    ("teukolsky", "fp32", "rhs_at"): (740, "profiles/traffic_full_size.md (one RK4 step at 128^3)"),
+    ("fmr", "fp64", "rhs_curv"): (906, "profiles/traffic_full_size.md (one RK4 step, 96^3 + 65^3 + 49^3)"),
+    ("fmr", "fp32", "rhs_at"): (534, "profiles/traffic_full_size.md (one RK4 step, 96^3 + 65^3 + 49^3)"),
+    ("axisymmetric", "fp64", "cartoon"): (1472, "profiles/traffic_full_size.md (one RK4 step, 256 x 512)"),
+    ("axisymmetric", "fp32", "cartoon"): (787, "profiles/traffic_full_size.md (one RK4 step, 256 x 512)"),
 }
 
 
@@ -1441,7 +1445,7 @@ def run_batch(args, world, rank, local):
                            "launches_per_step": evo.graph_launches}
             del evo
             torch.cuda.empty_cache()
-        headline = table[64][16]
+    headline = table[64][16]
     return {"metric": METRIC, "value": headline["updates_per_s"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": headline["ms_per_step"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",

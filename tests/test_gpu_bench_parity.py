@@ -62,6 +62,18 @@ def _report(tag, err):
     print(tag, {k: f"{v:.1e}" for k, v in err.items()})
 
 
+def _triangles(state, data, prefix, sets):
+    """Samples error of At's upper triangle (i <= j, the independent
+    components both codes evolve) and of its lower triangle."""
+    ix = np.ix_(*sets)
+    a = _host(state.traceless_K)[(Ellipsis,) + ix]
+    ref = data[f"{prefix}.traceless_K.samples"]
+    scale = float(np.max(data[f"{prefix}.traceless_K.max"]))
+    upper = max(float(np.max(np.abs(a[i, j] - ref[i, j]))) for i in range(3) for j in range(i, 3)) / scale
+    lower = max(float(np.max(np.abs(a[i, j] - ref[i, j]))) for i in range(3) for j in range(i)) / scale
+    return upper, lower
+
+
 def test_teukolsky128_one_and_ten_steps(cuda, native):
     from jax_bssn_gb300.evolution import time_evolve as te
     from jax_bssn_gb300.initial_data import teukolsky_config
@@ -73,6 +85,7 @@ def test_teukolsky128_one_and_ten_steps(cuda, native):
     one = te.rk4_step(state, params)
     e1 = _errors(one, data, "rk4_1", sets)
     _report("teukolsky128 1 step", e1)
+    print("teukolsky128 1 step At upper/lower triangle", _triangles(one, data, "rk4_1", sets))
     assert max(e1.values()) < STEP_TOL
     ten = te.rk4_steps(one, params, 9)
     e10 = _errors(ten, data, "rk4_10", sets)
