@@ -122,6 +122,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-graph", action="store_true", help="launch each step's kernels directly (no CUDA graph)")
+    ap.add_argument("--no-tune", action="store_true", help="keep the heuristic RHS launch shapes (no autotuning)")
     ap.add_argument("--no-extra", action="store_true",
                     help="default workload only: skip the FMR and axisymmetric measurements on the same line")
     return ap.parse_args()
@@ -959,6 +960,9 @@ def run_gb300(args, world, rank, local):
         profile and live roofline, and end-to-end public-API throughput."""
         points = wl.points
         evo = wl.resident(precision)
+        launch_shapes = None
+        if not args.no_tune and hasattr(evo, "tune"):
+            launch_shapes = evo.tune()      # autotuned RHS block sizes (untimed)
         for _ in range(args.warmup):
             evo.step(1)
         if not args.no_graph:
@@ -1028,7 +1032,8 @@ def run_gb300(args, world, rank, local):
             e2e = {"value": world * points * steps / (ems / 1e3), "unit": UNIT,
                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d, "ms_per_step": ems / steps}
         return {"evo": evo, "value": value, "ms": ms, "launches": launches, "clocks": clock_info,
-                "roofline": roofline, "compute": compute, "kernels": kernels, "e2e": e2e}
+                "roofline": roofline, "compute": compute, "kernels": kernels, "e2e": e2e,
+                "launch_shapes": launch_shapes or "heuristic (set_threads)"}
 
     def both_forms(wl, steps):
         plain, chosen = measure(wl, "fp64", steps), measure(wl, "fp32", steps)
@@ -1075,6 +1080,7 @@ def run_gb300(args, world, rank, local):
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
         "gpu_launches": launches, "clocks": clock_info, "kernels": kernel_table,
         "roofline_compute": plain["compute"], "fma_peaks_gflops": fma_peaks, "chosen_form": chosen_form,
+        "launch_shapes": {"fp64": plain["launch_shapes"], "fp32": chosen["launch_shapes"]},
     }
     if extra:
         line["workloads"] = extra
@@ -1429,6 +1435,8 @@ def run_batch(args, world, rank, local):
         table[n] = {}
         for b in (1, 2, 4, 8, 16):
             evo = BatchEvolution([state] * b, params)
+            if not args.no_tune:
+                evo.tune()
             for _ in range(args.warmup):
                 evo.step(1)
             evo.capture(1)

@@ -244,6 +244,20 @@ int bssn_adjoint_backward(double* adjoint, const BssnPatch* patch, int32_t ninst
                           int32_t steps, int32_t segment, int32_t store_stages, void* workspace, size_t workspace_bytes,
                           void* stream);
 
+/* No reference counterpart: launch-shape autotuning.  Times five RHS
+ * evaluations of this batch's state (ghosts refilled, owned values untouched)
+ * for each candidate block size (32, 64, 128 threads) of each RHS launch slot
+ * -- kernel class x interior/shell -- one slot at a time, and keeps the
+ * fastest when its time is below `margin` (> 0) x the time with the shapes in
+ * force (0.98: only a 2% gain changes a shape; 1 or more: always the fastest).
+ * Later launches of that slot at that launch size on this device in
+ * this arithmetic form use it (also single patches, FMR patches of the same
+ * padded extent, and CUDA-graph captures made afterwards); results are
+ * identical bit for bit.  Synchronises `stream`; refuses a stream that is being
+ * captured.  `report` (host, optional) receives a one-line summary. */
+int bssn_tune_patch(double* states, const BssnPatch* patch, int32_t ninst, const BssnParams* params, float margin,
+                    void* workspace, size_t workspace_bytes, char* report, size_t report_bytes, void* stream);
+
 /* Whole-array conversion between the reference layout (seven leaves) and the
  * 21-component layout, over all samples of an array of the given extent
  * (e.g. a padded FMR patch, whose guards are part of the array). */

@@ -144,6 +144,9 @@ SIGNATURES = {
                                                 ctypes.POINTER(BssnParams), ctypes.c_int32, ctypes.c_int32,
                                                 ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32), ctypes.c_void_p,
                                                 ctypes.c_size_t, ctypes.c_void_p]),
+    "bssn_tune_patch": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BssnPatch), ctypes.c_int32,
+                                       ctypes.POINTER(BssnParams), ctypes.c_float, ctypes.c_void_p, ctypes.c_size_t,
+                                       ctypes.c_char_p, ctypes.c_size_t, ctypes.c_void_p]),
     "bssn_fields_to_components": (ctypes.c_int, [ctypes.POINTER(BssnFields), ctypes.c_void_p, Shape3,
                                                  ctypes.c_void_p]),
     "bssn_components_to_fields": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BssnFields), Shape3,
@@ -285,3 +288,25 @@ def fma_peak_gflops(precision: int) -> float:
     out = ctypes.c_double(0.0)
     check(lib.bssn_probe_fma_peak(int(precision), ctypes.byref(out)), "bssn_probe_fma_peak")
     return out.value
+
+
+def tune_launch_shapes(state_ptr: int, shape, instances: int, cparams: BssnParams, device,
+                       workspace=None, margin: float = 0.98) -> str:
+    """Autotune the RHS launch shapes of a padded (ghost 4) batch state in
+    place (bssn_tune_patch): a slot takes the fastest candidate block size when
+    it times below ``margin`` x the current shapes; returns the report."""
+    import torch
+    from . import _device
+    lib = load()
+    patch = BssnPatch()
+    for d in range(3):
+        patch.n[d] = int(shape[d])
+    patch.ghost = 4
+    nbytes = lib.bssn_batch_workspace_bytes(patch, int(instances), cparams)
+    if workspace is None or workspace.numel() < nbytes:
+        workspace = torch.empty(nbytes, dtype=torch.uint8, device=device)
+    report = ctypes.create_string_buffer(4096)
+    check(lib.bssn_tune_patch(state_ptr, patch, int(instances), cparams, float(margin), workspace.data_ptr(),
+                              workspace.numel(),
+                              report, 4096, _device.stream_handle()), "bssn_tune_patch")
+    return report.value.decode()

@@ -497,16 +497,47 @@ cudaError_t launch_zero(double* u, long long n, cudaStream_t s) {
 // box B and the projection both before the first stage (serial stepper) and
 // after every combination.
 cudaError_t rk4_step_patch(double* u0, double* ustage, double* k, double* acc, const RhsWork& w,
-                           const Geo& G, const Box& B, bool fill, int final_form, cudaStream_t s) {
+                           const Geo& G, const Box& B, bool fill, int final_form, cudaStream_t s,
+                           const LowerTriangle* lower) {
     cudaError_t e;
     for (int stage = 1; stage <= 4; ++stage) {
         const double* src = stage == 1 ? u0 : ustage;
         if (fill && (e = launch_fill_periodic(const_cast<double*>(src), NCOMP, G, s)) != cudaSuccess) return e;
         if ((e = launch_rhs(src, k, w, G, B, s)) != cudaSuccess) return e;
+        if (lower && (e = launch_lower_triangle(src, w, lower->acc, lower->delta, G, B, stage, s)) != cudaSuccess)
+            return e;
         double* out = stage == 4 ? u0 : ustage;
         if ((e = launch_rk4_stage(u0, k, acc, out, G, B, stage, G.dt, final_form, 1, s)) != cudaSuccess) return e;
     }
     return cudaSuccess;
+}
+
+// delta_ij = At_ji - At_ij (i < j) of a reference-layout input, and the lower
+// triangle of an output as its upper triangle plus delta.
+__global__ void k_import_lower(const double* __restrict__ A, double* __restrict__ delta, Geo G, Box region,
+                               long long npts) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= region.count * 3) return;
+    const int k = (int)(t / region.count);
+    const long long r = t - (long long)k * region.count;
+    int ix[3];
+    region.coords(r, ix);
+    constexpr int pairs[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+    const int i = pairs[k][0], j = pairs[k][1];
+    delta[k * G.cs + lin(G, ix)] = A[(3 * j + i) * npts + r] - A[(3 * i + j) * npts + r];
+}
+
+__global__ void k_export_lower(double* __restrict__ A, const double* __restrict__ delta, Geo G, Box region,
+                               long long npts) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= region.count * 3) return;
+    const int k = (int)(t / region.count);
+    const long long r = t - (long long)k * region.count;
+    int ix[3];
+    region.coords(r, ix);
+    constexpr int pairs[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+    const int i = pairs[k][0], j = pairs[k][1];
+    A[(3 * j + i) * npts + r] = A[(3 * i + j) * npts + r] + delta[k * G.cs + lin(G, ix)];
 }
 
 }  // namespace bssn
@@ -557,10 +588,20 @@ LeavesOut leaves_out(BssnFields* f) {
                       f->conformal_connection, f->lapse, f->shift}};
 }
 
-size_t ref_workspace_values(int op, const RefLayout& L, bool with_mom) {
+// The reference-layout RK4 call carries the reference's At lower triangle
+// (launch_lower_triangle) in the plain FP64 form when a face is Sommerfeld.
+bool carries_lower_triangle(const BssnParams* p) {
+    if (!p || p->precision != BSSN_PRECISION_F64) return false;
+    for (int f = 0; f < 6; ++f)
+        if (p->bc[f] == 1) return true;
+    return false;
+}
+
+size_t ref_workspace_values(int op, const RefLayout& L, bool with_mom, bool lower = false) {
     if (op == BSSN_OP_CONSTRAINTS) return (size_t)(NCOMP + 3 * NMIX + 24) * (size_t)L.cs;
     size_t blocks = (op == BSSN_OP_RK4 ? 4 * NCOMP : 2 * NCOMP) + rhs_work_blocks(with_mom);
     if (op == BSSN_OP_RHS_MATTER) blocks += kMatterComps;
+    if (op == BSSN_OP_RK4 && lower) blocks += 6;
     return blocks * (size_t)L.cs;
 }
 
@@ -580,7 +621,7 @@ size_t bssn_workspace_bytes(int op, const int32_t shape[3], const BssnParams* pa
     RefLayout L;
     if (ref_layout(shape, L) != BSSN_OK) return 0;
     const bool with_mom = params && params->kappa != 0.0;
-    return ref_workspace_values(op, L, with_mom) * sizeof(double);
+    return ref_workspace_values(op, L, with_mom, carries_lower_triangle(params)) * sizeof(double);
 }
 
 int bssn_rhs(const BssnFields* in, BssnFields* out, const int32_t shape[3], const BssnParams* params,
@@ -643,7 +684,8 @@ int bssn_rk4_step(BssnFields* state, const int32_t shape[3], const BssnParams* p
     Geo G;
     if ((st = make_geo(params, L.S, L.org, L.P, G))) return st;
     const bool with_mom = params->kappa != 0.0;
-    if (!workspace || workspace_bytes < ref_workspace_values(BSSN_OP_RK4, L, with_mom) * sizeof(double))
+    const bool lower = carries_lower_triangle(params);
+    if (!workspace || workspace_bytes < ref_workspace_values(BSSN_OP_RK4, L, with_mom, lower) * sizeof(double))
         return fail(BSSN_ERR_WORKSPACE, "workspace missing or smaller than bssn_workspace_bytes(BSSN_OP_RK4)");
     cudaStream_t s = (cudaStream_t)stream;
     double* u0 = (double*)workspace;
@@ -651,15 +693,24 @@ int bssn_rk4_step(BssnFields* state, const int32_t shape[3], const BssnParams* p
     double* k = us + NCOMP * L.cs;
     double* acc = k + NCOMP * L.cs;
     RhsWork w = carve_rhs_work(acc + NCOMP * L.cs, L.cs, with_mom);
+    LowerTriangle lt;
+    lt.delta = acc + (NCOMP + rhs_work_blocks(with_mom)) * L.cs;
+    lt.acc = lt.delta + 3 * L.cs;
     const Box region = box_of(G);
     BSSN_LAUNCH(KC_IMPORT, k_import, nblocks(region.count * NCOMP), kThreads, s, leaves_in(state), u0, G, region, L.npts);
+    if (lower)
+        BSSN_LAUNCH(KC_IMPORT, k_import_lower, nblocks(region.count * 3), kThreads, s, state->traceless_K, lt.delta, G,
+                    region, L.npts);
     cudaError_t e = cudaGetLastError();
     for (int n = 0; n < steps && e == cudaSuccess; ++n) {
         e = launch_project(u0, G, region, s);
-        if (e == cudaSuccess) e = rk4_step_patch(u0, us, k, acc, w, G, region, true, 0, s);
+        if (e == cudaSuccess) e = rk4_step_patch(u0, us, k, acc, w, G, region, true, 0, s, lower ? &lt : nullptr);
     }
     if (e == cudaSuccess) {
         BSSN_LAUNCH(KC_EXPORT, k_export, nblocks(region.count * NCOMP), kThreads, s, u0, leaves_out(state), G, region, L.npts);
+        if (lower)
+            BSSN_LAUNCH(KC_EXPORT, k_export_lower, nblocks(region.count * 3), kThreads, s, state->traceless_K, lt.delta,
+                        G, region, L.npts);
         e = cudaGetLastError();
     }
     return cuda_status(e, "bssn_rk4_step");
@@ -895,6 +946,33 @@ int bssn_batch_rk4_monitored(double* states, const BssnPatch* patch, int32_t nin
         *steps_done = done;
     }
     return BSSN_OK;
+}
+
+int bssn_tune_patch(double* states, const BssnPatch* patch, int32_t ninst, const BssnParams* params, float margin,
+                    void* workspace, size_t workspace_bytes, char* report, size_t report_bytes, void* stream) {
+    if (!states) return fail(BSSN_ERR_INVALID, "null pointer");
+    if (!(margin > 0.0f)) return fail(BSSN_ERR_INVALID, "bssn_tune_patch: margin must be positive");
+    int st = validate_params(params);
+    if (st) return st;
+    Geo G;
+    if ((st = batch_geo(patch, ninst, params, G))) return st;
+    if (!workspace || workspace_bytes < bssn_batch_workspace_bytes(patch, ninst, params))
+        return fail(BSSN_ERR_WORKSPACE, "workspace missing or smaller than bssn_batch_workspace_bytes");
+    cudaStream_t s = (cudaStream_t)stream;
+    double* k = (double*)workspace + NCOMP * G.cs;
+    RhsWork w = carve_rhs_work(k + 2 * NCOMP * G.cs, G.cs, params->kappa != 0.0);
+    const Box region = box_of(G);
+    std::string text;
+    cudaError_t e = launch_fill_periodic(states, NCOMP, G, s);
+    if (e == cudaSuccess) e = tune_rhs(states, k, w, G, region, s, 5, margin, &text);
+    if (e == cudaErrorStreamCaptureUnsupported)
+        return fail(BSSN_ERR_INVALID, "bssn_tune_patch: the stream is being captured; tune before capturing");
+    if (e == cudaSuccess && report && report_bytes > 0) {
+        const size_t n = std::min(text.size(), report_bytes - 1);
+        std::memcpy(report, text.data(), n);
+        report[n] = '\0';
+    }
+    return cuda_status(e, "bssn_tune_patch");
 }
 
 // The single-patch calls are the one-instance batch.

@@ -1,6 +1,8 @@
 // Internal host-side interface between the C ABI and the kernel launchers.
 #pragma once
 
+#include <string>
+
 #include <cuda_runtime.h>
 
 #include "bssn_fields.cuh"
@@ -36,6 +38,21 @@ RhsWork carve_rhs_work(double* base, long long cs, bool with_mom);
 
 cudaError_t launch_rhs(const double* u, double* k, const RhsWork& w, const Geo& G, const Box& box,
                        cudaStream_t stream);
+
+// FP64 form with Sommerfeld faces: the source of the reference's At lower
+// triangle minus its upper one (3 blocks: xy, xz, yz) on the face shell at RK4
+// stage `stage`, accumulated with the RK4 weights in acc and added to delta
+// (dt/6 acc) at stage 4.  Reads w.d1 of the RHS just evaluated on u.
+cudaError_t launch_lower_triangle(const double* u, const RhsWork& w, double* acc, double* delta, const Geo& G,
+                                  const Box& box, int stage, cudaStream_t stream);
+
+// Launch-shape autotuning of the RHS of one geometry: times `reps` RHS
+// evaluations per candidate block size of each launch slot and records the
+// fastest for later launches of that slot at that size when its time is below
+// `margin` x the current shapes' time (synchronises `stream`; refuses a
+// capturing stream).  A summary is appended to *report when given.
+cudaError_t tune_rhs(const double* u, double* k, const RhsWork& w, const Geo& G, const Box& box, cudaStream_t s,
+                     int reps, float margin, std::string* report);
 
 // First derivatives of the NMIX fields (3 * NMIX blocks of d1, layout
 // d1[(d * NMIX + f) * cs + p]) on the box grown by the reach of the composed

@@ -42,6 +42,9 @@
 //           (large near punctures) is formed in FP64.  The RHS is written in
 //           FP64, and the RK4 combination stays FP64.
 #include <map>
+#include <mutex>
+#include <string>
+#include <vector>
 
 #include "bssn_fields.cuh"
 #include "bssn_kernels.h"
@@ -1249,12 +1252,66 @@ static BoxSet face_slabs(const Geo& G, const Box& box) {
     return S;
 }
 
+// ---------------------------------------------------------------------------
+// Launch-shape autotuning.  A box-set launch belongs to a slot -- its kernel
+// class and whether it is the interior or the shell instantiation -- and
+// takes its block size from the tuning table when bssn_tune_patch has timed
+// that slot at that launch size on this device in this arithmetic form, else
+// from the set_threads heuristic.  Tuning times whole RHS evaluations with
+// each candidate block size for one slot at a time (coordinate descent) and
+// keeps the fastest; only the launch shape changes, so results are identical
+// bit for bit.
+// ---------------------------------------------------------------------------
+constexpr int kTuneCandidates[3] = {32, 64, 128};
+
+struct TuneKey {
+    int dev, cls, shell, precision;
+    long long size;
+    bool operator<(const TuneKey& o) const {
+        if (dev != o.dev) return dev < o.dev;
+        if (cls != o.cls) return cls < o.cls;
+        if (shell != o.shell) return shell < o.shell;
+        if (precision != o.precision) return precision < o.precision;
+        return size < o.size;
+    }
+};
+
+static std::mutex g_tune_lock;
+static std::map<TuneKey, int> g_tuned;
+// while tuning (on the tuning thread): the slot under test, its forced block
+// size, and the launch size the slot was seen with
+static thread_local int t_force_cls = -1, t_force_shell = -1, t_force_threads = 0;
+static thread_local long long t_seen_size = -1;
+
+static int launch_threads(int cls, int shell, const BoxSet& S, const Geo& G) {
+    long long total = 0;
+    for (int i = 0; i < S.n; ++i) total += S.b[i].count * G.ninst;
+    if (cls == t_force_cls && shell == t_force_shell) {
+        t_seen_size = total;
+        return t_force_threads;
+    }
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return set_threads(S, G.ninst);
+    }
+    {
+        std::lock_guard<std::mutex> guard(g_tune_lock);
+        if (!g_tuned.empty()) {
+            const auto it = g_tuned.find(TuneKey{dev, cls, shell, G.precision, total});
+            if (it != g_tuned.end()) return it->second;
+        }
+    }
+    return set_threads(S, G.ninst);
+}
+
 // Launch over a box set; the launch's geometry must be in scope as G (its
-// instance count multiplies the threads).
-#define BSSN_LAUNCH_SET(cls, kernel, set, stream, ...)                                                     \
+// instance count multiplies the threads).  shell: 1 for the general (shell)
+// instantiation, 0 for the closure-free interior one.
+#define BSSN_LAUNCH_SET(cls, shell, kernel, set, stream, ...)                                              \
     do {                                                                                                  \
         if ((set).n > 0) {                                                                                \
-            const int threads_ = set_threads(set, G.ninst);                                               \
+            const int threads_ = launch_threads(cls, shell, set, G);                                      \
             const long long cover_ = largest(set) * G.ninst;                                              \
             BSSN_LAUNCH(cls, kernel, dim3((unsigned)((cover_ + threads_ - 1) / threads_), (set).n),         \
                         threads_, stream, __VA_ARGS__);                                                    \
@@ -1268,7 +1325,7 @@ cudaError_t launch_constraints(const double* u, const RhsWork& w, const Geo& G, 
     BSSN_LAUNCH(KC_MOM_DERIVED, k_mom_derived<double>, blocks_for(box_threads(G, ext)), kThreads, stream, u, u, w.der,
                 G, ext);
     const BoxSet es = single(ext);
-    BSSN_LAUNCH_SET(KC_FIRST, (k_first_derivs<double, true>), es, stream, u, w.der, w.d1, G, es, 0);
+    BSSN_LAUNCH_SET(KC_FIRST, 1, (k_first_derivs<double, true>), es, stream, u, w.der, w.d1, G, es, 0);
     BSSN_LAUNCH(KC_CONSTRAINTS, k_constraints, blocks_for(box.count), kThreads, stream, u, w.d1, w.der, G, box,
                 H, M, detm1, trA, gam);
     return cudaGetLastError();
@@ -1367,8 +1424,8 @@ static void launch_rhs_form(const R* u, const double* u64, double* k, R* d1, R* 
         cudaEventRecord(X->pre, stream);
         cudaStreamWaitEvent(stb, X->pre, 0);
     }
-    BSSN_LAUNCH_SET(KC_FIRST, (k_first_derivs<R, true>), se.shell, stb, u, der, d1, G, se.shell, with_mom);
-    BSSN_LAUNCH_SET(KC_FIRST, (k_first_derivs<R, false>), se.interior, stream, u, der, d1, G, se.interior, with_mom);
+    BSSN_LAUNCH_SET(KC_FIRST, 1, (k_first_derivs<R, true>), se.shell, stb, u, der, d1, G, se.shell, with_mom);
+    BSSN_LAUNCH_SET(KC_FIRST, 0, (k_first_derivs<R, false>), se.interior, stream, u, der, d1, G, se.interior, with_mom);
     if (X) {
         cudaEventRecord(X->fd, stb);
         cudaStreamWaitEvent(stream, X->fd, 0);
@@ -1384,29 +1441,29 @@ static void launch_rhs_form(const R* u, const double* u64, double* k, R* d1, R* 
     }
     // gauge: its own branch (b in the FP64 form, c in the FP32 form)
     const cudaStream_t stg = kPerturbative<R> ? stc : stb;
-    BSSN_LAUNCH_SET(KC_GAUGE, (k_rhs_gauge<R, false>), sb.interior, stg, u, u64, d1, k, G, sb.interior, nfield);
-    BSSN_LAUNCH_SET(KC_GAUGE, (k_rhs_gauge<R, true>), sb.shell, stg, u, u64, d1, k, G, sb.shell, nfield);
+    BSSN_LAUNCH_SET(KC_GAUGE, 0, (k_rhs_gauge<R, false>), sb.interior, stg, u, u64, d1, k, G, sb.interior, nfield);
+    BSSN_LAUNCH_SET(KC_GAUGE, 1, (k_rhs_gauge<R, true>), sb.shell, stg, u, u64, d1, k, G, sb.shell, nfield);
     // the shell's damping and curvature (pointwise in damp) run beside the
     // interior's: on c (FP64) or after the K/Gt RHS on b (FP32)
     const cudaStream_t sts = kPerturbative<R> ? stb : stc;
     if (with_mom) {
-        BSSN_LAUNCH_SET(KC_MOM_DAMP, (k_mom_damping<R, false>), sb.interior, stream, u, u64, der, d1, mat, damp, G,
+        BSSN_LAUNCH_SET(KC_MOM_DAMP, 0, (k_mom_damping<R, false>), sb.interior, stream, u, u64, der, d1, mat, damp, G,
                         sb.interior, nfield);
-        BSSN_LAUNCH_SET(KC_MOM_DAMP, (k_mom_damping<R, true>), sb.shell, sts, u, u64, der, d1, mat, damp, G,
+        BSSN_LAUNCH_SET(KC_MOM_DAMP, 1, (k_mom_damping<R, true>), sb.shell, sts, u, u64, der, d1, mat, damp, G,
                         sb.shell, nfield);
     }
     if constexpr (kPerturbative<R>) {
         // FP32 form: issue- and latency-bound, so the smaller split kernels run
         // at higher occupancy.
-        BSSN_LAUNCH_SET(KC_KGT, (k_rhs_kgt<R, false>), sb.interior, stb, u, u64, d1, mat, k, G, sb.interior, nfield);
-        BSSN_LAUNCH_SET(KC_KGT, (k_rhs_kgt<R, true>), sb.shell, stb, u, u64, d1, mat, k, G, sb.shell, nfield);
-        BSSN_LAUNCH_SET(KC_AT, (k_rhs_at<R, false>), sb.interior, stream, u, u64, d1, dmp, mat, k, G, sb.interior,
+        BSSN_LAUNCH_SET(KC_KGT, 0, (k_rhs_kgt<R, false>), sb.interior, stb, u, u64, d1, mat, k, G, sb.interior, nfield);
+        BSSN_LAUNCH_SET(KC_KGT, 1, (k_rhs_kgt<R, true>), sb.shell, stb, u, u64, d1, mat, k, G, sb.shell, nfield);
+        BSSN_LAUNCH_SET(KC_AT, 0, (k_rhs_at<R, false>), sb.interior, stream, u, u64, d1, dmp, mat, k, G, sb.interior,
                         nfield);
-        BSSN_LAUNCH_SET(KC_AT, (k_rhs_at<R, true>), sb.shell, sts, u, u64, d1, dmp, mat, k, G, sb.shell, nfield);
+        BSSN_LAUNCH_SET(KC_AT, 1, (k_rhs_at<R, true>), sb.shell, sts, u, u64, d1, dmp, mat, k, G, sb.shell, nfield);
     } else {
-        BSSN_LAUNCH_SET(KC_CURV, (k_rhs_curv<R, false>), sb.interior, stream, u, u64, d1, dmp, mat, k, G,
+        BSSN_LAUNCH_SET(KC_CURV, 0, (k_rhs_curv<R, false>), sb.interior, stream, u, u64, d1, dmp, mat, k, G,
                         sb.interior, nfield);
-        BSSN_LAUNCH_SET(KC_CURV, (k_rhs_curv<R, true>), sb.shell, sts, u, u64, d1, dmp, mat, k, G, sb.shell,
+        BSSN_LAUNCH_SET(KC_CURV, 1, (k_rhs_curv<R, true>), sb.shell, sts, u, u64, d1, dmp, mat, k, G, sb.shell,
                         nfield);
     }
     if (X) {
@@ -1417,12 +1474,135 @@ static void launch_rhs_form(const R* u, const double* u64, double* k, R* d1, R* 
     }
 }
 
+// ---------------------------------------------------------------------------
+// The reference's lower triangle of At.  It evolves all nine At_ij; the
+// Hessians in W^2 D_i D_j alpha and in the W terms of W^2 R_ij are formed as
+// D1_j(D1_i f) for the (i, j) entry (JAX_BSSN/bssn/geometry.py:47-56,
+// 131-135), so its lower triangle uses the other ordering than its (and this
+// code's) upper triangle.  The two orderings commute exactly but round
+// differently where the inner derivative's one-sided closure acts on O(1)
+// samples, i.e. on the rows next to a Sommerfeld face.  The difference
+// delta_ij = At_ji - At_ij (i < j) then obeys, to first order,
+//   d_t delta_ij = alpha W (dd_ji W - dd_ij W) - W^2 (dd_ji alpha - dd_ij alpha),
+// dd_ij f = D1_j(D1_i f); the other terms are first order in delta and change
+// it by parts in a thousand per step.  k_lower_triangle evaluates that source on
+// the shell slabs (the closure rows; elsewhere the orderings agree to
+// roundoff) and accumulates it with the RK4 weights: acc = S1 + 2 S2 + 2 S3 + S4,
+// delta += dt/6 acc.  Only the reference-layout RK4 call carries delta.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads)
+k_lower_triangle(const double* __restrict__ u, const double* __restrict__ d1, double* __restrict__ acc,
+                 double* __restrict__ delta, Geo G, BoxSet S, int stage, int nfield) {
+    PointCtx c;
+    if (!point(S.b[blockIdx.y], c, G)) return;
+    const long long cs = G.cs, p = c.p;
+    const double W = u[CW * cs + p], al = u[CALPHA * cs + p];
+    constexpr int pairs[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int i = pairs[k][0], j = pairs[k][1];
+        const double wu = D1<double, true>(d1ptr(d1, G, nfield, i, MIX_W, p), G, j, c.ix[j]);
+        const double wl = D1<double, true>(d1ptr(d1, G, nfield, j, MIX_W, p), G, i, c.ix[i]);
+        const double au = D1<double, true>(d1ptr(d1, G, nfield, i, MIX_ALPHA, p), G, j, c.ix[j]);
+        const double al_ = D1<double, true>(d1ptr(d1, G, nfield, j, MIX_ALPHA, p), G, i, c.ix[i]);
+        const double src = al * W * (wl - wu) - W * W * (al_ - au);
+        const long long q = k * cs + p;
+        const double a = stage == 1 ? src : fma(stage == 4 ? 1.0 : 2.0, src, acc[q]);
+        acc[q] = a;
+        if (stage == 4) delta[q] += (G.dt / 6.0) * a;
+    }
+}
+
+cudaError_t launch_lower_triangle(const double* u, const RhsWork& w, double* acc, double* delta, const Geo& G,
+                                  const Box& box, int stage, cudaStream_t stream) {
+    const int nfield = G.kappa != 0.0 ? NMIX + NMIX_MOM : NMIX;
+    const BoxSet shell = split_box(G, without_faces(G, box), false).shell;
+    BSSN_LAUNCH_SET(KC_OTHER, 1, k_lower_triangle, shell, stream, u, w.d1, acc, delta, G, shell, stage, nfield);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_inner_derivs(const double* u, double* d1, const Geo& G, const Box& box, cudaStream_t stream) {
     // periodic boxes have no closure rows: the closure-free instantiation
     // covers the box grown by the composition reach
     const BoxSet es = single(grown_box(box, G, composition_reach(G)));
-    BSSN_LAUNCH_SET(KC_FIRST, (k_first_derivs<double, false>), es, stream, u, (const double*)nullptr, d1, G, es, 0);
+    BSSN_LAUNCH_SET(KC_FIRST, 0, (k_first_derivs<double, false>), es, stream, u, (const double*)nullptr, d1, G, es, 0);
     return cudaGetLastError();
+}
+
+cudaError_t tune_rhs(const double* u, double* k, const RhsWork& w, const Geo& G, const Box& box, cudaStream_t s,
+                     int reps, float margin, std::string* report) {
+    cudaStreamCaptureStatus status = cudaStreamCaptureStatusNone;
+    cudaError_t e = cudaStreamIsCapturing(s, &status);
+    if (e != cudaSuccess) return e;
+    if (status != cudaStreamCaptureStatusNone) return cudaErrorStreamCaptureUnsupported;
+    int dev = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    std::vector<int> classes = {KC_FIRST, KC_GAUGE};
+    if (G.precision == kPrecisionF32) {
+        classes.push_back(KC_KGT);
+        classes.push_back(KC_AT);
+    } else {
+        classes.push_back(KC_CURV);
+    }
+    if (G.kappa != 0.0) classes.push_back(KC_MOM_DAMP);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if ((e = cudaEventCreate(&e0)) != cudaSuccess) return e;
+    if ((e = cudaEventCreate(&e1)) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return e;
+    }
+    auto time_rhs = [&](float& ms) -> cudaError_t {
+        cudaError_t r = cudaEventRecord(e0, s);
+        for (int i = 0; i < reps && r == cudaSuccess; ++i) r = launch_rhs(u, k, w, G, box, s);
+        if (r == cudaSuccess) r = cudaEventRecord(e1, s);
+        if (r == cudaSuccess) r = cudaEventSynchronize(e1);
+        if (r == cudaSuccess) r = cudaEventElapsedTime(&ms, e0, e1);
+        return r;
+    };
+    float ms = 0.0f, base = 0.0f;
+    e = time_rhs(ms);   // warm-up (streams, caches)
+    // the current shapes' time: a candidate must come in under margin x it
+    if (e == cudaSuccess) e = time_rhs(base);
+    for (size_t c = 0; c < classes.size() && e == cudaSuccess; ++c) {
+        for (int shell = 0; shell < 2 && e == cudaSuccess; ++shell) {
+            int best = 0;
+            float best_ms = 0.0f;
+            long long size = -1;
+            for (int t : kTuneCandidates) {
+                t_force_cls = classes[c];
+                t_force_shell = shell;
+                t_force_threads = t;
+                t_seen_size = -1;
+                e = time_rhs(ms);
+                if (e != cudaSuccess || t_seen_size < 0) break;   // slot not launched here
+                size = t_seen_size;
+                if (best == 0 || ms < best_ms) {
+                    best = t;
+                    best_ms = ms;
+                }
+            }
+            t_force_cls = t_force_shell = -1;
+            if (e != cudaSuccess || size < 0 || best == 0) continue;
+            if (best_ms > margin * base) {
+                if (report)
+                    *report += "class " + std::to_string(classes[c]) + (shell ? " shell" : " interior") +
+                               ": heuristic kept; ";
+                continue;
+            }
+            {
+                std::lock_guard<std::mutex> guard(g_tune_lock);
+                g_tuned[TuneKey{dev, classes[c], shell, G.precision, size}] = best;
+            }
+            base = best_ms;   // later slots are measured against the tuned whole
+            if (report)
+                *report += "class " + std::to_string(classes[c]) + (shell ? " shell" : " interior") + ": " +
+                           std::to_string(best) + " threads (" + std::to_string(best_ms / reps) + " ms per RHS); ";
+        }
+    }
+    t_force_cls = t_force_shell = -1;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return e;
 }
 
 cudaError_t launch_rhs_f32_prepared(const double* u, double* k, const RhsWork& w, const Geo& G, const Box& box,

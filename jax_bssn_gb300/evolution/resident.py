@@ -48,6 +48,13 @@ class PatchEvolution(GraphSteps):
                                               self.ws.data_ptr(), self.ws.numel(), _device.stream_handle()),
                       "bssn_patch_rk4")
 
+    def tune(self, margin: float = 0.98) -> str:
+        """Autotune the RHS launch shapes for this grid and arithmetic form
+        (later steps and graph captures use them; results are unchanged).  A
+        shape changes only when it is faster than ``margin`` x the current one."""
+        return _native.tune_launch_shapes(self.u.data_ptr(), self.shape, 1, self.cparams, self.device, self.ws,
+                                          margin)
+
     def state(self) -> BSSNVariables:
         out = _device.empty_state(self.shape, self.device)
         _native.check(self.lib.bssn_patch_export(self.u.data_ptr(), _device.fields_struct(out), self.patch,
@@ -127,6 +134,11 @@ class BatchEvolution(GraphSteps):
                                                  self.instances, int(instance), _device.stream_handle()),
                       "bssn_batch_export")
         return out
+
+    def tune(self, margin: float = 0.98) -> str:
+        """Autotune the RHS launch shapes for this batch and arithmetic form."""
+        return _native.tune_launch_shapes(self.u.data_ptr(), self.shape, self.instances, self.cparams, self.device,
+                                          self.ws, margin)
 
     def step_monitored(self, steps: int, check_every: int = 1) -> int:
         """``steps`` RK4 steps, counting non-finite values before the first and

@@ -368,6 +368,17 @@ class FMREvolution(GraphSteps):
                                                  int(steps), self.ws.data_ptr(), self.ws.numel(),
                                                  _device.stream_handle()), "fmr_rk4_step")
 
+    def tune(self, margin: float = 0.98) -> str:
+        """Autotune the RHS launch shapes of every patch (each patch's padded
+        extent is a single patch's, so the tuned shapes apply to its launches
+        inside the FMR step)."""
+        reports = []
+        for p, (u, n) in enumerate(zip(self.buffers, self.shapes)):
+            scratch = u.clone()     # tuning wraps the guards periodically; a child's are prolonged
+            reports.append(_native.tune_launch_shapes(scratch.data_ptr(), n, 1, self.cparams[p], self.device,
+                                                        margin=margin))
+        return " | ".join(reports)
+
     def states(self):
         return tuple(_from_components(u, n, self.device) for u, n in zip(self.buffers, self.shapes))
 

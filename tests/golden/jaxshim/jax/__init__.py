@@ -26,6 +26,7 @@ class _Config:
         setattr(self, name, value)
 
     jax_enable_x64 = True
+    x64_enabled = True
 
 
 config = _Config()
@@ -59,8 +60,11 @@ def vmap(fun, in_axes=0, out_axes=0):
         results = []
         for index in range(size):
             call = [arg if m is None else m[index] for arg, m in zip(args, moved)]
-            results.append(_np.asarray(fun(*call)))
-        return numpy.asarray(_np.moveaxis(_np.stack(results), 0, out_axes))
+            results.append(fun(*call))
+        if isinstance(results[0], tuple):       # several outputs: stack each
+            return tuple(numpy.asarray(_np.moveaxis(_np.stack([_np.asarray(r[k]) for r in results]), 0, out_axes))
+                         for k in range(len(results[0])))
+        return numpy.asarray(_np.moveaxis(_np.stack([_np.asarray(r) for r in results]), 0, out_axes))
 
     return mapped
 
@@ -155,12 +159,59 @@ def named_call(fun, name=None):
     return fun
 
 
+# Forward-mode derivatives by central differences.  JAX differentiates
+# exactly; these stand-ins are used where the result steers an iteration (the
+# horizon finder's Newton Jacobian) or enters a residual to about 1e-11 (the
+# metric derivative of the Hermite interpolant, piecewise cubic, by a
+# Richardson-extrapolated difference), so a converged answer still comes from
+# the reference's own residual.
+
 def linearize(fun, *primals):
-    raise NotImplementedError("jax.linearize is not available in the NumPy shim")
+    """(fun(*primals), jvp) with jvp(tangent) a central difference of step
+    1e-6 relative to the primal's scale (one primal)."""
+    if len(primals) != 1:
+        raise NotImplementedError("the NumPy shim linearizes functions of one argument")
+    x = _np.asarray(primals[0], dtype=_np.float64)
+    scale = max(float(_np.max(_np.abs(x))), 1.0)
+    value = fun(numpy.asarray(x))
+
+    def jvp(tangent):
+        t = _np.asarray(tangent, dtype=_np.float64)
+        h = 1.0e-6 * scale / max(float(_np.max(_np.abs(t))), 1e-300)
+        plus = _np.asarray(fun(numpy.asarray(x + h * t)))
+        minus = _np.asarray(fun(numpy.asarray(x - h * t)))
+        return numpy.asarray((plus - minus) / (2.0 * h))
+
+    return value, jvp
 
 
 def jacfwd(fun, argnums=0):
-    raise NotImplementedError("jax.jacfwd is not available in the NumPy shim")
+    """Jacobian by Richardson-extrapolated central differences (steps h and
+    h/2, h = 1e-5 max(|x|, 1)), one column per input element; shape fun's
+    output + input.  Exact to roundoff for polynomials of degree four."""
+
+    def central(args, x, index, h):
+        up, down = x.copy(), x.copy()
+        up[index] += h
+        down[index] -= h
+        call = list(args)
+        call[argnums] = numpy.asarray(up)
+        plus = _np.asarray(fun(*call))
+        call[argnums] = numpy.asarray(down)
+        minus = _np.asarray(fun(*call))
+        return (plus - minus) / (up[index] - down[index])
+
+    def jac(*args):
+        x = _np.asarray(args[argnums], dtype=_np.float64)
+        columns = []
+        for index in _np.ndindex(*x.shape):
+            h = 1.0e-5 * max(abs(float(x[index])), 1.0)
+            coarse, fine = central(args, x, index, h), central(args, x, index, 0.5 * h)
+            columns.append((4.0 * fine - coarse) / 3.0)
+        out_shape = columns[0].shape
+        return numpy.asarray(_np.stack(columns, axis=-1).reshape(out_shape + x.shape))
+
+    return jac
 
 
 class nn:

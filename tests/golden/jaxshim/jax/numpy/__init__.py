@@ -297,7 +297,7 @@ def power(x, y):
         return _wrap(_pow_minus_third(x.astype(_np.float64)))
     y = _np.asarray(y, dtype=_np.float64)
     xb, yb = _np.broadcast_arrays(x.astype(_np.float64), y)
-    out = _np.frompyfunc(math.pow, 2, 1)(xb, yb).astype(_np.float64)
+    out = _np.asarray(_np.frompyfunc(math.pow, 2, 1)(xb, yb), dtype=_np.float64)
     return _wrap(out)
 
 floor = _w(_np.floor)

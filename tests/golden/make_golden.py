@@ -492,6 +492,80 @@ def make_cartoon(out_dir: Path):
     np.savez_compressed(out_dir / "cartoon_spherical.npz", **data)
 
 
+# Apparent-horizon pins from the reference's own finder code
+# (JAX_BSSN/utilities/apparent_horizon.py, hermite_interpolation.py), run
+# unmodified under the stand-in.  There, jax.jacfwd (the metric derivative of
+# the Hermite interpolant, piecewise cubic) is a Richardson-extrapolated
+# central difference, accurate to about 1e-11, and jax.linearize (the Newton
+# Jacobian) a central difference that only steers Newton.  A dense Newton step
+# re-evaluates every node once per column, minutes per iteration here, so
+# complete finds are stored for the radial-line cases; for every layout and
+# slicing the pieces of the residual are stored on fixed inputs: sample (the
+# interpolated metric, its derivative, K and the resolved flag), surface (the
+# expansion and area density of a non-spherical surface), angular_derivatives
+# and interpolate_angular.
+HORIZON_FIND_OPTIONS = dict(n_theta=6, n_phi=12, max_angular=12, tolerance=1e-9, audit_tolerance=1.0,
+                            mass_tolerance=1.0)
+HORIZON_GRID = dict(volume_dx=0.1, volume_extent=3.0)
+
+
+def make_horizon(out_dir: Path):
+    import time
+    sys.path.insert(0, str(REPO / "tests"))
+    from horizon_cases import layout_case
+    from JAX_BSSN.utilities.apparent_horizon import (angular_derivatives, angular_grid, build_geometry,
+                                                     find_apparent_horizon, interpolate_angular, surface)
+    data = {"find_options": np.asarray(json.dumps(HORIZON_FIND_OPTIONS)),
+            "grid": np.asarray(json.dumps(HORIZON_GRID))}
+
+    def wavy(n_theta, n_phi, base, amp):
+        theta, phi, _ = angular_grid(n_theta, n_phi)
+        return base + amp * np.sin(theta[:, None]) ** 2 * np.cos(2 * phi[None, :])
+
+    # sample at seeded points (radii 1.2 .. 2.8, a few on axes and one outside)
+    rng = np.random.default_rng(7)
+    pts = rng.normal(size=(300, 3))
+    pts *= (rng.uniform(1.2, 2.8, size=300) / np.linalg.norm(pts, axis=1))[:, None]
+    pts[:5] = [[0, 0, 2.0], [2.0, 0, 0], [0, 2.0, 0], [1e-12, 0, 2.0], [0, 0, 40.0]]
+    data["sample.points"] = pts
+    for layout in ("line", "plane", "volume"):
+        for slicing in ("isotropic", "kerr_schild"):
+            axes, gamma, kij, mass, exact = layout_case(layout, slicing, **HORIZON_GRID)
+            table, sample = build_geometry(axes, gamma, kij, margin=4)
+            key = f"{layout}_{slicing}"
+            if slicing == "kerr_schild":
+                g, dg, k, valid = (np.asarray(a) for a in sample(table, pts))
+                for name, value in (("gamma", g), ("d_gamma", dg), ("curvature", k), ("valid", valid)):
+                    data[f"sample.{layout}.{name}"] = value
+            h = wavy(8, 16, 1.1 * exact, 0.03 * exact)
+            center = np.zeros(3) if layout == "line" else np.array([0.0, 0.0, 0.02])
+            expansion, density, usable = surface(h, center, table, sample)
+            data[f"surface.{key}.radius"] = h
+            data[f"surface.{key}.center"] = center
+            data[f"surface.{key}.expansion"] = np.asarray(expansion)
+            data[f"surface.{key}.density"] = np.asarray(density)
+            data[f"surface.{key}.usable"] = np.asarray(bool(usable))
+    field = wavy(10, 20, 1.1, 0.03) + 0.01 * np.random.default_rng(3).normal(size=(10, 20))
+    data["angular.field"] = field
+    for k, d in enumerate(angular_derivatives(field)):
+        data[f"angular.derivative{k}"] = np.asarray(d)
+    theta, phi, _ = angular_grid(22, 42)
+    data["angular.regrid"] = np.asarray(interpolate_angular(field, theta, phi))
+    for slicing, guess in (("isotropic", 1.15), ("kerr_schild", 0.9)):
+        axes, gamma, kij, mass, exact = layout_case("line", slicing, **HORIZON_GRID)
+        t = time.time()
+        found = find_apparent_horizon(axes, gamma, kij, center=(0.0, 0.0, 0.0), initial_radius=guess * exact,
+                                      **HORIZON_FIND_OPTIONS)
+        print(f"horizon line_{slicing}: mass {found['mass']:.10f} ({time.time() - t:.0f} s)", flush=True)
+        key = f"find.line_{slicing}"
+        data[f"{key}.guess"] = np.asarray(guess)
+        for name in ("radius", "expansion", "convergence"):
+            data[f"{key}.{name}"] = np.asarray(found[name])
+        for name in ("area", "mass", "residual", "audit_residual"):
+            data[f"{key}.{name}"] = np.asarray(found[name])
+    np.savez_compressed(out_dir / "horizon.npz", **data)
+
+
 def main(argv):
     args = [a for a in argv[1:] if not a.startswith("--")]
     reference = Path(args[0]) if args else Path("/root/reference")
@@ -500,7 +574,7 @@ def main(argv):
     parts = {"stencils": lambda: make_stencils(HERE / "stencils.npz"), "rhs": lambda: make_rhs(HERE),
              "fmr": lambda: make_fmr(HERE), "cartoon": lambda: make_cartoon(HERE),
              "matter": lambda: make_matter(HERE), "waves": lambda: make_waves(HERE),
-             "puncture": lambda: make_puncture(HERE),
+             "puncture": lambda: make_puncture(HERE), "horizon": lambda: make_horizon(HERE),
              "long": lambda: make_long_runs(HERE)}
     for name, build in parts.items():
         if only and name not in only:

@@ -93,3 +93,43 @@ def test_monitored_run_reports_non_finite_values(cuda, native):
     with pytest.raises(NonFiniteStateError, match="after step") as info:
         evo.step_monitored(6, check_every=2)
     assert info.value.steps_done == 2
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_autotuned_launch_shapes_leave_results_unchanged(cuda, native, precision):
+    """bssn_tune_patch times each RHS launch slot with 32, 64 and 128 threads
+    per block and keeps the fastest (margin 10: whatever the heuristic's time,
+    so the tuned table is exercised); later launches (direct and captured) use
+    it.  Every thread still computes the same point, so the evolution is
+    bit-identical to the heuristic launch shapes, for single patches, batches
+    and FMR patches."""
+    from jax_bssn_gb300.evolution import BatchEvolution, PatchEvolution
+    from jax_bssn_gb300.fmr import FMREvolution, initialize_tiled_fmr
+    from jax_bssn_gb300.initial_data import (fmr_linear_wave_hierarchy, fmr_linear_wave_root, linear_wave_callback,
+                                             teukolsky_config)
+    state, params = teukolsky_config(n=22)
+    before = PatchEvolution(state, params, precision=precision)
+    before.step(2)
+    batch_before = BatchEvolution([state, state], params, precision=precision)
+    batch_before.step(2)
+    hierarchy = fmr_linear_wave_hierarchy(24)
+    states, parameters, layouts = initialize_tiled_fmr(linear_wave_callback(), fmr_linear_wave_root(24), (24,) * 3,
+                                                       hierarchy)
+    fmr_before = FMREvolution(states, parameters, hierarchy, layouts, precision=precision)
+    fmr_before.step(2)
+
+    tuned = PatchEvolution(state, params, precision=precision)
+    assert "threads" in tuned.tune(margin=10.0)
+    tuned.step(2)
+    assert worst(field_errors(tuned.state(), before.state())) == 0.0
+    batch = BatchEvolution([state, state], params, precision=precision)
+    batch.tune(margin=10.0)
+    batch.capture(1)
+    batch.step(2)
+    for i in range(2):
+        assert worst(field_errors(batch.state(i), batch_before.state(i))) == 0.0
+    fmr = FMREvolution(states, parameters, hierarchy, layouts, precision=precision)
+    fmr.tune(margin=10.0)
+    fmr.step(2)
+    for a, b in zip(fmr.states(), fmr_before.states()):
+        assert worst(field_errors(a, b)) == 0.0

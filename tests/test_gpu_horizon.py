@@ -55,6 +55,93 @@ def test_exact_mass_all_layouts(ah, layout, slicing):
     np.testing.assert_allclose(horizon["mass"], ref["mass"], rtol=1.e-7)
 
 
+def _horizon_golden():
+    from .helpers import GOLDEN
+    with np.load(GOLDEN / "horizon.npz") as data:
+        return {k: data[k] for k in data.files}
+
+
+# Pins from the reference's own finder code, run unmodified under the NumPy
+# jax stand-in (tests/golden/make_golden.py, horizon section).  There the
+# metric derivative (jax.jacfwd) is a Richardson-extrapolated difference of
+# the piecewise-cubic Hermite interpolant, good to about 1e-11, hence the
+# 1e-9 bounds on the derivative and the expansion; the rest is exact
+# arithmetic in the reference's order.
+
+@pytest.mark.parametrize("layout", ["line", "plane", "volume"])
+def test_sample_matches_reference_code(ah, layout):
+    """build_geometry / sample (JAX_BSSN/utilities/apparent_horizon.py:22-98)."""
+    import json
+    data = _horizon_golden()
+    grid = json.loads(str(data["grid"]))
+    axes, gamma, kij, _, _ = layout_case(layout, "kerr_schild", **grid)
+    table, sample = ah.build_geometry(axes, gamma, kij)
+    pts = data["sample.points"]
+    g, dg, k, valid = (t.cpu().numpy() for t in sample(table, pts))
+    ovalid = data[f"sample.{layout}.valid"].astype(bool)
+    np.testing.assert_array_equal(valid.astype(bool), ovalid)
+    for got, key, tol in ((g, "gamma", 1e-12), (dg, "d_gamma", 1e-9), (k, "curvature", 1e-12)):
+        want = data[f"sample.{layout}.{key}"]
+        scale = np.max(np.abs(want[ovalid]))
+        np.testing.assert_allclose(got[ovalid], want[ovalid], rtol=0, atol=tol * scale, err_msg=key)
+
+
+@pytest.mark.parametrize("layout", ["line", "plane", "volume"])
+@pytest.mark.parametrize("slicing", ["isotropic", "kerr_schild"])
+def test_surface_matches_reference_code(ah, layout, slicing):
+    """surface (apparent_horizon.py:160-236): expansion and area density of a
+    non-spherical surface about an off-axis centre."""
+    import json
+    data = _horizon_golden()
+    grid = json.loads(str(data["grid"]))
+    axes, gamma, kij, _, _ = layout_case(layout, slicing, **grid)
+    table, _ = ah.build_geometry(axes, gamma, kij)
+    key = f"surface.{layout}_{slicing}"
+    exp, dens, usable = ah.surface(torch.as_tensor(data[f"{key}.radius"]).cuda(), data[f"{key}.center"], table)
+    assert bool(usable) == bool(data[f"{key}.usable"])
+    want = data[f"{key}.expansion"]
+    np.testing.assert_allclose(exp.cpu().numpy(), want, rtol=0, atol=1e-8 * np.max(np.abs(want)) + 1e-12)
+    np.testing.assert_allclose(dens.cpu().numpy(), data[f"{key}.density"], rtol=1e-12)
+
+
+def test_angular_operators_match_reference_code(ah):
+    """angular_derivatives (:125-144) and interpolate_angular (:147-157)."""
+    data = _horizon_golden()
+    field = data["angular.field"]
+    got = [d.cpu().numpy() for d in ah.angular_derivatives(torch.as_tensor(field).cuda())]
+    for k, g in enumerate(got):
+        w = data[f"angular.derivative{k}"]
+        np.testing.assert_allclose(g, w, rtol=1e-15, atol=1e-15 * np.max(np.abs(w)))
+    theta, phi, _ = ah.angular_grid(22, 42)
+    regrid = ah.interpolate_angular(torch.as_tensor(field).cuda(), theta, phi)
+    regrid = regrid.cpu().numpy() if hasattr(regrid, "cpu") else np.asarray(regrid)
+    np.testing.assert_allclose(regrid, data["angular.regrid"], rtol=1e-14)
+
+
+@pytest.mark.parametrize("slicing", ["isotropic", "kerr_schild"])
+def test_find_matches_reference_finder(ah, slicing):
+    """Complete finds of the reference's find_apparent_horizon (:246-338) on
+    the radial-line layout: 6 x 12, refined once to 12 x 24, Newton tolerance
+    1e-9.  Both finders stop once mean(h) max|Theta| < 1e-9, so the surfaces
+    agree to about that over |dTheta/dh|."""
+    import json
+    data = _horizon_golden()
+    grid = json.loads(str(data["grid"]))
+    options = json.loads(str(data["find_options"]))
+    axes, gamma, kij, _, exact = layout_case("line", slicing, **grid)
+    key = f"find.line_{slicing}"
+    got = ah.find_apparent_horizon(axes, gamma, kij, center=(0, 0, 0),
+                                   initial_radius=float(data[f"{key}.guess"]) * exact, **options)
+    ref = data[f"{key}.radius"]
+    assert got["radius"].shape == ref.shape
+    err = float(np.max(np.abs(got["radius"] - ref))) / exact
+    mass_err = abs(got["mass"] - float(data[f"{key}.mass"])) / float(data[f"{key}.mass"])
+    print(slicing, f"radius {err:.1e} of r, mass {mass_err:.1e}")
+    assert err < 1e-7
+    assert mass_err < 1e-7
+    np.testing.assert_allclose(np.asarray(got["convergence"])[:, 2], data[f"{key}.convergence"][:, 2], rtol=1e-7)
+
+
 def test_nonspherical_guess_and_fixed_displaced_center(ah):
     center = (0., 0., .15)
     x, z, gamma, kij = schwarzschild_plane(stretch=1.3, center_z=center[2], dx=.03)

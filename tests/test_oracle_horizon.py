@@ -74,3 +74,64 @@ def test_oracle_failures():
     bad[0, 0] *= -1
     with pytest.raises(RuntimeError, match="nonphysical"):
         H.find_apparent_horizon((r,), bad, kij, center=(0, 0, 0), initial_radius=1.)
+
+
+# ---------------------------------------------------------------------------
+# against the reference's own finder code (tests/golden/horizon.npz, made by
+# tests/golden/make_golden.py running JAX_BSSN/utilities/apparent_horizon.py
+# unmodified under the NumPy jax stand-in; its jacfwd is a Richardson
+# difference good to about 1e-11)
+# ---------------------------------------------------------------------------
+
+def _golden():
+    from tests.helpers import GOLDEN
+    with np.load(GOLDEN / "horizon.npz") as data:
+        return {k: data[k] for k in data.files}
+
+
+@pytest.mark.parametrize("layout", ["line", "plane", "volume"])
+def test_oracle_sample_and_surface_match_reference_code(layout):
+    import json
+    data = _golden()
+    grid = json.loads(str(data["grid"]))
+    axes, gamma, kij, _, _ = layout_case(layout, "kerr_schild", **grid)
+    g, dg, k, valid = H.build_geometry(axes, gamma, kij)(data["sample.points"])
+    ovalid = data[f"sample.{layout}.valid"].astype(bool)
+    np.testing.assert_array_equal(np.asarray(valid).astype(bool), ovalid)
+    for got, key, tol in ((g, "gamma", 1e-12), (dg, "d_gamma", 1e-9), (k, "curvature", 1e-12)):
+        want = data[f"sample.{layout}.{key}"]
+        np.testing.assert_allclose(np.asarray(got)[ovalid], want[ovalid], rtol=0,
+                                   atol=tol * np.max(np.abs(want[ovalid])), err_msg=key)
+    for slicing in ("isotropic", "kerr_schild"):
+        axes, gamma, kij, _, _ = layout_case(layout, slicing, **grid)
+        key = f"surface.{layout}_{slicing}"
+        exp, dens, usable = H.surface(data[f"{key}.radius"], data[f"{key}.center"], H.build_geometry(axes, gamma, kij))
+        assert bool(usable) == bool(data[f"{key}.usable"])
+        want = data[f"{key}.expansion"]
+        np.testing.assert_allclose(exp, want, rtol=0, atol=1e-8 * np.max(np.abs(want)) + 1e-12)
+        np.testing.assert_allclose(dens, data[f"{key}.density"], rtol=1e-12)
+
+
+def test_oracle_angular_operators_match_reference_code():
+    data = _golden()
+    field = data["angular.field"]
+    for k, got in enumerate(H.angular_derivatives(field)):
+        want = data[f"angular.derivative{k}"]
+        np.testing.assert_allclose(got, want, rtol=1e-15, atol=1e-15 * np.max(np.abs(want)))
+    theta, phi, _ = H.angular_grid(22, 42)
+    np.testing.assert_allclose(H.interpolate_angular(field, theta, phi), data["angular.regrid"], rtol=1e-14)
+
+
+@pytest.mark.parametrize("slicing", ["isotropic", "kerr_schild"])
+def test_oracle_find_matches_reference_finder(slicing):
+    import json
+    data = _golden()
+    grid = json.loads(str(data["grid"]))
+    options = json.loads(str(data["find_options"]))
+    axes, gamma, kij, _, exact = layout_case("line", slicing, **grid)
+    key = f"find.line_{slicing}"
+    h = H.find_apparent_horizon(axes, gamma, kij, center=(0, 0, 0), initial_radius=float(data[f"{key}.guess"]) * exact,
+                                **options)
+    assert h["radius"].shape == data[f"{key}.radius"].shape
+    assert np.max(np.abs(h["radius"] - data[f"{key}.radius"])) < 1e-7 * exact
+    assert abs(h["mass"] / float(data[f"{key}.mass"]) - 1) < 1e-7
