@@ -134,7 +134,12 @@ int bssn_rhs_noalloc(const BssnFields* in, BssnFields* out, const int32_t shape[
  * trace-free At.  In place on all samples of the array. */
 int bssn_project(BssnFields* state, const int32_t shape[3], void* stream);
 
-/* rk4_step(vars, params) (time_evolve.py:144-217), repeated `steps` times, in place. */
+/* rk4_step(vars, params) (time_evolve.py:144-217), repeated `steps` times, in place.
+ * In the FP64 form with a Sommerfeld face, the lower triangles of At and gt
+ * are carried as the reference evolves them: their differences from the upper
+ * triangles, which the reference's two orderings of the mixed derivatives
+ * create on the rows next to the faces, are read from the input there,
+ * evolved to first order and written back (work buffer: 24 more blocks). */
 int bssn_rk4_step(BssnFields* state, const int32_t shape[3], const BssnParams* params,
                   int32_t steps, void* workspace, size_t workspace_bytes, void* stream);
 

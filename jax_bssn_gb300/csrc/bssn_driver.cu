@@ -284,7 +284,12 @@ __global__ void k_fill_periodic(T* __restrict__ u, int ncomp, Geo G, Box region,
     for (int c = 0; c < ncomp; ++c) u[c * G.cs + dst] = u[c * G.cs + s];
 }
 
-// Bit-exact algebraic projection of one point held in registers.
+// Bit-exact algebraic projection of one point held in registers
+// (JAX_BSSN/evolution/time_evolve.py:94-141).  At's trace uses the
+// reference's Cholesky inverse in its rounding order, not a cheaper cofactor
+// form: a one-ulp change of At flips, here and there, the rounding of gt's
+// next RK4 combination, and the Ricci tensor's 1/dx^2 gain turns that ulp of
+// gt into ~1e-12 of At within three steps (measured at 32^3).
 __device__ __forceinline__ void project_point(double (&g)[6], double (&A)[6]) {
     const double s = inv_cbrt_cr(det_sym_rn(g));
 #pragma unroll
@@ -504,40 +509,63 @@ cudaError_t rk4_step_patch(double* u0, double* ustage, double* k, double* acc, c
         const double* src = stage == 1 ? u0 : ustage;
         if (fill && (e = launch_fill_periodic(const_cast<double*>(src), NCOMP, G, s)) != cudaSuccess) return e;
         if ((e = launch_rhs(src, k, w, G, B, s)) != cudaSuccess) return e;
-        if (lower && (e = launch_lower_triangle(src, w, lower->acc, lower->delta, G, B, stage, s)) != cudaSuccess)
-            return e;
+        if (lower) {
+            if ((e = launch_lower_triangle(src, w, *lower, G, B, stage, s)) != cudaSuccess) return e;
+            // periodic axes: the next reader's ghosts
+            if ((e = launch_fill_periodic(lower_triangle_output(*lower, stage), 6, G, s)) != cudaSuccess) return e;
+        }
         double* out = stage == 4 ? u0 : ustage;
         if ((e = launch_rk4_stage(u0, k, acc, out, G, B, stage, G.dt, final_form, 1, s)) != cudaSuccess) return e;
     }
     return cudaSuccess;
 }
 
-// delta_ij = At_ji - At_ij (i < j) of a reference-layout input, and the lower
-// triangle of an output as its upper triangle plus delta.
-__global__ void k_import_lower(const double* __restrict__ A, double* __restrict__ delta, Geo G, Box region,
-                               long long npts) {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= region.count * 3) return;
-    const int k = (int)(t / region.count);
-    const long long r = t - (long long)k * region.count;
-    int ix[3];
-    region.coords(r, ix);
-    constexpr int pairs[3][2] = {{0, 1}, {0, 2}, {1, 2}};
-    const int i = pairs[k][0], j = pairs[k][1];
-    delta[k * G.cs + lin(G, ix)] = A[(3 * j + i) * npts + r] - A[(3 * i + j) * npts + r];
+// delta_ij = T_ji - T_ij (i < j) of a reference-layout input's At and gt,
+// on the closure-row shell (zero elsewhere: an input whose triangles differ
+// in the interior evolves with its upper triangle there), and the lower
+// triangles of an output as their upper triangles plus delta.
+__device__ __forceinline__ bool in_closure_shell(const Geo& G, const int (&ix)[3]) {
+    bool shell = false;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const Axis& a = G.ax[d];
+        if (a.reduced) continue;
+        shell = shell || (a.lbc && ix[d] < a.start + kClosureRows) || (a.rbc && ix[d] >= a.end - kClosureRows);
+    }
+    return shell;
 }
 
-__global__ void k_export_lower(double* __restrict__ A, const double* __restrict__ delta, Geo G, Box region,
+__global__ void k_import_lower(const double* __restrict__ A, const double* __restrict__ g, double* __restrict__ delta,
+                               float* __restrict__ copy, float* __restrict__ other, Geo G, Box region,
                                long long npts) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= region.count * 3) return;
+    if (t >= region.count * 6) return;
     const int k = (int)(t / region.count);
     const long long r = t - (long long)k * region.count;
     int ix[3];
     region.coords(r, ix);
     constexpr int pairs[3][2] = {{0, 1}, {0, 2}, {1, 2}};
-    const int i = pairs[k][0], j = pairs[k][1];
-    A[(3 * j + i) * npts + r] = A[(3 * i + j) * npts + r] + delta[k * G.cs + lin(G, ix)];
+    const int i = pairs[k % 3][0], j = pairs[k % 3][1];
+    const double* T = k < 3 ? A : g;
+    const double d = in_closure_shell(G, ix) ? T[(3 * j + i) * npts + r] - T[(3 * i + j) * npts + r] : 0.0;
+    const long long q = k * G.cs + lin(G, ix);
+    delta[q] = d;
+    copy[q] = (float)d;    // stage 1 reads it
+    other[q] = 0.0f;       // off the shell, stage values stay zero
+}
+
+__global__ void k_export_lower(double* __restrict__ A, double* __restrict__ g, const double* __restrict__ delta,
+                               Geo G, Box region, long long npts) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= region.count * 6) return;
+    const int k = (int)(t / region.count);
+    const long long r = t - (long long)k * region.count;
+    int ix[3];
+    region.coords(r, ix);
+    constexpr int pairs[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+    const int i = pairs[k % 3][0], j = pairs[k % 3][1];
+    double* T = k < 3 ? A : g;
+    T[(3 * j + i) * npts + r] = T[(3 * i + j) * npts + r] + delta[k * G.cs + lin(G, ix)];
 }
 
 }  // namespace bssn
@@ -588,8 +616,9 @@ LeavesOut leaves_out(BssnFields* f) {
                       f->conformal_connection, f->lapse, f->shift}};
 }
 
-// The reference-layout RK4 call carries the reference's At lower triangle
-// (launch_lower_triangle) in the plain FP64 form when a face is Sommerfeld.
+// The reference-layout RK4 call carries the reference's At and gt lower
+// triangles (launch_lower_triangle) in the plain FP64 form when a face is
+// Sommerfeld.
 bool carries_lower_triangle(const BssnParams* p) {
     if (!p || p->precision != BSSN_PRECISION_F64) return false;
     for (int f = 0; f < 6; ++f)
@@ -601,7 +630,7 @@ size_t ref_workspace_values(int op, const RefLayout& L, bool with_mom, bool lowe
     if (op == BSSN_OP_CONSTRAINTS) return (size_t)(NCOMP + 3 * NMIX + 24) * (size_t)L.cs;
     size_t blocks = (op == BSSN_OP_RK4 ? 4 * NCOMP : 2 * NCOMP) + rhs_work_blocks(with_mom);
     if (op == BSSN_OP_RHS_MATTER) blocks += kMatterComps;
-    if (op == BSSN_OP_RK4 && lower) blocks += 6;
+    if (op == BSSN_OP_RK4 && lower) blocks += kLowerTriangleBlocks;
     return blocks * (size_t)L.cs;
 }
 
@@ -695,13 +724,21 @@ int bssn_rk4_step(BssnFields* state, const int32_t shape[3], const BssnParams* p
     RhsWork w = carve_rhs_work(acc + NCOMP * L.cs, L.cs, with_mom);
     LowerTriangle lt;
     lt.delta = acc + (NCOMP + rhs_work_blocks(with_mom)) * L.cs;
-    lt.acc = lt.delta + 3 * L.cs;
+    lt.acc = (float*)(lt.delta + 6 * L.cs);
+    lt.stage[0] = lt.acc + 6 * L.cs;
+    lt.stage[1] = lt.stage[0] + 6 * L.cs;
     const Box region = box_of(G);
     BSSN_LAUNCH(KC_IMPORT, k_import, nblocks(region.count * NCOMP), kThreads, s, leaves_in(state), u0, G, region, L.npts);
-    if (lower)
-        BSSN_LAUNCH(KC_IMPORT, k_import_lower, nblocks(region.count * 3), kThreads, s, state->traceless_K, lt.delta, G,
-                    region, L.npts);
     cudaError_t e = cudaGetLastError();
+    if (lower && e == cudaSuccess) {
+        // delta, its FP32 copy (stage 1's input) and zero stage values over
+        // the owned box; stencils reach no padding along closed axes
+        BSSN_LAUNCH(KC_IMPORT, k_import_lower, nblocks(region.count * 6), kThreads, s, state->traceless_K,
+                    state->conformal_metric, lt.delta, lower_triangle_input(lt, 1), lower_triangle_output(lt, 1), G,
+                    region, L.npts);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = launch_fill_periodic(lower_triangle_input(lt, 1), 6, G, s);
+    }
     for (int n = 0; n < steps && e == cudaSuccess; ++n) {
         e = launch_project(u0, G, region, s);
         if (e == cudaSuccess) e = rk4_step_patch(u0, us, k, acc, w, G, region, true, 0, s, lower ? &lt : nullptr);
@@ -709,8 +746,8 @@ int bssn_rk4_step(BssnFields* state, const int32_t shape[3], const BssnParams* p
     if (e == cudaSuccess) {
         BSSN_LAUNCH(KC_EXPORT, k_export, nblocks(region.count * NCOMP), kThreads, s, u0, leaves_out(state), G, region, L.npts);
         if (lower)
-            BSSN_LAUNCH(KC_EXPORT, k_export_lower, nblocks(region.count * 3), kThreads, s, state->traceless_K, lt.delta,
-                        G, region, L.npts);
+            BSSN_LAUNCH(KC_EXPORT, k_export_lower, nblocks(region.count * 6), kThreads, s, state->traceless_K,
+                        state->conformal_metric, lt.delta, G, region, L.npts);
         e = cudaGetLastError();
     }
     return cuda_status(e, "bssn_rk4_step");

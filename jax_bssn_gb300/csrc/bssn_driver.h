@@ -25,13 +25,6 @@ cudaError_t launch_project(double* u, const Geo& G, const Box& B, cudaStream_t s
 cudaError_t launch_rk4_stage(const double* u0, const double* k, double* acc, double* out, const Geo& G,
                              const Box& B, int stage, double dt, int final_form, int project, cudaStream_t s);
 cudaError_t launch_zero(double* u, long long n, cudaStream_t s);
-// The reference's At lower triangle minus the upper one (3 blocks each; see
-// launch_lower_triangle), carried by the reference-layout RK4 call.
-struct LowerTriangle {
-    double* delta = nullptr;
-    double* acc = nullptr;
-};
-
 cudaError_t rk4_step_patch(double* u0, double* ustage, double* k, double* acc, const RhsWork& w,
                            const Geo& G, const Box& B, bool fill, int final_form, cudaStream_t s,
                            const LowerTriangle* lower = nullptr);

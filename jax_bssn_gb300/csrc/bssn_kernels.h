@@ -39,12 +39,31 @@ RhsWork carve_rhs_work(double* base, long long cs, bool with_mom);
 cudaError_t launch_rhs(const double* u, double* k, const RhsWork& w, const Geo& G, const Box& box,
                        cudaStream_t stream);
 
-// FP64 form with Sommerfeld faces: the source of the reference's At lower
-// triangle minus its upper one (3 blocks: xy, xz, yz) on the face shell at RK4
-// stage `stage`, accumulated with the RK4 weights in acc and added to delta
-// (dt/6 acc) at stage 4.  Reads w.d1 of the RHS just evaluated on u.
-cudaError_t launch_lower_triangle(const double* u, const RhsWork& w, double* acc, double* delta, const Geo& G,
+// The reference's At and gt lower triangles minus their upper ones (6
+// components: At xy, xz, yz, then gt xy, xz, yz), zero off the closure-row
+// shell of the owned box: the step's values in FP64 (6 blocks), and in FP32
+// the RK4 accumulator and two stage-value buffers (6 blocks each; stage[1]
+// holds the FP32 copy of delta between steps).
+struct LowerTriangle {
+    double* delta = nullptr;
+    float* acc = nullptr;
+    float* stage[2] = {nullptr, nullptr};
+};
+constexpr size_t kLowerTriangleBlocks = 6 + 18 / 2;   // in FP64 blocks
+
+// FP64 form with Sommerfeld faces: RK4 stage `stage` of the lower-triangle
+// differences on the shell of `box` (first-order rates; reads w.d1 of the RHS
+// just evaluated on u).  Reads lower_triangle_input(lt, q) at the stencil taps
+// and writes lower_triangle_output(lt, q): the next stage's values, or after
+// stage 4 (which also updates delta) delta's FP32 copy.
+cudaError_t launch_lower_triangle(const double* u, const RhsWork& w, const LowerTriangle& lt, const Geo& G,
                                   const Box& box, int stage, cudaStream_t stream);
+inline float* lower_triangle_input(const LowerTriangle& lt, int stage) {
+    return lt.stage[(stage == 1 || stage == 3) ? 1 : 0];
+}
+inline float* lower_triangle_output(const LowerTriangle& lt, int stage) {
+    return lt.stage[(stage == 1 || stage == 3) ? 0 : 1];
+}
 
 // Launch-shape autotuning of the RHS of one geometry: times `reps` RHS
 // evaluations per candidate block size of each launch slot and records the

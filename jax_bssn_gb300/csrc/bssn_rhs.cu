@@ -1475,49 +1475,172 @@ static void launch_rhs_form(const R* u, const double* u64, double* k, R* d1, R* 
 }
 
 // ---------------------------------------------------------------------------
-// The reference's lower triangle of At.  It evolves all nine At_ij; the
-// Hessians in W^2 D_i D_j alpha and in the W terms of W^2 R_ij are formed as
-// D1_j(D1_i f) for the (i, j) entry (JAX_BSSN/bssn/geometry.py:47-56,
-// 131-135), so its lower triangle uses the other ordering than its (and this
-// code's) upper triangle.  The two orderings commute exactly but round
-// differently where the inner derivative's one-sided closure acts on O(1)
-// samples, i.e. on the rows next to a Sommerfeld face.  The difference
-// delta_ij = At_ji - At_ij (i < j) then obeys, to first order,
-//   d_t delta_ij = alpha W (dd_ji W - dd_ij W) - W^2 (dd_ji alpha - dd_ij alpha),
-// dd_ij f = D1_j(D1_i f); the other terms are first order in delta and change
-// it by parts in a thousand per step.  k_lower_triangle evaluates that source on
-// the shell slabs (the closure rows; elsewhere the orderings agree to
-// roundoff) and accumulates it with the RK4 weights: acc = S1 + 2 S2 + 2 S3 + S4,
-// delta += dt/6 acc.  Only the reference-layout RK4 call carries delta.
+// The reference's lower triangles of At and gt.  It evolves all nine entries
+// of both; the Hessians in W^2 D_i D_j alpha and in the W terms of W^2 R_ij
+// are formed as D1_j(D1_i f) for the (i, j) entry (JAX_BSSN/bssn/
+// geometry.py:47-56, 131-135), so its lower triangle uses the other ordering
+// than its (and this code's) upper triangle.  The two orderings commute in
+// exact arithmetic but round differently where the inner derivative's
+// one-sided closure acts on O(1) samples, i.e. on the rows next to a
+// Sommerfeld face.  The differences dA_ij = At_ji - At_ij and
+// dg_ij = gt_ji - gt_ij (i < j) then obey, to first order in them,
+//   d_t dA = alpha W (dd_ji W - dd_ij W) - W^2 (dd_ji alpha - dd_ij alpha)
+//            + beta.grad dA + KO dA + (alpha K - 2/3 div beta) dA
+//            - 1/2 alpha W^2 gt^mn d_m d_n dg,
+//   d_t dg = beta.grad dg + KO dg - 2/3 div beta dg - 2 alpha dA,
+// dd_ij f = D1_j(D1_i f), and the Sommerfeld condition (zero far value) on the
+// active faces (JAX_BSSN/bssn/extrinsic_curvature.py, conformal_metric.py,
+// evolution/boundaries.py:20-171, the terms of each that do not cancel
+// between (i, j) and (j, i)).  The Ricci term's gt^mn d_m d_n dg matters
+// because dg, though of order 1e-17, is as sharp as the closure rows.  Terms
+// of second order (At gt^-1 At, the Christoffel terms) are left out.
+//
+// The differences live on the closure rows (they fall by orders of magnitude
+// per row inward), so k_lower_triangle evaluates these rates only on the shell
+// slabs of the owned box and the difference fields are zero beyond it.  The
+// source -- a difference of two roundings -- is evaluated in FP64 from the
+// stored first derivatives as the reference rounds it; the terms linear in
+// the differences need only a few digits (they are 1e-17-sized corrections
+// of 1e-12-sized values) and run in FP32 on FP32 copies, which keeps the
+// shell's stencils off GB300's FP64 pipe.  RK4 stage q reads the stage values
+// at the stencil taps from one FP32 buffer (stage 1: the step's values) and
+// writes the next stage's values  delta + c dt rate  to the other; stage 4
+// adds dt/6 acc to the FP64 delta in place and writes its FP32 copy for the
+// next step's stage 1.  Only the reference-layout RK4 call carries the
+// differences.
 // ---------------------------------------------------------------------------
+
+// D1_n(D1_m f) at ix (m != n): the outer first derivative along n applied to
+// the inner one along m at its taps, with the closure rows of both axes.
+template <typename R>
+__device__ __forceinline__ R mixed_d1(const R* __restrict__ f, const Geo& G, int m, int n, const int (&ix)[3]) {
+    const Axis& a = G.ax[n];
+    if (a.reduced || G.ax[m].reduced) return R(0);
+    const long long s = G.st[n];
+    auto inner = [&](int o) { return D1<R, true>(f + o * s, G, m, ix[m]); };
+    auto row = [&](const double (&c)[5], int first) {
+        R acc = R(0);
+#pragma unroll
+        for (int t = 0; t < 5; ++t) acc += static_cast<R>(c[t]) * inner(first + t);
+        return acc * BSSN_CO(R, G, inv_dx);
+    };
+    constexpr double L0[5] = {-25.0 / 12.0, 4.0, -3.0, 4.0 / 3.0, -1.0 / 4.0};
+    constexpr double L1[5] = {-1.0 / 4.0, -5.0 / 6.0, 3.0 / 2.0, -1.0 / 2.0, 1.0 / 12.0};
+    constexpr double R0[5] = {1.0 / 4.0, -4.0 / 3.0, 3.0, -4.0, 25.0 / 12.0};
+    constexpr double R1[5] = {-1.0 / 12.0, 1.0 / 2.0, -3.0 / 2.0, 5.0 / 6.0, 1.0 / 4.0};
+    int r = right_row<true>(a, ix[n], 2);
+    if (r == 0) return row(R0, -4);
+    if (r == 1) return row(R1, -3);
+    r = left_row<true>(a, ix[n], 2);
+    if (r == 0) return row(L0, 0);
+    if (r == 1) return row(L1, -1);
+    const R c1 = inner(1) - inner(-1), c2 = inner(2) - inner(-2);
+    const R d4 = c1 * BSSN_CO(R, G, d1a) + c2 * BSSN_CO(R, G, d1b);
+    if (!a.mad) return d4;
+    const R c3 = inner(3) - inner(-3);
+    return BSSN_AQ(R, a) * d4
+           + BSSN_AOMQ(R, a) * ((R(0.75) * c1 - R(0.15) * c2 + c3 / R(60)) * BSSN_CO(R, G, inv_dx));
+}
+
 __global__ void __launch_bounds__(kThreads)
-k_lower_triangle(const double* __restrict__ u, const double* __restrict__ d1, double* __restrict__ acc,
-                 double* __restrict__ delta, Geo G, BoxSet S, int stage, int nfield) {
+k_lower_triangle(const double* __restrict__ u, const double* __restrict__ d1, const float* __restrict__ din,
+                 float* __restrict__ dout, double* __restrict__ delta, float* __restrict__ acc, Geo G, BoxSet S,
+                 int stage, int nfield) {
     PointCtx c;
     if (!point(S.b[blockIdx.y], c, G)) return;
     const long long cs = G.cs, p = c.p;
-    const double W = u[CW * cs + p], al = u[CALPHA * cs + p];
+    const int k = blockIdx.z;   // pair (0,1), (0,2), (1,2)
     constexpr int pairs[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+    const int i = pairs[k][0], j = pairs[k][1];
+    const float* fa = din + k * cs + p;          // dA_ij stage values
+    const float* fg = din + (3 + k) * cs + p;    // dg_ij stage values
+    bool face = false;
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        const int i = pairs[k][0], j = pairs[k][1];
+    for (int d = 0; d < 3; ++d) {
+        const Axis& a = G.ax[d];
+        face = face || (a.slo && c.ix[d] == a.start) || (a.shi && c.ix[d] == a.end - 1);
+    }
+    float ra, rg;
+    if (face) {
+        float X[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) X[d] = (float)(G.ax[d].xmin + G.dx * (double)(c.ix[d] - G.ax[d].org));
+        const float r = sqrtf(X[0] * X[0] + X[1] * X[1] + X[2] * X[2]);
+        const float rs = r > 0.0f ? r : 1.0f;
+        float radial_a = 0.0f, radial_g = 0.0f;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            radial_a += X[d] * D1<float, true>(fa, G, d, c.ix[d]);
+            radial_g += X[d] * D1<float, true>(fg, G, d, c.ix[d]);
+        }
+        ra = -(radial_a + fa[0]) / rs;
+        rg = -(radial_g + fg[0]) / rs;
+    } else {
+        const double W = u[CW * cs + p], al = u[CALPHA * cs + p];
+        // the commuted Hessians' difference (the source), as the reference rounds it
         const double wu = D1<double, true>(d1ptr(d1, G, nfield, i, MIX_W, p), G, j, c.ix[j]);
         const double wl = D1<double, true>(d1ptr(d1, G, nfield, j, MIX_W, p), G, i, c.ix[i]);
         const double au = D1<double, true>(d1ptr(d1, G, nfield, i, MIX_ALPHA, p), G, j, c.ix[j]);
         const double al_ = D1<double, true>(d1ptr(d1, G, nfield, j, MIX_ALPHA, p), G, i, c.ix[i]);
-        const double src = al * W * (wl - wu) - W * W * (al_ - au);
-        const long long q = k * cs + p;
-        const double a = stage == 1 ? src : fma(stage == 4 ? 1.0 : 2.0, src, acc[q]);
-        acc[q] = a;
-        if (stage == 4) delta[q] += (G.dt / 6.0) * a;
+        const float src = (float)(al * W * (wl - wu) - W * W * (al_ - au));
+        float beta[3], bs[3], g[6], gi[6];
+#pragma unroll
+        for (int s6 = 0; s6 < 6; ++s6) g[s6] = (float)u[(GXX + s6) * cs + p];
+        inverse_metric(g, gi);
+        float divb = 0.0f;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            beta[d] = (float)u[(BX + d) * cs + p];
+            divb += (float)d1ptr(d1, G, nfield, d, MIX_B + d, p)[0];
+        }
+        shift_over_12dx(G, beta, bs);
+        const float fal = (float)al, fW = (float)W, fK = (float)u[CK * cs + p];
+        // gt^mn d_m d_n dg
+        float lap = 0.0f;
+#pragma unroll
+        for (int m = 0; m < 3; ++m) {
+            lap += gi[sym(m, m)] * D2<float, true, true>(fg, G, m, c.ix[m]);
+#pragma unroll
+            for (int n = m + 1; n < 3; ++n) lap += 2.0f * gi[sym(m, n)] * mixed_d1(fg, G, m, n, c.ix);
+        }
+        const float da = fa[0], dg = fg[0];
+        ra = src + ADV<float, true, true>(fa, G, c.ix, beta, bs) + KO<float, true, true>(fa, G, c.ix)
+             + (fal * fK - (2.0f / 3.0f) * divb) * da - 0.5f * fal * fW * fW * lap;
+        rg = ADV<float, true, true>(fg, G, c.ix, beta, bs) + KO<float, true, true>(fg, G, c.ix)
+             - (2.0f / 3.0f) * divb * dg - 2.0f * fal * da;
+    }
+    const long long qa = k * cs + p, qg = (3 + k) * cs + p;
+    float aa = ra, ag = rg;
+    if (stage > 1) {
+        const float w = stage == 4 ? 1.0f : 2.0f;
+        aa = fmaf(w, ra, acc[qa]);
+        ag = fmaf(w, rg, acc[qg]);
+    }
+    if (stage < 4) {
+        acc[qa] = aa;
+        acc[qg] = ag;
+        const double h = stage == 3 ? G.dt : 0.5 * G.dt;
+        dout[qa] = (float)fma(h, (double)ra, delta[qa]);
+        dout[qg] = (float)fma(h, (double)rg, delta[qg]);
+    } else {
+        const double na = fma(G.dt / 6.0, (double)aa, delta[qa]);
+        const double ng = fma(G.dt / 6.0, (double)ag, delta[qg]);
+        delta[qa] = na;
+        delta[qg] = ng;
+        dout[qa] = (float)na;   // the next step's stage-1 values
+        dout[qg] = (float)ng;
     }
 }
 
-cudaError_t launch_lower_triangle(const double* u, const RhsWork& w, double* acc, double* delta, const Geo& G,
+cudaError_t launch_lower_triangle(const double* u, const RhsWork& w, const LowerTriangle& lt, const Geo& G,
                                   const Box& box, int stage, cudaStream_t stream) {
     const int nfield = G.kappa != 0.0 ? NMIX + NMIX_MOM : NMIX;
-    const BoxSet shell = split_box(G, without_faces(G, box), false).shell;
-    BSSN_LAUNCH_SET(KC_OTHER, 1, k_lower_triangle, shell, stream, u, w.d1, acc, delta, G, shell, stage, nfield);
+    const BoxSet shell = split_box(G, box, false).shell;
+    if (shell.n == 0) return cudaSuccess;
+    const int threads = set_threads(shell, 1);
+    const dim3 grid((unsigned)((largest(shell) + threads - 1) / threads), shell.n, 3);
+    BSSN_LAUNCH(KC_OTHER, k_lower_triangle, grid, threads, stream, u, w.d1, lower_triangle_input(lt, stage),
+                lower_triangle_output(lt, stage), lt.delta, lt.acc, G, shell, stage, nfield);
     return cudaGetLastError();
 }
 

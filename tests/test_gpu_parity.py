@@ -122,7 +122,10 @@ def test_teukolsky_24_steps(gb):
 
 
 def test_patch_evolution_matches_reference_layout(gb):
-    """The resident patch path is the same arithmetic as rk4_step."""
+    """The resident patch path is the same arithmetic as rk4_step on the
+    independent components (the tensors' upper triangles and the other
+    leaves); rk4_step also carries the reference's lower triangles, which the
+    resident path exports symmetric."""
     pkg, te, _ = gb
     from jax_bssn_gb300.evolution import PatchEvolution
     from jax_bssn_gb300.initial_data import teukolsky_config
@@ -130,7 +133,14 @@ def test_patch_evolution_matches_reference_layout(gb):
     ref = te.rk4_steps(state, params, 3)
     evo = PatchEvolution(state, params)
     evo.step(3)
-    err = field_errors(evo.state(), ref)
+    out = evo.state()
+    upper = [(i, j) for i in range(3) for j in range(i, 3)]
+    for leaf in ("conformal_metric", "traceless_K"):
+        a, b = (np.asarray(t.detach().cpu() if hasattr(t, "detach") else t)
+                for t in (getattr(out, leaf), getattr(ref, leaf)))
+        assert all(np.array_equal(a[i, j], b[i, j]) for i, j in upper), leaf
+        assert all(np.array_equal(a[j, i], a[i, j]) for i, j in upper), leaf
+    err = field_errors(out._replace(conformal_metric=ref.conformal_metric, traceless_K=ref.traceless_K), ref)
     assert worst(err) == 0.0, err
     assert evo.nonfinite_count() == 0
 
