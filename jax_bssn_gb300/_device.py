@@ -30,8 +30,10 @@ def require_cuda() -> torch.device:
 
 
 # Arithmetic of the RHS kernels for calls made in this context: "fp64" (plain
-# float64, the default) or "fp32" (float RHS arithmetic on a float64 state).
-PRECISIONS = {"fp64": _native.PRECISION_F64, "fp32": _native.PRECISION_F32}
+# float64, the default), "fp32" (float RHS arithmetic on a float64 state) or
+# "fp32_paired" (the same with the second-derivative fields as float pairs).
+PRECISIONS = {"fp64": _native.PRECISION_F64, "fp32": _native.PRECISION_F32,
+              "fp32_paired": _native.PRECISION_F32_PAIRED}
 _ARITHMETIC = contextvars.ContextVar("jax_bssn_gb300_arithmetic", default="fp64")
 
 
@@ -63,7 +65,7 @@ def arithmetic(name: str):
 def to_params(params, precision: str | None = None) -> _native.BssnParams:
     """BSSNParameters -> the C struct (JAX_BSSN/bssn/variables.py:19-46).
 
-    ``precision`` ("fp64" / "fp32") overrides the context's arithmetic."""
+    ``precision`` ("fp64" / "fp32" / "fp32_paired") overrides the context's arithmetic."""
     p = _native.BssnParams()
     p.precision = PRECISIONS[_checked(precision) if precision is not None else _ARITHMETIC.get()]
     p.eta, p.kappa, p.nu, p.g = float(params.eta), float(params.kappa), float(params.nu), float(params.g)

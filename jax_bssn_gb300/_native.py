@@ -27,6 +27,7 @@ BSSN_ERR_NOT_CONVERGED = 6
 
 PRECISION_F64 = 0
 PRECISION_F32 = 1
+PRECISION_F32_PAIRED = 2
 
 OP_RHS = 1
 OP_RK4 = 2

@@ -781,6 +781,11 @@ cudaError_t reconstruct_f32(const CartoonPlan& P, const BssnParams* p, const dou
     BSSN_LAUNCH(KC_CONVERT, k_compact_f32, blocks(P.C.cs * NCOMP), kThr, s, u, P.C, cf);
     BSSN_LAUNCH(KC_CARTOON, k_axi_reconstruct_f32, grid, kAxiThreads, s, cf, u, P.C, A, w.uf, P.scs, sx, sy, 4, 4, 4,
                 T);
+    // the support is reconstructed in float alone: zero low words
+    if (P.Gs.precision == kPrecisionF32Paired) {
+        e = cudaMemsetAsync(w.uf + (long long)NCOMP * P.scs, 0, (size_t)NMIX * P.scs * sizeof(float), s);
+        if (e != cudaSuccess) return e;
+    }
     return launch_fill_periodic(w.uf, NCOMP, P.Gs, s);
 }
 
@@ -790,7 +795,7 @@ cudaError_t compact_rhs(const CartoonPlan& P, const BssnParams* p, const double*
     double* ks = us + NCOMP * P.scs;
     const RhsWork w = carve_rhs_work(ks + NCOMP * P.scs, P.scs, P.with_mom);
     cudaError_t e;
-    if (P.axi && P.Gs.precision == kPrecisionF32) {
+    if (P.axi && float_form(P.Gs.precision)) {
         e = reconstruct_f32(P, p, u, us, w, s, T);
         if (e == cudaSuccess) e = launch_rhs_f32_prepared(us, ks, w, P.Gs, P.centre, s);
     } else {

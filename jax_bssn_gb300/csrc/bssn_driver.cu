@@ -49,8 +49,10 @@ int validate_params(const BssnParams* p) {
         if (p->bc[f] != 0 && p->bc[f] != 1)
             return fail(BSSN_ERR_INVALID, "boundary codes must be 0 (periodic) or 1 (Sommerfeld)");
     if (p->gauge != 0 && p->gauge != 1) return fail(BSSN_ERR_INVALID, "gauge must be 0 or 1");
-    if (p->precision != BSSN_PRECISION_F64 && p->precision != BSSN_PRECISION_F32)
-        return fail(BSSN_ERR_INVALID, "precision must be BSSN_PRECISION_F64 or BSSN_PRECISION_F32");
+    if (p->precision != BSSN_PRECISION_F64 && p->precision != BSSN_PRECISION_F32 &&
+        p->precision != BSSN_PRECISION_F32_PAIRED)
+        return fail(BSSN_ERR_INVALID,
+                    "precision must be BSSN_PRECISION_F64, BSSN_PRECISION_F32 or BSSN_PRECISION_F32_PAIRED");
     return BSSN_OK;
 }
 
@@ -165,11 +167,15 @@ RhsWork carve_rhs_work(double* base, long long cs, bool with_mom) {
         w.der = base + (long long)(3 * (NMIX + NMIX_MOM)) * cs;
         w.damp = w.der + 24LL * cs;
     }
-    // FP32 views of the same memory: 21 + 3 * nfield (+ 24 + 6) floats per
-    // sample, within the 3 * nfield (+ 24 + 6) doubles of the FP64 layout.
+    // FP32 views of the same memory: 21 perturbations, the low words of the
+    // NMIX second-derivative fields, then 3 * nfield (+ 24 + 6) floats per
+    // sample -- within the 3 * nfield (+ 24 + 6) doubles of the FP64 layout.
     const int nfield = with_mom ? NMIX + NMIX_MOM : NMIX;
+    static_assert(NCOMP + NMIX + 3 * NMIX <= 2 * 3 * NMIX, "FP32 views must fit the FP64 scratch");
+    static_assert(NCOMP + NMIX + 3 * (NMIX + NMIX_MOM) + 30 <= 2 * (3 * (NMIX + NMIX_MOM) + 30),
+                  "FP32 views must fit the FP64 scratch");
     w.uf = reinterpret_cast<float*>(base);
-    w.d1f = w.uf + (long long)NCOMP * cs;
+    w.d1f = w.uf + (long long)(NCOMP + NMIX) * cs;
     if (with_mom) {
         w.derf = w.d1f + (long long)(3 * nfield) * cs;
         w.dampf = w.derf + 24LL * cs;
@@ -339,7 +345,7 @@ __device__ __forceinline__ void project_point_light(double (&g)[6], double (&A)[
 }
 
 __device__ __forceinline__ void project_form(double (&g)[6], double (&A)[6], int precision) {
-    if (precision == kPrecisionF32) project_point_light(g, A);
+    if (float_form(precision)) project_point_light(g, A);
     else project_point(g, A);
 }
 
@@ -484,7 +490,7 @@ cudaError_t launch_rk4_stage(const double* u0, const double* k, double* acc, dou
                              const Box& B, int stage, double dt, int final_form, int project,
                              cudaStream_t s) {
     const double h = stage == 3 ? dt : 0.5 * dt;
-    if (G.precision == kPrecisionF32)
+    if (float_form(G.precision))
         BSSN_LAUNCH(KC_STAGE, k_rk4_stage<true>, nblocks(box_threads(G, B)), kThreads, s, u0, k, acc, out, G, B, stage, h, dt,
                     final_form, project);
     else

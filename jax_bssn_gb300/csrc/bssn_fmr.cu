@@ -646,7 +646,7 @@ Box owned_box(const Geo& G) { return box_of(G); }
 cudaError_t prolong_child(const FmrPlan& plan, double* const* u, int p, const std::vector<PatchWork>* w,
                           cudaStream_t s) {
     const int q = plan.parent[p];
-    if (w && plan.geo[p].precision == kPrecisionF32)
+    if (w && float_form(plan.geo[p].precision))
         return launch_fmr_prolong_f32(u[q], plan.dims[q], u[p], plan.dims[p], plan.lo[p].data(), (*w)[p].rw.uf, s);
     return launch_fmr_prolong(u[q], plan.dims[q], u[p], plan.dims[p], plan.lo[p].data(), s);
 }

@@ -138,11 +138,27 @@ k_perturb(const double* __restrict__ u, float* __restrict__ uf, Geo G, Box regio
     int ix[3];
     region.coords(t, ix);
     const long long p = lin(G, ix) + off, cs = G.cs;
-#pragma unroll
-    for (int c = 0; c < NCOMP; ++c) {
+    auto perturbation = [&](int c) {
         const double b = has_background(c) ? 1.0 : (state_background(c) ? u[c * cs + p0 + off] : 0.0);
-        uf[c * cs + p] = static_cast<float>(u[c * cs + p] - b);
+        return u[c * cs + p] - b;
+    };
+#pragma unroll
+    for (int c = 0; c < NCOMP; ++c) uf[c * cs + p] = static_cast<float>(perturbation(c));
+    // Paired form: low words of the fields whose second derivatives are
+    // taken.  hi + lo carries the perturbation to ~48 bits, so the 1/dx^2 of
+    // D2 does not amplify the float rounding of the samples themselves.
+    if (G.precision != kPrecisionF32Paired) return;
+#pragma unroll
+    for (int f = 0; f < NMIX; ++f) {
+        const int c = mix_source(f);
+        const double d = perturbation(c);
+        uf[(NCOMP + f) * cs + p] = static_cast<float>(d - (double)static_cast<float>(d));
     }
+}
+
+// The low word of NMIX field f in the FP32 form's perturbation array.
+__device__ __forceinline__ const float* low_word(const float* uf, const Geo& G, int f, long long p) {
+    return uf + (NCOMP + f) * G.cs + p;
 }
 
 // ---------------------------------------------------------------------------
@@ -166,8 +182,12 @@ k_first_derivs(const R* __restrict__ u, const R* __restrict__ der, R* __restrict
     for (int d = 0; d < 3; ++d) {
         if (!in_range(G.ax[d], ix[d])) continue;
 #pragma unroll 1
-        for (int f = 0; f < NMIX; ++f)
-            d1[((long long)(d * nfield + f)) * cs + p] = D1<R, Closed>(u + mix_source(f) * cs + p, G, d, ix[d]);
+        for (int f = 0; f < NMIX; ++f) {
+            R v = D1<R, Closed>(u + mix_source(f) * cs + p, G, d, ix[d]);
+            if constexpr (kPerturbative<R>)
+                if (G.precision == kPrecisionF32Paired) v += D1<R, Closed>(low_word(u, G, f, p), G, d, ix[d]);
+            d1[((long long)(d * nfield + f)) * cs + p] = v;
+        }
         if (with_mom) {
 #pragma unroll 1
             for (int f = 0; f < 7; ++f)  // At (6), K
@@ -215,6 +235,14 @@ __device__ __forceinline__ void hessian(const R* __restrict__ u, const R* d1, co
     h[0] = D2<R, Closed, Exact>(fp, G, 0, c.ix[0]);
     h[3] = D2<R, Closed, Exact>(fp, G, 1, c.ix[1]);
     h[5] = D2<R, Closed, Exact>(fp, G, 2, c.ix[2]);
+    if constexpr (kPerturbative<R>) {
+        if (G.precision == kPrecisionF32Paired) {
+            const float* lo = low_word(u, G, f, c.p);
+            h[0] += D2<R, Closed, false>(lo, G, 0, c.ix[0]);
+            h[3] += D2<R, Closed, false>(lo, G, 1, c.ix[1]);
+            h[5] += D2<R, Closed, false>(lo, G, 2, c.ix[2]);
+        }
+    }
     h[1] = mixed<R, Closed>(d1, G, nfield, f, 0, 1, c);
     h[2] = mixed<R, Closed>(d1, G, nfield, f, 0, 2, c);
     h[4] = mixed<R, Closed>(d1, G, nfield, f, 1, 2, c);
@@ -1599,14 +1627,14 @@ k_lower_triangle(const double* __restrict__ u, const double* __restrict__ d1, co
         float lap = 0.0f;
 #pragma unroll
         for (int m = 0; m < 3; ++m) {
-            lap += gi[sym(m, m)] * D2<float, true, true>(fg, G, m, c.ix[m]);
+            lap += gi[sym(m, m)] * D2<float, true, false>(fg, G, m, c.ix[m]);
 #pragma unroll
             for (int n = m + 1; n < 3; ++n) lap += 2.0f * gi[sym(m, n)] * mixed_d1(fg, G, m, n, c.ix);
         }
         const float da = fa[0], dg = fg[0];
-        ra = src + ADV<float, true, true>(fa, G, c.ix, beta, bs) + KO<float, true, true>(fa, G, c.ix)
+        ra = src + ADV<float, true, false>(fa, G, c.ix, beta, bs) + KO<float, true, false>(fa, G, c.ix)
              + (fal * fK - (2.0f / 3.0f) * divb) * da - 0.5f * fal * fW * fW * lap;
-        rg = ADV<float, true, true>(fg, G, c.ix, beta, bs) + KO<float, true, true>(fg, G, c.ix)
+        rg = ADV<float, true, false>(fg, G, c.ix, beta, bs) + KO<float, true, false>(fg, G, c.ix)
              - (2.0f / 3.0f) * divb * dg - 2.0f * fal * da;
     }
     const long long qa = k * cs + p, qg = (3 + k) * cs + p;
@@ -1661,7 +1689,7 @@ cudaError_t tune_rhs(const double* u, double* k, const RhsWork& w, const Geo& G,
     int dev = 0;
     if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
     std::vector<int> classes = {KC_FIRST, KC_GAUGE};
-    if (G.precision == kPrecisionF32) {
+    if (float_form(G.precision)) {
         classes.push_back(KC_KGT);
         classes.push_back(KC_AT);
     } else {
@@ -1736,7 +1764,7 @@ cudaError_t launch_rhs_f32_prepared(const double* u, double* k, const RhsWork& w
 
 cudaError_t launch_rhs(const double* u, double* k, const RhsWork& w, const Geo& G, const Box& box,
                        cudaStream_t stream) {
-    if (G.precision == kPrecisionF32) {
+    if (float_form(G.precision)) {
         // Every sample the RHS kernels read lies within 6 of the box: first
         // derivatives on the box grown by 3 with a 3-sample reach; KO and
         // upwind stencils reach 4.

@@ -24,7 +24,12 @@
 // those are left free for FMA contraction and regrouping.  R = float is the FP32-arithmetic form: the same
 // operators on float samples (perturbations about a constant background),
 // with every coefficient taken in float so no FP64 instruction is issued, and
-// contraction allowed throughout.
+// contraction allowed throughout.  Float numerators of operators whose
+// coefficients sum to zero (D2, the sixth difference, every closure) are
+// formed from differences to the centre sample, f(k) - f(0): a float sum of
+// like samples rounds at eps*|f|, which the 1/dx^2 scaling would turn into
+// noise far above the operator's value for a small, smooth perturbation,
+// while the differences round at eps times themselves.
 #pragma once
 
 #include <cstdint>
@@ -35,6 +40,9 @@ namespace bssn {
 constexpr int kSommerfeld = 1;
 constexpr int kPrecisionF64 = 0;   // plain FP64 arithmetic
 constexpr int kPrecisionF32 = 1;   // FP32 RHS arithmetic, FP64 state and RK4
+constexpr int kPrecisionF32Paired = 2;   // the same, second-derivative inputs as float pairs
+// Every form but the plain FP64 one runs the float kernels.
+__host__ __device__ constexpr bool float_form(int precision) { return precision != kPrecisionF64; }
 
 // One axis of a padded patch: extent, compute range, closure range and the
 // face/MAD policy for this array (JAX_BSSN/evolution/spatial_derivatives.py:18-41).
@@ -76,7 +84,7 @@ struct Geo {
     double eta, kappa, g, dt;
     int gauge, zero_shift;
     int any_sommerfeld;
-    int precision;    // kPrecisionF64 or kPrecisionF32
+    int precision;    // kPrecisionF64, kPrecisionF32 or kPrecisionF32Paired
     // Independent instances of the same patch in one launch: buffers are laid
     // out [component][instance][padded block], so cs = ninst * istride and an
     // instance starts istride samples after the previous one.
@@ -151,10 +159,20 @@ __device__ __forceinline__ R ordered(const R* __restrict__ p, long long s, const
 // ---------------------------------------------------------------------------
 template <typename R, int N>
 __device__ __forceinline__ R closure(const R* __restrict__ p, long long s, int first, const double (&c)[N]) {
-    R acc = Num<R>::mul(static_cast<R>(c[0]), ld(p, (long long)first * s));
+    if constexpr (std::is_same<R, float>::value) {
+        // the rows' coefficients sum to zero and include the centre sample
+        const float f0 = ld(p, 0);
+        float acc = 0.0f;
 #pragma unroll
-    for (int t = 1; t < N; ++t) acc = mac(acc, c[t], ld(p, (long long)(first + t) * s));
-    return acc;
+        for (int t = 0; t < N; ++t)
+            if (first + t != 0) acc += static_cast<float>(c[t]) * (ld(p, (long long)(first + t) * s) - f0);
+        return acc;
+    } else {
+        R acc = Num<R>::mul(static_cast<R>(c[0]), ld(p, (long long)first * s));
+#pragma unroll
+        for (int t = 1; t < N; ++t) acc = mac(acc, c[t], ld(p, (long long)(first + t) * s));
+        return acc;
+    }
 }
 
 // Which closure row (0, 1, 2) applies at padded index i, or -1.  The upper
@@ -227,26 +245,48 @@ __device__ __forceinline__ R D1(const R* __restrict__ p, const Geo& G, int d, in
 // field's own scale rather than to an O(1) offset, so the reference's term
 // order does not have to be kept: the terms are grouped into symmetric pairs
 // and fused multiply-adds.  Template argument Exact = false selects these.
+// Float: second differences (f(k) - f(0)) + (f(-k) - f(0)) of the pairs.
+template <typename R>
+__device__ __forceinline__ R second_difference(const R* __restrict__ p, long long s, int k, R f0) {
+    return (ld(p, k * s) - f0) + (ld(p, -k * s) - f0);
+}
 template <typename R>
 __device__ __forceinline__ R d2_num_pairs(const R* __restrict__ p, long long s) {
-    const R p1 = ld(p, s) + ld(p, -s);
-    const R p2 = ld(p, 2 * s) + ld(p, -2 * s);
-    return (R(16) * p1 - p2) + R(-30) * ld(p, 0);
+    if constexpr (std::is_same<R, float>::value) {
+        const float f0 = ld(p, 0);
+        return 16.0f * second_difference(p, s, 1, f0) - second_difference(p, s, 2, f0);
+    } else {
+        const R p1 = ld(p, s) + ld(p, -s);
+        const R p2 = ld(p, 2 * s) + ld(p, -2 * s);
+        return (R(16) * p1 - p2) + R(-30) * ld(p, 0);
+    }
 }
 template <typename R>
 __device__ __forceinline__ R ko_num_pairs(const R* __restrict__ p, long long s) {
-    const R p1 = ld(p, s) + ld(p, -s);
-    const R p2 = ld(p, 2 * s) + ld(p, -2 * s);
-    const R p3 = ld(p, 3 * s) + ld(p, -3 * s);
-    return ((p3 + R(-6) * p2) + R(15) * p1) + R(-20) * ld(p, 0);
+    if constexpr (std::is_same<R, float>::value) {
+        const float f0 = ld(p, 0);
+        return (second_difference(p, s, 3, f0) - 6.0f * second_difference(p, s, 2, f0))
+               + 15.0f * second_difference(p, s, 1, f0);
+    } else {
+        const R p1 = ld(p, s) + ld(p, -s);
+        const R p2 = ld(p, 2 * s) + ld(p, -2 * s);
+        const R p3 = ld(p, 3 * s) + ld(p, -3 * s);
+        return ((p3 + R(-6) * p2) + R(15) * p1) + R(-20) * ld(p, 0);
+    }
 }
 // Sixth-order D2 numerator (MAD blend) in symmetric pairs.
 template <typename R>
 __device__ __forceinline__ R d2_6_num_pairs(const R* __restrict__ p, long long s) {
-    const R p1 = ld(p, s) + ld(p, -s);
-    const R p2 = ld(p, 2 * s) + ld(p, -2 * s);
-    const R p3 = ld(p, 3 * s) + ld(p, -3 * s);
-    return ((R(1.0 / 90.0) * p3 + R(-3.0 / 20.0) * p2) + R(3.0 / 2.0) * p1) + R(-49.0 / 18.0) * ld(p, 0);
+    if constexpr (std::is_same<R, float>::value) {
+        const float f0 = ld(p, 0);
+        return (float(1.0 / 90.0) * second_difference(p, s, 3, f0) + float(-3.0 / 20.0) * second_difference(p, s, 2, f0))
+               + float(3.0 / 2.0) * second_difference(p, s, 1, f0);
+    } else {
+        const R p1 = ld(p, s) + ld(p, -s);
+        const R p2 = ld(p, 2 * s) + ld(p, -2 * s);
+        const R p3 = ld(p, 3 * s) + ld(p, -3 * s);
+        return ((R(1.0 / 90.0) * p3 + R(-3.0 / 20.0) * p2) + R(3.0 / 2.0) * p1) + R(-49.0 / 18.0) * ld(p, 0);
+    }
 }
 // Any numerator as a fused multiply-add chain.
 template <typename R, int N>

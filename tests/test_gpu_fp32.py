@@ -1,4 +1,5 @@
-"""The FP32-arithmetic form (float RHS arithmetic, float64 state and RK4)
+"""The FP32-arithmetic forms (float RHS arithmetic, float64 state and RK4;
+"fp32_paired" also holds the second-derivative fields as float pairs)
 against the float64 reference goldens.
 
 Error metric: per leaf, max|fp32-form - ref| divided by the leaf's deviation
@@ -48,29 +49,34 @@ def gb(cuda, native):
     return pkg, time_evolve
 
 
+FORMS = ["fp32", "fp32_paired"]
+
+
 def _inputs(data, pkg):
     return golden_state(data, "input", pkg.BSSNVariables), golden_params(data, pkg.BSSNParameters)
 
 
+@pytest.mark.parametrize("form", FORMS)
 @pytest.mark.parametrize("name", RHS_CASES)
-def test_fp32_rhs_against_reference(gb, name):
+def test_fp32_rhs_against_reference(gb, name, form):
     """RHS of the FP32 form, error relative to the reference RHS's own scale."""
     pkg, te = gb
     data = load_golden(f"rhs_{name}")
     state, params = _inputs(data, pkg)
-    with pkg.arithmetic("fp32"):
+    with pkg.arithmetic(form):
         rhs = te.compute_bssn_rhs(state, params)
     err = deviation_errors(rhs, golden_state(data, "rhs", OracleVars), background=False)
     print(name, "fp32 rhs", {k: f"{v:.1e}" for k, v in err.items()})
     assert max(err.values()) < 2e-4
 
 
+@pytest.mark.parametrize("form", FORMS)
 @pytest.mark.parametrize("name", RHS_CASES)
-def test_fp32_rk4_step_against_reference(gb, name):
+def test_fp32_rk4_step_against_reference(gb, name, form):
     pkg, te = gb
     data = load_golden(f"rhs_{name}")
     state, params = _inputs(data, pkg)
-    with pkg.arithmetic("fp32"):
+    with pkg.arithmetic(form):
         one = te.rk4_step(state, params)
     err = deviation_errors(one, golden_state(data, "rk4_1", OracleVars))
     print(name, "fp32 rk4 1", {k: f"{v:.1e}" for k, v in err.items()})
@@ -90,14 +96,15 @@ def test_fp32_gauge_wave_hundred_steps(gb):
     assert max(err.values()) < 1e-5
 
 
-def test_fp32_teukolsky_ten_steps_and_constraint_norms(gb):
+@pytest.mark.parametrize("form", FORMS)
+def test_fp32_teukolsky_ten_steps_and_constraint_norms(gb, form):
     """Teukolsky 24^3 (amplitude 1e-5, Sommerfeld faces): ten steps, then the
     Hamiltonian and momentum constraint L2 norms within 1% of the float64 run's."""
     pkg, te = gb
     from jax_bssn_gb300.bssn.constraints import compute_all_constraints, compute_constraint_norms
     data = load_golden("run_teukolsky24")
     state, params = _inputs(data, pkg)
-    with pkg.arithmetic("fp32"):
+    with pkg.arithmetic(form):
         ten = te.rk4_steps(state, params, 10)
     ref = golden_state(data, "rk4_10", OracleVars)
     err = deviation_errors(ten, ref)
@@ -110,20 +117,22 @@ def test_fp32_teukolsky_ten_steps_and_constraint_norms(gb):
         assert n32[key] == pytest.approx(n64[key], rel=1e-2), key
 
 
-def test_fp32_resident_patch_matches_drop_in(gb):
+@pytest.mark.parametrize("form", FORMS)
+def test_fp32_resident_patch_matches_drop_in(gb, form):
     pkg, te = gb
     from jax_bssn_gb300.evolution import PatchEvolution
     data = load_golden("run_teukolsky24")
     state, params = _inputs(data, pkg)
-    evo = PatchEvolution(state, params, precision="fp32")
+    evo = PatchEvolution(state, params, precision=form)
     evo.step(3)
-    with pkg.arithmetic("fp32"):
+    with pkg.arithmetic(form):
         want = te.rk4_steps(state, params, 3)
     for a, b in zip(evo.state(), want):
         np.testing.assert_array_equal(_np(a), _np(b))
 
 
-def test_fp32_fmr_against_reference(gb):
+@pytest.mark.parametrize("form", FORMS)
+def test_fp32_fmr_against_reference(gb, form):
     """Nested FMR (three levels, MAD): two stage-synchronous RK4 steps."""
     pkg, _ = gb
     from jax_bssn_gb300.fmr import FMRHierarchySpec, FMRPatchSpec, TileLayout, fmr_rk4_step, prepare_fmr_states
@@ -142,7 +151,7 @@ def test_fp32_fmr_against_reference(gb):
             leaves.append(full.reshape(leaf.shape[:-3] + (1, 1, 1) + full.shape[-3:]))
         raw.append(pkg.BSSNVariables(*leaves))
     initial = prepare_fmr_states(tuple(raw), params, h, layouts=layouts, project=False)
-    with pkg.arithmetic("fp32"):
+    with pkg.arithmetic(form):
         two = fmr_rk4_step(fmr_rk4_step(initial, params, h, layouts=layouts), params, h, layouts=layouts)
     expect = owned_states(data, "rk4_2", len(shapes))
     for p, n in enumerate(shapes):
@@ -152,13 +161,14 @@ def test_fp32_fmr_against_reference(gb):
         assert max(err.values()) < 1e-5, (p, err)
 
 
-def test_fp32_cartoon_against_reference(gb):
+@pytest.mark.parametrize("form", FORMS)
+def test_fp32_cartoon_against_reference(gb, form):
     pkg, _ = gb
     from jax_bssn_gb300.cartoon.axisymmetry import axisymmetric_rk4_step, compute_axisymmetric_rhs
     from jax_bssn_gb300.cartoon.spherical_symmetry import cartoon_rk4_step
     data = load_golden("cartoon_axisymmetric")
     state, params = _inputs(data, pkg)
-    with pkg.arithmetic("fp32"):
+    with pkg.arithmetic(form):
         rhs = compute_axisymmetric_rhs(state, params)
         two = axisymmetric_rk4_step(axisymmetric_rk4_step(state, params), params)
     e_rhs = deviation_errors(rhs, golden_state(data, "rhs", OracleVars), background=False)
@@ -168,11 +178,43 @@ def test_fp32_cartoon_against_reference(gb):
     assert max(e_two.values()) < 1e-5
     data = load_golden("cartoon_spherical")
     state, params = _inputs(data, pkg)
-    with pkg.arithmetic("fp32"):
+    with pkg.arithmetic(form):
         two = cartoon_rk4_step(cartoon_rk4_step(state, params), params)
     e_two = deviation_errors(two, golden_state(data, "rk4_2", OracleVars))
     print("fp32 spherical rk4 2", {k: f"{v:.1e}" for k, v in e_two.items()})
     assert max(e_two.values()) < 1e-5
+
+
+def test_paired_form_removes_the_second_derivative_rounding(gb):
+    """A 1e-8 plus-polarised wave at spacing 1/24 (the finest level of the
+    benchmarked FMR hierarchy), periodic.  Float rounding of the metric's
+    samples, amplified by 1/dx^2 in the Ricci tensor, dominates the plain
+    FP32 RHS of At (about eps * 5 / (k dx)^2 of the signal); at this spacing
+    even the FP64 form's unit-background numerators round at ~1e-5 of the
+    signal.  Against the oracle evaluated in long double on the same input
+    bits, the paired form must be at least five times more accurate than the
+    plain FP32 form and within twice the FP64 form's error."""
+    pkg, te = gb
+    from oracle import bssn as ob
+    from oracle.state import BSSNParameters as OracleParams
+    from jax_bssn_gb300.initial_data import linear_wave_state
+    n, dx = 96, 1.0 / 24.0
+    x = -2.0 + dx * np.arange(n)
+    X, Y, Z = np.meshgrid(x, x[:8], x[:8], indexing="ij")
+    host = linear_wave_state(X, Y, Z, 1.0e-8, 4.0)
+    state = pkg.BSSNVariables(*host)
+    kw = dict(dx=dx, dt=0.25 * dx, eta=0.0, kappa=0.0, nu=0.0, g=0.0, zero_shift=1, gauge=0)
+    params = pkg.BSSNParameters(**kw)
+    wide = ob.compute_rhs(OracleVars(*(np.asarray(f, dtype=np.longdouble) for f in host)), OracleParams(**kw))
+    ref = np.asarray(wide.traceless_K, dtype=np.float64)
+    err = {}
+    for form in ["fp64"] + FORMS:
+        with pkg.arithmetic(form):
+            got = _np(te.compute_bssn_rhs(state, params).traceless_K)
+        err[form] = float(np.max(np.abs(got - ref)) / np.max(np.abs(ref)))
+    print("At rhs error against the long-double oracle", {k: f"{v:.1e}" for k, v in err.items()})
+    assert err["fp32_paired"] < 0.2 * err["fp32"], err
+    assert err["fp32_paired"] < 2.0 * err["fp64"], err
 
 
 def test_precision_argument_is_validated(gb):
