@@ -268,6 +268,21 @@ int bssn_adjoint_backward(double* adjoint, const BssnPatch* patch, int32_t ninst
 int bssn_tune_patch(double* states, const BssnPatch* patch, int32_t ninst, const BssnParams* params, float margin,
                     void* workspace, size_t workspace_bytes, char* report, size_t report_bytes, void* stream);
 
+/* No reference counterpart: the FP32 forms' gauge RHS (dt gt, W, alpha,
+ * beta) runs on the box interior from TMA-staged shared-memory tiles where
+ * the geometry allows it -- one instance, a z pitch (nz + 2 ghost) that is a
+ * multiple of four, no MAD axis -- and from the generic kernel elsewhere.
+ * enabled != 0 (the default) keeps that; 0 uses the generic kernel everywhere
+ * (results agree to float rounding).  Process-wide; affects later launches
+ * and captures. */
+int bssn_set_tma(int32_t enabled);
+
+/* TMA kernel status: *timeouts receives the number of tile waits on the
+ * current device that gave up since the last call (each leaves its tile's RHS
+ * unwritten and should never happen; the count is reset), *launches the TMA
+ * kernel launches of the process so far (optional).  Synchronises the device. */
+int bssn_tma_status(int32_t* timeouts, int64_t* launches);
+
 /* Whole-array conversion between the reference layout (seven leaves) and the
  * 21-component layout, over all samples of an array of the given extent
  * (e.g. a padded FMR patch, whose guards are part of the array). */

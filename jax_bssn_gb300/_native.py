@@ -145,6 +145,8 @@ SIGNATURES = {
                                                 ctypes.POINTER(BssnParams), ctypes.c_int32, ctypes.c_int32,
                                                 ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32), ctypes.c_void_p,
                                                 ctypes.c_size_t, ctypes.c_void_p]),
+    "bssn_set_tma": (ctypes.c_int, [ctypes.c_int32]),
+    "bssn_tma_status": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int64)]),
     "bssn_tune_patch": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BssnPatch), ctypes.c_int32,
                                        ctypes.POINTER(BssnParams), ctypes.c_float, ctypes.c_void_p, ctypes.c_size_t,
                                        ctypes.c_char_p, ctypes.c_size_t, ctypes.c_void_p]),
@@ -311,3 +313,16 @@ def tune_launch_shapes(state_ptr: int, shape, instances: int, cparams: BssnParam
                               workspace.numel(),
                               report, 4096, _device.stream_handle()), "bssn_tune_patch")
     return report.value.decode()
+
+
+def set_tma(enabled: bool) -> None:
+    """TMA-staged gauge kernel of the FP32 forms on (default) or off (bssn_set_tma)."""
+    check(load().bssn_set_tma(1 if enabled else 0), "bssn_set_tma")
+
+
+def tma_status() -> tuple:
+    """(TMA tile waits that gave up since the last call, TMA launches so far)
+    (bssn_tma_status)."""
+    timeouts, launches = ctypes.c_int32(0), ctypes.c_int64(0)
+    check(load().bssn_tma_status(ctypes.byref(timeouts), ctypes.byref(launches)), "bssn_tma_status")
+    return timeouts.value, launches.value

@@ -1018,6 +1018,20 @@ int bssn_tune_patch(double* states, const BssnPatch* patch, int32_t ninst, const
     return cuda_status(e, "bssn_tune_patch");
 }
 
+int bssn_set_tma(int32_t enabled) {
+    set_tma_enabled(enabled != 0);
+    return BSSN_OK;
+}
+
+int bssn_tma_status(int32_t* timeouts, int64_t* launches) {
+    if (!timeouts) return fail(BSSN_ERR_INVALID, "null pointer");
+    int n = 0;
+    const cudaError_t e = tma_timeouts(&n);
+    *timeouts = n;
+    if (launches) *launches = tma_launches();
+    return cuda_status(e, "bssn_tma_status");
+}
+
 // The single-patch calls are the one-instance batch.
 size_t bssn_patch_values(const BssnPatch* patch) { return bssn_batch_values(patch, 1); }
 

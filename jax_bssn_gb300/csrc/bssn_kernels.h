@@ -65,6 +65,13 @@ inline float* lower_triangle_output(const LowerTriangle& lt, int stage) {
     return lt.stage[(stage == 1 || stage == 3) ? 0 : 1];
 }
 
+// The FP32 form's TMA gauge kernel: on (the default) wherever its geometry
+// allows, or off (the generic kernel everywhere); the number of its tile
+// waits that gave up since the last read, reset by reading.
+void set_tma_enabled(bool on);
+cudaError_t tma_timeouts(int* count);
+long long tma_launches();
+
 // Launch-shape autotuning of the RHS of one geometry: times `reps` RHS
 // evaluations per candidate block size of each launch slot and records the
 // fastest for later launches of that slot at that size when its time is below
