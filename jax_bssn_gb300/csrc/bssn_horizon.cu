@@ -688,90 +688,150 @@ k_band_step_fused(Band B, int k, int search, double* __restrict__ rhs, double* _
 }
 
 // Blocked form: one launch factors kPanel columns.  Every block factors the
-// panel (rows c0 .. c0 + kl + kPanel - 1 of columns c0 .. c0 + kPanel - 1) in
-// shared memory from a copy the previous launch left in `pin` (the same pivot
-// rule, swaps and eliminations as the column steps, in the same order), then
-// each warp applies the panel's swaps and eliminations to one trailing column
-// (or the right-hand side) held in shared memory.  The warps whose columns
-// form the next panel also write them to `pout`; block 0 writes the panel's U
-// rows and pivots back.  Needs kl + kPanel <= kPanelRows.
+// panel (rows c0 .. c0 + kl + kPanel - 1 of columns c0 .. c0 + kPanel - 1)
+// from a copy the previous launch left in `pin` (the same pivot rule, swaps
+// and eliminations as the column steps, in the same order), then each warp
+// applies the panel's swaps and eliminations to one trailing column (or the
+// right-hand side).  The warps whose columns form the next panel also write
+// them to `pout`; block 0 writes the panel's U rows and pivots back.  Needs
+// kl + kPanel <= kPanelRows.
+//
+// The panel lives in registers: thread t holds rows t, t + 128, t + 256 of all
+// kPanel columns, so a column step is one barrier.  Each warp reduces a pivot
+// candidate and its owner publishes the candidate row (and the owner of row jj
+// that row) to double-buffered shared slots; after the barrier every thread
+// picks the winner and eliminates its own rows.  A trailing column lives in
+// registers too (lane l holds rows l + 32 q): the row swap and the pivot-row
+// broadcast are shuffles, and only the L multipliers are read from shared memory.
 constexpr int kPanel = 8;
 constexpr int kPanelWarps = 4;
 constexpr int kPanelRows = 384;
+
+// v[q] for a q known only at run time, without dynamic register indexing.
+template <int N>
+__device__ __forceinline__ double pick(const double (&v)[N], int q) {
+    double out = 0.0;
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+        if (i == q) out = v[i];
+    return out;
+}
+template <int N>
+__device__ __forceinline__ void place(double (&v)[N], int q, double x) {
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+        if (i == q) v[i] = x;
+}
 
 __global__ void __launch_bounds__(kPanelWarps * 32)
 k_band_panel(Band B, int c0, const double* __restrict__ pin, double* __restrict__ pout, double* __restrict__ rhs,
              double* __restrict__ diag) {
     pdl_enter();
-    __shared__ double Ps[kPanel][kPanelRows];
+    constexpr int kThr = kPanelWarps * 32;
+    constexpr int kQP = (kPanelRows + kThr - 1) / kThr;   // panel rows per thread
+    constexpr int kQC = kPanelRows / 32;                  // trailing-column rows per lane
+    __shared__ double Ps[kPanel][kPanelRows];              // factored panel: L below, U on and above the diagonal
     __shared__ double Cs[kPanelWarps][kPanelRows];
+    __shared__ double s_cand[2][kPanelWarps][kPanel];      // each warp's pivot candidate row
+    __shared__ double s_cbest[2][kPanelWarps];
+    __shared__ int s_carg[2][kPanelWarps];
+    __shared__ double s_rowk[2][kPanel];                   // row jj before the step
     __shared__ int s_po[kPanel];
-    __shared__ double s_rp[kPanel], s_akk[kPanel], s_piv[kPanel], s_xk[kPanel], s_xp[kPanel];
+    __shared__ double s_piv[kPanel];
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const int P = B.kl + kPanel;
     const int nrow = min(P, B.n - c0);
     const int ncol = min(kPanel, B.n - c0);
-    {
-        constexpr int kQ = (kPanelRows + kPanelWarps * 32 - 1) / (kPanelWarps * 32);
-        double v[kPanel][kQ];  // every load issued before any is used
+
+    double v[kPanel][kQP];
 #pragma unroll
-        for (int jj = 0; jj < kPanel; ++jj)
+    for (int jj = 0; jj < kPanel; ++jj)
 #pragma unroll
-            for (int q = 0; q < kQ; ++q) {
-                const int o = tid + q * kPanelWarps * 32;
-                v[jj][q] = (jj < ncol && o < nrow) ? pin[jj * P + o] : 0.0;
-            }
+        for (int q = 0; q < kQP; ++q) {
+            const int o = tid + q * kThr;
+            v[jj][q] = (jj < ncol && o < nrow) ? pin[jj * P + o] : 0.0;
+        }
 #pragma unroll
-        for (int jj = 0; jj < kPanel; ++jj)
-#pragma unroll
-            for (int q = 0; q < kQ; ++q) {
-                const int o = tid + q * kPanelWarps * 32;
-                if (o < P) Ps[jj][o] = v[jj][q];
-            }
-    }
-    __syncthreads();
-    for (int jj = 0; jj < ncol; ++jj) {
+    for (int jj = 0; jj < kPanel; ++jj) {
+        if (jj >= ncol) break;
         const int omax = min(nrow - 1, jj + B.kl);
-        if (w == 0) {
-            double best = -1.0;
-            int arg = jj;
-            for (int o = jj + lane; o <= omax; o += 32) {
-                const double v = fabs(Ps[jj][o]);
-                if (v > best) { best = v; arg = o; }
+        const int sb = jj & 1;
+        // this thread's candidate, then the warp's (largest |value|, lowest row on ties)
+        double best = -1.0;
+        int arg = jj;
+#pragma unroll
+        for (int q = 0; q < kQP; ++q) {
+            const int o = tid + q * kThr;
+            if (o >= jj && o <= omax) {
+                const double a = fabs(v[jj][q]);
+                if (a > best) { best = a; arg = o; }
             }
-            for (int sh = 16; sh > 0; sh >>= 1) {
-                const double ob = __shfl_xor_sync(0xffffffffu, best, sh);
-                const int oa = __shfl_xor_sync(0xffffffffu, arg, sh);
-                if (ob > best || (ob == best && oa < arg)) { best = ob; arg = oa; }
-            }
-            if (lane == 0) {
-                s_po[jj] = arg;
-                s_piv[jj] = Ps[jj][arg];
-                s_akk[jj] = Ps[jj][jj];
-                s_rp[jj] = 1.0 / Ps[jj][arg];
-            }
-            // rows jj and po of the later panel columns, before any is rewritten
-            if (lane > jj && lane < ncol) {
-                s_xk[lane] = Ps[lane][jj];
-                s_xp[lane] = Ps[lane][arg];
-            }
+        }
+        for (int sh = 16; sh > 0; sh >>= 1) {
+            const double ob = __shfl_xor_sync(0xffffffffu, best, sh);
+            const int oa = __shfl_xor_sync(0xffffffffu, arg, sh);
+            if (ob > best || (ob == best && oa < arg)) { best = ob; arg = oa; }
+        }
+        if (lane == 0) {
+            s_cbest[sb][w] = best;
+            s_carg[sb][w] = arg;
+        }
+        if (best >= 0.0 && tid == arg % kThr) {
+#pragma unroll
+            for (int jc = 0; jc < kPanel; ++jc) s_cand[sb][w][jc] = pick(v[jc], arg / kThr);
+        }
+        if (tid == jj % kThr) {
+#pragma unroll
+            for (int jc = 0; jc < kPanel; ++jc) s_rowk[sb][jc] = v[jc][jj / kThr];
         }
         __syncthreads();
-        const int po = s_po[jj];
-        const double rp = s_rp[jj], akk = s_akk[jj];
-        // per row: the multiplier into column jj, then the swap and elimination
-        // of the later panel columns
-        for (int o = jj + 1 + tid; o <= omax; o += blockDim.x) {
-            const double l = (o == po ? akk : Ps[jj][o]) * rp;
-            Ps[jj][o] = l;
-            for (int jc = jj + 1; jc < ncol; ++jc) Ps[jc][o] = (o == po ? s_xk[jc] : Ps[jc][o]) - l * s_xp[jc];
+        int win = 0;
+        double wb = s_cbest[sb][0];
+        int wa = s_carg[sb][0];
+#pragma unroll
+        for (int ww = 1; ww < kPanelWarps; ++ww) {
+            const double ob = s_cbest[sb][ww];
+            const int oa = s_carg[sb][ww];
+            if (ob > wb || (ob == wb && oa < wa)) { wb = ob; wa = oa; win = ww; }
         }
+        const int po = wa;
+        double xp[kPanel], xk[kPanel];
+#pragma unroll
+        for (int jc = 0; jc < kPanel; ++jc) {
+            xp[jc] = s_cand[sb][win][jc];
+            xk[jc] = s_rowk[sb][jc];
+        }
+        const double piv = xp[jj], akk = xk[jj];
+        const double rp = 1.0 / piv;   // multipliers scaled by the reciprocal, as getf2 does
         if (tid == 0) {
-            Ps[jj][jj] = s_piv[jj];
-            for (int jc = jj + 1; jc < ncol; ++jc) Ps[jc][jj] = s_xp[jc];
+            s_po[jj] = po;
+            s_piv[jj] = piv;
         }
-        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < kQP; ++q) {
+            const int o = tid + q * kThr;
+            if (o > jj && o <= omax) {
+                const double l = (o == po ? akk : v[jj][q]) * rp;
+                v[jj][q] = l;
+#pragma unroll
+                for (int jc = jj + 1; jc < kPanel; ++jc)
+                    if (jc < ncol) v[jc][q] = (o == po ? xk[jc] : v[jc][q]) - l * xp[jc];
+            } else if (o == jj) {
+                v[jj][q] = piv;
+#pragma unroll
+                for (int jc = jj + 1; jc < kPanel; ++jc)
+                    if (jc < ncol) v[jc][q] = xp[jc];
+            }
+        }
     }
+#pragma unroll
+    for (int jj = 0; jj < kPanel; ++jj)
+#pragma unroll
+        for (int q = 0; q < kQP; ++q) {
+            const int o = tid + q * kThr;
+            if (o < kPanelRows) Ps[jj][o] = v[jj][q];
+        }
+    __syncthreads();
 
     // trailing columns (and the right-hand side)
     const int first = c0 + ncol;
@@ -784,39 +844,39 @@ k_band_panel(Band B, int c0, const double* __restrict__ pin, double* __restrict_
         double* col = is_rhs ? rhs : B.a + (long long)j * B.ld + (B.ku2 - j);  // col[r] = A(r, j)
         const int rlo = is_rhs ? 0 : j - B.ku2;                                 // rows inside the band
         const int rhi = is_rhs ? B.n - 1 : min(B.n - 1, j + B.kl);
-        double* cs = Cs[w];
-        {
-            constexpr int kQ = kPanelRows / 32;
-            double v[kQ];
+        double cr[kQC];
 #pragma unroll
-            for (int q = 0; q < kQ; ++q) {
-                const int o = lane + 32 * q, r = c0 + o;
-                v[q] = (o < nrow && r >= rlo && r <= rhi) ? col[r] : 0.0;
-            }
+        for (int q = 0; q < kQC; ++q) {
+            const int o = lane + 32 * q, r = c0 + o;
+            cr[q] = (o < nrow && r >= rlo && r <= rhi) ? col[r] : 0.0;
+        }
 #pragma unroll
-            for (int q = 0; q < kQ; ++q) {
+        for (int jj = 0; jj < kPanel; ++jj) {
+            if (jj >= ncol) break;
+            const int po = s_po[jj];
+            // swap rows jj (lane jj, slot 0) and po, then eliminate below jj
+            const double a_jj = __shfl_sync(0xffffffffu, cr[0], jj);
+            const double a_po = __shfl_sync(0xffffffffu, pick(cr, po >> 5), po & 31);
+            if (lane == jj) cr[0] = a_po;
+            if (po != jj && lane == (po & 31)) place(cr, po >> 5, a_jj);
+            const double xc = a_po;
+            const int omax = min(nrow - 1, jj + B.kl);
+#pragma unroll
+            for (int q = 0; q < kQC; ++q) {
                 const int o = lane + 32 * q;
-                if (o < nrow) cs[o] = v[q];
+                if (o > jj && o <= omax) cr[q] -= Ps[jj][o] * xc;
+            }
+        }
+        double* cs = Cs[w];
+#pragma unroll
+        for (int q = 0; q < kQC; ++q) {
+            const int o = lane + 32 * q, r = c0 + o;
+            if (o < nrow) {
+                cs[o] = cr[q];
+                if (r >= rlo && r <= rhi) col[r] = cr[q];
             }
         }
         __syncwarp();
-        for (int jj = 0; jj < ncol; ++jj) {
-            const int po = s_po[jj];
-            if (lane == 0 && po != jj) {
-                const double t = cs[jj];
-                cs[jj] = cs[po];
-                cs[po] = t;
-            }
-            __syncwarp();
-            const double xc = cs[jj];
-            const int omax = min(nrow - 1, jj + B.kl);
-            for (int o = jj + 1 + lane; o <= omax; o += 32) cs[o] -= Ps[jj][o] * xc;
-            __syncwarp();
-        }
-        for (int o = lane; o < nrow; o += 32) {
-            const int r = c0 + o;
-            if (r >= rlo && r <= rhi) col[r] = cs[o];
-        }
         // the next panel's copy
         const int nc0 = first;
         if (!is_rhs && j < nc0 + kPanel) {
@@ -825,9 +885,9 @@ k_band_panel(Band B, int c0, const double* __restrict__ pin, double* __restrict_
             for (int o = lane; o < nrow2; o += 32) {
                 const int r = nc0 + o;
                 const int local = r - c0;
-                double v = 0.0;
-                if (r >= rlo && r <= rhi) v = local < nrow ? cs[local] : col[r];
-                dst[o] = v;
+                double x = 0.0;
+                if (r >= rlo && r <= rhi) x = local < nrow ? cs[local] : col[r];
+                dst[o] = x;
             }
         }
     }
