@@ -204,35 +204,52 @@ __device__ __forceinline__ void leaf_of(int comp, int& leaf, int& idx) {
     else { leaf = 6; idx = comp - BX; }
 }
 
+// Reference-layout conversions run one thread per sample of a z row: grid
+// (z blocks, rows, components), blocks striding over the rows, so a thread
+// finds its sample with one 32-bit division per row.  r is the sample's index
+// in the reference layout (x, y, z order of the region).
+constexpr int kRowThreads = 128;
+dim3 row_grid(const Box& B, int ncomp) {
+    const long long rows = (long long)B.n[0] * B.n[1];
+    return dim3((unsigned)((B.n[2] + kRowThreads - 1) / kRowThreads), (unsigned)std::max(1LL, std::min(rows, 65535LL)),
+                (unsigned)ncomp);
+}
+template <typename F>
+__device__ __forceinline__ void for_rows(const Box& B, F f) {
+    const int z = blockIdx.x * blockDim.x + threadIdx.x;
+    if (z >= B.n[2]) return;
+    const int rows = B.n[0] * B.n[1];
+    for (int row = blockIdx.y; row < rows; row += gridDim.y) {
+        const int x = row / B.n[1], y = row - x * B.n[1];
+        const int ix[3] = {B.lo[0] + x, B.lo[1] + y, B.lo[2] + z};
+        f(ix, (long long)row * B.n[2] + z);
+    }
+}
+
 // reference layout (shape S) -> padded block at org
 __global__ void k_import(Leaves in, double* __restrict__ u, Geo G, Box region, long long npts) {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= region.count * NCOMP) return;
-    const int comp = (int)(t / region.count);
-    const long long r = t - (long long)comp * region.count;
-    int ix[3];
-    region.coords(r, ix);
+    const int comp = blockIdx.z;
     int leaf, idx;
     leaf_of(comp, leaf, idx);
-    u[comp * G.cs + lin(G, ix)] = in.f[leaf][idx * npts + r];
+    const double* src = in.f[leaf] + idx * npts;
+    double* dst = u + comp * G.cs;
+    for_rows(region, [&](const int (&ix)[3], long long r) { dst[lin(G, ix)] = src[r]; });
 }
 
 // padded block -> reference layout; symmetric tensors written to both halves
 __global__ void k_export(const double* __restrict__ u, LeavesOut out, Geo G, Box region, long long npts) {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= region.count * NCOMP) return;
-    const int comp = (int)(t / region.count);
-    const long long r = t - (long long)comp * region.count;
-    int ix[3];
-    region.coords(r, ix);
+    const int comp = blockIdx.z;
     int leaf, idx;
     leaf_of(comp, leaf, idx);
-    const double v = u[comp * G.cs + lin(G, ix)];
-    out.f[leaf][idx * npts + r] = v;
-    if (leaf == 0 || leaf == 2) {
-        const int i = idx / 3, j = idx % 3;
-        if (i != j) out.f[leaf][(3 * j + i) * npts + r] = v;
-    }
+    const double* src = u + comp * G.cs;
+    double* dst = out.f[leaf] + idx * npts;
+    const int i = idx / 3, j = idx % 3;
+    double* mirror = ((leaf == 0 || leaf == 2) && i != j) ? out.f[leaf] + (3 * j + i) * npts : nullptr;
+    for_rows(region, [&](const int (&ix)[3], long long r) {
+        const double v = src[lin(G, ix)];
+        dst[r] = v;
+        if (mirror) mirror[r] = v;
+    });
 }
 
 // Matter sources in the reference layout -> a padded block of kMatterComps
@@ -240,23 +257,19 @@ __global__ void k_export(const double* __restrict__ u, LeavesOut out, Geo G, Box
 __global__ void k_import_matter(const double* __restrict__ rho, const double* __restrict__ Si,
                                 const double* __restrict__ Sij, double* __restrict__ m, Geo G, Box region,
                                 long long npts) {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= region.count * kMatterComps) return;
-    const int comp = (int)(t / region.count);
-    const long long r = t - (long long)comp * region.count;
-    int ix[3];
-    region.coords(r, ix);
-    double v;
+    const int comp = blockIdx.z;
+    const double* src;
     if (comp == 0) {
-        v = rho[r];
+        src = rho;
     } else if (comp < 4) {
-        v = Si[(comp - 1) * npts + r];
+        src = Si + (comp - 1) * npts;
     } else {
         constexpr int ij[6][2] = {{0, 0}, {0, 1}, {0, 2}, {1, 1}, {1, 2}, {2, 2}};
         const int s = comp - 4;
-        v = Sij[(3 * ij[s][0] + ij[s][1]) * npts + r];
+        src = Sij + (3 * ij[s][0] + ij[s][1]) * npts;
     }
-    m[comp * G.cs + lin(G, ix)] = v;
+    double* dst = m + comp * G.cs;
+    for_rows(region, [&](const int (&ix)[3], long long r) { dst[lin(G, ix)] = src[r]; });
 }
 
 // Periodic wrap of the array region [lo, lo+n) into every other padded sample
@@ -544,34 +557,28 @@ __device__ __forceinline__ bool in_closure_shell(const Geo& G, const int (&ix)[3
 __global__ void k_import_lower(const double* __restrict__ A, const double* __restrict__ g, double* __restrict__ delta,
                                float* __restrict__ copy, float* __restrict__ other, Geo G, Box region,
                                long long npts) {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= region.count * 6) return;
-    const int k = (int)(t / region.count);
-    const long long r = t - (long long)k * region.count;
-    int ix[3];
-    region.coords(r, ix);
+    const int k = blockIdx.z;
     constexpr int pairs[3][2] = {{0, 1}, {0, 2}, {1, 2}};
     const int i = pairs[k % 3][0], j = pairs[k % 3][1];
     const double* T = k < 3 ? A : g;
-    const double d = in_closure_shell(G, ix) ? T[(3 * j + i) * npts + r] - T[(3 * i + j) * npts + r] : 0.0;
-    const long long q = k * G.cs + lin(G, ix);
-    delta[q] = d;
-    copy[q] = (float)d;    // stage 1 reads it
-    other[q] = 0.0f;       // off the shell, stage values stay zero
+    for_rows(region, [&](const int (&ix)[3], long long r) {
+        const double d = in_closure_shell(G, ix) ? T[(3 * j + i) * npts + r] - T[(3 * i + j) * npts + r] : 0.0;
+        const long long q = k * G.cs + lin(G, ix);
+        delta[q] = d;
+        copy[q] = (float)d;    // stage 1 reads it
+        other[q] = 0.0f;       // off the shell, stage values stay zero
+    });
 }
 
 __global__ void k_export_lower(double* __restrict__ A, double* __restrict__ g, const double* __restrict__ delta,
                                Geo G, Box region, long long npts) {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= region.count * 6) return;
-    const int k = (int)(t / region.count);
-    const long long r = t - (long long)k * region.count;
-    int ix[3];
-    region.coords(r, ix);
+    const int k = blockIdx.z;
     constexpr int pairs[3][2] = {{0, 1}, {0, 2}, {1, 2}};
     const int i = pairs[k % 3][0], j = pairs[k % 3][1];
     double* T = k < 3 ? A : g;
-    T[(3 * j + i) * npts + r] = T[(3 * i + j) * npts + r] + delta[k * G.cs + lin(G, ix)];
+    for_rows(region, [&](const int (&ix)[3], long long r) {
+        T[(3 * j + i) * npts + r] = T[(3 * i + j) * npts + r] + delta[k * G.cs + lin(G, ix)];
+    });
 }
 
 }  // namespace bssn
@@ -682,18 +689,18 @@ int bssn_rhs(const BssnFields* in, BssnFields* out, const int32_t shape[3], cons
     double* k = u + NCOMP * L.cs;
     RhsWork w = carve_rhs_work(k + NCOMP * L.cs, L.cs, with_mom);
     const Box region = box_of(G);
-    BSSN_LAUNCH(KC_IMPORT, k_import, nblocks(region.count * NCOMP), kThreads, s, leaves_in(in), u, G, region, L.npts);
+    BSSN_LAUNCH(KC_IMPORT, k_import, row_grid(region, NCOMP), kRowThreads, s, leaves_in(in), u, G, region, L.npts);
     cudaError_t e = launch_fill_periodic(u, NCOMP, G, s);
     if (e == cudaSuccess && with_matter) {
         double* m = k + (long long)(NCOMP + rhs_work_blocks(with_mom)) * L.cs;
-        BSSN_LAUNCH(KC_IMPORT, k_import_matter, nblocks(region.count * kMatterComps), kThreads, s,
+        BSSN_LAUNCH(KC_IMPORT, k_import_matter, row_grid(region, kMatterComps), kRowThreads, s,
                     matter->energy_density, matter->momentum_density, matter->spatial_stress, m, G, region, L.npts);
         e = launch_fill_periodic(m, kMatterComps, G, s);
         w.mat = m;
     }
     if (e == cudaSuccess) e = launch_rhs(u, k, w, G, region, s);
     if (e == cudaSuccess) {
-        BSSN_LAUNCH(KC_EXPORT, k_export, nblocks(region.count * NCOMP), kThreads, s, k, leaves_out(out), G, region, L.npts);
+        BSSN_LAUNCH(KC_EXPORT, k_export, row_grid(region, NCOMP), kRowThreads, s, k, leaves_out(out), G, region, L.npts);
         e = cudaGetLastError();
     }
     return cuda_status(e, "bssn_rhs");
@@ -734,12 +741,12 @@ int bssn_rk4_step(BssnFields* state, const int32_t shape[3], const BssnParams* p
     lt.stage[0] = lt.acc + 6 * L.cs;
     lt.stage[1] = lt.stage[0] + 6 * L.cs;
     const Box region = box_of(G);
-    BSSN_LAUNCH(KC_IMPORT, k_import, nblocks(region.count * NCOMP), kThreads, s, leaves_in(state), u0, G, region, L.npts);
+    BSSN_LAUNCH(KC_IMPORT, k_import, row_grid(region, NCOMP), kRowThreads, s, leaves_in(state), u0, G, region, L.npts);
     cudaError_t e = cudaGetLastError();
     if (lower && e == cudaSuccess) {
         // delta, its FP32 copy (stage 1's input) and zero stage values over
         // the owned box; stencils reach no padding along closed axes
-        BSSN_LAUNCH(KC_IMPORT, k_import_lower, nblocks(region.count * 6), kThreads, s, state->traceless_K,
+        BSSN_LAUNCH(KC_IMPORT, k_import_lower, row_grid(region, 6), kRowThreads, s, state->traceless_K,
                     state->conformal_metric, lt.delta, lower_triangle_input(lt, 1), lower_triangle_output(lt, 1), G,
                     region, L.npts);
         e = cudaGetLastError();
@@ -750,9 +757,9 @@ int bssn_rk4_step(BssnFields* state, const int32_t shape[3], const BssnParams* p
         if (e == cudaSuccess) e = rk4_step_patch(u0, us, k, acc, w, G, region, true, 0, s, lower ? &lt : nullptr);
     }
     if (e == cudaSuccess) {
-        BSSN_LAUNCH(KC_EXPORT, k_export, nblocks(region.count * NCOMP), kThreads, s, u0, leaves_out(state), G, region, L.npts);
+        BSSN_LAUNCH(KC_EXPORT, k_export, row_grid(region, NCOMP), kRowThreads, s, u0, leaves_out(state), G, region, L.npts);
         if (lower)
-            BSSN_LAUNCH(KC_EXPORT, k_export_lower, nblocks(region.count * 6), kThreads, s, state->traceless_K,
+            BSSN_LAUNCH(KC_EXPORT, k_export_lower, row_grid(region, 6), kRowThreads, s, state->traceless_K,
                         state->conformal_metric, lt.delta, G, region, L.npts);
         e = cudaGetLastError();
     }
@@ -779,7 +786,7 @@ int bssn_constraints(const BssnFields* in, const int32_t shape[3], const BssnPar
     w.d1 = u + NCOMP * L.cs;
     w.der = w.d1 + 3LL * NMIX * L.cs;
     const Box region = box_of(G);
-    BSSN_LAUNCH(KC_IMPORT, k_import, nblocks(region.count * NCOMP), kThreads, s, leaves_in(in), u, G, region, L.npts);
+    BSSN_LAUNCH(KC_IMPORT, k_import, row_grid(region, NCOMP), kRowThreads, s, leaves_in(in), u, G, region, L.npts);
     cudaError_t e = launch_fill_periodic(u, NCOMP, G, s);
     if (e == cudaSuccess)
         e = launch_constraints(u, w, G, region, hamiltonian, momentum, det_gamma, trace_A, gamma_condition, s);
@@ -807,7 +814,7 @@ int bssn_fields_to_components(const BssnFields* in, double* state, const int32_t
         if (extent[d] < 1) return fail(BSSN_ERR_INVALID, "array extents must be positive");
     const Geo G = plain_geo(extent);
     const Box region = full_box(G);
-    BSSN_LAUNCH(KC_IMPORT, k_import, nblocks(region.count * NCOMP), kThreads, (cudaStream_t)stream, leaves_in(in),
+    BSSN_LAUNCH(KC_IMPORT, k_import, row_grid(region, NCOMP), kRowThreads, (cudaStream_t)stream, leaves_in(in),
                 state, G, region, region.count);
     return cuda_status(cudaGetLastError(), "bssn_fields_to_components");
 }
@@ -818,7 +825,7 @@ int bssn_components_to_fields(const double* state, BssnFields* out, const int32_
         if (extent[d] < 1) return fail(BSSN_ERR_INVALID, "array extents must be positive");
     const Geo G = plain_geo(extent);
     const Box region = full_box(G);
-    BSSN_LAUNCH(KC_EXPORT, k_export, nblocks(region.count * NCOMP), kThreads, (cudaStream_t)stream, state,
+    BSSN_LAUNCH(KC_EXPORT, k_export, row_grid(region, NCOMP), kRowThreads, (cudaStream_t)stream, state,
                 leaves_out(out), G, region, region.count);
     return cuda_status(cudaGetLastError(), "bssn_components_to_fields");
 }
@@ -891,7 +898,7 @@ int bssn_batch_import(const BssnFields* in, double* states, const BssnPatch* pat
     Geo G;
     if ((st = batch_geo(patch, ninst, nullptr, G))) return st;
     const Box region = box_of(G);
-    BSSN_LAUNCH(KC_IMPORT, k_import, nblocks(region.count * NCOMP), kThreads, (cudaStream_t)stream, leaves_in(in),
+    BSSN_LAUNCH(KC_IMPORT, k_import, row_grid(region, NCOMP), kRowThreads, (cudaStream_t)stream, leaves_in(in),
                 states + (long long)instance * G.istride, G, region, region.count);
     return cuda_status(cudaGetLastError(), "bssn_batch_import");
 }
@@ -904,7 +911,7 @@ int bssn_batch_export(const double* states, BssnFields* out, const BssnPatch* pa
     Geo G;
     if ((st = batch_geo(patch, ninst, nullptr, G))) return st;
     const Box region = box_of(G);
-    BSSN_LAUNCH(KC_EXPORT, k_export, nblocks(region.count * NCOMP), kThreads, (cudaStream_t)stream,
+    BSSN_LAUNCH(KC_EXPORT, k_export, row_grid(region, NCOMP), kRowThreads, (cudaStream_t)stream,
                 states + (long long)instance * G.istride, leaves_out(out), G, region, region.count);
     return cuda_status(cudaGetLastError(), "bssn_batch_export");
 }
