@@ -686,6 +686,134 @@ k_rhs_gauge_tma(const __grid_constant__ CUtensorMap map, const float* __restrict
 }
 
 // ---------------------------------------------------------------------------
+// FP32 forms, interior first derivatives of the NMIX fields from TMA tiles:
+// the same 32 x 8 x 4 tiles and four z samples per thread as the gauge
+// kernel, halo 2 in x and y (4 in z for the 16-byte rule), a three-deep ring
+// of 40 x 12 x 8 boxes.  The paired form streams each field's low word too
+// (the low words follow the 21 perturbations, so one tensor map of 32
+// components covers both).  Closure-free, no MAD axis, kappa = 0.
+// ---------------------------------------------------------------------------
+namespace tma {
+constexpr int DHZ = TZ + 8, DHY = TY + 4, DHX = TX + 4;        // 40 x 12 x 8
+constexpr int DSY = DHZ, DSX = DHZ * DHY;
+constexpr int DFIELD = DHZ * DHY * DHX;                        // 3840 floats
+constexpr unsigned DFIELD_BYTES = DFIELD * 4;                  // 15360 (a multiple of 128)
+constexpr int DNBUF = 3;
+constexpr size_t DSMEM = (size_t)DNBUF * DFIELD_BYTES + DNBUF * sizeof(unsigned long long);
+static_assert(DFIELD_BYTES % 128 == 0, "tile buffers must stay 128-byte aligned");
+
+__device__ __forceinline__ void load_box(float* dst, const CUtensorMap* map, int z, int y, int x, int inst, int comp,
+                                         unsigned long long* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, %6}], [%7];"
+        ::"r"(smem_addr(dst)), "l"(map), "r"(z), "r"(y), "r"(x), "r"(inst), "r"(comp), "r"(smem_addr(bar))
+        : "memory");
+}
+}  // namespace tma
+
+__global__ void __launch_bounds__(tma::THREADS)
+k_first_derivs_tma(const __grid_constant__ CUtensorMap map, float* __restrict__ d1, Geo G, Box B, int z_base,
+                   int tiles_z, int tiles_y, int nfield, int paired, int* __restrict__ timeouts) {
+    using namespace tma;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    float* ring = reinterpret_cast<float*>(smem_raw);
+    unsigned long long* bars = reinterpret_cast<unsigned long long*>(ring + DNBUF * DFIELD);
+    const int tile = blockIdx.x, inst = blockIdx.y;
+    const int z0 = z_base + TZ * (tile % tiles_z);
+    const int y0 = B.lo[1] + TY * ((tile / tiles_z) % tiles_y);
+    const int x0 = B.lo[0] + TX * (tile / (tiles_z * tiles_y));
+    const int t = threadIdx.x;
+    const int tz4 = t & 7, ty = (t >> 3) & 7, tx = t >> 6;
+    const int x = x0 + tx, y = y0 + ty, zq = z0 + 4 * tz4;
+    const bool col = x >= B.lo[0] && x < B.lo[0] + B.n[0] && y >= B.lo[1] && y < B.lo[1] + B.n[1];
+    // as the generic kernel: the derivative along an axis only where the
+    // sample lies in that axis' compute range (not in the grown box's ghosts)
+    bool write[3][4];
+    bool all[3];
+#pragma unroll
+    for (int dd = 0; dd < 3; ++dd) all[dd] = true;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const bool v = col && zq + j >= B.lo[2] && zq + j < B.lo[2] + B.n[2];
+        const int c3[3] = {x, y, zq + j};
+#pragma unroll
+        for (int dd = 0; dd < 3; ++dd) {
+            write[dd][j] = v && c3[dd] >= G.ax[dd].lo && c3[dd] < G.ax[dd].hi;
+            all[dd] = all[dd] && write[dd][j];
+        }
+    }
+    // tiles: field f's value, then (paired) its low word
+    const int ntile = paired ? 2 * NMIX : NMIX;
+    auto comp_of = [&](int i) { return paired ? ((i & 1) ? NCOMP + (i >> 1) : mix_source(i >> 1)) : mix_source(i); };
+    if (t == 0) {
+        for (int b = 0; b < DNBUF; ++b) bar_init(&bars[b]);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    if (t == 0)
+        for (int i = 0; i < DNBUF && i < ntile; ++i)
+            load_box(ring + i * DFIELD, &map, z0 - 4, y0 - 2, x0 - 2, inst, comp_of(i), &bars[i], DFIELD_BYTES);
+    const long long cs = G.cs;
+    const long long p0 = ((long long)x * G.ax[1].P + y) * G.ax[2].P + zq + (long long)inst * G.istride;
+    const int base = ((tx + 2) * DHY + (ty + 2)) * DHZ + 4 + 4 * tz4;
+    const float a1 = G.gf.d1a, a2 = G.gf.d1b;
+    float acc[3][4];
+    for (int i = 0; i < ntile; ++i) {
+        const int b = i % DNBUF;
+        const int missing = !bar_wait(&bars[b], (unsigned)((i / DNBUF) & 1));
+        if (__syncthreads_or(missing)) {
+            if (t == 0) {
+                atomicAdd(timeouts, 1);
+                for (int g = i; g < i + DNBUF && g < ntile; ++g) bar_wait(&bars[g % DNBUF], (unsigned)((g / DNBUF) & 1));
+            }
+            return;
+        }
+        const float* s = ring + b * DFIELD + base;
+        float d[3][4];
+        {   // z: a 12-sample window
+            const float4 m = ld4(s - 4), c = ld4(s), q = ld4(s + 4);
+            const float w[12] = {m.x, m.y, m.z, m.w, c.x, c.y, c.z, c.w, q.x, q.y, q.z, q.w};
+#pragma unroll
+            for (int j = 0; j < 4; ++j) d[2][j] = (w[5 + j] - w[3 + j]) * a1 + (w[6 + j] - w[2 + j]) * a2;
+        }
+#pragma unroll
+        for (int dd = 0; dd < 2; ++dd) {   // x (0), y (1)
+            const int st = dd == 0 ? DSX : DSY;
+            const float4 m2 = ld4(s - 2 * st), m1 = ld4(s - st), p1 = ld4(s + st), p2 = ld4(s + 2 * st);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) d[dd][j] = (at(p1, j) - at(m1, j)) * a1 + (at(p2, j) - at(m2, j)) * a2;
+        }
+        const bool lo_word = paired && (i & 1);
+#pragma unroll
+        for (int dd = 0; dd < 3; ++dd)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc[dd][j] = lo_word ? acc[dd][j] + d[dd][j] : d[dd][j];
+        if (!paired || lo_word) {
+            const int f = paired ? (i >> 1) : i;
+#pragma unroll
+            for (int dd = 0; dd < 3; ++dd) {
+                float* out = d1 + ((long long)(dd * nfield + f)) * cs + p0;
+                if (all[dd]) {
+                    *reinterpret_cast<float4*>(out) = make_float4(acc[dd][0], acc[dd][1], acc[dd][2], acc[dd][3]);
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 4; ++j)
+                        if (write[dd][j]) out[j] = acc[dd][j];
+                }
+            }
+        }
+        __syncthreads();   // every thread is done with tile b
+        if (t == 0 && i + DNBUF < ntile) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            load_box(ring + b * DFIELD, &map, z0 - 4, y0 - 2, x0 - 2, inst, comp_of(i + DNBUF), &bars[b], DFIELD_BYTES);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // dt K and dt Gt^i
 // ---------------------------------------------------------------------------
 template <typename R, bool Closed>
@@ -1670,6 +1798,9 @@ cudaError_t tma_device(TmaDevice& out) {
     TmaDevice& d = devices[dev];
     if (!d.ready) {
         e = cudaFuncSetAttribute(k_rhs_gauge_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tma::SMEM);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_first_derivs_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)tma::DSMEM);
         if (e == cudaSuccess) e = cudaGetSymbolAddress(reinterpret_cast<void**>(&d.timeouts), g_tma_timeouts);
         if (e != cudaSuccess) return e;
         d.ready = true;
@@ -1732,6 +1863,49 @@ static bool launch_gauge_tma(const float* u, const double* u64, const float* d1,
     return true;
 }
 
+// The interior first derivatives of the FP32 forms from TMA tiles (kappa = 0:
+// the NMIX fields only); false leaves the launch to the generic kernel.
+static bool launch_first_derivs_tma(const float* u, float* d1, const Geo& G, const BoxSet& S, int with_mom,
+                                    cudaStream_t stream) {
+    if (!g_tma_enabled.load() || with_mom || S.n != 1 || G.ninst < 1 || G.ninst > 65535) return false;
+    for (int d = 0; d < 3; ++d)
+        if (G.ax[d].mad || G.ax[d].reduced) return false;
+    if (G.ax[2].P % 4 != 0 || reinterpret_cast<uintptr_t>(u) % 16 != 0 || reinterpret_cast<uintptr_t>(d1) % 16 != 0)
+        return false;
+    const EncodeTiled encode = encode_tiled();
+    if (!encode) return false;
+    TmaDevice dev;
+    if (tma_device(dev) != cudaSuccess) return false;
+    const Box& B = S.b[0];
+    const long long istride = G.istride;
+    // (z, y, x, instance, component): the 21 perturbations and the 11 low words
+    const cuuint64_t dims[5] = {(cuuint64_t)G.ax[2].P, (cuuint64_t)G.ax[1].P, (cuuint64_t)G.ax[0].P,
+                                (cuuint64_t)G.ninst, (cuuint64_t)(NCOMP + NMIX)};
+    const cuuint64_t strides[4] = {(cuuint64_t)G.st[1] * 4, (cuuint64_t)G.st[0] * 4, (cuuint64_t)istride * 4,
+                                   (cuuint64_t)G.cs * 4};
+    const cuuint32_t box[5] = {tma::DHZ, tma::DHY, tma::DHX, 1, 1};
+    const cuuint32_t unit[5] = {1, 1, 1, 1, 1};
+    if (istride * 4 % 16 != 0) return false;
+    CUtensorMap map;
+    if (encode(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 5, const_cast<float*>(u), dims, strides, box, unit,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return false;
+    const int z_base = B.lo[2] & ~3;
+    const int tiles_z = (B.lo[2] + B.n[2] - z_base + tma::TZ - 1) / tma::TZ;
+    const int tiles_y = (B.n[1] + tma::TY - 1) / tma::TY;
+    const int tiles_x = (B.n[0] + tma::TX - 1) / tma::TX;
+    const long long tiles = (long long)tiles_z * tiles_y * tiles_x;
+    if (tiles <= 0 || tiles > 0x7fffffffLL) return false;
+    const int paired = G.precision == kPrecisionF32Paired ? 1 : 0;
+    prof_begin(KC_FIRST, stream);
+    k_first_derivs_tma<<<dim3((unsigned)tiles, (unsigned)G.ninst), tma::THREADS, tma::DSMEM, stream>>>(
+        map, d1, G, B, z_base, tiles_z, tiles_y, NMIX, paired, dev.timeouts);
+    prof_end(KC_FIRST, stream);
+    g_tma_launches.fetch_add(1);
+    return true;
+}
+
 // ---------------------------------------------------------------------------
 // host-side launch sequence of one RHS evaluation: every stencil kernel runs
 // as a closure-free instantiation on the box interior and a general one on
@@ -1785,7 +1959,11 @@ static void launch_rhs_form(const R* u, const double* u64, double* k, R* d1, R* 
         cudaStreamWaitEvent(stb, X->pre, 0);
     }
     BSSN_LAUNCH_SET(KC_FIRST, 1, (k_first_derivs<R, true>), se.shell, stb, u, der, d1, G, se.shell, with_mom);
-    BSSN_LAUNCH_SET(KC_FIRST, 0, (k_first_derivs<R, false>), se.interior, stream, u, der, d1, G, se.interior, with_mom);
+    bool derivs_done = false;
+    if constexpr (kPerturbative<R>) derivs_done = launch_first_derivs_tma(u, d1, G, se.interior, with_mom, stream);
+    if (!derivs_done)
+        BSSN_LAUNCH_SET(KC_FIRST, 0, (k_first_derivs<R, false>), se.interior, stream, u, der, d1, G, se.interior,
+                        with_mom);
     if (X) {
         cudaEventRecord(X->fd, stb);
         cudaStreamWaitEvent(stream, X->fd, 0);
