@@ -268,14 +268,20 @@ int bssn_adjoint_backward(double* adjoint, const BssnPatch* patch, int32_t ninst
 int bssn_tune_patch(double* states, const BssnPatch* patch, int32_t ninst, const BssnParams* params, float margin,
                     void* workspace, size_t workspace_bytes, char* report, size_t report_bytes, void* stream);
 
-/* No reference counterpart: the FP32 forms' gauge RHS (dt gt, W, alpha,
- * beta) runs on the box interior from TMA-staged shared-memory tiles where
- * the geometry allows it -- one instance, a z pitch (nz + 2 ghost) that is a
- * multiple of four, no MAD axis -- and from the generic kernel elsewhere.
- * enabled != 0 (the default) keeps that; 0 uses the generic kernel everywhere
- * (results agree to float rounding).  Process-wide; affects later launches
- * and captures. */
-int bssn_set_tma(int32_t enabled);
+/* No reference counterpart: the float forms' TMA-staged kernels.  On the box
+ * interior, where the geometry allows it -- a z pitch (nz + 2 ghost) that is a
+ * multiple of four, no MAD axis (and kappa = 0 for the derivatives) -- the
+ * gauge RHS (dt gt, W, alpha, beta; BSSN_TMA_GAUGE) and the first derivatives
+ * (BSSN_TMA_DERIVS) can run from TMA-staged shared-memory tiles instead of
+ * the generic kernels.  `kernels` is the mask of those to use (default
+ * BSSN_TMA_DERIVS: the gauge kernel is faster alone but slows the whole RHS,
+ * whose other kernels it crowds out; 0: the generic kernels everywhere);
+ * results agree to float rounding.  Process-wide; affects later launches and
+ * captures. */
+#define BSSN_TMA_GAUGE 1
+#define BSSN_TMA_DERIVS 2
+#define BSSN_TMA_ALL 3
+int bssn_set_tma(int32_t kernels);
 
 /* TMA kernel status: *timeouts receives the number of tile waits on the
  * current device that gave up since the last call (each leaves its tile's RHS

@@ -315,9 +315,15 @@ def tune_launch_shapes(state_ptr: int, shape, instances: int, cparams: BssnParam
     return report.value.decode()
 
 
-def set_tma(enabled: bool) -> None:
-    """TMA-staged gauge kernel of the FP32 forms on (default) or off (bssn_set_tma)."""
-    check(load().bssn_set_tma(1 if enabled else 0), "bssn_set_tma")
+TMA_GAUGE, TMA_DERIVS, TMA_ALL = 1, 2, 3
+
+
+def set_tma(kernels) -> None:
+    """The float forms' TMA-staged kernels to use (bssn_set_tma): True or
+    TMA_ALL, False or 0, or a mask of TMA_GAUGE and TMA_DERIVS (the library's
+    default is TMA_DERIVS)."""
+    mask = TMA_ALL if kernels is True else (0 if kernels is False else int(kernels))
+    check(load().bssn_set_tma(mask), "bssn_set_tma")
 
 
 def tma_status() -> tuple:

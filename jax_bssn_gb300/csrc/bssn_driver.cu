@@ -1025,8 +1025,9 @@ int bssn_tune_patch(double* states, const BssnPatch* patch, int32_t ninst, const
     return cuda_status(e, "bssn_tune_patch");
 }
 
-int bssn_set_tma(int32_t enabled) {
-    set_tma_enabled(enabled != 0);
+int bssn_set_tma(int32_t kernels) {
+    if (kernels < 0 || kernels > BSSN_TMA_ALL) return fail(BSSN_ERR_INVALID, "kernels must be a mask of BSSN_TMA_*");
+    set_tma_kernels(kernels);
     return BSSN_OK;
 }
 

@@ -65,10 +65,12 @@ inline float* lower_triangle_output(const LowerTriangle& lt, int stage) {
     return lt.stage[(stage == 1 || stage == 3) ? 0 : 1];
 }
 
-// The FP32 form's TMA gauge kernel: on (the default) wherever its geometry
-// allows, or off (the generic kernel everywhere); the number of its tile
-// waits that gave up since the last read, reset by reading.
-void set_tma_enabled(bool on);
+// The float forms' TMA kernels, by bit (kTmaGauge, kTmaDerivs): each runs
+// wherever its geometry allows when its bit is set (the derivatives by
+// default), else the generic kernel; the number of tile waits that gave up
+// since the last read, reset by reading; the TMA launches so far.
+constexpr int kTmaGauge = 1, kTmaDerivs = 2, kTmaAll = 3;
+void set_tma_kernels(int mask);
 cudaError_t tma_timeouts(int* count);
 long long tma_launches();
 

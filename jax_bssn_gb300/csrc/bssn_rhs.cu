@@ -1779,7 +1779,11 @@ EncodeTiled encode_tiled() {
     }();
     return fn;
 }
-std::atomic<bool> g_tma_enabled{true};
+// default: the derivatives only.  The gauge kernel is faster alone (206 vs
+// 276 us at 128^3) but runs beside the main stream's kernels, and its 90 KB
+// of shared memory per CTA crowds them out: the FP32 step took 9.55 ms with
+// it against 9.42 without (9.34 with the derivatives only).
+std::atomic<int> g_tma_mask{kTmaDerivs};
 std::atomic<long long> g_tma_launches{0};
 __device__ int g_tma_timeouts;
 
@@ -1810,7 +1814,7 @@ cudaError_t tma_device(TmaDevice& out) {
 }
 }  // namespace
 
-void set_tma_enabled(bool on) { g_tma_enabled.store(on); }
+void set_tma_kernels(int mask) { g_tma_mask.store(mask & kTmaAll); }
 
 long long tma_launches() { return g_tma_launches.load(); }
 
@@ -1825,7 +1829,7 @@ cudaError_t tma_timeouts(int* count) {
 // allows it; false leaves the launch to the generic kernel.
 static bool launch_gauge_tma(const float* u, const double* u64, const float* d1, double* k, const Geo& G,
                              const BoxSet& S, int nfield, cudaStream_t stream) {
-    if (!g_tma_enabled.load() || S.n != 1 || G.ninst < 1 || G.ninst > 65535) return false;
+    if (!(g_tma_mask.load() & kTmaGauge) || S.n != 1 || G.ninst < 1 || G.ninst > 65535) return false;
     for (int d = 0; d < 3; ++d)
         if (G.ax[d].mad || G.ax[d].reduced) return false;
     if (G.ax[2].P % 4 != 0 || reinterpret_cast<uintptr_t>(u) % 16 != 0) return false;
@@ -1867,7 +1871,7 @@ static bool launch_gauge_tma(const float* u, const double* u64, const float* d1,
 // the NMIX fields only); false leaves the launch to the generic kernel.
 static bool launch_first_derivs_tma(const float* u, float* d1, const Geo& G, const BoxSet& S, int with_mom,
                                     cudaStream_t stream) {
-    if (!g_tma_enabled.load() || with_mom || S.n != 1 || G.ninst < 1 || G.ninst > 65535) return false;
+    if (!(g_tma_mask.load() & kTmaDerivs) || with_mom || S.n != 1 || G.ninst < 1 || G.ninst > 65535) return false;
     for (int d = 0; d < 3; ++d)
         if (G.ax[d].mad || G.ax[d].reduced) return false;
     if (G.ax[2].P % 4 != 0 || reinterpret_cast<uintptr_t>(u) % 16 != 0 || reinterpret_cast<uintptr_t>(d1) % 16 != 0)

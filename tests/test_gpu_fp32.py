@@ -234,13 +234,14 @@ def test_tma_kernels_match_the_generic_kernels(gb, form, faces):
     params = pkg.BSSNParameters(**kw)
     _, before = _native.tma_status()
     with pkg.arithmetic(form):
-        tiled = te.compute_bssn_rhs(state, params)
-        _, after = _native.tma_status()
-        _native.set_tma(False)
         try:
+            _native.set_tma(_native.TMA_ALL)
+            tiled = te.compute_bssn_rhs(state, params)
+            _, after = _native.tma_status()
+            _native.set_tma(False)
             generic = te.compute_bssn_rhs(state, params)
         finally:
-            _native.set_tma(True)
+            _native.set_tma(_native.TMA_DERIVS)   # the library's default
     timeouts, last = _native.tma_status()
     assert after == before + 2 and last == after, (before, after, last)   # both kernels tiled, then neither
     assert timeouts == 0
