@@ -1103,7 +1103,7 @@ def run_gb300(args, world, rank, local):
                     ("adjoint", run_adjoint, dict(steps=1, warmup=1, adjoint_steps=20, adjoint_fd=1, no_e2e=True)),
                     ("batch", run_batch, dict(steps=5, warmup=2)),
                     ("puncture", run_puncture, dict(steps=3, warmup=1)),
-                    ("horizon", run_horizon, dict(steps=3, warmup=1))):
+                    ("horizon", run_horizon, dict(steps=5, warmup=2))):
                 sub = argparse.Namespace(**vars(args))
                 sub.workload, sub.n, sub.no_cpu = name, None, True
                 for key, val in over.items():
