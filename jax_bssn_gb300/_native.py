@@ -319,10 +319,10 @@ TMA_GAUGE, TMA_DERIVS, TMA_ALL = 1, 2, 3
 
 
 def set_tma(kernels) -> None:
-    """The float forms' TMA-staged kernels to use (bssn_set_tma): True or
-    TMA_ALL, False or 0, or a mask of TMA_GAUGE and TMA_DERIVS (the library's
-    default is TMA_DERIVS)."""
-    mask = TMA_ALL if kernels is True else (0 if kernels is False else int(kernels))
+    """The float forms' TMA-staged kernels to use (bssn_set_tma): a mask of
+    TMA_GAUGE and TMA_DERIVS; True is the library's default (TMA_DERIVS) and
+    False the generic kernels everywhere."""
+    mask = TMA_DERIVS if kernels is True else (0 if kernels is False else int(kernels))
     check(load().bssn_set_tma(mask), "bssn_set_tma")
 
 
