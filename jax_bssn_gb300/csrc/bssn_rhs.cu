@@ -2100,11 +2100,12 @@ k_lower_triangle(const double* __restrict__ u, const double* __restrict__ d1, co
     const int i = pairs[k][0], j = pairs[k][1];
     const float* fa = din + k * cs + p;          // dA_ij stage values
     const float* fg = din + (3 + k) * cs + p;    // dg_ij stage values
-    bool face = false;
+    bool face = false, row1 = false;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         const Axis& a = G.ax[d];
         face = face || (a.slo && c.ix[d] == a.start) || (a.shi && c.ix[d] == a.end - 1);
+        row1 = row1 || (a.lbc && c.ix[d] == a.start + 1) || (a.rbc && c.ix[d] == a.end - 2);
     }
     float ra, rg;
     if (face) {
@@ -2123,12 +2124,18 @@ k_lower_triangle(const double* __restrict__ u, const double* __restrict__ d1, co
         rg = -(radial_g + fg[0]) / rs;
     } else {
         const double W = u[CW * cs + p], al = u[CALPHA * cs + p];
-        // the commuted Hessians' difference (the source), as the reference rounds it
-        const double wu = D1<double, true>(d1ptr(d1, G, nfield, i, MIX_W, p), G, j, c.ix[j]);
-        const double wl = D1<double, true>(d1ptr(d1, G, nfield, j, MIX_W, p), G, i, c.ix[i]);
-        const double au = D1<double, true>(d1ptr(d1, G, nfield, i, MIX_ALPHA, p), G, j, c.ix[j]);
-        const double al_ = D1<double, true>(d1ptr(d1, G, nfield, j, MIX_ALPHA, p), G, i, c.ix[i]);
-        const float src = (float)(al * W * (wl - wu) - W * W * (al_ - au));
+        // the commuted Hessians' difference (the source), as the reference
+        // rounds it: on the second row from a face, where the inner
+        // derivative's one-sided closure acts (further in, both orderings use
+        // centred stencils and the difference is below 1e-20)
+        float src = 0.0f;
+        if (row1) {
+            const double wu = D1<double, true>(d1ptr(d1, G, nfield, i, MIX_W, p), G, j, c.ix[j]);
+            const double wl = D1<double, true>(d1ptr(d1, G, nfield, j, MIX_W, p), G, i, c.ix[i]);
+            const double au = D1<double, true>(d1ptr(d1, G, nfield, i, MIX_ALPHA, p), G, j, c.ix[j]);
+            const double al_ = D1<double, true>(d1ptr(d1, G, nfield, j, MIX_ALPHA, p), G, i, c.ix[i]);
+            src = (float)(al * W * (wl - wu) - W * W * (al_ - au));
+        }
         float beta[3], bs[3], g[6], gi[6];
 #pragma unroll
         for (int s6 = 0; s6 < 6; ++s6) g[s6] = (float)u[(GXX + s6) * cs + p];
