@@ -270,17 +270,21 @@ int bssn_tune_patch(double* states, const BssnPatch* patch, int32_t ninst, const
 
 /* No reference counterpart: the float forms' TMA-staged kernels.  On the box
  * interior, where the geometry allows it -- a z pitch (nz + 2 ghost) that is a
- * multiple of four, no MAD axis (and kappa = 0 for the derivatives) -- the
- * gauge RHS (dt gt, W, alpha, beta; BSSN_TMA_GAUGE) and the first derivatives
- * (BSSN_TMA_DERIVS) can run from TMA-staged shared-memory tiles instead of
- * the generic kernels.  `kernels` is the mask of those to use (default
- * BSSN_TMA_DERIVS: the gauge kernel is faster alone but slows the whole RHS,
- * whose other kernels it crowds out; 0: the generic kernels everywhere);
- * results agree to float rounding.  Process-wide; affects later launches and
- * captures. */
+ * multiple of four, no MAD axis, kappa = 0 for all but the gauge RHS, vacuum
+ * for the curvature RHS -- the gauge RHS (dt gt, W, alpha, beta;
+ * BSSN_TMA_GAUGE), the first derivatives (BSSN_TMA_DERIVS), dt At
+ * (BSSN_TMA_AT) and dt K with dt Gt (BSSN_TMA_KGT) can run from TMA-staged
+ * shared-memory tiles instead of the generic kernels.  `kernels` is the mask
+ * of those to use (default BSSN_TMA_DERIVS | BSSN_TMA_AT | BSSN_TMA_KGT: the
+ * gauge kernel is faster alone but slows the whole RHS, whose other kernels
+ * it crowds out; 0: the generic kernels everywhere); results agree to float
+ * rounding.
+ * Process-wide; affects later launches and captures. */
 #define BSSN_TMA_GAUGE 1
 #define BSSN_TMA_DERIVS 2
-#define BSSN_TMA_ALL 3
+#define BSSN_TMA_AT 4
+#define BSSN_TMA_KGT 8
+#define BSSN_TMA_ALL 15
 int bssn_set_tma(int32_t kernels);
 
 /* TMA kernel status: *timeouts receives the number of tile waits on the

@@ -315,14 +315,15 @@ def tune_launch_shapes(state_ptr: int, shape, instances: int, cparams: BssnParam
     return report.value.decode()
 
 
-TMA_GAUGE, TMA_DERIVS, TMA_ALL = 1, 2, 3
+TMA_GAUGE, TMA_DERIVS, TMA_AT, TMA_KGT, TMA_ALL = 1, 2, 4, 8, 15
+TMA_DEFAULT = TMA_DERIVS | TMA_AT | TMA_KGT
 
 
 def set_tma(kernels) -> None:
     """The float forms' TMA-staged kernels to use (bssn_set_tma): a mask of
-    TMA_GAUGE and TMA_DERIVS; True is the library's default (TMA_DERIVS) and
-    False the generic kernels everywhere."""
-    mask = TMA_DERIVS if kernels is True else (0 if kernels is False else int(kernels))
+    TMA_GAUGE, TMA_DERIVS, TMA_AT and TMA_KGT; True is the library's default
+    (TMA_DEFAULT) and False the generic kernels everywhere."""
+    mask = TMA_DEFAULT if kernels is True else (0 if kernels is False else int(kernels))
     check(load().bssn_set_tma(mask), "bssn_set_tma")
 
 

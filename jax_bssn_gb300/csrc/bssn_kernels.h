@@ -65,11 +65,11 @@ inline float* lower_triangle_output(const LowerTriangle& lt, int stage) {
     return lt.stage[(stage == 1 || stage == 3) ? 0 : 1];
 }
 
-// The float forms' TMA kernels, by bit (kTmaGauge, kTmaDerivs): each runs
+// The float forms' TMA kernels, by bit (kTmaGauge, kTmaDerivs, kTmaAt, kTmaKgt): each runs
 // wherever its geometry allows when its bit is set (the derivatives by
 // default), else the generic kernel; the number of tile waits that gave up
 // since the last read, reset by reading; the TMA launches so far.
-constexpr int kTmaGauge = 1, kTmaDerivs = 2, kTmaAll = 3;
+constexpr int kTmaGauge = 1, kTmaDerivs = 2, kTmaAt = 4, kTmaKgt = 8, kTmaAll = 15;
 void set_tma_kernels(int mask);
 cudaError_t tma_timeouts(int* count);
 long long tma_launches();

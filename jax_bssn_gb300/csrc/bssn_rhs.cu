@@ -814,6 +814,590 @@ k_first_derivs_tma(const __grid_constant__ CUtensorMap map, float* __restrict__ 
 }
 
 // ---------------------------------------------------------------------------
+// FP32 forms, interior curvature RHS from TMA tiles.  The generic float
+// kernels k_rhs_at and k_rhs_kgt spend their issue slots on the address
+// arithmetic and latency of several hundred scalar stencil taps per point.
+// Here a CTA of 512 threads owns a 32 (z) x 4 (y) x 4 (x) tile, one sample
+// per thread, and streams every stencilled input through a four-deep ring of
+// shared-memory boxes, each one cp.async.bulk.tensor load completing on an
+// mbarrier:
+//   a field's Hessian  value box, halo 2: the pure second derivatives (the
+//                      paired form adds its low word's from a second box);
+//                      boxes of its stored first derivatives along x and y,
+//                      halo 2 along the outer axis only: d_y d_x, d_z d_x and
+//                      d_z d_y;
+//   Gt^i (dt At)       value box, halo 2: its first derivatives;
+//   At_ij, K, Gt^i     value box, halo 3: upwind advection and dissipation
+//                      (and K's first derivatives).
+// The RHS is linear in every one of these, so each box is folded into a few
+// accumulators as soon as it is read; the pointwise terms are formed from
+// single-sample reads while the first boxes load and wait in shared memory.
+// Same terms as the generic kernels' interior instantiation (closure-free, no
+// MAD axis, kappa = 0, vacuum), regrouped.
+// ---------------------------------------------------------------------------
+namespace tma {
+constexpr int AZ = 32, AY = 4, AX = 4;                    // tile; one sample per thread
+constexpr int A_THREADS = AZ * AY * AX;                   // 512
+constexpr int AHZ = AZ + 8;                               // z halo 4 keeps the origin on 16 bytes
+constexpr int ANBUF = 4;
+enum CurvBox { kBoxV2 = 0, kBoxDX = 1, kBoxDY = 2, kBoxV3 = 3 };
+__host__ __device__ constexpr int a_hy(int kind) { return kind == kBoxV3 ? AY + 6 : (kind == kBoxDY ? AY : AY + 4); }
+__host__ __device__ constexpr int a_hx(int kind) { return kind == kBoxV3 ? AX + 6 : (kind == kBoxV2 ? AX + 4 : AX); }
+__host__ __device__ constexpr unsigned a_bytes(int kind) { return 4u * AHZ * a_hy(kind) * a_hx(kind); }
+constexpr unsigned A_SLOT = a_bytes(kBoxV3);              // 16000 bytes, the largest box
+// the ring, nq pointwise terms per sample, the ring's barriers
+__host__ __device__ constexpr size_t curv_smem(int nq) {
+    return (size_t)ANBUF * A_SLOT + (size_t)nq * A_THREADS * 4 + ANBUF * sizeof(unsigned long long);
+}
+constexpr int AT_NQ = 6, KGT_NQ = 4;
+static_assert(A_SLOT % 128 == 0, "ring slots must stay 128-byte aligned");
+static_assert(a_bytes(kBoxV2) % 16 == 0 && a_bytes(kBoxDX) % 16 == 0 && a_bytes(kBoxDY) % 16 == 0,
+              "box sizes are multiples of 16 bytes");
+// The boxes' tensor maps, by CurvBox: the FP32 state (components 0..NCOMP-1
+// and the low words after them) with halo 2 and 3, and the first-derivative
+// buffer with the d_x and the d_y box.
+struct CurvMaps {
+    CUtensorMap map[4];
+};
+struct CurvTile {
+    int kind, comp;
+};
+// Box r of the Hessian group of stored field f: the value box, (paired) the
+// low word's, the d_x box, the d_y box.
+__device__ __forceinline__ CurvTile hessian_tile(int f, int r, int paired, int nfield) {
+    if (r == 0) return {kBoxV2, mix_source(f)};
+    if (paired && r == 1) return {kBoxV2, NCOMP + f};
+    return (r - paired == 1) ? CurvTile{kBoxDX, f} : CurvTile{kBoxDY, nfield + f};
+}
+enum CurvSeq { kSeqAt = 0, kSeqKgt = 1 };
+__host__ __device__ constexpr int seq_tiles(int seq, int paired) {
+    return seq == kSeqAt ? 33 + 8 * paired : 16 + 4 * paired;
+}
+// Box i of a kernel's fixed sequence.
+//   dt At:       Hessian groups of gt_ij, W and alpha (stored fields 0..7),
+//                the three Gt^i value boxes, the six At_ij halo-3 boxes;
+//   dt K, Gt^i:  Hessian groups of alpha and beta^i (stored fields 7..10),
+//                K's and the three Gt^i's halo-3 boxes.
+template <int Seq>
+__device__ __forceinline__ CurvTile seq_tile(int i, int paired, int nfield) {
+    const int gsz = 3 + paired;
+    if constexpr (Seq == kSeqAt) {
+        if (i < 8 * gsz) return hessian_tile(i / gsz, i % gsz, paired, nfield);
+        i -= 8 * gsz;
+        if (i < 3) return {kBoxV2, GTX + i};
+        return {kBoxV3, AXX + (i - 3)};
+    } else {
+        if (i < 4 * gsz) return hessian_tile(MIX_ALPHA + i / gsz, i % gsz, paired, nfield);
+        i -= 4 * gsz;
+        return {kBoxV3, i == 0 ? CK : GTX + (i - 1)};
+    }
+}
+// Fourth-order centred numerators from a shared-memory box at compile-time strides.
+__device__ __forceinline__ float d2_box(const float* s, int st) {   // units of 1/(12 dx^2)
+    const float f0 = s[0];
+    return 16.0f * ((s[st] - f0) + (s[-st] - f0)) - ((s[2 * st] - f0) + (s[-2 * st] - f0));
+}
+__device__ __forceinline__ float d1_box(const float* s, int st, float a1, float a2) {
+    return (s[st] - s[-st]) * a1 + (s[2 * st] - s[-2 * st]) * a2;
+}
+// Shared-memory strides and this thread's centre in each box kind.
+constexpr int V2X = AHZ * (AY + 4), V3X = AHZ * (AY + 6), SYB = AHZ;
+
+// The ring of one CTA: box ti is taken (its wait may give up: `missing`),
+// read, and given back, after which its slot loads box ti + ANBUF.  give()
+// is the CTA's one barrier per box; when any wait of the CTA gave up, the
+// copies in flight get one more bounded wait and give() returns false, and
+// the CTA leaves.
+template <int Seq>
+struct BoxRing {
+    const CurvMaps* maps;
+    float* ring;
+    unsigned long long* bars;
+    int* timeouts;
+    int ntile, paired, nfield, z0, y0, x0, inst, t;
+    int cV2, cDX, cDY, cV3;
+    int ti;
+    bool missing;
+
+    __device__ __forceinline__ void issue(int i) {
+        const CurvTile tl = seq_tile<Seq>(i, paired, nfield);
+        const int b = i % ANBUF;
+        load_box(ring + b * (A_SLOT / 4), &maps->map[tl.kind], z0 - 4, y0 - (a_hy(tl.kind) - AY) / 2,
+                 x0 - (a_hx(tl.kind) - AX) / 2, inst, tl.comp, &bars[b], a_bytes(tl.kind));
+    }
+    __device__ __forceinline__ void start(int tz, int ty, int tx) {
+        cV2 = ((tx + 2) * (AY + 4) + (ty + 2)) * AHZ + 4 + tz;
+        cDX = (tx * (AY + 4) + (ty + 2)) * AHZ + 4 + tz;
+        cDY = (tx * AY + ty) * AHZ + 4 + tz;
+        cV3 = ((tx + 3) * (AY + 6) + (ty + 3)) * AHZ + 4 + tz;
+        ti = 0;
+        missing = false;
+        if (t == 0) {
+            for (int b = 0; b < ANBUF; ++b) bar_init(&bars[b]);
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        }
+        __syncthreads();
+        if (t == 0)
+            for (int i = 0; i < ANBUF && i < ntile; ++i) issue(i);
+    }
+    __device__ __forceinline__ const float* take() {
+        const int b = ti % ANBUF;
+        missing = missing || !bar_wait(&bars[b], (unsigned)((ti / ANBUF) & 1));
+        return ring + b * (A_SLOT / 4);
+    }
+    __device__ __forceinline__ bool give() {
+        if (__syncthreads_or(missing)) {
+            if (t == 0) {
+                atomicAdd(timeouts, 1);
+                for (int i = ti; i < ti + ANBUF && i < ntile; ++i) bar_wait(&bars[i % ANBUF], (unsigned)((i / ANBUF) & 1));
+            }
+            return false;
+        }
+        if (t == 0 && ti + ANBUF < ntile) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue(ti + ANBUF);
+        }
+        ++ti;
+        return true;
+    }
+    // The Hessian h[sym(i,j)] = d_i d_j f of the next Hessian group.
+    __device__ __forceinline__ bool hessian(float (&h)[6], float i12, float a1, float a2) {
+        const float* v = take() + cV2;
+        float n0 = d2_box(v, V2X), n3 = d2_box(v, SYB), n5 = d2_box(v, 1);
+        if (!give()) return false;
+        if (paired) {
+            v = take() + cV2;
+            n0 += d2_box(v, V2X);
+            n3 += d2_box(v, SYB);
+            n5 += d2_box(v, 1);
+            if (!give()) return false;
+        }
+        h[0] = n0 * i12;
+        h[3] = n3 * i12;
+        h[5] = n5 * i12;
+        v = take() + cDX;
+        h[1] = d1_box(v, SYB, a1, a2);
+        h[2] = d1_box(v, 1, a1, a2);
+        if (!give()) return false;
+        v = take() + cDY;
+        h[4] = d1_box(v, 1, a1, a2);
+        return give();
+    }
+    // Advection (upwind by the sign of beta) and the summed sixth-difference
+    // numerators of the next halo-3 box, with its first derivatives when asked.
+    __device__ __forceinline__ bool transport(const float (&beta)[3], float inv12, float& adv, float& dis,
+                                              float* d1out = nullptr, float a1 = 0.0f, float a2 = 0.0f) {
+        const float* v = take() + cV3;
+        float ad[3], di[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const int st = d == 0 ? V3X : (d == 1 ? SYB : 1);
+            float a[7];
+#pragma unroll
+            for (int o = 0; o < 7; ++o) a[o] = v[(o - 3) * st];
+            ad[d] = beta[d] * inv12 * up1(a, beta[d]);
+            di[d] = ko(a);
+            if (d1out) d1out[d] = (a[4] - a[2]) * a1 + (a[5] - a[1]) * a2;
+        }
+        adv = (ad[0] + ad[1]) + ad[2];
+        dis = (di[0] + di[1]) + di[2];
+        return give();
+    }
+};
+}  // namespace tma
+
+// dt At_ij = TF[S_ij + alpha W gt_ij (gt^mn d_m d_n W)] + Q_ij + adv + KO, with
+//   S_ij = alpha W^2 (-1/2 gt^mn d_m d_n gt_ij + gt_k(i d_j) Gt^k)
+//          + alpha W d_i d_j W - W^2 d_i d_j alpha,
+// TF the trace-free part and Q the pointwise terms (Christoffel products, the
+// first-derivative parts of the W and lapse Hessians, At algebra and Lie
+// terms; JAX_BSSN/bssn/extrinsic_curvature.py:119-224, geometry.py:21-186).
+__global__ void __launch_bounds__(tma::A_THREADS, 2)
+k_rhs_at_tma(const __grid_constant__ tma::CurvMaps maps, const float* __restrict__ u, const double* __restrict__ u64,
+             const float* __restrict__ d1, double* __restrict__ k, Geo G, Box B, int z_base, int tiles_z, int tiles_y,
+             int nfield, int paired, int* __restrict__ timeouts) {
+    using namespace tma;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    float* ring = reinterpret_cast<float*>(smem_raw);
+    float* qbuf = ring + ANBUF * (A_SLOT / 4);   // [AT_NQ][A_THREADS]
+    const int tile = blockIdx.x, inst = blockIdx.y;
+    const int z0 = z_base + AZ * (tile % tiles_z);
+    const int y0 = B.lo[1] + AY * ((tile / tiles_z) % tiles_y);
+    const int x0 = B.lo[0] + AX * (tile / (tiles_z * tiles_y));
+    const int t = threadIdx.x;
+    const int tz = t & 31, ty = (t >> 5) & 3, tx = t >> 7;
+    const int x = x0 + tx, y = y0 + ty, z = z0 + tz;
+    const bool valid = x < B.lo[0] + B.n[0] && y < B.lo[1] + B.n[1] && z >= B.lo[2] && z < B.lo[2] + B.n[2];
+    BoxRing<kSeqAt> R;
+    R.maps = &maps;
+    R.ring = ring;
+    R.bars = reinterpret_cast<unsigned long long*>(qbuf + AT_NQ * A_THREADS);
+    R.timeouts = timeouts;
+    R.ntile = seq_tiles(kSeqAt, paired);
+    R.paired = paired;
+    R.nfield = nfield;
+    R.z0 = z0;
+    R.y0 = y0;
+    R.x0 = x0;
+    R.inst = inst;
+    R.t = t;
+    R.start(tz, ty, tx);
+
+    // ---- pointwise terms, while the first boxes load ----
+    const long long cs = G.cs;
+    const long long p = ((long long)x * G.ax[1].P + y) * G.ax[2].P + z + (long long)inst * G.istride;
+    float g[6] = {1.0f, 0.0f, 0.0f, 1.0f, 0.0f, 1.0f}, gi[6] = {1.0f, 0.0f, 0.0f, 1.0f, 0.0f, 1.0f};
+    float W = 1.0f, alpha = 1.0f;
+    if (valid) {
+#pragma unroll
+        for (int s = 0; s < 6; ++s) g[s] = u[(GXX + s) * cs + p] + (unit_diagonal(s) ? 1.0f : 0.0f);
+        inverse_metric(g, gi);
+        W = static_cast<float>(u64[CW * cs + p]);
+        alpha = static_cast<float>(u64[CALPHA * cs + p]);
+        const float aW = alpha * W, W2 = W * W, aW2 = aW * W;
+        float PT[6];   // pointwise part of [alpha W^2 R_ij - W^2 D_i D_j alpha]
+        {
+            float c1[3][6], c2[3][6];
+            {
+                float dg[3][6];
+#pragma unroll
+                for (int kk = 0; kk < 3; ++kk)
+#pragma unroll
+                    for (int s = 0; s < 6; ++s) dg[kk][s] = d1[((long long)(kk * nfield + MIX_G + s)) * cs + p];
+                christoffel(dg, gi, c1, c2);
+            }
+            {   // 1/2 Gt^m d_m gt_ij = 1/2 Gt^m (Gamma_ijm + Gamma_jim)
+                const float Gt[3] = {u[GTX * cs + p], u[GTY * cs + p], u[GTZ * cs + p]};
+#pragma unroll
+                for (int i = 0; i < 3; ++i)
+#pragma unroll
+                    for (int j = i; j < 3; ++j) {
+                        float t3 = 0.0f;
+#pragma unroll
+                        for (int m = 0; m < 3; ++m) t3 += Gt[m] * (c1[i][sym(j, m)] + c1[j][sym(i, m)]);
+                        PT[sym(i, j)] = 0.5f * t3;
+                    }
+            }
+            // the Christoffel products (term4 + term5 of the conformal Ricci tensor)
+#pragma unroll
+            for (int kk = 0; kk < 3; ++kk) {
+                float X[3][3];
+#pragma unroll
+                for (int a = 0; a < 3; ++a)
+#pragma unroll
+                    for (int b = 0; b < 3; ++b)
+                        X[a][b] = gi[sym(0, a)] * c2[kk][sym(0, b)] + gi[sym(1, a)] * c2[kk][sym(1, b)]
+                                  + gi[sym(2, a)] * c2[kk][sym(2, b)];
+#pragma unroll
+                for (int i = 0; i < 3; ++i)
+#pragma unroll
+                    for (int j = i; j < 3; ++j) {
+                        float acc = PT[sym(i, j)];
+#pragma unroll
+                        for (int n = 0; n < 3; ++n)
+                            acc += X[n][i] * (c1[j][sym(kk, n)] + c1[kk][sym(j, n)]) + X[n][j] * c1[i][sym(kk, n)];
+                        PT[sym(i, j)] = acc;
+                    }
+            }
+            float dW[3], da[3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                dW[d] = d1[((long long)(d * nfield + MIX_W)) * cs + p];
+                da[d] = d1[((long long)(d * nfield + MIX_ALPHA)) * cs + p];
+            }
+            float grad2 = 0.0f, gw = 0.0f;   // gt^mn d_m W d_n W, gt^mn d_m W d_n alpha
+#pragma unroll
+            for (int n = 0; n < 3; ++n) {
+                const float gdw = gi[sym(0, n)] * dW[0] + gi[sym(1, n)] * dW[1] + gi[sym(2, n)] * dW[2];
+                grad2 += gdw * dW[n];
+                gw += gdw * da[n];
+            }
+            float cW[6], cA[6];   // Gamma^m_ij d_m W, Gamma^m_ij d_m alpha
+#pragma unroll
+            for (int s = 0; s < 6; ++s) {
+                cW[s] = c2[0][s] * dW[0] + c2[1][s] * dW[1] + c2[2][s] * dW[2];
+                cA[s] = c2[0][s] * da[0] + c2[1][s] * da[1] + c2[2][s] * da[2];
+            }
+            const float gicW = contract_sym(gi, cW);
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = i; j < 3; ++j) {
+                    const int s = sym(i, j);
+                    const float grad = dW[i] * da[j] + dW[j] * da[i] - g[s] * gw;
+                    PT[s] = (aW2 * PT[s] - aW * (cW[s] + g[s] * gicW)) - 2.0f * alpha * g[s] * grad2
+                            + (W2 * cA[s] - W * grad);
+                }
+        }
+        const float trP = contract_sym(gi, PT);
+        // alpha K At_ij - 2 alpha At_ik gt^kl At_lj + Lie terms - 2/3 At_ij div beta
+        const float K = static_cast<float>(u64[CK * cs + p]);
+        float A[6];
+#pragma unroll
+        for (int s = 0; s < 6; ++s) A[s] = u[(AXX + s) * cs + p];
+        float db[3][3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) db[i][j] = d1[((long long)(j * nfield + MIX_B + i)) * cs + p];
+        const float div = db[0][0] + db[1][1] + db[2][2];
+        float M[3][3];   // M[k][j] = gt^kl At_lj
+#pragma unroll
+        for (int kk = 0; kk < 3; ++kk)
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+                M[kk][j] = gi[sym(kk, 0)] * A[sym(0, j)] + gi[sym(kk, 1)] * A[sym(1, j)] + gi[sym(kk, 2)] * A[sym(2, j)];
+        const float aK = alpha * K, m2a = -2.0f * alpha, m23div = (-2.0f / 3.0f) * div;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = i; j < 3; ++j) {
+                float AgA = 0.0f, lie = 0.0f;
+#pragma unroll
+                for (int kk = 0; kk < 3; ++kk) {
+                    AgA += A[sym(i, kk)] * M[kk][j];
+                    lie += A[sym(kk, i)] * db[kk][j] + A[sym(kk, j)] * db[kk][i];
+                }
+                const int s = sym(i, j);
+                qbuf[s * A_THREADS + t] =
+                    (PT[s] - (1.0f / 3.0f) * g[s] * trP) + ((aK * A[s] + m2a * AgA) + lie + m23div * A[s]);
+            }
+    } else {
+#pragma unroll
+        for (int s = 0; s < AT_NQ; ++s) qbuf[s * A_THREADS + t] = 0.0f;
+    }
+
+    // ---- the boxes ----
+    const float aW = alpha * W, W2 = W * W, aW2 = aW * W;
+    const float chg[6] = {-0.5f * aW2 * gi[0], -aW2 * gi[1], -aW2 * gi[2],
+                          -0.5f * aW2 * gi[3], -aW2 * gi[4], -0.5f * aW2 * gi[5]};
+    const float i12 = G.gf.inv_12dx2, a1 = G.gf.d1a, a2 = G.gf.d1b;
+    float S[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    float L = 0.0f;   // gt^mn d_m d_n W (stencil parts)
+    // Hessians of gt_ij (-1/2 alpha W^2 gt^mn d_m d_n gt_ij), W (alpha W d_i d_j W
+    // and its trace) and alpha (-W^2 d_i d_j alpha)
+#pragma unroll 1
+    for (int f = 0; f < 8; ++f) {
+        float h[6];
+        if (!R.hessian(h, i12, a1, a2)) return;
+        if (f < 6) {
+            const float r = ((chg[0] * h[0] + chg[3] * h[3]) + chg[5] * h[5])
+                            + ((chg[1] * h[1] + chg[2] * h[2]) + chg[4] * h[4]);
+#pragma unroll
+            for (int q = 0; q < 6; ++q)
+                if (q == f) S[q] += r;
+        } else {
+            if (f == 6) L = contract_sym(gi, h);
+            const float c = f == 6 ? aW : -W2;
+#pragma unroll
+            for (int q = 0; q < 6; ++q) S[q] += c * h[q];
+        }
+    }
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {   // alpha W^2 gt_k(i d_j) Gt^k
+        const float* v = R.take() + R.cV2;
+        const float e[3] = {0.5f * aW2 * d1_box(v, V2X, a1, a2), 0.5f * aW2 * d1_box(v, SYB, a1, a2),
+                            0.5f * aW2 * d1_box(v, 1, a1, a2)};
+        if (!R.give()) return;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = i; j < 3; ++j) S[sym(i, j)] += g[sym(m, i)] * e[j] + g[sym(m, j)] * e[i];
+    }
+    {   // the trace-free part plus the pointwise terms, back into qbuf
+#pragma unroll
+        for (int s = 0; s < 6; ++s) S[s] += aW * g[s] * L;
+        const float tr = contract_sym(gi, S);
+#pragma unroll
+        for (int s = 0; s < 6; ++s) qbuf[s * A_THREADS + t] += S[s] - (1.0f / 3.0f) * g[s] * tr;
+    }
+    float beta[3] = {0.0f, 0.0f, 0.0f};
+    if (valid)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) beta[d] = static_cast<float>(u64[(BX + d) * cs + p]);
+    const float inv12 = G.gf.inv_12dx, scale = G.gf.ko_scale;
+#pragma unroll 1
+    for (int s = 0; s < 6; ++s) {   // advection and dissipation of At_ij
+        float adv, dis;
+        if (!R.transport(beta, inv12, adv, dis)) return;
+        if (valid) k[(AXX + s) * cs + p] = (qbuf[s * A_THREADS + t] + adv) + scale * dis;
+    }
+}
+
+// dt K    = -W^2 gt^mn d_m d_n alpha + PK + adv + KO,
+// dt Gt^i = gt^mn d_m d_n beta^i + 1/3 gt^ij d_j d_l beta^l - 4/3 alpha gt^ij d_j K
+//           + PG^i + adv + KO,
+// PK and PG^i the pointwise terms (JAX_BSSN/bssn/extrinsic_curvature.py:31-92,
+// conformal_connection.py:19-162).
+__global__ void __launch_bounds__(tma::A_THREADS, 2)
+k_rhs_kgt_tma(const __grid_constant__ tma::CurvMaps maps, const float* __restrict__ u, const double* __restrict__ u64,
+              const float* __restrict__ d1, double* __restrict__ k, Geo G, Box B, int z_base, int tiles_z,
+              int tiles_y, int nfield, int paired, int* __restrict__ timeouts) {
+    using namespace tma;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    float* ring = reinterpret_cast<float*>(smem_raw);
+    float* qbuf = ring + ANBUF * (A_SLOT / 4);   // [KGT_NQ][A_THREADS]: PK, PG^0..2
+    const int tile = blockIdx.x, inst = blockIdx.y;
+    const int z0 = z_base + AZ * (tile % tiles_z);
+    const int y0 = B.lo[1] + AY * ((tile / tiles_z) % tiles_y);
+    const int x0 = B.lo[0] + AX * (tile / (tiles_z * tiles_y));
+    const int t = threadIdx.x;
+    const int tz = t & 31, ty = (t >> 5) & 3, tx = t >> 7;
+    const int x = x0 + tx, y = y0 + ty, z = z0 + tz;
+    const bool valid = x < B.lo[0] + B.n[0] && y < B.lo[1] + B.n[1] && z >= B.lo[2] && z < B.lo[2] + B.n[2];
+    BoxRing<kSeqKgt> R;
+    R.maps = &maps;
+    R.ring = ring;
+    R.bars = reinterpret_cast<unsigned long long*>(qbuf + KGT_NQ * A_THREADS);
+    R.timeouts = timeouts;
+    R.ntile = seq_tiles(kSeqKgt, paired);
+    R.paired = paired;
+    R.nfield = nfield;
+    R.z0 = z0;
+    R.y0 = y0;
+    R.x0 = x0;
+    R.inst = inst;
+    R.t = t;
+    R.start(tz, ty, tx);
+
+    // ---- pointwise terms, while the first boxes load ----
+    const long long cs = G.cs;
+    const long long p = ((long long)x * G.ax[1].P + y) * G.ax[2].P + z + (long long)inst * G.istride;
+    float gi[6] = {1.0f, 0.0f, 0.0f, 1.0f, 0.0f, 1.0f};
+    float W = 1.0f, alpha = 1.0f;
+    if (valid) {
+        float g[6];
+#pragma unroll
+        for (int s = 0; s < 6; ++s) g[s] = u[(GXX + s) * cs + p] + (unit_diagonal(s) ? 1.0f : 0.0f);
+        inverse_metric(g, gi);
+        W = static_cast<float>(u64[CW * cs + p]);
+        alpha = static_cast<float>(u64[CALPHA * cs + p]);
+        const float K = static_cast<float>(u64[CK * cs + p]);
+        float c2[3][6];
+        {
+            float dg[3][6], c1[3][6];
+#pragma unroll
+            for (int kk = 0; kk < 3; ++kk)
+#pragma unroll
+                for (int s = 0; s < 6; ++s) dg[kk][s] = d1[((long long)(kk * nfield + MIX_G + s)) * cs + p];
+            christoffel(dg, gi, c1, c2);
+        }
+        float dW[3], da[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            dW[d] = d1[((long long)(d * nfield + MIX_W)) * cs + p];
+            da[d] = d1[((long long)(d * nfield + MIX_ALPHA)) * cs + p];
+        }
+        float A[6], Au[6];   // Au = A^ij = gt^ik (A_kl gt^lj)
+#pragma unroll
+        for (int s = 0; s < 6; ++s) A[s] = u[(AXX + s) * cs + p];
+        {
+            float M[3][3];
+#pragma unroll
+            for (int kk = 0; kk < 3; ++kk)
+#pragma unroll
+                for (int j = 0; j < 3; ++j)
+                    M[kk][j] = A[sym(kk, 0)] * gi[sym(0, j)] + A[sym(kk, 1)] * gi[sym(1, j)] + A[sym(kk, 2)] * gi[sym(2, j)];
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = i; j < 3; ++j)
+                    Au[sym(i, j)] = gi[sym(i, 0)] * M[0][j] + gi[sym(i, 1)] * M[1][j] + gi[sym(i, 2)] * M[2][j];
+        }
+        {   // dt K: gt^ij (W^2 Gamma^m_ij d_m alpha - W grad_ij) + alpha At_ij A^ij + alpha K^2 / 3
+            float gw = 0.0f;
+#pragma unroll
+            for (int n = 0; n < 3; ++n) gw += (gi[sym(0, n)] * dW[0] + gi[sym(1, n)] * dW[1] + gi[sym(2, n)] * dW[2]) * da[n];
+            float cA[6], gr[6];
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = i; j < 3; ++j) {
+                    const int s = sym(i, j);
+                    cA[s] = c2[0][s] * da[0] + c2[1][s] * da[1] + c2[2][s] * da[2];
+                    gr[s] = dW[i] * da[j] + dW[j] * da[i] - g[s] * gw;
+                }
+            qbuf[t] = ((W * W) * contract_sym(gi, cA) - W * contract_sym(gi, gr)) + alpha * contract_sym(A, Au)
+                      + alpha * (K * K) / 3.0f;
+        }
+        {   // dt Gt^i: 2 alpha Gamma^i_jk A^jk - 6 alpha/W A^ij d_j W - 2 A^ij d_j alpha
+            //          + 2/3 Gt^i div beta - Gt^j d_j beta^i
+            float db[3][3];
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) db[i][j] = d1[((long long)(j * nfield + MIX_B + i)) * cs + p];
+            const float div = db[0][0] + db[1][1] + db[2][2];
+            const float six_alpha_over_w = -6.0f * alpha * static_cast<float>(1.0 / fmax(u64[CW * cs + p], 1.0e-12));
+            const float Gt[3] = {u[GTX * cs + p], u[GTY * cs + p], u[GTZ * cs + p]};
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                float t3 = 0.0f, t4 = 0.0f, t7 = 0.0f;
+#pragma unroll
+                for (int j = 0; j < 3; ++j) {
+                    t3 += Au[sym(i, j)] * dW[j];
+                    t4 += Au[sym(i, j)] * da[j];
+                    t7 += Gt[j] * db[i][j];
+                }
+                const float t2 = contract_sym(c2[i], Au);
+                qbuf[(1 + i) * A_THREADS + t] = (((2.0f * alpha) * t2 + six_alpha_over_w * t3) - 2.0f * t4)
+                                                + ((2.0f / 3.0f) * Gt[i] * div - t7);
+            }
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < KGT_NQ; ++q) qbuf[q * A_THREADS + t] = 0.0f;
+    }
+
+    // ---- the boxes ----
+    const float i12 = G.gf.inv_12dx2, a1 = G.gf.d1a, a2 = G.gf.d1b;
+    float accK = 0.0f;
+    float accG[3] = {0.0f, 0.0f, 0.0f};
+    float graddiv[3] = {0.0f, 0.0f, 0.0f};   // d_m d_l beta^l
+    // Hessians of alpha (-W^2 gt^mn d_m d_n alpha) and beta^l (gt^mn d_m d_n beta^l)
+#pragma unroll 1
+    for (int f = 0; f < 4; ++f) {
+        float h[6];
+        if (!R.hessian(h, i12, a1, a2)) return;
+        const float c = contract_sym(gi, h);
+        if (f == 0) {
+            accK = -(W * W) * c;
+        } else {
+#pragma unroll
+            for (int l = 0; l < 3; ++l)
+                if (l == f - 1) {
+                    accG[l] += c;
+#pragma unroll
+                    for (int m = 0; m < 3; ++m) graddiv[m] += h[sym(m, l)];
+                }
+        }
+    }
+    float beta[3] = {0.0f, 0.0f, 0.0f};
+    if (valid)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) beta[d] = static_cast<float>(u64[(BX + d) * cs + p]);
+    const float inv12 = G.gf.inv_12dx, scale = G.gf.ko_scale;
+    {   // K: its first derivatives, advection and dissipation
+        float adv, dis, dK[3];
+        if (!R.transport(beta, inv12, adv, dis, dK, a1, a2)) return;
+        if (valid) k[CK * cs + p] = ((accK + qbuf[t]) + adv) + scale * dis;
+        const float m43a = (-4.0f / 3.0f) * alpha;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+            accG[i] += m43a * (gi[sym(i, 0)] * dK[0] + gi[sym(i, 1)] * dK[1] + gi[sym(i, 2)] * dK[2])
+                       + (1.0f / 3.0f) * (gi[sym(i, 0)] * graddiv[0] + gi[sym(i, 1)] * graddiv[1]
+                                          + gi[sym(i, 2)] * graddiv[2]);
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {   // Gt^i: advection and dissipation
+        float adv, dis;
+        if (!R.transport(beta, inv12, adv, dis)) return;
+        if (valid) k[(GTX + i) * cs + p] = ((accG[i] + qbuf[(1 + i) * A_THREADS + t]) + adv) + scale * dis;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // dt K and dt Gt^i
 // ---------------------------------------------------------------------------
 template <typename R, bool Closed>
@@ -1779,11 +2363,13 @@ EncodeTiled encode_tiled() {
     }();
     return fn;
 }
-// default: the derivatives only.  The gauge kernel is faster alone (206 vs
-// 276 us at 128^3) but runs beside the main stream's kernels, and its 90 KB
-// of shared memory per CTA crowds them out: the FP32 step took 9.55 ms with
-// it against 9.42 without (9.34 with the derivatives only).
-std::atomic<int> g_tma_mask{kTmaDerivs};
+// default: the derivatives and the curvature RHS.  The gauge kernel is faster
+// alone (206 vs 276 us at 128^3) but runs beside the main stream's kernels,
+// and its 90 KB of shared memory per CTA crowds them out: the FP32 step took
+// 9.55 ms with it against 9.42 without (9.34 with the derivatives only).  The
+// At kernel then took the 128^3 FP32 step from 8.60 to 8.13 ms and the K/Gt
+// kernel to 7.77 ms (paired: 10.12, 9.43, 9.01 ms).
+std::atomic<int> g_tma_mask{kTmaDerivs | kTmaAt | kTmaKgt};
 std::atomic<long long> g_tma_launches{0};
 __device__ int g_tma_timeouts;
 
@@ -1805,6 +2391,12 @@ cudaError_t tma_device(TmaDevice& out) {
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(k_first_derivs_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)tma::DSMEM);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_rhs_at_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)tma::curv_smem(tma::AT_NQ));
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_rhs_kgt_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)tma::curv_smem(tma::KGT_NQ));
         if (e == cudaSuccess) e = cudaGetSymbolAddress(reinterpret_cast<void**>(&d.timeouts), g_tma_timeouts);
         if (e != cudaSuccess) return e;
         d.ready = true;
@@ -1910,6 +2502,65 @@ static bool launch_first_derivs_tma(const float* u, float* d1, const Geo& G, con
     return true;
 }
 
+// The interior curvature RHS of the FP32 forms from TMA boxes (kappa = 0,
+// vacuum): dt At (kc = KC_AT, mask bit kTmaAt) or dt K and dt Gt^i (KC_KGT,
+// kTmaKgt); false leaves the launch to the generic kernel.
+static bool launch_curv_tma(int kc, const float* u, const double* u64, const float* d1, const float* damp,
+                            const double* mat, double* k, const Geo& G, const BoxSet& S, int nfield,
+                            cudaStream_t stream) {
+    const int bit = kc == KC_AT ? kTmaAt : kTmaKgt;
+    if (!(g_tma_mask.load() & bit) || damp != nullptr || mat != nullptr || nfield != NMIX || S.n != 1 ||
+        G.ninst < 1 || G.ninst > 65535)
+        return false;
+    for (int d = 0; d < 3; ++d)
+        if (G.ax[d].mad || G.ax[d].reduced) return false;
+    if (G.ax[2].P % 4 != 0 || reinterpret_cast<uintptr_t>(u) % 16 != 0 || reinterpret_cast<uintptr_t>(d1) % 16 != 0)
+        return false;
+    const long long istride = G.istride;
+    if (istride * 4 % 16 != 0) return false;
+    const EncodeTiled encode = encode_tiled();
+    if (!encode) return false;
+    TmaDevice dev;
+    if (tma_device(dev) != cudaSuccess) return false;
+    const Box& B = S.b[0];
+    // (z, y, x, instance, component) over the FP32 state with its low words,
+    // and over the first-derivative buffer (3 nfield components)
+    const cuuint64_t strides[4] = {(cuuint64_t)G.st[1] * 4, (cuuint64_t)G.st[0] * 4, (cuuint64_t)istride * 4,
+                                   (cuuint64_t)G.cs * 4};
+    const cuuint32_t unit[5] = {1, 1, 1, 1, 1};
+    tma::CurvMaps maps;
+    for (int kind = 0; kind < 4; ++kind) {
+        const bool state = kind == tma::kBoxV2 || kind == tma::kBoxV3;
+        const cuuint64_t dims[5] = {(cuuint64_t)G.ax[2].P, (cuuint64_t)G.ax[1].P, (cuuint64_t)G.ax[0].P,
+                                    (cuuint64_t)G.ninst, (cuuint64_t)(state ? NCOMP + NMIX : 3 * nfield)};
+        const cuuint32_t box[5] = {(cuuint32_t)tma::AHZ, (cuuint32_t)tma::a_hy(kind), (cuuint32_t)tma::a_hx(kind), 1,
+                                   1};
+        void* base = state ? const_cast<float*>(u) : const_cast<float*>(d1);
+        if (encode(&maps.map[kind], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 5, base, dims, strides, box, unit,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return false;
+    }
+    const int z_base = B.lo[2] & ~3;
+    const int tiles_z = (B.lo[2] + B.n[2] - z_base + tma::AZ - 1) / tma::AZ;
+    const int tiles_y = (B.n[1] + tma::AY - 1) / tma::AY;
+    const int tiles_x = (B.n[0] + tma::AX - 1) / tma::AX;
+    const long long tiles = (long long)tiles_z * tiles_y * tiles_x;
+    if (tiles <= 0 || tiles > 0x7fffffffLL) return false;
+    const int paired = G.precision == kPrecisionF32Paired ? 1 : 0;
+    const dim3 grid((unsigned)tiles, (unsigned)G.ninst);
+    prof_begin(kc, stream);
+    if (kc == KC_AT)
+        k_rhs_at_tma<<<grid, tma::A_THREADS, tma::curv_smem(tma::AT_NQ), stream>>>(
+            maps, u, u64, d1, k, G, B, z_base, tiles_z, tiles_y, nfield, paired, dev.timeouts);
+    else
+        k_rhs_kgt_tma<<<grid, tma::A_THREADS, tma::curv_smem(tma::KGT_NQ), stream>>>(
+            maps, u, u64, d1, k, G, B, z_base, tiles_z, tiles_y, nfield, paired, dev.timeouts);
+    prof_end(kc, stream);
+    g_tma_launches.fetch_add(1);
+    return true;
+}
+
 // ---------------------------------------------------------------------------
 // host-side launch sequence of one RHS evaluation: every stencil kernel runs
 // as a closure-free instantiation on the box interior and a general one on
@@ -2001,10 +2652,13 @@ static void launch_rhs_form(const R* u, const double* u64, double* k, R* d1, R* 
     if constexpr (kPerturbative<R>) {
         // FP32 form: issue- and latency-bound, so the smaller split kernels run
         // at higher occupancy.
-        BSSN_LAUNCH_SET(KC_KGT, 0, (k_rhs_kgt<R, false>), sb.interior, stb, u, u64, d1, mat, k, G, sb.interior, nfield);
+        if (!launch_curv_tma(KC_KGT, u, u64, d1, dmp, mat, k, G, sb.interior, nfield, stb))
+            BSSN_LAUNCH_SET(KC_KGT, 0, (k_rhs_kgt<R, false>), sb.interior, stb, u, u64, d1, mat, k, G, sb.interior,
+                            nfield);
         BSSN_LAUNCH_SET(KC_KGT, 1, (k_rhs_kgt<R, true>), sb.shell, stb, u, u64, d1, mat, k, G, sb.shell, nfield);
-        BSSN_LAUNCH_SET(KC_AT, 0, (k_rhs_at<R, false>), sb.interior, stream, u, u64, d1, dmp, mat, k, G, sb.interior,
-                        nfield);
+        if (!launch_curv_tma(KC_AT, u, u64, d1, dmp, mat, k, G, sb.interior, nfield, stream))
+            BSSN_LAUNCH_SET(KC_AT, 0, (k_rhs_at<R, false>), sb.interior, stream, u, u64, d1, dmp, mat, k, G,
+                            sb.interior, nfield);
         BSSN_LAUNCH_SET(KC_AT, 1, (k_rhs_at<R, true>), sb.shell, sts, u, u64, d1, dmp, mat, k, G, sb.shell, nfield);
     } else {
         BSSN_LAUNCH_SET(KC_CURV, 0, (k_rhs_curv<R, false>), sb.interior, stream, u, u64, d1, dmp, mat, k, G,

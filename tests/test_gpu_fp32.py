@@ -220,10 +220,11 @@ def test_paired_form_removes_the_second_derivative_rounding(gb):
 @pytest.mark.parametrize("form", FORMS)
 @pytest.mark.parametrize("faces", ["periodic", "sommerfeld"])
 def test_tma_kernels_match_the_generic_kernels(gb, form, faces):
-    """The FP32 forms' TMA-staged kernels (the gauge RHS and the first
-    derivatives of the interior; z pitch a multiple of four: 24 + 8) against
-    the generic kernels on the same state: every RHS leaf equal to float
-    rounding (1e-6 of its scale), with no tile wait given up."""
+    """The FP32 forms' TMA-staged kernels (the gauge RHS, the first
+    derivatives, dt At and dt K with dt Gt of the interior; z pitch a multiple
+    of four: 24 + 8)
+    against the generic kernels on the same state: every RHS leaf equal to
+    float rounding (1e-6 of its scale), with no tile wait given up."""
     pkg, te = gb
     from jax_bssn_gb300 import _native
     from jax_bssn_gb300.initial_data import random_smooth_state
@@ -241,9 +242,9 @@ def test_tma_kernels_match_the_generic_kernels(gb, form, faces):
             _native.set_tma(False)
             generic = te.compute_bssn_rhs(state, params)
         finally:
-            _native.set_tma(_native.TMA_DERIVS)   # the library's default
+            _native.set_tma(True)   # the library's default
     timeouts, last = _native.tma_status()
-    assert after == before + 2 and last == after, (before, after, last)   # both kernels tiled, then neither
+    assert after == before + 4 and last == after, (before, after, last)   # the four kernels tiled, then none
     assert timeouts == 0
     for leaf in ("conformal_metric", "conformal_factor", "traceless_K", "trace_K", "conformal_connection", "lapse",
                  "shift"):
