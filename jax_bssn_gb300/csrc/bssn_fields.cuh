@@ -255,7 +255,7 @@ __device__ __forceinline__ double inv_cbrt_cr(double x) {
 //   c2[i][sym(j,k)] = Gamma^i_jk = g^im Gamma_mjk
 // ---------------------------------------------------------------------------
 template <typename R>
-__device__ __forceinline__ void christoffel(const R (&dg)[3][6], const R (&gi)[6], R (&c1)[3][6], R (&c2)[3][6]) {
+__device__ __forceinline__ void christoffel_first(const R (&dg)[3][6], R (&c1)[3][6]) {
     // Index patterns whose terms cancel are written out: Gamma_iii = d_i g_ii / 2,
     // Gamma_ijj = d_j g_ij - d_i g_jj / 2, Gamma_iik = Gamma_iki = d_k g_ii / 2.
 #pragma unroll
@@ -272,6 +272,10 @@ __device__ __forceinline__ void christoffel(const R (&dg)[3][6], const R (&gi)[6
                 else v = R(0.5) * (dg[k][sym(i, j)] + dg[j][sym(i, k)] - dg[i][sym(j, k)]);
                 c1[i][sym(j, k)] = v;
             }
+}
+template <typename R>
+__device__ __forceinline__ void christoffel(const R (&dg)[3][6], const R (&gi)[6], R (&c1)[3][6], R (&c2)[3][6]) {
+    christoffel_first(dg, c1);
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll

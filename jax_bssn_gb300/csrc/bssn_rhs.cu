@@ -1058,17 +1058,24 @@ k_rhs_at_tma(const __grid_constant__ tma::CurvMaps maps, const float* __restrict
         const float aW = alpha * W, W2 = W * W, aW2 = aW * W;
         float PT[6];   // pointwise part of [alpha W^2 R_ij - W^2 D_i D_j alpha]
         {
-            float c1[3][6], c2[3][6];
+            float c1[3][6];
             {
                 float dg[3][6];
 #pragma unroll
                 for (int kk = 0; kk < 3; ++kk)
 #pragma unroll
                     for (int s = 0; s < 6; ++s) dg[kk][s] = d1[((long long)(kk * nfield + MIX_G + s)) * cs + p];
-                christoffel(dg, gi, c1, c2);
+                christoffel_first(dg, c1);
+            }
+            float dW[3], da[3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                dW[d] = d1[((long long)(d * nfield + MIX_W)) * cs + p];
+                da[d] = d1[((long long)(d * nfield + MIX_ALPHA)) * cs + p];
             }
             {   // 1/2 Gt^m d_m gt_ij = 1/2 Gt^m (Gamma_ijm + Gamma_jim)
                 const float Gt[3] = {u[GTX * cs + p], u[GTY * cs + p], u[GTZ * cs + p]};
+                const float h = 0.5f * aW2;
 #pragma unroll
                 for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -1076,35 +1083,40 @@ k_rhs_at_tma(const __grid_constant__ tma::CurvMaps maps, const float* __restrict
                         float t3 = 0.0f;
 #pragma unroll
                         for (int m = 0; m < 3; ++m) t3 += Gt[m] * (c1[i][sym(j, m)] + c1[j][sym(i, m)]);
-                        PT[sym(i, j)] = 0.5f * t3;
+                        PT[sym(i, j)] = h * t3;
                     }
             }
-            // the Christoffel products (term4 + term5 of the conformal Ricci tensor)
+            // One row Gamma^k_ij of the second kind at a time: the Christoffel
+            // products (term4 + term5 of the conformal Ricci tensor) and the
+            // first-derivative parts Gamma^k_ij d_k W, Gamma^k_ij d_k alpha of
+            // the W and lapse Hessians.
+            float gicW = 0.0f;   // gt^ij Gamma^k_ij d_k W
 #pragma unroll
             for (int kk = 0; kk < 3; ++kk) {
+                float c2k[6];
+#pragma unroll
+                for (int s = 0; s < 6; ++s)
+                    c2k[s] = gi[sym(kk, 0)] * c1[0][s] + gi[sym(kk, 1)] * c1[1][s] + gi[sym(kk, 2)] * c1[2][s];
                 float X[3][3];
 #pragma unroll
                 for (int a = 0; a < 3; ++a)
 #pragma unroll
                     for (int b = 0; b < 3; ++b)
-                        X[a][b] = gi[sym(0, a)] * c2[kk][sym(0, b)] + gi[sym(1, a)] * c2[kk][sym(1, b)]
-                                  + gi[sym(2, a)] * c2[kk][sym(2, b)];
+                        X[a][b] = gi[sym(0, a)] * c2k[sym(0, b)] + gi[sym(1, a)] * c2k[sym(1, b)]
+                                  + gi[sym(2, a)] * c2k[sym(2, b)];
+                gicW += dW[kk] * contract_sym(gi, c2k);
+                const float ck = W2 * da[kk] - aW * dW[kk];
 #pragma unroll
                 for (int i = 0; i < 3; ++i)
 #pragma unroll
                     for (int j = i; j < 3; ++j) {
-                        float acc = PT[sym(i, j)];
+                        float acc = 0.0f;
 #pragma unroll
                         for (int n = 0; n < 3; ++n)
                             acc += X[n][i] * (c1[j][sym(kk, n)] + c1[kk][sym(j, n)]) + X[n][j] * c1[i][sym(kk, n)];
-                        PT[sym(i, j)] = acc;
+                        const int s = sym(i, j);
+                        PT[s] += aW2 * acc + c2k[s] * ck;
                     }
-            }
-            float dW[3], da[3];
-#pragma unroll
-            for (int d = 0; d < 3; ++d) {
-                dW[d] = d1[((long long)(d * nfield + MIX_W)) * cs + p];
-                da[d] = d1[((long long)(d * nfield + MIX_ALPHA)) * cs + p];
             }
             float grad2 = 0.0f, gw = 0.0f;   // gt^mn d_m W d_n W, gt^mn d_m W d_n alpha
 #pragma unroll
@@ -1113,21 +1125,13 @@ k_rhs_at_tma(const __grid_constant__ tma::CurvMaps maps, const float* __restrict
                 grad2 += gdw * dW[n];
                 gw += gdw * da[n];
             }
-            float cW[6], cA[6];   // Gamma^m_ij d_m W, Gamma^m_ij d_m alpha
-#pragma unroll
-            for (int s = 0; s < 6; ++s) {
-                cW[s] = c2[0][s] * dW[0] + c2[1][s] * dW[1] + c2[2][s] * dW[2];
-                cA[s] = c2[0][s] * da[0] + c2[1][s] * da[1] + c2[2][s] * da[2];
-            }
-            const float gicW = contract_sym(gi, cW);
 #pragma unroll
             for (int i = 0; i < 3; ++i)
 #pragma unroll
                 for (int j = i; j < 3; ++j) {
                     const int s = sym(i, j);
                     const float grad = dW[i] * da[j] + dW[j] * da[i] - g[s] * gw;
-                    PT[s] = (aW2 * PT[s] - aW * (cW[s] + g[s] * gicW)) - 2.0f * alpha * g[s] * grad2
-                            + (W2 * cA[s] - W * grad);
+                    PT[s] += -g[s] * (aW * gicW + 2.0f * alpha * grad2) - W * grad;
                 }
         }
         const float trP = contract_sym(gi, PT);
@@ -1170,8 +1174,6 @@ k_rhs_at_tma(const __grid_constant__ tma::CurvMaps maps, const float* __restrict
 
     // ---- the boxes ----
     const float aW = alpha * W, W2 = W * W, aW2 = aW * W;
-    const float chg[6] = {-0.5f * aW2 * gi[0], -aW2 * gi[1], -aW2 * gi[2],
-                          -0.5f * aW2 * gi[3], -aW2 * gi[4], -0.5f * aW2 * gi[5]};
     const float i12 = G.gf.inv_12dx2, a1 = G.gf.d1a, a2 = G.gf.d1b;
     float S[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
     float L = 0.0f;   // gt^mn d_m d_n W (stencil parts)
@@ -1182,8 +1184,8 @@ k_rhs_at_tma(const __grid_constant__ tma::CurvMaps maps, const float* __restrict
         float h[6];
         if (!R.hessian(h, i12, a1, a2)) return;
         if (f < 6) {
-            const float r = ((chg[0] * h[0] + chg[3] * h[3]) + chg[5] * h[5])
-                            + ((chg[1] * h[1] + chg[2] * h[2]) + chg[4] * h[4]);
+            const float r = -aW2 * (0.5f * ((gi[0] * h[0] + gi[3] * h[3]) + gi[5] * h[5])
+                                    + ((gi[1] * h[1] + gi[2] * h[2]) + gi[4] * h[4]));
 #pragma unroll
             for (int q = 0; q < 6; ++q)
                 if (q == f) S[q] += r;
@@ -1274,14 +1276,14 @@ k_rhs_kgt_tma(const __grid_constant__ tma::CurvMaps maps, const float* __restric
         W = static_cast<float>(u64[CW * cs + p]);
         alpha = static_cast<float>(u64[CALPHA * cs + p]);
         const float K = static_cast<float>(u64[CK * cs + p]);
-        float c2[3][6];
+        float c1[3][6];
         {
-            float dg[3][6], c1[3][6];
+            float dg[3][6];
 #pragma unroll
             for (int kk = 0; kk < 3; ++kk)
 #pragma unroll
                 for (int s = 0; s < 6; ++s) dg[kk][s] = d1[((long long)(kk * nfield + MIX_G + s)) * cs + p];
-            christoffel(dg, gi, c1, c2);
+            christoffel_first(dg, c1);
         }
         float dW[3], da[3];
 #pragma unroll
@@ -1305,21 +1307,28 @@ k_rhs_kgt_tma(const __grid_constant__ tma::CurvMaps maps, const float* __restric
                 for (int j = i; j < 3; ++j)
                     Au[sym(i, j)] = gi[sym(i, 0)] * M[0][j] + gi[sym(i, 1)] * M[1][j] + gi[sym(i, 2)] * M[2][j];
         }
+        // One row Gamma^i_jk of the second kind at a time: Gamma^i_jk A^jk (dt Gt^i)
+        // and gt^jk Gamma^i_jk d_i alpha (dt K)
+        float t2[3], gicA = 0.0f;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            float c2i[6];
+#pragma unroll
+            for (int s = 0; s < 6; ++s)
+                c2i[s] = gi[sym(i, 0)] * c1[0][s] + gi[sym(i, 1)] * c1[1][s] + gi[sym(i, 2)] * c1[2][s];
+            t2[i] = contract_sym(c2i, Au);
+            gicA += da[i] * contract_sym(gi, c2i);
+        }
         {   // dt K: gt^ij (W^2 Gamma^m_ij d_m alpha - W grad_ij) + alpha At_ij A^ij + alpha K^2 / 3
             float gw = 0.0f;
 #pragma unroll
             for (int n = 0; n < 3; ++n) gw += (gi[sym(0, n)] * dW[0] + gi[sym(1, n)] * dW[1] + gi[sym(2, n)] * dW[2]) * da[n];
-            float cA[6], gr[6];
+            float gr[6];
 #pragma unroll
             for (int i = 0; i < 3; ++i)
 #pragma unroll
-                for (int j = i; j < 3; ++j) {
-                    const int s = sym(i, j);
-                    cA[s] = c2[0][s] * da[0] + c2[1][s] * da[1] + c2[2][s] * da[2];
-                    gr[s] = dW[i] * da[j] + dW[j] * da[i] - g[s] * gw;
-                }
-            qbuf[t] = ((W * W) * contract_sym(gi, cA) - W * contract_sym(gi, gr)) + alpha * contract_sym(A, Au)
-                      + alpha * (K * K) / 3.0f;
+                for (int j = i; j < 3; ++j) gr[sym(i, j)] = dW[i] * da[j] + dW[j] * da[i] - g[sym(i, j)] * gw;
+            qbuf[t] = ((W * W) * gicA - W * contract_sym(gi, gr)) + alpha * contract_sym(A, Au) + alpha * (K * K) / 3.0f;
         }
         {   // dt Gt^i: 2 alpha Gamma^i_jk A^jk - 6 alpha/W A^ij d_j W - 2 A^ij d_j alpha
             //          + 2/3 Gt^i div beta - Gt^j d_j beta^i
@@ -1340,8 +1349,7 @@ k_rhs_kgt_tma(const __grid_constant__ tma::CurvMaps maps, const float* __restric
                     t4 += Au[sym(i, j)] * da[j];
                     t7 += Gt[j] * db[i][j];
                 }
-                const float t2 = contract_sym(c2[i], Au);
-                qbuf[(1 + i) * A_THREADS + t] = (((2.0f * alpha) * t2 + six_alpha_over_w * t3) - 2.0f * t4)
+                qbuf[(1 + i) * A_THREADS + t] = (((2.0f * alpha) * t2[i] + six_alpha_over_w * t3) - 2.0f * t4)
                                                 + ((2.0f / 3.0f) * Gt[i] * div - t7);
             }
         }
