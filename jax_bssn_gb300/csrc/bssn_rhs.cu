@@ -818,9 +818,10 @@ k_first_derivs_tma(const __grid_constant__ CUtensorMap map, float* __restrict__ 
 // kernels k_rhs_at and k_rhs_kgt spend their issue slots on the address
 // arithmetic and latency of several hundred scalar stencil taps per point.
 // Here a CTA of 512 threads owns a 32 (z) x 4 (y) x 4 (x) tile, one sample
-// per thread, and streams every stencilled input through a four-deep ring of
-// shared-memory boxes, each one cp.async.bulk.tensor load completing on an
-// mbarrier:
+// per thread, and streams every stencilled input through a three-deep ring
+// of shared-memory boxes, each one cp.async.bulk.tensor load completing on an
+// mbarrier (three slots: two cost the loads' latency, four or a six-deep ring
+// released in pairs crowd out the RHS kernels beside them):
 //   a field's Hessian  value box, halo 2: the pure second derivatives (the
 //                      paired form adds its low word's from a second box);
 //                      boxes of its stored first derivatives along x and y,
@@ -839,7 +840,7 @@ namespace tma {
 constexpr int AZ = 32, AY = 4, AX = 4;                    // tile; one sample per thread
 constexpr int A_THREADS = AZ * AY * AX;                   // 512
 constexpr int AHZ = AZ + 8;                               // z halo 4 keeps the origin on 16 bytes
-constexpr int ANBUF = 4;
+constexpr int ANBUF = 3;
 enum CurvBox { kBoxV2 = 0, kBoxDX = 1, kBoxDY = 2, kBoxV3 = 3 };
 __host__ __device__ constexpr int a_hy(int kind) { return kind == kBoxV3 ? AY + 6 : (kind == kBoxDY ? AY : AY + 4); }
 __host__ __device__ constexpr int a_hx(int kind) { return kind == kBoxV3 ? AX + 6 : (kind == kBoxV2 ? AX + 4 : AX); }
