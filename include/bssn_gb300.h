@@ -275,10 +275,8 @@ int bssn_tune_patch(double* states, const BssnPatch* patch, int32_t ninst, const
  * BSSN_TMA_GAUGE), the first derivatives (BSSN_TMA_DERIVS), dt At
  * (BSSN_TMA_AT) and dt K with dt Gt (BSSN_TMA_KGT) can run from TMA-staged
  * shared-memory tiles instead of the generic kernels.  `kernels` is the mask
- * of those to use (default BSSN_TMA_DERIVS | BSSN_TMA_AT | BSSN_TMA_KGT: the
- * gauge kernel is faster alone but slows the whole RHS, whose other kernels
- * it crowds out; 0: the generic kernels everywhere); results agree to float
- * rounding.
+ * of those to use (default BSSN_TMA_ALL; 0: the generic kernels everywhere);
+ * results agree to float rounding.
  * Process-wide; affects later launches and captures. */
 #define BSSN_TMA_GAUGE 1
 #define BSSN_TMA_DERIVS 2

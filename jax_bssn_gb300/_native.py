@@ -316,7 +316,7 @@ def tune_launch_shapes(state_ptr: int, shape, instances: int, cparams: BssnParam
 
 
 TMA_GAUGE, TMA_DERIVS, TMA_AT, TMA_KGT, TMA_ALL = 1, 2, 4, 8, 15
-TMA_DEFAULT = TMA_DERIVS | TMA_AT | TMA_KGT
+TMA_DEFAULT = TMA_ALL
 
 
 def set_tma(kernels) -> None:

@@ -462,51 +462,23 @@ k_rhs_gauge(const R* __restrict__ u, const double* __restrict__ u64, const R* __
 }
 
 // ---------------------------------------------------------------------------
-// FP32 form, interior of the gauge RHS from TMA-staged tiles.
-//
-// k_rhs_gauge<float, false> spends its issue slots on the 64-bit address
-// arithmetic of ~374 scalar stencil taps per point.  Here a CTA owns a
-// 32 (z) x 8 (y) x 4 (x) tile of the interior box; the eleven stencilled
-// fields (gt, W, alpha, beta) stream through a two-deep ring of shared-memory
-// tiles, each one cp.async.bulk.tensor load of the field's 40 x 14 x 10 halo
-// box (halo 3 in x and y; 4 in z, keeping the box's z origin on a 16-byte
-// boundary) completing on an mbarrier.  A thread computes four consecutive z
-// samples from aligned 128-bit shared loads at compile-time offsets: 15 vector
-// loads per field instead of ~136 scalar ones.  The pointwise parts (Lie
-// terms, slicing, Gamma-driver) are formed first, while the first two tiles
-// are in flight, and staged in shared memory.  Same arithmetic as the
-// generic kernel's interior instantiation (closure-free, no MAD axis).
+// FP32 forms: shared pieces of the TMA-staged interior kernels.  Each stages
+// halo boxes of the float state (or of its stored first derivatives) in
+// shared memory with cp.async.bulk.tensor loads that complete on mbarriers;
+// every wait is bounded, and a CTA whose wait gives up counts a timeout,
+// waits once more (bounded) for its copies in flight and leaves its samples
+// unwritten.
 // ---------------------------------------------------------------------------
 namespace tma {
-constexpr int TZ = 32, TY = 8, TX = 4;                   // interior tile
-constexpr int HZ = TZ + 8, HY = TY + 6, HX = TX + 6;     // halo box (40 x 14 x 10)
-constexpr int SY = HZ, SX = HZ * HY;                     // shared strides (floats)
-constexpr int FIELD = HZ * HY * HX;                      // 5600 floats
-constexpr unsigned FIELD_BYTES = FIELD * 4;              // 22400 (a multiple of 128)
-constexpr int NBUF = 2;
-constexpr int NF = 11;                                   // gt (6), W, alpha, beta (3)
-constexpr int PTS = TZ * TY * TX;                        // 1024
-constexpr int THREADS = 256;
-constexpr size_t SMEM = (size_t)NBUF * FIELD_BYTES + (size_t)NF * PTS * 4 + NBUF * sizeof(unsigned long long);
+constexpr int TZ = 32, TY = 8, TX = 4;                   // first-derivative tile
+constexpr int THREADS = 256;                             // four z samples per thread
 constexpr long long kWaitLimit = 1LL << 24;              // try_wait polls before giving up
-static_assert(FIELD_BYTES % 128 == 0, "tile buffers must stay 128-byte aligned");
 static_assert(TX * TY * (TZ / 4) == THREADS, "one thread per four z samples");
-
-__host__ __device__ constexpr int field_comp(int f) { return f < 6 ? GXX + f : (f == 6 ? CW : (f == 7 ? CALPHA : BX + (f - 8))); }
 
 __device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
 
 __device__ __forceinline__ void bar_init(unsigned long long* bar) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
-}
-__device__ __forceinline__ void load_field(float* dst, const CUtensorMap* map, int z, int y, int x, int inst, int comp,
-                                           unsigned long long* bar) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(FIELD_BYTES)
-                 : "memory");
-    asm volatile(
-        "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, %6}], [%7];"
-        ::"r"(smem_addr(dst)), "l"(map), "r"(z), "r"(y), "r"(x), "r"(inst), "r"(comp), "r"(smem_addr(bar))
-        : "memory");
 }
 // Bounded wait on a tile's mbarrier phase; false when it gave up.
 __device__ __forceinline__ bool bar_wait(unsigned long long* bar, unsigned phase) {
@@ -520,8 +492,8 @@ __device__ __forceinline__ bool bar_wait(unsigned long long* bar, unsigned phase
     return false;
 }
 
-// Upwind numerator (units of 1/(12 dx)) of four samples from a 7-tap window
-// a[k + 3] = f(+k), the side chosen by c (the generic kernel's up1_num_fused).
+// Upwind numerator (units of 1/(12 dx)) from a 7-tap window a[k + 3] = f(+k),
+// the side chosen by c (the generic kernel's up1_num_fused).
 __device__ __forceinline__ float up1(const float (&a)[7], float c) {
     if (c > 0.0f) return (((-3.0f * a[2] + -10.0f * a[3]) + 18.0f * a[4]) + -6.0f * a[5]) + a[6];
     return (((-a[0] + 6.0f * a[1]) + -18.0f * a[2]) + 10.0f * a[3]) + 3.0f * a[4];
@@ -535,155 +507,6 @@ __device__ __forceinline__ float ko(const float (&a)[7]) {
 __device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
 __device__ __forceinline__ float at(const float4& v, int j) { return j == 0 ? v.x : (j == 1 ? v.y : (j == 2 ? v.z : v.w)); }
 }  // namespace tma
-
-__global__ void __launch_bounds__(tma::THREADS, 2)
-k_rhs_gauge_tma(const __grid_constant__ CUtensorMap map, const float* __restrict__ u, const double* __restrict__ u64,
-                const float* __restrict__ d1, double* __restrict__ k, Geo G, Box B, int z_base, int tiles_z,
-                int tiles_y, int nfield, int* __restrict__ timeouts) {
-    using namespace tma;
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    float* ring = reinterpret_cast<float*>(smem_raw);
-    float* part = ring + NBUF * FIELD;                               // [NF][PTS] pointwise parts
-    unsigned long long* bars = reinterpret_cast<unsigned long long*>(part + NF * PTS);
-
-    const int tile = blockIdx.x;
-    const int inst = blockIdx.y;   // instance of a batch
-    const int z0 = z_base + TZ * (tile % tiles_z);
-    const int y0 = B.lo[1] + TY * ((tile / tiles_z) % tiles_y);
-    const int x0 = B.lo[0] + TX * (tile / (tiles_z * tiles_y));
-    const int t = threadIdx.x;
-    const int tz4 = t & 7, ty = (t >> 3) & 7, tx = t >> 6;
-    const int x = x0 + tx, y = y0 + ty, zq = z0 + 4 * tz4;
-    const bool col = x >= B.lo[0] && x < B.lo[0] + B.n[0] && y >= B.lo[1] && y < B.lo[1] + B.n[1];
-    bool valid[4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) valid[j] = col && zq + j >= B.lo[2] && zq + j < B.lo[2] + B.n[2];
-
-    if (t == 0) {
-        for (int b = 0; b < NBUF; ++b) bar_init(&bars[b]);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    }
-    __syncthreads();
-    if (t == 0)
-        for (int f = 0; f < NBUF; ++f)
-            load_field(ring + f * FIELD, &map, z0 - 4, y0 - 3, x0 - 3, inst, field_comp(f), &bars[f]);
-
-    // pointwise parts, while the first tiles load
-    const long long cs = G.cs;
-    const long long p0 = ((long long)x * G.ax[1].P + y) * G.ax[2].P + zq + (long long)inst * G.istride;
-    const int lp = (tx * TY + ty) * TZ + 4 * tz4;
-    float beta[4][3];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        float pv[NF];
-        if (!valid[j]) {
-#pragma unroll
-            for (int f = 0; f < NF; ++f) pv[f] = 0.0f;
-#pragma unroll
-            for (int d = 0; d < 3; ++d) beta[j][d] = 0.0f;
-        } else {
-            const long long p = p0 + j;
-#pragma unroll
-            for (int d = 0; d < 3; ++d) beta[j][d] = static_cast<float>(u64[(BX + d) * cs + p]);
-            float db[3][3];
-#pragma unroll
-            for (int i = 0; i < 3; ++i)
-#pragma unroll
-                for (int jj = 0; jj < 3; ++jj) db[i][jj] = d1[((long long)(jj * nfield + MIX_B + i)) * cs + p];
-            const float div = db[0][0] + db[1][1] + db[2][2];
-            const float alpha = static_cast<float>(u64[CALPHA * cs + p]);
-            const float K = static_cast<float>(u64[CK * cs + p]);
-            const float W = static_cast<float>(u64[CW * cs + p]);
-            float g[6];
-#pragma unroll
-            for (int s2 = 0; s2 < 6; ++s2) g[s2] = u[(GXX + s2) * cs + p] + (unit_diagonal(s2) ? 1.0f : 0.0f);
-            const float m23div = -2.0f / 3.0f * div, m2a = -2.0f * alpha;
-#pragma unroll
-            for (int i = 0; i < 3; ++i)
-#pragma unroll
-                for (int jj = i; jj < 3; ++jj) {
-                    float lie = 0.0f;
-#pragma unroll
-                    for (int m = 0; m < 3; ++m) lie += g[sym(m, i)] * db[m][jj] + g[sym(m, jj)] * db[m][i];
-                    const int s2 = sym(i, jj);
-                    pv[s2] = lie + m23div * g[s2] + m2a * u[(AXX + s2) * cs + p];
-                }
-            pv[6] = (1.0f / 3.0f) * alpha * W * K - (1.0f / 3.0f) * W * div;
-            pv[7] = (G.gauge == 0) ? -(alpha * alpha) * K : -2.0f * alpha * K;
-#pragma unroll
-            for (int i = 0; i < 3; ++i)
-                pv[8 + i] = G.zero_shift ? 0.0f * beta[j][i]
-                                         : G.gf.g * u[(GTX + i) * cs + p] + (-G.gf.eta) * beta[j][i];
-        }
-#pragma unroll
-        for (int f = 0; f < NF; ++f) part[f * PTS + lp + j] = pv[f];
-    }
-
-    const int base = ((tx + 3) * HY + (ty + 3)) * HZ + 4 + 4 * tz4;   // this thread's first sample in a tile
-    const float scale = G.gf.ko_scale, inv12 = G.gf.inv_12dx;
-    for (int f = 0; f < NF; ++f) {
-        const int b = f % NBUF;
-        const int missing = !bar_wait(&bars[b], (unsigned)((f / NBUF) & 1));
-        if (__syncthreads_or(missing)) {
-            // a tile that never arrived (the whole CTA agrees): record it, give
-            // the copies in flight one more bounded wait, and leave
-            if (t == 0) {
-                atomicAdd(timeouts, 1);
-                for (int g = f; g < f + NBUF && g < NF; ++g) bar_wait(&bars[g % NBUF], (unsigned)((g / NBUF) & 1));
-            }
-            return;
-        }
-        const float* s = ring + b * FIELD + base;
-        const float4 pf = ld4(part + f * PTS + lp);
-        float adv[4][3], dis[4][3];
-        {   // z: one 12-sample window serves the four samples
-            const float4 m = ld4(s - 4), c = ld4(s), q = ld4(s + 4);
-            const float w[12] = {m.x, m.y, m.z, m.w, c.x, c.y, c.z, c.w, q.x, q.y, q.z, q.w};
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                float a[7];
-#pragma unroll
-                for (int o = 0; o < 7; ++o) a[o] = w[j + 1 + o];
-                adv[j][2] = beta[j][2] * inv12 * up1(a, beta[j][2]);
-                dis[j][2] = ko(a);
-            }
-        }
-#pragma unroll
-        for (int d = 0; d < 2; ++d) {   // x (d = 0) and y (d = 1): a vector per offset
-            const int st = d == 0 ? SX : SY;
-            float4 v[7];
-#pragma unroll
-            for (int o = 0; o < 7; ++o) v[o] = ld4(s + (o - 3) * st);
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                float a[7];
-#pragma unroll
-                for (int o = 0; o < 7; ++o) a[o] = at(v[o], j);
-                adv[j][d] = beta[j][d] * inv12 * up1(a, beta[j][d]);
-                dis[j][d] = ko(a);
-            }
-        }
-        const int comp = field_comp(f);
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            if (!valid[j]) continue;
-            const float A = (adv[j][0] + adv[j][1]) + adv[j][2];
-            const float D = scale * ((dis[j][0] + dis[j][1]) + dis[j][2]);
-            const float P = at(pf, j);
-            float v;
-            if (f >= 8 && G.zero_shift) v = P;
-            else if (f == 7) v = (P + A) + D;
-            else v = (A + P) + D;
-            k[comp * cs + p0 + j] = v;
-        }
-        __syncthreads();   // every thread is done with tile b
-        if (t == 0 && f + NBUF < NF) {
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            load_field(ring + b * FIELD, &map, z0 - 4, y0 - 3, x0 - 3, inst, field_comp(f + NBUF), &bars[b]);
-        }
-    }
-}
 
 // ---------------------------------------------------------------------------
 // FP32 forms, interior first derivatives of the NMIX fields from TMA tiles:
@@ -814,9 +637,10 @@ k_first_derivs_tma(const __grid_constant__ CUtensorMap map, float* __restrict__ 
 }
 
 // ---------------------------------------------------------------------------
-// FP32 forms, interior curvature RHS from TMA tiles.  The generic float
-// kernels k_rhs_at and k_rhs_kgt spend their issue slots on the address
-// arithmetic and latency of several hundred scalar stencil taps per point.
+// FP32 forms, interior curvature and gauge RHS from TMA boxes.  The generic
+// float kernels k_rhs_at, k_rhs_kgt and k_rhs_gauge spend their issue slots
+// on the address arithmetic and latency of several hundred scalar stencil
+// taps per point.
 // Here a CTA of 512 threads owns a 32 (z) x 4 (y) x 4 (x) tile, one sample
 // per thread, and streams every stencilled input through a three-deep ring
 // of shared-memory boxes, each one cp.async.bulk.tensor load completing on an
@@ -828,13 +652,14 @@ k_first_derivs_tma(const __grid_constant__ CUtensorMap map, float* __restrict__ 
 //                      halo 2 along the outer axis only: d_y d_x, d_z d_x and
 //                      d_z d_y;
 //   Gt^i (dt At)       value box, halo 2: its first derivatives;
-//   At_ij, K, Gt^i     value box, halo 3: upwind advection and dissipation
-//                      (and K's first derivatives).
+//   At_ij, K, Gt^i,    value box, halo 3: upwind advection and dissipation
+//   gt, W, alpha, beta (and K's first derivatives).
 // The RHS is linear in every one of these, so each box is folded into a few
 // accumulators as soon as it is read; the pointwise terms are formed from
-// single-sample reads while the first boxes load and wait in shared memory.
-// Same terms as the generic kernels' interior instantiation (closure-free, no
-// MAD axis, kappa = 0, vacuum), regrouped.
+// single-sample reads while the first boxes load, and wait in registers
+// (gauge) or shared memory (curvature).  Same terms as the generic kernels'
+// interior instantiation (closure-free, no MAD axis; the curvature RHS for
+// kappa = 0 in vacuum), regrouped.
 // ---------------------------------------------------------------------------
 namespace tma {
 constexpr int AZ = 32, AY = 4, AX = 4;                    // tile; one sample per thread
@@ -870,15 +695,16 @@ __device__ __forceinline__ CurvTile hessian_tile(int f, int r, int paired, int n
     if (paired && r == 1) return {kBoxV2, NCOMP + f};
     return (r - paired == 1) ? CurvTile{kBoxDX, f} : CurvTile{kBoxDY, nfield + f};
 }
-enum CurvSeq { kSeqAt = 0, kSeqKgt = 1 };
+enum CurvSeq { kSeqAt = 0, kSeqKgt = 1, kSeqGauge = 2 };
 __host__ __device__ constexpr int seq_tiles(int seq, int paired) {
-    return seq == kSeqAt ? 33 + 8 * paired : 16 + 4 * paired;
+    return seq == kSeqAt ? 33 + 8 * paired : (seq == kSeqKgt ? 16 + 4 * paired : NMIX);
 }
 // Box i of a kernel's fixed sequence.
 //   dt At:       Hessian groups of gt_ij, W and alpha (stored fields 0..7),
 //                the three Gt^i value boxes, the six At_ij halo-3 boxes;
 //   dt K, Gt^i:  Hessian groups of alpha and beta^i (stored fields 7..10),
-//                K's and the three Gt^i's halo-3 boxes.
+//                K's and the three Gt^i's halo-3 boxes;
+//   gauge:       the halo-3 boxes of gt_ij, W, alpha and beta^i.
 template <int Seq>
 __device__ __forceinline__ CurvTile seq_tile(int i, int paired, int nfield) {
     const int gsz = 3 + paired;
@@ -887,10 +713,12 @@ __device__ __forceinline__ CurvTile seq_tile(int i, int paired, int nfield) {
         i -= 8 * gsz;
         if (i < 3) return {kBoxV2, GTX + i};
         return {kBoxV3, AXX + (i - 3)};
-    } else {
+    } else if constexpr (Seq == kSeqKgt) {
         if (i < 4 * gsz) return hessian_tile(MIX_ALPHA + i / gsz, i % gsz, paired, nfield);
         i -= 4 * gsz;
         return {kBoxV3, i == 0 ? CK : GTX + (i - 1)};
+    } else {
+        return {kBoxV3, mix_source(i)};
     }
 }
 // Fourth-order centred numerators from a shared-memory box at compile-time strides.
@@ -1403,6 +1231,93 @@ k_rhs_kgt_tma(const __grid_constant__ tma::CurvMaps maps, const float* __restric
         float adv, dis;
         if (!R.transport(beta, inv12, adv, dis)) return;
         if (valid) k[(GTX + i) * cs + p] = ((accG[i] + qbuf[(1 + i) * A_THREADS + t]) + adv) + scale * dis;
+    }
+}
+
+// dt gt_ij, dt W, dt alpha, dt beta^i (JAX_BSSN/bssn/spatial_metric.py:17-106,
+// shift_and_lapse.py:65-132): each field's pointwise part (Lie terms,
+// slicing, Gamma-driver) in registers, then its advection and dissipation
+// from its halo-3 box.  Same terms as k_rhs_gauge<float, false>.
+__global__ void __launch_bounds__(tma::A_THREADS, 2)
+k_rhs_gauge_tma(const __grid_constant__ tma::CurvMaps maps, const float* __restrict__ u, const double* __restrict__ u64,
+                const float* __restrict__ d1, double* __restrict__ k, Geo G, Box B, int z_base, int tiles_z,
+                int tiles_y, int nfield, int paired, int* __restrict__ timeouts) {
+    using namespace tma;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    float* ring = reinterpret_cast<float*>(smem_raw);
+    const int tile = blockIdx.x, inst = blockIdx.y;
+    const int z0 = z_base + AZ * (tile % tiles_z);
+    const int y0 = B.lo[1] + AY * ((tile / tiles_z) % tiles_y);
+    const int x0 = B.lo[0] + AX * (tile / (tiles_z * tiles_y));
+    const int t = threadIdx.x;
+    const int tz = t & 31, ty = (t >> 5) & 3, tx = t >> 7;
+    const int x = x0 + tx, y = y0 + ty, z = z0 + tz;
+    const bool valid = x < B.lo[0] + B.n[0] && y < B.lo[1] + B.n[1] && z >= B.lo[2] && z < B.lo[2] + B.n[2];
+    BoxRing<kSeqGauge> R;
+    R.maps = &maps;
+    R.ring = ring;
+    R.bars = reinterpret_cast<unsigned long long*>(ring + ANBUF * (A_SLOT / 4));
+    R.timeouts = timeouts;
+    R.ntile = seq_tiles(kSeqGauge, paired);
+    R.paired = paired;
+    R.nfield = nfield;
+    R.z0 = z0;
+    R.y0 = y0;
+    R.x0 = x0;
+    R.inst = inst;
+    R.t = t;
+    R.start(tz, ty, tx);
+
+    const long long cs = G.cs;
+    const long long p = ((long long)x * G.ax[1].P + y) * G.ax[2].P + z + (long long)inst * G.istride;
+    float P[NMIX], beta[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+    for (int f = 0; f < NMIX; ++f) P[f] = 0.0f;
+    if (valid) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) beta[d] = static_cast<float>(u64[(BX + d) * cs + p]);
+        float db[3][3];   // db[i][j] = d_j beta^i
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) db[i][j] = d1[((long long)(j * nfield + MIX_B + i)) * cs + p];
+        const float div = db[0][0] + db[1][1] + db[2][2];
+        const float alpha = static_cast<float>(u64[CALPHA * cs + p]);
+        const float K = static_cast<float>(u64[CK * cs + p]);
+        const float W = static_cast<float>(u64[CW * cs + p]);
+        float g[6];
+#pragma unroll
+        for (int s = 0; s < 6; ++s) g[s] = u[(GXX + s) * cs + p] + (unit_diagonal(s) ? 1.0f : 0.0f);
+        const float m23div = (-2.0f / 3.0f) * div, m2a = -2.0f * alpha;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = i; j < 3; ++j) {
+                float lie = 0.0f;
+#pragma unroll
+                for (int m = 0; m < 3; ++m) lie += g[sym(m, i)] * db[m][j] + g[sym(m, j)] * db[m][i];
+                const int s = sym(i, j);
+                P[s] = lie + m23div * g[s] + m2a * u[(AXX + s) * cs + p];
+            }
+        P[MIX_W] = (1.0f / 3.0f) * alpha * W * K - (1.0f / 3.0f) * W * div;
+        P[MIX_ALPHA] = (G.gauge == 0) ? -(alpha * alpha) * K : -2.0f * alpha * K;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+            P[MIX_B + i] = G.zero_shift ? 0.0f * beta[i] : G.gf.g * u[(GTX + i) * cs + p] + (-G.gf.eta) * beta[i];
+    }
+    const float inv12 = G.gf.inv_12dx, scale = G.gf.ko_scale;
+#pragma unroll 1
+    for (int f = 0; f < NMIX; ++f) {
+        float adv, dis;
+        if (!R.transport(beta, inv12, adv, dis)) return;
+        float pf = P[0];
+#pragma unroll
+        for (int q = 1; q < NMIX; ++q) pf = q == f ? P[q] : pf;
+        float v;
+        if (f >= MIX_B && G.zero_shift) v = pf;
+        else if (f == MIX_ALPHA) v = (pf + adv) + scale * dis;
+        else v = (adv + pf) + scale * dis;
+        if (valid && !R.missing) k[mix_source(f) * cs + p] = v;
     }
 }
 
@@ -2372,13 +2287,12 @@ EncodeTiled encode_tiled() {
     }();
     return fn;
 }
-// default: the derivatives and the curvature RHS.  The gauge kernel is faster
-// alone (206 vs 276 us at 128^3) but runs beside the main stream's kernels,
-// and its 90 KB of shared memory per CTA crowds them out: the FP32 step took
-// 9.55 ms with it against 9.42 without (9.34 with the derivatives only).  The
-// At kernel then took the 128^3 FP32 step from 8.60 to 8.13 ms and the K/Gt
-// kernel to 7.77 ms (paired: 10.12, 9.43, 9.01 ms).
-std::atomic<int> g_tma_mask{kTmaDerivs | kTmaAt | kTmaKgt};
+// default: all four.  At 128^3 the FP32 step took 8.60 ms with the
+// derivatives alone, 8.13 with the At kernel, 7.77 with the K/Gt kernel and
+// 7.34 with the gauge kernel (paired: 10.12, 9.43, 9.01, 8.57 ms).  A gauge
+// kernel with four samples per thread and 90 KB of shared memory per CTA was
+// faster alone but crowded out the kernels beside it (9.55 against 9.42 ms).
+std::atomic<int> g_tma_mask{kTmaAll};
 std::atomic<long long> g_tma_launches{0};
 __device__ int g_tma_timeouts;
 
@@ -2396,7 +2310,8 @@ cudaError_t tma_device(TmaDevice& out) {
     std::lock_guard<std::mutex> guard(lock);
     TmaDevice& d = devices[dev];
     if (!d.ready) {
-        e = cudaFuncSetAttribute(k_rhs_gauge_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tma::SMEM);
+        e = cudaFuncSetAttribute(k_rhs_gauge_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)tma::curv_smem(0));
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(k_first_derivs_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)tma::DSMEM);
@@ -2424,48 +2339,6 @@ cudaError_t tma_timeouts(int* count) {
     cudaError_t e = cudaMemcpyFromSymbol(count, g_tma_timeouts, sizeof(int));
     if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_tma_timeouts, &zero, sizeof(int));
     return e;
-}
-
-// Launches the TMA gauge kernel on the interior box set when the geometry
-// allows it; false leaves the launch to the generic kernel.
-static bool launch_gauge_tma(const float* u, const double* u64, const float* d1, double* k, const Geo& G,
-                             const BoxSet& S, int nfield, cudaStream_t stream) {
-    if (!(g_tma_mask.load() & kTmaGauge) || S.n != 1 || G.ninst < 1 || G.ninst > 65535) return false;
-    for (int d = 0; d < 3; ++d)
-        if (G.ax[d].mad || G.ax[d].reduced) return false;
-    if (G.ax[2].P % 4 != 0 || reinterpret_cast<uintptr_t>(u) % 16 != 0) return false;
-    const EncodeTiled encode = encode_tiled();
-    if (!encode) return false;
-    TmaDevice dev;
-    if (tma_device(dev) != cudaSuccess) return false;
-    const Box& B = S.b[0];
-    // (z, y, x, instance, component); a single patch is a batch of one
-    const long long istride = G.istride;   // = cs for a single patch
-    const cuuint64_t dims[5] = {(cuuint64_t)G.ax[2].P, (cuuint64_t)G.ax[1].P, (cuuint64_t)G.ax[0].P,
-                                (cuuint64_t)G.ninst, (cuuint64_t)NCOMP};
-    const cuuint64_t strides[4] = {(cuuint64_t)G.st[1] * 4, (cuuint64_t)G.st[0] * 4, (cuuint64_t)istride * 4,
-                                   (cuuint64_t)G.cs * 4};
-    const cuuint32_t box[5] = {tma::HZ, tma::HY, tma::HX, 1, 1};
-    const cuuint32_t unit[5] = {1, 1, 1, 1, 1};
-    if (istride * 4 % 16 != 0) return false;
-    CUtensorMap map;
-    if (encode(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 5, const_cast<float*>(u), dims, strides, box, unit,
-               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-        return false;
-    const int z_base = B.lo[2] & ~3;   // tile z origins on 16-byte boundaries
-    const int tiles_z = (B.lo[2] + B.n[2] - z_base + tma::TZ - 1) / tma::TZ;
-    const int tiles_y = (B.n[1] + tma::TY - 1) / tma::TY;
-    const int tiles_x = (B.n[0] + tma::TX - 1) / tma::TX;
-    const long long tiles = (long long)tiles_z * tiles_y * tiles_x;
-    if (tiles <= 0 || tiles > 0x7fffffffLL) return false;
-    prof_begin(KC_GAUGE, stream);
-    const dim3 grid((unsigned)tiles, (unsigned)G.ninst);
-    k_rhs_gauge_tma<<<grid, tma::THREADS, tma::SMEM, stream>>>(map, u, u64, d1, k, G, B, z_base, tiles_z, tiles_y,
-                                                              nfield, dev.timeouts);
-    prof_end(KC_GAUGE, stream);
-    g_tma_launches.fetch_add(1);
-    return true;
 }
 
 // The interior first derivatives of the FP32 forms from TMA tiles (kappa = 0:
@@ -2511,15 +2384,17 @@ static bool launch_first_derivs_tma(const float* u, float* d1, const Geo& G, con
     return true;
 }
 
-// The interior curvature RHS of the FP32 forms from TMA boxes (kappa = 0,
-// vacuum): dt At (kc = KC_AT, mask bit kTmaAt) or dt K and dt Gt^i (KC_KGT,
-// kTmaKgt); false leaves the launch to the generic kernel.
+// The interior RHS of the FP32 forms from TMA boxes: dt At (kc = KC_AT, mask
+// bit kTmaAt) or dt K and dt Gt^i (KC_KGT, kTmaKgt), both for kappa = 0 in
+// vacuum, or the gauge RHS (KC_GAUGE, kTmaGauge); false leaves the launch to
+// the generic kernel.
 static bool launch_curv_tma(int kc, const float* u, const double* u64, const float* d1, const float* damp,
                             const double* mat, double* k, const Geo& G, const BoxSet& S, int nfield,
                             cudaStream_t stream) {
-    const int bit = kc == KC_AT ? kTmaAt : kTmaKgt;
-    if (!(g_tma_mask.load() & bit) || damp != nullptr || mat != nullptr || nfield != NMIX || S.n != 1 ||
-        G.ninst < 1 || G.ninst > 65535)
+    const int bit = kc == KC_AT ? kTmaAt : (kc == KC_KGT ? kTmaKgt : kTmaGauge);
+    const bool curvature = kc != KC_GAUGE;
+    if (!(g_tma_mask.load() & bit) || (curvature && (damp != nullptr || mat != nullptr || nfield != NMIX)) ||
+        S.n != 1 || G.ninst < 1 || G.ninst > 65535)
         return false;
     for (int d = 0; d < 3; ++d)
         if (G.ax[d].mad || G.ax[d].reduced) return false;
@@ -2562,8 +2437,11 @@ static bool launch_curv_tma(int kc, const float* u, const double* u64, const flo
     if (kc == KC_AT)
         k_rhs_at_tma<<<grid, tma::A_THREADS, tma::curv_smem(tma::AT_NQ), stream>>>(
             maps, u, u64, d1, k, G, B, z_base, tiles_z, tiles_y, nfield, paired, dev.timeouts);
-    else
+    else if (kc == KC_KGT)
         k_rhs_kgt_tma<<<grid, tma::A_THREADS, tma::curv_smem(tma::KGT_NQ), stream>>>(
+            maps, u, u64, d1, k, G, B, z_base, tiles_z, tiles_y, nfield, paired, dev.timeouts);
+    else
+        k_rhs_gauge_tma<<<grid, tma::A_THREADS, tma::curv_smem(0), stream>>>(
             maps, u, u64, d1, k, G, B, z_base, tiles_z, tiles_y, nfield, paired, dev.timeouts);
     prof_end(kc, stream);
     g_tma_launches.fetch_add(1);
@@ -2644,7 +2522,8 @@ static void launch_rhs_form(const R* u, const double* u64, double* k, R* d1, R* 
     // gauge: its own branch (b in the FP64 form, c in the FP32 form)
     const cudaStream_t stg = kPerturbative<R> ? stc : stb;
     bool gauge_done = false;
-    if constexpr (kPerturbative<R>) gauge_done = launch_gauge_tma(u, u64, d1, k, G, sb.interior, nfield, stg);
+    if constexpr (kPerturbative<R>)
+        gauge_done = launch_curv_tma(KC_GAUGE, u, u64, d1, nullptr, nullptr, k, G, sb.interior, nfield, stg);
     if (!gauge_done)
         BSSN_LAUNCH_SET(KC_GAUGE, 0, (k_rhs_gauge<R, false>), sb.interior, stg, u, u64, d1, k, G, sb.interior,
                         nfield);
