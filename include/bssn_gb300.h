@@ -213,13 +213,15 @@ int bssn_batch_rk4_monitored(double* states, const BssnPatch* patch, int32_t nin
                              void* workspace, size_t workspace_bytes, void* stream);
 
 /* ---------------- adjoint (reverse mode) ----------------
- * Gradients of periodic evolutions.  The reference has no hand-written
- * adjoint: differentiating its rk4_step (JAX_BSSN/evolution/time_evolve.py:144-217)
+ * Gradients of evolutions.  The reference has no hand-written adjoint:
+ * differentiating its rk4_step (JAX_BSSN/evolution/time_evolve.py:144-217)
  * means jax.grad / jax.vjp through XLA.  These entry points are the
  * vector-Jacobian products of the same forward path, on instance batches
- * (layout of bssn_batch_*).  Scope: every face periodic (bc all 0),
- * kappa = 0, no matter sources, BSSN_PRECISION_F64, at least 8 samples per
- * axis; anything else returns BSSN_ERR_INVALID.  Adjoint arrays have the
+ * (layout of bssn_batch_*).  Scope: every face periodic (bc all 0) or every
+ * face Sommerfeld (bc all 1: the one-sided closure rows and the radial face
+ * condition are transposed too), kappa = 0, no matter sources,
+ * BSSN_PRECISION_F64, at least 8 samples per axis; anything else returns
+ * BSSN_ERR_INVALID.  Adjoint arrays have the
  * batch layout; only their owned samples carry values (ghosts are scratch).
  * Gradients are with respect to the 21 independent components. */
 
@@ -227,7 +229,7 @@ int bssn_batch_rk4_monitored(double* states, const BssnPatch* patch, int32_t nin
 size_t bssn_rhs_vjp_workspace_bytes(const BssnPatch* patch, int32_t ninst);
 /* state_adjoint = (d RHS / d state)^T rhs_adjoint at `states`
  * (compute_bssn_rhs, time_evolve.py:41-57).  Fills the ghosts of `states`
- * and `rhs_adjoint` (periodic wrap) in place. */
+ * and `rhs_adjoint` (periodic wrap, on periodic grids) in place. */
 int bssn_rhs_vjp(double* states, double* rhs_adjoint, double* state_adjoint, const BssnPatch* patch, int32_t ninst,
                  const BssnParams* params, void* workspace, size_t workspace_bytes, void* stream);
 

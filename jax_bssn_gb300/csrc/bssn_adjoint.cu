@@ -1,4 +1,4 @@
-// Reverse-mode (adjoint) kernels of the periodic BSSN evolution on GB300.
+// Reverse-mode (adjoint) kernels of the BSSN evolution on GB300.
 //
 // The forward path is rk4_step (JAX_BSSN/evolution/time_evolve.py:144-217)
 // with its RHS compute_bssn_rhs (time_evolve.py:41-57).  The reference never
@@ -38,7 +38,8 @@
 // the cheap stage kernels), 2 the stage states as well.  With 1 or 2 the
 // forward pass records the last segment itself.
 // Everything runs on instance batches (layout [component][instance][block]).
-// Scope: all faces periodic, kappa = 0, no matter, FP64 arithmetic.
+// Scope: every face periodic, or every face Sommerfeld (the band kernels
+// below); kappa = 0, no matter, FP64 arithmetic.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -112,8 +113,133 @@ __device__ __forceinline__ bool owned_point(const Geo& G, const Box& B, Pt& c) {
 }
 
 // ---------------------------------------------------------------------------
+// Sommerfeld faces.  On an axis closed by Sommerfeld faces the forward
+// replaces the RHS on the face planes by the radial condition and uses
+// one-sided rows next to them: D1 and D2 on rows 0-1 from a face, the sixth
+// difference on rows 0-2, and the centred D1 in place of the upwind one for
+// advection on rows 0-2 (JAX_BSSN/evolution/derivatives.py:42-338,
+// spatial_derivatives.py:18-92, boundaries.py:150-171).  Rows 0-2 at each
+// closed face form the axis' band.  The interior transposes gather from the
+// sources outside the bands (masked taps); sources in a band scatter their
+// rows' own weights with atomic adds (k_adj_band_mixed, k_adj_band_field).
+// The face planes' bulk RHS is never formed, so their kbar enters only the
+// transpose of the radial condition (k_adj_sommerfeld).
+// ---------------------------------------------------------------------------
+struct BandRow {
+    int r;        // row from the nearer closed face (0..2), or -1
+    bool right;   // that face is the upper one
+};
+// The upper face is checked first, as the forward's closures do.
+__device__ __forceinline__ BandRow band_row(const Axis& A, int i) {
+    if (A.rbc) {
+        const int r = A.end - 1 - i;
+        if (r >= 0 && r < 3) return {r, true};
+    }
+    if (A.lbc) {
+        const int r = i - A.start;
+        if (r >= 0 && r < 3) return {r, false};
+    }
+    return {-1, false};
+}
+// Sources the interior transposes gather along A: outside the bands and not
+// beyond a closed face.
+__device__ __forceinline__ bool gathers(const Axis& A, int i) {
+    return !(A.lbc && i < A.start + 3) && !(A.rbc && i > A.end - 4);
+}
+__device__ __forceinline__ bool face_along(const Axis& A, int i) {
+    return (A.slo && i == A.start) || (A.shi && i == A.end - 1);
+}
+// A point whose RHS the forward replaces by the radial condition.
+__device__ __forceinline__ bool face_point(const Geo& G, const int (&ix)[3]) {
+    return face_along(G.ax[0], ix[0]) || face_along(G.ax[1], ix[1]) || face_along(G.ax[2], ix[2]);
+}
+// ... on a face plane of an axis other than a: then so is every source
+// along a of this point.
+__device__ __forceinline__ bool face_off_axis(const Geo& G, const int (&ix)[3], int a) {
+    bool f = false;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) f = f || (d != a && face_along(G.ax[d], ix[d]));
+    return f;
+}
+
+// One-sided rows at the lower face (row r's taps start at offset -r); the
+// upper face's are their mirror images (odd in the offset for D1).
+__constant__ double kBandD1[2][5] = {{-25.0 / 12.0, 4.0, -3.0, 4.0 / 3.0, -1.0 / 4.0},
+                                      {-1.0 / 4.0, -5.0 / 6.0, 3.0 / 2.0, -1.0 / 2.0, 1.0 / 12.0}};
+__constant__ double kBandD2[2][6] = {{15.0 / 4.0, -77.0 / 6.0, 107.0 / 6.0, -13.0, 61.0 / 12.0, -5.0 / 6.0},
+                                      {5.0 / 6.0, -5.0 / 4.0, -1.0 / 3.0, 7.0 / 6.0, -1.0 / 2.0, 1.0 / 12.0}};
+__constant__ double kBandKO[3][8] = {{4.0, -27.0, 78.0, -125.0, 120.0, -69.0, 22.0, -3.0},
+                                      {3.0, -20.0, 57.0, -90.0, 85.0, -48.0, 15.0, -2.0},
+                                      {2.0, -13.0, 36.0, -55.0, 50.0, -27.0, 8.0, -1.0}};
+// centred rows, offsets -2..2
+__constant__ double kMidD1[5] = {1.0 / 12.0, -2.0 / 3.0, 0.0, 2.0 / 3.0, -1.0 / 12.0};
+__constant__ double kMidD2[5] = {-1.0 / 12.0, 16.0 / 12.0, -30.0 / 12.0, 16.0 / 12.0, -1.0 / 12.0};
+__constant__ double kMidKO[7] = {1.0, -6.0, 15.0, -20.0, 15.0, -6.0, 1.0};
+
+enum BandOp { kOpD1 = 0, kOpD2 = 1, kOpKO = 2 };
+// Calls tap(offset, weight) for every tap of the row the forward applies at
+// band row b (b.r < 0: an interior sample), weights before the operator's
+// factor (1/dx, 1/dx^2, the KO factor).  D1 and D2 are one-sided on rows 0-1
+// and centred beyond; the sixth difference is one-sided on rows 0-2.
+template <typename F>
+__device__ __forceinline__ void band_taps(int op, BandRow b, F&& tap) {
+    if (op == kOpKO && b.r >= 0) {
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+            const int o = t - b.r;
+            tap(b.right ? -o : o, kBandKO[b.r][t]);
+        }
+    } else if (op == kOpKO) {
+#pragma unroll
+        for (int t = 0; t < 7; ++t) tap(t - 3, kMidKO[t]);
+    } else if (b.r < 0 || b.r > 1) {
+#pragma unroll
+        for (int t = 0; t < 5; ++t) tap(t - 2, op == kOpD1 ? kMidD1[t] : kMidD2[t]);
+    } else if (op == kOpD1) {
+#pragma unroll
+        for (int t = 0; t < 5; ++t) {
+            const int o = t - b.r;
+            tap(b.right ? -o : o, b.right ? -kBandD1[b.r][t] : kBandD1[b.r][t]);
+        }
+    } else {
+#pragma unroll
+        for (int t = 0; t < 6; ++t) {
+            const int o = t - b.r;
+            tap(b.right ? -o : o, kBandD2[b.r][t]);
+        }
+    }
+}
+
+// The forward's centred D1 and D2 along axis a at index j of x (x points at
+// sample j) over the sources the gathers take; on periodic geometries the
+// forward's own stencil (every source, MAD blend included).
+template <bool Closed>
+__device__ __forceinline__ double g_d1(const double* x, const Geo& G, int a, int j) {
+    if constexpr (!Closed) {
+        return D1<double, false>(x, G, a, j);
+    } else {
+        const Axis& A = G.ax[a];
+        const long long s = G.st[a];
+        auto v = [&](int o) { return gathers(A, j + o) ? x[o * s] : 0.0; };
+        return (v(1) - v(-1)) * G.d1a + (v(2) - v(-2)) * G.d1b;
+    }
+}
+template <bool Closed>
+__device__ __forceinline__ double g_d2(const double* x, const Geo& G, int a, int j) {
+    if constexpr (!Closed) {
+        return D2<double, false, false>(x, G, a, j);
+    } else {
+        const Axis& A = G.ax[a];
+        const long long s = G.st[a];
+        auto v = [&](int o) { return gathers(A, j + o) ? x[o * s] : 0.0; };
+        return ((16.0 * (v(1) + v(-1)) - (v(2) + v(-2))) + -30.0 * v(0)) * G.inv_12dx2;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // point kernel: inputs of F by the forward's stencil helpers, reverse sweep
 // ---------------------------------------------------------------------------
+template <bool Closed>
 __global__ void __launch_bounds__(kThreads)
 k_adj_point(const double* __restrict__ u, const double* __restrict__ d1, const double* __restrict__ kbar,
             double kscale, double* __restrict__ ubar, double* __restrict__ coef, Geo G, Box B, PointParams pp,
@@ -121,20 +247,28 @@ k_adj_point(const double* __restrict__ u, const double* __restrict__ d1, const d
     Pt c;
     if (!owned_point(G, B, c)) return;
     const long long cs = G.cs, p = c.p;
+    if constexpr (Closed) {
+        if (face_point(G, c.ix)) {   // the forward replaces this RHS: no bulk terms
+            if (!accumulate)
+                for (int f = 0; f < NCOMP; ++f) ubar[f * cs + p] = 0.0;
+            for (int k = 0; k < NCOEF; ++k) coef[(long long)k * cs + p] = 0.0;
+            return;
+        }
+    }
     double x[kPointInputs];
 #pragma unroll
     for (int f = 0; f < NCOMP; ++f) x[f] = u[f * cs + p];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
 #pragma unroll
-        for (int s = 0; s < 6; ++s) x[I_DG + 6 * a + s] = D1<double, false>(u + (GXX + s) * cs + p, G, a, c.ix[a]);
-        x[I_DW + a] = D1<double, false>(u + CW * cs + p, G, a, c.ix[a]);
-        x[I_DAL + a] = D1<double, false>(u + CALPHA * cs + p, G, a, c.ix[a]);
-        x[I_DK + a] = D1<double, false>(u + CK * cs + p, G, a, c.ix[a]);
+        for (int s = 0; s < 6; ++s) x[I_DG + 6 * a + s] = D1<double, Closed>(u + (GXX + s) * cs + p, G, a, c.ix[a]);
+        x[I_DW + a] = D1<double, Closed>(u + CW * cs + p, G, a, c.ix[a]);
+        x[I_DAL + a] = D1<double, Closed>(u + CALPHA * cs + p, G, a, c.ix[a]);
+        x[I_DK + a] = D1<double, Closed>(u + CK * cs + p, G, a, c.ix[a]);
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
-            x[I_DB + 3 * i + a] = D1<double, false>(u + (BX + i) * cs + p, G, a, c.ix[a]);
-            x[I_DGT + 3 * a + i] = D1<double, false>(u + (GTX + i) * cs + p, G, a, c.ix[a]);
+            x[I_DB + 3 * i + a] = D1<double, Closed>(u + (BX + i) * cs + p, G, a, c.ix[a]);
+            x[I_DGT + 3 * a + i] = D1<double, Closed>(u + (GTX + i) * cs + p, G, a, c.ix[a]);
         }
     }
     // second derivatives: D2 on the diagonal, D1 along the larger axis of the
@@ -147,8 +281,8 @@ k_adj_point(const double* __restrict__ u, const double* __restrict__ d1, const d
 #pragma unroll
             for (int f = 0; f < NMIX; ++f) {
                 const double v = m == n
-                    ? D2<double, false, false>(u + mix_source(f) * cs + p, G, m, c.ix[m])
-                    : D1<double, false>(d1 + (long long)(m * NMIX + f) * cs + p, G, n, c.ix[n]);
+                    ? D2<double, Closed, false>(u + mix_source(f) * cs + p, G, m, c.ix[m])
+                    : D1<double, Closed>(d1 + (long long)(m * NMIX + f) * cs + p, G, n, c.ix[n]);
                 x[21 + c2_block(f, pr)] = v;
             }
         }
@@ -165,6 +299,7 @@ k_adj_point(const double* __restrict__ u, const double* __restrict__ d1, const d
 
 // m_a = -c1_a + sum_{b > a} D1_b(c2_ab) for the NMIX fields, into mbuf
 // (layout of the inner-derivative buffer: block a * NMIX + f).
+template <bool Closed>
 __global__ void __launch_bounds__(kThreads)
 k_adj_mixed(const double* __restrict__ coef, double* __restrict__ mbuf, Geo G, Box B) {
     Pt c;
@@ -176,9 +311,9 @@ k_adj_mixed(const double* __restrict__ coef, double* __restrict__ mbuf, Geo G, B
         const double* c01 = coef + (long long)c2_block(f, sym(0, 1)) * cs + p;
         const double* c02 = coef + (long long)c2_block(f, sym(0, 2)) * cs + p;
         const double* c12 = coef + (long long)c2_block(f, sym(1, 2)) * cs + p;
-        const double m0 = -coef[(long long)c1_block(comp, 0) * cs + p] + D1<double, false>(c01, G, 1, c.ix[1])
-                          + D1<double, false>(c02, G, 2, c.ix[2]);
-        const double m1 = -coef[(long long)c1_block(comp, 1) * cs + p] + D1<double, false>(c12, G, 2, c.ix[2]);
+        const double m0 = -coef[(long long)c1_block(comp, 0) * cs + p] + g_d1<Closed>(c01, G, 1, c.ix[1])
+                          + g_d1<Closed>(c02, G, 2, c.ix[2]);
+        const double m1 = -coef[(long long)c1_block(comp, 1) * cs + p] + g_d1<Closed>(c12, G, 2, c.ix[2]);
         const double m2 = -coef[(long long)c1_block(comp, 2) * cs + p];
         mbuf[(long long)(0 * NMIX + f) * cs + p] = m0;
         mbuf[(long long)(1 * NMIX + f) * cs + p] = m1;
@@ -193,7 +328,10 @@ __constant__ double kUp4[2][9] = {{0, 0, 0, -3, -10, 18, -6, 1, 0}, {0, -1, 6, -
 __constant__ double kUp6[2][9] = {{0, 0, 2, -24, -35, 80, -30, 8, -1}, {1, -8, 30, -80, 35, 24, -2, 0, 0}};
 
 // Transposed stencils of every component at one point, the dissipation and
-// advection transposes, and the shift's adjoint from the advection terms.
+// advection transposes, and the shift's adjoint from the advection terms
+// (with Sommerfeld faces: the gathered part; k_adj_band_field adds the band
+// sources').
+template <bool Closed>
 __global__ void __launch_bounds__(kThreads)
 k_adj_field(const double* __restrict__ u, const double* __restrict__ kbar, double kscale,
             const double* __restrict__ coef, const double* __restrict__ mbuf, double* __restrict__ ubar, Geo G,
@@ -201,6 +339,12 @@ k_adj_field(const double* __restrict__ u, const double* __restrict__ kbar, doubl
     Pt c;
     if (!owned_point(G, B, c)) return;
     const long long cs = G.cs, p = c.p;
+    // bulk[a]: the sources along a carry a bulk RHS (not on another axis' face plane)
+    bool bulk[3] = {true, true, true};
+    if constexpr (Closed) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) bulk[a] = !face_off_axis(G, c.ix, a);
+    }
     // w[a][k + 4]: weight of kbar_f at q - k e_a in the transposed advection
     double w[3][9];
 #pragma unroll
@@ -209,11 +353,13 @@ k_adj_field(const double* __restrict__ u, const double* __restrict__ kbar, doubl
         const long long s = G.st[a];
 #pragma unroll
         for (int k = -4; k <= 4; ++k) {
-            const double b = u[(BX + a) * cs + p - k * s];
+            bool take = !ax.reduced;
+            if constexpr (Closed) take = take && bulk[a] && gathers(ax, c.ix[a] - k);
+            const double b = take ? u[(BX + a) * cs + p - k * s] : 0.0;
             const int side = b > 0.0 ? 0 : 1;
             double c4 = kUp4[side][k + 4] * G.inv_12dx;
             if (ax.mad) c4 = ax.q * c4 + ax.omq * (kUp6[side][k + 4] * G.inv_60dx);
-            w[a][k + 4] = (b == 0.0 || ax.reduced) ? 0.0 : b * c4;
+            w[a][k + 4] = b == 0.0 ? 0.0 : b * c4;
         }
     }
     // Where the shift vanishes on every tap of every lane of the warp the
@@ -235,17 +381,32 @@ k_adj_field(const double* __restrict__ u, const double* __restrict__ kbar, doubl
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
             if (mf >= 0) {
-                r += D1<double, false>(mbuf + (long long)(a * NMIX + mf) * cs + p, G, a, c.ix[a]);
-                r += D2<double, false, false>(coef + (long long)c2_block(mf, sym(a, a)) * cs + p, G, a, c.ix[a]);
+                r += g_d1<Closed>(mbuf + (long long)(a * NMIX + mf) * cs + p, G, a, c.ix[a]);
+                r += g_d2<Closed>(coef + (long long)c2_block(mf, sym(a, a)) * cs + p, G, a, c.ix[a]);
             } else {
                 const int cb = c1_block(f, a);
-                if (cb >= 0) r -= D1<double, false>(coef + (long long)cb * cs + p, G, a, c.ix[a]);
+                if (cb >= 0) r -= g_d1<Closed>(coef + (long long)cb * cs + p, G, a, c.ix[a]);
             }
         }
         const bool row_on = !(f >= BX && G.zero_shift);
         if (row_on) {
             const double* kf = kbar + f * cs + p;
-            double lin = KO<double, false, false>(kf, G, c.ix);
+            double lin;
+            if constexpr (Closed) {
+                double t = 0.0;
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    if (!bulk[a]) continue;
+                    const Axis& A = G.ax[a];
+                    const long long s = G.st[a];
+#pragma unroll
+                    for (int o = -3; o <= 3; ++o)
+                        if (gathers(A, c.ix[a] + o)) t = fma(kMidKO[o + 3], kf[o * s], t);
+                }
+                lin = G.ko_scale * t;
+            } else {
+                lin = KO<double, false, false>(kf, G, c.ix);
+            }
             if (moving) {
                 double adv = 0.0;
 #pragma unroll
@@ -257,15 +418,121 @@ k_adj_field(const double* __restrict__ u, const double* __restrict__ kbar, doubl
                 lin += adv;
             }
             r = fma(kscale, lin, r);
-            const double kq = kscale * kf[0];
+            // the shift's adjoint from this point's own advection terms (none
+            // on a face plane, whose RHS the radial condition replaces)
+            bool own = true;
+            if constexpr (Closed) own = !face_point(G, c.ix);
+            if (own) {
+                const double kq = kscale * kf[0];
 #pragma unroll
-            for (int a = 0; a < 3; ++a)
-                shift_bar[a] = fma(kq, UP1<double, false, false>(u + f * cs + p, G, a, c.ix[a], beta[a]), shift_bar[a]);
+                for (int a = 0; a < 3; ++a)
+                    shift_bar[a] =
+                        fma(kq, UP1<double, Closed, false>(u + f * cs + p, G, a, c.ix[a], beta[a]), shift_bar[a]);
+            }
         }
         ubar[f * cs + p] = r;
     }
 #pragma unroll
     for (int a = 0; a < 3; ++a) ubar[(BX + a) * cs + p] += shift_bar[a];
+}
+
+// Band sources of the mixed-derivative transposes: mbuf_a(f) -= D1_b^T of the
+// c2_ab coefficients at sources in axis b's band (the old sign convention of
+// k_adj_mixed: mbuf holds -(c1_a + sum_b D1_b^T c2_ab)).
+__global__ void __launch_bounds__(kThreads)
+k_adj_band_mixed(const double* __restrict__ coef, double* __restrict__ mbuf, Geo G, Box B) {
+    Pt c;
+    if (!owned_point(G, B, c)) return;
+    const long long cs = G.cs, p = c.p;
+#pragma unroll 1
+    for (int b = 1; b < 3; ++b) {
+        const BandRow br = band_row(G.ax[b], c.ix[b]);
+        if (br.r < 0) continue;
+        const long long s = G.st[b];
+#pragma unroll 1
+        for (int f = 0; f < NMIX; ++f)
+#pragma unroll 1
+            for (int a = 0; a < b; ++a) {
+                const double v = coef[(long long)c2_block(f, sym(a, b)) * cs + p] * G.inv_dx;
+                if (v == 0.0) continue;
+                double* dst = mbuf + (long long)(a * NMIX + f) * cs + p;
+                band_taps(kOpD1, br, [&](int o, double wt) { atomicAdd(dst + o * s, -wt * v); });
+            }
+    }
+}
+
+// Band sources of the field transposes: for each closed axis a whose band
+// holds this point, the first- and second-derivative transposes of its
+// coefficients and, off the face planes, the dissipation and advection
+// transposes of its kbar, each with the row's own weights.
+__global__ void __launch_bounds__(kThreads)
+k_adj_band_field(const double* __restrict__ u, const double* __restrict__ kbar, double kscale,
+                 const double* __restrict__ coef, const double* __restrict__ mbuf, double* __restrict__ ubar, Geo G,
+                 Box B) {
+    Pt c;
+    if (!owned_point(G, B, c)) return;
+    const long long cs = G.cs, p = c.p;
+    const bool face = face_point(G, c.ix);
+#pragma unroll 1
+    for (int a = 0; a < 3; ++a) {
+        const BandRow br = band_row(G.ax[a], c.ix[a]);
+        if (br.r < 0) continue;
+        const long long s = G.st[a];
+        const double beta = u[(BX + a) * cs + p];
+#pragma unroll 1
+        for (int f = 0; f < NCOMP; ++f) {
+            double* dst = ubar + f * cs + p;
+            const int mf = mix_of(f);
+            double v1, v2 = 0.0;   // D1 and D2 transposes' source values (times their factors)
+            if (mf >= 0) {
+                v1 = -mbuf[(long long)(a * NMIX + mf) * cs + p] * G.inv_dx;
+                v2 = coef[(long long)c2_block(mf, sym(a, a)) * cs + p] * G.inv_dx2;
+            } else {
+                const int cb = c1_block(f, a);
+                v1 = cb >= 0 ? coef[(long long)cb * cs + p] * G.inv_dx : 0.0;
+            }
+            double vko = 0.0;
+            if (!face && !(f >= BX && G.zero_shift)) {
+                const double kb = kscale * kbar[f * cs + p];
+                v1 += beta * kb * G.inv_dx;   // advection: the centred D1 rows
+                vko = kb * G.ko_scale;
+            }
+            if (v1 != 0.0) band_taps(kOpD1, br, [&](int o, double wt) { atomicAdd(dst + o * s, wt * v1); });
+            if (v2 != 0.0) band_taps(kOpD2, br, [&](int o, double wt) { atomicAdd(dst + o * s, wt * v2); });
+            if (vko != 0.0) band_taps(kOpKO, br, [&](int o, double wt) { atomicAdd(dst + o * s, wt * vko); });
+        }
+    }
+}
+
+// Transpose of the radial condition on the face planes
+// (JAX_BSSN/evolution/boundaries.py:150-171): k_f = -(x^d D1_d f + f - f_far) / r
+// scatters -kbar_f / r to the point and -kbar_f x^d / r through each axis' D1
+// row.
+__global__ void __launch_bounds__(kThreads)
+k_adj_sommerfeld(const double* __restrict__ kbar, double kscale, double* __restrict__ ubar, Geo G, Box B) {
+    Pt c;
+    if (!owned_point(G, B, c)) return;
+    if (!face_point(G, c.ix)) return;
+    const long long cs = G.cs, p = c.p;
+    double X[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) X[d] = G.ax[d].xmin + G.dx * (double)(c.ix[d] - G.ax[d].org);
+    const double r = sqrt(X[0] * X[0] + X[1] * X[1] + X[2] * X[2]);
+    const double rs = r > 0.0 ? r : 1.0;
+#pragma unroll 1
+    for (int f = 0; f < NCOMP; ++f) {
+        const double kb = kscale * kbar[f * cs + p];
+        if (kb == 0.0) continue;
+        double* dst = ubar + f * cs + p;
+        atomicAdd(dst, -kb / rs);
+#pragma unroll 1
+        for (int d = 0; d < 3; ++d) {
+            const double g = -kb * X[d] / rs * G.inv_dx;
+            const BandRow br = band_row(G.ax[d], c.ix[d]);
+            const long long s = G.st[d];
+            band_taps(kOpD1, br, [&](int o, double wt) { atomicAdd(dst + o * s, wt * g); });
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -374,8 +641,10 @@ struct Plan {
 int validate(const BssnParams* p, const char* where) {
     int st = validate_params(p);
     if (st) return st;
-    for (int f = 0; f < 6; ++f)
-        if (p->bc[f] != 0) return fail(BSSN_ERR_INVALID, std::string(where) + ": the adjoint needs periodic faces");
+    int sommerfeld = 0;
+    for (int f = 0; f < 6; ++f) sommerfeld += p->bc[f] != 0;
+    if (sommerfeld != 0 && sommerfeld != 6)
+        return fail(BSSN_ERR_INVALID, std::string(where) + ": the adjoint needs every face periodic or every face Sommerfeld");
     if (p->kappa != 0.0) return fail(BSSN_ERR_INVALID, std::string(where) + ": the adjoint needs kappa = 0");
     if (p->precision != BSSN_PRECISION_F64)
         return fail(BSSN_ERR_INVALID, std::string(where) + ": the adjoint runs in FP64 arithmetic");
@@ -467,23 +736,34 @@ void step_buffers(const Layout& L, const Plan& P, int n, double* K[4], double* V
 }
 
 // RHS VJP: ubar (= or +=) (dRHS/du)^T kbar at state u; u and kbar ghost-filled.
-cudaError_t rhs_vjp(const double* u, const double* kbar, double kscale, double* ubar, int accumulate, double* coef,
-                    double* d1, const Geo& G, const Box& B, cudaStream_t s) {
+template <bool Closed>
+cudaError_t rhs_vjp_form(const double* u, const double* kbar, double kscale, double* ubar, int accumulate,
+                         double* coef, double* d1, const Geo& G, const Box& B, cudaStream_t s) {
     cudaError_t e = launch_inner_derivs(u, d1, G, B, s);
     if (e != cudaSuccess) return e;
     const unsigned nb = blocks_of(box_threads(G, B));
-    BSSN_LAUNCH(KC_ADJ_POINT, k_adj_point, nb, kThreads, s, u, d1, kbar, kscale, ubar, coef, G, B, point_params(G),
-                accumulate);
+    BSSN_LAUNCH(KC_ADJ_POINT, k_adj_point<Closed>, nb, kThreads, s, u, d1, kbar, kscale, ubar, coef, G, B,
+                point_params(G), accumulate);
     // Stencils read the neighbours of the first-derivative coefficients of K
     // and Gt (blocks 24..26 and 36..44) and of every second-derivative
     // coefficient (45..110); the NMIX fields' first-derivative coefficients
     // are read at their own point only.
     if ((e = fill(coef + (long long)(I_DK - 21) * G.cs, 3, G, s)) != cudaSuccess) return e;
     if ((e = fill(coef + (long long)(I_DGT - 21) * G.cs, NCOEF - (I_DGT - 21), G, s)) != cudaSuccess) return e;
-    BSSN_LAUNCH(KC_ADJ_STENCIL, k_adj_mixed, nb, kThreads, s, coef, d1, G, B);
+    BSSN_LAUNCH(KC_ADJ_STENCIL, k_adj_mixed<Closed>, nb, kThreads, s, coef, d1, G, B);
+    if constexpr (Closed) BSSN_LAUNCH(KC_ADJ_STENCIL, k_adj_band_mixed, nb, kThreads, s, coef, d1, G, B);
     if ((e = fill(d1, 3 * NMIX, G, s)) != cudaSuccess) return e;
-    BSSN_LAUNCH(KC_ADJ_STENCIL, k_adj_field, nb, kThreads, s, u, kbar, kscale, coef, d1, ubar, G, B);
+    BSSN_LAUNCH(KC_ADJ_STENCIL, k_adj_field<Closed>, nb, kThreads, s, u, kbar, kscale, coef, d1, ubar, G, B);
+    if constexpr (Closed) {
+        BSSN_LAUNCH(KC_ADJ_STENCIL, k_adj_band_field, nb, kThreads, s, u, kbar, kscale, coef, d1, ubar, G, B);
+        BSSN_LAUNCH(KC_ADJ_STENCIL, k_adj_sommerfeld, nb, kThreads, s, kbar, kscale, ubar, G, B);
+    }
     return cudaGetLastError();
+}
+cudaError_t rhs_vjp(const double* u, const double* kbar, double kscale, double* ubar, int accumulate, double* coef,
+                    double* d1, const Geo& G, const Box& B, cudaStream_t s) {
+    return G.any_sommerfeld ? rhs_vjp_form<true>(u, kbar, kscale, ubar, accumulate, coef, d1, G, B, s)
+                            : rhs_vjp_form<false>(u, kbar, kscale, ubar, accumulate, coef, d1, G, B, s);
 }
 
 // One forward RK4 step from u_n (owned values) recording the stage states V

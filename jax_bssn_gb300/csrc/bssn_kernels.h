@@ -84,8 +84,8 @@ cudaError_t tune_rhs(const double* u, double* k, const RhsWork& w, const Geo& G,
 
 // First derivatives of the NMIX fields (3 * NMIX blocks of d1, layout
 // d1[(d * NMIX + f) * cs + p]) on the box grown by the reach of the composed
-// mixed derivatives, for an all-periodic FP64 geometry: the inner factors the
-// RHS kernels differentiate again.
+// mixed derivatives (closed axes are not grown), for an FP64 geometry with
+// kappa = 0: the inner factors the RHS kernels differentiate again.
 cudaError_t launch_inner_derivs(const double* u, double* d1, const Geo& G, const Box& box, cudaStream_t stream);
 
 // FP32 form with w.uf already holding the float perturbations of the whole

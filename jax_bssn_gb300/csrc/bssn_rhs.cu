@@ -2741,9 +2741,15 @@ cudaError_t launch_lower_triangle(const double* u, const RhsWork& w, const Lower
 
 cudaError_t launch_inner_derivs(const double* u, double* d1, const Geo& G, const Box& box, cudaStream_t stream) {
     // periodic boxes have no closure rows: the closure-free instantiation
-    // covers the box grown by the composition reach
+    // covers the box grown by the composition reach; with Sommerfeld faces
+    // the closure rows take the general one (closed axes are not grown)
     const BoxSet es = single(grown_box(box, G, composition_reach(G)));
-    BSSN_LAUNCH_SET(KC_FIRST, 0, (k_first_derivs<double, false>), es, stream, u, (const double*)nullptr, d1, G, es, 0);
+    if (G.any_sommerfeld)
+        BSSN_LAUNCH_SET(KC_FIRST, 1, (k_first_derivs<double, true>), es, stream, u, (const double*)nullptr, d1, G, es,
+                        0);
+    else
+        BSSN_LAUNCH_SET(KC_FIRST, 0, (k_first_derivs<double, false>), es, stream, u, (const double*)nullptr, d1, G, es,
+                        0);
     return cudaGetLastError();
 }
 

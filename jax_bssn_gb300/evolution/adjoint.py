@@ -1,4 +1,4 @@
-"""Reverse-mode differentiation of periodic evolutions on the GPU.
+"""Reverse-mode differentiation of BSSN evolutions on the GPU.
 
 The reference has no adjoint of its own: a gradient through its rk4_step
 (JAX_BSSN/evolution/time_evolve.py:144-217) would be jax.grad over XLA's
@@ -15,7 +15,9 @@ reference's seven leaves.  Gradients are taken with respect to these 21
 components; for a symmetric tensor the off-diagonal component's gradient is
 the sum over both halves of a full 3x3 array.
 
-Scope: every face periodic, kappa = 0, no matter sources, FP64 arithmetic.
+Scope: every face periodic, or every face Sommerfeld (the one-sided closure
+rows and the radial face condition are transposed as well); kappa = 0, no
+matter sources, FP64 arithmetic.
 """
 
 from __future__ import annotations
@@ -48,9 +50,9 @@ def leaves(u: torch.Tensor) -> BSSNVariables:
 
 
 def _validate(params: BSSNParameters) -> None:
-    faces = (params.xl_bc, params.xr_bc, params.yl_bc, params.yr_bc, params.zl_bc, params.zr_bc)
-    if any(int(f) for f in faces):
-        raise ValueError("the adjoint evolves periodic grids only (every face code 0)")
+    faces = tuple(int(f) for f in (params.xl_bc, params.xr_bc, params.yl_bc, params.yr_bc, params.zl_bc, params.zr_bc))
+    if faces not in ((0,) * 6, (1,) * 6):
+        raise ValueError("the adjoint needs every face periodic (code 0) or every face Sommerfeld (code 1)")
     if float(params.kappa) != 0.0:
         raise ValueError("the adjoint needs kappa = 0")
     if params.guard_cells or params.owned_shape is not None:
