@@ -217,8 +217,8 @@ int bssn_batch_rk4_monitored(double* states, const BssnPatch* patch, int32_t nin
  * differentiating its rk4_step (JAX_BSSN/evolution/time_evolve.py:144-217)
  * means jax.grad / jax.vjp through XLA.  These entry points are the
  * vector-Jacobian products of the same forward path, on instance batches
- * (layout of bssn_batch_*).  Scope: every face periodic (bc all 0) or every
- * face Sommerfeld (bc all 1: the one-sided closure rows and the radial face
+ * (layout of bssn_batch_*).  Scope: both faces of each axis periodic (bc 0)
+ * or both Sommerfeld (bc 1: the one-sided closure rows and the radial face
  * condition are transposed too), kappa = 0, no matter sources,
  * BSSN_PRECISION_F64, at least 8 samples per axis; anything else returns
  * BSSN_ERR_INVALID.  Adjoint arrays have the

@@ -38,8 +38,8 @@
 // the cheap stage kernels), 2 the stage states as well.  With 1 or 2 the
 // forward pass records the last segment itself.
 // Everything runs on instance batches (layout [component][instance][block]).
-// Scope: every face periodic, or every face Sommerfeld (the band kernels
-// below); kappa = 0, no matter, FP64 arithmetic.
+// Scope: each axis periodic or closed by Sommerfeld faces at both ends (the
+// band kernels below); kappa = 0, no matter, FP64 arithmetic.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -528,9 +528,17 @@ k_adj_sommerfeld(const double* __restrict__ kbar, double kscale, double* __restr
 #pragma unroll 1
         for (int d = 0; d < 3; ++d) {
             const double g = -kb * X[d] / rs * G.inv_dx;
-            const BandRow br = band_row(G.ax[d], c.ix[d]);
+            const Axis& A = G.ax[d];
+            const BandRow br = band_row(A, c.ix[d]);
             const long long s = G.st[d];
-            band_taps(kOpD1, br, [&](int o, double wt) { atomicAdd(dst + o * s, wt * g); });
+            const int L = A.end - A.start;
+            // along a periodic axis a tap beyond the owned samples is the
+            // ghost copy of an owned one: its adjoint goes to that sample
+            band_taps(kOpD1, br, [&](int o, double wt) {
+                int i = c.ix[d] + o;
+                if (!A.lbc && !A.rbc) i = i < A.start ? i + L : (i >= A.end ? i - L : i);
+                atomicAdd(dst + (long long)(i - c.ix[d]) * s, wt * g);
+            });
         }
     }
 }
@@ -641,10 +649,10 @@ struct Plan {
 int validate(const BssnParams* p, const char* where) {
     int st = validate_params(p);
     if (st) return st;
-    int sommerfeld = 0;
-    for (int f = 0; f < 6; ++f) sommerfeld += p->bc[f] != 0;
-    if (sommerfeld != 0 && sommerfeld != 6)
-        return fail(BSSN_ERR_INVALID, std::string(where) + ": the adjoint needs every face periodic or every face Sommerfeld");
+    for (int d = 0; d < 3; ++d)
+        if (p->bc[2 * d] != p->bc[2 * d + 1])
+            return fail(BSSN_ERR_INVALID,
+                        std::string(where) + ": the adjoint needs both faces of an axis periodic or both Sommerfeld");
     if (p->kappa != 0.0) return fail(BSSN_ERR_INVALID, std::string(where) + ": the adjoint needs kappa = 0");
     if (p->precision != BSSN_PRECISION_F64)
         return fail(BSSN_ERR_INVALID, std::string(where) + ": the adjoint runs in FP64 arithmetic");

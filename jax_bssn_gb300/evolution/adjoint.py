@@ -15,9 +15,9 @@ reference's seven leaves.  Gradients are taken with respect to these 21
 components; for a symmetric tensor the off-diagonal component's gradient is
 the sum over both halves of a full 3x3 array.
 
-Scope: every face periodic, or every face Sommerfeld (the one-sided closure
-rows and the radial face condition are transposed as well); kappa = 0, no
-matter sources, FP64 arithmetic.
+Scope: each axis periodic or closed by Sommerfeld faces at both ends (the
+one-sided closure rows and the radial face condition are transposed as well);
+kappa = 0, no matter sources, FP64 arithmetic.
 """
 
 from __future__ import annotations
@@ -51,8 +51,8 @@ def leaves(u: torch.Tensor) -> BSSNVariables:
 
 def _validate(params: BSSNParameters) -> None:
     faces = tuple(int(f) for f in (params.xl_bc, params.xr_bc, params.yl_bc, params.yr_bc, params.zl_bc, params.zr_bc))
-    if faces not in ((0,) * 6, (1,) * 6):
-        raise ValueError("the adjoint needs every face periodic (code 0) or every face Sommerfeld (code 1)")
+    if any(f not in (0, 1) for f in faces) or any(faces[2 * d] != faces[2 * d + 1] for d in range(3)):
+        raise ValueError("the adjoint needs both faces of each axis periodic (code 0) or both Sommerfeld (code 1)")
     if float(params.kappa) != 0.0:
         raise ValueError("the adjoint needs kappa = 0")
     if params.guard_cells or params.owned_shape is not None:

@@ -60,10 +60,12 @@ def _configs():
         ("sommerfeld", [random_smooth_state(shape, seed=s) for s in (6, 7)],
          BSSNParameters(gauge=1, xl_bc=1, xr_bc=1, yl_bc=1, yr_bc=1, zl_bc=1, zr_bc=1,
                         x_min=-0.5, y_min=-0.45, z_min=-0.6, **base)),
+        ("sommerfeld_x_z_periodic_y", [random_smooth_state(shape, seed=8)],
+         BSSNParameters(gauge=1, xl_bc=1, xr_bc=1, zl_bc=1, zr_bc=1, x_min=-0.5, y_min=0.0, z_min=-0.6, **base)),
     ]
 
 
-@pytest.mark.parametrize("case", range(5))
+@pytest.mark.parametrize("case", range(6))
 def test_rhs_vjp_dot_product(cuda, native, case):
     from jax_bssn_gb300.evolution.adjoint import rhs_vjp
     name, states, params = _configs()[case]
@@ -86,7 +88,7 @@ def test_rhs_vjp_dot_product(cuda, native, case):
     print(name, "rhs vjp worst", f"{worst:.2e}")
 
 
-@pytest.mark.parametrize("case", (0, 4))
+@pytest.mark.parametrize("case", (0, 4, 5))
 def test_rk4_step_vjp_dot_product(cuda, native, case):
     from jax_bssn_gb300.evolution import BatchEvolution
     from jax_bssn_gb300.evolution.adjoint import CheckpointedEvolution, components, leaves
@@ -258,7 +260,7 @@ def test_adjoint_rejects_unsupported_configurations(cuda, native):
     from jax_bssn_gb300 import BSSNParameters
     from jax_bssn_gb300.evolution.adjoint import rhs_vjp
     u = torch.zeros((21, 1, 10, 10, 10), dtype=torch.float64, device="cuda")
-    with pytest.raises(ValueError, match="periodic"):
+    with pytest.raises(ValueError, match="both faces"):
         rhs_vjp(u, u, BSSNParameters(dx=0.1, xl_bc=1))
     with pytest.raises(ValueError, match="kappa"):
         rhs_vjp(u, u, BSSNParameters(dx=0.1, kappa=0.1))
