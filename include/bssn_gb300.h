@@ -271,15 +271,16 @@ int bssn_tune_patch(double* states, const BssnPatch* patch, int32_t ninst, const
                     void* workspace, size_t workspace_bytes, char* report, size_t report_bytes, void* stream);
 
 /* No reference counterpart: the float forms' TMA-staged kernels.  On the box
- * interior, where the geometry allows it -- a z pitch (nz + 2 ghost) that is a
- * multiple of four, no MAD axis, kappa = 0 for all but the gauge RHS, vacuum
- * for the curvature RHS -- the gauge RHS (dt gt, W, alpha, beta;
- * BSSN_TMA_GAUGE), the first derivatives (BSSN_TMA_DERIVS), dt At
+ * interior, and where every closed axis has Sommerfeld faces at both ends also
+ * on the rows next to them, where the geometry allows it -- a z pitch
+ * (nz + 2 ghost) that is a multiple of four, no MAD axis, kappa = 0 for all
+ * but the gauge RHS, vacuum for the curvature RHS -- the gauge RHS (dt gt, W,
+ * alpha, beta; BSSN_TMA_GAUGE), the first derivatives (BSSN_TMA_DERIVS), dt At
  * (BSSN_TMA_AT) and dt K with dt Gt (BSSN_TMA_KGT) can run from TMA-staged
  * shared-memory tiles instead of the generic kernels.  `kernels` is the mask
  * of those to use (default BSSN_TMA_ALL; 0: the generic kernels everywhere);
- * results agree to float rounding.
- * Process-wide; affects later launches and captures. */
+ * results agree to float rounding.  Process-wide; affects later launches and
+ * captures. */
 #define BSSN_TMA_GAUGE 1
 #define BSSN_TMA_DERIVS 2
 #define BSSN_TMA_AT 4

@@ -42,6 +42,7 @@
 //           (large near punctures) is formed in FP64.  The RHS is written in
 //           FP64, and the RK4 combination stays FP64.
 #include <atomic>
+#include <climits>
 #include <cstdint>
 #include <map>
 #include <mutex>
@@ -657,9 +658,12 @@ k_first_derivs_tma(const __grid_constant__ CUtensorMap map, float* __restrict__ 
 // The RHS is linear in every one of these, so each box is folded into a few
 // accumulators as soon as it is read; the pointwise terms are formed from
 // single-sample reads while the first boxes load, and wait in registers
-// (gauge) or shared memory (curvature).  Same terms as the generic kernels'
-// interior instantiation (closure-free, no MAD axis; the curvature RHS for
-// kappa = 0 in vacuum), regrouped.
+// (gauge) or shared memory (curvature).  With Sommerfeld faces closed at both
+// ends of every closed axis the kernels also take the two rows next to each
+// face, with the forward's one-sided rows (d1_row, d2_row, ko_row) and box
+// origins lowered at the upper faces; the face planes stay the radial
+// condition's.  Same terms as the generic kernels (no MAD axis; the curvature
+// RHS for kappa = 0 in vacuum), regrouped.
 // ---------------------------------------------------------------------------
 namespace tma {
 constexpr int AZ = 32, AY = 4, AX = 4;                    // tile; one sample per thread
@@ -729,36 +733,134 @@ __device__ __forceinline__ float d2_box(const float* s, int st) {   // units of 
 __device__ __forceinline__ float d1_box(const float* s, int st, float a1, float a2) {
     return (s[st] - s[-st]) * a1 + (s[2 * st] - s[-2 * st]) * a2;
 }
+// Rows next to a Sommerfeld face, by row code: +1 / +2 the second / third
+// sample from the lower face, -1 / -2 from the upper one, 0 elsewhere (the
+// face plane itself is the radial condition's).  As the forward's float
+// closures: one-sided D1 and D2 on rows 1, one-sided sixth differences on
+// rows 1-2, in differences to the centre (each row's weights sum to zero);
+// the upper face mirrors the lower (D1 changes sign).
+__device__ __forceinline__ float d1_row(const float* s, int st, int code, float a1, float a2, float inv_dx) {
+    if (code == 1 || code == -1) {   // {-1/4, -5/6, 3/2, -1/2, 1/12} at -1..3
+        const int t = code * st;
+        const float f0 = s[0];
+        const float v = ((-0.25f * (s[-t] - f0) + 1.5f * (s[t] - f0)) + -0.5f * (s[2 * t] - f0))
+                        + (1.0f / 12.0f) * (s[3 * t] - f0);
+        return (code > 0 ? v : -v) * inv_dx;
+    }
+    return d1_box(s, st, a1, a2);
+}
+__device__ __forceinline__ float d2_row(const float* s, int st, int code, float i12, float inv_dx2) {
+    if (code == 1 || code == -1) {   // {5/6, -5/4, -1/3, 7/6, -1/2, 1/12} at -1..4
+        const int t = code * st;
+        const float f0 = s[0];
+        const float v = ((5.0f / 6.0f) * (s[-t] - f0) + (-1.0f / 3.0f) * (s[t] - f0))
+                        + ((7.0f / 6.0f) * (s[2 * t] - f0) + -0.5f * (s[3 * t] - f0)) + (1.0f / 12.0f) * (s[4 * t] - f0);
+        return v * inv_dx2;
+    }
+    return d2_box(s, st) * i12;
+}
+// Sixth-difference numerator on rows +-1 ({3, -20, 57, -90, 85, -48, 15, -2}
+// at -1..6) and +-2 ({2, -13, 36, -55, 50, -27, 8, -1} at -2..5).
+__device__ __forceinline__ float ko_row(const float* s, int st, int code) {
+    const int t = (code > 0 ? 1 : -1) * st;
+    const float f0 = s[0];
+    auto d = [&](int o) { return s[o * t] - f0; };
+    if (code == 1 || code == -1)
+        return ((3.0f * d(-1) + 57.0f * d(1)) + (-90.0f * d(2) + 85.0f * d(3)))
+               + ((-48.0f * d(4) + 15.0f * d(5)) + -2.0f * d(6));
+    return ((2.0f * d(-2) + -13.0f * d(-1)) + (-55.0f * d(1) + 50.0f * d(2)))
+           + ((-27.0f * d(3) + 8.0f * d(4)) + -1.0f * d(5));
+}
 // Shared-memory strides and this thread's centre in each box kind.
 constexpr int V2X = AHZ * (AY + 4), V3X = AHZ * (AY + 6), SYB = AHZ;
+
+// Where a box of kind `kind` starts relative to the tile origin (x0, y0, z0):
+// halo 2 or 3 below the tile in x and y, 4 in z (a 16-byte origin).  A tile
+// that holds the rows next to an upper Sommerfeld face starts its boxes
+// lower, far enough for those rows' one-sided stencils (they reach 4 below
+// the face in D1 and mixed D1, 5 in D2, 7 in the sixth difference); the box
+// sizes still cover every valid sample's taps above.
+__device__ __forceinline__ int upper_face_in(const Axis& A, int t0, int T, int blo, int bhi) {
+    if (!A.rbc) return INT_MIN;
+    const int xf = A.end - 1;
+    const int lo = max(t0, max(xf - 2, blo)), hi = min(t0 + T - 1, min(xf - 1, bhi - 1));
+    return lo <= hi ? xf : INT_MIN;
+}
+__device__ __forceinline__ void box_origin(int kind, int x0, int y0, int z0, const Geo& G, const Box& B, int& ox, int& oy,
+                                           int& oz) {
+    const int hx = (a_hx(kind) - AX) / 2, hy = (a_hy(kind) - AY) / 2;
+    const int reach = kind == kBoxV3 ? 7 : (kind == kBoxV2 ? 5 : 4);   // below an upper face
+    ox = -hx;
+    oy = -hy;
+    oz = -4;
+    int f = hx ? upper_face_in(G.ax[0], x0, AX, B.lo[0], B.lo[0] + B.n[0]) : INT_MIN;
+    if (f != INT_MIN) ox = min(ox, f - reach - x0);
+    f = hy ? upper_face_in(G.ax[1], y0, AY, B.lo[1], B.lo[1] + B.n[1]) : INT_MIN;
+    if (f != INT_MIN) oy = min(oy, f - reach - y0);
+    f = upper_face_in(G.ax[2], z0, AZ, B.lo[2], B.lo[2] + B.n[2]);
+    if (f != INT_MIN && f - reach - z0 < oz) oz = -((z0 - (f - reach) + 3) & ~3);
+}
+// Row code of index c along A (see d1_row): the upper face is checked first,
+// as the forward's closures do.
+__device__ __forceinline__ int row_code(const Axis& A, int c) {
+    if (A.rbc) {
+        const int r = A.end - 1 - c;
+        if (r == 1 || r == 2) return -r;
+    }
+    if (A.lbc) {
+        const int r = c - A.start;
+        if (r == 1 || r == 2) return r;
+    }
+    return 0;
+}
 
 // The ring of one CTA: box ti is taken (its wait may give up: `missing`),
 // read, and given back, after which its slot loads box ti + ANBUF.  give()
 // is the CTA's one barrier per box; when any wait of the CTA gave up, the
 // copies in flight get one more bounded wait and give() returns false, and
-// the CTA leaves.
+// the CTA leaves.  Stencils near Sommerfeld faces take the rows of this
+// sample's row codes (codes, three fields of 3 bits).
 template <int Seq>
 struct BoxRing {
     const CurvMaps* maps;
+    const Geo* G;
+    const Box* B;
     float* ring;
     unsigned long long* bars;
     int* timeouts;
     int ntile, paired, nfield, z0, y0, x0, inst, t;
     int cV2, cDX, cDY, cV3;
+    int codes;
     int ti;
     bool missing;
 
+    __device__ __forceinline__ int code(int d) const { return ((codes >> (3 * d)) & 7) - 2; }
     __device__ __forceinline__ void issue(int i) {
         const CurvTile tl = seq_tile<Seq>(i, paired, nfield);
         const int b = i % ANBUF;
-        load_box(ring + b * (A_SLOT / 4), &maps->map[tl.kind], z0 - 4, y0 - (a_hy(tl.kind) - AY) / 2,
-                 x0 - (a_hx(tl.kind) - AX) / 2, inst, tl.comp, &bars[b], a_bytes(tl.kind));
+        int ox, oy, oz;
+        box_origin(tl.kind, x0, y0, z0, *G, *B, ox, oy, oz);
+        load_box(ring + b * (A_SLOT / 4), &maps->map[tl.kind], z0 + oz, y0 + oy, x0 + ox, inst, tl.comp, &bars[b],
+                 a_bytes(tl.kind));
     }
-    __device__ __forceinline__ void start(int tz, int ty, int tx) {
-        cV2 = ((tx + 2) * (AY + 4) + (ty + 2)) * AHZ + 4 + tz;
-        cDX = (tx * (AY + 4) + (ty + 2)) * AHZ + 4 + tz;
-        cDY = (tx * AY + ty) * AHZ + 4 + tz;
-        cV3 = ((tx + 3) * (AY + 6) + (ty + 3)) * AHZ + 4 + tz;
+    // A sample outside the box reads (and discards) as if it sat at the tile
+    // origin with interior stencils: a box lowered for an upper face ends too
+    // low for the tile's samples beyond that face.
+    __device__ __forceinline__ void start(int tz, int ty, int tx, bool valid) {
+        const int cx = valid ? x0 + tx : 0, cy = valid ? y0 + ty : 0, cz = valid ? z0 + tz : 0;
+        if (!valid) tx = ty = tz = 0;
+        auto centre = [&](int kind) {
+            int ox, oy, oz;
+            box_origin(kind, x0, y0, z0, *G, *B, ox, oy, oz);
+            return ((tx - ox) * a_hy(kind) + (ty - oy)) * AHZ + (tz - oz);
+        };
+        cV2 = centre(kBoxV2);
+        cDX = centre(kBoxDX);
+        cDY = centre(kBoxDY);
+        cV3 = centre(kBoxV3);
+        codes = valid ? (row_code(G->ax[0], cx) + 2) | ((row_code(G->ax[1], cy) + 2) << 3)
+                            | ((row_code(G->ax[2], cz) + 2) << 6)
+                      : 2 | (2 << 3) | (2 << 6);
         ti = 0;
         missing = false;
         if (t == 0) {
@@ -790,44 +892,58 @@ struct BoxRing {
         ++ti;
         return true;
     }
+    // The first derivative along axis d from the centre v of a box whose
+    // stride along d is st.
+    __device__ __forceinline__ float d1(const float* v, int st, int d) const {
+        return d1_row(v, st, code(d), G->gf.d1a, G->gf.d1b, G->gf.inv_dx);
+    }
     // The Hessian h[sym(i,j)] = d_i d_j f of the next Hessian group.
-    __device__ __forceinline__ bool hessian(float (&h)[6], float i12, float a1, float a2) {
+    __device__ __forceinline__ bool hessian(float (&h)[6]) {
+        const float i12 = G->gf.inv_12dx2, idx2 = G->gf.inv_dx2;
         const float* v = take() + cV2;
-        float n0 = d2_box(v, V2X), n3 = d2_box(v, SYB), n5 = d2_box(v, 1);
+        h[0] = d2_row(v, V2X, code(0), i12, idx2);
+        h[3] = d2_row(v, SYB, code(1), i12, idx2);
+        h[5] = d2_row(v, 1, code(2), i12, idx2);
         if (!give()) return false;
         if (paired) {
             v = take() + cV2;
-            n0 += d2_box(v, V2X);
-            n3 += d2_box(v, SYB);
-            n5 += d2_box(v, 1);
+            h[0] += d2_row(v, V2X, code(0), i12, idx2);
+            h[3] += d2_row(v, SYB, code(1), i12, idx2);
+            h[5] += d2_row(v, 1, code(2), i12, idx2);
             if (!give()) return false;
         }
-        h[0] = n0 * i12;
-        h[3] = n3 * i12;
-        h[5] = n5 * i12;
         v = take() + cDX;
-        h[1] = d1_box(v, SYB, a1, a2);
-        h[2] = d1_box(v, 1, a1, a2);
+        h[1] = d1(v, SYB, 1);
+        h[2] = d1(v, 1, 2);
         if (!give()) return false;
         v = take() + cDY;
-        h[4] = d1_box(v, 1, a1, a2);
+        h[4] = d1(v, 1, 2);
         return give();
     }
-    // Advection (upwind by the sign of beta) and the summed sixth-difference
+    // Advection (upwind by the sign of beta; the centred or one-sided D1 on
+    // the rows next to a Sommerfeld face) and the summed sixth-difference
     // numerators of the next halo-3 box, with its first derivatives when asked.
-    __device__ __forceinline__ bool transport(const float (&beta)[3], float inv12, float& adv, float& dis,
-                                              float* d1out = nullptr, float a1 = 0.0f, float a2 = 0.0f) {
+    __device__ __forceinline__ bool transport(const float (&beta)[3], float& adv, float& dis, float* d1out = nullptr) {
+        const float inv12 = G->gf.inv_12dx, a1 = G->gf.d1a, a2 = G->gf.d1b;
         const float* v = take() + cV3;
         float ad[3], di[3];
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             const int st = d == 0 ? V3X : (d == 1 ? SYB : 1);
-            float a[7];
+            const int c = code(d);
+            if (c == 0) {
+                float a[7];
 #pragma unroll
-            for (int o = 0; o < 7; ++o) a[o] = v[(o - 3) * st];
-            ad[d] = beta[d] * inv12 * up1(a, beta[d]);
-            di[d] = ko(a);
-            if (d1out) d1out[d] = (a[4] - a[2]) * a1 + (a[5] - a[1]) * a2;
+                for (int o = 0; o < 7; ++o) a[o] = v[(o - 3) * st];
+                ad[d] = beta[d] * inv12 * up1(a, beta[d]);
+                di[d] = ko(a);
+                if (d1out) d1out[d] = (a[4] - a[2]) * a1 + (a[5] - a[1]) * a2;
+            } else {
+                const float g = d1(v, st, d);
+                ad[d] = beta[d] * g;
+                di[d] = ko_row(v, st, c);
+                if (d1out) d1out[d] = g;
+            }
         }
         adv = (ad[0] + ad[1]) + ad[2];
         dis = (di[0] + di[1]) + di[2];
@@ -860,6 +976,8 @@ k_rhs_at_tma(const __grid_constant__ tma::CurvMaps maps, const float* __restrict
     const bool valid = x < B.lo[0] + B.n[0] && y < B.lo[1] + B.n[1] && z >= B.lo[2] && z < B.lo[2] + B.n[2];
     BoxRing<kSeqAt> R;
     R.maps = &maps;
+    R.G = &G;
+    R.B = &B;
     R.ring = ring;
     R.bars = reinterpret_cast<unsigned long long*>(qbuf + AT_NQ * A_THREADS);
     R.timeouts = timeouts;
@@ -871,7 +989,7 @@ k_rhs_at_tma(const __grid_constant__ tma::CurvMaps maps, const float* __restrict
     R.x0 = x0;
     R.inst = inst;
     R.t = t;
-    R.start(tz, ty, tx);
+    R.start(tz, ty, tx, valid);
 
     // ---- pointwise terms, while the first boxes load ----
     const long long cs = G.cs;
@@ -1003,7 +1121,6 @@ k_rhs_at_tma(const __grid_constant__ tma::CurvMaps maps, const float* __restrict
 
     // ---- the boxes ----
     const float aW = alpha * W, W2 = W * W, aW2 = aW * W;
-    const float i12 = G.gf.inv_12dx2, a1 = G.gf.d1a, a2 = G.gf.d1b;
     float S[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
     float L = 0.0f;   // gt^mn d_m d_n W (stencil parts)
     // Hessians of gt_ij (-1/2 alpha W^2 gt^mn d_m d_n gt_ij), W (alpha W d_i d_j W
@@ -1011,7 +1128,7 @@ k_rhs_at_tma(const __grid_constant__ tma::CurvMaps maps, const float* __restrict
 #pragma unroll 1
     for (int f = 0; f < 8; ++f) {
         float h[6];
-        if (!R.hessian(h, i12, a1, a2)) return;
+        if (!R.hessian(h)) return;
         if (f < 6) {
             const float r = -aW2 * (0.5f * ((gi[0] * h[0] + gi[3] * h[3]) + gi[5] * h[5])
                                     + ((gi[1] * h[1] + gi[2] * h[2]) + gi[4] * h[4]));
@@ -1028,8 +1145,7 @@ k_rhs_at_tma(const __grid_constant__ tma::CurvMaps maps, const float* __restrict
 #pragma unroll
     for (int m = 0; m < 3; ++m) {   // alpha W^2 gt_k(i d_j) Gt^k
         const float* v = R.take() + R.cV2;
-        const float e[3] = {0.5f * aW2 * d1_box(v, V2X, a1, a2), 0.5f * aW2 * d1_box(v, SYB, a1, a2),
-                            0.5f * aW2 * d1_box(v, 1, a1, a2)};
+        const float e[3] = {0.5f * aW2 * R.d1(v, V2X, 0), 0.5f * aW2 * R.d1(v, SYB, 1), 0.5f * aW2 * R.d1(v, 1, 2)};
         if (!R.give()) return;
 #pragma unroll
         for (int i = 0; i < 3; ++i)
@@ -1047,11 +1163,11 @@ k_rhs_at_tma(const __grid_constant__ tma::CurvMaps maps, const float* __restrict
     if (valid)
 #pragma unroll
         for (int d = 0; d < 3; ++d) beta[d] = static_cast<float>(u64[(BX + d) * cs + p]);
-    const float inv12 = G.gf.inv_12dx, scale = G.gf.ko_scale;
+    const float scale = G.gf.ko_scale;
 #pragma unroll 1
     for (int s = 0; s < 6; ++s) {   // advection and dissipation of At_ij
         float adv, dis;
-        if (!R.transport(beta, inv12, adv, dis)) return;
+        if (!R.transport(beta, adv, dis)) return;
         if (valid) k[(AXX + s) * cs + p] = (qbuf[s * A_THREADS + t] + adv) + scale * dis;
     }
 }
@@ -1079,6 +1195,8 @@ k_rhs_kgt_tma(const __grid_constant__ tma::CurvMaps maps, const float* __restric
     const bool valid = x < B.lo[0] + B.n[0] && y < B.lo[1] + B.n[1] && z >= B.lo[2] && z < B.lo[2] + B.n[2];
     BoxRing<kSeqKgt> R;
     R.maps = &maps;
+    R.G = &G;
+    R.B = &B;
     R.ring = ring;
     R.bars = reinterpret_cast<unsigned long long*>(qbuf + KGT_NQ * A_THREADS);
     R.timeouts = timeouts;
@@ -1090,7 +1208,7 @@ k_rhs_kgt_tma(const __grid_constant__ tma::CurvMaps maps, const float* __restric
     R.x0 = x0;
     R.inst = inst;
     R.t = t;
-    R.start(tz, ty, tx);
+    R.start(tz, ty, tx, valid);
 
     // ---- pointwise terms, while the first boxes load ----
     const long long cs = G.cs;
@@ -1188,7 +1306,6 @@ k_rhs_kgt_tma(const __grid_constant__ tma::CurvMaps maps, const float* __restric
     }
 
     // ---- the boxes ----
-    const float i12 = G.gf.inv_12dx2, a1 = G.gf.d1a, a2 = G.gf.d1b;
     float accK = 0.0f;
     float accG[3] = {0.0f, 0.0f, 0.0f};
     float graddiv[3] = {0.0f, 0.0f, 0.0f};   // d_m d_l beta^l
@@ -1196,7 +1313,7 @@ k_rhs_kgt_tma(const __grid_constant__ tma::CurvMaps maps, const float* __restric
 #pragma unroll 1
     for (int f = 0; f < 4; ++f) {
         float h[6];
-        if (!R.hessian(h, i12, a1, a2)) return;
+        if (!R.hessian(h)) return;
         const float c = contract_sym(gi, h);
         if (f == 0) {
             accK = -(W * W) * c;
@@ -1214,10 +1331,10 @@ k_rhs_kgt_tma(const __grid_constant__ tma::CurvMaps maps, const float* __restric
     if (valid)
 #pragma unroll
         for (int d = 0; d < 3; ++d) beta[d] = static_cast<float>(u64[(BX + d) * cs + p]);
-    const float inv12 = G.gf.inv_12dx, scale = G.gf.ko_scale;
+    const float scale = G.gf.ko_scale;
     {   // K: its first derivatives, advection and dissipation
         float adv, dis, dK[3];
-        if (!R.transport(beta, inv12, adv, dis, dK, a1, a2)) return;
+        if (!R.transport(beta, adv, dis, dK)) return;
         if (valid) k[CK * cs + p] = ((accK + qbuf[t]) + adv) + scale * dis;
         const float m43a = (-4.0f / 3.0f) * alpha;
 #pragma unroll
@@ -1229,7 +1346,7 @@ k_rhs_kgt_tma(const __grid_constant__ tma::CurvMaps maps, const float* __restric
 #pragma unroll
     for (int i = 0; i < 3; ++i) {   // Gt^i: advection and dissipation
         float adv, dis;
-        if (!R.transport(beta, inv12, adv, dis)) return;
+        if (!R.transport(beta, adv, dis)) return;
         if (valid) k[(GTX + i) * cs + p] = ((accG[i] + qbuf[(1 + i) * A_THREADS + t]) + adv) + scale * dis;
     }
 }
@@ -1255,6 +1372,8 @@ k_rhs_gauge_tma(const __grid_constant__ tma::CurvMaps maps, const float* __restr
     const bool valid = x < B.lo[0] + B.n[0] && y < B.lo[1] + B.n[1] && z >= B.lo[2] && z < B.lo[2] + B.n[2];
     BoxRing<kSeqGauge> R;
     R.maps = &maps;
+    R.G = &G;
+    R.B = &B;
     R.ring = ring;
     R.bars = reinterpret_cast<unsigned long long*>(ring + ANBUF * (A_SLOT / 4));
     R.timeouts = timeouts;
@@ -1266,7 +1385,7 @@ k_rhs_gauge_tma(const __grid_constant__ tma::CurvMaps maps, const float* __restr
     R.x0 = x0;
     R.inst = inst;
     R.t = t;
-    R.start(tz, ty, tx);
+    R.start(tz, ty, tx, valid);
 
     const long long cs = G.cs;
     const long long p = ((long long)x * G.ax[1].P + y) * G.ax[2].P + z + (long long)inst * G.istride;
@@ -1305,11 +1424,11 @@ k_rhs_gauge_tma(const __grid_constant__ tma::CurvMaps maps, const float* __restr
         for (int i = 0; i < 3; ++i)
             P[MIX_B + i] = G.zero_shift ? 0.0f * beta[i] : G.gf.g * u[(GTX + i) * cs + p] + (-G.gf.eta) * beta[i];
     }
-    const float inv12 = G.gf.inv_12dx, scale = G.gf.ko_scale;
+    const float scale = G.gf.ko_scale;
 #pragma unroll 1
     for (int f = 0; f < NMIX; ++f) {
         float adv, dis;
-        if (!R.transport(beta, inv12, adv, dis)) return;
+        if (!R.transport(beta, adv, dis)) return;
         float pf = P[0];
 #pragma unroll
         for (int q = 1; q < NMIX; ++q) pf = q == f ? P[q] : pf;
@@ -2288,8 +2407,9 @@ EncodeTiled encode_tiled() {
     return fn;
 }
 // default: all four.  At 128^3 the FP32 step took 8.60 ms with the
-// derivatives alone, 8.13 with the At kernel, 7.77 with the K/Gt kernel and
-// 7.34 with the gauge kernel (paired: 10.12, 9.43, 9.01, 8.57 ms).  A gauge
+// derivatives alone, 8.13 with the At kernel, 7.77 with the K/Gt kernel,
+// 7.34 with the gauge kernel and 7.18 with the rows next to the Sommerfeld
+// faces in the boxes (paired: 10.12, 9.43, 9.01, 8.57, 8.35 ms).  A gauge
 // kernel with four samples per thread and 90 KB of shared memory per CTA was
 // faster alone but crowded out the kernels beside it (9.55 against 9.42 ms).
 std::atomic<int> g_tma_mask{kTmaAll};
@@ -2381,6 +2501,24 @@ static bool launch_first_derivs_tma(const float* u, float* d1, const Geo& G, con
         map, d1, G, B, z_base, tiles_z, tiles_y, NMIX, paired, dev.timeouts);
     prof_end(KC_FIRST, stream);
     g_tma_launches.fetch_add(1);
+    return true;
+}
+
+// Whether the TMA box kernels can take the whole box minus its face planes:
+// every axis either without closures (periodic, the box's ghosts filled) or
+// closed by Sommerfeld faces at both ends with the face condition active, the
+// box spanning its owned samples and at least 16 of them (so that the rows
+// next to the two faces never share a tile), and no MAD or reduced axis.
+static bool tma_whole_box(const Geo& G, const Box& box) {
+    if (!G.any_sommerfeld) return false;
+    for (int d = 0; d < 3; ++d) {
+        const Axis& a = G.ax[d];
+        if (a.mad || a.reduced || a.lbc != a.rbc) return false;
+        if (!a.lbc) continue;
+        if (a.slo != 1 || a.shi != 1 || box.lo[d] != a.start || box.lo[d] + box.n[d] != a.end ||
+            a.end - a.start < 16)
+            return false;
+    }
     return true;
 }
 
@@ -2521,13 +2659,21 @@ static void launch_rhs_form(const R* u, const double* u64, double* k, R* d1, R* 
     }
     // gauge: its own branch (b in the FP64 form, c in the FP32 form)
     const cudaStream_t stg = kPerturbative<R> ? stc : stb;
+    // FP32 forms: where every closed axis is closed at both faces, the TMA box
+    // kernels apply the closure rows themselves and take the whole box minus
+    // the face planes, shell included (tma_whole_box)
+    const bool whole = kPerturbative<R> && tma_whole_box(G, box);
+    const BoxSet tma_set = whole ? single(without_faces(G, box)) : sb.interior;
+    BoxSet none;
+    none.n = 0;
     bool gauge_done = false;
     if constexpr (kPerturbative<R>)
-        gauge_done = launch_curv_tma(KC_GAUGE, u, u64, d1, nullptr, nullptr, k, G, sb.interior, nfield, stg);
+        gauge_done = launch_curv_tma(KC_GAUGE, u, u64, d1, nullptr, nullptr, k, G, tma_set, nfield, stg);
     if (!gauge_done)
         BSSN_LAUNCH_SET(KC_GAUGE, 0, (k_rhs_gauge<R, false>), sb.interior, stg, u, u64, d1, k, G, sb.interior,
                         nfield);
-    BSSN_LAUNCH_SET(KC_GAUGE, 1, (k_rhs_gauge<R, true>), sb.shell, stg, u, u64, d1, k, G, sb.shell, nfield);
+    const BoxSet& gauge_shell = gauge_done && whole ? none : sb.shell;
+    BSSN_LAUNCH_SET(KC_GAUGE, 1, (k_rhs_gauge<R, true>), gauge_shell, stg, u, u64, d1, k, G, gauge_shell, nfield);
     // the shell's damping and curvature (pointwise in damp) run beside the
     // interior's: on c (FP64) or after the K/Gt RHS on b (FP32)
     const cudaStream_t sts = kPerturbative<R> ? stb : stc;
@@ -2540,14 +2686,18 @@ static void launch_rhs_form(const R* u, const double* u64, double* k, R* d1, R* 
     if constexpr (kPerturbative<R>) {
         // FP32 form: issue- and latency-bound, so the smaller split kernels run
         // at higher occupancy.
-        if (!launch_curv_tma(KC_KGT, u, u64, d1, dmp, mat, k, G, sb.interior, nfield, stb))
+        const bool kgt_done = launch_curv_tma(KC_KGT, u, u64, d1, dmp, mat, k, G, tma_set, nfield, stb);
+        if (!kgt_done)
             BSSN_LAUNCH_SET(KC_KGT, 0, (k_rhs_kgt<R, false>), sb.interior, stb, u, u64, d1, mat, k, G, sb.interior,
                             nfield);
-        BSSN_LAUNCH_SET(KC_KGT, 1, (k_rhs_kgt<R, true>), sb.shell, stb, u, u64, d1, mat, k, G, sb.shell, nfield);
-        if (!launch_curv_tma(KC_AT, u, u64, d1, dmp, mat, k, G, sb.interior, nfield, stream))
+        const BoxSet& kgt_shell = kgt_done && whole ? none : sb.shell;
+        BSSN_LAUNCH_SET(KC_KGT, 1, (k_rhs_kgt<R, true>), kgt_shell, stb, u, u64, d1, mat, k, G, kgt_shell, nfield);
+        const bool at_done = launch_curv_tma(KC_AT, u, u64, d1, dmp, mat, k, G, tma_set, nfield, stream);
+        if (!at_done)
             BSSN_LAUNCH_SET(KC_AT, 0, (k_rhs_at<R, false>), sb.interior, stream, u, u64, d1, dmp, mat, k, G,
                             sb.interior, nfield);
-        BSSN_LAUNCH_SET(KC_AT, 1, (k_rhs_at<R, true>), sb.shell, sts, u, u64, d1, dmp, mat, k, G, sb.shell, nfield);
+        const BoxSet& at_shell = at_done && whole ? none : sb.shell;
+        BSSN_LAUNCH_SET(KC_AT, 1, (k_rhs_at<R, true>), at_shell, sts, u, u64, d1, dmp, mat, k, G, at_shell, nfield);
     } else {
         BSSN_LAUNCH_SET(KC_CURV, 0, (k_rhs_curv<R, false>), sb.interior, stream, u, u64, d1, dmp, mat, k, G,
                         sb.interior, nfield);

@@ -218,17 +218,21 @@ def test_paired_form_removes_the_second_derivative_rounding(gb):
 
 
 @pytest.mark.parametrize("form", FORMS)
-@pytest.mark.parametrize("faces", ["periodic", "sommerfeld"])
-def test_tma_kernels_match_the_generic_kernels(gb, form, faces):
+@pytest.mark.parametrize("faces,shape", [("periodic", (24, 20, 24)), ("sommerfeld", (24, 20, 24)),
+                                         ("sommerfeld", (23, 22, 20)), ("sommerfeld", (26, 21, 28)),
+                                         ("sommerfeld", (18, 25, 24))])
+def test_tma_kernels_match_the_generic_kernels(gb, form, faces, shape):
     """The FP32 forms' TMA-staged kernels (the gauge RHS, the first
-    derivatives, dt At and dt K with dt Gt of the interior; z pitch a multiple
-    of four: 24 + 8)
-    against the generic kernels on the same state: every RHS leaf equal to
-    float rounding (1e-6 of its scale), with no tile wait given up."""
+    derivatives, dt At and dt K with dt Gt; z pitch a multiple of four) against
+    the generic kernels on the same state: every RHS leaf equal to float
+    rounding (1e-6 of its scale), with no tile wait given up.  With Sommerfeld
+    faces the box kernels also take the rows next to the faces (their
+    one-sided stencils, and at the upper faces lowered box origins): the
+    shapes put those rows at every position within a tile along x and y."""
     pkg, te = gb
     from jax_bssn_gb300 import _native
     from jax_bssn_gb300.initial_data import random_smooth_state
-    state = random_smooth_state((24, 20, 24), seed=8)
+    state = random_smooth_state(shape, seed=8)
     kw = dict(eta=1.5, kappa=0.0, nu=0.05, g=0.75, dx=0.08, dt=0.02, gauge=1)
     if faces == "sommerfeld":
         kw.update(xl_bc=1, xr_bc=1, yl_bc=1, yr_bc=1, zl_bc=1, zr_bc=1, x_min=-1.0, y_min=-0.8, z_min=-0.9)
@@ -251,7 +255,7 @@ def test_tma_kernels_match_the_generic_kernels(gb, form, faces):
         a, b = _np(getattr(tiled, leaf)), _np(getattr(generic, leaf))
         scale = float(np.max(np.abs(b)))
         err = float(np.max(np.abs(a - b))) / scale
-        print(form, faces, leaf, f"{err:.1e}")
+        print(form, faces, shape, leaf, f"{err:.1e}")
         assert err < 1e-6, (leaf, err)
 
 
