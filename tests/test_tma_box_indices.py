@@ -1,0 +1,105 @@
+"""Shared-memory indices of the FP32 TMA box kernels near Sommerfeld faces,
+replayed on the CPU.
+
+The box kernels (jax_bssn_gb300/csrc/bssn_rhs.cu: box_origin, row_code,
+BoxRing::start, d1_row / d2_row / ko_row and the interior stencils) read every
+tap of every thread -- valid or not -- from a shared-memory box whose origin
+is lowered in tiles that hold the rows next to an upper Sommerfeld face.
+This test restates those rules and checks, for every tile and thread of
+several grid shapes (the upper-face rows at every position within a tile),
+that each tap lies inside its box and that every valid sample's taps lie
+inside the padded block.  Samples outside the launch box read as if at the
+tile origin with interior stencils; without that rule the lowered boxes end
+below the tile's samples beyond the face.
+"""
+
+import itertools
+
+import pytest
+
+AZ, AY, AX, AHZ = 32, 4, 4, 40
+# kind: (box extent y, box extent x, reach below an upper face)
+KINDS = {"V2": (AY + 4, AX + 4, 5), "DX": (AY + 4, AX, 4), "DY": (AY, AX, 4), "V3": (AY + 6, AX + 6, 7)}
+# stencils each box kind serves along (x, y, z)
+OPS = {"V2": (("D2", "D1"), ("D2", "D1"), ("D2", "D1")), "DX": ((), ("D1",), ("D1",)), "DY": ((), (), ("D1",)),
+       "V3": (("T",), ("T",), ("T",))}
+
+
+def _upper_face_in(start, end, t0, extent, blo, bhi):
+    xf = end - 1
+    lo, hi = max(t0, xf - 2, blo), min(t0 + extent - 1, xf - 1, bhi - 1)
+    return xf if lo <= hi else None
+
+
+def _origin(kind, tile, axes, box):
+    hy_box, hx_box, reach = KINDS[kind]
+    hx, hy = (hx_box - AX) // 2, (hy_box - AY) // 2
+    x0, y0, z0 = tile
+    ox, oy, oz = -hx, -hy, -4
+    f = _upper_face_in(*axes[0], x0, AX, *box[0]) if hx else None
+    if f is not None:
+        ox = min(ox, f - reach - x0)
+    f = _upper_face_in(*axes[1], y0, AY, *box[1]) if hy else None
+    if f is not None:
+        oy = min(oy, f - reach - y0)
+    f = _upper_face_in(*axes[2], z0, AZ, *box[2])
+    if f is not None and f - reach - z0 < oz:
+        oz = -((z0 - (f - reach) + 3) & ~3)
+    return ox, oy, oz
+
+
+def _row_code(start, end, c):
+    r = end - 1 - c
+    if r in (1, 2):
+        return -r
+    r = c - start
+    return r if r in (1, 2) else 0
+
+
+def _taps(op, code):
+    """Offsets an operator reads along its axis at a row code."""
+    side = 1 if code > 0 else -1
+    if op == "D1":
+        return [side * o for o in (-1, 0, 1, 2, 3)] if abs(code) == 1 else [-2, -1, 1, 2]
+    if op == "D2":
+        return [side * o for o in (-1, 0, 1, 2, 3, 4)] if abs(code) == 1 else [-2, -1, 0, 1, 2]
+    if code == 0:                     # transport window
+        return list(range(-3, 4))
+    ko = (-1, 0, 1, 2, 3, 4, 5, 6) if abs(code) == 1 else (-2, -1, 0, 1, 2, 3, 4, 5)
+    return [side * o for o in ko] + _taps("D1", code)
+
+
+def _out_of_box_taps(n, ghost=4):
+    padded = [m + 2 * ghost for m in n]
+    axes = [(ghost, ghost + m) for m in n]            # owned [start, end)
+    box = [(s + 1, e - 1) for s, e in axes]           # without the face planes
+    z_base = box[2][0] & ~3
+    tiles = [range(box[0][0], box[0][1], AX), range(box[1][0], box[1][1], AY), range(z_base, box[2][1], AZ)]
+    bad = 0
+    for tile in itertools.product(*tiles):
+        origins = {k: _origin(k, tile, axes, box) for k in KINDS}
+        for off in itertools.product(range(AX), range(AY), range(AZ)):
+            pos = [t + o for t, o in zip(tile, off)]
+            valid = all(lo <= c < hi for c, (lo, hi) in zip(pos, box))
+            local = off if valid else (0, 0, 0)
+            codes = [_row_code(*axes[d], pos[d]) for d in range(3)] if valid else [0, 0, 0]
+            for kind, (hy_box, hx_box, _) in KINDS.items():
+                o = origins[kind]
+                assert (tile[2] + o[2]) % 4 == 0          # 16-byte box origin in z
+                centre = [local[d] - o[d] for d in range(3)]
+                for d, ops in enumerate(OPS[kind]):
+                    for op in ops:
+                        for t in _taps(op, codes[d]):
+                            ix = list(centre)
+                            ix[d] += t
+                            if not (0 <= ix[0] < hx_box and 0 <= ix[1] < hy_box and 0 <= ix[2] < AHZ):
+                                bad += 1
+                            elif valid:
+                                g = [tile[i] + o[i] + ix[i] for i in range(3)]
+                                assert all(0 <= g[i] < padded[i] for i in range(3))
+    return bad
+
+
+@pytest.mark.parametrize("shape", [(24, 20, 24), (23, 22, 20), (26, 21, 28), (18, 25, 24), (17, 19, 20)])
+def test_box_taps_stay_in_their_boxes(shape):
+    assert _out_of_box_taps(shape) == 0
