@@ -220,7 +220,7 @@ def test_paired_form_removes_the_second_derivative_rounding(gb):
 @pytest.mark.parametrize("form", FORMS)
 @pytest.mark.parametrize("faces,shape", [("periodic", (24, 20, 24)), ("sommerfeld", (24, 20, 24)),
                                          ("sommerfeld", (23, 22, 20)), ("sommerfeld", (26, 21, 28)),
-                                         ("sommerfeld", (18, 25, 24))])
+                                         ("sommerfeld", (18, 25, 24)), ("sommerfeld_x_z", (21, 23, 24))])
 def test_tma_kernels_match_the_generic_kernels(gb, form, faces, shape):
     """The FP32 forms' TMA-staged kernels (the gauge RHS, the first
     derivatives, dt At and dt K with dt Gt; z pitch a multiple of four) against
@@ -236,6 +236,8 @@ def test_tma_kernels_match_the_generic_kernels(gb, form, faces, shape):
     kw = dict(eta=1.5, kappa=0.0, nu=0.05, g=0.75, dx=0.08, dt=0.02, gauge=1)
     if faces == "sommerfeld":
         kw.update(xl_bc=1, xr_bc=1, yl_bc=1, yr_bc=1, zl_bc=1, zr_bc=1, x_min=-1.0, y_min=-0.8, z_min=-0.9)
+    elif faces == "sommerfeld_x_z":   # y periodic: the boxes wrap through its filled ghosts
+        kw.update(xl_bc=1, xr_bc=1, zl_bc=1, zr_bc=1, x_min=-1.0, y_min=0.0, z_min=-0.9)
     params = pkg.BSSNParameters(**kw)
     _, before = _native.tma_status()
     with pkg.arithmetic(form):
