@@ -738,38 +738,50 @@ __device__ __forceinline__ float d1_box(const float* s, int st, float a1, float 
 // face plane itself is the radial condition's).  As the forward's float
 // closures: one-sided D1 and D2 on rows 1, one-sided sixth differences on
 // rows 1-2, in differences to the centre (each row's weights sum to zero);
-// the upper face mirrors the lower (D1 changes sign).
+// the upper face mirrors the lower (D1 changes sign).  The centred taps are
+// read by every sample first, so in a warp that mixes rows only the one-sided
+// rows' outer taps and sums diverge.
 __device__ __forceinline__ float d1_row(const float* s, int st, int code, float a1, float a2, float inv_dx) {
+    const float m2 = s[-2 * st], m1 = s[-st], p1 = s[st], p2 = s[2 * st];
     if (code == 1 || code == -1) {   // {-1/4, -5/6, 3/2, -1/2, 1/12} at -1..3
-        const int t = code * st;
         const float f0 = s[0];
-        const float v = ((-0.25f * (s[-t] - f0) + 1.5f * (s[t] - f0)) + -0.5f * (s[2 * t] - f0))
-                        + (1.0f / 12.0f) * (s[3 * t] - f0);
+        const float b1 = code > 0 ? m1 : p1, f1 = code > 0 ? p1 : m1, f2 = code > 0 ? p2 : m2;
+        const float f3 = s[3 * code * st];
+        const float v = ((-0.25f * (b1 - f0) + 1.5f * (f1 - f0)) + -0.5f * (f2 - f0)) + (1.0f / 12.0f) * (f3 - f0);
         return (code > 0 ? v : -v) * inv_dx;
     }
-    return d1_box(s, st, a1, a2);
+    return (p1 - m1) * a1 + (p2 - m2) * a2;
 }
 __device__ __forceinline__ float d2_row(const float* s, int st, int code, float i12, float inv_dx2) {
+    const float f0 = s[0], m2 = s[-2 * st], m1 = s[-st], p1 = s[st], p2 = s[2 * st];
     if (code == 1 || code == -1) {   // {5/6, -5/4, -1/3, 7/6, -1/2, 1/12} at -1..4
-        const int t = code * st;
-        const float f0 = s[0];
-        const float v = ((5.0f / 6.0f) * (s[-t] - f0) + (-1.0f / 3.0f) * (s[t] - f0))
-                        + ((7.0f / 6.0f) * (s[2 * t] - f0) + -0.5f * (s[3 * t] - f0)) + (1.0f / 12.0f) * (s[4 * t] - f0);
+        const float b1 = code > 0 ? m1 : p1, f1 = code > 0 ? p1 : m1, f2 = code > 0 ? p2 : m2;
+        const float f3 = s[3 * code * st], f4 = s[4 * code * st];
+        const float v = ((5.0f / 6.0f) * (b1 - f0) + (-1.0f / 3.0f) * (f1 - f0))
+                        + ((7.0f / 6.0f) * (f2 - f0) + -0.5f * (f3 - f0)) + (1.0f / 12.0f) * (f4 - f0);
         return v * inv_dx2;
     }
-    return d2_box(s, st) * i12;
+    return (16.0f * ((p1 - f0) + (m1 - f0)) - ((p2 - f0) + (m2 - f0))) * i12;
 }
 // Sixth-difference numerator on rows +-1 ({3, -20, 57, -90, 85, -48, 15, -2}
-// at -1..6) and +-2 ({2, -13, 36, -55, 50, -27, 8, -1} at -2..5).
-__device__ __forceinline__ float ko_row(const float* s, int st, int code) {
-    const int t = (code > 0 ? 1 : -1) * st;
-    const float f0 = s[0];
-    auto d = [&](int o) { return s[o * t] - f0; };
-    if (code == 1 || code == -1)
-        return ((3.0f * d(-1) + 57.0f * d(1)) + (-90.0f * d(2) + 85.0f * d(3)))
-               + ((-48.0f * d(4) + 15.0f * d(5)) + -2.0f * d(6));
-    return ((2.0f * d(-2) + -13.0f * d(-1)) + (-55.0f * d(1) + 50.0f * d(2)))
-           + ((-27.0f * d(3) + 8.0f * d(4)) + -1.0f * d(5));
+// at -1..6) and +-2 ({2, -13, 36, -55, 50, -27, 8, -1} at -2..5), from the
+// centred window a[k + 3] = f(k) and the taps beyond it.
+__device__ __forceinline__ float ko_row(const float (&a)[7], const float* s, int st, int code) {
+    const bool up = code > 0;
+    const int sg = up ? 1 : -1;
+    const float f0 = a[3];
+    // w(o) = f(sg o) - f0 for |o| <= 3, with compile-time window indices
+    auto w = [&](int o) {
+        const float lo = o == -2 ? a[1] : (o == -1 ? a[2] : (o == 1 ? a[4] : (o == 2 ? a[5] : a[6])));
+        const float hi = o == -2 ? a[5] : (o == -1 ? a[4] : (o == 1 ? a[2] : (o == 2 ? a[1] : a[0])));
+        return (up ? lo : hi) - f0;
+    };
+    const float e4 = s[4 * sg * st] - f0, e5 = s[5 * sg * st] - f0;
+    if (code == 1 || code == -1) {
+        const float e6 = s[6 * sg * st] - f0;
+        return ((3.0f * w(-1) + 57.0f * w(1)) + (-90.0f * w(2) + 85.0f * w(3))) + ((-48.0f * e4 + 15.0f * e5) + -2.0f * e6);
+    }
+    return ((2.0f * w(-2) + -13.0f * w(-1)) + (-55.0f * w(1) + 50.0f * w(2))) + ((-27.0f * w(3) + 8.0f * e4) + -1.0f * e5);
 }
 // Shared-memory strides and this thread's centre in each box kind.
 constexpr int V2X = AHZ * (AY + 4), V3X = AHZ * (AY + 6), SYB = AHZ;
@@ -931,17 +943,27 @@ struct BoxRing {
         for (int d = 0; d < 3; ++d) {
             const int st = d == 0 ? V3X : (d == 1 ? SYB : 1);
             const int c = code(d);
-            if (c == 0) {
-                float a[7];
+            float a[7];
 #pragma unroll
-                for (int o = 0; o < 7; ++o) a[o] = v[(o - 3) * st];
+            for (int o = 0; o < 7; ++o) a[o] = v[(o - 3) * st];
+            if (c == 0) {
                 ad[d] = beta[d] * inv12 * up1(a, beta[d]);
                 di[d] = ko(a);
                 if (d1out) d1out[d] = (a[4] - a[2]) * a1 + (a[5] - a[1]) * a2;
             } else {
-                const float g = d1(v, st, d);
+                // the centred D1 on rows +-2, the one-sided one on rows +-1
+                float g = (a[4] - a[2]) * a1 + (a[5] - a[1]) * a2;
+                if (c == 1 || c == -1) {
+                    const bool up = c > 0;
+                    const float f0 = a[3];
+                    const float b1 = up ? a[2] : a[4], f1 = up ? a[4] : a[2], f2 = up ? a[5] : a[1],
+                                f3 = up ? a[6] : a[0];
+                    const float u1 = ((-0.25f * (b1 - f0) + 1.5f * (f1 - f0)) + -0.5f * (f2 - f0))
+                                     + (1.0f / 12.0f) * (f3 - f0);
+                    g = (c > 0 ? u1 : -u1) * G->gf.inv_dx;
+                }
                 ad[d] = beta[d] * g;
-                di[d] = ko_row(v, st, c);
+                di[d] = ko_row(a, v, st, c);
                 if (d1out) d1out[d] = g;
             }
         }

@@ -57,16 +57,18 @@ def _row_code(start, end, c):
 
 
 def _taps(op, code):
-    """Offsets an operator reads along its axis at a row code."""
+    """Offsets an operator reads along its axis at a row code: the centred
+    taps always (every sample reads them first), and on the one-sided rows the
+    outer taps beyond them."""
     side = 1 if code > 0 else -1
     if op == "D1":
-        return [side * o for o in (-1, 0, 1, 2, 3)] if abs(code) == 1 else [-2, -1, 1, 2]
+        return [-2, -1, 1, 2] + ([0, 3 * side] if abs(code) == 1 else [])
     if op == "D2":
-        return [side * o for o in (-1, 0, 1, 2, 3, 4)] if abs(code) == 1 else [-2, -1, 0, 1, 2]
-    if code == 0:                     # transport window
-        return list(range(-3, 4))
-    ko = (-1, 0, 1, 2, 3, 4, 5, 6) if abs(code) == 1 else (-2, -1, 0, 1, 2, 3, 4, 5)
-    return [side * o for o in ko] + _taps("D1", code)
+        return [-2, -1, 0, 1, 2] + ([3 * side, 4 * side] if abs(code) == 1 else [])
+    window = list(range(-3, 4))       # transport: the centred 7-tap window
+    if code == 0:
+        return window
+    return window + [side * o for o in ((4, 5, 6) if abs(code) == 1 else (4, 5))]
 
 
 def _out_of_box_taps(n, ghost=4):
