@@ -477,6 +477,14 @@ constexpr long long kWaitLimit = 1LL << 24;              // try_wait polls befor
 static_assert(TX * TY * (TZ / 4) == THREADS, "one thread per four z samples");
 
 __device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+// A global load the compiler may not merge with an earlier load of the same
+// address: re-reading a value (an L1 hit) instead of holding it in a register
+// across a phase that would spill.
+__device__ __forceinline__ float reload(const float* q) {
+    float v;
+    asm volatile("ld.global.nc.f32 %0, [%1];" : "=f"(v) : "l"(q));
+    return v;
+}
 
 __device__ __forceinline__ void bar_init(unsigned long long* bar) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
@@ -1025,6 +1033,42 @@ k_rhs_at_tma(const __grid_constant__ tma::CurvMaps maps, const float* __restrict
         W = static_cast<float>(u64[CW * cs + p]);
         alpha = static_cast<float>(u64[CALPHA * cs + p]);
         const float aW = alpha * W, W2 = W * W, aW2 = aW * W;
+        // alpha K At_ij - 2 alpha At_ik gt^kl At_lj + Lie terms - 2/3 At_ij div
+        // beta first, parked in shared memory (volatile, so that none of it
+        // stays in registers across the Christoffel rows)
+        volatile float* Q = qbuf + t;
+        {
+        const float K = static_cast<float>(u64[CK * cs + p]);
+        float A[6];
+#pragma unroll
+        for (int s = 0; s < 6; ++s) A[s] = u[(AXX + s) * cs + p];
+        float db[3][3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) db[i][j] = d1[((long long)(j * nfield + MIX_B + i)) * cs + p];
+        const float div = db[0][0] + db[1][1] + db[2][2];
+        float M[3][3];   // M[k][j] = gt^kl At_lj
+#pragma unroll
+        for (int kk = 0; kk < 3; ++kk)
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+                M[kk][j] = gi[sym(kk, 0)] * A[sym(0, j)] + gi[sym(kk, 1)] * A[sym(1, j)] + gi[sym(kk, 2)] * A[sym(2, j)];
+        const float aK = alpha * K, m2a = -2.0f * alpha, m23div = (-2.0f / 3.0f) * div;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = i; j < 3; ++j) {
+                float AgA = 0.0f, lie = 0.0f;
+#pragma unroll
+                for (int kk = 0; kk < 3; ++kk) {
+                    AgA += A[sym(i, kk)] * M[kk][j];
+                    lie += A[sym(kk, i)] * db[kk][j] + A[sym(kk, j)] * db[kk][i];
+                }
+                const int s = sym(i, j);
+                Q[s * A_THREADS] = (aK * A[s] + m2a * AgA) + lie + m23div * A[s];
+            }
+        }
         float PT[6];   // pointwise part of [alpha W^2 R_ij - W^2 D_i D_j alpha]
         {
             float c1[3][6];
@@ -1066,27 +1110,42 @@ k_rhs_at_tma(const __grid_constant__ tma::CurvMaps maps, const float* __restrict
 #pragma unroll
                 for (int s = 0; s < 6; ++s)
                     c2k[s] = gi[sym(kk, 0)] * c1[0][s] + gi[sym(kk, 1)] * c1[1][s] + gi[sym(kk, 2)] * c1[2][s];
-                float X[3][3];
-#pragma unroll
-                for (int a = 0; a < 3; ++a)
-#pragma unroll
-                    for (int b = 0; b < 3; ++b)
-                        X[a][b] = gi[sym(0, a)] * c2k[sym(0, b)] + gi[sym(1, a)] * c2k[sym(1, b)]
-                                  + gi[sym(2, a)] * c2k[sym(2, b)];
                 gicW += dW[kk] * contract_sym(gi, c2k);
                 const float ck = W2 * da[kk] - aW * dW[kk];
+                // X[n][b] = gt^na Gamma^k_ab, one column b at a time (three
+                // columns live instead of nine).
+                auto xcol = [&](int b, float (&xc)[3]) {
 #pragma unroll
-                for (int i = 0; i < 3; ++i)
+                    for (int n = 0; n < 3; ++n)
+                        xc[n] = gi[sym(0, n)] * c2k[sym(0, b)] + gi[sym(1, n)] * c2k[sym(1, b)]
+                                + gi[sym(2, n)] * c2k[sym(2, b)];
+                };
+#pragma unroll
+                for (int i = 0; i < 3; ++i) {
+                    float xi[3];
+                    xcol(i, xi);
 #pragma unroll
                     for (int j = i; j < 3; ++j) {
+                        float xj[3];
+                        if (j == i) {
+#pragma unroll
+                            for (int n = 0; n < 3; ++n) xj[n] = xi[n];
+                        } else {
+                            xcol(j, xj);
+                        }
                         float acc = 0.0f;
 #pragma unroll
                         for (int n = 0; n < 3; ++n)
-                            acc += X[n][i] * (c1[j][sym(kk, n)] + c1[kk][sym(j, n)]) + X[n][j] * c1[i][sym(kk, n)];
+                            acc += xi[n] * (c1[j][sym(kk, n)] + c1[kk][sym(j, n)]) + xj[n] * c1[i][sym(kk, n)];
                         const int s = sym(i, j);
                         PT[s] += aW2 * acc + c2k[s] * ck;
                     }
+                }
             }
+            // gt_ij is read again (an L1 hit) rather than held across the
+            // Christoffel rows
+#pragma unroll
+            for (int s = 0; s < 6; ++s) g[s] = reload(u + (GXX + s) * cs + p) + (unit_diagonal(s) ? 1.0f : 0.0f);
             float grad2 = 0.0f, gw = 0.0f;   // gt^mn d_m W d_n W, gt^mn d_m W d_n alpha
 #pragma unroll
             for (int n = 0; n < 3; ++n) {
@@ -1104,38 +1163,8 @@ k_rhs_at_tma(const __grid_constant__ tma::CurvMaps maps, const float* __restrict
                 }
         }
         const float trP = contract_sym(gi, PT);
-        // alpha K At_ij - 2 alpha At_ik gt^kl At_lj + Lie terms - 2/3 At_ij div beta
-        const float K = static_cast<float>(u64[CK * cs + p]);
-        float A[6];
 #pragma unroll
-        for (int s = 0; s < 6; ++s) A[s] = u[(AXX + s) * cs + p];
-        float db[3][3];
-#pragma unroll
-        for (int i = 0; i < 3; ++i)
-#pragma unroll
-            for (int j = 0; j < 3; ++j) db[i][j] = d1[((long long)(j * nfield + MIX_B + i)) * cs + p];
-        const float div = db[0][0] + db[1][1] + db[2][2];
-        float M[3][3];   // M[k][j] = gt^kl At_lj
-#pragma unroll
-        for (int kk = 0; kk < 3; ++kk)
-#pragma unroll
-            for (int j = 0; j < 3; ++j)
-                M[kk][j] = gi[sym(kk, 0)] * A[sym(0, j)] + gi[sym(kk, 1)] * A[sym(1, j)] + gi[sym(kk, 2)] * A[sym(2, j)];
-        const float aK = alpha * K, m2a = -2.0f * alpha, m23div = (-2.0f / 3.0f) * div;
-#pragma unroll
-        for (int i = 0; i < 3; ++i)
-#pragma unroll
-            for (int j = i; j < 3; ++j) {
-                float AgA = 0.0f, lie = 0.0f;
-#pragma unroll
-                for (int kk = 0; kk < 3; ++kk) {
-                    AgA += A[sym(i, kk)] * M[kk][j];
-                    lie += A[sym(kk, i)] * db[kk][j] + A[sym(kk, j)] * db[kk][i];
-                }
-                const int s = sym(i, j);
-                qbuf[s * A_THREADS + t] =
-                    (PT[s] - (1.0f / 3.0f) * g[s] * trP) + ((aK * A[s] + m2a * AgA) + lie + m23div * A[s]);
-            }
+        for (int s = 0; s < 6; ++s) Q[s * A_THREADS] += PT[s] - (1.0f / 3.0f) * g[s] * trP;
     } else {
 #pragma unroll
         for (int s = 0; s < AT_NQ; ++s) qbuf[s * A_THREADS + t] = 0.0f;
