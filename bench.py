@@ -98,7 +98,7 @@ LEAVES = ("conformal_metric", "conformal_factor", "traceless_K", "trace_K", "con
 # the points of a launch, so a launch's traffic is this times its points.
 MEASURED_TRAFFIC = {
     ("teukolsky", "fp64", "rhs_curv"): (1221, "profiles/traffic_full_size.md (one RK4 step at 128^3)"),
-    ("teukolsky", "fp32", "rhs_at"): (491, "profiles/traffic_full_size.md (the FP32 run of the bench at 128^3)"),
+    ("teukolsky", "fp32", "rhs_at"): (410, "profiles/traffic_full_size.md (the FP32 run of the bench at 128^3)"),
     ("fmr", "fp64", "rhs_curv"): (906, "profiles/traffic_full_size.md (one RK4 step, 96^3 + 65^3 + 49^3)"),
     ("fmr", "fp32", "rhs_at"): (534, "profiles/traffic_full_size.md (one RK4 step, 96^3 + 65^3 + 49^3)"),
     ("axisymmetric", "fp64", "cartoon"): (1472, "profiles/traffic_full_size.md (one RK4 step, 256 x 512)"),
