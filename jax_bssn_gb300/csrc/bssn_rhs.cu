@@ -518,12 +518,14 @@ __device__ __forceinline__ float at(const float4& v, int j) { return j == 0 ? v.
 }  // namespace tma
 
 // ---------------------------------------------------------------------------
-// FP32 forms, interior first derivatives of the NMIX fields from TMA tiles:
-// the same 32 x 8 x 4 tiles and four z samples per thread as the gauge
-// kernel, halo 2 in x and y (4 in z for the 16-byte rule), a three-deep ring
-// of 40 x 12 x 8 boxes.  The paired form streams each field's low word too
-// (the low words follow the 21 perturbations, so one tensor map of 32
-// components covers both).  Closure-free, no MAD axis, kappa = 0.
+// FP32 forms, first derivatives of the NMIX fields from TMA tiles: 32 x 8 x 4
+// tiles with four z samples per thread, halo 2 in x and y (4 in z for the
+// 16-byte rule), a three-deep ring of 40 x 12 x 8 boxes.  The paired form
+// streams each field's low word too (the low words follow the 21
+// perturbations, so one tensor map of 32 components covers both).  No MAD
+// axis, kappa = 0.  Either the closure-free interior, or (where every closed
+// axis is Sommerfeld at both ends) the whole box with the two D1 closure rows
+// next to each face, face planes included.
 // ---------------------------------------------------------------------------
 namespace tma {
 constexpr int DHZ = TZ + 8, DHY = TY + 4, DHX = TX + 4;        // 40 x 12 x 8
@@ -533,6 +535,41 @@ constexpr unsigned DFIELD_BYTES = DFIELD * 4;                  // 15360 (a multi
 constexpr int DNBUF = 3;
 constexpr size_t DSMEM = (size_t)DNBUF * DFIELD_BYTES + DNBUF * sizeof(unsigned long long);
 static_assert(DFIELD_BYTES % 128 == 0, "tile buffers must stay 128-byte aligned");
+
+// Closure rows of D1 (the forward's d1_closed): code +1 / -1 the lower / upper
+// face plane, +2 / -2 the row next to it, 0 elsewhere; the upper face first.
+__device__ __forceinline__ int d1_code(const Axis& A, int c) {
+    if (A.rbc) {
+        const int r = A.end - 1 - c;
+        if (r == 0 || r == 1) return -(r + 1);
+    }
+    if (A.lbc) {
+        const int r = c - A.start;
+        if (r == 0 || r == 1) return r + 1;
+    }
+    return 0;
+}
+// D1 on a closure row from its taps counted inward from the face (f1..f4 at
+// 1..4 samples inward, fb one sample outward, on the row next to the face
+// only), in difference form: rows 0 {-25/12, 4, -3, 4/3, -1/4} at 0..4 and 1
+// {-1/4, -5/6, 3/2, -1/2, 1/12} at -1..3; an upper face mirrors them.
+__device__ __forceinline__ float d1_closure(int code, float f0, float f1, float f2, float f3, float fx,
+                                            float inv_dx) {
+    const bool face = code == 1 || code == -1;   // fx is f4 on the face plane, fb on the next row
+    const float v = face ? ((4.0f * (f1 - f0) + -3.0f * (f2 - f0)) + (4.0f / 3.0f) * (f3 - f0)) + -0.25f * (fx - f0)
+                         : ((-0.25f * (fx - f0) + 1.5f * (f1 - f0)) + -0.5f * (f2 - f0)) + (1.0f / 12.0f) * (f3 - f0);
+    return (code > 0 ? v : -v) * inv_dx;
+}
+// Box origin along x or y of a first-derivative tile starting at t0 (T
+// samples): halo 2, lowered in a tile that holds an upper-face closure row so
+// that the face plane's D1 reaches 4 below it (the box of 4 + T samples still
+// covers every valid sample's taps above).
+__device__ __forceinline__ int d1_origin(const Axis& A, int t0, int T, int blo, int bhi) {
+    if (!A.rbc) return -2;
+    const int xf = A.end - 1;
+    const int lo = max(t0, max(xf - 1, blo)), hi = min(t0 + T - 1, min(xf, bhi - 1));
+    return lo <= hi ? min(-2, xf - 4 - t0) : -2;
+}
 
 __device__ __forceinline__ void load_box(float* dst, const CUtensorMap* map, int z, int y, int x, int inst, int comp,
                                          unsigned long long* bar, unsigned bytes) {
@@ -545,6 +582,10 @@ __device__ __forceinline__ void load_box(float* dst, const CUtensorMap* map, int
 }
 }  // namespace tma
 
+// Closed: the box may hold the two D1 closure rows next to Sommerfeld faces
+// (their one-sided rows, the face planes included; box origins lowered at the
+// upper faces); else it is closure-free.
+template <bool Closed>
 __global__ void __launch_bounds__(tma::THREADS)
 k_first_derivs_tma(const __grid_constant__ CUtensorMap map, float* __restrict__ d1, Geo G, Box B, int z_base,
                    int tiles_z, int tiles_y, int nfield, int paired, int* __restrict__ timeouts) {
@@ -560,6 +601,18 @@ k_first_derivs_tma(const __grid_constant__ CUtensorMap map, float* __restrict__ 
     const int tz4 = t & 7, ty = (t >> 3) & 7, tx = t >> 6;
     const int x = x0 + tx, y = y0 + ty, zq = z0 + 4 * tz4;
     const bool col = x >= B.lo[0] && x < B.lo[0] + B.n[0] && y >= B.lo[1] && y < B.lo[1] + B.n[1];
+    // box origins in x and y; a column outside the box reads as if at the
+    // tile origin (a lowered box ends below it)
+    const int ox = Closed ? d1_origin(G.ax[0], x0, TX, B.lo[0], B.lo[0] + B.n[0]) : -2;
+    const int oy = Closed ? d1_origin(G.ax[1], y0, TY, B.lo[1], B.lo[1] + B.n[1]) : -2;
+    const int rx = Closed && !col ? 0 : tx, ry = Closed && !col ? 0 : ty;
+    int code[3][4];   // D1 closure rows (x and y per column, z per sample)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        code[0][j] = Closed && col ? d1_code(G.ax[0], x) : 0;
+        code[1][j] = Closed && col ? d1_code(G.ax[1], y) : 0;
+        code[2][j] = Closed && col ? d1_code(G.ax[2], zq + j) : 0;
+    }
     // as the generic kernel: the derivative along an axis only where the
     // sample lies in that axis' compute range (not in the grown box's ghosts)
     bool write[3][4];
@@ -587,11 +640,16 @@ k_first_derivs_tma(const __grid_constant__ CUtensorMap map, float* __restrict__ 
     __syncthreads();
     if (t == 0)
         for (int i = 0; i < DNBUF && i < ntile; ++i)
-            load_box(ring + i * DFIELD, &map, z0 - 4, y0 - 2, x0 - 2, inst, comp_of(i), &bars[i], DFIELD_BYTES);
+            load_box(ring + i * DFIELD, &map, z0 - 4, y0 + oy, x0 + ox, inst, comp_of(i), &bars[i], DFIELD_BYTES);
     const long long cs = G.cs;
     const long long p0 = ((long long)x * G.ax[1].P + y) * G.ax[2].P + zq + (long long)inst * G.istride;
-    const int base = ((tx + 2) * DHY + (ty + 2)) * DHZ + 4 + 4 * tz4;
-    const float a1 = G.gf.d1a, a2 = G.gf.d1b;
+    const int base = ((rx - ox) * DHY + (ry - oy)) * DHZ + 4 + 4 * tz4;
+    const float a1 = G.gf.d1a, a2 = G.gf.d1b, inv_dx = G.gf.inv_dx;
+    bool closure_x = false, closure_y = false, closure_z = false;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) closure_z = closure_z || code[2][j] != 0;
+    closure_x = code[0][0] != 0;
+    closure_y = code[1][0] != 0;
     float acc[3][4];
     for (int i = 0; i < ntile; ++i) {
         const int b = i % DNBUF;
@@ -610,10 +668,36 @@ k_first_derivs_tma(const __grid_constant__ CUtensorMap map, float* __restrict__ 
             const float w[12] = {m.x, m.y, m.z, m.w, c.x, c.y, c.z, c.w, q.x, q.y, q.z, q.w};
 #pragma unroll
             for (int j = 0; j < 4; ++j) d[2][j] = (w[5 + j] - w[3 + j]) * a1 + (w[6 + j] - w[2 + j]) * a2;
+            if (Closed && closure_z) {
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int c = code[2][j];
+                    if (c == 0) continue;
+                    const bool up = c < 0, face = c == 1 || c == -1;
+                    // taps inward from the face, from the 12-sample window
+                    const float f0 = w[4 + j];
+                    const float f1 = up ? w[3 + j] : w[5 + j], f2 = up ? w[2 + j] : w[6 + j];
+                    const float f3 = up ? w[1 + j] : w[7 + j];
+                    const float fx = face ? (up ? w[j] : w[8 + j]) : (up ? w[5 + j] : w[3 + j]);
+                    d[2][j] = d1_closure(c, f0, f1, f2, f3, fx, inv_dx);
+                }
+            }
         }
 #pragma unroll
         for (int dd = 0; dd < 2; ++dd) {   // x (0), y (1)
             const int st = dd == 0 ? DSX : DSY;
+            const int c = code[dd][0];
+            if (Closed && (dd == 0 ? closure_x : closure_y)) {
+                // a column on a closure row: its taps inward from the face
+                const int sg = c > 0 ? st : -st;
+                const bool face = c == 1 || c == -1;
+                const float4 f0 = ld4(s), f1 = ld4(s + sg), f2 = ld4(s + 2 * sg), f3 = ld4(s + 3 * sg);
+                const float4 fx = ld4(s + (face ? 4 * sg : -sg));
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    d[dd][j] = d1_closure(c, at(f0, j), at(f1, j), at(f2, j), at(f3, j), at(fx, j), inv_dx);
+                continue;
+            }
             const float4 m2 = ld4(s - 2 * st), m1 = ld4(s - st), p1 = ld4(s + st), p2 = ld4(s + 2 * st);
 #pragma unroll
             for (int j = 0; j < 4; ++j) d[dd][j] = (at(p1, j) - at(m1, j)) * a1 + (at(p2, j) - at(m2, j)) * a2;
@@ -640,7 +724,8 @@ k_first_derivs_tma(const __grid_constant__ CUtensorMap map, float* __restrict__ 
         __syncthreads();   // every thread is done with tile b
         if (t == 0 && i + DNBUF < ntile) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            load_box(ring + b * DFIELD, &map, z0 - 4, y0 - 2, x0 - 2, inst, comp_of(i + DNBUF), &bars[b], DFIELD_BYTES);
+            load_box(ring + b * DFIELD, &map, z0 - 4, y0 + oy, x0 + ox, inst, comp_of(i + DNBUF), &bars[b],
+                     DFIELD_BYTES);
         }
     }
 }
@@ -2486,7 +2571,10 @@ cudaError_t tma_device(TmaDevice& out) {
         e = cudaFuncSetAttribute(k_rhs_gauge_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)tma::curv_smem(0));
         if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(k_first_derivs_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            e = cudaFuncSetAttribute(k_first_derivs_tma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)tma::DSMEM);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_first_derivs_tma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)tma::DSMEM);
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(k_rhs_at_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -2516,8 +2604,10 @@ cudaError_t tma_timeouts(int* count) {
 
 // The interior first derivatives of the FP32 forms from TMA tiles (kappa = 0:
 // the NMIX fields only); false leaves the launch to the generic kernel.
+// closed: S may hold the D1 closure rows next to Sommerfeld faces (the whole
+// box, on a grid where tma_whole_box holds).
 static bool launch_first_derivs_tma(const float* u, float* d1, const Geo& G, const BoxSet& S, int with_mom,
-                                    cudaStream_t stream) {
+                                    bool closed, cudaStream_t stream) {
     if (!(g_tma_mask.load() & kTmaDerivs) || with_mom || S.n != 1 || G.ninst < 1 || G.ninst > 65535) return false;
     for (int d = 0; d < 3; ++d)
         if (G.ax[d].mad || G.ax[d].reduced) return false;
@@ -2550,8 +2640,12 @@ static bool launch_first_derivs_tma(const float* u, float* d1, const Geo& G, con
     if (tiles <= 0 || tiles > 0x7fffffffLL) return false;
     const int paired = G.precision == kPrecisionF32Paired ? 1 : 0;
     prof_begin(KC_FIRST, stream);
-    k_first_derivs_tma<<<dim3((unsigned)tiles, (unsigned)G.ninst), tma::THREADS, tma::DSMEM, stream>>>(
-        map, d1, G, B, z_base, tiles_z, tiles_y, NMIX, paired, dev.timeouts);
+    if (closed)
+        k_first_derivs_tma<true><<<dim3((unsigned)tiles, (unsigned)G.ninst), tma::THREADS, tma::DSMEM, stream>>>(
+            map, d1, G, B, z_base, tiles_z, tiles_y, NMIX, paired, dev.timeouts);
+    else
+        k_first_derivs_tma<false><<<dim3((unsigned)tiles, (unsigned)G.ninst), tma::THREADS, tma::DSMEM, stream>>>(
+            map, d1, G, B, z_base, tiles_z, tiles_y, NMIX, paired, dev.timeouts);
     prof_end(KC_FIRST, stream);
     g_tma_launches.fetch_add(1);
     return true;
@@ -2691,12 +2785,21 @@ static void launch_rhs_form(const R* u, const double* u64, double* k, R* d1, R* 
         cudaEventRecord(X->pre, stream);
         cudaStreamWaitEvent(stb, X->pre, 0);
     }
-    BSSN_LAUNCH_SET(KC_FIRST, 1, (k_first_derivs<R, true>), se.shell, stb, u, der, d1, G, se.shell, with_mom);
-    bool derivs_done = false;
-    if constexpr (kPerturbative<R>) derivs_done = launch_first_derivs_tma(u, d1, G, se.interior, with_mom, stream);
-    if (!derivs_done)
-        BSSN_LAUNCH_SET(KC_FIRST, 0, (k_first_derivs<R, false>), se.interior, stream, u, der, d1, G, se.interior,
-                        with_mom);
+    // FP32 forms on a grid whose closed axes are Sommerfeld at both ends: one
+    // TMA launch over the whole box, closure rows included; else the interior
+    // (TMA or generic) and the generic shell slabs beside it.
+    bool derivs_whole = false;
+    if constexpr (kPerturbative<R>)
+        derivs_whole = tma_whole_box(G, box) && launch_first_derivs_tma(u, d1, G, single(ext), with_mom, true, stream);
+    if (!derivs_whole) {
+        BSSN_LAUNCH_SET(KC_FIRST, 1, (k_first_derivs<R, true>), se.shell, stb, u, der, d1, G, se.shell, with_mom);
+        bool derivs_done = false;
+        if constexpr (kPerturbative<R>)
+            derivs_done = launch_first_derivs_tma(u, d1, G, se.interior, with_mom, false, stream);
+        if (!derivs_done)
+            BSSN_LAUNCH_SET(KC_FIRST, 0, (k_first_derivs<R, false>), se.interior, stream, u, der, d1, G, se.interior,
+                            with_mom);
+    }
     if (X) {
         cudaEventRecord(X->fd, stb);
         cudaStreamWaitEvent(stream, X->fd, 0);

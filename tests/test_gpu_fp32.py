@@ -227,8 +227,9 @@ def test_tma_kernels_match_the_generic_kernels(gb, form, faces, shape):
     the generic kernels on the same state: every RHS leaf equal to float
     rounding (1e-6 of its scale), with no tile wait given up.  With Sommerfeld
     faces the box kernels also take the rows next to the faces (their
-    one-sided stencils, and at the upper faces lowered box origins): the
-    shapes put those rows at every position within a tile along x and y."""
+    one-sided stencils, and at the upper faces lowered box origins), and the
+    first derivatives the face planes too: the shapes put those rows at
+    several positions within a tile along x and y."""
     pkg, te = gb
     from jax_bssn_gb300 import _native
     from jax_bssn_gb300.initial_data import random_smooth_state

@@ -105,3 +105,96 @@ def _out_of_box_taps(n, ghost=4):
 @pytest.mark.parametrize("shape", [(24, 20, 24), (23, 22, 20), (26, 21, 28), (18, 25, 24), (17, 19, 20)])
 def test_box_taps_stay_in_their_boxes(shape):
     assert _out_of_box_taps(shape) == 0
+
+
+# ---------------------------------------------------------------------------
+# The first-derivative kernel (k_first_derivs_tma<true>): 32 (z) x 8 (y) x 4
+# (x) tiles, four z samples per thread, 40 x 12 x 8 boxes (halo 4 in z, 2 in y
+# and x) over the whole box, face planes included, with the D1 closure rows
+# (d1_code, d1_origin, the z window of twelve samples and the ld4 taps).
+TZ, TY, TX = 32, 8, 4
+DHZ, DHY, DHX = TZ + 8, TY + 4, TX + 4
+
+
+def _d1_code(start, end, c, closed=True):
+    if not closed:
+        return 0
+    r = end - 1 - c
+    if r in (0, 1):
+        return -(r + 1)
+    r = c - start
+    return r + 1 if r in (0, 1) else 0
+
+
+def _d1_origin(start, end, t0, extent, blo, bhi, closed=True):
+    if not closed:
+        return -2
+    xf = end - 1
+    lo, hi = max(t0, xf - 1, blo), min(t0 + extent - 1, xf, bhi - 1)
+    return min(-2, xf - 4 - t0) if lo <= hi else -2
+
+
+def _derivative_taps_out_of_box(n, periodic_y=False, ghost=4):
+    padded = [m + 2 * ghost for m in n]
+    axes = [(ghost, ghost + m) for m in n]
+    closed = [True, not periodic_y, True]
+    # the launch box: the owned samples, grown by the composition reach (2) on
+    # a periodic axis
+    box = [(s - (0 if c else 2), e + (0 if c else 2)) for (s, e), c in zip(axes, closed)]
+    z_base = box[2][0] & ~3
+    bad = 0
+    for x0, y0, z0 in itertools.product(range(box[0][0], box[0][1], TX), range(box[1][0], box[1][1], TY),
+                                        range(z_base, box[2][1], TZ)):
+        assert (z0 - 4) % 4 == 0
+        ox = _d1_origin(*axes[0], x0, TX, *box[0], closed[0])
+        oy = _d1_origin(*axes[1], y0, TY, *box[1], closed[1])
+        for tx, ty, tz4 in itertools.product(range(TX), range(TY), range(TZ // 4)):
+            x, y, zq = x0 + tx, y0 + ty, z0 + 4 * tz4
+            col = box[0][0] <= x < box[0][1] and box[1][0] <= y < box[1][1]
+            rx, ry = (tx, ty) if col else (0, 0)
+            base = ((rx - ox) * DHY + (ry - oy)) * DHZ + 4 + 4 * tz4
+            cx = _d1_code(*axes[0], x, closed[0]) if col else 0
+            cy = _d1_code(*axes[1], y, closed[1]) if col else 0
+            reads = [base - 4 + i for i in range(12)]           # the z window
+            for c, st in ((cx, DHY * DHZ), (cy, DHZ)):
+                if c:
+                    sg = st if c > 0 else -st
+                    offs = [0, sg, 2 * sg, 3 * sg, 4 * sg if abs(c) == 1 else -sg]
+                else:
+                    offs = [-2 * st, -st, st, 2 * st]
+                reads += [base + o + i for o in offs for i in range(4)]
+            for r in reads:
+                if not 0 <= r < DHZ * DHY * DHX:
+                    bad += 1
+                    continue
+                if col:   # a valid column reads real samples of the padded block
+                    g = (x0 + ox + r // (DHY * DHZ), y0 + oy + (r // DHZ) % DHY, z0 - 4 + r % DHZ)
+                    zs = [zq + j for j in range(4) if box[2][0] <= zq + j < box[2][1]]
+                    if zs and (r % DHZ) in range(4 + 4 * tz4 - 4, 4 + 4 * tz4 + 8):
+                        bad += not (0 <= g[0] < padded[0] and 0 <= g[1] < padded[1])
+            # the z closure taps of every sample stay inside the window
+            for j in range(4):
+                cz = _d1_code(*axes[2], zq + j, closed[2]) if col else 0
+                if cz:
+                    up = cz < 0
+                    idx = [4 + j + (-k if up else k) for k in (1, 2, 3)]
+                    idx.append(4 + j + ((-4 if up else 4) if abs(cz) == 1 else (1 if up else -1)))
+                    assert all(0 <= i < 12 for i in idx)
+    return bad
+
+
+# the upper faces at every position within a tile along x (4) and y (8)
+D1_SHAPES = [((16 + k, 17 + k, 20 + k), False) for k in range(8)] + [((21, 23, 24), True), ((128, 128, 128), False)]
+
+
+@pytest.mark.parametrize("shape,periodic_y", D1_SHAPES)
+def test_first_derivative_taps_stay_in_their_boxes(shape, periodic_y):
+    assert _derivative_taps_out_of_box(shape, periodic_y) == 0
+
+
+def test_first_derivative_replay_finds_unlowered_boxes(monkeypatch):
+    """The replay is sensitive: boxes left at halo 2 in tiles that hold an
+    upper face plane read below their boxes."""
+    import sys
+    monkeypatch.setattr(sys.modules[__name__], "_d1_origin", lambda *a, **k: -2)
+    assert sum(_derivative_taps_out_of_box(shape, py) for shape, py in D1_SHAPES[:8]) > 0
