@@ -2118,15 +2118,31 @@ k_sommerfeld(const R* __restrict__ u, const double* __restrict__ u64, double* __
         face = face || (a.slo && c.ix[d] == a.start) || (a.shi && c.ix[d] == a.end - 1);
     }
     if (!(face && owned)) return;
-    double X[3];
+    R xr[3], rr;
+    if constexpr (kPerturbative<R>) {
+        // float forms: the radial direction in float (FP64 arithmetic runs
+        // at a small fraction of the float rate here, and these values end
+        // up in float anyway)
+        float r2 = 0.0f;
 #pragma unroll
-    for (int d = 0; d < 3; ++d) X[d] = __dadd_rn(G.ax[d].xmin, __dmul_rn(G.dx, (double)(c.ix[d] - G.ax[d].org)));
-    const double r = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(X[0], X[0]), __dmul_rn(X[1], X[1])),
-                                          __dmul_rn(X[2], X[2])));
-    const double rs = r > 0.0 ? r : 1.0;
+        for (int d = 0; d < 3; ++d) {
+            xr[d] = static_cast<float>(G.ax[d].xmin) + static_cast<float>(G.dx) * (float)(c.ix[d] - G.ax[d].org);
+            r2 += xr[d] * xr[d];
+        }
+        const float r = sqrtf(r2);
+        rr = r > 0.0f ? r : 1.0f;
+    } else {
+        // FP64 form: the reference's operation order
+        double X[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) X[d] = __dadd_rn(G.ax[d].xmin, __dmul_rn(G.dx, (double)(c.ix[d] - G.ax[d].org)));
+        const double r = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(X[0], X[0]), __dmul_rn(X[1], X[1])),
+                                              __dmul_rn(X[2], X[2])));
+#pragma unroll
+        for (int d = 0; d < 3; ++d) xr[d] = X[d];
+        rr = r > 0.0 ? r : 1.0;
+    }
     const long long cs = G.cs, p = c.p;
-    const R xr[3] = {static_cast<R>(X[0]), static_cast<R>(X[1]), static_cast<R>(X[2])};
-    const R rr = static_cast<R>(rs);
     // blockIdx.z picks a group of kSommerfeldGroup components: short per-thread
     // chains and enough threads for the few face samples
 #pragma unroll 1
