@@ -2561,9 +2561,9 @@ EncodeTiled encode_tiled() {
 // default: all four.  At 128^3 the FP32 step took 8.60 ms with the
 // derivatives alone, 8.13 with the At kernel, 7.77 with the K/Gt kernel,
 // 7.34 with the gauge kernel, 7.18 with the rows next to the Sommerfeld
-// faces in the boxes, 6.93 once those rows share the centred taps and 6.90
-// with the At kernel's spills cut (paired: 10.12, 9.43, 9.01, 8.57, 8.35,
-// 8.09, 8.05 ms).  A gauge
+// faces in the boxes, 6.93 once those rows share the centred taps, 6.90
+// with the At kernel's spills cut and 6.79 with the first derivatives over the
+// whole box (paired: 10.12, 9.43, 9.01, 8.57, 8.35, 8.09, 8.05, 7.85 ms).  A gauge
 // kernel with four samples per thread and 90 KB of shared memory per CTA was
 // faster alone but crowded out the kernels beside it (9.55 against 9.42 ms).
 std::atomic<int> g_tma_mask{kTmaAll};
